@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""Benchmark of the NuFFT operator on the config-1 workload.
+
+Workload (one "step"): the per-coil NFFT forward (32 coil images -> k-space)
+followed by the per-coil adjoint (k-space -> 32 coil images) of a 256^2 image,
+32 coils, golden-angle radial trajectory of 403 spokes x 512 samples, sigma=2
+(512^2 oversampled grid), Kaiser-Bessel m=4.  Seeded synthetic inputs stand in
+for scanner data (none is published for this path).
+
+Metric: NuFFT GB/s = algorithmic bytes of one forward+adjoint (per-pass model:
+deapodise/pad, FFT, interpolation; spreading, FFT, crop/deapodise) / time.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is device-resident (inputs already in HBM, device pointers through the
+C ABI, L2 flushed before each timed step); `e2e` is the same metric through
+the C ABI with pinned HOST buffers, host<->device copies inside the timed
+region.  The reference arm times the FP64 CPU restatement of the reference's
+NFFT3 path (oracle/, the reference itself cannot be built: see the design doc).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "NuFFT GB/s (per-coil NFFT forward + adjoint)"
+UNIT = "GB/s"
+N, NC, SPOKES, SAMPLES, SIGMA, M_KB = 256, 32, 403, 512, 2.0, 4
+WORKLOAD = ("config 1: NuFFT forward+adjoint, 256^2 image x 32 coils, golden-angle radial "
+            "403x512 (M=206336), sigma=2 (512^2 grid), KB m=4")
+
+
+def algorithmic_bytes(N, n, M, d, nc):
+    """Per-pass byte model (complex64 = 8 B, coordinates float32)."""
+    img = nc * N ** d * 8
+    grid = nc * n ** d * 8
+    ks = nc * M * 8
+    coords = M * d * 4
+    b = {
+        "pad_deapod": img + grid,
+        "fft": 2 * grid,                 # per transform
+        "interp": grid + coords + ks,
+        "spread": coords + ks + grid,
+        "crop_deapod": grid + img,
+    }
+    b["forward"] = b["pad_deapod"] + b["fft"] + b["interp"]
+    b["adjoint"] = b["spread"] + b["fft"] + b["crop_deapod"]
+    b["step"] = b["forward"] + b["adjoint"]
+    return b
+
+
+def workload_data(seed=20261204):
+    from codeare_gb300 import synth
+    k = synth.radial2d(SPOKES, SAMPLES, golden=True)
+    rng = np.random.default_rng(seed)
+    fh = (rng.standard_normal((NC, N, N)) + 1j * rng.standard_normal((NC, N, N))).astype(np.complex64)
+    return k, fh
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (clocks and throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [q.strip() for q in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_nfft_step_time(k, fh, threads, reps=1):
+    """FP64 CPU restatement of the reference's per-coil NFFT3 trafo+adjoint."""
+    from oracle import oracle as O
+    O.build()
+    P = O.NFFT((N, N), k.shape[0], m=M_KB, alpha=SIGMA)
+    P.set_x(k.astype(np.float64))
+    fh64 = fh.astype(np.complex128)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        f = P.trafo_batch(fh64, threads=threads)
+        P.adjoint_batch(f, threads=threads)
+    return (time.perf_counter() - t0) / reps
+
+
+def run_reference(args):
+    ws, rank, local = dist_setup()
+    if rank != 0:
+        return 0
+    k, fh = workload_data()
+    threads = os.cpu_count() or 1
+    nc_s = min(NC, max(1, threads))  # one coil per host thread per step
+    sample = fh[:nc_s]
+    b = algorithmic_bytes(N, int(N * SIGMA), k.shape[0], 2, nc_s)["step"]
+    for _ in range(args.warmup):
+        cpu_nfft_step_time(k, sample, threads)
+    times = [cpu_nfft_step_time(k, sample, threads) for _ in range(args.steps)]
+    t = sum(times) / len(times)
+    v = b / t / 1e9
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)", "impl": "reference",
+        "config": {"workload": WORKLOAD, "sample_coils_per_step": nc_s},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d of 32 coils per step (one per host thread), full trajectory; "
+                                   "FP64 C restatement of the NFFT3 path with the project's own FFT "
+                                   "(the reference needs NFFT3/FFTW/Boost, absent here)" % nc_s},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import codeare_gb300 as cg
+    from codeare_gb300 import capi
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if ws == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    k, fh = workload_data()
+    M = k.shape[0]
+    n = int(N * SIGMA)
+    bytes_model = algorithmic_bytes(N, n, M, 2, NC)
+    plan = cg.Plan((N, N), M, ncoils=NC, m=M_KB, alpha=SIGMA)
+    plan.set_kspace(k)
+    stream = torch.cuda.current_stream()
+    fh_d = torch.from_numpy(fh).cuda()
+    f_d = torch.empty((NC, M), dtype=torch.complex64, device="cuda")
+    img_d = torch.empty((NC, N, N), dtype=torch.complex64, device="cuda")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 126 MB L2
+
+    def step():
+        plan.nfft_trafo(fh_d, f_d, stream=stream)
+        plan.nfft_adjoint(f_d, img_d, stream=stream)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps, L2 flushed before each, CUDA events on the launching stream
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize()
+    l0 = cg.kernel_launches()
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    launches = cg.kernel_launches() - l0
+    clk = clocks.stop()
+    t_step = sum(a.elapsed_time(b) for a, b in ev) / args.steps * 1e-3
+    t_step = max_over_ranks(t_step)
+    value = ws * bytes_model["step"] / t_step / 1e9
+
+    # ---- per-kernel CUDA-event profile over the same steps
+    capi.profile_enable(True)
+    for i in range(args.steps):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    prof = capi.profile_collect()
+    capi.profile_enable(False)
+    per_kernel = {}
+    kb = {"interp": bytes_model["interp"], "spread": bytes_model["spread"],
+          # FFT passes: 2 launches per transform; model bytes per transform include pad/crop
+          "fft": (bytes_model["pad_deapod"] + bytes_model["fft"] + bytes_model["fft"] +
+                  bytes_model["crop_deapod"]) / 4.0}
+    for cat, (ms, cnt) in prof.items():
+        if cnt:
+            avg = ms / cnt * 1e-3
+            per_kernel[cat] = {"launches": cnt, "avg_ms": avg * 1e3, "alg_bytes_per_launch": kb[cat],
+                               "GBps": kb[cat] / avg / 1e9}
+    dom = max(per_kernel, key=lambda c: prof[c][0]) if per_kernel else None
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    traffic = None
+    try:
+        tj = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        traffic = tj.get(dom)
+    except Exception:
+        pass
+    roofline = None
+    if dom:
+        a = per_kernel[dom]["GBps"]
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": a, "peak": hbm, "peak_source": peak_src,
+                    "unit": "GB/s", "frac": a / hbm, "traffic": traffic,
+                    "alg_bytes_per_launch": per_kernel[dom]["alg_bytes_per_launch"]}
+
+    # ---- e2e through the C ABI with pinned host buffers
+    fh_h = torch.from_numpy(fh).pin_memory().numpy()
+    f_h = torch.empty((NC, M), dtype=torch.complex64).pin_memory().numpy()
+    img_h = torch.empty((NC, N, N), dtype=torch.complex64).pin_memory().numpy()
+
+    def step_host():
+        plan.nfft_trafo(fh_h, f_h)
+        plan.nfft_adjoint(f_h, img_h)
+
+    for _ in range(2):
+        step_host()
+    tt = 0.0
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step_host()
+        tt += time.perf_counter() - t0
+    t_e2e = max_over_ranks(tt / args.steps)
+    h2d = fh_h.nbytes + f_h.nbytes
+    d2h = f_h.nbytes + img_h.nbytes
+    e2e = {"value": ws * bytes_model["step"] / t_e2e / 1e9, "unit": UNIT, "ms_per_step": t_e2e * 1e3,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    # ---- CPU baseline (rank 0, N = 1): bounded sample, one coil per host thread
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        nc_s = min(NC, threads)
+        t_cpu = cpu_nfft_step_time(k, fh[:nc_s], threads)
+        b = algorithmic_bytes(N, n, M, 2, nc_s)["step"]
+        cpu = {"value": b / t_cpu / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d of 32 coils, one forward+adjoint, one coil per thread; FP64 C restatement of "
+                         "the NFFT3 path (own FFT; FFTW absent)" % nc_s, "seconds": t_cpu}
+
+    plan.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "N": N, "n": n, "M": M, "ncoils": NC, "m": M_KB,
+                       "alg_bytes_per_step": bytes_model["step"],
+                       "l2": "flushed before every timed step (512 MiB write, untimed)",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "roofline": roofline, "kernels": per_kernel, "cpu_baseline": cpu, "e2e": e2e,
+            "clocks": clk, "gpu_launches": launches,
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

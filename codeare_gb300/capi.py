@@ -1,0 +1,215 @@
+"""ctypes binding of libcgs.so (include/cgs.h).
+
+The product path is the CUDA library; there is no CPU fallback.  Loading fails
+loudly when libcgs.so is missing or was built for another machine.
+
+Arrays may be numpy (host) or torch CUDA tensors (device); both are passed as
+raw pointers and the library stages host data itself.  Layouts are the C-order
+views of codeare's column-major matrices (see codeare_gb300/synth.py).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libcgs.so")
+
+CGS_OK, CGS_ERR_BAD_ARG, CGS_ERR_OOM, CGS_ERR_CUDA, CGS_ERR_TIMEOUT, CGS_ERR_NAN, CGS_ERR_STATE = range(7)
+MODE_CODEARE, MODE_STANDARD = 0, 1
+
+EXPORTED = [
+    "cgs_plan_create", "cgs_plan_destroy", "cgs_set_kspace", "cgs_set_weights",
+    "cgs_set_sensitivities", "cgs_nfft_trafo", "cgs_nfft_adjoint", "cgs_nfft_itrafo",
+    "cgs_sense_trafo", "cgs_sense_adjoint_codeare", "cgs_sense_adjoint", "cgs_solve",
+    "cgs_plan_info", "cgs_sync", "cgs_kernel_launches", "cgs_last_error",
+    "cgs_profile_enable", "cgs_profile_collect",
+]
+PROFILE_CATEGORIES = ("fft", "interp", "spread")
+
+
+class PlanDesc(C.Structure):
+    _fields_ = [("rank", C.c_int), ("N", C.c_int * 3), ("alpha", C.c_double), ("m", C.c_int),
+                ("M", C.c_int64), ("ncoils", C.c_int)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("mode", C.c_int), ("cgiter", C.c_int), ("cgeps", C.c_double),
+                ("lam", C.c_double), ("ftiter", C.c_int), ("fteps", C.c_double),
+                ("weighted", C.c_int)]
+
+
+class SolveReport(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("res_first", C.c_double), ("res_last", C.c_double),
+                ("seconds", C.c_double), ("res_hist", C.c_double * 256)]
+
+
+class CgsError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("cgs status %d: %s" % (status, msg))
+        self.status = status
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libcgs.so (raises if absent: the CUDA library is the only path)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError("libcgs.so not built (run __graft_entry__.build()): %s" % path)
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.cgs_plan_create.argtypes = [C.POINTER(vp), C.POINTER(PlanDesc)]
+    L.cgs_plan_destroy.argtypes = [vp]
+    L.cgs_set_kspace.argtypes = [vp, vp]
+    L.cgs_set_weights.argtypes = [vp, vp]
+    L.cgs_set_sensitivities.argtypes = [vp, vp]
+    L.cgs_nfft_trafo.argtypes = [vp, vp, vp, vp]
+    L.cgs_nfft_adjoint.argtypes = [vp, vp, vp, vp]
+    L.cgs_nfft_itrafo.argtypes = [vp, vp, vp, C.c_int, C.c_double, vp]
+    L.cgs_sense_trafo.argtypes = [vp, vp, vp, vp]
+    L.cgs_sense_adjoint_codeare.argtypes = [vp, vp, vp, C.c_int, C.c_double, vp]
+    L.cgs_sense_adjoint.argtypes = [vp, vp, vp, C.c_int, vp]
+    L.cgs_solve.argtypes = [vp, vp, vp, C.POINTER(SolveOpts), C.POINTER(SolveReport), vp]
+    L.cgs_plan_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                C.POINTER(C.c_int64), C.POINTER(C.c_int)]
+    L.cgs_sync.argtypes = [vp]
+    L.cgs_kernel_launches.restype = C.c_int64
+    L.cgs_last_error.restype = C.c_char_p
+    L.cgs_profile_enable.argtypes = [C.c_int]
+    L.cgs_profile_enable.restype = None
+    L.cgs_profile_collect.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    L.cgs_profile_collect.restype = None
+    for name in EXPORTED:
+        if name not in ("cgs_kernel_launches", "cgs_last_error", "cgs_profile_enable",
+                        "cgs_profile_collect"):
+            getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def _check(status):
+    if status != CGS_OK:
+        raise CgsError(status, load().cgs_last_error().decode())
+
+
+def _ptr(a):
+    """raw pointer of a numpy array or torch tensor (no copy)"""
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return C.c_void_p(a.ctypes.data)
+    if hasattr(a, "data_ptr"):
+        if not a.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return C.c_void_p(a.data_ptr())
+    raise TypeError("expected numpy array or torch tensor")
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if hasattr(s, "cuda_stream"):
+        return C.c_void_p(s.cuda_stream)
+    return C.c_void_p(int(s))
+
+
+def kernel_launches() -> int:
+    return int(load().cgs_kernel_launches())
+
+
+def profile_enable(on: bool = True):
+    load().cgs_profile_enable(int(bool(on)))
+
+
+def profile_collect():
+    """{category: (total ms, launches)} accumulated since the last collect"""
+    ms = (C.c_double * 3)()
+    cnt = (C.c_int64 * 3)()
+    load().cgs_profile_collect(ms, cnt)
+    return {PROFILE_CATEGORIES[i]: (ms[i], cnt[i]) for i in range(3)}
+
+
+class Plan:
+    """One NFFT / NCSENSE operator on the current CUDA device."""
+
+    def __init__(self, shape, M, ncoils=1, m=1, alpha=1.0):
+        L = load()
+        self.shape = tuple(int(s) for s in shape)
+        self.d = len(self.shape)
+        self.M = int(M)
+        self.nc = int(ncoils)
+        desc = PlanDesc(self.d, (C.c_int * 3)(*self.shape, *([1] * (3 - self.d))), float(alpha), int(m),
+                        self.M, self.nc)
+        h = C.c_void_p()
+        _check(L.cgs_plan_create(C.byref(h), C.byref(desc)))
+        self._h = h
+        N = (C.c_int * 3)(); n = (C.c_int * 3)(); r = C.c_int(); Mo = C.c_int64(); nc = C.c_int()
+        _check(L.cgs_plan_info(h, C.byref(r), N, n, C.byref(Mo), C.byref(nc)))
+        self.n = tuple(n[i] for i in range(self.d))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().cgs_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- setup -------------------------------------------------------------
+    def set_kspace(self, k):
+        _check(load().cgs_set_kspace(self._h, _ptr(k)))
+
+    def set_weights(self, w):
+        _check(load().cgs_set_weights(self._h, _ptr(w)))
+
+    def set_sensitivities(self, s):
+        _check(load().cgs_set_sensitivities(self._h, _ptr(s)))
+
+    def sync(self):
+        _check(load().cgs_sync(self._h))
+
+    # -- operators (out must be preallocated, same memory kind as in) -------
+    def nfft_trafo(self, fhat, out, stream=None):
+        _check(load().cgs_nfft_trafo(self._h, _ptr(fhat), _ptr(out), _stream(stream)))
+        return out
+
+    def nfft_adjoint(self, f, out, stream=None):
+        _check(load().cgs_nfft_adjoint(self._h, _ptr(f), _ptr(out), _stream(stream)))
+        return out
+
+    def nfft_itrafo(self, f, out, maxit=3, eps=1e-3, stream=None):
+        _check(load().cgs_nfft_itrafo(self._h, _ptr(f), _ptr(out), int(maxit), float(eps), _stream(stream)))
+        return out
+
+    def sense_trafo(self, x, out, stream=None):
+        _check(load().cgs_sense_trafo(self._h, _ptr(x), _ptr(out), _stream(stream)))
+        return out
+
+    def sense_adjoint_codeare(self, y, out, ftiter=3, fteps=1e-3, stream=None):
+        _check(load().cgs_sense_adjoint_codeare(self._h, _ptr(y), _ptr(out), int(ftiter), float(fteps),
+                                                 _stream(stream)))
+        return out
+
+    def sense_adjoint(self, y, out, weighted=True, stream=None):
+        _check(load().cgs_sense_adjoint(self._h, _ptr(y), _ptr(out), int(bool(weighted)), _stream(stream)))
+        return out
+
+    def solve(self, y, out, mode=MODE_CODEARE, cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3,
+              weighted=True, stream=None):
+        o = SolveOpts(int(mode), int(cgiter), float(cgeps), float(lam), int(ftiter), float(fteps),
+                      int(bool(weighted)))
+        rep = SolveReport()
+        _check(load().cgs_solve(self._h, _ptr(y), _ptr(out), C.byref(o), C.byref(rep), _stream(stream)))
+        n = rep.iterations
+        hist = [rep.res_hist[i] for i in range(min(256, n + 1))]
+        return dict(iterations=n, res_first=rep.res_first, res_last=rep.res_last, seconds=rep.seconds,
+                    res_hist=hist)

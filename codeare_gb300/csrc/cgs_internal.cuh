@@ -1,0 +1,207 @@
+// cgs_internal.cuh -- shared declarations of the sm_103a kernels and the plan.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/cgs.h"
+
+namespace cgs {
+
+// ---------------------------------------------------------------------------
+// error plumbing (host)
+// ---------------------------------------------------------------------------
+void set_error(const std::string &msg);
+void count_launch(int n = 1);
+
+// Optional per-kernel timing with CUDA events on the launching stream
+// (cgs_profile_enable / cgs_profile_collect).  Categories:
+enum ProfCat { PROF_FFT = 0, PROF_INTERP = 1, PROF_SPREAD = 2, PROF_NCAT = 3 };
+void prof_begin(int cat, cudaStream_t st);
+void prof_end(int cat, cudaStream_t st);
+
+#define CGS_CUDA(call)                                                              \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            ::cgs::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));  \
+            return CGS_ERR_CUDA;                                                    \
+        }                                                                           \
+    } while (0)
+
+#define CGS_LAUNCH_CHECK()                                                          \
+    do {                                                                            \
+        cudaError_t e_ = cudaGetLastError();                                        \
+        if (e_ != cudaSuccess) {                                                    \
+            ::cgs::set_error(std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+            return CGS_ERR_CUDA;                                                    \
+        }                                                                           \
+        ::cgs::count_launch();                                                      \
+    } while (0)
+
+#define CGS_TRY(expr)                         \
+    do {                                      \
+        cgs_status s_ = (expr);               \
+        if (s_ != CGS_OK) return s_;          \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Kaiser-Bessel window, FP32 device version.
+// phi(tau) = (b/pi) * sinh(z)/z,  z = b*sqrt(m^2 - tau^2)  (|tau| < m)
+//          = (b/pi) * sin(z)/z,   z = b*sqrt(tau^2 - m^2)  (|tau| > m)
+//          = b/pi                                           (|tau| = m)
+// tau is the distance node - grid point in grid units.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float kb_phi(float tau, float m, float b)
+{
+    const float s2 = fmaf(-tau, tau, m * m);
+    const float bp = b * 0.31830988618379067f;  // b/pi
+    if (s2 > 0.f) {
+        const float z = b * sqrtf(s2);
+        if (z < 1e-3f) return bp * (1.f + z * z * (1.f / 6.f));
+        const float E = expm1f(z);             // sinh(z) = E (2+E) / (2 (1+E))
+        return bp * (0.5f * E * ((2.f + E) / (1.f + E))) / z;
+    } else if (s2 < 0.f) {
+        const float z = b * sqrtf(-s2);
+        if (z < 1e-3f) return bp * (1.f - z * z * (1.f / 6.f));
+        return bp * sinf(z) / z;
+    }
+    return bp;
+}
+
+// ---------------------------------------------------------------------------
+// FFT axis pass descriptors
+// ---------------------------------------------------------------------------
+enum LoadMode : int {
+    LOAD_PLAIN = 0,     // src[o][a][i]
+    LOAD_IMAGE = 1,     // image-side first pass: img (broadcast or per-coil) * sens * mask * deapod
+};
+enum StoreMode : int {
+    STORE_PLAIN = 0,    // dst[o][a][i]
+    STORE_DEAPOD = 1,   // dst[o][a][i] * deapod(o,a)
+    STORE_COMBINE = 2,  // out[o][a] = scale(o,a) * deapod * sum_i conj(S[o][a][i]) val_i
+};
+
+struct AxisPass {
+    // geometry: data[outer][L][inner]; transform length n along L
+    int64_t outer, inner;
+    int n;            // FFT length
+    int Lin, Lout;    // axis lengths of src and dst
+    int in_centred;   // src axis is image side: index a holds frequency a - Lin/2 (pad into n)
+    int out_centred;  // dst axis is image side: index a takes frequency a - Lout/2 (crop from n)
+    int sign;         // -1 forward, +1 inverse
+    const float2 *src;
+    float2 *dst;
+    const float2 *tw; // twiddles exp(-2 pi i t / n), t < n
+    int nfac, fac[12];
+    // fused image-side terms (first forward pass / last inverse pass)
+    int load_mode, store_mode;
+    const float2 *img;     // LOAD_IMAGE: image [outer][Lin] (broadcast) or [outer][Lin][inner]
+    int img_per_coil;
+    const float2 *sens;    // [outer][Lin|Lout][inner] sensitivities (coil innermost), nullable
+    const float *mask;     // [outer][Lin] real pixel mask (nullable)
+    const float *scale;    // STORE_COMBINE: per-pixel real scale (intensity map), nullable
+    const float *deap_ax;  // 1/phihut along the axis, length N of the axis
+    const float *deap_o1;  // 1/phihut along outer dim closest to the axis (2-D: y; 3-D: y)
+    const float *deap_o0;  // 1/phihut along the outermost dim (3-D: z), nullable
+    int o1_len;            // length of the o1 image dim (to split outer = o0 * o1_len + o1)
+    int64_t combine_stride;// STORE_COMBINE output: out[o*Lout + a]
+    float2 *combine_out;
+};
+
+cgs_status launch_axis_pass(const AxisPass &p, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Gridding (KB interpolation / spreading) over tiles of the oversampled grid
+// ---------------------------------------------------------------------------
+struct GridGeom {
+    int d;            // 2 or 3
+    int n[3];         // oversampled grid per dim (dim 0 slowest)
+    int m;            // KB cut-off; 2m+2 taps per dim
+    float b[3];       // KB shape per dim
+    int T;            // tile side (footprint-start bins)
+    int nt[3];        // tiles per dim
+    int nc;           // coils (innermost in grid and k-space)
+};
+
+struct NodeSet {
+    int64_t M;          // nodes
+    const float4 *nodes;// per node: 2-D {frac0, frac1, c0 bits, c1 bits}; 3-D two float4 per node
+    const int *perm;    // sorted position -> original node index
+    const float *w;     // density weights in sorted order (nullable)
+    int nwork;          // work items
+    const int4 *work;   // {tile index, first node, node count, 0}
+};
+
+// y[s][c] (sorted, coil innermost) = sum over footprint of grid[...][c]
+cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,
+                         cudaStream_t st);
+// grid[...][c] += sum_s phi * (w_s if weighted) * ks[s][c]; grid must be zeroed first
+cgs_status launch_spread(const GridGeom &g, const NodeSet &ns, const float2 *ks, int weighted,
+                         float2 *grid, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// vector kernels (cgs_vec.cu)
+// ---------------------------------------------------------------------------
+// user (NC, M) coil-major unsorted  <->  ks[s][c] sorted coil-minor
+cgs_status launch_gather_ks(const float2 *user, const int *perm, int64_t M, int nc, float2 *ks,
+                            cudaStream_t st);
+cgs_status launch_scatter_ks(const float2 *ks, const int *perm, int64_t M, int nc, float2 *user,
+                             cudaStream_t st);
+// coil-major (NC, P) <-> coil-minor [P][NC]
+cgs_status launch_to_coil_minor(const float2 *a, int64_t P, int nc, float2 *out, cudaStream_t st);
+cgs_status launch_to_coil_major(const float2 *a, int64_t P, int nc, float2 *out, cudaStream_t st);
+
+// Deterministic FP64-accumulated per-column dots over rows:
+// out[c] = sum_r wr[r] * Re(conj(a[r][c]) * b[r][c]), wr nullable (1).
+// partial must hold nblk*nc doubles (nblk = dot_blocks()).
+int dot_blocks();
+cgs_status launch_coldot(const float2 *a, const float2 *b, const float *wr, int64_t rows, int nc,
+                         double *partial, double *out, cudaStream_t st);
+
+// scalar CG bookkeeping on device (one thread per coil)
+// mode 0: CGNR start of step: active[c] &= (dot_r[c] >= eps)
+// mode 1: alpha[c] = active ? dot_z[c] / dot_v[c] : 0
+// mode 2: beta[c] = active ? dz_new/dot_z : 0; dot_z = active ? dz_new : dot_z
+cgs_status launch_cgnr_scalars(int mode, int nc, double eps, int *active, const double *dot_r,
+                               double *dot_z, const double *dot_v, const double *dz_new,
+                               double *alpha, double *beta, cudaStream_t st);
+
+// per-column update kernels (coil-minor [rows][nc])
+// x[r][c] += alpha[c] * (mask? mask[r] : 1) * p[r][c]
+cgs_status launch_axpy_cols(float2 *x, const double *alpha, double alpha_sign, const float *mask,
+                            const float2 *p, int64_t rows, int nc, cudaStream_t st);
+// p[r][c] = z[r][c] + beta[c] * p[r][c]   (only where active[c])
+cgs_status launch_xpby_cols(float2 *p, const float2 *z, const double *beta, const int *active,
+                            int64_t rows, int nc, cudaStream_t st);
+cgs_status launch_zero(void *p, size_t bytes, cudaStream_t st);
+
+// CGLS (single image) kernels: scalars live in a small device struct
+struct CGScalars {
+    double rn, xn, rno, pq, ts, beta, lambda;
+    int done;
+};
+// q += lambda * p ; then pq = Re<p,q> is computed by coldot
+cgs_status launch_add_scaled(float2 *q, const float2 *p, const CGScalars *sc, int64_t n,
+                             cudaStream_t st);
+// x += ts p ; r -= ts q  (ts = rn / pq computed in-kernel)
+cgs_status launch_cg_update_xr(float2 *x, float2 *r, const float2 *p, const float2 *q,
+                               CGScalars *sc, int64_t n, cudaStream_t st);
+// p = r + (rn/rno) p
+cgs_status launch_cg_update_p(float2 *p, const float2 *r, const CGScalars *sc, int64_t n,
+                              cudaStream_t st);
+// sc->field = value (device scalar copy)
+cgs_status launch_scalar_op(CGScalars *sc, const double *src, int op, cudaStream_t st);
+
+// x[p] = (I ? I[p] : 1) * sum_c conj(S[p][c]) * F[p][c]   (coil-minor F, S)
+cgs_status launch_coil_combine(const float2 *F, const float2 *S, const float *I, int64_t P, int nc,
+                               float2 *x, cudaStream_t st);
+// intensity map I = 1/(sqrt(sum_c |S_c|^2) + 1e-9) from coil-minor sens
+cgs_status launch_intensity(const float2 *sens_cm, int64_t P, int nc, float *I, cudaStream_t st);
+// x *= real scale (elementwise, single image)
+cgs_status launch_scale_real(float2 *x, const float *s, int64_t n, cudaStream_t st);
+
+}  // namespace cgs

@@ -1,0 +1,834 @@
+// cgs_plan.cu -- the plan object and the C ABI (include/cgs.h).
+//
+// Host orchestration only: every arithmetic step runs in the kernels of
+// cgs_fft.cu, cgs_grid.cu and cgs_vec.cu on the plan's stream.  Device data
+// layouts (all complex float):
+//   grid       [n0][n1][n2][NC]       oversampled grid, coil innermost
+//   k-space    [s][NC]                nodes in tile-sorted order s, coil innermost
+//   coil image [p][NC]                image pixel p (NFFT order), coil innermost
+//   image      [p]
+// The caller's layouts (coil slowest, nodes in trajectory order) are converted
+// at the boundary only.
+#include "cgs_internal.cuh"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+namespace cgs {
+
+static thread_local std::string g_last_error;
+static std::atomic<int64_t> g_launches{0};
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// per-kernel event profiler (off unless cgs_profile_enable(1))
+namespace {
+struct ProfRec { int cat; cudaEvent_t a, b; };
+std::mutex g_prof_mu;
+bool g_prof_on = false;
+std::vector<ProfRec> g_prof_recs;
+std::vector<cudaEvent_t> g_prof_pool;
+int g_prof_open = -1;
+double g_prof_ms[PROF_NCAT] = {0, 0, 0};
+int64_t g_prof_cnt[PROF_NCAT] = {0, 0, 0};
+
+cudaEvent_t prof_event()
+{
+    if (!g_prof_pool.empty()) { cudaEvent_t e = g_prof_pool.back(); g_prof_pool.pop_back(); return e; }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void prof_drain()
+{
+    for (auto &r : g_prof_recs) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            g_prof_ms[r.cat] += ms;
+            g_prof_cnt[r.cat] += 1;
+        }
+        g_prof_pool.push_back(r.a);
+        g_prof_pool.push_back(r.b);
+    }
+    g_prof_recs.clear();
+}
+}  // namespace
+
+void prof_begin(int cat, cudaStream_t st)
+{
+    if (!g_prof_on) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (g_prof_recs.size() > 4096) prof_drain();
+    ProfRec r{cat, prof_event(), prof_event()};
+    cudaEventRecord(r.a, st);
+    g_prof_recs.push_back(r);
+    g_prof_open = (int)g_prof_recs.size() - 1;
+}
+
+void prof_end(int cat, cudaStream_t st)
+{
+    if (!g_prof_on) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (g_prof_open >= 0 && g_prof_recs[g_prof_open].cat == cat) cudaEventRecord(g_prof_recs[g_prof_open].b, st);
+    g_prof_open = -1;
+}
+
+// modified Bessel I0 by its power series, FP64 (host; used for 1/phihut tables)
+static double bessel_i0(double x)
+{
+    double y = 0.25 * x * x, term = 1.0, sum = 1.0;
+    for (int k = 1; k < 1000; ++k) {
+        term *= y / ((double)k * (double)k);
+        sum += term;
+        if (term < 1e-18 * sum) break;
+    }
+    return sum;
+}
+
+static bool factorize(int n, int *fac, int *nf)
+{
+    int r = n, k = 0;
+    while (r % 8 == 0 && k < 12) { fac[k++] = 8; r /= 8; }
+    while (r % 4 == 0 && k < 12) { fac[k++] = 4; r /= 4; }
+    while (r % 2 == 0 && k < 12) { fac[k++] = 2; r /= 2; }
+    const int primes[] = {3, 5, 7};
+    for (int q : primes)
+        while (r % q == 0 && k < 12) { fac[k++] = q; r /= q; }
+    *nf = k;
+    return r == 1;
+}
+
+}  // namespace cgs
+
+using namespace cgs;
+
+struct cgs_plan {
+    int d = 0, N[3] = {1, 1, 1}, n[3] = {1, 1, 1}, m = 1, nc = 1;
+    double alpha = 1.0;
+    int64_t M = 0, Nt = 1, ntot = 1;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+
+    // per-dimension FFT twiddles and deapodisation 1/phihut
+    float2 *tw[3] = {nullptr, nullptr, nullptr};
+    int fac[3][12] = {}, nfac[3] = {0, 0, 0};
+    float *deap[3] = {nullptr, nullptr, nullptr};
+
+    // trajectory
+    bool have_k = false, have_w = false, have_s = false;
+    float4 *nodes = nullptr;
+    int *perm = nullptr;
+    float *w = nullptr;
+    int4 *work = nullptr;
+    int nwork = 0;
+    GridGeom geom{};
+
+    // image-side maps
+    float *mask = nullptr;   // damping mask What (N^d)
+    float *imap = nullptr;   // intensity map I (N^d)
+    float2 *sens = nullptr;  // [p][NC]
+
+    // scratch
+    float2 *grid = nullptr, *t1 = nullptr, *t2 = nullptr;
+    float2 *ksY = nullptr, *ksR = nullptr, *ksV = nullptr;
+    float2 *cF = nullptr, *cP = nullptr, *cZ = nullptr;
+    float2 *vX = nullptr, *vR = nullptr, *vP = nullptr, *vQ = nullptr;
+    float2 *ioA = nullptr, *ioB = nullptr;
+    double *partial = nullptr, *dots = nullptr;  // dots: 8 arrays of NC
+    int *active = nullptr;
+    CGScalars *sc = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    double *dot_r() { return dots; }
+    double *dot_z() { return dots + nc; }
+    double *dot_v() { return dots + 2 * nc; }
+    double *dz_new() { return dots + 3 * nc; }
+    double *alpha_c() { return dots + 4 * nc; }
+    double *beta_c() { return dots + 5 * nc; }
+    double *scal() { return dots + 6 * nc; }  // single-image dots
+};
+
+namespace {
+
+template <class T>
+cgs_status dev_alloc(T **p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        *p = nullptr;
+        return CGS_ERR_OOM;
+    }
+    return CGS_OK;
+}
+
+void dev_free(void *p)
+{
+    if (p) cudaFree(p);
+}
+
+bool is_device_ptr(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+cudaStream_t pick_stream(cgs_plan *p, void *s) { return s ? (cudaStream_t)s : p->stream; }
+
+// bring caller data onto the device (returns a device pointer)
+cgs_status stage_in(const void *src, size_t bytes, void *staging, const void **dev, cudaStream_t st)
+{
+    if (is_device_ptr(src)) { *dev = src; return CGS_OK; }
+    CGS_CUDA(cudaMemcpyAsync(staging, src, bytes, cudaMemcpyHostToDevice, st));
+    *dev = staging;
+    return CGS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// NFFT building blocks on device layouts
+// ---------------------------------------------------------------------------
+AxisPass base_pass(cgs_plan *p, int t)
+{
+    AxisPass a{};
+    a.n = p->n[t];
+    a.tw = p->tw[t];
+    a.nfac = p->nfac[t];
+    for (int i = 0; i < 12; ++i) a.fac[i] = p->fac[t][i];
+    a.load_mode = LOAD_PLAIN;
+    a.store_mode = STORE_PLAIN;
+    a.o1_len = 1;
+    return a;
+}
+
+// forward NFFT of all coils.  src_img: single image (expand with sens) when
+// per_coil == 0, else coil-minor per-coil images.  mask may be null.
+cgs_status op_forward(cgs_plan *p, const float2 *src_img, int per_coil, const float *mask, float2 *ks,
+                      cudaStream_t st)
+{
+    const int d = p->d, nc = p->nc;
+    // pass over the fastest image axis (t = d-1), from the image side
+    {
+        AxisPass a = base_pass(p, d - 1);
+        int64_t outer = 1;
+        for (int t = 0; t < d - 1; ++t) outer *= p->N[t];
+        a.outer = outer; a.inner = nc; a.Lin = p->N[d - 1]; a.Lout = p->n[d - 1]; a.sign = -1; a.in_centred = 1;
+        a.load_mode = LOAD_IMAGE;
+        a.img = src_img; a.img_per_coil = per_coil;
+        a.sens = per_coil ? nullptr : p->sens;
+        a.mask = mask;
+        a.deap_ax = p->deap[d - 1];
+        a.deap_o1 = p->deap[d - 2]; a.o1_len = p->N[d - 2];
+        a.deap_o0 = (d == 3) ? p->deap[0] : nullptr;
+        a.dst = (d == 2) ? p->t1 : p->t1;
+        CGS_TRY(launch_axis_pass(a, st));
+    }
+    if (d == 2) {
+        AxisPass a = base_pass(p, 0);
+        a.outer = 1; a.inner = (int64_t)p->n[1] * nc; a.Lin = p->N[0]; a.Lout = p->n[0]; a.sign = -1; a.in_centred = 1;
+        a.src = p->t1; a.dst = p->grid;
+        CGS_TRY(launch_axis_pass(a, st));
+    } else {
+        AxisPass a = base_pass(p, 1);
+        a.outer = p->N[0]; a.inner = (int64_t)p->n[2] * nc; a.Lin = p->N[1]; a.Lout = p->n[1]; a.sign = -1; a.in_centred = 1;
+        a.src = p->t1; a.dst = p->t2;
+        CGS_TRY(launch_axis_pass(a, st));
+        AxisPass b = base_pass(p, 0);
+        b.outer = 1; b.inner = (int64_t)p->n[1] * p->n[2] * nc; b.Lin = p->N[0]; b.Lout = p->n[0]; b.sign = -1; b.in_centred = 1;
+        b.src = p->t2; b.dst = p->grid;
+        CGS_TRY(launch_axis_pass(b, st));
+    }
+    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work};
+    return launch_interp(p->geom, ns, p->grid, ks, st);
+}
+
+// adjoint NFFT of all coils into coil-minor per-coil images (deapodised)
+cgs_status op_adjoint(cgs_plan *p, const float2 *ks, int weighted, float2 *out, cudaStream_t st)
+{
+    const int d = p->d, nc = p->nc;
+    CGS_TRY(launch_zero(p->grid, sizeof(float2) * (size_t)p->ntot * nc, st));
+    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work};
+    CGS_TRY(launch_spread(p->geom, ns, ks, weighted && p->w != nullptr, p->grid, st));
+    const float2 *cur = p->grid;
+    if (d == 3) {
+        AxisPass a = base_pass(p, 0);
+        a.outer = 1; a.inner = (int64_t)p->n[1] * p->n[2] * nc; a.Lin = p->n[0]; a.Lout = p->N[0]; a.sign = +1; a.out_centred = 1;
+        a.src = cur; a.dst = p->t2;
+        CGS_TRY(launch_axis_pass(a, st));
+        AxisPass b = base_pass(p, 1);
+        b.outer = p->N[0]; b.inner = (int64_t)p->n[2] * nc; b.Lin = p->n[1]; b.Lout = p->N[1]; b.sign = +1; b.out_centred = 1;
+        b.src = p->t2; b.dst = p->t1;
+        CGS_TRY(launch_axis_pass(b, st));
+    } else {
+        AxisPass a = base_pass(p, 0);
+        a.outer = 1; a.inner = (int64_t)p->n[1] * nc; a.Lin = p->n[0]; a.Lout = p->N[0]; a.sign = +1; a.out_centred = 1;
+        a.src = cur; a.dst = p->t1;
+        CGS_TRY(launch_axis_pass(a, st));
+    }
+    AxisPass c = base_pass(p, d - 1);
+    int64_t outer = 1;
+    for (int t = 0; t < d - 1; ++t) outer *= p->N[t];
+    c.outer = outer; c.inner = nc; c.Lin = p->n[d - 1]; c.Lout = p->N[d - 1]; c.sign = +1; c.out_centred = 1;
+    c.src = p->t1; c.dst = out;
+    c.store_mode = STORE_DEAPOD;
+    c.deap_ax = p->deap[d - 1];
+    c.deap_o1 = p->deap[d - 2]; c.o1_len = p->N[d - 2];
+    c.deap_o0 = (d == 3) ? p->deap[0] : nullptr;
+    return launch_axis_pass(c, st);
+}
+
+// CGNR inverse NFFT per coil (codeare's NFFT::Adjoint) on sorted k-space ksIn
+// into coil-minor images cF.
+cgs_status op_itrafo(cgs_plan *p, const float2 *ksIn, int maxit, double eps, cudaStream_t st)
+{
+    const int nc = p->nc;
+    const int64_t M = p->M, Nt = p->Nt;
+    const float *w = p->w;
+    CGS_TRY(launch_zero(p->cF, sizeof(float2) * Nt * nc, st));
+    CGS_CUDA(cudaMemcpyAsync(p->ksR, ksIn, sizeof(float2) * M * nc, cudaMemcpyDeviceToDevice, st));
+    CGS_TRY(launch_coldot(p->ksR, p->ksR, w, M, nc, p->partial, p->dot_r(), st));
+    CGS_TRY(op_adjoint(p, p->ksR, 1, p->cZ, st));
+    CGS_CUDA(cudaMemcpyAsync(p->cP, p->cZ, sizeof(float2) * Nt * nc, cudaMemcpyDeviceToDevice, st));
+    CGS_TRY(launch_coldot(p->cZ, p->cZ, p->mask, Nt, nc, p->partial, p->dot_z(), st));
+    CGS_CUDA(cudaMemsetAsync(p->active, 0x01, sizeof(int) * nc, st));
+    for (int l = 0; l < maxit; ++l) {
+        CGS_TRY(launch_cgnr_scalars(0, nc, eps, p->active, p->dot_r(), p->dot_z(), p->dot_v(),
+                                    p->dz_new(), p->alpha_c(), p->beta_c(), st));
+        CGS_TRY(op_forward(p, p->cP, 1, p->mask, p->ksV, st));
+        CGS_TRY(launch_coldot(p->ksV, p->ksV, w, M, nc, p->partial, p->dot_v(), st));
+        CGS_TRY(launch_cgnr_scalars(1, nc, eps, p->active, p->dot_r(), p->dot_z(), p->dot_v(),
+                                    p->dz_new(), p->alpha_c(), p->beta_c(), st));
+        CGS_TRY(launch_axpy_cols(p->cF, p->alpha_c(), 1.0, p->mask, p->cP, Nt, nc, st));
+        CGS_TRY(launch_axpy_cols(p->ksR, p->alpha_c(), -1.0, nullptr, p->ksV, M, nc, st));
+        CGS_TRY(launch_coldot(p->ksR, p->ksR, w, M, nc, p->partial, p->dot_r(), st));
+        CGS_TRY(op_adjoint(p, p->ksR, 1, p->cZ, st));
+        CGS_TRY(launch_coldot(p->cZ, p->cZ, p->mask, Nt, nc, p->partial, p->dz_new(), st));
+        CGS_TRY(launch_cgnr_scalars(2, nc, eps, p->active, p->dot_r(), p->dot_z(), p->dot_v(),
+                                    p->dz_new(), p->alpha_c(), p->beta_c(), st));
+        CGS_TRY(launch_xpby_cols(p->cP, p->cZ, p->beta_c(), p->active, Nt, nc, st));
+    }
+    return CGS_OK;
+}
+
+// codeare E^H: x = I . sum conj(S) . itrafo(ks)
+cgs_status op_eh_codeare(cgs_plan *p, const float2 *ks, int ftiter, double fteps, float2 *x,
+                         cudaStream_t st)
+{
+    CGS_TRY(op_itrafo(p, ks, ftiter, fteps, st));
+    return launch_coil_combine(p->cF, p->sens, p->imap, p->Nt, p->nc, x, st);
+}
+
+// true E^H W: x = sum conj(S) . A^H (w ks)
+cgs_status op_eh(cgs_plan *p, const float2 *ks, int weighted, float2 *x, cudaStream_t st)
+{
+    CGS_TRY(op_adjoint(p, ks, weighted, p->cF, st));
+    return launch_coil_combine(p->cF, p->sens, nullptr, p->Nt, p->nc, x, st);
+}
+
+cgs_status check_ready(cgs_plan *p, bool need_w, bool need_s)
+{
+    if (!p) { set_error("null plan"); return CGS_ERR_BAD_ARG; }
+    if (!p->have_k) { set_error("k-space not set"); return CGS_ERR_STATE; }
+    if (need_w && !p->have_w) { set_error("weights not set"); return CGS_ERR_STATE; }
+    if (need_s && !p->have_s) { set_error("sensitivities not set"); return CGS_ERR_STATE; }
+    if (cudaSetDevice(p->device) != cudaSuccess) { set_error("cudaSetDevice failed"); return CGS_ERR_CUDA; }
+    return CGS_OK;
+}
+
+cgs_status read_scalars(cgs_plan *p, CGScalars *h, cudaStream_t st)
+{
+    CGS_CUDA(cudaMemcpyAsync(h, p->sc, sizeof(CGScalars), cudaMemcpyDeviceToHost, st));
+    CGS_CUDA(cudaStreamSynchronize(st));
+    return CGS_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char *cgs_last_error(void) { return g_last_error.c_str(); }
+
+int64_t cgs_kernel_launches(void) { return g_launches.load(); }
+
+void cgs_profile_enable(int on)
+{
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (!on) prof_drain();
+    g_prof_on = (on != 0);
+}
+
+void cgs_profile_collect(double *ms, int64_t *count)
+{
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    prof_drain();
+    for (int c = 0; c < PROF_NCAT; ++c) {
+        if (ms) ms[c] = g_prof_ms[c];
+        if (count) count[c] = g_prof_cnt[c];
+        g_prof_ms[c] = 0.0;
+        g_prof_cnt[c] = 0;
+    }
+}
+
+cgs_status cgs_plan_create(cgs_plan **out, const cgs_plan_desc *desc)
+{
+    if (!out || !desc) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    *out = nullptr;
+    if (desc->rank != 2 && desc->rank != 3) { set_error("rank must be 2 or 3"); return CGS_ERR_BAD_ARG; }
+    if (desc->ncoils < 1 || desc->M < 1 || desc->m < 0 || desc->m > 8 || !(desc->alpha >= 1.0)) {
+        set_error("bad ncoils / M / m / alpha");
+        return CGS_ERR_BAD_ARG;
+    }
+    if (desc->M > 0x7fffffffLL) { set_error("M too large"); return CGS_ERR_BAD_ARG; }
+    cgs_plan *p = new cgs_plan();
+    p->d = desc->rank; p->m = desc->m; p->nc = desc->ncoils; p->M = desc->M; p->alpha = desc->alpha;
+    for (int t = 0; t < p->d; ++t) {
+        if (desc->N[t] < 2 || (desc->N[t] & 1)) { delete p; set_error("N must be even and >= 2"); return CGS_ERR_BAD_ARG; }
+        p->N[t] = desc->N[t];
+        p->n[t] = (int)std::ceil(desc->alpha * desc->N[t]);
+        if (p->n[t] < p->N[t]) p->n[t] = p->N[t];
+        if (p->n[t] > 2048) { delete p; set_error("oversampled grid side above 2048"); return CGS_ERR_BAD_ARG; }
+        if (!factorize(p->n[t], p->fac[t], &p->nfac[t])) {
+            delete p;
+            set_error("oversampled size must factor into 2, 3, 5 and 7");
+            return CGS_ERR_BAD_ARG;
+        }
+        p->Nt *= p->N[t];
+        p->ntot *= p->n[t];
+    }
+    cudaGetDevice(&p->device);
+    cgs_status st = CGS_OK;
+#define ALLOC(ptr, cnt) do { st = dev_alloc(&(ptr), (cnt)); if (st != CGS_OK) { cgs_plan_destroy(p); return st; } } while (0)
+    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete p; set_error("stream creation failed"); return CGS_ERR_CUDA;
+    }
+    cudaEventCreate(&p->ev0);
+    cudaEventCreate(&p->ev1);
+    // twiddles and deapodisation tables
+    for (int t = 0; t < p->d; ++t) {
+        const int n = p->n[t], N = p->N[t];
+        std::vector<float2> tw(n);
+        for (int i = 0; i < n; ++i) {
+            const double a = -2.0 * M_PI * (double)i / (double)n;
+            tw[i] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+        const double sigma = (double)n / (double)N;
+        const double b = M_PI * (2.0 - 1.0 / sigma);
+        p->geom.b[t] = (float)b;
+        std::vector<float> dp(N);
+        for (int i = 0; i < N; ++i) {
+            const double w = 2.0 * M_PI * (double)(i - N / 2) / (double)n;
+            double a = b * b - w * w;
+            if (a < 0) a = 0;
+            dp[i] = (float)(1.0 / bessel_i0((double)p->m * std::sqrt(a)));
+        }
+        ALLOC(p->tw[t], n);
+        ALLOC(p->deap[t], N);
+        cudaMemcpy(p->tw[t], tw.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
+        cudaMemcpy(p->deap[t], dp.data(), sizeof(float) * N, cudaMemcpyHostToDevice);
+    }
+    // geometry of the gridding tiles
+    GridGeom &g = p->geom;
+    g.d = p->d; g.m = p->m; g.nc = p->nc;
+    g.T = (p->d == 2) ? 32 : 8;
+    for (int t = 0; t < p->d; ++t) {
+        if (g.T > p->n[t]) g.T = p->n[t];
+    }
+    for (int t = 0; t < 3; ++t) { g.n[t] = (t < p->d) ? p->n[t] : 1; g.nt[t] = 1; }
+    for (int t = 0; t < p->d; ++t) g.nt[t] = (p->n[t] + g.T - 1) / g.T;
+    const int64_t nc = p->nc, M = p->M, Nt = p->Nt, nT = p->ntot;
+    // damping mask What (NFFTTraits.hpp:225-260): radius N[0]/2 around index N[0]/2
+    {
+        std::vector<float> mk(Nt);
+        const int N0 = p->N[0], NH = (int)(0.5 * N0);
+        for (int64_t k = 0; k < Nt; ++k) {
+            int64_t r = k;
+            double s = 0;
+            for (int t = p->d - 1; t >= 0; --t) {
+                const int i = (int)(r % p->N[t]);
+                r /= p->N[t];
+                const double q = (double)(i - NH);
+                s += q * q;
+            }
+            mk[k] = (std::sqrt(s) > (double)NH) ? 0.f : 1.f;
+        }
+        ALLOC(p->mask, Nt);
+        cudaMemcpy(p->mask, mk.data(), sizeof(float) * Nt, cudaMemcpyHostToDevice);
+    }
+    ALLOC(p->imap, Nt);
+    ALLOC(p->sens, Nt * nc);
+    ALLOC(p->grid, nT * nc);
+    {
+        int64_t t1 = 1;
+        for (int t = 0; t < p->d - 1; ++t) t1 *= p->N[t];
+        t1 *= p->n[p->d - 1];
+        ALLOC(p->t1, t1 * nc);
+        if (p->d == 3) ALLOC(p->t2, (int64_t)p->N[0] * p->n[1] * p->n[2] * nc);
+    }
+    ALLOC(p->ksY, M * nc); ALLOC(p->ksR, M * nc); ALLOC(p->ksV, M * nc);
+    ALLOC(p->cF, Nt * nc); ALLOC(p->cP, Nt * nc); ALLOC(p->cZ, Nt * nc);
+    ALLOC(p->vX, Nt); ALLOC(p->vR, Nt); ALLOC(p->vP, Nt); ALLOC(p->vQ, Nt);
+    const int64_t io = std::max(Nt * nc, M * nc);
+    ALLOC(p->ioA, io); ALLOC(p->ioB, io);
+    ALLOC(p->partial, (size_t)dot_blocks() * std::max<int64_t>(nc, 1));
+    ALLOC(p->dots, 8 * nc + 8);
+    ALLOC(p->active, nc);
+    ALLOC(p->sc, 1);
+    ALLOC(p->nodes, (size_t)M * (p->d == 2 ? 1 : 2));
+    ALLOC(p->perm, M);
+    ALLOC(p->w, M);
+#undef ALLOC
+    *out = p;
+    return CGS_OK;
+}
+
+cgs_status cgs_plan_destroy(cgs_plan *p)
+{
+    if (!p) return CGS_OK;
+    cudaSetDevice(p->device);
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    void *bufs[] = {p->tw[0], p->tw[1], p->tw[2], p->deap[0], p->deap[1], p->deap[2], p->nodes, p->perm,
+                    p->w, p->work, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
+                    p->cF, p->cP, p->cZ, p->vX, p->vR, p->vP, p->vQ, p->ioA, p->ioB, p->partial, p->dots,
+                    p->active, p->sc};
+    for (void *b : bufs) dev_free(b);
+    if (p->ev0) cudaEventDestroy(p->ev0);
+    if (p->ev1) cudaEventDestroy(p->ev1);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+    return CGS_OK;
+}
+
+cgs_status cgs_plan_info(const cgs_plan *p, int *rank, int *N, int *n, int64_t *M, int *ncoils)
+{
+    if (!p) { set_error("null plan"); return CGS_ERR_BAD_ARG; }
+    if (rank) *rank = p->d;
+    for (int t = 0; t < 3; ++t) {
+        if (N) N[t] = p->N[t];
+        if (n) n[t] = p->n[t];
+    }
+    if (M) *M = p->M;
+    if (ncoils) *ncoils = p->nc;
+    return CGS_OK;
+}
+
+cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
+{
+    if (!p || !k_in) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    CGS_CUDA(cudaSetDevice(p->device));
+    const int d = p->d;
+    const int64_t M = p->M;
+    std::vector<float> k((size_t)M * d);
+    if (is_device_ptr(k_in)) {
+        CGS_CUDA(cudaMemcpy(k.data(), k_in, sizeof(float) * k.size(), cudaMemcpyDeviceToHost));
+    } else {
+        std::memcpy(k.data(), k_in, sizeof(float) * k.size());
+    }
+    const GridGeom &g = p->geom;
+    int ntiles = 1;
+    for (int t = 0; t < d; ++t) ntiles *= g.nt[t];
+    std::vector<int> tile(M), cnt(ntiles + 1, 0);
+    std::vector<float> frac((size_t)M * d);
+    std::vector<int> cc((size_t)M * d);
+    for (int64_t j = 0; j < M; ++j) {
+        int ti = 0;
+        for (int t = 0; t < d; ++t) {
+            const double x = (double)k[(size_t)j * d + t];
+            if (!(x >= -0.5 && x < 0.5)) {
+                set_error("k-space coordinate outside [-0.5, 0.5)");
+                return CGS_ERR_BAD_ARG;
+            }
+            const double nx = (double)p->n[t] * x;
+            const double c = std::floor(nx);
+            frac[(size_t)j * d + t] = (float)(nx - c);
+            cc[(size_t)j * d + t] = (int)c;
+            int u = ((int)c - p->m) % p->n[t];
+            if (u < 0) u += p->n[t];
+            ti = ti * g.nt[t] + u / g.T;
+        }
+        tile[j] = ti;
+        cnt[ti + 1]++;
+    }
+    for (int i = 0; i < ntiles; ++i) cnt[i + 1] += cnt[i];
+    std::vector<int> perm(M), fill(cnt.begin(), cnt.end() - 1);
+    for (int64_t j = 0; j < M; ++j) perm[fill[tile[j]]++] = (int)j;
+    const int per = (d == 2) ? 1 : 2;
+    std::vector<float4> nodes((size_t)M * per);
+    for (int64_t s = 0; s < M; ++s) {
+        const int j = perm[s];
+        if (d == 2) {
+            float4 a;
+            a.x = frac[(size_t)j * 2]; a.y = frac[(size_t)j * 2 + 1];
+            int c0 = cc[(size_t)j * 2], c1 = cc[(size_t)j * 2 + 1];
+            std::memcpy(&a.z, &c0, 4); std::memcpy(&a.w, &c1, 4);
+            nodes[s] = a;
+        } else {
+            float4 a, b;
+            a.x = frac[(size_t)j * 3]; a.y = frac[(size_t)j * 3 + 1]; a.z = frac[(size_t)j * 3 + 2]; a.w = 0.f;
+            int c0 = cc[(size_t)j * 3], c1 = cc[(size_t)j * 3 + 1], c2 = cc[(size_t)j * 3 + 2], z = 0;
+            std::memcpy(&b.x, &c0, 4); std::memcpy(&b.y, &c1, 4); std::memcpy(&b.z, &c2, 4); std::memcpy(&b.w, &z, 4);
+            nodes[2 * s] = a; nodes[2 * s + 1] = b;
+        }
+    }
+    // work items: bins split into slices of at most kWork nodes
+    const int kWork = 1024;
+    std::vector<int4> work;
+    for (int ti = 0; ti < ntiles; ++ti) {
+        for (int s0 = cnt[ti]; s0 < cnt[ti + 1]; s0 += kWork) {
+            const int c = std::min(kWork, cnt[ti + 1] - s0);
+            work.push_back(make_int4(ti, s0, c, 0));
+        }
+    }
+    dev_free(p->work);
+    p->work = nullptr;
+    CGS_TRY(dev_alloc(&p->work, work.size()));
+    p->nwork = (int)work.size();
+    CGS_CUDA(cudaMemcpy(p->work, work.data(), sizeof(int4) * work.size(), cudaMemcpyHostToDevice));
+    CGS_CUDA(cudaMemcpy(p->nodes, nodes.data(), sizeof(float4) * nodes.size(), cudaMemcpyHostToDevice));
+    CGS_CUDA(cudaMemcpy(p->perm, perm.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+    p->have_k = true;
+    // weights (if already given) must follow the new order: reset to "unset"
+    p->have_w = false;
+    CGS_CUDA(cudaMemset(p->w, 0, sizeof(float) * M));
+    return CGS_OK;
+}
+
+cgs_status cgs_set_weights(cgs_plan *p, const float *w_in)
+{
+    if (!p || !w_in) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    if (!p->have_k) { set_error("set k-space before weights (NFFT.hpp:281-296 needs the nodes)"); return CGS_ERR_STATE; }
+    CGS_CUDA(cudaSetDevice(p->device));
+    const int64_t M = p->M;
+    std::vector<float> w(M), ws(M);
+    std::vector<int> perm(M);
+    if (is_device_ptr(w_in)) CGS_CUDA(cudaMemcpy(w.data(), w_in, sizeof(float) * M, cudaMemcpyDeviceToHost));
+    else std::memcpy(w.data(), w_in, sizeof(float) * M);
+    CGS_CUDA(cudaMemcpy(perm.data(), p->perm, sizeof(int) * M, cudaMemcpyDeviceToHost));
+    for (int64_t s = 0; s < M; ++s) ws[s] = w[perm[s]];
+    CGS_CUDA(cudaMemcpy(p->w, ws.data(), sizeof(float) * M, cudaMemcpyHostToDevice));
+    p->have_w = true;
+    return CGS_OK;
+}
+
+cgs_status cgs_set_sensitivities(cgs_plan *p, const float *s_in)
+{
+    if (!p || !s_in) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    CGS_CUDA(cudaSetDevice(p->device));
+    cudaStream_t st = p->stream;
+    const void *src;
+    CGS_TRY(stage_in(s_in, sizeof(float2) * p->Nt * p->nc, p->ioA, &src, st));
+    CGS_TRY(launch_to_coil_minor((const float2 *)src, p->Nt, p->nc, p->sens, st));
+    CGS_TRY(launch_intensity(p->sens, p->Nt, p->nc, p->imap, st));
+    CGS_CUDA(cudaStreamSynchronize(st));
+    p->have_s = true;
+    return CGS_OK;
+}
+
+cgs_status cgs_sync(cgs_plan *p)
+{
+    if (!p) { set_error("null plan"); return CGS_ERR_BAD_ARG; }
+    CGS_CUDA(cudaStreamSynchronize(p->stream));
+    return CGS_OK;
+}
+
+// per-coil images (coil-major, caller) -> samples (coil-major, caller)
+cgs_status cgs_nfft_trafo(cgs_plan *p, const float *fhat, float *f, void *stream)
+{
+    CGS_TRY(check_ready(p, false, false));
+    if (!fhat || !f) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    cudaStream_t st = pick_stream(p, stream);
+    const void *src;
+    CGS_TRY(stage_in(fhat, sizeof(float2) * p->Nt * p->nc, p->ioA, &src, st));
+    CGS_TRY(launch_to_coil_minor((const float2 *)src, p->Nt, p->nc, p->cF, st));
+    CGS_TRY(op_forward(p, p->cF, 1, nullptr, p->ksV, st));
+    const bool dev = is_device_ptr(f);
+    float2 *dst = dev ? (float2 *)f : p->ioB;
+    CGS_TRY(launch_scatter_ks(p->ksV, p->perm, p->M, p->nc, dst, st));
+    if (!dev) {
+        CGS_CUDA(cudaMemcpyAsync(f, dst, sizeof(float2) * p->M * p->nc, cudaMemcpyDeviceToHost, st));
+        CGS_CUDA(cudaStreamSynchronize(st));
+    }
+    return CGS_OK;
+}
+
+static cgs_status ks_in(cgs_plan *p, const float *y, cudaStream_t st)
+{
+    const void *src;
+    CGS_TRY(stage_in(y, sizeof(float2) * p->M * p->nc, p->ioA, &src, st));
+    return launch_gather_ks((const float2 *)src, p->perm, p->M, p->nc, p->ksY, st);
+}
+
+static cgs_status coil_images_out(cgs_plan *p, const float2 *cm, float *out, cudaStream_t st)
+{
+    const bool dev = is_device_ptr(out);
+    float2 *dst = dev ? (float2 *)out : p->ioB;
+    CGS_TRY(launch_to_coil_major(cm, p->Nt, p->nc, dst, st));
+    if (!dev) {
+        CGS_CUDA(cudaMemcpyAsync(out, dst, sizeof(float2) * p->Nt * p->nc, cudaMemcpyDeviceToHost, st));
+        CGS_CUDA(cudaStreamSynchronize(st));
+    }
+    return CGS_OK;
+}
+
+static cgs_status image_out(cgs_plan *p, const float2 *img, float *out, cudaStream_t st)
+{
+    if (is_device_ptr(out)) {
+        if ((const void *)img != (const void *)out)
+            CGS_CUDA(cudaMemcpyAsync(out, img, sizeof(float2) * p->Nt, cudaMemcpyDeviceToDevice, st));
+    } else {
+        CGS_CUDA(cudaMemcpyAsync(out, img, sizeof(float2) * p->Nt, cudaMemcpyDeviceToHost, st));
+        CGS_CUDA(cudaStreamSynchronize(st));
+    }
+    return CGS_OK;
+}
+
+cgs_status cgs_nfft_adjoint(cgs_plan *p, const float *f, float *fhat, void *stream)
+{
+    CGS_TRY(check_ready(p, false, false));
+    if (!fhat || !f) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    cudaStream_t st = pick_stream(p, stream);
+    CGS_TRY(ks_in(p, f, st));
+    CGS_TRY(op_adjoint(p, p->ksY, 0, p->cF, st));
+    return coil_images_out(p, p->cF, fhat, st);
+}
+
+cgs_status cgs_nfft_itrafo(cgs_plan *p, const float *f, float *fhat, int maxit, double eps, void *stream)
+{
+    CGS_TRY(check_ready(p, true, false));
+    if (!fhat || !f || maxit < 0) { set_error("bad argument"); return CGS_ERR_BAD_ARG; }
+    cudaStream_t st = pick_stream(p, stream);
+    CGS_TRY(ks_in(p, f, st));
+    CGS_TRY(op_itrafo(p, p->ksY, maxit, eps, st));
+    return coil_images_out(p, p->cF, fhat, st);
+}
+
+cgs_status cgs_sense_trafo(cgs_plan *p, const float *x, float *y, void *stream)
+{
+    CGS_TRY(check_ready(p, false, true));
+    if (!x || !y) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    cudaStream_t st = pick_stream(p, stream);
+    const void *src;
+    CGS_TRY(stage_in(x, sizeof(float2) * p->Nt, p->ioA, &src, st));
+    CGS_TRY(op_forward(p, (const float2 *)src, 0, nullptr, p->ksV, st));
+    const bool dev = is_device_ptr(y);
+    float2 *dst = dev ? (float2 *)y : p->ioB;
+    CGS_TRY(launch_scatter_ks(p->ksV, p->perm, p->M, p->nc, dst, st));
+    if (!dev) {
+        CGS_CUDA(cudaMemcpyAsync(y, dst, sizeof(float2) * p->M * p->nc, cudaMemcpyDeviceToHost, st));
+        CGS_CUDA(cudaStreamSynchronize(st));
+    }
+    return CGS_OK;
+}
+
+cgs_status cgs_sense_adjoint_codeare(cgs_plan *p, const float *y, float *x, int ftiter, double fteps,
+                                     void *stream)
+{
+    CGS_TRY(check_ready(p, true, true));
+    if (!x || !y || ftiter < 0) { set_error("bad argument"); return CGS_ERR_BAD_ARG; }
+    cudaStream_t st = pick_stream(p, stream);
+    CGS_TRY(ks_in(p, y, st));
+    CGS_TRY(op_eh_codeare(p, p->ksY, ftiter, fteps, p->vX, st));
+    return image_out(p, p->vX, x, st);
+}
+
+cgs_status cgs_sense_adjoint(cgs_plan *p, const float *y, float *x, int weighted, void *stream)
+{
+    CGS_TRY(check_ready(p, weighted != 0, true));
+    if (!x || !y) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    cudaStream_t st = pick_stream(p, stream);
+    CGS_TRY(ks_in(p, y, st));
+    CGS_TRY(op_eh(p, p->ksY, weighted, p->vX, st));
+    return image_out(p, p->vX, x, st);
+}
+
+cgs_status cgs_solve(cgs_plan *p, const float *y, float *x, const cgs_solve_opts *o,
+                     cgs_solve_report *rep, void *stream)
+{
+    if (!o) { set_error("null options"); return CGS_ERR_BAD_ARG; }
+    const bool codeare = (o->mode == CGS_MODE_CODEARE);
+    CGS_TRY(check_ready(p, codeare || o->weighted, true));
+    if (!x || !y || o->cgiter < 0 || o->ftiter < 0) { set_error("bad argument"); return CGS_ERR_BAD_ARG; }
+    cudaStream_t st = pick_stream(p, stream);
+    const int64_t Nt = p->Nt;
+    if (rep) std::memset(rep, 0, sizeof(*rep));
+    CGS_CUDA(cudaEventRecord(p->ev0, st));
+    CGS_TRY(ks_in(p, y, st));
+    // p = A/b (codeare) or b = E^H W y (standard)
+    if (codeare) CGS_TRY(op_eh_codeare(p, p->ksY, o->ftiter, o->fteps, p->vP, st));
+    else CGS_TRY(op_eh(p, p->ksY, o->weighted, p->vP, st));
+    int iters = 0;
+    cgs_status result = CGS_OK;
+    if (o->cgiter == 0 && codeare) {
+        CGS_CUDA(cudaMemcpyAsync(p->vX, p->vP, sizeof(float2) * Nt, cudaMemcpyDeviceToDevice, st));
+    } else {
+        CGScalars init{};
+        init.lambda = o->lambda;
+        CGS_CUDA(cudaMemcpyAsync(p->sc, &init, sizeof(init), cudaMemcpyHostToDevice, st));
+        CGS_CUDA(cudaMemcpyAsync(p->vR, p->vP, sizeof(float2) * Nt, cudaMemcpyDeviceToDevice, st));
+        CGS_TRY(launch_zero(p->vX, sizeof(float2) * Nt, st));
+        CGS_TRY(launch_coldot(p->vR, p->vP, nullptr, Nt, 1, p->partial, p->scal(), st));
+        CGS_TRY(launch_scalar_op(p->sc, p->scal(), 0, st));
+        for (int i = 0; i < o->cgiter; ++i) {
+            CGScalars h;
+            CGS_TRY(read_scalars(p, &h, st));
+            const double res = codeare ? h.rn / h.xn : std::sqrt(h.rn / h.xn);
+            if (rep) {
+                if (i == 0) rep->res_first = res;
+                if (i < 256) rep->res_hist[i] = res;
+                rep->res_last = res;
+            }
+            if (std::isnan(res)) { result = CGS_ERR_NAN; break; }
+            if (res <= o->cgeps) break;
+            if (codeare) {
+                CGS_TRY(op_forward(p, p->vP, 0, nullptr, p->ksV, st));
+                CGS_TRY(op_eh_codeare(p, p->ksV, o->ftiter, o->fteps, p->vQ, st));
+            } else {
+                CGS_TRY(op_forward(p, p->vP, 0, nullptr, p->ksV, st));
+                CGS_TRY(op_eh(p, p->ksV, o->weighted, p->vQ, st));
+            }
+            if (o->lambda != 0.0) CGS_TRY(launch_add_scaled(p->vQ, p->vP, p->sc, Nt, st));
+            CGS_TRY(launch_coldot(p->vP, p->vQ, nullptr, Nt, 1, p->partial, p->scal(), st));
+            CGS_TRY(launch_scalar_op(p->sc, p->scal(), 1, st));
+            CGS_TRY(launch_cg_update_xr(p->vX, p->vR, p->vP, p->vQ, p->sc, Nt, st));
+            CGS_TRY(launch_coldot(p->vR, p->vR, nullptr, Nt, 1, p->partial, p->scal(), st));
+            CGS_TRY(launch_scalar_op(p->sc, p->scal(), 2, st));
+            CGS_TRY(launch_cg_update_p(p->vP, p->vR, p->sc, Nt, st));
+            iters = i + 1;
+        }
+        if (!codeare || o->cgiter > 0) {
+            // residual after the last update (standard mode reports it)
+            CGScalars h;
+            CGS_TRY(read_scalars(p, &h, st));
+            if (rep && !codeare) {
+                const double res = std::sqrt(h.rn / h.xn);
+                rep->res_last = res;
+                if (iters < 256) rep->res_hist[iters] = res;
+            }
+        }
+    }
+    CGS_CUDA(cudaEventRecord(p->ev1, st));
+    CGS_TRY(image_out(p, p->vX, x, st));
+    CGS_CUDA(cudaEventSynchronize(p->ev1));
+    if (rep) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+        rep->seconds = ms * 1e-3;
+        rep->iterations = iters;
+    }
+    return result;
+}
+
+}  // extern "C"

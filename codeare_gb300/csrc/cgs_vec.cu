@@ -1,0 +1,408 @@
+// cgs_vec.cu -- memory-bound vector kernels of the CG-SENSE path.
+//
+// Dot products take FP32 operands and accumulate in FP64 per thread, then in a
+// fixed-shape block tree and a fixed-order final pass, so results do not depend
+// on scheduling (the reference's dotc accumulates sequentially in
+// complex<float>, src/matrix/linalg/Lapack.hpp:619-624).
+#include "cgs_internal.cuh"
+
+namespace cgs {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kDotBlocks = 304;  // 2 x 152 SMs
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// user[c][perm[s]] -> ks[s][c]
+__global__ void gather_ks_kernel(const float2 *__restrict__ user, const int *__restrict__ perm,
+                                 int64_t M, int nc, float2 *__restrict__ ks)
+{
+    const int64_t total = M * nc;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = e / nc;
+        const int c = (int)(e % nc);
+        ks[e] = user[(int64_t)c * M + perm[s]];
+    }
+}
+
+__global__ void scatter_ks_kernel(const float2 *__restrict__ ks, const int *__restrict__ perm,
+                                  int64_t M, int nc, float2 *__restrict__ user)
+{
+    const int64_t total = M * nc;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = e / nc;
+        const int c = (int)(e % nc);
+        user[(int64_t)c * M + perm[s]] = ks[e];
+    }
+}
+
+// tiled transpose between (nc, P) and (P, nc)
+__global__ void transpose_kernel(const float2 *__restrict__ a, int64_t rows, int64_t cols,
+                                 float2 *__restrict__ out)
+{
+    __shared__ float2 t[32][33];
+    const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
+    for (int k = threadIdx.y; k < 32; k += 8) {
+        const int64_t r = r0 + k, c = c0 + threadIdx.x;
+        if (r < rows && c < cols) t[k][threadIdx.x] = a[r * cols + c];
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += 8) {
+        const int64_t c = c0 + k, r = r0 + threadIdx.x;
+        if (r < rows && c < cols) out[c * rows + r] = t[threadIdx.x][k];
+    }
+}
+
+// per-column partial dots; block b handles a contiguous row range
+__global__ void __launch_bounds__(kThreads)
+coldot_partial_kernel(const float2 *__restrict__ a, const float2 *__restrict__ b,
+                      const float *__restrict__ wr, int64_t rows, int nc, double *__restrict__ partial)
+{
+    extern __shared__ double sred[];
+    const int64_t per = (rows + gridDim.x - 1) / gridDim.x;
+    const int64_t rbeg = (int64_t)blockIdx.x * per;
+    const int64_t rend = min(rows, rbeg + per);
+    // thread layout: column c = t % ncl, row lane = t / ncl, with ncl = min(nc, 256)
+    const int ncl = nc < kThreads ? nc : kThreads;
+    const int lanes = kThreads / ncl;
+    const int t = threadIdx.x;
+    const int lr = t / ncl;
+    for (int cb = 0; cb < nc; cb += ncl) {
+        const int c = cb + t % ncl;
+        double acc = 0.0;
+        if (lr < lanes && c < nc) {
+            for (int64_t r = rbeg + lr; r < rend; r += lanes) {
+                const float2 x = a[r * nc + c], y = b[r * nc + c];
+                float v = fmaf(x.x, y.x, x.y * y.y);
+                double dv = (double)v;
+                if (wr) dv *= (double)wr[r];
+                acc += dv;
+            }
+        }
+        sred[t] = (lr < lanes) ? acc : 0.0;
+        __syncthreads();
+        // reduce over the row lanes of each column (fixed order)
+        if (t < ncl) {
+            double s = 0.0;
+            for (int l = 0; l < lanes; ++l) s += sred[l * ncl + t];
+            if (cb + t < nc) partial[(int64_t)blockIdx.x * nc + cb + t] = s;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void coldot_final_kernel(const double *__restrict__ partial, int nblk, int nc,
+                                    double *__restrict__ out)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int b = 0; b < nblk; ++b) s += partial[(int64_t)b * nc + c];
+        out[c] = s;
+    }
+}
+
+__global__ void cgnr_scalars_kernel(int mode, int nc, double eps, int *active, const double *dot_r,
+                                    double *dot_z, const double *dot_v, const double *dz_new,
+                                    double *alpha, double *beta)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    if (mode == 0) {
+        active[c] = active[c] && !(dot_r[c] < eps);
+    } else if (mode == 1) {
+        alpha[c] = active[c] ? dot_z[c] / dot_v[c] : 0.0;
+    } else {
+        if (active[c]) {
+            beta[c] = dz_new[c] / dot_z[c];
+            dot_z[c] = dz_new[c];
+        } else {
+            beta[c] = 0.0;
+        }
+    }
+}
+
+__global__ void axpy_cols_kernel(float2 *__restrict__ x, const double *__restrict__ alpha, double sgn,
+                                 const float *__restrict__ mask, const float2 *__restrict__ p,
+                                 int64_t rows, int nc)
+{
+    const int64_t total = rows * nc;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / nc;
+        const int c = (int)(e % nc);
+        const double a = sgn * alpha[c];
+        if (a == 0.0) continue;
+        float s = (float)a;
+        if (mask) s *= mask[r];
+        const float2 v = p[e];
+        float2 y = x[e];
+        y.x = fmaf(s, v.x, y.x); y.y = fmaf(s, v.y, y.y);
+        x[e] = y;
+    }
+}
+
+__global__ void xpby_cols_kernel(float2 *__restrict__ p, const float2 *__restrict__ z,
+                                 const double *__restrict__ beta, const int *__restrict__ active,
+                                 int64_t rows, int nc)
+{
+    const int64_t total = rows * nc;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(e % nc);
+        if (active && !active[c]) continue;
+        const float bb = (float)beta[c];
+        const float2 v = z[e];
+        float2 y = p[e];
+        y.x = fmaf(bb, y.x, v.x); y.y = fmaf(bb, y.y, v.y);
+        p[e] = y;
+    }
+}
+
+__global__ void add_scaled_kernel(float2 *__restrict__ q, const float2 *__restrict__ p,
+                                  const CGScalars *__restrict__ sc, int64_t n)
+{
+    if (sc->done) return;
+    const float l = (float)sc->lambda;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        float2 a = q[e];
+        const float2 b = p[e];
+        a.x = fmaf(l, b.x, a.x); a.y = fmaf(l, b.y, a.y);
+        q[e] = a;
+    }
+}
+
+__global__ void cg_update_xr_kernel(float2 *__restrict__ x, float2 *__restrict__ r,
+                                    const float2 *__restrict__ p, const float2 *__restrict__ q,
+                                    CGScalars *__restrict__ sc, int64_t n)
+{
+    if (sc->done) return;
+    const double tsd = sc->rn / sc->pq;
+    const float ts = (float)tsd;
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->ts = tsd;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const float2 pv = p[e], qv = q[e];
+        float2 xv = x[e], rv = r[e];
+        xv.x = fmaf(ts, pv.x, xv.x); xv.y = fmaf(ts, pv.y, xv.y);
+        rv.x = fmaf(-ts, qv.x, rv.x); rv.y = fmaf(-ts, qv.y, rv.y);
+        x[e] = xv; r[e] = rv;
+    }
+}
+
+__global__ void cg_update_p_kernel(float2 *__restrict__ p, const float2 *__restrict__ r,
+                                   const CGScalars *__restrict__ sc, int64_t n)
+{
+    if (sc->done) return;
+    const float bb = (float)(sc->rn / sc->rno);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const float2 rv = r[e];
+        float2 pv = p[e];
+        pv.x = fmaf(bb, pv.x, rv.x); pv.y = fmaf(bb, pv.y, rv.y);
+        p[e] = pv;
+    }
+}
+
+// op 0: rn = xn = *src; 1: pq = *src; 2: rno = rn, rn = *src
+__global__ void scalar_op_kernel(CGScalars *sc, const double *src, int op)
+{
+    if (op == 0) { sc->rn = *src; sc->xn = *src; }
+    else if (op == 1) { sc->pq = *src; }
+    else if (op == 2) { sc->rno = sc->rn; sc->rn = *src; }
+}
+
+__global__ void intensity_kernel(const float2 *__restrict__ S, int64_t P, int nc, float *__restrict__ I)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int c = 0; c < nc; ++c) {
+            const float2 v = S[p * nc + c];
+            s = fmaf(v.x, v.x, fmaf(v.y, v.y, s));
+        }
+        I[p] = 1.f / (sqrtf(s) + 1.0e-9f);
+    }
+}
+
+__global__ void coil_combine_kernel(const float2 *__restrict__ F, const float2 *__restrict__ S,
+                                    const float *__restrict__ I, int64_t P, int nc, float2 *__restrict__ x)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        float ax = 0.f, ay = 0.f;
+        for (int c = 0; c < nc; ++c) {
+            const float2 f = F[p * nc + c], s = S[p * nc + c];
+            // conj(s) * f
+            ax = fmaf(s.x, f.x, fmaf(s.y, f.y, ax));
+            ay = fmaf(s.x, f.y, fmaf(-s.y, f.x, ay));
+        }
+        const float g = I ? I[p] : 1.f;
+        x[p] = make_float2(ax * g, ay * g);
+    }
+}
+
+__global__ void scale_real_kernel(float2 *__restrict__ x, const float *__restrict__ s, int64_t n)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const float f = s[e];
+        float2 v = x[e];
+        v.x *= f; v.y *= f;
+        x[e] = v;
+    }
+}
+
+unsigned grid_for(int64_t n)
+{
+    int64_t b = (n + kThreads - 1) / kThreads;
+    if (b > 152 * 16) b = 152 * 16;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+}  // namespace
+
+int dot_blocks() { return kDotBlocks; }
+
+cgs_status launch_gather_ks(const float2 *user, const int *perm, int64_t M, int nc, float2 *ks,
+                            cudaStream_t st)
+{
+    if (M * nc == 0) return CGS_OK;
+    gather_ks_kernel<<<grid_for(M * nc), kThreads, 0, st>>>(user, perm, M, nc, ks);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_scatter_ks(const float2 *ks, const int *perm, int64_t M, int nc, float2 *user,
+                             cudaStream_t st)
+{
+    if (M * nc == 0) return CGS_OK;
+    scatter_ks_kernel<<<grid_for(M * nc), kThreads, 0, st>>>(ks, perm, M, nc, user);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_to_coil_minor(const float2 *a, int64_t P, int nc, float2 *out, cudaStream_t st)
+{
+    // a: (nc rows, P cols) -> out: (P rows, nc cols)
+    if (P * nc == 0) return CGS_OK;
+    dim3 grd((unsigned)((P + 31) / 32), (unsigned)((nc + 31) / 32));
+    transpose_kernel<<<grd, dim3(32, 8), 0, st>>>(a, nc, P, out);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_to_coil_major(const float2 *a, int64_t P, int nc, float2 *out, cudaStream_t st)
+{
+    if (P * nc == 0) return CGS_OK;
+    dim3 grd((unsigned)((nc + 31) / 32), (unsigned)((P + 31) / 32));
+    transpose_kernel<<<grd, dim3(32, 8), 0, st>>>(a, P, nc, out);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_coldot(const float2 *a, const float2 *b, const float *wr, int64_t rows, int nc,
+                         double *partial, double *out, cudaStream_t st)
+{
+    coldot_partial_kernel<<<kDotBlocks, kThreads, kThreads * sizeof(double), st>>>(a, b, wr, rows, nc,
+                                                                                  partial);
+    CGS_LAUNCH_CHECK();
+    coldot_final_kernel<<<(nc + 127) / 128, 128, 0, st>>>(partial, kDotBlocks, nc, out);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_cgnr_scalars(int mode, int nc, double eps, int *active, const double *dot_r,
+                               double *dot_z, const double *dot_v, const double *dz_new,
+                               double *alpha, double *beta, cudaStream_t st)
+{
+    cgnr_scalars_kernel<<<(nc + 127) / 128, 128, 0, st>>>(mode, nc, eps, active, dot_r, dot_z, dot_v,
+                                                         dz_new, alpha, beta);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_axpy_cols(float2 *x, const double *alpha, double alpha_sign, const float *mask,
+                            const float2 *p, int64_t rows, int nc, cudaStream_t st)
+{
+    axpy_cols_kernel<<<grid_for(rows * nc), kThreads, 0, st>>>(x, alpha, alpha_sign, mask, p, rows, nc);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_xpby_cols(float2 *p, const float2 *z, const double *beta, const int *active,
+                            int64_t rows, int nc, cudaStream_t st)
+{
+    xpby_cols_kernel<<<grid_for(rows * nc), kThreads, 0, st>>>(p, z, beta, active, rows, nc);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_zero(void *p, size_t bytes, cudaStream_t st)
+{
+    if (bytes) CGS_CUDA(cudaMemsetAsync(p, 0, bytes, st));
+    return CGS_OK;
+}
+
+cgs_status launch_add_scaled(float2 *q, const float2 *p, const CGScalars *sc, int64_t n,
+                             cudaStream_t st)
+{
+    add_scaled_kernel<<<grid_for(n), kThreads, 0, st>>>(q, p, sc, n);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_cg_update_xr(float2 *x, float2 *r, const float2 *p, const float2 *q,
+                               CGScalars *sc, int64_t n, cudaStream_t st)
+{
+    cg_update_xr_kernel<<<grid_for(n), kThreads, 0, st>>>(x, r, p, q, sc, n);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_cg_update_p(float2 *p, const float2 *r, const CGScalars *sc, int64_t n,
+                              cudaStream_t st)
+{
+    cg_update_p_kernel<<<grid_for(n), kThreads, 0, st>>>(p, r, sc, n);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_scalar_op(CGScalars *sc, const double *src, int op, cudaStream_t st)
+{
+    scalar_op_kernel<<<1, 1, 0, st>>>(sc, src, op);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_intensity(const float2 *sens_cm, int64_t P, int nc, float *I, cudaStream_t st)
+{
+    intensity_kernel<<<grid_for(P), kThreads, 0, st>>>(sens_cm, P, nc, I);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_coil_combine(const float2 *F, const float2 *S, const float *I, int64_t P, int nc,
+                               float2 *x, cudaStream_t st)
+{
+    coil_combine_kernel<<<grid_for(P), kThreads, 0, st>>>(F, S, I, P, nc, x);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_scale_real(float2 *x, const float *s, int64_t n, cudaStream_t st)
+{
+    scale_real_kernel<<<grid_for(n), kThreads, 0, st>>>(x, s, n);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+}  // namespace cgs

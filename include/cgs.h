@@ -1,0 +1,166 @@
+/*
+ * cgs.h -- C ABI of the GB300 non-Cartesian CG-SENSE library (libcgs.so).
+ *
+ * Plain C: opaque plan handle, plain pointers and sizes, status codes, no
+ * exceptions and no CUDA or torch types in any signature (a stream is passed
+ * as `void*` holding a cudaStream_t; NULL selects the plan's own stream).
+ *
+ * Every data pointer may be host memory (pageable or pinned) or device memory
+ * of the plan's GPU; the library detects which and stages host data itself.
+ * Layouts are the reference's (codeare `Matrix` is column-major, first index
+ * fastest, src/matrix/Matrix.hpp:165-200):
+ *   image      complex float, N^d, codeare x index fastest (== NFFT3 f_hat
+ *              order with NFFT dimension 0 slowest, src/matrix/ft/NFFT.hpp:340-346)
+ *   coil image complex float, (N^d, NC): coil c is the c-th contiguous image
+ *   kspace     float, (d, M): node j at k[d*j .. d*j+d-1], row 0 pairs with the
+ *              slowest image axis (NFFT.hpp:267-268), each value in [-0.5, 0.5)
+ *   weights    float, (M)
+ *   signals    complex float, (M, NC): coil c is the c-th contiguous block
+ * Complex values are interleaved (re, im) float pairs.
+ *
+ * Threading: one plan serves one caller thread at a time (as the reference's
+ * NFFT/NCSENSE objects, whose scratch buffers are mutable members,
+ * src/matrix/ft/NCSENSE.hpp:485); different plans are independent.
+ */
+#ifndef CGS_H
+#define CGS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    CGS_OK = 0,
+    CGS_ERR_BAD_ARG = 1,   /* invalid size, pointer or parameter            */
+    CGS_ERR_OOM = 2,       /* device allocation failed                      */
+    CGS_ERR_CUDA = 3,      /* a CUDA call failed (cgs_last_error() says which) */
+    CGS_ERR_TIMEOUT = 4,   /* a bounded device wait gave up                  */
+    CGS_ERR_NAN = 5,       /* the solver met a NaN residual                  */
+    CGS_ERR_STATE = 6      /* call out of order (e.g. no k-space set yet)    */
+} cgs_status;
+
+typedef struct cgs_plan cgs_plan;
+
+/* Geometry of one NFFT / NCSENSE operator.
+ * Replaces the Params consumed by NFFT::NFFT (src/matrix/ft/NFFT.hpp:66-191:
+ * keys nk, imsz, m, alpha; n_i = ceil(alpha * N_i)) and NCSENSE::NCSENSE
+ * (src/matrix/ft/NCSENSE.hpp:69-184: sensitivities give NC). */
+typedef struct {
+    int rank;        /* 2 or 3                                             */
+    int N[3];        /* image side per NFFT dimension (dimension 0 slowest); even */
+    double alpha;    /* oversampling factor sigma (reference default 1.0)  */
+    int m;           /* Kaiser-Bessel cut-off (reference default 1)        */
+    int64_t M;       /* k-space nodes per coil ("nk")                      */
+    int ncoils;      /* NC; 1 for a plain NFFT                             */
+} cgs_plan_desc;
+
+/* Create / destroy.  Allocates all device scratch up front. */
+cgs_status cgs_plan_create(cgs_plan **plan, const cgs_plan_desc *desc);
+cgs_status cgs_plan_destroy(cgs_plan *plan);
+
+/* K-space trajectory, (d, M) floats.  Replaces NFFT::KSpace
+ * (src/matrix/ft/NFFT.hpp:258-273) and NCSENSE::KSpace (NCSENSE.hpp:204-236).
+ * Sorts the nodes into grid tiles (done once per trajectory). */
+cgs_status cgs_set_kspace(cgs_plan *plan, const float *k);
+
+/* Density weights (M).  Replaces NFFT::Weights (NFFT.hpp:281-296) together
+ * with the damping mask it builds (NFFTTraits.hpp:225-260). */
+cgs_status cgs_set_weights(cgs_plan *plan, const float *w);
+
+/* Coil sensitivities, (N^d, NC) complex; also builds the intensity map
+ * I = 1/(sqrt(sum|S|^2)+1e-9).  Replaces NCSENSE::Sensitivities
+ * (NCSENSE.hpp:192-196) and IntensityMap (src/matrix/mri/MRI.hpp:7-29). */
+cgs_status cgs_set_sensitivities(cgs_plan *plan, const float *sens);
+
+/* Per-coil NFFT trafo: f_c = A fhat_c for every coil (NC images in, (M,NC) out).
+ * Replaces NFFT::Trafo (NFFT.hpp:305-361) / NFFT3 nfft_trafo. */
+cgs_status cgs_nfft_trafo(cgs_plan *plan, const float *fhat, float *f, void *stream);
+
+/* Per-coil true adjoint NFFT: fhat_c = A^H f_c (no iteration).
+ * The operation NFFT3's nfft_adjoint computes (called inside NFFTTraits.hpp:201-204). */
+cgs_status cgs_nfft_adjoint(cgs_plan *plan, const float *f, float *fhat, void *stream);
+
+/* Per-coil inverse NFFT by CGNR with the density weights and damping mask:
+ * what codeare's NFFT::Adjoint returns (NFFT.hpp:370-436 ->
+ * NFFTTraits::ITrafo, NFFTTraits.hpp:122-138): zero start, at most `maxit`
+ * steps, a coil stops once its W-weighted squared residual is below `eps`. */
+cgs_status cgs_nfft_itrafo(cgs_plan *plan, const float *f, float *fhat, int maxit,
+                           double eps, void *stream);
+
+/* SENSE encoding E: y_c = A (S_c . x).  Replaces NCSENSE::Trafo / operator*
+ * (NCSENSE.hpp:310-348, 421-423). */
+cgs_status cgs_sense_trafo(cgs_plan *plan, const float *x, float *y, void *stream);
+
+/* codeare's E^H: x = I . sum_c conj(S_c) . itrafo_c(y_c).  Replaces
+ * NCSENSE::operator/ (NCSENSE.hpp:251-301). */
+cgs_status cgs_sense_adjoint_codeare(cgs_plan *plan, const float *y, float *x, int ftiter,
+                                     double fteps, void *stream);
+
+/* True adjoint with weights: x = sum_c conj(S_c) . A^H (w . y_c)
+ * (w = 1 when `weighted` is 0).  No reference counterpart: the building block
+ * of the standard (Pruessmann) CG-SENSE normal equations. */
+cgs_status cgs_sense_adjoint(cgs_plan *plan, const float *y, float *x, int weighted,
+                             void *stream);
+
+/* Solver options and report. */
+typedef enum {
+    CGS_MODE_CODEARE = 0,   /* CGLS over codeare's E^H (bit-for-bit semantics of the reference) */
+    CGS_MODE_STANDARD = 1   /* CG on (E^H W E + lambda) x = E^H W y, true adjoint      */
+} cgs_mode;
+
+typedef struct {
+    int mode;          /* cgs_mode                                           */
+    int cgiter;        /* outer iterations (reference "cgmaxit", default 10) */
+    double cgeps;      /* codeare mode: break when rn/xn <= cgeps (squared ratio);
+                          standard mode: break when ||r||/||r0|| <= cgeps      */
+    double lambda;     /* Tikhonov weight (reference "lambda")               */
+    int ftiter;        /* inner CGNR steps (reference "ftmaxit", default 3)  */
+    double fteps;      /* inner CGNR threshold (reference "fteps", 1e-3)     */
+    int weighted;      /* standard mode: use the density weights W           */
+} cgs_solve_opts;
+
+typedef struct {
+    int iterations;        /* outer iterations performed                     */
+    double res_first;      /* first residual measure (rn/xn or ||r||/||r0||) */
+    double res_last;       /* residual measure at exit                       */
+    double seconds;        /* device time of the solve                       */
+    double res_hist[256];  /* residual measure per check, up to 256          */
+} cgs_solve_report;
+
+/* Full CG-SENSE solve (signals -> image).  CGS_MODE_CODEARE replaces
+ * NCSENSE::Adjoint -> CGLS::Solve (NCSENSE.hpp:408-414, 434-436;
+ * src/optimisation/CGLS.hpp:30-59) and the body of CGSENSE::Process
+ * (src/modules/CGSENSE.cpp:165-179).  `report` may be NULL. */
+cgs_status cgs_solve(cgs_plan *plan, const float *y, float *x, const cgs_solve_opts *opts,
+                     cgs_solve_report *report, void *stream);
+
+/* Sizes of the plan (for host wrappers). */
+cgs_status cgs_plan_info(const cgs_plan *plan, int *rank, int *N, int *n, int64_t *M,
+                         int *ncoils);
+
+/* Synchronise the plan's stream. */
+cgs_status cgs_sync(cgs_plan *plan);
+
+/* Number of this library's kernels launched since load (a launch counter). */
+int64_t cgs_kernel_launches(void);
+
+/* Per-kernel timing with CUDA events recorded on the launching stream around
+ * every FFT pass, interpolation and spreading launch (instrumentation; no
+ * reference counterpart -- the reference times whole modules with
+ * SimpleTimer, src/core/Queue.cpp:59-60).  cgs_profile_collect waits for the
+ * recorded events, writes the accumulated milliseconds and launch counts per
+ * category (0 = FFT axis passes, 1 = interpolation, 2 = spreading) into
+ * ms[3] / count[3] (either may be NULL) and resets them. */
+void cgs_profile_enable(int on);
+void cgs_profile_collect(double *ms, int64_t *count);
+
+/* Text of the last error on this thread ("" if none). */
+const char *cgs_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CGS_H */

@@ -1,0 +1,54 @@
+"""CPU-only checks of the C ABI library and the host-side helpers (no GPU calls)."""
+import os
+import re
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", fn)).read()
+            names += re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(cgs_[a-z_0-9]+)\s*\(", txt, re.M)
+    return sorted(set(names))
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    from codeare_gb300 import build, capi
+    build.build()
+    L = capi.load()
+    names = declared_functions()
+    assert len(names) >= 16
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    assert set(capi.EXPORTED) <= set(names)
+
+
+def test_synthetic_configs_shapes_and_ranges():
+    from codeare_gb300 import synth
+    c0 = synth.config0()
+    assert c0["k"].shape == (96 * 256, 2) and c0["k"].dtype == np.float32
+    assert c0["sens"].shape == (8, 128, 128)
+    assert np.all(c0["k"] >= -0.5) and np.all(c0["k"] < 0.5)
+    c1 = synth.config1()
+    assert c1["k"].shape == (403 * 512, 2)
+    assert c1["sens"].shape == (32, 256, 256)
+    k3 = synth.kooshball3d(100, 64)
+    assert k3.shape == (6400, 3) and np.all(k3 < 0.5) and np.all(k3 >= -0.5)
+    sp = synth.spiral2d(16, 4096)
+    assert sp.shape == (65536, 2)
+
+
+def test_phantom_values():
+    from codeare_gb300 import synth
+    p = synth.phantom(128)
+    vals = set(np.round(np.unique(p.real), 4).tolist())
+    # every pixel is a sum of tabulated intensities; background is 0, skull 1.0
+    assert 0.0 in vals and 1.0 in vals
+    assert abs(p[64, 64].real - 0.2) < 1e-6 or p[64, 64].real > 0
+    assert np.all(p.imag == 0)
+    p3 = synth.phantom3d(32)
+    assert p3.shape == (32, 32, 32) and p3.max().real <= 2.0 + 1e-6
