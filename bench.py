@@ -202,7 +202,10 @@ def run_ours(args):
     bytes_model = algorithmic_bytes(N, n, M, 2, NC)
     plan = cg.Plan((N, N), M, ncoils=NC, m=M_KB, alpha=SIGMA)
     plan.set_kspace(k)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: torch's default stream has handle 0, which the C ABI
+    # reads as "the plan's own stream"
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     fh_d = torch.from_numpy(fh).cuda()
     f_d = torch.empty((NC, M), dtype=torch.complex64, device="cuda")
     img_d = torch.empty((NC, N, N), dtype=torch.complex64, device="cuda")

@@ -68,7 +68,37 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, LIB)
+    build_host(force=True)
     return LIB
+
+
+HOST = os.path.join(HERE, "host")
+PLUGIN = os.path.join(LIBDIR, "CGSENSE.so")
+DRIVER = os.path.join(LIBDIR, "cgsense_run")
+
+
+def build_host(force: bool = False) -> str:
+    """The C++ drop-in layer: CGSENSE.so (ReconStrategy plugin over libcgs.so)
+    and cgsense_run (a dlopen host that drives a plugin's lifecycle)."""
+    srcs = [os.path.join(HOST, f) for f in ("CGSENSE.cpp", "cgsense_run.cpp")]
+    hdrs = [os.path.join(HOST, "codeare", f) for f in os.listdir(os.path.join(HOST, "codeare"))]
+    newest = max(os.path.getmtime(f) for f in srcs + hdrs + [LIB])
+    if not force and os.path.exists(PLUGIN) and os.path.exists(DRIVER) and \
+            min(os.path.getmtime(PLUGIN), os.path.getmtime(DRIVER)) >= newest:
+        return PLUGIN
+    common = ["g++", "-O2", "-std=c++17", "-Wall", "-I" + HOST, "-I" + os.path.join(ROOT, "include")]
+    cmds = [
+        common + ["-fPIC", "-shared", srcs[0], "-o", PLUGIN + ".tmp", "-L" + LIBDIR, "-lcgs",
+                  "-Wl,-rpath,$ORIGIN"],
+        common + [srcs[1], "-o", DRIVER + ".tmp", "-ldl", "-rdynamic"],
+    ]
+    for cmd in cmds:
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("host build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(PLUGIN + ".tmp", PLUGIN)
+    os.replace(DRIVER + ".tmp", DRIVER)
+    return PLUGIN
 
 
 if __name__ == "__main__":

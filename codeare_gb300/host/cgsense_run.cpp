@@ -1,0 +1,109 @@
+// cgsense_run.cpp -- a minimal host that loads a ReconStrategy plugin the way
+// codeare's ReconContext does (dlopen(name + ".so", RTLD_NOW), dlsym("create"),
+// src/core/Loader.hpp.in:46-118, src/core/ReconContext.cpp:44-51) and drives
+// Init / Prepare / Process / Finalise on workspace matrices read from a file.
+//
+//   cgsense_run <plugin.so> <config.xml> <in.cgsm> <out.cgsm> [output names...]
+//
+// The .cgsm container holds named matrices: "CGSM" u32 count, then per entry
+// u32 name length, name bytes, u32 type (0 float, 1 complex float), u32 ndims,
+// u64 dims[ndims] (codeare order, first index fastest), raw data.
+#include <dlfcn.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "codeare/ReconStrategy.hpp"
+
+static bool read_cgsm(const char *path, Workspace &ws)
+{
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return false;
+    char magic[4];
+    uint32_t n = 0;
+    f.read(magic, 4);
+    f.read((char *)&n, 4);
+    if (std::memcmp(magic, "CGSM", 4) != 0) return false;
+    for (uint32_t e = 0; e < n; ++e) {
+        uint32_t len = 0, type = 0, nd = 0;
+        f.read((char *)&len, 4);
+        std::string name(len, '\0');
+        f.read(&name[0], len);
+        f.read((char *)&type, 4);
+        f.read((char *)&nd, 4);
+        std::vector<size_t> dims(nd);
+        for (uint32_t i = 0; i < nd; ++i) { uint64_t d; f.read((char *)&d, 8); dims[i] = (size_t)d; }
+        if (type == 0) {
+            Matrix<float> &m = ws.AddMatrix<float>(name);
+            m = Matrix<float>(dims);
+            f.read((char *)m.Ptr(), m.Size() * sizeof(float));
+        } else {
+            Matrix<cxfl> &m = ws.AddMatrix<cxfl>(name);
+            m = Matrix<cxfl>(dims);
+            f.read((char *)m.Ptr(), m.Size() * sizeof(cxfl));
+        }
+        if (!f) return false;
+    }
+    return true;
+}
+
+static bool write_cgsm(const char *path, Workspace &ws, const std::vector<std::string> &names)
+{
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return false;
+    f.write("CGSM", 4);
+    uint32_t n = (uint32_t)names.size();
+    f.write((const char *)&n, 4);
+    for (const auto &name : names) {
+        const Matrix<cxfl> &m = ws.Get<cxfl>(name);
+        uint32_t len = (uint32_t)name.size(), type = 1, nd = (uint32_t)m.NDim();
+        f.write((const char *)&len, 4);
+        f.write(name.data(), len);
+        f.write((const char *)&type, 4);
+        f.write((const char *)&nd, 4);
+        for (uint32_t i = 0; i < nd; ++i) { uint64_t d = m.Dim(i); f.write((const char *)&d, 8); }
+        f.write((const char *)m.Ptr(), m.Size() * sizeof(cxfl));
+    }
+    return (bool)f;
+}
+
+int main(int argc, char **argv)
+{
+    if (argc < 5) {
+        std::fprintf(stderr, "usage: %s plugin.so config.xml in.cgsm out.cgsm [outputs...]\n", argv[0]);
+        return 2;
+    }
+    std::ifstream cf(argv[2]);
+    std::stringstream ss;
+    ss << cf.rdbuf();
+    const std::string xml = ss.str();
+    Workspace &ws = Workspace::Instance();
+    if (!read_cgsm(argv[3], ws)) { std::fprintf(stderr, "cannot read %s\n", argv[3]); return 3; }
+    void *h = dlopen(argv[1], RTLD_NOW);
+    if (!h) { std::fprintf(stderr, "dlopen: %s\n", dlerror()); return 4; }
+    create_t *create = (create_t *)dlsym(h, "create");
+    destroy_t *destroy = (destroy_t *)dlsym(h, "destroy");
+    if (!create || !destroy) { std::fprintf(stderr, "plugin lacks create/destroy\n"); return 5; }
+    RRStrategy::ReconStrategy *rs = create();
+    rs->Name("CGSENSE");
+    rs->WSpace(&ws);
+    rs->SetConfig(xml.c_str());
+    codeare::error_code e = rs->Init();
+    if (e == codeare::OK) e = rs->Prepare();
+    if (e == codeare::OK) e = rs->Process();
+    if (e == codeare::OK) e = rs->Finalise();
+    std::vector<std::string> outs;
+    for (int i = 5; i < argc; ++i) outs.push_back(argv[i]);
+    if (outs.empty()) outs.push_back("image");
+    if (e == codeare::OK && !write_cgsm(argv[4], ws, outs)) e = codeare::FILE_WRITE_FAILED;
+    destroy(rs);
+    ws.Clear();  // entries the plugin added carry deleters that live in the plugin
+    dlclose(h);
+    std::printf("cgsense_run: status %d\n", (int)e);
+    return e == codeare::OK ? 0 : 10 + (int)e;
+}

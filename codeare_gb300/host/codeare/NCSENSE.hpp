@@ -1,0 +1,220 @@
+// NCSENSE.hpp -- GB300 non-Cartesian SENSE operator with the interface of
+// codeare's NCSENSE<T> (reference: src/matrix/ft/NCSENSE.hpp:47-493).
+//
+// Params keys and defaults as the reference constructor (NCSENSE.hpp:69-184):
+// sensitivities (required, (N.., NC)), nk, ftiter = 3, fteps = 1e-3,
+// alpha = 1, m = 1, cgiter = 0, cgeps = 1e-6, lambda = 1e-6, verbose.  New
+// optional keys: "mode" ("codeare" = the reference's CGLS over its CGNR-based
+// E^H, the default; "standard" = CG on E^H W E + lambda with the true adjoint)
+// and "weighted" (standard mode: use the density weights, default 1).
+//
+//   Trafo / operator*   E: y_c = NFFT(S_c . x)            (NCSENSE.hpp:310-348)
+//   operator/           codeare's E^H (mode codeare) or E^H W (standard)
+//                                                          (NCSENSE.hpp:251-301)
+//   Adjoint / ->*       the full CG-SENSE solve            (NCSENSE.hpp:408-436)
+//
+// The whole solve runs on the GPU (libcgs.so cgs_solve); unlike the
+// reference's CGLS member, no residual history survives between solves.
+// Not supported (the constructor throws): nmany / dim4 / dim5 batches and a
+// Cartesian third dimension.
+#pragma once
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "NFFT.hpp"
+
+enum FT_EXCEPTION { NCSENSE_KSPACE_DIMENSIONS };
+
+template <class T> class NCSENSE : public FT<T> {
+    typedef typename TypeTraits<T>::RT RT;
+
+public:
+    NCSENSE() {}
+
+    explicit NCSENSE(const Params &params) : FT<T>(params)
+    {
+        if (!params.exists("sensitivities")) throw std::invalid_argument("NCSENSE: sensitivities required");
+        m_sm = params.Get<Matrix<T>>("sensitivities");
+        m_ftiter = params.exists("ftiter") ? unsigned_cast(params["ftiter"]) : 3;
+        m_fteps = params.exists("fteps") ? fp_cast(params["fteps"]) : 1.0e-3;
+        m_alpha = params.exists("alpha") ? fp_cast(params["alpha"]) : 1.0;
+        m_m = params.exists("m") ? unsigned_cast(params["m"]) : 1;
+        m_nk = params.exists("nk") ? unsigned_cast(params["nk"]) : 1;
+        try { m_cgiter = params.Get<size_t>("cgiter"); } catch (...) {}
+        try { m_cgeps = params.Get<RT>("cgeps"); } catch (...) {}
+        try { m_lambda = params.Get<RT>("lambda"); } catch (...) {}
+        try { m_verbose = params.Get<int>("verbose") > 0; } catch (...) {}
+        if (params.exists("mode")) {
+            const std::string md = params.Get<std::string>("mode");
+            if (md == "standard") m_mode = CGS_MODE_STANDARD;
+            else if (md == "codeare") m_mode = CGS_MODE_CODEARE;
+            else throw std::invalid_argument("NCSENSE: mode must be codeare or standard");
+        }
+        m_weighted = try_to_fetch<int>(params, "weighted", 1);
+        if (try_to_fetch<bool>(params, "3rd_dim_cart", false))
+            throw std::invalid_argument("NCSENSE: a Cartesian third dimension is not supported");
+        if (params.exists("dim4") || params.exists("dim5"))
+            throw std::invalid_argument("NCSENSE: multi-volume batches (dim4/dim5) are not supported");
+        plan();
+    }
+
+    NCSENSE(const NCSENSE &o) : FT<T>(o) { *this = o; }
+
+    NCSENSE &operator=(const NCSENSE &o)
+    {
+        if (this == &o) return *this;
+        release();
+        this->m_params = o.m_params;
+        m_sm = o.m_sm; m_k = o.m_k; m_w = o.m_w;
+        m_ftiter = o.m_ftiter; m_fteps = o.m_fteps; m_alpha = o.m_alpha; m_m = o.m_m; m_nk = o.m_nk;
+        m_cgiter = o.m_cgiter; m_cgeps = o.m_cgeps; m_lambda = o.m_lambda; m_verbose = o.m_verbose;
+        m_mode = o.m_mode; m_weighted = o.m_weighted; m_have_k = o.m_have_k; m_have_w = o.m_have_w;
+        if (o.m_plan) {
+            plan();
+            if (m_have_k) KSpace(m_k);
+            if (m_have_w) Weights(m_w);
+        }
+        return *this;
+    }
+
+    NCSENSE(NCSENSE &&o) noexcept : FT<T>(o) { steal(o); }
+    NCSENSE &operator=(NCSENSE &&o) noexcept
+    {
+        if (this != &o) { release(); this->m_params = o.m_params; steal(o); }
+        return *this;
+    }
+
+    virtual ~NCSENSE() { release(); }
+
+    virtual void Sensitivities(const Matrix<T> &sm)
+    {
+        if (sm.Size() != m_sm.Size()) throw std::invalid_argument("NCSENSE: sensitivity size changed");
+        m_sm = sm;
+        cgs_host::check(cgs_set_sensitivities(m_plan, reinterpret_cast<const float *>(m_sm.Ptr())),
+                        "cgs_set_sensitivities");
+    }
+
+    virtual void KSpace(const Matrix<RT> &k)
+    {
+        if (size(k, 1) != m_nk || size(k, 0) != m_rank) throw NCSENSE_KSPACE_DIMENSIONS;
+        m_k = k;
+        cgs_host::check(cgs_set_kspace(m_plan, k.Ptr()), "cgs_set_kspace");
+        m_have_k = true;
+        if (m_have_w) cgs_host::check(cgs_set_weights(m_plan, m_w.Ptr()), "cgs_set_weights");
+    }
+
+    virtual void Weights(const Matrix<RT> &w)
+    {
+        if (w.Size() != m_nk) throw std::invalid_argument("NCSENSE: weights must hold nk values");
+        m_w = w;
+        m_have_w = true;
+        if (m_have_k) cgs_host::check(cgs_set_weights(m_plan, w.Ptr()), "cgs_set_weights");
+    }
+
+    virtual Matrix<T> Trafo(const MatrixType<T> &m) const
+    {
+        Matrix<T> out(m_nk, m_nc);
+        cgs_host::check(cgs_sense_trafo(m_plan, reinterpret_cast<const float *>(m.Ptr()),
+                                        reinterpret_cast<float *>(out.Ptr()), nullptr), "cgs_sense_trafo");
+        return squeeze(out);
+    }
+    virtual Matrix<T> Trafo(const MatrixType<T> &m, const MatrixType<T> &, const bool & = true) const { return Trafo(m); }
+
+    virtual Matrix<T> operator/(const MatrixType<T> &m) const
+    {
+        Matrix<T> out(m_imsz);
+        if (m_mode == CGS_MODE_CODEARE)
+            cgs_host::check(cgs_sense_adjoint_codeare(m_plan, reinterpret_cast<const float *>(m.Ptr()),
+                                                      reinterpret_cast<float *>(out.Ptr()), (int)m_ftiter,
+                                                      (double)m_fteps, nullptr), "cgs_sense_adjoint_codeare");
+        else
+            cgs_host::check(cgs_sense_adjoint(m_plan, reinterpret_cast<const float *>(m.Ptr()),
+                                              reinterpret_cast<float *>(out.Ptr()), m_weighted, nullptr),
+                            "cgs_sense_adjoint");
+        return out;
+    }
+
+    virtual Matrix<T> Adjoint(const MatrixType<T> &m) const
+    {
+        Matrix<T> out(m_imsz);
+        cgs_solve_opts o{};
+        o.mode = m_mode; o.cgiter = (int)m_cgiter; o.cgeps = m_cgeps; o.lambda = m_lambda;
+        o.ftiter = (int)m_ftiter; o.fteps = m_fteps; o.weighted = m_weighted;
+        cgs_solve_report r{};
+        cgs_status s = cgs_solve(m_plan, reinterpret_cast<const float *>(m.Ptr()), reinterpret_cast<float *>(out.Ptr()),
+                                 &o, &r, nullptr);
+        if (s != CGS_OK && s != CGS_ERR_NAN) cgs_host::check(s, "cgs_solve");
+        m_last = r;
+        // the reference prints the residual at which it stopped (CGLS.hpp:42-46)
+        const int last = r.iterations < 256 ? r.iterations : 255;
+        if (m_verbose)
+            for (int i = 0; i <= last && i < 256; ++i) std::printf("    %03d %.7f\n", i, r.res_hist[i]);
+        return out;
+    }
+    virtual Matrix<T> Adjoint(const MatrixType<T> &m, const MatrixType<T> &, const bool = false) const { return Adjoint(m); }
+
+    virtual Matrix<T> operator*(const MatrixType<T> &m) const { return Trafo(m); }
+    virtual Matrix<T> operator->*(const MatrixType<T> &m) const { return Adjoint(m); }
+
+    size_t KSpaceSize() const { return m_nk; }
+    const cgs_solve_report &LastReport() const { return m_last; }
+
+    virtual std::ostream &Print(std::ostream &os) const
+    {
+        Operator<T>::Print(os);
+        os << "    NCCG: eps(" << m_cgeps << ") iter(" << m_cgiter << ") lambda(" << m_lambda << ")\n";
+        os << "    channels(" << m_nc << ") mode(" << (m_mode == CGS_MODE_CODEARE ? "codeare" : "standard") << ")\n";
+        return os;
+    }
+
+private:
+    void plan()
+    {
+        const size_t nd = ndims(m_sm);
+        if (nd < 3 || nd > 4) throw std::invalid_argument("NCSENSE: sensitivities must be (N,N[,N],NC)");
+        m_rank = nd - 1;
+        m_nc = size(m_sm, nd - 1);
+        m_imsz.assign(m_rank, 0);
+        for (size_t i = 0; i < m_rank; ++i) m_imsz[i] = size(m_sm, i);
+        cgs_plan_desc d{};
+        d.rank = (int)m_rank;
+        for (size_t t = 0; t < m_rank; ++t) d.N[t] = (int)m_imsz[m_rank - 1 - t];
+        d.alpha = m_alpha;
+        d.m = (int)m_m;
+        d.M = (int64_t)m_nk;
+        d.ncoils = (int)m_nc;
+        cgs_host::check(cgs_plan_create(&m_plan, &d), "cgs_plan_create");
+        cgs_host::check(cgs_set_sensitivities(m_plan, reinterpret_cast<const float *>(m_sm.Ptr())),
+                        "cgs_set_sensitivities");
+    }
+
+    void release()
+    {
+        if (m_plan) cgs_plan_destroy(m_plan);
+        m_plan = nullptr;
+    }
+
+    void steal(NCSENSE &o)
+    {
+        m_plan = o.m_plan; o.m_plan = nullptr;
+        m_sm = std::move(o.m_sm); m_k = std::move(o.m_k); m_w = std::move(o.m_w); m_imsz = o.m_imsz;
+        m_rank = o.m_rank; m_nc = o.m_nc; m_nk = o.m_nk; m_ftiter = o.m_ftiter; m_m = o.m_m;
+        m_cgiter = o.m_cgiter; m_fteps = o.m_fteps; m_alpha = o.m_alpha; m_cgeps = o.m_cgeps;
+        m_lambda = o.m_lambda; m_verbose = o.m_verbose; m_have_k = o.m_have_k; m_have_w = o.m_have_w;
+        m_mode = o.m_mode; m_weighted = o.m_weighted; m_last = o.m_last;
+    }
+
+    cgs_plan *m_plan = nullptr;
+    Matrix<T> m_sm;
+    Matrix<RT> m_k, m_w;
+    std::vector<size_t> m_imsz;
+    size_t m_rank = 2, m_nc = 1, m_nk = 1, m_ftiter = 3, m_m = 1, m_cgiter = 0;
+    double m_fteps = 1e-3, m_alpha = 1.0;
+    RT m_cgeps = 1.0e-6f, m_lambda = 1.0e-6f;
+    bool m_verbose = false, m_have_k = false, m_have_w = false;
+    int m_mode = CGS_MODE_CODEARE, m_weighted = 1;
+    mutable cgs_solve_report m_last{};
+};

@@ -27,6 +27,15 @@ def test_library_builds_and_exports_every_declared_symbol():
     assert set(capi.EXPORTED) <= set(names)
 
 
+def test_plugin_exports_reconstrategy_factories():
+    import ctypes
+    from codeare_gb300 import build
+    build.build()
+    P = ctypes.CDLL(build.PLUGIN)
+    assert hasattr(P, "create") and hasattr(P, "destroy")
+    assert os.access(build.DRIVER, os.X_OK)
+
+
 def test_synthetic_configs_shapes_and_ranges():
     from codeare_gb300 import synth
     c0 = synth.config0()

@@ -1,0 +1,75 @@
+"""The CGSENSE.so plugin driven through its ReconStrategy lifecycle by a dlopen
+host (cgsense_run), as codeare's ReconContext loads modules, compared with the
+FP64 oracle of the reference semantics (CGLS over the CGNR-based E^H)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_IMG = 1e-4
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))
+
+
+def run_plugin(tmp_path, mats, attrs):
+    from codeare_gb300 import build, cgsm
+    build.build()
+    inp, out, xml = tmp_path / "in.cgsm", tmp_path / "out.cgsm", tmp_path / "cfg.xml"
+    cgsm.write(str(inp), mats)
+    xml.write_text("<CGSENSE " + " ".join('%s="%s"' % kv for kv in attrs.items()) + "/>\n")
+    r = subprocess.run([build.DRIVER, build.PLUGIN, str(xml), str(inp), str(out), "image"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return cgsm.read(str(out))["image"], r.stdout
+
+
+@pytest.mark.parametrize("alpha,m", [(2.0, 4), (1.0, 1)])
+def test_plugin_matches_reference_semantics(gpu, oracle, tmp_path, alpha, m):
+    from codeare_gb300 import synth
+    cfg = synth.small_config(N=32, nc=4, nspokes=32, nsamp=64, alpha=alpha, m=m)
+    k, w, S = cfg["k"], cfg["w"], cfg["sens"]
+    s = oracle.Sense(S, k, w=w, m=m, alpha=alpha)
+    y = synth.add_noise(s.trafo(cfg["image"]), 1e-3, seed=4)
+    xo, _ = s.cgls_codeare(y, cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3)
+    mats = {"sensitivities": S, "kspace": k, "weights": w, "signals": y.astype(np.complex64)}
+    attrs = dict(nk=k.shape[0], lambda_=0.05, m=m, cgeps=1e-6, cgmaxit=10, ftmaxit=3, fteps=0.001,
+                 noise=0, testcase=0, threads=1, verbose=0)
+    attrs["lambda"] = attrs.pop("lambda_")
+    if alpha != 1.0:
+        attrs["alpha"] = alpha
+    img, log = run_plugin(tmp_path, mats, attrs)
+    assert img.shape == (32, 32)
+    assert rel(img, xo) < TOL_IMG, log
+
+
+def test_plugin_testcase_mode(gpu, oracle, tmp_path):
+    """testcase=1: the plugin encodes its own Shepp-Logan phantom (CGSENSE.cpp:171-172)."""
+    from codeare_gb300 import synth
+    cfg = synth.small_config(N=32, nc=4, nspokes=32, nsamp=64, alpha=2.0, m=4)
+    k, w, S = cfg["k"], cfg["w"], cfg["sens"]
+    s = oracle.Sense(S, k, w=w, m=4, alpha=2.0)
+    xo, _ = s.cgls_codeare(s.trafo(synth.phantom(32)), cgiter=6, cgeps=1e-7, lam=5e-2)
+    mats = {"sensitivities": S, "kspace": k, "weights": w}
+    attrs = {"nk": k.shape[0], "lambda": 0.05, "m": 4, "alpha": 2.0, "cgeps": 1e-7, "cgmaxit": 6,
+             "ftmaxit": 3, "fteps": 0.001, "noise": 0, "testcase": 1, "threads": 1, "verbose": 1}
+    img, log = run_plugin(tmp_path, mats, attrs)
+    assert rel(img, xo) < TOL_IMG, log
+
+
+def test_plugin_standard_mode(gpu, oracle, tmp_path):
+    from codeare_gb300 import synth
+    cfg = synth.small_config(N=32, nc=4, nspokes=32, nsamp=64, alpha=2.0, m=4)
+    k, w, S = cfg["k"], cfg["w"], cfg["sens"]
+    s = oracle.Sense(S, k, w=w, m=4, alpha=2.0)
+    y = s.trafo(cfg["image"])
+    xo, _ = s.cg(y, maxit=12, tol=1e-12, lam=0.0, weighted=True)
+    mats = {"sensitivities": S, "kspace": k, "weights": w, "signals": y.astype(np.complex64)}
+    attrs = {"nk": k.shape[0], "lambda": 0.0, "m": 4, "alpha": 2.0, "cgeps": 1e-12, "cgmaxit": 12,
+             "ftmaxit": 3, "fteps": 0.001, "noise": 0, "testcase": 0, "mode": "standard"}
+    img, log = run_plugin(tmp_path, mats, attrs)
+    assert rel(img, xo) < TOL_IMG, log
