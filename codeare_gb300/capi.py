@@ -25,7 +25,7 @@ EXPORTED = [
     "cgs_set_sensitivities", "cgs_nfft_trafo", "cgs_nfft_adjoint", "cgs_nfft_itrafo",
     "cgs_sense_trafo", "cgs_sense_adjoint_codeare", "cgs_sense_adjoint", "cgs_solve",
     "cgs_plan_info", "cgs_sync", "cgs_kernel_launches", "cgs_last_error",
-    "cgs_profile_enable", "cgs_profile_collect",
+    "cgs_profile_enable", "cgs_profile_collect", "cgs_nfft2d_trafo_noalloc",
 ]
 PROFILE_CATEGORIES = ("fft", "interp", "spread")
 
@@ -85,6 +85,7 @@ def load(path: str = LIB_PATH):
     L.cgs_profile_enable.restype = None
     L.cgs_profile_collect.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     L.cgs_profile_collect.restype = None
+    L.cgs_nfft2d_trafo_noalloc.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int64, vp, vp, vp, vp]
     for name in EXPORTED:
         if name not in ("cgs_kernel_launches", "cgs_last_error", "cgs_profile_enable",
                         "cgs_profile_collect"):

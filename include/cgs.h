@@ -147,6 +147,22 @@ cgs_status cgs_sync(cgs_plan *plan);
 /* Number of this library's kernels launched since load (a launch counter). */
 int64_t cgs_kernel_launches(void);
 
+/* Allocation-free 2-D NFFT forward for one coil: f = A fhat.
+ * No counterpart in the reference.  It exists for callers that must not
+ * allocate device memory while they run: a real-time reconstruction loop
+ * next to an acquisition stream (cudaMalloc / cudaFree synchronise the
+ * device and would stall it), or a host that owns a fixed device-memory
+ * budget through its own pool.  It uses no plan; its scratch is one static
+ * device array of 2^19 complex floats (4 MiB) that every GPU loading this
+ * library keeps until exit.  Limit: N*n + n*n + 2n + N <= 2^19 with
+ * n = ceil(alpha*N) (square N x N image; N = 256 at alpha = 2); larger
+ * sizes return CGS_ERR_BAD_ARG.  k (M x 2 floats), fhat (N x N complex) and
+ * f (M complex) must be device pointers.  All calls share the array, so
+ * calls that overlap on the GPU race; the first call on a device resolves
+ * the array's address and should come before any stream capture. */
+cgs_status cgs_nfft2d_trafo_noalloc(int N, double alpha, int m, int64_t M, const float *k,
+                                    const float *fhat, float *f, void *stream);
+
 /* Per-kernel timing with CUDA events recorded on the launching stream around
  * every FFT pass, interpolation and spreading launch (instrumentation; no
  * reference counterpart -- the reference times whole modules with
