@@ -150,29 +150,43 @@ axis_fft_kernel(const __grid_constant__ AxisPass p, int BO, int BI, int64_t nib)
     // ---- load: fill all n positions of every column (zeros where padded) ----
     const int tot = n * B;
     const bool pos_fast = (BI == 1);
-    for (int e = threadIdx.x; e < tot; e += kThreads) {
-        int pos, b;
-        if (pos_fast) { b = e / n; pos = e % n; }
-        else { pos = e / B; b = e % B; }
-        const int64_t o = ob0 + b / BI;
-        const int64_t i = ib0 + b % BI;
-        float2 v = make_float2(0.f, 0.f);
-        if (o < p.outer && i < p.inner) {
-            const int a = in_pos_to_axis(pos, p.Lin, n, p.in_centred);
-            if (a >= 0) {
-                const int64_t pix = o * p.Lin + a;
-                if (p.load_mode == LOAD_PLAIN) {
-                    v = p.src[pix * p.inner + i];
-                } else {
-                    v = p.img_per_coil ? p.img[pix * p.inner + i] : p.img[pix];
-                    if (p.sens) v = cmul(v, p.sens[pix * p.inner + i]);
-                    float s = deapod(p, o, a);
-                    if (p.mask) s *= p.mask[pix];
-                    v = cscale(v, s);
+    // batches of kUnroll independent global loads per thread keep enough bytes
+    // in flight to stream at HBM rate
+    constexpr int kUnroll = 8;
+    for (int e0 = threadIdx.x; e0 < tot; e0 += kThreads * kUnroll) {
+        float2 v[kUnroll];
+        int slot[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const int e = e0 + u * kThreads;
+            v[u] = make_float2(0.f, 0.f);
+            slot[u] = -1;
+            if (e >= tot) continue;
+            int pos, b;
+            if (pos_fast) { b = e / n; pos = e % n; }
+            else { pos = e / B; b = e % B; }
+            slot[u] = pos * P + b;
+            const int64_t o = ob0 + b / BI;
+            const int64_t i = ib0 + b % BI;
+            if (o < p.outer && i < p.inner) {
+                const int a = in_pos_to_axis(pos, p.Lin, n, p.in_centred);
+                if (a >= 0) {
+                    const int64_t pix = o * p.Lin + a;
+                    if (p.load_mode == LOAD_PLAIN) {
+                        v[u] = p.src[pix * p.inner + i];
+                    } else {
+                        float2 x = p.img_per_coil ? p.img[pix * p.inner + i] : p.img[pix];
+                        if (p.sens) x = cmul(x, p.sens[pix * p.inner + i]);
+                        float s = deapod(p, o, a);
+                        if (p.mask) s *= p.mask[pix];
+                        v[u] = cscale(x, s);
+                    }
                 }
             }
         }
-        bufA[pos * P + b] = v;
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+            if (slot[u] >= 0) bufA[slot[u]] = v[u];
     }
     __syncthreads();
 

@@ -13,6 +13,8 @@
 // node and tap.  Grid and k-space data keep the coil index innermost.
 #include "cgs_internal.cuh"
 
+#include <algorithm>
+
 namespace cgs {
 
 namespace {
@@ -227,6 +229,175 @@ spread_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSe
     }
 }
 
+// ---------------------------------------------------------------------------
+// Output-stationary 2-D spreading.  Lane l of a warp owns grid point
+// (py0 + l/8, px0 + l%8) of a 4 x 8 patch and accumulates CC coils in
+// registers while the warp walks the patch's node list; every node value is
+// one uniform (broadcast) load per coil, no atomics anywhere.  A crowded patch
+// is split into several work items whose partial sums land in `partial` and
+// are added in slot order by patch_reduce_kernel, so results are bitwise
+// reproducible.
+// ---------------------------------------------------------------------------
+__global__ void node_weights_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
+                                    int2 *__restrict__ nodeU, float *__restrict__ nodeW)
+{
+    const int taps = 2 * g.m + 2;
+    const float mf = (float)g.m;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < ns.M; s += (int64_t)gridDim.x * blockDim.x) {
+        float frac[3]; int c[3];
+        node_read<2>(ns.nodes, s, frac, c);
+        nodeU[s] = make_int2(wrapi(c[0] - g.m, g.n[0]), wrapi(c[1] - g.m, g.n[1]));
+        float *w = nodeW + s * 2 * taps;
+        for (int t = 0; t < 2; ++t)
+            for (int q = 0; q < taps; ++q) w[t * taps + q] = kb_phi(frac[t] + mf - (float)q, mf, g.b[t]);
+    }
+}
+
+template <int CC>
+__global__ void __launch_bounds__(256)
+spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
+                    const float2 *__restrict__ ks, const float *__restrict__ dens, int weighted,
+                    float2 *__restrict__ grid)
+{
+    const int lane = threadIdx.x & 31;
+    const int wi = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (wi >= ps.nwork) return;
+    const int c0 = blockIdx.y * CC;
+    const int ccn = min(CC, g.nc - c0);
+    const int4 wk = ps.work[wi];
+    const int n0 = g.n[0], n1 = g.n[1];
+    const int py = (wk.x / ps.npx) * kPatchH + (lane >> 3);
+    const int px = (wk.x % ps.npx) * kPatchW + (lane & 7);
+    const bool inside = (py < n0) && (px < n1);
+    const int taps = 2 * g.m + 2;
+    float ax[CC], ay[CC];
+#pragma unroll
+    for (int c = 0; c < CC; ++c) { ax[c] = 0.f; ay[c] = 0.f; }
+    const bool vec = ((g.nc & 1) == 0) && ((CC & 1) == 0) && (ccn == CC);
+    for (int e = wk.y; e < wk.y + wk.z; ++e) {
+        const int s = ps.entries[e];
+        const int2 u = ps.nodeU[s];
+        float w = 0.f;
+        if (inside) {
+            int dy = py - u.x; if (dy < 0) dy += n0;
+            int dx = px - u.y; if (dx < 0) dx += n1;
+            const float *W = ps.nodeW + (size_t)s * 2 * taps;
+            float wy = 0.f, wx = 0.f;
+            for (int q = dy; q < taps; q += n0) wy += W[q];
+            for (int q = dx; q < taps; q += n1) wx += W[taps + q];
+            w = wy * wx;
+            if (weighted) w *= dens[s];
+        }
+        const float2 *v = ks + (size_t)s * g.nc + c0;
+        if (vec) {
+            const float4 *v4 = reinterpret_cast<const float4 *>(v);
+#pragma unroll
+            for (int c = 0; c < CC / 2; ++c) {
+                const float4 q = v4[c];
+                ax[2 * c] = fmaf(w, q.x, ax[2 * c]); ay[2 * c] = fmaf(w, q.y, ay[2 * c]);
+                ax[2 * c + 1] = fmaf(w, q.z, ax[2 * c + 1]); ay[2 * c + 1] = fmaf(w, q.w, ay[2 * c + 1]);
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < CC; ++c)
+                if (c < ccn) { const float2 q = v[c]; ax[c] = fmaf(w, q.x, ax[c]); ay[c] = fmaf(w, q.y, ay[c]); }
+        }
+    }
+    if (!inside) return;
+    float2 *dst = (wk.w < 0) ? grid + ((size_t)py * n1 + px) * g.nc + c0
+                             : ps.partial + ((size_t)wk.w * 32 + lane) * g.nc + c0;
+#pragma unroll
+    for (int c = 0; c < CC; ++c)
+        if (c < ccn) dst[c] = make_float2(ax[c], ay[c]);
+}
+
+// ---------------------------------------------------------------------------
+// 2-D interpolation with the coil index on the lanes.  A CTA stages the padded
+// (T+2m+1)^2 tile of CC coils ([point][coil], coil innermost); a group of CC
+// lanes serves one node, so every tap is one conflict-free read of CC
+// consecutive complex values, and the node's 2 x TAPS weights (precomputed
+// once per trajectory) sit in registers.
+// ---------------------------------------------------------------------------
+template <int TAPS, int CC>
+__global__ void __launch_bounds__(256)
+interp2_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
+               const int2 *__restrict__ nodeU, const float *__restrict__ nodeW,
+               const float2 *__restrict__ grid, float2 *__restrict__ ks)
+{
+    extern __shared__ float4 smem4[];
+    float2 *tile = reinterpret_cast<float2 *>(smem4);
+    const int E = g.T + TAPS - 1;
+    const int4 wk = ns.work[blockIdx.x];
+    const int c0 = blockIdx.y * CC;
+    const int ccn = min(CC, g.nc - c0);
+    const int o0 = (wk.x / g.nt[1]) * g.T, o1 = (wk.x % g.nt[1]) * g.T;
+    constexpr int kUnroll = 8;  // independent loads in flight per thread
+    const int tot = E * E * CC;
+    for (int e0 = threadIdx.x; e0 < tot; e0 += 256 * kUnroll) {
+        float2 v[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const int e = e0 + u * 256;
+            const int c = e % CC, pt = e / CC;
+            const int ly = pt / E, lx = pt % E;
+            v[u] = make_float2(0.f, 0.f);
+            if (e < tot && c < ccn)
+                v[u] = grid[((size_t)wrapi(o0 + ly, g.n[0]) * g.n[1] + wrapi(o1 + lx, g.n[1])) * g.nc + c0 + c];
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+            if (e0 + u * 256 < tot) tile[e0 + u * 256] = v[u];
+    }
+    __syncthreads();
+    constexpr int NPW = 32 / CC;           // nodes served by one warp at a time
+    const int lane = threadIdx.x & 31, c = lane % CC, slot = lane / CC;
+    const int warp = threadIdx.x >> 5;
+    for (int i = warp * NPW + slot; i < wk.z; i += 8 * NPW) {
+        const int64_t s = (int64_t)wk.y + i;
+        const int2 u = nodeU[s];
+        const int y0 = u.x - o0, x0 = u.y - o1;
+        const float *W = nodeW + s * 2 * TAPS;
+        float w0[TAPS], w1[TAPS];
+#pragma unroll
+        for (int q = 0; q < TAPS; ++q) { w0[q] = W[q]; w1[q] = W[TAPS + q]; }
+        float ax = 0.f, ay = 0.f;
+#pragma unroll
+        for (int a = 0; a < TAPS; ++a) {
+            const float2 *row = tile + ((y0 + a) * E + x0) * CC + c;
+            float rx = 0.f, ry = 0.f;
+#pragma unroll
+            for (int b = 0; b < TAPS; ++b) {
+                const float2 v = row[b * CC];
+                rx = fmaf(w1[b], v.x, rx); ry = fmaf(w1[b], v.y, ry);
+            }
+            ax = fmaf(w0[a], rx, ax); ay = fmaf(w0[a], ry, ay);
+        }
+        if (c < ccn) ks[s * g.nc + c0 + c] = make_float2(ax, ay);
+    }
+}
+
+// sum the partial slots of split patches in slot order and store them
+__global__ void patch_reduce_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
+                                    float2 *__restrict__ grid)
+{
+    const int nc = g.nc;
+    const int64_t total = (int64_t)ps.nmulti * 32 * nc;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(e % nc);
+        const int lane = (int)((e / nc) % 32);
+        const int4 mu = ps.multi[e / ((int64_t)32 * nc)];
+        const int py = (mu.x / ps.npx) * kPatchH + (lane >> 3);
+        const int px = (mu.x % ps.npx) * kPatchW + (lane & 7);
+        if (py >= g.n[0] || px >= g.n[1]) continue;
+        float sx = 0.f, sy = 0.f;
+        for (int k = 0; k < mu.z; ++k) {
+            const float2 v = ps.partial[((size_t)(mu.y + k) * 32 + lane) * nc + c];
+            sx += v.x; sy += v.y;
+        }
+        grid[((size_t)py * g.n[1] + px) * nc + c] = make_float2(sx, sy);
+    }
+}
+
 GridCfg pick_cfg(const GridGeom &g)
 {
     GridCfg c;
@@ -252,11 +423,49 @@ size_t smem_bytes(const GridGeom &g, const GridCfg &c)
 
 }  // namespace
 
+template <int TAPS>
+cgs_status launch_interp2_taps(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks, int CC,
+                               cudaStream_t st)
+{
+    const int E = g.T + TAPS - 1;
+    const size_t smem = (size_t)E * E * CC * sizeof(float2);
+    dim3 grd(ns.nwork, (g.nc + CC - 1) / CC);
+#define CGS_I2(CCV)                                                                                         \
+    do {                                                                                                  \
+        CGS_CUDA(cudaFuncSetAttribute(interp2_kernel<TAPS, CCV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                      (int)smem));                                                         \
+        interp2_kernel<TAPS, CCV><<<grd, 256, smem, st>>>(g, ns, ns.nodeU, ns.nodeW, grid, ks);            \
+    } while (0)
+    if (CC == 16) CGS_I2(16);
+    else if (CC == 4) CGS_I2(4);
+    else CGS_I2(1);
+#undef CGS_I2
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
 cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,
                          cudaStream_t st)
 {
     if (ns.nwork == 0 || g.nc == 0) return CGS_OK;
     if (2 * g.m + 2 > kMaxTaps) { set_error("m too large"); return CGS_ERR_BAD_ARG; }
+    const int taps = 2 * g.m + 2;
+    if (g.d == 2 && ns.nodeU && ns.nodeW && taps <= 10) {
+        const int CC = g.nc >= 16 ? 16 : (g.nc >= 4 ? 4 : 1);
+        const int E = g.T + taps - 1;
+        if ((size_t)E * E * CC * sizeof(float2) <= 200 * 1024) {
+            cgs_status r;
+            prof_begin(PROF_INTERP, st);
+            switch (taps) {
+                case 4: r = launch_interp2_taps<4>(g, ns, grid, ks, CC, st); break;
+                case 6: r = launch_interp2_taps<6>(g, ns, grid, ks, CC, st); break;
+                case 8: r = launch_interp2_taps<8>(g, ns, grid, ks, CC, st); break;
+                default: r = launch_interp2_taps<10>(g, ns, grid, ks, CC, st); break;
+            }
+            prof_end(PROF_INTERP, st);
+            return r;
+        }
+    }
     GridCfg c = pick_cfg(g);
     size_t smem = smem_bytes(g, c);
     if (smem > 200 * 1024) { set_error("gridding tile does not fit in shared memory"); return CGS_ERR_BAD_ARG; }
@@ -271,6 +480,42 @@ cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *gri
     }
     prof_end(PROF_INTERP, st);
     CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_node_weights(const GridGeom &g, const NodeSet &ns, int2 *nodeU, float *nodeW,
+                               cudaStream_t st)
+{
+    if (g.d != 2) { set_error("node weight tables are 2-D only"); return CGS_ERR_BAD_ARG; }
+    if (ns.M == 0) return CGS_OK;
+    const int64_t blocks = std::min<int64_t>((ns.M + 255) / 256, 152 * 16);
+    node_weights_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, ns, nodeU, nodeW);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const float2 *ks, const float *dens,
+                               int weighted, float2 *grid, cudaStream_t st)
+{
+    if (ps.nwork == 0) return CGS_OK;
+    const int CC = g.nc >= 16 ? 16 : (g.nc >= 8 ? 8 : (g.nc >= 4 ? 4 : (g.nc >= 2 ? 2 : 1)));
+    dim3 grd((ps.nwork + 7) / 8, (g.nc + CC - 1) / CC);
+    prof_begin(PROF_SPREAD, st);
+    switch (CC) {
+        case 16: spread_patch_kernel<16><<<grd, 256, 0, st>>>(g, ps, ks, dens, weighted, grid); break;
+        case 8: spread_patch_kernel<8><<<grd, 256, 0, st>>>(g, ps, ks, dens, weighted, grid); break;
+        case 4: spread_patch_kernel<4><<<grd, 256, 0, st>>>(g, ps, ks, dens, weighted, grid); break;
+        case 2: spread_patch_kernel<2><<<grd, 256, 0, st>>>(g, ps, ks, dens, weighted, grid); break;
+        default: spread_patch_kernel<1><<<grd, 256, 0, st>>>(g, ps, ks, dens, weighted, grid); break;
+    }
+    CGS_LAUNCH_CHECK();
+    if (ps.nmulti > 0) {
+        const int64_t total = (int64_t)ps.nmulti * 32 * g.nc;
+        const int64_t blocks = std::min<int64_t>((total + 255) / 256, 152 * 16);
+        patch_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, ps, grid);
+        CGS_LAUNCH_CHECK();
+    }
+    prof_end(PROF_SPREAD, st);
     return CGS_OK;
 }
 

@@ -134,7 +134,31 @@ struct NodeSet {
     const float *w;     // density weights in sorted order (nullable)
     int nwork;          // work items
     const int4 *work;   // {tile index, first node, node count, 0}
+    const int2 *nodeU;  // 2-D: per node wrapped footprint start (nullable)
+    const float *nodeW; // 2-D: per node [2][2m+2] window weights (nullable)
 };
+
+// Output-stationary 2-D spreading: one warp per work item over a PH x PW patch
+// of grid points (lane = point), FP32 accumulators for a coil chunk in
+// registers, walking the list of nodes whose footprint covers the patch.
+constexpr int kPatchH = 4, kPatchW = 8;
+struct PatchSet {
+    int npx;               // patches per grid row
+    int nwork;             // work items
+    const int *entries;    // node (sorted index) lists, patch after patch
+    const int4 *work;      // {patch, first entry, count, partial slot or -1}
+    const int2 *nodeU;     // per node: wrapped footprint start (u0, u1)
+    const float *nodeW;    // per node: [2][2m+2] window weights
+    float2 *partial;       // [slot][32 points][nc] partial sums of split patches
+    int nmulti;            // patches split into several slots
+    const int4 *multi;     // {patch, first slot, slots, 0}
+};
+// node weights and footprint starts from the node records (once per trajectory)
+cgs_status launch_node_weights(const GridGeom &g, const NodeSet &ns, int2 *nodeU, float *nodeW,
+                               cudaStream_t st);
+// grid[...][c] = sum_s phi * (w_s if weighted) * ks[s][c]; writes every grid point
+cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const float2 *ks, const float *dens,
+                               int weighted, float2 *grid, cudaStream_t st);
 
 // y[s][c] (sorted, coil innermost) = sum over footprint of grid[...][c]
 cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,

@@ -128,6 +128,13 @@ struct cgs_plan {
     int4 *work = nullptr;
     int nwork = 0;
     GridGeom geom{};
+    // 2-D output-stationary spreading: per-patch node lists and weight tables
+    int2 *nodeU = nullptr;
+    float *nodeW = nullptr;
+    int *pentries = nullptr;
+    int4 *pwork = nullptr, *pmulti = nullptr;
+    float2 *ppartial = nullptr;
+    PatchSet pset{};
 
     // image-side maps
     float *mask = nullptr;   // damping mask What (N^d)
@@ -249,7 +256,7 @@ cgs_status op_forward(cgs_plan *p, const float2 *src_img, int per_coil, const fl
         b.src = p->t2; b.dst = p->grid;
         CGS_TRY(launch_axis_pass(b, st));
     }
-    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work};
+    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW};
     return launch_interp(p->geom, ns, p->grid, ks, st);
 }
 
@@ -257,9 +264,14 @@ cgs_status op_forward(cgs_plan *p, const float2 *src_img, int per_coil, const fl
 cgs_status op_adjoint(cgs_plan *p, const float2 *ks, int weighted, float2 *out, cudaStream_t st)
 {
     const int d = p->d, nc = p->nc;
-    CGS_TRY(launch_zero(p->grid, sizeof(float2) * (size_t)p->ntot * nc, st));
-    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work};
-    CGS_TRY(launch_spread(p->geom, ns, ks, weighted && p->w != nullptr, p->grid, st));
+    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW};
+    if (d == 2) {
+        // writes every grid point: no clearing pass
+        CGS_TRY(launch_spread_patch(p->geom, p->pset, ks, p->w, weighted && p->w != nullptr, p->grid, st));
+    } else {
+        CGS_TRY(launch_zero(p->grid, sizeof(float2) * (size_t)p->ntot * nc, st));
+        CGS_TRY(launch_spread(p->geom, ns, ks, weighted && p->w != nullptr, p->grid, st));
+    }
     const float2 *cur = p->grid;
     if (d == 3) {
         AxisPass a = base_pass(p, 0);
@@ -334,6 +346,100 @@ cgs_status op_eh(cgs_plan *p, const float2 *ks, int weighted, float2 *x, cudaStr
 {
     CGS_TRY(op_adjoint(p, ks, weighted, p->cF, st));
     return launch_coil_combine(p->cF, p->sens, nullptr, p->Nt, p->nc, x, st);
+}
+
+// Per 4 x 8 patch of the 2-D grid, the sorted indices of the nodes whose
+// footprint (2m+2 taps per axis, wrapped) covers any point of the patch; work
+// items of at most `chunk` nodes, crowded patches spread over several partial
+// slots; node weights precomputed on the device.  `cc` holds each node's
+// integer grid cell floor(n x) in trajectory order.
+cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
+{
+    const int n0 = p->n[0], n1 = p->n[1], m = p->m, taps = 2 * m + 2;
+    const int npy = (n0 + kPatchH - 1) / kPatchH, npx = (n1 + kPatchW - 1) / kPatchW;
+    const int64_t P = (int64_t)npy * npx, M = p->M;
+    std::vector<int> perm(M);
+    CGS_CUDA(cudaMemcpy(perm.data(), p->perm, sizeof(int) * M, cudaMemcpyDeviceToHost));
+    auto axis_patches = [taps](int u, int n, int ph, int *out) {
+        int k = 0;
+        for (int i = 0; i < taps; ++i) {
+            const int q = ((u + i) % n) / ph;
+            bool seen = false;
+            for (int j = 0; j < k; ++j) seen = seen || (out[j] == q);
+            if (!seen) out[k++] = q;
+        }
+        return k;
+    };
+    std::vector<int64_t> cnt(P + 1, 0);
+    std::vector<int> ru(M), cu(M);
+    int rows[64], cols[64];
+    for (int64_t s = 0; s < M; ++s) {
+        const int j = perm[s];
+        int u0 = (cc[(size_t)j * 2] - m) % n0; if (u0 < 0) u0 += n0;
+        int u1 = (cc[(size_t)j * 2 + 1] - m) % n1; if (u1 < 0) u1 += n1;
+        ru[s] = u0; cu[s] = u1;
+        const int nr = axis_patches(u0, n0, kPatchH, rows), ncl = axis_patches(u1, n1, kPatchW, cols);
+        for (int a = 0; a < nr; ++a)
+            for (int b = 0; b < ncl; ++b) cnt[(int64_t)rows[a] * npx + cols[b] + 1]++;
+    }
+    for (int64_t q = 0; q < P; ++q) cnt[q + 1] += cnt[q];
+    const int64_t E = cnt[P];
+    if (E > 0x7fffffffLL) { set_error("patch lists too long"); return CGS_ERR_BAD_ARG; }
+    std::vector<int> entries(E > 0 ? E : 1);
+    std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+    for (int64_t s = 0; s < M; ++s) {
+        const int nr = axis_patches(ru[s], n0, kPatchH, rows), ncl = axis_patches(cu[s], n1, kPatchW, cols);
+        for (int a = 0; a < nr; ++a)
+            for (int b = 0; b < ncl; ++b) entries[fill[(int64_t)rows[a] * npx + cols[b]]++] = (int)s;
+    }
+    // work items: a chunk bound that keeps every warp's list short
+    const int64_t avg = std::max<int64_t>(1, E / std::max<int64_t>(P, 1));
+    const int chunk = (int)std::min<int64_t>(1024, std::max<int64_t>(128, 2 * avg));
+    std::vector<int4> work, multi;
+    int slots = 0;
+    for (int64_t q = 0; q < P; ++q) {
+        const int64_t a = cnt[q], c = cnt[q + 1] - cnt[q];
+        const int64_t nch = std::max<int64_t>(1, (c + chunk - 1) / chunk);
+        if (nch == 1) {
+            work.push_back(make_int4((int)q, (int)a, (int)c, -1));
+        } else {
+            multi.push_back(make_int4((int)q, slots, (int)nch, 0));
+            for (int64_t k = 0; k < nch; ++k) {
+                const int64_t b = a + k * chunk;
+                work.push_back(make_int4((int)q, (int)b, (int)std::min<int64_t>(chunk, a + c - b), slots++));
+            }
+        }
+    }
+    // longest lists first, so the long ones do not form the tail
+    std::stable_sort(work.begin(), work.end(), [](const int4 &x, const int4 &y) { return x.z > y.z; });
+    for (void *b : {(void *)p->nodeU, (void *)p->nodeW, (void *)p->pentries, (void *)p->pwork, (void *)p->pmulti,
+                    (void *)p->ppartial}) dev_free(b);
+    p->nodeU = nullptr; p->nodeW = nullptr; p->pentries = nullptr; p->pwork = nullptr; p->pmulti = nullptr;
+    p->ppartial = nullptr;
+    CGS_TRY(dev_alloc(&p->nodeU, M));
+    CGS_TRY(dev_alloc(&p->nodeW, (size_t)M * 2 * taps));
+    CGS_TRY(dev_alloc(&p->pentries, entries.size()));
+    CGS_TRY(dev_alloc(&p->pwork, work.size()));
+    CGS_TRY(dev_alloc(&p->pmulti, std::max<size_t>(1, multi.size())));
+    CGS_TRY(dev_alloc(&p->ppartial, (size_t)std::max(slots, 1) * 32 * p->nc));
+    CGS_CUDA(cudaMemcpy(p->pentries, entries.data(), sizeof(int) * entries.size(), cudaMemcpyHostToDevice));
+    CGS_CUDA(cudaMemcpy(p->pwork, work.data(), sizeof(int4) * work.size(), cudaMemcpyHostToDevice));
+    if (!multi.empty())
+        CGS_CUDA(cudaMemcpy(p->pmulti, multi.data(), sizeof(int4) * multi.size(), cudaMemcpyHostToDevice));
+    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW};
+    CGS_TRY(launch_node_weights(p->geom, ns, p->nodeU, p->nodeW, p->stream));
+    CGS_CUDA(cudaStreamSynchronize(p->stream));
+    PatchSet &ps = p->pset;
+    ps.npx = npx;
+    ps.nwork = (int)work.size();
+    ps.entries = p->pentries;
+    ps.work = p->pwork;
+    ps.nodeU = p->nodeU;
+    ps.nodeW = p->nodeW;
+    ps.partial = p->ppartial;
+    ps.nmulti = (int)multi.size();
+    ps.multi = p->pmulti;
+    return CGS_OK;
 }
 
 cgs_status check_ready(cgs_plan *p, bool need_w, bool need_s)
@@ -443,7 +549,7 @@ cgs_status cgs_plan_create(cgs_plan **out, const cgs_plan_desc *desc)
     // geometry of the gridding tiles
     GridGeom &g = p->geom;
     g.d = p->d; g.m = p->m; g.nc = p->nc;
-    g.T = (p->d == 2) ? 32 : 8;
+    g.T = (p->d == 2) ? 16 : 8;
     for (int t = 0; t < p->d; ++t) {
         if (g.T > p->n[t]) g.T = p->n[t];
     }
@@ -501,7 +607,7 @@ cgs_status cgs_plan_destroy(cgs_plan *p)
     cudaSetDevice(p->device);
     if (p->stream) cudaStreamSynchronize(p->stream);
     void *bufs[] = {p->tw[0], p->tw[1], p->tw[2], p->deap[0], p->deap[1], p->deap[2], p->nodes, p->perm,
-                    p->w, p->work, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
+                    p->w, p->work, p->nodeU, p->nodeW, p->pentries, p->pwork, p->pmulti, p->ppartial, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
                     p->cF, p->cP, p->cZ, p->vX, p->vR, p->vP, p->vQ, p->ioA, p->ioB, p->partial, p->dots,
                     p->active, p->sc};
     for (void *b : bufs) dev_free(b);
@@ -599,6 +705,7 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
     CGS_CUDA(cudaMemcpy(p->work, work.data(), sizeof(int4) * work.size(), cudaMemcpyHostToDevice));
     CGS_CUDA(cudaMemcpy(p->nodes, nodes.data(), sizeof(float4) * nodes.size(), cudaMemcpyHostToDevice));
     CGS_CUDA(cudaMemcpy(p->perm, perm.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+    if (d == 2) CGS_TRY(build_patches(p, cc));
     p->have_k = true;
     // weights (if already given) must follow the new order: reset to "unset"
     p->have_w = false;
