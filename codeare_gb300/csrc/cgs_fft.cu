@@ -1,7 +1,7 @@
 // cgs_fft.cu -- oversampled FFT passes of the NFFT, one axis per launch.
 //
 // Each CTA transforms B columns of data[outer][L][inner] along L entirely in
-// shared memory (mixed-radix Stockham, radices 2/4/8 in registers, 3/5/7
+// one shared buffer (mixed-radix Stockham, radices 2/4/8 in registers, 3/5/7
 // through the twiddle table).  Zero padding (image side ->
 // oversampled grid) and cropping (grid -> image side) are index maps in the
 // load / store phases, so padded zeros are never read from or written to HBM.
@@ -78,32 +78,58 @@ __device__ __forceinline__ void bfly(float2 *v, int sign, const float2 *tw, int 
     }
 }
 
-template <int R>
-__device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, float2 *__restrict__ dst,
-                                              const float2 *tw, int n, int Ns, int B, int P, int sign)
+// Elements of one CTA's column block: n * B <= kElems, so every thread holds at
+// most kElems / kThreads values of a pass in registers.
+constexpr int kElems = 2048;
+
+// One in-place Stockham pass: every thread first reads and transforms all of
+// its butterflies into registers, then (after a barrier) writes them back, so
+// a single shared buffer serves as source and destination.
+template <int R> struct Log2R { static constexpr int v = R == 8 ? 3 : (R == 4 ? 2 : (R == 2 ? 1 : 0)); };
+
+template <int R, bool POW2>
+__device__ __forceinline__ void stockham_pass(float2 *buf, const float2 *tw, int n, int Ns, int logNs, int B,
+                                              int logB, int P, int sign)
 {
+    constexpr int NB = (kElems / kThreads + R - 1) / R;
     const int nR = n / R;
-    const int step = n / (Ns * R);
+    const int step = POW2 ? (n >> (logNs + Log2R<R>::v)) : n / (Ns * R);
     const int total = B * nR;
-    for (int q = threadIdx.x; q < total; q += kThreads) {
-        const int b = q % B, j = q / B;
-        const int k = j % Ns;
-        float2 v[R];
+    float2 v[NB][R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = src[(j + r * nR) * P + b];
-        if (Ns > 1) {
+    for (int t = 0; t < NB; ++t) {
+        const int q = threadIdx.x + t * kThreads;
+        if (q < total) {
+            const int b = POW2 ? (q & (B - 1)) : q % B;
+            const int j = POW2 ? (q >> logB) : q / B;
+            const int k = POW2 ? (j & (Ns - 1)) : j % Ns;
 #pragma unroll
-            for (int r = 1; r < R; ++r) {
-                float2 w = tw[k * r * step];
-                if (sign > 0) w.y = -w.y;
-                v[r] = cmul(v[r], w);
+            for (int r = 0; r < R; ++r) v[t][r] = buf[(j + r * nR) * P + b];
+            if (Ns > 1) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    float2 w = tw[k * r * step];
+                    if (sign > 0) w.y = -w.y;
+                    v[t][r] = cmul(v[t][r], w);
+                }
             }
+            bfly<R>(v[t], sign, tw, nR);
         }
-        bfly<R>(v, sign, tw, nR);
-        const int base = (j / Ns) * Ns * R + k;
-#pragma unroll
-        for (int r = 0; r < R; ++r) dst[(base + r * Ns) * P + b] = v[r];
     }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < NB; ++t) {
+        const int q = threadIdx.x + t * kThreads;
+        if (q < total) {
+            const int b = POW2 ? (q & (B - 1)) : q % B;
+            const int j = POW2 ? (q >> logB) : q / B;
+            const int k = POW2 ? (j & (Ns - 1)) : j % Ns;
+            const int base = (POW2 ? ((j >> logNs) << (logNs + Log2R<R>::v)) : (j / Ns) * Ns * R) + k;
+#pragma unroll
+            for (int r = 0; r < R; ++r) buf[(base + r * Ns) * P + b] = v[t][r];
+        }
+    }
+    __syncthreads();
 }
 
 __device__ __forceinline__ int in_pos_to_axis(int pos, int Lin, int n, int centred)
@@ -130,22 +156,40 @@ __device__ __forceinline__ float deapod(const AxisPass &p, int64_t o, int a)
     return d;
 }
 
-__global__ void __launch_bounds__(kThreads)
+// MIXED = false: radices 8/4/2 only, every size a power of two, index math by
+// shifts; MIXED = true: also radices 3/5/7 with general division
+template <bool MIXED>
+__global__ void __launch_bounds__(kThreads, MIXED ? 1 : 3)
 axis_fft_kernel(const __grid_constant__ AxisPass p, int BO, int BI, int64_t nib)
 {
     extern __shared__ float2 smem[];
+    constexpr bool POW2 = !MIXED;
     const int n = p.n;
     const int B = BO * BI;
     const int P = B + 1;
+    const int logB = 31 - __clz(B), logBI = 31 - __clz(BI), logn = 31 - __clz(n);
     float2 *tw = smem;
     float2 *bufA = smem + n;
-    float2 *bufB = bufA + (size_t)n * P;
+    float *dcol = reinterpret_cast<float *>(bufA + (size_t)n * P);  // [B] outer deapodisation per column
 
     const int64_t blk = blockIdx.x;
     const int64_t ib0 = (blk % nib) * BI;
     const int64_t ob0 = (blk / nib) * BO;
 
     for (int t = threadIdx.x; t < n; t += kThreads) tw[t] = p.tw[t];
+    const bool fused = (p.load_mode == LOAD_IMAGE) || (p.store_mode == STORE_DEAPOD);
+    if (fused) {
+        for (int b = threadIdx.x; b < B; b += kThreads) {
+            const int64_t o = ob0 + (POW2 ? (b >> logBI) : b / BI);
+            float d = 1.f;
+            if (o < p.outer) {
+                if (p.deap_o1) d *= p.deap_o1[o % p.o1_len];
+                if (p.deap_o0) d *= p.deap_o0[o / p.o1_len];
+            }
+            dcol[b] = d;
+        }
+        __syncthreads();
+    }
 
     // ---- load: fill all n positions of every column (zeros where padded) ----
     const int tot = n * B;
@@ -163,11 +207,11 @@ axis_fft_kernel(const __grid_constant__ AxisPass p, int BO, int BI, int64_t nib)
             slot[u] = -1;
             if (e >= tot) continue;
             int pos, b;
-            if (pos_fast) { b = e / n; pos = e % n; }
-            else { pos = e / B; b = e % B; }
+            if (pos_fast) { b = POW2 ? (e >> logn) : e / n; pos = POW2 ? (e & (n - 1)) : e % n; }
+            else { pos = POW2 ? (e >> logB) : e / B; b = POW2 ? (e & (B - 1)) : e % B; }
             slot[u] = pos * P + b;
-            const int64_t o = ob0 + b / BI;
-            const int64_t i = ib0 + b % BI;
+            const int64_t o = ob0 + (POW2 ? (b >> logBI) : b / BI);
+            const int64_t i = ib0 + (POW2 ? (b & (BI - 1)) : b % BI);
             if (o < p.outer && i < p.inner) {
                 const int a = in_pos_to_axis(pos, p.Lin, n, p.in_centred);
                 if (a >= 0) {
@@ -177,9 +221,9 @@ axis_fft_kernel(const __grid_constant__ AxisPass p, int BO, int BI, int64_t nib)
                     } else {
                         float2 x = p.img_per_coil ? p.img[pix * p.inner + i] : p.img[pix];
                         if (p.sens) x = cmul(x, p.sens[pix * p.inner + i]);
-                        float s = deapod(p, o, a);
-                        if (p.mask) s *= p.mask[pix];
-                        v[u] = cscale(x, s);
+                        float sc = dcol[b] * (p.deap_ax ? p.deap_ax[a] : 1.f);
+                        if (p.mask) sc *= p.mask[pix];
+                        v[u] = cscale(x, sc);
                     }
                 }
             }
@@ -190,38 +234,36 @@ axis_fft_kernel(const __grid_constant__ AxisPass p, int BO, int BI, int64_t nib)
     }
     __syncthreads();
 
-    // ---- Stockham passes, ping-pong in shared memory ----
-    float2 *src = bufA, *dst = bufB;
-    int Ns = 1;
+    // ---- Stockham passes, in place in shared memory ----
+    int Ns = 1, logNs = 0;
     for (int s = 0; s < p.nfac; ++s) {
         const int R = p.fac[s];
         switch (R) {
-            case 8: stockham_pass<8>(src, dst, tw, n, Ns, B, P, p.sign); break;
-            case 4: stockham_pass<4>(src, dst, tw, n, Ns, B, P, p.sign); break;
-            case 2: stockham_pass<2>(src, dst, tw, n, Ns, B, P, p.sign); break;
-            case 3: stockham_pass<3>(src, dst, tw, n, Ns, B, P, p.sign); break;
-            case 5: stockham_pass<5>(src, dst, tw, n, Ns, B, P, p.sign); break;
-            case 7: stockham_pass<7>(src, dst, tw, n, Ns, B, P, p.sign); break;
+            case 8: stockham_pass<8, POW2>(bufA, tw, n, Ns, logNs, B, logB, P, p.sign); logNs += 3; break;
+            case 4: stockham_pass<4, POW2>(bufA, tw, n, Ns, logNs, B, logB, P, p.sign); logNs += 2; break;
+            case 2: stockham_pass<2, POW2>(bufA, tw, n, Ns, logNs, B, logB, P, p.sign); logNs += 1; break;
+            case 3: if (MIXED) stockham_pass<3, false>(bufA, tw, n, Ns, logNs, B, logB, P, p.sign); break;
+            case 5: if (MIXED) stockham_pass<5, false>(bufA, tw, n, Ns, logNs, B, logB, P, p.sign); break;
+            case 7: if (MIXED) stockham_pass<7, false>(bufA, tw, n, Ns, logNs, B, logB, P, p.sign); break;
             default: break;  // host rejects other primes
         }
-        __syncthreads();
-        float2 *t = src; src = dst; dst = t;
         Ns *= R;
     }
+    const float2 *src = bufA;
 
     // ---- store: Lout positions of every column ----
     const int totO = p.Lout * B;
     for (int e = threadIdx.x; e < totO; e += kThreads) {
         int a, b;
         if (pos_fast) { b = e / p.Lout; a = e % p.Lout; }
-        else { a = e / B; b = e % B; }
-        const int64_t o = ob0 + b / BI;
-        const int64_t i = ib0 + b % BI;
+        else { a = POW2 ? (e >> logB) : e / B; b = POW2 ? (e & (B - 1)) : e % B; }
+        const int64_t o = ob0 + (POW2 ? (b >> logBI) : b / BI);
+        const int64_t i = ib0 + (POW2 ? (b & (BI - 1)) : b % BI);
         if (o >= p.outer || i >= p.inner) continue;
         const int pos = out_axis_to_pos(a, p.Lout, n, p.out_centred);
         float2 v = src[pos * P + b];
         const int64_t pix = o * p.Lout + a;
-        if (p.store_mode == STORE_DEAPOD) v = cscale(v, deapod(p, o, a));
+        if (p.store_mode == STORE_DEAPOD) v = cscale(v, dcol[b] * (p.deap_ax ? p.deap_ax[a] : 1.f));
         p.dst[pix * p.inner + i] = v;
     }
 }
@@ -232,31 +274,34 @@ cgs_status launch_axis_pass(const AxisPass &p, cudaStream_t st)
 {
     if (p.outer <= 0 || p.inner <= 0) return CGS_OK;
     const int n = p.n;
-    // shared memory budget ~100 KB: twiddles + two n x (B+1) buffers
-    const int budget = 100 * 1024 / 8;
-    int B = (budget - n) / (2 * n) - 1;
-    int Bp = 1;
-    while (Bp * 2 <= B && Bp * 2 <= 32) Bp *= 2;
-    B = Bp;
+    // columns per CTA: n * B <= kElems values (one shared buffer + twiddles)
+    int B = 0;
+    for (int c = 1; c <= 32 && (int64_t)n * c <= kElems; c *= 2) B = c;
     if (B < 1) {
         set_error("FFT length too large for the shared-memory axis pass");
         return CGS_ERR_BAD_ARG;
     }
-    const int BI = (int)(p.inner < B ? p.inner : B);
+    int BI = 1;  // largest power of two <= min(inner, B)
+    while (BI * 2 <= B && BI * 2 <= p.inner) BI *= 2;
     const int BO = B / BI;
     const int64_t nib = (p.inner + BI - 1) / BI;
     const int64_t nob = (p.outer + BO - 1) / BO;
-    const size_t smem = ((size_t)n + 2 * (size_t)n * (BO * BI + 1)) * sizeof(float2);
+    const size_t smem = ((size_t)n + (size_t)n * (BO * BI + 1)) * sizeof(float2) + (size_t)B * sizeof(float);
+    bool mixed = false;
+    for (int i = 0; i < p.nfac; ++i) mixed = mixed || (p.fac[i] != 2 && p.fac[i] != 4 && p.fac[i] != 8);
     static bool attr_set = false;
     if (!attr_set) {
-        CGS_CUDA(cudaFuncSetAttribute(axis_fft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CGS_CUDA(cudaFuncSetAttribute(axis_fft_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      110 * 1024));
+        CGS_CUDA(cudaFuncSetAttribute(axis_fft_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       110 * 1024));
         attr_set = true;
     }
     const int64_t nblocks = nib * nob;
     if (nblocks > 0x7fffffffLL) { set_error("axis pass grid too large"); return CGS_ERR_BAD_ARG; }
     prof_begin(PROF_FFT, st);
-    axis_fft_kernel<<<(unsigned)nblocks, kThreads, smem, st>>>(p, BO, BI, nib);
+    if (mixed) axis_fft_kernel<true><<<(unsigned)nblocks, kThreads, smem, st>>>(p, BO, BI, nib);
+    else axis_fft_kernel<false><<<(unsigned)nblocks, kThreads, smem, st>>>(p, BO, BI, nib);
     prof_end(PROF_FFT, st);
     CGS_LAUNCH_CHECK();
     return CGS_OK;

@@ -253,15 +253,38 @@ __global__ void node_weights_kernel(const __grid_constant__ GridGeom g, const __
     }
 }
 
+// Per-warp staging in shared memory of a batch of 32 list entries: lane l
+// fetches entry l's node weights, values and density weight with independent
+// loads, so one global round trip serves 32 entries; the accumulation loop
+// then reads only shared memory (broadcasts and conflict-free rows).  The
+// value rows are padded to a 16-byte multiple so two coils come per load.
+template <int CC> struct SpreadRow { static constexpr int v = CC + ((CC & 1) ? 1 : 2); };
+
+template <int CC>
+__host__ __device__ __forceinline__ size_t spread_patch_smem_per_warp(int taps)
+{
+    return (size_t)32 * ((2 * taps + 1) * sizeof(float) + SpreadRow<CC>::v * sizeof(float2) + sizeof(int2) +
+                         sizeof(float));
+}
+
 template <int CC>
 __global__ void __launch_bounds__(256)
 spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
                     const float2 *__restrict__ ks, const float *__restrict__ dens, int weighted,
                     float2 *__restrict__ grid)
 {
-    const int lane = threadIdx.x & 31;
-    const int wi = blockIdx.x * 8 + (threadIdx.x >> 5);
+    extern __shared__ float4 smem4[];
+    constexpr int RS = SpreadRow<CC>::v;                  // value row stride (float2)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wi = blockIdx.x * 8 + warp;
     if (wi >= ps.nwork) return;
+    const int taps = 2 * g.m + 2;
+    const int WS = 2 * taps + 1;                          // padded weight row (conflict-free fill)
+    char *base = reinterpret_cast<char *>(smem4) + warp * spread_patch_smem_per_warp<CC>(taps);
+    float2 *sv = reinterpret_cast<float2 *>(base);        // [32][RS]
+    float *sw = reinterpret_cast<float *>(sv + 32 * RS);  // [32][WS]
+    int2 *su = reinterpret_cast<int2 *>(sw + 32 * WS);    // [32]
+    float *sd = reinterpret_cast<float *>(su + 32);       // [32]
     const int c0 = blockIdx.y * CC;
     const int ccn = min(CC, g.nc - c0);
     const int4 wk = ps.work[wi];
@@ -269,39 +292,66 @@ spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ 
     const int py = (wk.x / ps.npx) * kPatchH + (lane >> 3);
     const int px = (wk.x % ps.npx) * kPatchW + (lane & 7);
     const bool inside = (py < n0) && (px < n1);
-    const int taps = 2 * g.m + 2;
+    const bool wide = (n0 >= taps) && (n1 >= taps);       // no footprint wraps onto itself
     float ax[CC], ay[CC];
 #pragma unroll
     for (int c = 0; c < CC; ++c) { ax[c] = 0.f; ay[c] = 0.f; }
-    const bool vec = ((g.nc & 1) == 0) && ((CC & 1) == 0) && (ccn == CC);
-    for (int e = wk.y; e < wk.y + wk.z; ++e) {
-        const int s = ps.entries[e];
-        const int2 u = ps.nodeU[s];
-        float w = 0.f;
-        if (inside) {
-            int dy = py - u.x; if (dy < 0) dy += n0;
-            int dx = px - u.y; if (dx < 0) dx += n1;
-            const float *W = ps.nodeW + (size_t)s * 2 * taps;
-            float wy = 0.f, wx = 0.f;
-            for (int q = dy; q < taps; q += n0) wy += W[q];
-            for (int q = dx; q < taps; q += n1) wx += W[taps + q];
-            w = wy * wx;
-            if (weighted) w *= dens[s];
-        }
-        const float2 *v = ks + (size_t)s * g.nc + c0;
-        if (vec) {
-            const float4 *v4 = reinterpret_cast<const float4 *>(v);
-#pragma unroll
-            for (int c = 0; c < CC / 2; ++c) {
-                const float4 q = v4[c];
-                ax[2 * c] = fmaf(w, q.x, ax[2 * c]); ay[2 * c] = fmaf(w, q.y, ay[2 * c]);
-                ax[2 * c + 1] = fmaf(w, q.z, ax[2 * c + 1]); ay[2 * c + 1] = fmaf(w, q.w, ay[2 * c + 1]);
+    const int end = wk.y + wk.z;
+    for (int e0 = wk.y; e0 < end; e0 += 32) {
+        const int cnt = min(32, end - e0);
+        // ---- stage: lane l fetches entry e0 + l ----
+        if (lane < cnt) {
+            const int s = ps.entries[e0 + lane];
+            su[lane] = ps.nodeU[s];
+            sd[lane] = weighted ? dens[s] : 1.f;
+            const float2 *W2 = reinterpret_cast<const float2 *>(ps.nodeW + (size_t)s * 2 * taps);
+            for (int q = 0; q < taps; ++q) {
+                const float2 w = W2[q];
+                sw[lane * WS + 2 * q] = w.x;
+                sw[lane * WS + 2 * q + 1] = w.y;
             }
-        } else {
+            const float2 *v = ks + (size_t)s * g.nc + c0;
 #pragma unroll
             for (int c = 0; c < CC; ++c)
-                if (c < ccn) { const float2 q = v[c]; ax[c] = fmaf(w, q.x, ax[c]); ay[c] = fmaf(w, q.y, ay[c]); }
+                sv[lane * RS + c] = (c < ccn) ? v[c] : make_float2(0.f, 0.f);
         }
+        __syncwarp();
+        // ---- accumulate ----
+        for (int i = 0; i < cnt; ++i) {
+            const int2 u = su[i];
+            float w = 0.f;
+            if (inside) {
+                int dy = py - u.x; if (dy < 0) dy += n0;
+                int dx = px - u.y; if (dx < 0) dx += n1;
+                const float *W = sw + i * WS;
+                float wy = 0.f, wx = 0.f;
+                if (wide) {
+                    wy = (dy < taps) ? W[dy] : 0.f;
+                    wx = (dx < taps) ? W[taps + dx] : 0.f;
+                } else {
+                    for (int q = dy; q < taps; q += n0) wy += W[q];
+                    for (int q = dx; q < taps; q += n1) wx += W[taps + q];
+                }
+                w = wy * wx * sd[i];
+            }
+            if constexpr ((CC & 1) == 0) {
+                const float4 *v = reinterpret_cast<const float4 *>(sv + i * RS);
+#pragma unroll
+                for (int c = 0; c < CC / 2; ++c) {
+                    const float4 q = v[c];
+                    ax[2 * c] = fmaf(w, q.x, ax[2 * c]); ay[2 * c] = fmaf(w, q.y, ay[2 * c]);
+                    ax[2 * c + 1] = fmaf(w, q.z, ax[2 * c + 1]); ay[2 * c + 1] = fmaf(w, q.w, ay[2 * c + 1]);
+                }
+            } else {
+                const float2 *v = sv + i * RS;
+#pragma unroll
+                for (int c = 0; c < CC; ++c) {
+                    const float2 q = v[c];
+                    ax[c] = fmaf(w, q.x, ax[c]); ay[c] = fmaf(w, q.y, ay[c]);
+                }
+            }
+        }
+        __syncwarp();
     }
     if (!inside) return;
     float2 *dst = (wk.w < 0) ? grid + ((size_t)py * n1 + px) * g.nc + c0
@@ -309,6 +359,28 @@ spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ 
 #pragma unroll
     for (int c = 0; c < CC; ++c)
         if (c < ccn) dst[c] = make_float2(ax[c], ay[c]);
+}
+
+// sum the partial slots of split patches in slot order and store them
+__global__ void patch_reduce_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
+                                    float2 *__restrict__ grid)
+{
+    const int nc = g.nc;
+    const int64_t total = (int64_t)ps.nmulti * 32 * nc;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(e % nc);
+        const int lane = (int)((e / nc) % 32);
+        const int4 mu = ps.multi[e / ((int64_t)32 * nc)];
+        const int py = (mu.x / ps.npx) * kPatchH + (lane >> 3);
+        const int px = (mu.x % ps.npx) * kPatchW + (lane & 7);
+        if (py >= g.n[0] || px >= g.n[1]) continue;
+        float sx = 0.f, sy = 0.f;
+        for (int k = 0; k < mu.z; ++k) {
+            const float2 v = ps.partial[((size_t)(mu.y + k) * 32 + lane) * nc + c];
+            sx += v.x; sy += v.y;
+        }
+        grid[((size_t)py * g.n[1] + px) * nc + c] = make_float2(sx, sy);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -376,28 +448,6 @@ interp2_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeS
     }
 }
 
-// sum the partial slots of split patches in slot order and store them
-__global__ void patch_reduce_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
-                                    float2 *__restrict__ grid)
-{
-    const int nc = g.nc;
-    const int64_t total = (int64_t)ps.nmulti * 32 * nc;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-        const int c = (int)(e % nc);
-        const int lane = (int)((e / nc) % 32);
-        const int4 mu = ps.multi[e / ((int64_t)32 * nc)];
-        const int py = (mu.x / ps.npx) * kPatchH + (lane >> 3);
-        const int px = (mu.x % ps.npx) * kPatchW + (lane & 7);
-        if (py >= g.n[0] || px >= g.n[1]) continue;
-        float sx = 0.f, sy = 0.f;
-        for (int k = 0; k < mu.z; ++k) {
-            const float2 v = ps.partial[((size_t)(mu.y + k) * 32 + lane) * nc + c];
-            sx += v.x; sy += v.y;
-        }
-        grid[((size_t)py * g.n[1] + px) * nc + c] = make_float2(sx, sy);
-    }
-}
-
 GridCfg pick_cfg(const GridGeom &g)
 {
     GridCfg c;
@@ -437,6 +487,7 @@ cgs_status launch_interp2_taps(const GridGeom &g, const NodeSet &ns, const float
         interp2_kernel<TAPS, CCV><<<grd, 256, smem, st>>>(g, ns, ns.nodeU, ns.nodeW, grid, ks);            \
     } while (0)
     if (CC == 16) CGS_I2(16);
+    else if (CC == 8) CGS_I2(8);
     else if (CC == 4) CGS_I2(4);
     else CGS_I2(1);
 #undef CGS_I2
@@ -451,7 +502,8 @@ cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *gri
     if (2 * g.m + 2 > kMaxTaps) { set_error("m too large"); return CGS_ERR_BAD_ARG; }
     const int taps = 2 * g.m + 2;
     if (g.d == 2 && ns.nodeU && ns.nodeW && taps <= 10) {
-        const int CC = g.nc >= 16 ? 16 : (g.nc >= 4 ? 4 : 1);
+        // 8 coils per CTA: 40 KB tiles leave room for 4 CTAs per SM
+        const int CC = g.nc >= 8 ? 8 : (g.nc >= 4 ? 4 : 1);
         const int E = g.T + taps - 1;
         if ((size_t)E * E * CC * sizeof(float2) <= 200 * 1024) {
             cgs_status r;
@@ -498,16 +550,27 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
                                int weighted, float2 *grid, cudaStream_t st)
 {
     if (ps.nwork == 0) return CGS_OK;
-    const int CC = g.nc >= 16 ? 16 : (g.nc >= 8 ? 8 : (g.nc >= 4 ? 4 : (g.nc >= 2 ? 2 : 1)));
+    const int CC = g.nc >= 32 ? 32 : (g.nc >= 16 ? 16 : (g.nc >= 8 ? 8 : (g.nc >= 4 ? 4 : (g.nc >= 2 ? 2 : 1))));
+    const int taps = 2 * g.m + 2;
+    if (taps > kMaxTaps) { set_error("m too large"); return CGS_ERR_BAD_ARG; }
     dim3 grd((ps.nwork + 7) / 8, (g.nc + CC - 1) / CC);
     prof_begin(PROF_SPREAD, st);
+#define CGS_SP(CCV)                                                                                        \
+    do {                                                                                                 \
+        const size_t sm = 8 * spread_patch_smem_per_warp<CCV>(taps);                                     \
+        CGS_CUDA(cudaFuncSetAttribute(spread_patch_kernel<CCV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                      (int)sm));                                                          \
+        spread_patch_kernel<CCV><<<grd, 256, sm, st>>>(g, ps, ks, dens, weighted, grid);                   \
+    } while (0)
     switch (CC) {
-        case 16: spread_patch_kernel<16><<<grd, 256, 0, st>>>(g, ps, ks, dens, weighted, grid); break;
-        case 8: spread_patch_kernel<8><<<grd, 256, 0, st>>>(g, ps, ks, dens, weighted, grid); break;
-        case 4: spread_patch_kernel<4><<<grd, 256, 0, st>>>(g, ps, ks, dens, weighted, grid); break;
-        case 2: spread_patch_kernel<2><<<grd, 256, 0, st>>>(g, ps, ks, dens, weighted, grid); break;
-        default: spread_patch_kernel<1><<<grd, 256, 0, st>>>(g, ps, ks, dens, weighted, grid); break;
+        case 32: CGS_SP(32); break;
+        case 16: CGS_SP(16); break;
+        case 8: CGS_SP(8); break;
+        case 4: CGS_SP(4); break;
+        case 2: CGS_SP(2); break;
+        default: CGS_SP(1); break;
     }
+#undef CGS_SP
     CGS_LAUNCH_CHECK();
     if (ps.nmulti > 0) {
         const int64_t total = (int64_t)ps.nmulti * 32 * g.nc;
