@@ -172,6 +172,63 @@ def run_reference(args):
     return 0
 
 
+def cgsense_section(cpu_too: bool):
+    """Config 0: 128^2 Shepp-Logan, 8 coils, 96 uniform spokes x 256, sigma=2, m=4.
+    Times (GPU, inputs already on the device through the C ABI):
+      - codeare mode (CGLS over the CGNR-based E^H), 10 iterations, lambda = 5e-2;
+      - standard mode (true adjoint) to ||r||/||r0|| = 1e-4, with E^H W E applied by the
+        NFFT pair and by the Toeplitz embedding.
+    The CPU leg runs the FP64 oracle's codeare-mode solve on the same input."""
+    import torch
+    import codeare_gb300 as cg
+    from codeare_gb300 import synth
+    c = synth.config0()
+    N, nc = c["shape"][0], c["sens"].shape[0]
+    k, w, S = c["k"], c["w"], c["sens"]
+    M = k.shape[0]
+    p = cg.Plan((N, N), M, ncoils=nc, m=c["m"], alpha=c["alpha"])
+    p.set_kspace(k)
+    p.set_weights(w)
+    p.set_sensitivities(S)
+    y = np.zeros((nc, M), np.complex64)
+    p.sense_trafo(np.ascontiguousarray(c["image"]), y)
+    y = synth.add_noise(y, c["noise"], seed=c["seed"])
+    yd = torch.from_numpy(y).cuda()
+    xd = torch.zeros((N, N), dtype=torch.complex64, device="cuda")
+    out = {"workload": "config 0: 128^2, 8 coils, 96x256 uniform radial, sigma=2, m=4, 1e-3 noise"}
+
+    def timed(**kw):
+        p.solve(yd, xd, **kw)  # warm-up (and Toeplitz kernel build)
+        best = None
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rep = p.solve(yd, xd, **kw)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+            if best is None or wall < best[0]:
+                best = (wall, rep)
+        wall, rep = best
+        return {"iterations": rep["iterations"], "wall_ms": wall * 1e3, "device_ms": rep["seconds"] * 1e3,
+                "res_last": rep["res_last"]}
+
+    out["codeare_10it"] = timed(mode=cg.MODE_CODEARE, cgiter=10, cgeps=1e-7, lam=5e-2, ftiter=3, fteps=1e-3)
+    out["standard_to_1e-4_nfft"] = timed(mode=cg.MODE_STANDARD, cgiter=200, cgeps=1e-4, lam=0.0, weighted=True)
+    out["standard_to_1e-4_toeplitz"] = timed(mode=cg.MODE_STANDARD, cgiter=200, cgeps=1e-4, lam=0.0,
+                                             weighted=True, toeplitz=True)
+    p.close()
+    if cpu_too:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        s = O.Sense(S, k, w=w, m=c["m"], alpha=c["alpha"], threads=threads)
+        t0 = time.perf_counter()
+        s.cgls_codeare(y, cgiter=10, cgeps=1e-7, lam=5e-2, ftiter=3, fteps=1e-3)
+        t = time.perf_counter() - t0
+        out["cpu_codeare_10it"] = {"wall_ms": t * 1e3, "cores": threads, "kind": "port",
+                                   "note": "FP64 oracle restatement, one coil per thread"}
+    return out
+
+
 def run_ours(args):
     import torch
     import codeare_gb300 as cg
@@ -316,6 +373,9 @@ def run_ours(args):
                          "the NFFT3 path (own FFT; FFTW absent)" % nc_s, "seconds": t_cpu}
 
     plan.close()
+    cgs_part = None
+    if rank == 0 and not args.no_cgsense:
+        cgs_part = cgsense_section(cpu_too=(ws == 1 and not args.no_cpu))
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -326,7 +386,7 @@ def run_ours(args):
                        "l2": "flushed before every timed step (512 MiB write, untimed)",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "roofline": roofline, "kernels": per_kernel, "cpu_baseline": cpu, "e2e": e2e,
-            "clocks": clk, "gpu_launches": launches,
+            "clocks": clk, "gpu_launches": launches, "cgsense": cgs_part,
         }
         print(json.dumps(line))
     if ws > 1:
@@ -342,6 +402,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-cgsense", action="store_true", help="skip the config-0 CG-SENSE section")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -38,7 +38,7 @@ class PlanDesc(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("mode", C.c_int), ("cgiter", C.c_int), ("cgeps", C.c_double),
                 ("lam", C.c_double), ("ftiter", C.c_int), ("fteps", C.c_double),
-                ("weighted", C.c_int)]
+                ("weighted", C.c_int), ("toeplitz", C.c_int)]
 
 
 class SolveReport(C.Structure):
@@ -205,9 +205,9 @@ class Plan:
         return out
 
     def solve(self, y, out, mode=MODE_CODEARE, cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3,
-              weighted=True, stream=None):
+              weighted=True, toeplitz=False, stream=None):
         o = SolveOpts(int(mode), int(cgiter), float(cgeps), float(lam), int(ftiter), float(fteps),
-                      int(bool(weighted)))
+                      int(bool(weighted)), int(bool(toeplitz)))
         rep = SolveReport()
         _check(load().cgs_solve(self._h, _ptr(y), _ptr(out), C.byref(o), C.byref(rep), _stream(stream)))
         n = rep.iterations

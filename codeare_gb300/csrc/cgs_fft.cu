@@ -235,19 +235,35 @@ axis_fft_kernel(const __grid_constant__ AxisPass p, int BO, int BI, int64_t nib)
     __syncthreads();
 
     // ---- Stockham passes, in place in shared memory ----
-    int Ns = 1, logNs = 0;
-    for (int s = 0; s < p.nfac; ++s) {
-        const int R = p.fac[s];
-        switch (R) {
-            case 8: stockham_pass<8, POW2>(bufA, tw, n, Ns, logNs, B, logB, P, p.sign); logNs += 3; break;
-            case 4: stockham_pass<4, POW2>(bufA, tw, n, Ns, logNs, B, logB, P, p.sign); logNs += 2; break;
-            case 2: stockham_pass<2, POW2>(bufA, tw, n, Ns, logNs, B, logB, P, p.sign); logNs += 1; break;
-            case 3: if (MIXED) stockham_pass<3, false>(bufA, tw, n, Ns, logNs, B, logB, P, p.sign); break;
-            case 5: if (MIXED) stockham_pass<5, false>(bufA, tw, n, Ns, logNs, B, logB, P, p.sign); break;
-            case 7: if (MIXED) stockham_pass<7, false>(bufA, tw, n, Ns, logNs, B, logB, P, p.sign); break;
-            default: break;  // host rejects other primes
+    const int rounds = p.toep_k ? 2 : 1;
+    for (int round = 0; round < rounds; ++round) {
+        const int sign = round == 0 ? p.sign : +1;
+        int Ns = 1, logNs = 0;
+        for (int s = 0; s < p.nfac; ++s) {
+            const int R = p.fac[s];
+            switch (R) {
+                case 8: stockham_pass<8, POW2>(bufA, tw, n, Ns, logNs, B, logB, P, sign); logNs += 3; break;
+                case 4: stockham_pass<4, POW2>(bufA, tw, n, Ns, logNs, B, logB, P, sign); logNs += 2; break;
+                case 2: stockham_pass<2, POW2>(bufA, tw, n, Ns, logNs, B, logB, P, sign); logNs += 1; break;
+                case 3: if (MIXED) stockham_pass<3, false>(bufA, tw, n, Ns, logNs, B, logB, P, sign); break;
+                case 5: if (MIXED) stockham_pass<5, false>(bufA, tw, n, Ns, logNs, B, logB, P, sign); break;
+                case 7: if (MIXED) stockham_pass<7, false>(bufA, tw, n, Ns, logNs, B, logB, P, sign); break;
+                default: break;  // host rejects other primes
+            }
+            Ns *= R;
         }
-        Ns *= R;
+        if (round == 0 && p.toep_k) {
+            // pointwise multiply by the real Toeplitz kernel of this column block
+            const int64_t kstride = p.inner / p.toep_nc;
+            for (int e = threadIdx.x; e < tot; e += kThreads) {
+                int pos, b;
+                if (pos_fast) { b = POW2 ? (e >> logn) : e / n; pos = POW2 ? (e & (n - 1)) : e % n; }
+                else { pos = POW2 ? (e >> logB) : e / B; b = POW2 ? (e & (B - 1)) : e % B; }
+                const int64_t i = ib0 + (POW2 ? (b & (BI - 1)) : b % BI);
+                if (i < p.inner) bufA[pos * P + b] = cscale(bufA[pos * P + b], p.toep_k[pos * kstride + i / p.toep_nc]);
+            }
+            __syncthreads();
+        }
     }
     const float2 *src = bufA;
 

@@ -110,6 +110,11 @@ struct AxisPass {
     int o1_len;            // length of the o1 image dim (to split outer = o0 * o1_len + o1)
     int64_t combine_stride;// STORE_COMBINE output: out[o*Lout + a]
     float2 *combine_out;
+    // Toeplitz: after the forward transform, multiply by a real kernel and
+    // transform back (sign +1) before the store: K[pos][i / toep_nc] with
+    // row stride inner / toep_nc (outer must be 1)
+    const float *toep_k;
+    int toep_nc;
 };
 
 cgs_status launch_axis_pass(const AxisPass &p, cudaStream_t st);
@@ -207,7 +212,17 @@ cgs_status launch_zero(void *p, size_t bytes, cudaStream_t st);
 struct CGScalars {
     double rn, xn, rno, pq, ts, beta, lambda;
     int done;
+    // device-driven loop control
+    double tol;          // break when the residual measure <= tol
+    int iter, maxit;     // updates made / allowed
+    int sqrt_mode;       // residual measure: 0 rn/xn (codeare), 1 sqrt(rn/xn)
+    int nan_flag;
+    double hist[256];    // residual measure per check
 };
+// Loop check (one thread): records the residual measure of the current
+// iterate, decides whether another update follows, and sets the conditional
+// handle of the enclosing while node accordingly.
+cgs_status launch_cg_check(CGScalars *sc, cudaGraphConditionalHandle h, cudaStream_t st);
 // q += lambda * p ; then pq = Re<p,q> is computed by coldot
 cgs_status launch_add_scaled(float2 *q, const float2 *p, const CGScalars *sc, int64_t n,
                              cudaStream_t st);

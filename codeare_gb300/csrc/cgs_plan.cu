@@ -60,9 +60,15 @@ void prof_drain()
 }
 }  // namespace
 
+static bool capturing(cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
 void prof_begin(int cat, cudaStream_t st)
 {
-    if (!g_prof_on) return;
+    if (!g_prof_on || capturing(st)) return;
     std::lock_guard<std::mutex> lk(g_prof_mu);
     if (g_prof_recs.size() > 4096) prof_drain();
     ProfRec r{cat, prof_event(), prof_event()};
@@ -73,7 +79,7 @@ void prof_begin(int cat, cudaStream_t st)
 
 void prof_end(int cat, cudaStream_t st)
 {
-    if (!g_prof_on) return;
+    if (!g_prof_on || capturing(st)) return;
     std::lock_guard<std::mutex> lk(g_prof_mu);
     if (g_prof_open >= 0 && g_prof_recs[g_prof_open].cat == cat) cudaEventRecord(g_prof_recs[g_prof_open].b, st);
     g_prof_open = -1;
@@ -103,6 +109,26 @@ static bool factorize(int n, int *fac, int *nf)
     *nf = k;
     return r == 1;
 }
+
+namespace toepk {
+__global__ void toep_prepare_kernel(float2 *T, int d, int n0, int n1, int n2)
+{
+    const int64_t tot = (int64_t)n0 * n1 * n2;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+        const int i2 = (int)(e % n2), i1 = (int)((e / n2) % n1), i0 = (int)(e / ((int64_t)n1 * n2));
+        bool edge = (i0 == 0) || (i1 == 0);
+        if (d == 3) edge = edge || (i2 == 0);
+        if (edge) T[e] = make_float2(0.f, 0.f);
+    }
+}
+
+__global__ void toep_real_kernel(const float2 *K, float *out, int64_t tot, float scale)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x)
+        out[e] = K[e].x * scale;
+}
+
+}  // namespace toepk
 
 }  // namespace cgs
 
@@ -136,6 +162,17 @@ struct cgs_plan {
     float2 *ppartial = nullptr;
     PatchSet pset{};
 
+    // host copies of the trajectory and weights (the Toeplitz kernel is built from them)
+    std::vector<float> k_host, w_host;
+    // Toeplitz embedding of E^H W E (standard mode)
+    bool toep_valid = false;
+    int toep_weighted = -1;
+    int n2[3] = {1, 1, 1};
+    float2 *tw2[3] = {nullptr, nullptr, nullptr};
+    int fac2[3][12] = {}, nfac2[3] = {0, 0, 0};
+    float *toepK = nullptr;
+    float2 *tA = nullptr, *tB = nullptr;
+
     // image-side maps
     float *mask = nullptr;   // damping mask What (N^d)
     float *imap = nullptr;   // intensity map I (N^d)
@@ -151,6 +188,11 @@ struct cgs_plan {
     int *active = nullptr;
     CGScalars *sc = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // captured solve: prologue + while(iteration) as one CUDA graph
+    cudaGraphExec_t solve_exec = nullptr;
+    int sg_mode = -1, sg_toep = -1, sg_weighted = -1, sg_ftiter = -1;
+    double sg_fteps = -1.0;
+    int64_t sg_kpro = 0, sg_kbody = 0;
 
     double *dot_r() { return dots; }
     double *dot_z() { return dots + nc; }
@@ -442,6 +484,244 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     return CGS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Toeplitz embedding of A^H W A (per coil, shared kernel):
+//   (A^H W A f)_k = sum_k' T[k - k'] f_k',  T[d] = sum_j w_j exp(+2 pi i d.x_j),
+// d in [-N, N)^d, computed once as the adjoint NFFT of the weights on a 2N
+// image.  The circulant extension C (C = T with the unused d = -N faces
+// zeroed, so C is Hermitian) has a real 2N-point DFT K; the operator is then
+// pad(N -> 2N) . FFT . (K / (2N)^d) . IFFT . crop(2N -> N).
+// ---------------------------------------------------------------------------
+AxisPass toep_pass(cgs_plan *p, int t)
+{
+    AxisPass a{};
+    a.n = p->n2[t];
+    a.tw = p->tw2[t];
+    a.nfac = p->nfac2[t];
+    for (int i = 0; i < 12; ++i) a.fac[i] = p->fac2[t][i];
+    a.load_mode = LOAD_PLAIN;
+    a.store_mode = STORE_PLAIN;
+    a.o1_len = 1;
+    return a;
+}
+
+cgs_status build_toeplitz(cgs_plan *p, int weighted, cudaStream_t st)
+{
+    const int d = p->d;
+    int64_t T2 = 1;
+    for (int t = 0; t < d; ++t) {
+        p->n2[t] = 2 * p->N[t];
+        if (!factorize(p->n2[t], p->fac2[t], &p->nfac2[t])) { set_error("2N must factor into 2, 3, 5, 7"); return CGS_ERR_BAD_ARG; }
+        T2 *= p->n2[t];
+        if (!p->tw2[t]) {
+            std::vector<float2> tw(p->n2[t]);
+            for (int i = 0; i < p->n2[t]; ++i) {
+                const double a = -2.0 * M_PI * (double)i / (double)p->n2[t];
+                tw[i] = make_float2((float)std::cos(a), (float)std::sin(a));
+            }
+            CGS_TRY(dev_alloc(&p->tw2[t], (size_t)p->n2[t]));
+            CGS_CUDA(cudaMemcpy(p->tw2[t], tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice));
+        }
+    }
+    const int64_t nc = p->nc;
+    if (!p->tA) {
+        // 2-D: [N0][2N1][NC]; 3-D: [N0][N1][2N2][NC] and [N0][2N1][2N2][NC]
+        int64_t a = (d == 2) ? (int64_t)p->N[0] * p->n2[1] : (int64_t)p->N[0] * p->N[1] * p->n2[2];
+        CGS_TRY(dev_alloc(&p->tA, (size_t)(a * nc)));
+        if (d == 3) CGS_TRY(dev_alloc(&p->tB, (size_t)((int64_t)p->N[0] * p->n2[1] * p->n2[2] * nc)));
+        CGS_TRY(dev_alloc(&p->toepK, (size_t)T2));
+    }
+    // point-spread function through a one-coil plan on the 2N image
+    cgs_plan_desc sd{};
+    sd.rank = d;
+    for (int t = 0; t < d; ++t) sd.N[t] = p->n2[t];
+    sd.alpha = p->alpha; sd.m = p->m; sd.M = p->M; sd.ncoils = 1;
+    cgs_plan *sub = nullptr;
+    CGS_TRY(cgs_plan_create(&sub, &sd));
+    float2 *wc = nullptr, *T = nullptr;
+    cgs_status r = cgs_set_kspace(sub, p->k_host.data());
+    if (r == CGS_OK) r = dev_alloc(&wc, (size_t)p->M);
+    if (r == CGS_OK) r = dev_alloc(&T, (size_t)T2);
+    if (r == CGS_OK) {
+        std::vector<float2> wh(p->M);
+        for (int64_t j = 0; j < p->M; ++j) wh[j] = make_float2(weighted ? p->w_host[j] : 1.f, 0.f);
+        if (cudaMemcpy(wc, wh.data(), sizeof(float2) * wh.size(), cudaMemcpyHostToDevice) != cudaSuccess) r = CGS_ERR_CUDA;
+    }
+    if (r == CGS_OK) r = cgs_nfft_adjoint(sub, (const float *)wc, (float *)T, st);
+    if (r == CGS_OK && cudaStreamSynchronize(st) != cudaSuccess) r = CGS_ERR_CUDA;
+    cgs_plan_destroy(sub);
+    if (r == CGS_OK) {
+        toepk::toep_prepare_kernel<<<1024, 256, 0, st>>>(T, d, p->n2[0], p->n2[1], d == 3 ? p->n2[2] : 1);
+        if (cudaGetLastError() != cudaSuccess) r = CGS_ERR_CUDA;
+        count_launch();
+    }
+    // DFT of the circulant kernel: centred input (index d + N <-> position d mod 2N), full output
+    for (int t = 0; t < d && r == CGS_OK; ++t) {
+        AxisPass a = toep_pass(p, t);
+        int64_t outer = 1, inner = 1;
+        for (int u = 0; u < t; ++u) outer *= p->n2[u];
+        for (int u = t + 1; u < d; ++u) inner *= p->n2[u];
+        a.outer = outer; a.inner = inner; a.Lin = p->n2[t]; a.Lout = p->n2[t]; a.sign = -1;
+        a.in_centred = 1; a.out_centred = 0;
+        a.src = T; a.dst = T;  // in place: every CTA reads its columns before writing them
+        r = launch_axis_pass(a, st);
+    }
+    if (r == CGS_OK) {
+        toepk::toep_real_kernel<<<1024, 256, 0, st>>>(T, p->toepK, T2, (float)(1.0 / (double)T2));
+        if (cudaGetLastError() != cudaSuccess) r = CGS_ERR_CUDA;
+        count_launch();
+    }
+    if (r == CGS_OK && cudaStreamSynchronize(st) != cudaSuccess) r = CGS_ERR_CUDA;
+    dev_free(wc);
+    dev_free(T);
+    if (r != CGS_OK) return r;
+    p->toep_valid = true;
+    p->toep_weighted = weighted;
+    return CGS_OK;
+}
+
+// out = sum_c conj(S_c) (A^H W A)(S_c x) through the Toeplitz kernel
+cgs_status op_ehe_toeplitz(cgs_plan *p, const float2 *x, float2 *out, cudaStream_t st)
+{
+    const int d = p->d, nc = p->nc;
+    {   // pad the fastest axis: image -> [..][2N][NC], with the coil expansion
+        AxisPass a = toep_pass(p, d - 1);
+        int64_t outer = 1;
+        for (int t = 0; t < d - 1; ++t) outer *= p->N[t];
+        a.outer = outer; a.inner = nc; a.Lin = p->N[d - 1]; a.Lout = p->n2[d - 1]; a.sign = -1; a.in_centred = 1;
+        a.load_mode = LOAD_IMAGE; a.img = x; a.img_per_coil = 0; a.sens = p->sens;
+        a.dst = p->tA;
+        CGS_TRY(launch_axis_pass(a, st));
+    }
+    float2 *cur = p->tA;
+    if (d == 3) {
+        AxisPass a = toep_pass(p, 1);
+        a.outer = p->N[0]; a.inner = (int64_t)p->n2[2] * nc; a.Lin = p->N[1]; a.Lout = p->n2[1]; a.sign = -1;
+        a.in_centred = 1; a.src = p->tA; a.dst = p->tB;
+        CGS_TRY(launch_axis_pass(a, st));
+        cur = p->tB;
+    }
+    {   // slowest axis: FFT, multiply by K, inverse FFT, crop (in place)
+        AxisPass a = toep_pass(p, 0);
+        int64_t inner = nc;
+        for (int t = 1; t < d; ++t) inner *= p->n2[t];
+        a.outer = 1; a.inner = inner; a.Lin = p->N[0]; a.Lout = p->N[0]; a.sign = -1;
+        a.in_centred = 1; a.out_centred = 1; a.src = cur; a.dst = cur;
+        a.toep_k = p->toepK; a.toep_nc = nc;
+        CGS_TRY(launch_axis_pass(a, st));
+    }
+    if (d == 3) {
+        AxisPass a = toep_pass(p, 1);
+        a.outer = p->N[0]; a.inner = (int64_t)p->n2[2] * nc; a.Lin = p->n2[1]; a.Lout = p->N[1]; a.sign = +1;
+        a.out_centred = 1; a.src = p->tB; a.dst = p->tA;
+        CGS_TRY(launch_axis_pass(a, st));
+    }
+    {   // crop the fastest axis back to the image
+        AxisPass a = toep_pass(p, d - 1);
+        int64_t outer = 1;
+        for (int t = 0; t < d - 1; ++t) outer *= p->N[t];
+        a.outer = outer; a.inner = nc; a.Lin = p->n2[d - 1]; a.Lout = p->N[d - 1]; a.sign = +1; a.out_centred = 1;
+        a.src = p->tA; a.dst = p->cF;
+        CGS_TRY(launch_axis_pass(a, st));
+    }
+    return launch_coil_combine(p->cF, p->sens, nullptr, p->Nt, nc, out, st);
+}
+
+// One CG-SENSE iteration (either mode) on the plan's buffers.
+cgs_status cg_iteration(cgs_plan *p, const cgs_solve_opts *o, cudaStream_t st)
+{
+    const int64_t Nt = p->Nt;
+    if (o->mode == CGS_MODE_CODEARE) {
+        CGS_TRY(op_forward(p, p->vP, 0, nullptr, p->ksV, st));
+        CGS_TRY(op_eh_codeare(p, p->ksV, o->ftiter, o->fteps, p->vQ, st));
+    } else if (o->toeplitz) {
+        CGS_TRY(op_ehe_toeplitz(p, p->vP, p->vQ, st));
+    } else {
+        CGS_TRY(op_forward(p, p->vP, 0, nullptr, p->ksV, st));
+        CGS_TRY(op_eh(p, p->ksV, o->weighted, p->vQ, st));
+    }
+    CGS_TRY(launch_add_scaled(p->vQ, p->vP, p->sc, Nt, st));
+    CGS_TRY(launch_coldot(p->vP, p->vQ, nullptr, Nt, 1, p->partial, p->scal(), st));
+    CGS_TRY(launch_scalar_op(p->sc, p->scal(), 1, st));
+    CGS_TRY(launch_cg_update_xr(p->vX, p->vR, p->vP, p->vQ, p->sc, Nt, st));
+    CGS_TRY(launch_coldot(p->vR, p->vR, nullptr, Nt, 1, p->partial, p->scal(), st));
+    CGS_TRY(launch_scalar_op(p->sc, p->scal(), 2, st));
+    return launch_cg_update_p(p->vP, p->vR, p->sc, Nt, st);
+}
+
+// Capture the whole solve once per (mode, operator, weighting, inner CGNR
+// setting): a prologue (E^H of the data, r = p, rn = xn, first check) and a
+// while node whose body is one iteration followed by the check.  The check
+// kernel decides on the device whether the loop continues, so a solve is one
+// graph launch and one read-back.
+cgs_status build_solve_graph(cgs_plan *p, const cgs_solve_opts *o, cudaStream_t st)
+{
+    if (p->solve_exec) { cudaGraphExecDestroy(p->solve_exec); p->solve_exec = nullptr; }
+    const int64_t Nt = p->Nt;
+    cudaGraph_t g = nullptr;
+    CGS_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    cgs_status r = CGS_OK;
+    if (cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) r = CGS_ERR_CUDA;
+    const int64_t c0 = cgs_kernel_launches();
+    std::vector<cudaGraphNode_t> frontier;
+    if (r == CGS_OK && cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+        r = CGS_ERR_CUDA;
+    if (r == CGS_OK) {
+        cgs_status q = (o->mode == CGS_MODE_CODEARE) ? op_eh_codeare(p, p->ksY, o->ftiter, o->fteps, p->vP, st)
+                                                      : op_eh(p, p->ksY, o->weighted, p->vP, st);
+        if (q == CGS_OK && cudaMemcpyAsync(p->vR, p->vP, sizeof(float2) * Nt, cudaMemcpyDeviceToDevice, st) != cudaSuccess) q = CGS_ERR_CUDA;
+        if (q == CGS_OK) q = launch_zero(p->vX, sizeof(float2) * Nt, st);
+        if (q == CGS_OK) q = launch_coldot(p->vR, p->vP, nullptr, Nt, 1, p->partial, p->scal(), st);
+        if (q == CGS_OK) q = launch_scalar_op(p->sc, p->scal(), 0, st);
+        if (q == CGS_OK) q = launch_cg_check(p->sc, h, st);
+        if (q == CGS_OK) {
+            cudaStreamCaptureStatus cs;
+            const cudaGraphNode_t *deps = nullptr;
+            size_t nd = 0;
+            if (cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd) != cudaSuccess) q = CGS_ERR_CUDA;
+            else frontier.assign(deps, deps + nd);
+        }
+        cudaGraph_t gg = g;
+        if (cudaStreamEndCapture(st, &gg) != cudaSuccess && q == CGS_OK) q = CGS_ERR_CUDA;
+        r = q;
+    }
+    p->sg_kpro = cgs_kernel_launches() - c0;
+    cudaGraphNode_t cond = nullptr;
+    cudaGraph_t body = nullptr;
+    if (r == CGS_OK) {
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        if (cudaGraphAddNode(&cond, g, frontier.data(), nullptr, frontier.size(), &cp) != cudaSuccess) r = CGS_ERR_CUDA;
+        else body = cp.conditional.phGraph_out[0];
+    }
+    const int64_t c1 = cgs_kernel_launches();
+    if (r == CGS_OK && cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+        r = CGS_ERR_CUDA;
+    if (r == CGS_OK) {
+        cgs_status q = cg_iteration(p, o, st);
+        if (q == CGS_OK) q = launch_cg_check(p->sc, h, st);
+        cudaGraph_t bb = body;
+        if (cudaStreamEndCapture(st, &bb) != cudaSuccess && q == CGS_OK) q = CGS_ERR_CUDA;
+        r = q;
+    }
+    p->sg_kbody = cgs_kernel_launches() - c1;
+    count_launch((int)-(cgs_kernel_launches() - c0));  // captured launches run only when the graph runs
+    if (r == CGS_OK && cudaGraphInstantiate(&p->solve_exec, g, 0) != cudaSuccess) {
+        set_error("cudaGraphInstantiate of the solve graph failed");
+        r = CGS_ERR_CUDA;
+    }
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (r != CGS_OK) { p->solve_exec = nullptr; return r; }
+    p->sg_mode = o->mode; p->sg_toep = o->toeplitz; p->sg_weighted = o->weighted;
+    p->sg_ftiter = o->ftiter; p->sg_fteps = o->fteps;
+    return CGS_OK;
+}
+
 cgs_status check_ready(cgs_plan *p, bool need_w, bool need_s)
 {
     if (!p) { set_error("null plan"); return CGS_ERR_BAD_ARG; }
@@ -611,6 +891,9 @@ cgs_status cgs_plan_destroy(cgs_plan *p)
                     p->cF, p->cP, p->cZ, p->vX, p->vR, p->vP, p->vQ, p->ioA, p->ioB, p->partial, p->dots,
                     p->active, p->sc};
     for (void *b : bufs) dev_free(b);
+    for (void *b : {(void *)p->tw2[0], (void *)p->tw2[1], (void *)p->tw2[2], (void *)p->toepK, (void *)p->tA,
+                    (void *)p->tB}) dev_free(b);
+    if (p->solve_exec) cudaGraphExecDestroy(p->solve_exec);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -643,6 +926,7 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
     } else {
         std::memcpy(k.data(), k_in, sizeof(float) * k.size());
     }
+    p->toep_valid = false;
     const GridGeom &g = p->geom;
     int ntiles = 1;
     for (int t = 0; t < d; ++t) ntiles *= g.nt[t];
@@ -706,6 +990,7 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
     CGS_CUDA(cudaMemcpy(p->nodes, nodes.data(), sizeof(float4) * nodes.size(), cudaMemcpyHostToDevice));
     CGS_CUDA(cudaMemcpy(p->perm, perm.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
     if (d == 2) CGS_TRY(build_patches(p, cc));
+    p->k_host = k;
     p->have_k = true;
     // weights (if already given) must follow the new order: reset to "unset"
     p->have_w = false;
@@ -726,6 +1011,8 @@ cgs_status cgs_set_weights(cgs_plan *p, const float *w_in)
     CGS_CUDA(cudaMemcpy(perm.data(), p->perm, sizeof(int) * M, cudaMemcpyDeviceToHost));
     for (int64_t s = 0; s < M; ++s) ws[s] = w[perm[s]];
     CGS_CUDA(cudaMemcpy(p->w, ws.data(), sizeof(float) * M, cudaMemcpyHostToDevice));
+    p->w_host = w;
+    p->toep_valid = false;
     p->have_w = true;
     return CGS_OK;
 }
@@ -871,59 +1158,45 @@ cgs_status cgs_solve(cgs_plan *p, const float *y, float *x, const cgs_solve_opts
     cudaStream_t st = pick_stream(p, stream);
     const int64_t Nt = p->Nt;
     if (rep) std::memset(rep, 0, sizeof(*rep));
+    if (!codeare && o->toeplitz) {
+        const int wtd = (o->weighted && p->have_w) ? 1 : 0;
+        if (!p->toep_valid || p->toep_weighted != wtd) CGS_TRY(build_toeplitz(p, wtd, st));
+    }
     CGS_CUDA(cudaEventRecord(p->ev0, st));
     CGS_TRY(ks_in(p, y, st));
-    // p = A/b (codeare) or b = E^H W y (standard)
-    if (codeare) CGS_TRY(op_eh_codeare(p, p->ksY, o->ftiter, o->fteps, p->vP, st));
-    else CGS_TRY(op_eh(p, p->ksY, o->weighted, p->vP, st));
     int iters = 0;
     cgs_status result = CGS_OK;
     if (o->cgiter == 0 && codeare) {
-        CGS_CUDA(cudaMemcpyAsync(p->vX, p->vP, sizeof(float2) * Nt, cudaMemcpyDeviceToDevice, st));
+        // CGLS with no iterations returns A/b (CGLS.hpp:32-33)
+        CGS_TRY(op_eh_codeare(p, p->ksY, o->ftiter, o->fteps, p->vX, st));
     } else {
+        const bool same = p->solve_exec && p->sg_mode == o->mode && p->sg_toep == (codeare ? 0 : o->toeplitz) &&
+                          p->sg_weighted == o->weighted && p->sg_ftiter == o->ftiter && p->sg_fteps == o->fteps;
+        if (!same) {
+            cgs_solve_opts oo = *o;
+            if (codeare) oo.toeplitz = 0;
+            CGS_TRY(build_solve_graph(p, &oo, st));
+        }
         CGScalars init{};
         init.lambda = o->lambda;
+        init.tol = o->cgeps;
+        init.maxit = o->cgiter;
+        init.sqrt_mode = codeare ? 0 : 1;
         CGS_CUDA(cudaMemcpyAsync(p->sc, &init, sizeof(init), cudaMemcpyHostToDevice, st));
-        CGS_CUDA(cudaMemcpyAsync(p->vR, p->vP, sizeof(float2) * Nt, cudaMemcpyDeviceToDevice, st));
-        CGS_TRY(launch_zero(p->vX, sizeof(float2) * Nt, st));
-        CGS_TRY(launch_coldot(p->vR, p->vP, nullptr, Nt, 1, p->partial, p->scal(), st));
-        CGS_TRY(launch_scalar_op(p->sc, p->scal(), 0, st));
-        for (int i = 0; i < o->cgiter; ++i) {
-            CGScalars h;
-            CGS_TRY(read_scalars(p, &h, st));
-            const double res = codeare ? h.rn / h.xn : std::sqrt(h.rn / h.xn);
-            if (rep) {
-                if (i == 0) rep->res_first = res;
-                if (i < 256) rep->res_hist[i] = res;
-                rep->res_last = res;
-            }
-            if (std::isnan(res)) { result = CGS_ERR_NAN; break; }
-            if (res <= o->cgeps) break;
-            if (codeare) {
-                CGS_TRY(op_forward(p, p->vP, 0, nullptr, p->ksV, st));
-                CGS_TRY(op_eh_codeare(p, p->ksV, o->ftiter, o->fteps, p->vQ, st));
-            } else {
-                CGS_TRY(op_forward(p, p->vP, 0, nullptr, p->ksV, st));
-                CGS_TRY(op_eh(p, p->ksV, o->weighted, p->vQ, st));
-            }
-            if (o->lambda != 0.0) CGS_TRY(launch_add_scaled(p->vQ, p->vP, p->sc, Nt, st));
-            CGS_TRY(launch_coldot(p->vP, p->vQ, nullptr, Nt, 1, p->partial, p->scal(), st));
-            CGS_TRY(launch_scalar_op(p->sc, p->scal(), 1, st));
-            CGS_TRY(launch_cg_update_xr(p->vX, p->vR, p->vP, p->vQ, p->sc, Nt, st));
-            CGS_TRY(launch_coldot(p->vR, p->vR, nullptr, Nt, 1, p->partial, p->scal(), st));
-            CGS_TRY(launch_scalar_op(p->sc, p->scal(), 2, st));
-            CGS_TRY(launch_cg_update_p(p->vP, p->vR, p->sc, Nt, st));
-            iters = i + 1;
-        }
-        if (!codeare || o->cgiter > 0) {
-            // residual after the last update (standard mode reports it)
-            CGScalars h;
-            CGS_TRY(read_scalars(p, &h, st));
-            if (rep && !codeare) {
-                const double res = std::sqrt(h.rn / h.xn);
-                rep->res_last = res;
-                if (iters < 256) rep->res_hist[iters] = res;
-            }
+        CGS_CUDA(cudaGraphLaunch(p->solve_exec, st));
+        CGScalars h;
+        CGS_TRY(read_scalars(p, &h, st));
+        iters = h.iter;
+        count_launch((int)(p->sg_kpro + (int64_t)h.iter * p->sg_kbody));
+        if (h.nan_flag) result = CGS_ERR_NAN;
+        if (rep) {
+            const int nh = std::min(256, h.iter + 1);
+            for (int i = 0; i < nh; ++i) rep->res_hist[i] = h.hist[i];
+            rep->res_first = h.hist[0];
+            // the measure after the last update (the loop's final check records it unless maxit ended it)
+            const double ratio = h.rn / h.xn;
+            rep->res_last = codeare ? ratio : std::sqrt(ratio);
+            if (!codeare && h.iter < 256) rep->res_hist[h.iter] = rep->res_last;
         }
     }
     CGS_CUDA(cudaEventRecord(p->ev1, st));

@@ -211,6 +211,28 @@ __global__ void cg_update_p_kernel(float2 *__restrict__ p, const float2 *__restr
     }
 }
 
+__global__ void cg_check_kernel(CGScalars *sc, cudaGraphConditionalHandle h)
+{
+    unsigned int go = 0;
+    if (!sc->done) {
+        if (sc->iter >= sc->maxit) {
+            sc->done = 1;
+        } else if (sc->sqrt_mode && sc->xn == 0.0) {
+            // zero right-hand side: x = 0 is the solution
+            if (sc->iter < 256) sc->hist[sc->iter] = 0.0;
+            sc->done = 1;
+        } else {
+            const double ratio = sc->rn / sc->xn;
+            const double res = sc->sqrt_mode ? sqrt(ratio) : ratio;
+            if (sc->iter < 256) sc->hist[sc->iter] = res;
+            if (isnan(res)) { sc->nan_flag = 1; sc->done = 1; }
+            else if (res <= sc->tol) { sc->done = 1; }
+            else { sc->iter += 1; go = 1; }
+        }
+    }
+    cudaGraphSetConditional(h, go);
+}
+
 // op 0: rn = xn = *src; 1: pq = *src; 2: rno = rn, rn = *src
 __global__ void scalar_op_kernel(CGScalars *sc, const double *src, int op)
 {
@@ -379,6 +401,13 @@ cgs_status launch_cg_update_p(float2 *p, const float2 *r, const CGScalars *sc, i
 cgs_status launch_scalar_op(CGScalars *sc, const double *src, int op, cudaStream_t st)
 {
     scalar_op_kernel<<<1, 1, 0, st>>>(sc, src, op);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_cg_check(CGScalars *sc, cudaGraphConditionalHandle h, cudaStream_t st)
+{
+    cg_check_kernel<<<1, 1, 0, st>>>(sc, h);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }

@@ -120,6 +120,10 @@ typedef struct {
     int ftiter;        /* inner CGNR steps (reference "ftmaxit", default 3)  */
     double fteps;      /* inner CGNR threshold (reference "fteps", 1e-3)     */
     int weighted;      /* standard mode: use the density weights W           */
+    int toeplitz;      /* standard mode: apply E^H W E by Toeplitz embedding
+                          (2N-grid FFT convolution with the weighted point-spread
+                          function, computed once per trajectory and weights);
+                          no reference counterpart                            */
 } cgs_solve_opts;
 
 typedef struct {

@@ -220,3 +220,40 @@ def test_edge_nodes_in_one_tile_and_boundary(gpu, oracle):
     img = np.zeros((2, N, N), np.complex64)
     p.nfft_adjoint(ys, img)
     assert rel(img, np.stack([P.adjoint(ys[c]) for c in range(2)])) < TOL_OP
+
+
+@pytest.mark.parametrize("weighted", [True, False])
+def test_standard_cg_toeplitz_2d(gpu, oracle, weighted):
+    """Standard-mode CG with E^H W E applied by Toeplitz embedding (2N-grid FFT
+    convolution) against the oracle's NFFT-based CG at the same iteration count."""
+    from codeare_gb300 import synth
+    cfg = synth.small_config(N=32, nc=4, nspokes=40, nsamp=64, alpha=2.0, m=4)
+    s = oracle.Sense(cfg["sens"], cfg["k"], w=cfg["w"], m=4, alpha=2.0)
+    y = s.trafo(cfg["image"])
+    xo, reso = s.cg(y, maxit=8, tol=1e-12, lam=1e-3, weighted=weighted)
+    p = make_plan(gpu, (32, 32), cfg["k"], 4, 4, 2.0, w=cfg["w"], S=cfg["sens"])
+    x = np.zeros((32, 32), np.complex64)
+    rep = p.solve(c64(y), x, mode=gpu.MODE_STANDARD, cgiter=8, cgeps=1e-12, lam=1e-3, weighted=weighted,
+                  toeplitz=True)
+    assert rep["iterations"] == 8
+    assert rel(x, xo) < TOL_IMG
+    np.testing.assert_allclose(rep["res_hist"][:9], reso[:9], rtol=2e-3)
+
+
+def test_standard_cg_toeplitz_3d(gpu, oracle):
+    from codeare_gb300 import synth
+    N, nc = 16, 2
+    k = synth.kooshball3d(300, 32)
+    w = synth.ramp_weights(k) ** 2 + 1e-3
+    S = synth.coils3d(N, nc)
+    s = oracle.Sense(S, k, w=w, m=3, alpha=2.0)
+    xt = synth.phantom3d(N)
+    y = s.trafo(xt)
+    xo, _ = s.cg(y, maxit=6, tol=1e-12, lam=1e-3, weighted=True)
+    p = make_plan(gpu, (N, N, N), k, nc, 3, 2.0, w=w, S=S)
+    x = np.zeros((N, N, N), np.complex64)
+    p.solve(c64(y), x, mode=gpu.MODE_STANDARD, cgiter=6, cgeps=1e-12, lam=1e-3, weighted=True, toeplitz=True)
+    assert rel(x, xo) < TOL_IMG
+    x2 = np.zeros_like(x)
+    p.solve(c64(y), x2, mode=gpu.MODE_STANDARD, cgiter=6, cgeps=1e-12, lam=1e-3, weighted=True, toeplitz=False)
+    assert rel(x2, xo) < TOL_IMG
