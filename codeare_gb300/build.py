@@ -74,30 +74,33 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
 
 HOST = os.path.join(HERE, "host")
 PLUGIN = os.path.join(LIBDIR, "CGSENSE.so")
+PLUGIN_NUFFT = os.path.join(LIBDIR, "NuFFT.so")
 DRIVER = os.path.join(LIBDIR, "cgsense_run")
 
 
 def build_host(force: bool = False) -> str:
-    """The C++ drop-in layer: CGSENSE.so (ReconStrategy plugin over libcgs.so)
-    and cgsense_run (a dlopen host that drives a plugin's lifecycle)."""
-    srcs = [os.path.join(HOST, f) for f in ("CGSENSE.cpp", "cgsense_run.cpp")]
+    """The C++ drop-in layer: CGSENSE.so and NuFFT.so (ReconStrategy plugins
+    over libcgs.so) and cgsense_run (a dlopen host that drives a plugin)."""
+    srcs = [os.path.join(HOST, f) for f in ("CGSENSE.cpp", "cgsense_run.cpp", "NuFFT.cpp")]
     hdrs = [os.path.join(HOST, "codeare", f) for f in os.listdir(os.path.join(HOST, "codeare"))]
     newest = max(os.path.getmtime(f) for f in srcs + hdrs + [LIB])
-    if not force and os.path.exists(PLUGIN) and os.path.exists(DRIVER) and \
-            min(os.path.getmtime(PLUGIN), os.path.getmtime(DRIVER)) >= newest:
+    outs = (PLUGIN, DRIVER, PLUGIN_NUFFT)
+    if not force and all(os.path.exists(o) for o in outs) and min(os.path.getmtime(o) for o in outs) >= newest:
         return PLUGIN
     common = ["g++", "-O2", "-std=c++17", "-Wall", "-I" + HOST, "-I" + os.path.join(ROOT, "include")]
     cmds = [
         common + ["-fPIC", "-shared", srcs[0], "-o", PLUGIN + ".tmp", "-L" + LIBDIR, "-lcgs",
                   "-Wl,-rpath,$ORIGIN"],
         common + [srcs[1], "-o", DRIVER + ".tmp", "-ldl", "-rdynamic"],
+        common + ["-fPIC", "-shared", srcs[2], "-o", PLUGIN_NUFFT + ".tmp", "-L" + LIBDIR, "-lcgs",
+                  "-Wl,-rpath,$ORIGIN"],
     ]
     for cmd in cmds:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("host build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
-    os.replace(PLUGIN + ".tmp", PLUGIN)
-    os.replace(DRIVER + ".tmp", DRIVER)
+    for o in outs:
+        os.replace(o + ".tmp", o)
     return PLUGIN
 
 

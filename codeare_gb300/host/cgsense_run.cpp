@@ -90,7 +90,14 @@ int main(int argc, char **argv)
     destroy_t *destroy = (destroy_t *)dlsym(h, "destroy");
     if (!create || !destroy) { std::fprintf(stderr, "plugin lacks create/destroy\n"); return 5; }
     RRStrategy::ReconStrategy *rs = create();
-    rs->Name("CGSENSE");
+    {   // the module name is the plugin file's base name, as codeare's loader uses it
+        std::string nm(argv[1]);
+        const size_t sl = nm.find_last_of('/');
+        if (sl != std::string::npos) nm = nm.substr(sl + 1);
+        const size_t dot = nm.find('.');
+        if (dot != std::string::npos) nm = nm.substr(0, dot);
+        rs->Name(nm.c_str());
+    }
     rs->WSpace(&ws);
     rs->SetConfig(xml.c_str());
     codeare::error_code e = rs->Init();

@@ -38,8 +38,17 @@ public:
         m_N = p.Get<std::vector<size_t>>("imsz");
         if (try_to_fetch<bool>(p, "3rd_dim_cart", false))
             throw std::invalid_argument("NFFT: a Cartesian third dimension is not supported");
-        if (p.exists("b0") || p.exists("timing") || p.exists("pc"))
-            throw std::invalid_argument("NFFT: off-resonance (b0/timing) and phase correction are not supported");
+        // off-resonance data only takes effect when its size matches the image
+        // (NFFT.hpp:113-140 of the reference warns and ignores it otherwise)
+        size_t nimg = 1;
+        for (size_t v : m_N) nimg *= v;
+        if (p.exists("b0")) {
+            bool fits = false;
+            try { fits = p.Get<Matrix<RT>>("b0").Size() == nimg; } catch (...) {}
+            if (fits) throw std::invalid_argument("NFFT: off-resonance correction (b0) is not supported");
+            std::printf("  WARNING - NFFT: b0 field does not fit to image space. Defaulting to flat b0 = 0\n");
+        }
+        if (p.exists("pc")) throw std::invalid_argument("NFFT: phase correction (pc) is not supported");
         m_m = try_to_fetch<size_t>(p, "m", 1);
         m_alpha = try_to_fetch<float>(p, "alpha", 1.0f);
         m_epsilon = try_to_fetch<float>(p, "epsilon", 7.0e-4f);

@@ -73,3 +73,29 @@ def test_plugin_standard_mode(gpu, oracle, tmp_path):
              "ftmaxit": 3, "fteps": 0.001, "noise": 0, "testcase": 0, "mode": "standard"}
     img, log = run_plugin(tmp_path, mats, attrs)
     assert rel(img, xo) < TOL_IMG, log
+
+
+def test_nufft_plugin_matches_reference_semantics(gpu, oracle, tmp_path):
+    """NuFFT.so: img = NFFT ->* data, the CGNR inverse NFFT with the reference's
+    unforwarded defaults (3 steps, epsilon 7e-4) whatever maxit/epsilon say
+    (src/modules/NuFFT.cpp:74-75 vs :99-108)."""
+    from codeare_gb300 import build, cgsm, synth
+    build.build()
+    N = 32
+    k = synth.radial2d(24, 64, golden=True)
+    w = synth.ramp_weights(k)
+    M = k.shape[0]
+    P = oracle.NFFT((N, N), M, m=2, alpha=1.5)
+    P.set_x(k)
+    data = P.trafo(synth.phantom(N)).astype(np.complex64)
+    ref, _, _ = P.itrafo(data, w, oracle.damp_mask((N, N)), maxit=3, eps=7e-4)
+    inp, out, xml = tmp_path / "in.cgsm", tmp_path / "out.cgsm", tmp_path / "cfg.xml"
+    cgsm.write(str(inp), {"kspace": k, "weights": w, "data": data[None, :]})
+    xml.write_text('<NuFFT dim="2" nx="%d" ny="%d" M="%d" shots="1" maxit="20" epsilon="1e-9" m="2" '
+                   'alpha="1.5" dft_3rd_dim="0" test_case="0"/>\n' % (N, N, M))
+    r = subprocess.run([build.DRIVER, build.PLUGIN_NUFFT, str(xml), str(inp), str(out), "img"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    img = cgsm.read(str(out))["img"]
+    assert img.shape == (N, N)
+    assert rel(img, ref) < TOL_IMG, r.stdout
