@@ -26,6 +26,8 @@ EXPORTED = [
     "cgs_sense_trafo", "cgs_sense_adjoint_codeare", "cgs_sense_adjoint", "cgs_solve",
     "cgs_plan_info", "cgs_sync", "cgs_kernel_launches", "cgs_last_error",
     "cgs_profile_enable", "cgs_profile_collect", "cgs_nfft2d_trafo_noalloc",
+    "cgs_net_num_params", "cgs_net_create", "cgs_net_destroy", "cgs_net_set_weights", "cgs_net_get_weights",
+    "cgs_net_forward", "cgs_net_gradients", "cgs_net_train_step", "cgs_solve_fcg", "cgs_normal_apply",
 ]
 PROFILE_CATEGORIES = ("fft", "interp", "spread")
 
@@ -38,12 +40,12 @@ class PlanDesc(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("mode", C.c_int), ("cgiter", C.c_int), ("cgeps", C.c_double),
                 ("lam", C.c_double), ("ftiter", C.c_int), ("fteps", C.c_double),
-                ("weighted", C.c_int), ("toeplitz", C.c_int)]
+                ("weighted", C.c_int), ("toeplitz", C.c_int), ("jacobi", C.c_int)]
 
 
 class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int), ("res_first", C.c_double), ("res_last", C.c_double),
-                ("seconds", C.c_double), ("res_hist", C.c_double * 256)]
+                ("seconds", C.c_double), ("res_hist", C.c_double * 256), ("fallback_at", C.c_int)]
 
 
 class CgsError(RuntimeError):
@@ -86,9 +88,19 @@ def load(path: str = LIB_PATH):
     L.cgs_profile_collect.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     L.cgs_profile_collect.restype = None
     L.cgs_nfft2d_trafo_noalloc.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int64, vp, vp, vp, vp]
+    L.cgs_solve_fcg.argtypes = [vp, vp, vp, vp, C.POINTER(SolveOpts), vp, C.POINTER(SolveReport), vp]
+    L.cgs_normal_apply.argtypes = [vp, vp, vp, C.POINTER(SolveOpts), vp]
+    L.cgs_net_num_params.restype = C.c_int64
+    L.cgs_net_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int]
+    L.cgs_net_destroy.argtypes = [vp]
+    L.cgs_net_set_weights.argtypes = [vp, vp]
+    L.cgs_net_get_weights.argtypes = [vp, vp]
+    L.cgs_net_forward.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp]
+    L.cgs_net_gradients.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
+    L.cgs_net_train_step.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_float, vp, vp]
     for name in EXPORTED:
         if name not in ("cgs_kernel_launches", "cgs_last_error", "cgs_profile_enable",
-                        "cgs_profile_collect"):
+                        "cgs_profile_collect", "cgs_net_num_params"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -134,6 +146,13 @@ def profile_collect():
     cnt = (C.c_int64 * 3)()
     load().cgs_profile_collect(ms, cnt)
     return {PROFILE_CATEGORIES[i]: (ms[i], cnt[i]) for i in range(3)}
+
+
+def _report(rep):
+    n = rep.iterations
+    hist = [rep.res_hist[i] for i in range(min(256, n + 1))]
+    return dict(iterations=n, res_first=rep.res_first, res_last=rep.res_last, seconds=rep.seconds,
+                res_hist=hist, fallback_at=rep.fallback_at)
 
 
 class Plan:
@@ -210,7 +229,75 @@ class Plan:
                       int(bool(weighted)), int(bool(toeplitz)))
         rep = SolveReport()
         _check(load().cgs_solve(self._h, _ptr(y), _ptr(out), C.byref(o), C.byref(rep), _stream(stream)))
-        n = rep.iterations
-        hist = [rep.res_hist[i] for i in range(min(256, n + 1))]
-        return dict(iterations=n, res_first=rep.res_first, res_last=rep.res_last, seconds=rep.seconds,
-                    res_hist=hist)
+        return _report(rep)
+
+    def solve_fcg(self, out, y=None, rhs=None, net=None, cgiter=200, cgeps=1e-4, lam=0.0, weighted=True,
+                  toeplitz=True, jacobi=False, stream=None):
+        """flexible CG with the learned preconditioner `net`; without one, plain CG
+        or (jacobi=True) CG preconditioned by the exact diagonal of the normal
+        operator"""
+        o = SolveOpts(MODE_STANDARD, int(cgiter), float(cgeps), float(lam), 0, 0.0, int(bool(weighted)),
+                      int(bool(toeplitz)), int(bool(jacobi)))
+        rep = SolveReport()
+        _check(load().cgs_solve_fcg(self._h, None if y is None else _ptr(y), None if rhs is None else _ptr(rhs),
+                                    _ptr(out), C.byref(o), None if net is None else net._h, C.byref(rep),
+                                    _stream(stream)))
+        return _report(rep)
+
+    def normal_apply(self, x, out, lam=0.0, weighted=True, toeplitz=True, stream=None):
+        o = SolveOpts(MODE_STANDARD, 0, 0.0, float(lam), 0, 0.0, int(bool(weighted)), int(bool(toeplitz)))
+        _check(load().cgs_normal_apply(self._h, _ptr(x), _ptr(out), C.byref(o), _stream(stream)))
+        return out
+
+
+class Net:
+    """The learned preconditioner's CNN (2 -> 32 -> 32 -> 32 -> 32 -> 2, 3x3)."""
+
+    def __init__(self, max_batch=1, max_h=256, max_w=256):
+        L = load()
+        h = C.c_void_p()
+        _check(L.cgs_net_create(C.byref(h), int(max_batch), int(max_h), int(max_w)))
+        self._h = h
+        self.nparams = int(L.cgs_net_num_params())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().cgs_net_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def weights(self):
+        w = np.zeros(self.nparams, np.float32)
+        _check(load().cgs_net_get_weights(self._h, _ptr(w)))
+        return w
+
+    def set_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        _check(load().cgs_net_set_weights(self._h, _ptr(w)))
+
+    def forward(self, x, out=None, stream=None):
+        B, H, W, _ = x.shape
+        if out is None:
+            out = np.zeros_like(x) if isinstance(x, np.ndarray) else x.new_empty(x.shape)
+        _check(load().cgs_net_forward(self._h, _ptr(x), _ptr(out), B, H, W, _stream(stream)))
+        return out
+
+    def gradients(self, x, t, stream=None):
+        B, H, W, _ = x.shape
+        g = np.zeros(self.nparams, np.float32)
+        loss = np.zeros(1, np.float32)
+        _check(load().cgs_net_gradients(self._h, _ptr(x), _ptr(t), B, H, W, _ptr(g), _ptr(loss),
+                                        _stream(stream)))
+        return float(loss[0]), g
+
+    def train_step(self, x, t, lr=1e-3, stream=None, want_loss=True):
+        B, H, W, _ = x.shape
+        loss = np.zeros(1, np.float32)
+        _check(load().cgs_net_train_step(self._h, _ptr(x), _ptr(t), B, H, W, float(lr),
+                                         _ptr(loss) if want_loss else None, _stream(stream)))
+        return float(loss[0]) if want_loss else None

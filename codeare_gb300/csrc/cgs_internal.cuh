@@ -219,6 +219,30 @@ struct CGScalars {
     int nan_flag;
     double hist[256];    // residual measure per check
 };
+// Flexible CG (preconditioner may change per iteration): Polak-Ribiere beta,
+// fallback to plain CG when the residual stalls or <r, z> <= 0.
+struct FCGScalars {
+    CGScalars cg;        // lambda, done, iter, maxit, tol, hist, nan_flag
+    double rr, rr0, rz, pq, zr, zro, beta, best;
+    int stall, fallback, use_r, restart, fallback_at;
+    int mode;            // 0 plain, 1 Jacobi, 2 scaled network
+    double sumw, tt;     // sum of the density weights; |d . r|^2 for the net
+};
+cgs_status launch_fcg_kernels(int which, FCGScalars *fs, float2 *x, float2 *r, float2 *rold, float2 *p,
+                              const float2 *q, float2 *z, int64_t n, cudaGraphConditionalHandle h,
+                              cudaStream_t st);
+enum FcgOp { FCG_INIT = 0, FCG_UPDATE_XR = 1, FCG_DECIDE = 2, FCG_SELECT = 3, FCG_BETA = 4, FCG_P = 5, FCG_CHECK = 6 };
+// d[p] = 1/sqrt(sum_c |S[p][c]|^2 * sumw + lambda) from the coil-minor sensitivities
+cgs_status launch_jacobi_scale(const float2 *sens, int64_t P, int nc, const FCGScalars *fs, float *d,
+                               cudaStream_t st);
+// out = d^power . (in + add) (power 1 or 2; add may be null), the diagonal
+// scaling steps of the preconditioner
+cgs_status launch_diag_scale(const float2 *in, const float2 *add, const float *d, int power, int64_t n,
+                             float2 *out, cudaStream_t st);
+// z = M(r): the learned preconditioner on one complex image (cgs_cnn.cu);
+// nrm2 = sum |r|^2 on the device sets the input scale
+cgs_status net_apply_image(cgs_net *n, const float2 *r, const double *nrm2, int H, int W, float2 *z,
+                           cudaStream_t st);
 // Loop check (one thread): records the residual measure of the current
 // iterate, decides whether another update follows, and sets the conditional
 // handle of the enclosing while node accordingly.

@@ -188,6 +188,14 @@ struct cgs_plan {
     int *active = nullptr;
     CGScalars *sc = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // flexible CG state and graph
+    float2 *vB = nullptr, *vZ = nullptr, *vO = nullptr, *vT = nullptr;
+    float *dscale = nullptr;
+    FCGScalars *fs = nullptr;
+    cudaGraphExec_t fcg_exec = nullptr;
+    int fg_src = -1, fg_toep = -1, fg_weighted = -1, fg_mode = -1;
+    cgs_net *fg_net = nullptr;
+    int64_t fg_kpro = 0, fg_kbody = 0;
     // captured solve: prologue + while(iteration) as one CUDA graph
     cudaGraphExec_t solve_exec = nullptr;
     int sg_mode = -1, sg_toep = -1, sg_weighted = -1, sg_ftiter = -1;
@@ -722,6 +730,137 @@ cgs_status build_solve_graph(cgs_plan *p, const cgs_solve_opts *o, cudaStream_t 
     return CGS_OK;
 }
 
+// q = (E^H W E + lambda) p on the device buffers (lambda from the scalars)
+cgs_status op_normal(cgs_plan *p, const float2 *x, float2 *q, int toeplitz, int weighted, CGScalars *sc,
+                     cudaStream_t st)
+{
+    if (toeplitz) {
+        CGS_TRY(op_ehe_toeplitz(p, x, q, st));
+    } else {
+        CGS_TRY(op_forward(p, x, 0, nullptr, p->ksV, st));
+        CGS_TRY(op_eh(p, p->ksV, weighted, q, st));
+    }
+    return launch_add_scaled(q, x, sc, p->Nt, st);
+}
+
+cgs_status fcg_alloc(cgs_plan *p)
+{
+    if (!p->vB) CGS_TRY(dev_alloc(&p->vB, (size_t)p->Nt));
+    if (!p->vZ) CGS_TRY(dev_alloc(&p->vZ, (size_t)p->Nt));
+    if (!p->vO) CGS_TRY(dev_alloc(&p->vO, (size_t)p->Nt));
+    if (!p->vT) CGS_TRY(dev_alloc(&p->vT, (size_t)p->Nt));
+    if (!p->dscale) CGS_TRY(dev_alloc(&p->dscale, (size_t)p->Nt));
+    if (!p->fs) CGS_TRY(dev_alloc(&p->fs, 1));
+    return CGS_OK;
+}
+
+// z = M(r): mode 2 d . (t + net(t)) with t = d . r (the network corrects the
+// Jacobi step); mode 1 d^2 . r; mode 0 (or after the fallback) z = r
+cgs_status fcg_precondition(cgs_plan *p, cgs_net *net, int mode, cudaStream_t st)
+{
+    const int64_t Nt = p->Nt;
+    if (mode == 2) {
+        CGS_TRY(launch_diag_scale(p->vR, nullptr, p->dscale, 1, Nt, p->vT, st));
+        CGS_TRY(launch_coldot(p->vT, p->vT, nullptr, Nt, 1, p->partial, &p->fs->tt, st));
+        CGS_TRY(net_apply_image(net, p->vT, &p->fs->tt, p->N[0], p->N[1], p->vZ, st));
+        CGS_TRY(launch_diag_scale(p->vZ, p->vT, p->dscale, 1, Nt, p->vZ, st));
+    } else if (mode == 1) {
+        CGS_TRY(launch_diag_scale(p->vR, nullptr, p->dscale, 2, Nt, p->vZ, st));
+    }
+    return launch_fcg_kernels(FCG_SELECT, p->fs, p->vX, p->vR, p->vO, p->vP, p->vQ, p->vZ, Nt,
+                              cudaGraphConditionalHandle(), st);
+}
+
+// Capture flexible CG: prologue (b, r = b, x = 0, z = M(r), p = z) and a
+// while node over one iteration plus the device-side check.
+cgs_status build_fcg_graph(cgs_plan *p, int from_data, int toeplitz, int weighted, cgs_net *net, int mode,
+                           cudaStream_t st)
+{
+    if (p->fcg_exec) { cudaGraphExecDestroy(p->fcg_exec); p->fcg_exec = nullptr; }
+    const int64_t Nt = p->Nt;
+    FCGScalars *fs = p->fs;
+    auto K = [&](int which, cudaGraphConditionalHandle h) {
+        return launch_fcg_kernels(which, fs, p->vX, p->vR, p->vO, p->vP, p->vQ, p->vZ, Nt, h, st);
+    };
+    cudaGraph_t g = nullptr;
+    CGS_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    cgs_status r = CGS_OK;
+    if (cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) r = CGS_ERR_CUDA;
+    const int64_t c0 = cgs_kernel_launches();
+    std::vector<cudaGraphNode_t> frontier;
+    if (r == CGS_OK && cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+        r = CGS_ERR_CUDA;
+    if (r == CGS_OK) {
+        cgs_status q = CGS_OK;
+        if (from_data) q = op_eh(p, p->ksY, weighted, p->vR, st);
+        else if (cudaMemcpyAsync(p->vR, p->vB, sizeof(float2) * Nt, cudaMemcpyDeviceToDevice, st) != cudaSuccess) q = CGS_ERR_CUDA;
+        if (q == CGS_OK) q = launch_zero(p->vX, sizeof(float2) * Nt, st);
+        if (q == CGS_OK) q = launch_zero(p->vP, sizeof(float2) * Nt, st);
+        if (q == CGS_OK) q = launch_zero(p->vO, sizeof(float2) * Nt, st);
+        if (q == CGS_OK && mode != 0) q = launch_jacobi_scale(p->sens, Nt, p->nc, fs, p->dscale, st);
+        if (q == CGS_OK) q = launch_coldot(p->vR, p->vR, nullptr, Nt, 1, p->partial, &fs->rr, st);
+        if (q == CGS_OK) q = K(FCG_INIT, h);
+        if (q == CGS_OK) q = fcg_precondition(p, net, mode, st);
+        if (q == CGS_OK) q = launch_coldot(p->vZ, p->vR, nullptr, Nt, 1, p->partial, &fs->zr, st);
+        if (q == CGS_OK) q = K(FCG_BETA, h);
+        if (q == CGS_OK) q = K(FCG_P, h);
+        if (q == CGS_OK) q = K(FCG_CHECK, h);
+        if (q == CGS_OK) {
+            cudaStreamCaptureStatus cs;
+            const cudaGraphNode_t *deps = nullptr;
+            size_t nd = 0;
+            if (cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd) != cudaSuccess) q = CGS_ERR_CUDA;
+            else frontier.assign(deps, deps + nd);
+        }
+        cudaGraph_t gg = g;
+        if (cudaStreamEndCapture(st, &gg) != cudaSuccess && q == CGS_OK) q = CGS_ERR_CUDA;
+        r = q;
+    }
+    p->fg_kpro = cgs_kernel_launches() - c0;
+    cudaGraph_t body = nullptr;
+    if (r == CGS_OK) {
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cond;
+        if (cudaGraphAddNode(&cond, g, frontier.data(), nullptr, frontier.size(), &cp) != cudaSuccess) r = CGS_ERR_CUDA;
+        else body = cp.conditional.phGraph_out[0];
+    }
+    const int64_t c1 = cgs_kernel_launches();
+    if (r == CGS_OK && cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+        r = CGS_ERR_CUDA;
+    if (r == CGS_OK) {
+        cgs_status q = op_normal(p, p->vP, p->vQ, toeplitz, weighted, &fs->cg, st);
+        if (q == CGS_OK) q = launch_coldot(p->vP, p->vQ, nullptr, Nt, 1, p->partial, &fs->pq, st);
+        if (q == CGS_OK) q = K(FCG_UPDATE_XR, h);
+        if (q == CGS_OK) q = launch_coldot(p->vR, p->vR, nullptr, Nt, 1, p->partial, &fs->rr, st);
+        if (q == CGS_OK) q = K(FCG_DECIDE, h);
+        if (q == CGS_OK) q = fcg_precondition(p, net, mode, st);
+        if (q == CGS_OK) q = launch_coldot(p->vZ, p->vR, nullptr, Nt, 1, p->partial, &fs->zr, st);
+        if (q == CGS_OK) q = launch_coldot(p->vZ, p->vO, nullptr, Nt, 1, p->partial, &fs->zro, st);
+        if (q == CGS_OK) q = K(FCG_BETA, h);
+        if (q == CGS_OK) q = K(FCG_P, h);
+        if (q == CGS_OK) q = K(FCG_CHECK, h);
+        cudaGraph_t bb = body;
+        if (cudaStreamEndCapture(st, &bb) != cudaSuccess && q == CGS_OK) q = CGS_ERR_CUDA;
+        r = q;
+    }
+    p->fg_kbody = cgs_kernel_launches() - c1;
+    count_launch((int)-(cgs_kernel_launches() - c0));
+    if (r == CGS_OK && cudaGraphInstantiate(&p->fcg_exec, g, 0) != cudaSuccess) {
+        set_error("cudaGraphInstantiate of the flexible-CG graph failed");
+        r = CGS_ERR_CUDA;
+    }
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (r != CGS_OK) { p->fcg_exec = nullptr; return r; }
+    p->fg_src = from_data; p->fg_toep = toeplitz; p->fg_weighted = weighted; p->fg_net = net; p->fg_mode = mode;
+    return CGS_OK;
+}
+
 cgs_status check_ready(cgs_plan *p, bool need_w, bool need_s)
 {
     if (!p) { set_error("null plan"); return CGS_ERR_BAD_ARG; }
@@ -894,6 +1033,9 @@ cgs_status cgs_plan_destroy(cgs_plan *p)
     for (void *b : {(void *)p->tw2[0], (void *)p->tw2[1], (void *)p->tw2[2], (void *)p->toepK, (void *)p->tA,
                     (void *)p->tB}) dev_free(b);
     if (p->solve_exec) cudaGraphExecDestroy(p->solve_exec);
+    if (p->fcg_exec) cudaGraphExecDestroy(p->fcg_exec);
+    for (void *b : {(void *)p->vB, (void *)p->vZ, (void *)p->vO, (void *)p->vT, (void *)p->dscale, (void *)p->fs})
+        dev_free(b);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -1157,7 +1299,7 @@ cgs_status cgs_solve(cgs_plan *p, const float *y, float *x, const cgs_solve_opts
     if (!x || !y || o->cgiter < 0 || o->ftiter < 0) { set_error("bad argument"); return CGS_ERR_BAD_ARG; }
     cudaStream_t st = pick_stream(p, stream);
     const int64_t Nt = p->Nt;
-    if (rep) std::memset(rep, 0, sizeof(*rep));
+    if (rep) { std::memset(rep, 0, sizeof(*rep)); rep->fallback_at = -1; }
     if (!codeare && o->toeplitz) {
         const int wtd = (o->weighted && p->have_w) ? 1 : 0;
         if (!p->toep_valid || p->toep_weighted != wtd) CGS_TRY(build_toeplitz(p, wtd, st));
@@ -1209,6 +1351,90 @@ cgs_status cgs_solve(cgs_plan *p, const float *y, float *x, const cgs_solve_opts
         rep->iterations = iters;
     }
     return result;
+}
+
+cgs_status cgs_normal_apply(cgs_plan *p, const float *x, float *out, const cgs_solve_opts *o, void *stream)
+{
+    if (!o) { set_error("null options"); return CGS_ERR_BAD_ARG; }
+    CGS_TRY(check_ready(p, o->weighted != 0, true));
+    if (!x || !out) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    cudaStream_t st = pick_stream(p, stream);
+    if (o->toeplitz) {
+        const int wtd = (o->weighted && p->have_w) ? 1 : 0;
+        if (!p->toep_valid || p->toep_weighted != wtd) CGS_TRY(build_toeplitz(p, wtd, st));
+    }
+    CGScalars init{};
+    init.lambda = o->lambda;
+    CGS_CUDA(cudaMemcpyAsync(p->sc, &init, sizeof(init), cudaMemcpyHostToDevice, st));
+    const void *src;
+    CGS_TRY(stage_in(x, sizeof(float2) * p->Nt, p->ioA, &src, st));
+    CGS_TRY(fcg_alloc(p));
+    CGS_CUDA(cudaMemcpyAsync(p->vZ, src, sizeof(float2) * p->Nt, cudaMemcpyDeviceToDevice, st));
+    CGS_TRY(op_normal(p, p->vZ, p->vQ, o->toeplitz, o->weighted, p->sc, st));
+    return image_out(p, p->vQ, out, st);
+}
+
+cgs_status cgs_solve_fcg(cgs_plan *p, const float *y, const float *rhs, float *x, const cgs_solve_opts *o,
+                         cgs_net *net, cgs_solve_report *rep, void *stream)
+{
+    if (!o) { set_error("null options"); return CGS_ERR_BAD_ARG; }
+    CGS_TRY(check_ready(p, o->weighted != 0, true));
+    if (!x || (!y && !rhs) || o->cgiter < 0) { set_error("bad argument"); return CGS_ERR_BAD_ARG; }
+    if (p->d != 2) { set_error("the learned preconditioner is 2-D"); return CGS_ERR_BAD_ARG; }
+    cudaStream_t st = pick_stream(p, stream);
+    if (rep) std::memset(rep, 0, sizeof(*rep));
+    CGS_TRY(fcg_alloc(p));
+    if (o->toeplitz) {
+        const int wtd = (o->weighted && p->have_w) ? 1 : 0;
+        if (!p->toep_valid || p->toep_weighted != wtd) CGS_TRY(build_toeplitz(p, wtd, st));
+    }
+    const int from_data = y ? 1 : 0;
+    if (from_data) {
+        CGS_TRY(ks_in(p, y, st));
+    } else {
+        const void *src;
+        CGS_TRY(stage_in(rhs, sizeof(float2) * p->Nt, p->ioA, &src, st));
+        CGS_CUDA(cudaMemcpyAsync(p->vB, src, sizeof(float2) * p->Nt, cudaMemcpyDeviceToDevice, st));
+    }
+    const int mode = net ? 2 : (o->jacobi ? 1 : 0);
+    const bool same = p->fcg_exec && p->fg_src == from_data && p->fg_toep == o->toeplitz &&
+                      p->fg_weighted == o->weighted && p->fg_net == net && p->fg_mode == mode;
+    if (!same) CGS_TRY(build_fcg_graph(p, from_data, o->toeplitz, o->weighted, net, mode, st));
+    double sumw = (double)p->M;
+    if (o->weighted && p->have_w) {
+        sumw = 0.0;
+        for (float v : p->w_host) sumw += (double)v;
+    }
+    FCGScalars init{};
+    init.cg.lambda = o->lambda;
+    init.cg.tol = o->cgeps;
+    init.cg.maxit = o->cgiter;
+    init.cg.sqrt_mode = 1;
+    init.fallback = 0;
+    init.mode = mode;
+    init.sumw = sumw;
+    CGS_CUDA(cudaEventRecord(p->ev0, st));
+    CGS_CUDA(cudaMemcpyAsync(p->fs, &init, sizeof(init), cudaMemcpyHostToDevice, st));
+    CGS_CUDA(cudaGraphLaunch(p->fcg_exec, st));
+    CGS_CUDA(cudaEventRecord(p->ev1, st));
+    FCGScalars h;
+    CGS_CUDA(cudaMemcpyAsync(&h, p->fs, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CGS_CUDA(cudaStreamSynchronize(st));
+    count_launch((int)(p->fg_kpro + (int64_t)h.cg.iter * p->fg_kbody));
+    if (rep) {
+        const int nh = std::min(256, h.cg.iter + 1);
+        for (int i = 0; i < nh; ++i) rep->res_hist[i] = h.cg.hist[i];
+        rep->iterations = h.cg.iter;
+        rep->res_first = h.cg.hist[0];
+        rep->res_last = h.rr0 > 0 ? std::sqrt(h.rr / h.rr0) : 0.0;
+        if (h.cg.iter < 256) rep->res_hist[h.cg.iter] = rep->res_last;
+        rep->fallback_at = (net && h.fallback) ? h.fallback_at : -1;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+        rep->seconds = ms * 1e-3;
+    }
+    CGS_TRY(image_out(p, p->vX, x, st));
+    return h.cg.nan_flag ? CGS_ERR_NAN : CGS_OK;
 }
 
 }  // extern "C"

@@ -233,6 +233,103 @@ __global__ void cg_check_kernel(CGScalars *sc, cudaGraphConditionalHandle h)
     cudaGraphSetConditional(h, go);
 }
 
+// ---- flexible CG ----------------------------------------------------------
+__global__ void fcg_init_kernel(FCGScalars *fs)
+{
+    fs->rr0 = fs->rr;
+    fs->best = fs->rr;
+    fs->stall = 0;
+    fs->restart = 1;
+    fs->use_r = 0;
+    fs->fallback_at = -1;
+}
+
+// alpha = rz / pq; x += alpha p; rold = r; r -= alpha q
+__global__ void fcg_update_xr_kernel(FCGScalars *fs, float2 *__restrict__ x, float2 *__restrict__ r,
+                                     float2 *__restrict__ rold, const float2 *__restrict__ p,
+                                     const float2 *__restrict__ q, int64_t n)
+{
+    const float a = (float)(fs->rz / fs->pq);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const float2 pv = p[e], qv = q[e], rv = r[e];
+        float2 xv = x[e];
+        xv.x = fmaf(a, pv.x, xv.x); xv.y = fmaf(a, pv.y, xv.y);
+        x[e] = xv;
+        rold[e] = rv;
+        r[e] = make_float2(fmaf(-a, qv.x, rv.x), fmaf(-a, qv.y, rv.y));
+    }
+}
+
+// stall bookkeeping on the new residual (network mode only): kStallChecks
+// checks without a new best residual switch to plain CG (restarted)
+constexpr int kStallChecks = 6;
+__global__ void fcg_decide_kernel(FCGScalars *fs)
+{
+    if (fs->rr < fs->best) { fs->best = fs->rr; fs->stall = 0; }
+    else fs->stall += 1;
+    if (fs->mode == 2 && !fs->fallback && fs->stall >= kStallChecks) {
+        fs->fallback = 1;
+        fs->restart = 1;
+        fs->fallback_at = fs->cg.iter;
+    }
+}
+
+__global__ void fcg_select_kernel(const FCGScalars *fs, float2 *__restrict__ z, const float2 *__restrict__ r, int64_t n)
+{
+    if (!fs->fallback && fs->mode != 0) return;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) z[e] = r[e];
+}
+
+__global__ void fcg_beta_kernel(FCGScalars *fs)
+{
+    if (fs->mode == 2 && !fs->fallback && !(fs->zr > 0.0)) {   // the network gave no descent direction
+        fs->fallback = 1;
+        fs->restart = 1;
+        fs->use_r = 1;
+        fs->fallback_at = fs->cg.iter;
+    }
+    const double zr = fs->use_r ? fs->rr : fs->zr;
+    if (fs->restart) { fs->beta = 0.0; fs->restart = 0; }
+    else fs->beta = (fs->zr - fs->zro) / fs->rz;
+    fs->rz = zr;
+}
+
+// p = (use_r ? r : z) + beta p
+__global__ void fcg_p_kernel(const FCGScalars *fs, float2 *__restrict__ p, const float2 *__restrict__ z,
+                             const float2 *__restrict__ r, int64_t n)
+{
+    const float b = (float)fs->beta;
+    const float2 *src = fs->use_r ? r : z;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const float2 s = src[e];
+        float2 pv = p[e];
+        p[e] = make_float2(fmaf(b, pv.x, s.x), fmaf(b, pv.y, s.y));
+    }
+}
+
+// residual check ||r|| / ||r0|| as the plain standard-mode loop
+__global__ void fcg_check_kernel(FCGScalars *fs, cudaGraphConditionalHandle h)
+{
+    CGScalars *sc = &fs->cg;
+    unsigned int go = 0;
+    fs->use_r = 0;
+    if (!sc->done) {
+        if (sc->iter >= sc->maxit) {
+            sc->done = 1;
+        } else if (fs->rr0 == 0.0) {
+            if (sc->iter < 256) sc->hist[sc->iter] = 0.0;
+            sc->done = 1;
+        } else {
+            const double res = sqrt(fs->rr / fs->rr0);
+            if (sc->iter < 256) sc->hist[sc->iter] = res;
+            if (isnan(res)) { sc->nan_flag = 1; sc->done = 1; }
+            else if (res <= sc->tol) { sc->done = 1; }
+            else { sc->iter += 1; go = 1; }
+        }
+    }
+    cudaGraphSetConditional(h, go);
+}
+
 // op 0: rn = xn = *src; 1: pq = *src; 2: rno = rn, rn = *src
 __global__ void scalar_op_kernel(CGScalars *sc, const double *src, int op)
 {
@@ -401,6 +498,66 @@ cgs_status launch_cg_update_p(float2 *p, const float2 *r, const CGScalars *sc, i
 cgs_status launch_scalar_op(CGScalars *sc, const double *src, int op, cudaStream_t st)
 {
     scalar_op_kernel<<<1, 1, 0, st>>>(sc, src, op);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+__global__ void jacobi_scale_kernel(const float2 *__restrict__ S, int64_t P, int nc, const FCGScalars *fs,
+                                    float *__restrict__ d)
+{
+    const double sw = fs->sumw, lam = fs->cg.lambda;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int c = 0; c < nc; ++c) {
+            const float2 v = S[p * nc + c];
+            s += (double)v.x * v.x + (double)v.y * v.y;
+        }
+        const double D = s * sw + lam;
+        d[p] = D > 0.0 ? (float)(1.0 / sqrt(D)) : 0.f;
+    }
+}
+
+__global__ void diag_scale_kernel(const float2 *in, const float2 *add, const float *__restrict__ d, int power,
+                                  int64_t n, float2 *out)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        float f = d[e];
+        if (power == 2) f *= f;
+        float2 v = in[e];
+        if (add) { const float2 a = add[e]; v.x += a.x; v.y += a.y; }
+        out[e] = make_float2(v.x * f, v.y * f);
+    }
+}
+
+cgs_status launch_jacobi_scale(const float2 *sens, int64_t P, int nc, const FCGScalars *fs, float *d,
+                               cudaStream_t st)
+{
+    jacobi_scale_kernel<<<grid_for(P), kThreads, 0, st>>>(sens, P, nc, fs, d);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_diag_scale(const float2 *in, const float2 *add, const float *d, int power, int64_t n,
+                             float2 *out, cudaStream_t st)
+{
+    diag_scale_kernel<<<grid_for(n), kThreads, 0, st>>>(in, add, d, power, n, out);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_fcg_kernels(int which, FCGScalars *fs, float2 *x, float2 *r, float2 *rold, float2 *p,
+                              const float2 *q, float2 *z, int64_t n, cudaGraphConditionalHandle h,
+                              cudaStream_t st)
+{
+    switch (which) {
+        case FCG_INIT: fcg_init_kernel<<<1, 1, 0, st>>>(fs); break;
+        case FCG_UPDATE_XR: fcg_update_xr_kernel<<<grid_for(n), kThreads, 0, st>>>(fs, x, r, rold, p, q, n); break;
+        case FCG_DECIDE: fcg_decide_kernel<<<1, 1, 0, st>>>(fs); break;
+        case FCG_SELECT: fcg_select_kernel<<<grid_for(n), kThreads, 0, st>>>(fs, z, r, n); break;
+        case FCG_BETA: fcg_beta_kernel<<<1, 1, 0, st>>>(fs); break;
+        case FCG_P: fcg_p_kernel<<<grid_for(n), kThreads, 0, st>>>(fs, p, z, r, n); break;
+        default: fcg_check_kernel<<<1, 1, 0, st>>>(fs, h); break;
+    }
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }

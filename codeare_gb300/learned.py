@@ -1,0 +1,187 @@
+"""Learned preconditioner for flexible CG-SENSE (configuration 4 workload).
+
+Problem family: 2-D radial, 256^2 image, 16 coils, golden-angle radial with
+32-100 spokes of 512 samples, random phantoms of 8-20 ellipses with uniform
+complex intensities.  The normal equations are the standard-mode ones,
+(E^H W E + lambda I) x = E^H W y, applied by Toeplitz embedding.
+
+Training pairs (residual r, correction e): r is a plain-CG residual
+b - A x_k at a random iteration k of a random problem, e = CG_20(A, r) is the
+20-iteration plain-CG solution of A e = r from zero.  The preconditioner is
+z = d . (t + net(t)), t = d . r, with d = diag(A)^-1/2 (exact: sum_c |S_c|^2
+sum_j w_j + lambda): the network corrects the Jacobi step on the unit-diagonal
+system d A d, so its pairs are (t, e / d - t), both divided by the RMS of t (the network is positively
+homogeneous, so the scale is exact) and stored as [H][W][2] float.  The
+network is include/cgs.h's cgs_net_*; cgs_solve_fcg applies the scaling.
+
+All compute runs in libcgs.so; torch only holds device buffers and slices
+random training crops.
+"""
+from __future__ import annotations
+
+import math
+import os
+import struct
+
+import numpy as np
+
+from . import capi, synth
+
+WEIGHTS_MAGIC = b"CGSN"
+
+
+def ellipse_phantom(n: int, rng) -> np.ndarray:
+    """8-20 random ellipses with uniform complex intensities (|v| <= 1)."""
+    img = np.zeros((n, n), np.complex64)
+    yy, xx = np.meshgrid((np.arange(n) - n / 2) / (n / 2), (np.arange(n) - n / 2) / (n / 2), indexing="ij")
+    for _ in range(int(rng.integers(8, 21))):
+        a, b = rng.uniform(0.05, 0.6, 2)
+        cy, cx = rng.uniform(-0.6, 0.6, 2)
+        th = rng.uniform(0, math.pi)
+        v = complex(rng.uniform(-1, 1), rng.uniform(-1, 1))
+        xr = (xx - cx) * math.cos(th) + (yy - cy) * math.sin(th)
+        yr = -(xx - cx) * math.sin(th) + (yy - cy) * math.cos(th)
+        img[(xr / a) ** 2 + (yr / b) ** 2 <= 1.0] += v
+    return img
+
+
+def density(k):
+    """ramp density compensation with a floor so the k-space centre keeps weight"""
+    w = synth.ramp_weights(k)
+    return (w + 0.5 / 512.0).astype(np.float32)
+
+
+class Problem:
+    """One configuration-4 instance on the GPU (plan, data, normal-equation rhs)."""
+
+    def __init__(self, seed: int, N: int = 256, nc: int = 16, nsamp: int = 512, spokes=None,
+                 sens=None, lam_rel: float = 1e-3, noise: float = 1e-3):
+        import torch
+        rng = np.random.default_rng(seed)
+        self.N, self.nc = N, nc
+        self.spokes = int(spokes if spokes is not None else rng.integers(32, 101))
+        self.k = synth.radial2d(self.spokes, nsamp, golden=True)
+        self.w = density(self.k)
+        self.S = sens if sens is not None else synth.coils2d(N, nc)
+        self.x_true = ellipse_phantom(N, rng)
+        M = self.k.shape[0]
+        self.plan = capi.Plan((N, N), M, ncoils=nc, m=4, alpha=2.0)
+        self.plan.set_kspace(self.k)
+        self.plan.set_weights(self.w)
+        self.plan.set_sensitivities(np.ascontiguousarray(self.S))
+        y = np.zeros((nc, M), np.complex64)
+        self.plan.sense_trafo(self.x_true, y)
+        self.y = synth.add_noise(y, noise, seed=seed + 7)
+        # Tikhonov weight relative to the mean diagonal of E^H W E
+        diag = float(np.sum(self.w)) * float(np.mean(np.sum(np.abs(self.S) ** 2, axis=0)))
+        self.diag = diag
+        self.lam = lam_rel * diag
+        ssq = np.sum(np.abs(self.S) ** 2, axis=0)
+        self.d = torch.from_numpy((1.0 / np.sqrt(ssq * float(np.sum(self.w, dtype=np.float64)) + self.lam))
+                                  .astype(np.float32)).cuda()
+        self.y_d = torch.from_numpy(self.y).cuda()
+        b = torch.zeros((N, N), dtype=torch.complex64, device="cuda")
+        self.plan.sense_adjoint(self.y_d, b, weighted=True)
+        self.b = b
+
+    def solve(self, x, rhs=None, net=None, cgiter=500, cgeps=1e-4, jacobi=False):
+        return self.plan.solve_fcg(x, rhs=self.b if rhs is None else rhs, net=net, cgiter=cgiter, cgeps=cgeps,
+                                   lam=self.lam, weighted=True, toeplitz=True, jacobi=jacobi)
+
+    def apply(self, x, out):
+        return self.plan.normal_apply(x, out, lam=self.lam, weighted=True, toeplitz=True)
+
+    def close(self):
+        self.plan.close()
+
+
+def as_channels(z):
+    """complex [H][W] tensor -> float [H][W][2]"""
+    import torch
+    return torch.view_as_real(z).contiguous()
+
+
+def generate_pairs(n_pairs: int, seed: int = 20261207, per_problem: int = 8, N: int = 256, nc: int = 16,
+                   k_max: int = 60, corr_iters: int = 20, log=None):
+    """(t = d . residual, correction / d - t) pairs on the GPU, each divided by the
+    RMS of t."""
+    import torch
+    X = torch.empty((n_pairs, N, N, 2), dtype=torch.float32, device="cuda")
+    T = torch.empty_like(X)
+    rng = np.random.default_rng(seed)
+    S = synth.coils2d(N, nc)
+    i = 0
+    prob_id = 0
+    while i < n_pairs:
+        pr = Problem(seed + 1000 * prob_id, N=N, nc=nc, sens=S)
+        prob_id += 1
+        x = torch.zeros((N, N), dtype=torch.complex64, device="cuda")
+        Ax = torch.zeros_like(x)
+        e = torch.zeros_like(x)
+        for _ in range(per_problem):
+            if i >= n_pairs:
+                break
+            kk = int(rng.integers(0, k_max + 1))
+            if kk == 0:
+                r = pr.b.clone()
+            else:
+                pr.solve(x, cgiter=kk, cgeps=0.0)
+                pr.apply(x, Ax)
+                r = pr.b - Ax
+            pr.solve(e, rhs=r.contiguous(), cgiter=corr_iters, cgeps=0.0)
+            rs = r * pr.d
+            s = torch.sqrt(torch.mean(torch.view_as_real(rs) ** 2)).clamp_min(1e-30)
+            X[i] = as_channels(rs / s)
+            T[i] = as_channels((e / pr.d - rs) / s)
+            i += 1
+        pr.close()
+        if log and prob_id % 16 == 0:
+            log("pairs %d / %d" % (i, n_pairs))
+    return X, T
+
+
+def train(net, X, T, steps: int = 2000, batch: int = 32, crop: int = 64, lr: float = 1e-3, seed: int = 3,
+          log=None):
+    """Adam on random crops; returns the loss history."""
+    import torch
+    P, N = X.shape[0], X.shape[1]
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    xb = torch.empty((batch, crop, crop, 2), dtype=torch.float32, device="cuda")
+    tb = torch.empty_like(xb)
+    hist = []
+    for it in range(steps):
+        idx = torch.randint(0, P, (batch,), generator=g)
+        oy = torch.randint(0, N - crop + 1, (batch,), generator=g)
+        ox = torch.randint(0, N - crop + 1, (batch,), generator=g)
+        for b in range(batch):
+            xb[b] = X[idx[b], oy[b]:oy[b] + crop, ox[b]:ox[b] + crop]
+            tb[b] = T[idx[b], oy[b]:oy[b] + crop, ox[b]:ox[b] + crop]
+        step_lr = lr * (0.5 * (1 + math.cos(math.pi * it / steps)))
+        want = (it % 50 == 0) or it == steps - 1
+        loss = net.train_step(xb, tb, lr=step_lr, want_loss=want)
+        if want:
+            hist.append((it, loss))
+            if log:
+                log("step %d loss %.4e" % (it, loss))
+    return hist
+
+
+def save_weights(path: str, w: np.ndarray, meta: str = ""):
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    mb = meta.encode()
+    with open(path, "wb") as f:
+        f.write(WEIGHTS_MAGIC)
+        f.write(struct.pack("<II", w.size, len(mb)))
+        f.write(mb)
+        f.write(w.tobytes())
+
+
+def load_weights(path: str) -> np.ndarray:
+    with open(path, "rb") as f:
+        assert f.read(4) == WEIGHTS_MAGIC
+        n, lm = struct.unpack("<II", f.read(8))
+        f.read(lm)
+        return np.frombuffer(f.read(4 * n), dtype=np.float32).copy()
+
+
+WEIGHTS_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "precond_weights.bin")

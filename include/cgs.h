@@ -124,6 +124,9 @@ typedef struct {
                           (2N-grid FFT convolution with the weighted point-spread
                           function, computed once per trajectory and weights);
                           no reference counterpart                            */
+    int jacobi;        /* cgs_solve_fcg without a net: precondition with the exact
+                          diagonal D of E^H W E + lambda (D^-1 r); no reference
+                          counterpart                                        */
 } cgs_solve_opts;
 
 typedef struct {
@@ -132,6 +135,8 @@ typedef struct {
     double res_last;       /* residual measure at exit                       */
     double seconds;        /* device time of the solve                       */
     double res_hist[256];  /* residual measure per check, up to 256          */
+    int fallback_at;       /* flexible CG: iteration at which it fell back to
+                              plain CG, -1 if it never did                   */
 } cgs_solve_report;
 
 /* Full CG-SENSE solve (signals -> image).  CGS_MODE_CODEARE replaces
@@ -140,6 +145,48 @@ typedef struct {
  * (src/modules/CGSENSE.cpp:165-179).  `report` may be NULL. */
 cgs_status cgs_solve(cgs_plan *plan, const float *y, float *x, const cgs_solve_opts *opts,
                      cgs_solve_report *report, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Learned preconditioner (no reference counterpart): a 5-layer 3x3 CNN on a
+ * complex image held as 2 real channels, 2 -> 32 -> 32 -> 32 -> 32 -> 2, ReLU
+ * between layers, no biases (so M(c r) = c M(r) for c > 0), BF16 weights and
+ * activations with FP32 accumulation.  Tensors are [B][H][W][2] float
+ * (channel 0 real, 1 imaginary); weights are cgs_net_num_params() floats,
+ * layer after layer, each [9 taps][Cout][Cin], tap = 3*dy + dx for the
+ * offset (dy-1, dx-1).
+ * ------------------------------------------------------------------------- */
+typedef struct cgs_net cgs_net;
+int64_t cgs_net_num_params(void);
+cgs_status cgs_net_create(cgs_net **net, int max_batch, int max_h, int max_w);
+cgs_status cgs_net_destroy(cgs_net *net);
+cgs_status cgs_net_set_weights(cgs_net *net, const float *w);
+cgs_status cgs_net_get_weights(cgs_net *net, float *w);
+cgs_status cgs_net_forward(cgs_net *net, const float *x, float *y, int B, int H, int W, void *stream);
+/* mean-squared-error gradients w.r.t. all weights (for checks) */
+cgs_status cgs_net_gradients(cgs_net *net, const float *x, const float *target, int B, int H, int W,
+                             float *grad, float *loss, void *stream);
+/* one Adam step on the mean-squared error between net(x) and target */
+cgs_status cgs_net_train_step(cgs_net *net, const float *x, const float *target, int B, int H, int W,
+                              float lr, float *loss, void *stream);
+
+/* Flexible CG-SENSE with the learned preconditioner (no reference
+ * counterpart): standard-mode normal equations (E^H W E + lambda) x = b with
+ * z = d . net(d . r) as a variable preconditioner, d = D^-1/2 the exact
+ * diagonal scaling (D = sum_c |S_c|^2 sum_j w_j + lambda, so the network
+ * works on the unit-diagonal system), Polak-Ribiere beta, and a fallback
+ * to plain CG (restarted) once the residual stalls for three iterations or the
+ * network gives <r, z> <= 0.  Stops at ||r||/||r0|| <= cgeps.  The right-hand
+ * side is b = E^H W y from k-space data y, or the image `rhs` when y is NULL.
+ * net == NULL runs the same loop as plain CG (Polak-Ribiere beta), or Jacobi
+ * preconditioned CG when opts->jacobi is set.  The plan's
+ * image must be 2-D and fit the net's maximum image size. */
+cgs_status cgs_solve_fcg(cgs_plan *plan, const float *y, const float *rhs, float *x,
+                         const cgs_solve_opts *opts, cgs_net *net, cgs_solve_report *report,
+                         void *stream);
+
+/* out = (E^H W E + lambda) x for an image x (Toeplitz or NFFT pair as opts say). */
+cgs_status cgs_normal_apply(cgs_plan *plan, const float *x, float *out, const cgs_solve_opts *opts,
+                            void *stream);
 
 /* Sizes of the plan (for host wrappers). */
 cgs_status cgs_plan_info(const cgs_plan *plan, int *rank, int *N, int *n, int64_t *M,

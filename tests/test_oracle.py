@@ -168,3 +168,19 @@ def test_golden_3d(oracle):
     P.set_x(g["k"])
     assert rel(P.trafo(g["fh"][0]), g["trafo"][0]) < 1e-12
     assert rel(P.adjoint(g["ys"][1]), g["adjoint"][1]) < 1e-12
+
+
+def test_cnn_oracle_gradients_match_finite_differences():
+    from oracle import cnn
+    rng = np.random.default_rng(0)
+    w = rng.standard_normal(28800) * 0.1
+    x = rng.standard_normal((1, 6, 7, 2))
+    t = rng.standard_normal((1, 6, 7, 2))
+    _, g = cnn.gradients(w, x, t)
+    eps = 1e-6
+    for i in [5, 700, 10000, 20000, 28500]:
+        wp, wm = w.copy(), w.copy()
+        wp[i] += eps
+        wm[i] -= eps
+        fd = (cnn.gradients(wp, x, t)[0] - cnn.gradients(wm, x, t)[0]) / (2 * eps)
+        assert abs(fd - g[i]) < 1e-6 * max(1.0, abs(g[i])) + 1e-9
