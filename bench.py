@@ -229,6 +229,23 @@ def cgsense_section(cpu_too: bool):
     return out
 
 
+def learned_section():
+    """Config 4: learned-preconditioned flexible CG against plain GPU CG (and
+    Jacobi CG) to relative residual 1e-4 on a held-out 256^2, 16-coil
+    golden-angle problem, with each image's error against the converged plain
+    solve.  Uses the committed trained weights; null when they are absent."""
+    from codeare_gb300 import learned
+    net = learned.load_net()
+    if net is None:
+        return None
+    r = learned.compare(net, seed=777)
+    net.close()
+    r["workload"] = ("config 4: 256^2, 16 coils, golden-angle radial x 512, random-ellipse phantom, "
+                     "Toeplitz E^H W E, lambda = 1e-3 mean diagonal, to ||r||/||r0|| = 1e-4")
+    r["speedup_vs_plain"] = r["plain"]["ms"] / r["learned"]["ms"]
+    return r
+
+
 def run_ours(args):
     import torch
     import codeare_gb300 as cg
@@ -374,8 +391,10 @@ def run_ours(args):
 
     plan.close()
     cgs_part = None
+    learned_part = None
     if rank == 0 and not args.no_cgsense:
         cgs_part = cgsense_section(cpu_too=(ws == 1 and not args.no_cpu))
+        learned_part = learned_section()
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -386,7 +405,7 @@ def run_ours(args):
                        "l2": "flushed before every timed step (512 MiB write, untimed)",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "roofline": roofline, "kernels": per_kernel, "cpu_baseline": cpu, "e2e": e2e,
-            "clocks": clk, "gpu_launches": launches, "cgsense": cgs_part,
+            "clocks": clk, "gpu_launches": launches, "cgsense": cgs_part, "learned_fcg": learned_part,
         }
         print(json.dumps(line))
     if ws > 1:
@@ -402,7 +421,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--no-cgsense", action="store_true", help="skip the config-0 CG-SENSE section")
+    ap.add_argument("--no-cgsense", action="store_true", help="skip the config-0 and config-4 CG-SENSE sections")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -185,3 +185,73 @@ def load_weights(path: str) -> np.ndarray:
 
 
 WEIGHTS_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "precond_weights.bin")
+
+
+def load_net(path: str = WEIGHTS_FILE):
+    """the trained network from `path`, or None when there is no weights file"""
+    if not os.path.exists(path):
+        return None
+    net = capi.Net(max_batch=1, max_h=256, max_w=256)
+    net.set_weights(load_weights(path))
+    return net
+
+
+def compare(net, seed: int, cgeps: float = 1e-4, ref_eps: float = 1e-6, repeats: int = 2):
+    """Plain CG, Jacobi-preconditioned CG and learned flexible CG on one held-out
+    problem to relative residual `cgeps` (the second of `repeats` timed solves
+    is kept: the first builds the solve graph), each image's relative L2 error
+    against the plain solve converged to `ref_eps`."""
+    import torch
+    pr = Problem(seed)
+    N = pr.N
+    ref = torch.zeros((N, N), dtype=torch.complex64, device="cuda")
+    pr.solve(ref, cgiter=2000, cgeps=ref_eps)
+    out = {"seed": seed, "spokes": pr.spokes}
+    arms = [("plain", {}), ("jacobi", {"jacobi": True})]
+    if net is not None:
+        arms.append(("learned", {"net": net}))
+    for name, kw in arms:
+        x = torch.zeros_like(ref)
+        for _ in range(repeats):
+            rep = pr.solve(x, cgiter=2000, cgeps=cgeps, **kw)
+        err = float(torch.linalg.vector_norm(x - ref) / torch.linalg.vector_norm(ref))
+        out[name] = {"iterations": rep["iterations"], "ms": 1e3 * rep["seconds"], "res": rep["res_last"],
+                     "fallback_at": rep["fallback_at"], "image_err": err}
+    pr.close()
+    return out
+
+
+def main(argv=None):
+    """python -m codeare_gb300.learned [--pairs P] [--steps S] [--lr LR] [--out FILE]:
+    generate pairs with the plain solver, train on the GPU, write the weights."""
+    import argparse
+    import time
+    import torch
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--pairs", type=int, default=20000)
+    ap.add_argument("--steps", type=int, default=6000)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--out", default=WEIGHTS_FILE)
+    a = ap.parse_args(argv)
+    log = lambda m: print(m, flush=True)
+    t0 = time.time()
+    X, T = generate_pairs(a.pairs, log=log)
+    torch.cuda.synchronize()
+    ms = float((T ** 2).mean())
+    log("pairs %d in %.1f s, target mean square %.4g" % (a.pairs, time.time() - t0, ms))
+    net = capi.Net(max_batch=32, max_h=256, max_w=256)
+    t0 = time.time()
+    hist = train(net, X, T, steps=a.steps, lr=a.lr)
+    torch.cuda.synchronize()
+    last = float(np.mean([h[1] for h in hist[-5:]]))
+    log("trained %d steps in %.1f s, relative loss %.3f -> %.3f" % (a.steps, time.time() - t0, hist[0][1] / ms,
+                                                                    last / ms))
+    save_weights(a.out, net.weights(), "pairs=%d steps=%d lr=%g rel_loss=%.4f" % (a.pairs, a.steps, a.lr,
+                                                                                   last / ms))
+    del X, T
+    for seed in (777, 778):
+        log(str(compare(net, seed)))
+
+
+if __name__ == "__main__":
+    main()

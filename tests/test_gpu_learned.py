@@ -75,3 +75,26 @@ def test_cnn_training_reduces_loss(gpu):
         last = net.train_step(x, t, lr=1e-3)
     assert last < 0.5 * first
     net.close()
+
+
+def test_learned_preconditioner_against_plain_cg(gpu):
+    """What the trained network gains over the method without it, on a held-out
+    256^2, 16-coil problem: plain CG, Jacobi CG (the network's skip path alone)
+    and learned flexible CG to relative residual 1e-4.  Every arm must reach the
+    tolerance (plain CG is the fallback) and land within 5x plain CG's
+    final-image error against the converged plain solve; the iteration and time
+    ratios are printed, not asserted."""
+    from codeare_gb300 import capi, learned
+    net = learned.load_net()
+    if net is None:
+        X, T = learned.generate_pairs(256, per_problem=8)
+        net = capi.Net(max_batch=32, max_h=256, max_w=256)
+        learned.train(net, X, T, steps=300)
+    r = learned.compare(net, seed=777)
+    for arm in ("plain", "jacobi", "learned"):
+        assert r[arm]["res"] <= 1e-4, r
+        assert r[arm]["image_err"] <= 5 * r["plain"]["image_err"] + 1e-4, r
+    print("learned vs plain: iterations %d vs %d, time %.1f ms vs %.1f ms (x%.2f), jacobi %d its" % (
+        r["learned"]["iterations"], r["plain"]["iterations"], r["learned"]["ms"], r["plain"]["ms"],
+        r["plain"]["ms"] / r["learned"]["ms"], r["jacobi"]["iterations"]))
+    net.close()
