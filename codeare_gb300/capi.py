@@ -28,6 +28,8 @@ EXPORTED = [
     "cgs_profile_enable", "cgs_profile_collect", "cgs_nfft2d_trafo_noalloc",
     "cgs_net_num_params", "cgs_net_create", "cgs_net_destroy", "cgs_net_set_weights", "cgs_net_get_weights",
     "cgs_net_forward", "cgs_net_gradients", "cgs_net_train_step", "cgs_solve_fcg", "cgs_normal_apply",
+    "cgs_get_tuning", "cgs_set_tuning", "cgs_autotune", "cgs_batch_create", "cgs_batch_solve",
+    "cgs_batch_destroy",
 ]
 PROFILE_CATEGORIES = ("fft", "interp", "spread")
 
@@ -46,6 +48,14 @@ class SolveOpts(C.Structure):
 class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int), ("res_first", C.c_double), ("res_last", C.c_double),
                 ("seconds", C.c_double), ("res_hist", C.c_double * 256), ("fallback_at", C.c_int)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("tile", C.c_int), ("work_slice", C.c_int), ("spread_chunk", C.c_int),
+                ("interp_coils", C.c_int), ("spread_coils", C.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class CgsError(RuntimeError):
@@ -90,6 +100,13 @@ def load(path: str = LIB_PATH):
     L.cgs_nfft2d_trafo_noalloc.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int64, vp, vp, vp, vp]
     L.cgs_solve_fcg.argtypes = [vp, vp, vp, vp, C.POINTER(SolveOpts), vp, C.POINTER(SolveReport), vp]
     L.cgs_normal_apply.argtypes = [vp, vp, vp, C.POINTER(SolveOpts), vp]
+    L.cgs_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    L.cgs_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    L.cgs_autotune.argtypes = [vp, C.POINTER(Tuning), C.POINTER(C.c_double), vp]
+    L.cgs_batch_create.argtypes = [C.POINTER(vp), C.POINTER(vp), C.POINTER(SolveOpts), C.c_int, vp]
+    L.cgs_batch_solve.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(SolveReport),
+                                  C.POINTER(C.c_double)]
+    L.cgs_batch_destroy.argtypes = [vp]
     L.cgs_net_num_params.restype = C.c_int64
     L.cgs_net_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int]
     L.cgs_net_destroy.argtypes = [vp]
@@ -231,6 +248,26 @@ class Plan:
         _check(load().cgs_solve(self._h, _ptr(y), _ptr(out), C.byref(o), C.byref(rep), _stream(stream)))
         return _report(rep)
 
+    def tuning(self):
+        t = Tuning()
+        _check(load().cgs_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **kw):
+        t = Tuning()
+        _check(load().cgs_get_tuning(self._h, C.byref(t)))
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        _check(load().cgs_set_tuning(self._h, C.byref(t)))
+
+    def autotune(self, stream=None):
+        """times candidate gridding decompositions, applies the fastest; returns
+        (tuning dict, interpolation + spreading milliseconds)"""
+        t = Tuning()
+        ms = C.c_double()
+        _check(load().cgs_autotune(self._h, C.byref(t), C.byref(ms), _stream(stream)))
+        return t.as_dict(), ms.value
+
     def solve_fcg(self, out, y=None, rhs=None, net=None, cgiter=200, cgeps=1e-4, lam=0.0, weighted=True,
                   toeplitz=True, jacobi=False, stream=None):
         """flexible CG with the learned preconditioner `net`; without one, plain CG
@@ -301,3 +338,47 @@ class Net:
         _check(load().cgs_net_train_step(self._h, _ptr(x), _ptr(t), B, H, W, float(lr),
                                          _ptr(loss) if want_loss else None, _stream(stream)))
         return float(loss[0]) if want_loss else None
+
+
+def solve_opts(mode=MODE_CODEARE, cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3, weighted=True,
+               toeplitz=False):
+    return SolveOpts(int(mode), int(cgiter), float(cgeps), float(lam), int(ftiter), float(fteps),
+                     int(bool(weighted)), int(bool(toeplitz)), 0)
+
+
+class Batch:
+    """Solves of several plans in one CUDA graph (include/cgs.h, cgs_batch_*).
+    `opts` is one solve_opts(...) per plan, or one for all."""
+
+    def __init__(self, plans, opts, stream=None):
+        L = load()
+        n = len(plans)
+        if isinstance(opts, SolveOpts):
+            opts = [opts] * n
+        self.plans = list(plans)
+        self._ph = (C.c_void_p * n)(*[p._h.value for p in plans])
+        self._opts = (SolveOpts * n)(*opts)
+        h = C.c_void_p()
+        _check(L.cgs_batch_create(C.byref(h), self._ph, self._opts, n, _stream(stream)))
+        self._h = h
+
+    def solve(self, ys, xs):
+        """ys[i] -> xs[i]; returns (reports, device seconds of the graph launch)"""
+        n = len(self.plans)
+        yp = (C.c_void_p * n)(*[_ptr(y).value for y in ys])
+        xp = (C.c_void_p * n)(*[_ptr(x).value for x in xs])
+        reps = (SolveReport * n)()
+        sec = C.c_double()
+        _check(load().cgs_batch_solve(self._h, yp, xp, reps, C.byref(sec)))
+        return [_report(r) for r in reps], sec.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().cgs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -17,6 +17,8 @@
 // No reference counterpart (the reference has no learned component).
 #include "cgs_internal.cuh"
 
+#include <atomic>
+
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -374,6 +376,7 @@ struct cgs_net {
     __nv_bfloat16 *dA = nullptr, *dB = nullptr;                           // gradient ping-pong
     float *loss = nullptr, *scale = nullptr;
     int64_t step = 0;
+    uint64_t serial = 0;              // unique per created network (graphs key on it, not the address)
 };
 
 namespace {
@@ -448,6 +451,8 @@ cgs_status net_check(cgs_net *n, int B, int H, int W)
 
 // internal use by the flexible-CG solver: z = M(r) for one complex image
 namespace cgs {
+uint64_t net_serial(const cgs_net *n) { return n ? n->serial : 0; }
+
 cgs_status net_apply_image(cgs_net *n, const float2 *r, const double *nrm2, int H, int W, float2 *z, cudaStream_t st)
 {
     CGS_TRY(net_check(n, 1, H, W));
@@ -468,7 +473,9 @@ int64_t cgs_net_num_params(void) { return kParams; }
 cgs_status cgs_net_create(cgs_net **out, int max_batch, int max_h, int max_w)
 {
     if (!out || max_batch < 1 || max_h < 1 || max_w < 1) { set_error("bad net size"); return CGS_ERR_BAD_ARG; }
+    static std::atomic<uint64_t> next_serial{1};
     cgs_net *n = new cgs_net();
+    n->serial = next_serial++;
     n->maxB = max_batch; n->maxH = max_h; n->maxW = max_w;
     const int64_t P = (int64_t)max_batch * max_h * max_w;
     bool ok = true;

@@ -502,8 +502,8 @@ cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *gri
     if (2 * g.m + 2 > kMaxTaps) { set_error("m too large"); return CGS_ERR_BAD_ARG; }
     const int taps = 2 * g.m + 2;
     if (g.d == 2 && ns.nodeU && ns.nodeW && taps <= 10) {
-        // 8 coils per CTA: 40 KB tiles leave room for 4 CTAs per SM
-        const int CC = g.nc >= 8 ? 8 : (g.nc >= 4 ? 4 : 1);
+        // 8 coils per CTA by default: 40 KB tiles leave room for 4 CTAs per SM
+        const int CC = g.icc > 0 ? g.icc : (g.nc >= 8 ? 8 : (g.nc >= 4 ? 4 : 1));
         const int E = g.T + taps - 1;
         if ((size_t)E * E * CC * sizeof(float2) <= 200 * 1024) {
             cgs_status r;
@@ -550,7 +550,8 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
                                int weighted, float2 *grid, cudaStream_t st)
 {
     if (ps.nwork == 0) return CGS_OK;
-    const int CC = g.nc >= 32 ? 32 : (g.nc >= 16 ? 16 : (g.nc >= 8 ? 8 : (g.nc >= 4 ? 4 : (g.nc >= 2 ? 2 : 1))));
+    const int CC = g.scc > 0 ? g.scc
+                             : (g.nc >= 32 ? 32 : (g.nc >= 16 ? 16 : (g.nc >= 8 ? 8 : (g.nc >= 4 ? 4 : (g.nc >= 2 ? 2 : 1)))));
     const int taps = 2 * g.m + 2;
     if (taps > kMaxTaps) { set_error("m too large"); return CGS_ERR_BAD_ARG; }
     dim3 grd((ps.nwork + 7) / 8, (g.nc + CC - 1) / CC);

@@ -130,6 +130,8 @@ struct GridGeom {
     int T;            // tile side (footprint-start bins)
     int nt[3];        // tiles per dim
     int nc;           // coils (innermost in grid and k-space)
+    int icc;          // coils per interpolation CTA (1, 4, 8, 16; 0 = automatic)
+    int scc;          // coils per spreading warp (1, 2, 4, 8, 16, 32; 0 = automatic)
 };
 
 struct NodeSet {
@@ -241,12 +243,15 @@ cgs_status launch_diag_scale(const float2 *in, const float2 *add, const float *d
                              float2 *out, cudaStream_t st);
 // z = M(r): the learned preconditioner on one complex image (cgs_cnn.cu);
 // nrm2 = sum |r|^2 on the device sets the input scale
+uint64_t net_serial(const cgs_net *n);   // 0 for null, else unique per created network
 cgs_status net_apply_image(cgs_net *n, const float2 *r, const double *nrm2, int H, int W, float2 *z,
                            cudaStream_t st);
 // Loop check (one thread): records the residual measure of the current
 // iterate, decides whether another update follows, and sets the conditional
 // handle of the enclosing while node accordingly.
 cgs_status launch_cg_check(CGScalars *sc, cudaGraphConditionalHandle h, cudaStream_t st);
+// resets the loop scalars on the device (a graph-resident replacement for the host upload)
+cgs_status launch_cg_init(CGScalars *sc, double lambda, double tol, int maxit, int sqrt_mode, cudaStream_t st);
 // q += lambda * p ; then pq = Re<p,q> is computed by coldot
 cgs_status launch_add_scaled(float2 *q, const float2 *p, const CGScalars *sc, int64_t n,
                              cudaStream_t st);

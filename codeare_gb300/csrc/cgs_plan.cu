@@ -12,6 +12,7 @@
 #include "cgs_internal.cuh"
 
 #include <algorithm>
+#include <initializer_list>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -110,6 +111,18 @@ static bool factorize(int n, int *fac, int *nf)
     return r == 1;
 }
 
+namespace tunek {
+// deterministic scratch values in [-0.5, 0.5) for timing runs
+__global__ void fill_pattern_kernel(float2 *a, int64_t n, uint32_t seed)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t h = (uint32_t)i * 2654435761u ^ seed;
+        h ^= h >> 15; h *= 2246822519u; h ^= h >> 13; h *= 3266489917u; h ^= h >> 16;
+        a[i] = make_float2((float)(h & 0xffff) / 65536.f - 0.5f, (float)(h >> 16) / 65536.f - 0.5f);
+    }
+}
+}  // namespace tunek
+
 namespace toepk {
 __global__ void toep_prepare_kernel(float2 *T, int d, int n0, int n1, int n2)
 {
@@ -164,6 +177,8 @@ struct cgs_plan {
 
     // host copies of the trajectory and weights (the Toeplitz kernel is built from them)
     std::vector<float> k_host, w_host;
+    cgs_tuning tune{};     // gridding decomposition (zeros: defaults)
+    uint64_t gen = 0;      // bumped whenever captured graphs of this plan become stale
     // Toeplitz embedding of E^H W E (standard mode)
     bool toep_valid = false;
     int toep_weighted = -1;
@@ -194,7 +209,7 @@ struct cgs_plan {
     FCGScalars *fs = nullptr;
     cudaGraphExec_t fcg_exec = nullptr;
     int fg_src = -1, fg_toep = -1, fg_weighted = -1, fg_mode = -1;
-    cgs_net *fg_net = nullptr;
+    uint64_t fg_net = 0;
     int64_t fg_kpro = 0, fg_kbody = 0;
     // captured solve: prologue + while(iteration) as one CUDA graph
     cudaGraphExec_t solve_exec = nullptr;
@@ -398,6 +413,19 @@ cgs_status op_eh(cgs_plan *p, const float2 *ks, int weighted, float2 *x, cudaStr
     return launch_coil_combine(p->cF, p->sens, nullptr, p->Nt, p->nc, x, st);
 }
 
+// bins and per-launch coil counts from the plan's tuning
+void apply_tiles(cgs_plan *p)
+{
+    GridGeom &g = p->geom;
+    g.T = (p->d == 2) ? (p->tune.tile > 0 ? p->tune.tile : 16) : 8;
+    for (int t = 0; t < p->d; ++t)
+        if (g.T > p->n[t]) g.T = p->n[t];
+    for (int t = 0; t < 3; ++t) g.nt[t] = 1;
+    for (int t = 0; t < p->d; ++t) g.nt[t] = (p->n[t] + g.T - 1) / g.T;
+    g.icc = p->tune.interp_coils;
+    g.scc = p->tune.spread_coils;
+}
+
 // Per 4 x 8 patch of the 2-D grid, the sorted indices of the nodes whose
 // footprint (2m+2 taps per axis, wrapped) covers any point of the patch; work
 // items of at most `chunk` nodes, crowded patches spread over several partial
@@ -444,7 +472,8 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     }
     // work items: a chunk bound that keeps every warp's list short
     const int64_t avg = std::max<int64_t>(1, E / std::max<int64_t>(P, 1));
-    const int chunk = (int)std::min<int64_t>(1024, std::max<int64_t>(128, 2 * avg));
+    const int chunk = p->tune.spread_chunk > 0 ? p->tune.spread_chunk
+                                               : (int)std::min<int64_t>(1024, std::max<int64_t>(128, 2 * avg));
     std::vector<int4> work, multi;
     int slots = 0;
     for (int64_t q = 0; q < P; ++q) {
@@ -513,8 +542,19 @@ AxisPass toep_pass(cgs_plan *p, int t)
     return a;
 }
 
+// Captured solve graphs hold the trajectory's work lists and the Toeplitz
+// kernel by address: any change to those drops them (they are rebuilt on the
+// next solve).
+void drop_graphs(cgs_plan *p)
+{
+    p->gen++;
+    if (p->solve_exec) { cudaGraphExecDestroy(p->solve_exec); p->solve_exec = nullptr; }
+    if (p->fcg_exec) { cudaGraphExecDestroy(p->fcg_exec); p->fcg_exec = nullptr; }
+}
+
 cgs_status build_toeplitz(cgs_plan *p, int weighted, cudaStream_t st)
 {
+    drop_graphs(p);
     const int d = p->d;
     int64_t T2 = 1;
     for (int t = 0; t < d; ++t) {
@@ -662,22 +702,33 @@ cgs_status cg_iteration(cgs_plan *p, const cgs_solve_opts *o, cudaStream_t st)
 // while node whose body is one iteration followed by the check.  The check
 // kernel decides on the device whether the loop continues, so a solve is one
 // graph launch and one read-back.
-cgs_status build_solve_graph(cgs_plan *p, const cgs_solve_opts *o, cudaStream_t st)
+// Appends one device-driven solve to graph g as an independent branch: the
+// prologue (E^H y, r = p = that, first dot, check) and a WHILE node whose body
+// is one CG iteration plus the check that sets its condition.  With
+// init_in_graph the loop scalars are reset by a kernel (batch graphs);
+// otherwise the caller uploads them before each launch.
+cgs_status append_solve(cgs_plan *p, const cgs_solve_opts *o, cudaGraph_t g, bool init_in_graph, cudaStream_t st,
+                        int64_t *kpro, int64_t *kbody)
 {
-    if (p->solve_exec) { cudaGraphExecDestroy(p->solve_exec); p->solve_exec = nullptr; }
     const int64_t Nt = p->Nt;
-    cudaGraph_t g = nullptr;
-    CGS_CUDA(cudaGraphCreate(&g, 0));
     cudaGraphConditionalHandle h;
+    if (cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("cudaGraphConditionalHandleCreate failed");
+        return CGS_ERR_CUDA;
+    }
     cgs_status r = CGS_OK;
-    if (cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) r = CGS_ERR_CUDA;
     const int64_t c0 = cgs_kernel_launches();
     std::vector<cudaGraphNode_t> frontier;
-    if (r == CGS_OK && cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+    if (cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
         r = CGS_ERR_CUDA;
     if (r == CGS_OK) {
-        cgs_status q = (o->mode == CGS_MODE_CODEARE) ? op_eh_codeare(p, p->ksY, o->ftiter, o->fteps, p->vP, st)
-                                                      : op_eh(p, p->ksY, o->weighted, p->vP, st);
+        cgs_status q = CGS_OK;
+        if (init_in_graph)
+            q = launch_cg_init(p->sc, o->lambda, o->cgeps, o->cgiter, o->mode == CGS_MODE_CODEARE ? 0 : 1, st);
+        if (q == CGS_OK)
+            q = (o->mode == CGS_MODE_CODEARE) ? op_eh_codeare(p, p->ksY, o->ftiter, o->fteps, p->vP, st)
+                                              : op_eh(p, p->ksY, o->weighted, p->vP, st);
         if (q == CGS_OK && cudaMemcpyAsync(p->vR, p->vP, sizeof(float2) * Nt, cudaMemcpyDeviceToDevice, st) != cudaSuccess) q = CGS_ERR_CUDA;
         if (q == CGS_OK) q = launch_zero(p->vX, sizeof(float2) * Nt, st);
         if (q == CGS_OK) q = launch_coldot(p->vR, p->vP, nullptr, Nt, 1, p->partial, p->scal(), st);
@@ -694,7 +745,7 @@ cgs_status build_solve_graph(cgs_plan *p, const cgs_solve_opts *o, cudaStream_t 
         if (cudaStreamEndCapture(st, &gg) != cudaSuccess && q == CGS_OK) q = CGS_ERR_CUDA;
         r = q;
     }
-    p->sg_kpro = cgs_kernel_launches() - c0;
+    *kpro = cgs_kernel_launches() - c0;
     cudaGraphNode_t cond = nullptr;
     cudaGraph_t body = nullptr;
     if (r == CGS_OK) {
@@ -716,8 +767,18 @@ cgs_status build_solve_graph(cgs_plan *p, const cgs_solve_opts *o, cudaStream_t 
         if (cudaStreamEndCapture(st, &bb) != cudaSuccess && q == CGS_OK) q = CGS_ERR_CUDA;
         r = q;
     }
-    p->sg_kbody = cgs_kernel_launches() - c1;
+    *kbody = cgs_kernel_launches() - c1;
     count_launch((int)-(cgs_kernel_launches() - c0));  // captured launches run only when the graph runs
+    cudaGetLastError();
+    return r;
+}
+
+cgs_status build_solve_graph(cgs_plan *p, const cgs_solve_opts *o, cudaStream_t st)
+{
+    if (p->solve_exec) { cudaGraphExecDestroy(p->solve_exec); p->solve_exec = nullptr; }
+    cudaGraph_t g = nullptr;
+    CGS_CUDA(cudaGraphCreate(&g, 0));
+    cgs_status r = append_solve(p, o, g, false, st, &p->sg_kpro, &p->sg_kbody);
     if (r == CGS_OK && cudaGraphInstantiate(&p->solve_exec, g, 0) != cudaSuccess) {
         set_error("cudaGraphInstantiate of the solve graph failed");
         r = CGS_ERR_CUDA;
@@ -857,7 +918,7 @@ cgs_status build_fcg_graph(cgs_plan *p, int from_data, int toeplitz, int weighte
     cudaGraphDestroy(g);
     cudaGetLastError();
     if (r != CGS_OK) { p->fcg_exec = nullptr; return r; }
-    p->fg_src = from_data; p->fg_toep = toeplitz; p->fg_weighted = weighted; p->fg_net = net; p->fg_mode = mode;
+    p->fg_src = from_data; p->fg_toep = toeplitz; p->fg_weighted = weighted; p->fg_net = net_serial(net); p->fg_mode = mode;
     return CGS_OK;
 }
 
@@ -968,12 +1029,8 @@ cgs_status cgs_plan_create(cgs_plan **out, const cgs_plan_desc *desc)
     // geometry of the gridding tiles
     GridGeom &g = p->geom;
     g.d = p->d; g.m = p->m; g.nc = p->nc;
-    g.T = (p->d == 2) ? 16 : 8;
-    for (int t = 0; t < p->d; ++t) {
-        if (g.T > p->n[t]) g.T = p->n[t];
-    }
-    for (int t = 0; t < 3; ++t) { g.n[t] = (t < p->d) ? p->n[t] : 1; g.nt[t] = 1; }
-    for (int t = 0; t < p->d; ++t) g.nt[t] = (p->n[t] + g.T - 1) / g.T;
+    for (int t = 0; t < 3; ++t) g.n[t] = (t < p->d) ? p->n[t] : 1;
+    apply_tiles(p);
     const int64_t nc = p->nc, M = p->M, Nt = p->Nt, nT = p->ntot;
     // damping mask What (NFFTTraits.hpp:225-260): radius N[0]/2 around index N[0]/2
     {
@@ -1069,6 +1126,8 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
         std::memcpy(k.data(), k_in, sizeof(float) * k.size());
     }
     p->toep_valid = false;
+    drop_graphs(p);
+    apply_tiles(p);
     const GridGeom &g = p->geom;
     int ntiles = 1;
     for (int t = 0; t < d; ++t) ntiles *= g.nt[t];
@@ -1116,7 +1175,7 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
         }
     }
     // work items: bins split into slices of at most kWork nodes
-    const int kWork = 1024;
+    const int kWork = p->tune.work_slice > 0 ? p->tune.work_slice : 1024;
     std::vector<int4> work;
     for (int ti = 0; ti < ntiles; ++ti) {
         for (int s0 = cnt[ti]; s0 < cnt[ti + 1]; s0 += kWork) {
@@ -1155,6 +1214,7 @@ cgs_status cgs_set_weights(cgs_plan *p, const float *w_in)
     CGS_CUDA(cudaMemcpy(p->w, ws.data(), sizeof(float) * M, cudaMemcpyHostToDevice));
     p->w_host = w;
     p->toep_valid = false;
+    drop_graphs(p);
     p->have_w = true;
     return CGS_OK;
 }
@@ -1398,7 +1458,7 @@ cgs_status cgs_solve_fcg(cgs_plan *p, const float *y, const float *rhs, float *x
     }
     const int mode = net ? 2 : (o->jacobi ? 1 : 0);
     const bool same = p->fcg_exec && p->fg_src == from_data && p->fg_toep == o->toeplitz &&
-                      p->fg_weighted == o->weighted && p->fg_net == net && p->fg_mode == mode;
+                      p->fg_weighted == o->weighted && p->fg_net == net_serial(net) && p->fg_mode == mode;
     if (!same) CGS_TRY(build_fcg_graph(p, from_data, o->toeplitz, o->weighted, net, mode, st));
     double sumw = (double)p->M;
     if (o->weighted && p->have_w) {
@@ -1435,6 +1495,271 @@ cgs_status cgs_solve_fcg(cgs_plan *p, const float *y, const float *rhs, float *x
     }
     CGS_TRY(image_out(p, p->vX, x, st));
     return h.cg.nan_flag ? CGS_ERR_NAN : CGS_OK;
+}
+
+
+cgs_status cgs_get_tuning(const cgs_plan *p, cgs_tuning *out)
+{
+    if (!p || !out) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    *out = p->tune;
+    return CGS_OK;
+}
+
+static cgs_status rebin(cgs_plan *p)
+{
+    if (!p->have_k) return CGS_OK;
+    const std::vector<float> k = p->k_host, w = p->w_host;
+    const bool hw = p->have_w;
+    CGS_TRY(cgs_set_kspace(p, k.data()));
+    if (hw) CGS_TRY(cgs_set_weights(p, w.data()));
+    return CGS_OK;
+}
+
+cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
+{
+    if (!p || !t) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    auto in = [](int v, std::initializer_list<int> ok) {
+        for (int o : ok) if (v == o) return true;
+        return false;
+    };
+    if (!in(t->tile, {0, 8, 16, 32}) || !in(t->interp_coils, {0, 1, 4, 8, 16}) ||
+        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) ||
+        (t->work_slice != 0 && (t->work_slice < 32 || t->work_slice > 65536)) ||
+        (t->spread_chunk != 0 && (t->spread_chunk < 32 || t->spread_chunk > 65536))) {
+        set_error("tuning value out of range");
+        return CGS_ERR_BAD_ARG;
+    }
+    CGS_CUDA(cudaSetDevice(p->device));
+    const bool bins = t->tile != p->tune.tile || t->work_slice != p->tune.work_slice ||
+                      t->spread_chunk != p->tune.spread_chunk;
+    p->tune = *t;
+    apply_tiles(p);
+    drop_graphs(p);
+    if (bins) CGS_TRY(rebin(p));
+    return CGS_OK;
+}
+
+cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *stream)
+{
+    if (!p) { set_error("null plan"); return CGS_ERR_BAD_ARG; }
+    if (!p->have_k) { set_error("autotune needs the k-space"); return CGS_ERR_STATE; }
+    if (p->d != 2) { set_error("the autotuner covers 2-D plans"); return CGS_ERR_BAD_ARG; }
+    CGS_CUDA(cudaSetDevice(p->device));
+    cudaStream_t st = pick_stream(p, stream);
+    const int64_t gridN = p->ntot * p->nc, ksN = p->M * p->nc;
+    auto fill = [&](float2 *a, int64_t n, uint32_t seed) -> cgs_status {
+        const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 8);
+        tunek::fill_pattern_kernel<<<blocks, 256, 0, st>>>(a, n, seed);
+        CGS_LAUNCH_CHECK();
+        return CGS_OK;
+    };
+    auto timed = [&](auto &&launch, double *out) -> cgs_status {
+        CGS_TRY(launch());
+        CGS_CUDA(cudaEventRecord(p->ev0, st));
+        for (int i = 0; i < 3; ++i) CGS_TRY(launch());
+        CGS_CUDA(cudaEventRecord(p->ev1, st));
+        CGS_CUDA(cudaEventSynchronize(p->ev1));
+        float t = 0.f;
+        CGS_CUDA(cudaEventElapsedTime(&t, p->ev0, p->ev1));
+        *out = t / 3.0;
+        return CGS_OK;
+    };
+    auto interp = [&]() -> cgs_status {
+        NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW};
+        return launch_interp(p->geom, ns, p->grid, p->ksR, st);
+    };
+    auto spread = [&]() -> cgs_status {
+        return launch_spread_patch(p->geom, p->pset, p->ksV, p->w, 0, p->grid, st);
+    };
+    std::vector<int> iccs, sccs;
+    for (int c : {1, 4, 8, 16})
+        if (c == 1 || c <= p->nc) iccs.push_back(c);
+    for (int c : {32, 16, 8, 4, 2, 1})
+        if (c <= p->nc && (int)sccs.size() < 3) sccs.push_back(c);
+    cgs_tuning best = p->tune, cur = p->tune;
+    double t_int = 1e30, t_spr = 1e30, t = 0.0;
+    // interpolation: bin side and coils per CTA, then the work slice
+    CGS_TRY(fill(p->grid, gridN, 0x9e3779b9u));
+    for (int tile : {8, 16, 32}) {
+        if (tile > p->n[0] || tile > p->n[1]) continue;
+        cur = best; cur.tile = tile; cur.work_slice = 1024;
+        p->tune = cur;
+        CGS_TRY(rebin(p));
+        const int E = std::min(tile, std::min(p->n[0], p->n[1])) + 2 * p->m + 1;
+        for (int c : iccs) {
+            if ((size_t)E * E * c * sizeof(float2) > 200 * 1024) continue;  // keeps the register-tile kernel
+            p->tune.interp_coils = c;
+            apply_tiles(p);
+            CGS_TRY(timed(interp, &t));
+            if (t < t_int) { t_int = t; best.tile = tile; best.work_slice = 1024; best.interp_coils = c; }
+        }
+    }
+    for (int slice : {512, 2048}) {
+        cur = best; cur.work_slice = slice;
+        p->tune = cur;
+        CGS_TRY(rebin(p));
+        CGS_TRY(timed(interp, &t));
+        if (t < t_int) { t_int = t; best.work_slice = slice; }
+    }
+    // spreading: chunk bound and coils per warp
+    CGS_TRY(fill(p->ksV, ksN, 0x85ebca6bu));
+    for (int chunk : {0, 128, 256, 512, 1024}) {
+        cur = best; cur.spread_chunk = chunk;
+        p->tune = cur;
+        CGS_TRY(rebin(p));
+        for (int c : sccs) {
+            p->tune.spread_coils = c;
+            apply_tiles(p);
+            CGS_TRY(timed(spread, &t));
+            if (t < t_spr) { t_spr = t; best.spread_chunk = chunk; best.spread_coils = c; }
+        }
+    }
+    p->tune = best;
+    apply_tiles(p);
+    CGS_TRY(rebin(p));
+    if (chosen) *chosen = best;
+    if (ms) *ms = t_int + t_spr;
+    return CGS_OK;
+}
+
+
+}  // extern "C"
+
+struct cgs_batch {
+    std::vector<cgs_plan *> plans;
+    std::vector<cgs_solve_opts> opts;
+    std::vector<uint64_t> gens;
+    std::vector<int64_t> kpro, kbody;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    CGScalars *host_sc = nullptr;  // pinned, one per plan
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int device = 0;
+};
+
+extern "C" {
+
+cgs_status cgs_batch_destroy(cgs_batch *b)
+{
+    if (!b) return CGS_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->host_sc) cudaFreeHost(b->host_sc);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return CGS_OK;
+}
+
+cgs_status cgs_batch_create(cgs_batch **out, cgs_plan *const *plans, const cgs_solve_opts *opts, int count,
+                            void *stream)
+{
+    if (!out || !plans || !opts || count < 1) { set_error("bad argument"); return CGS_ERR_BAD_ARG; }
+    *out = nullptr;
+    for (int i = 0; i < count; ++i) {
+        cgs_plan *p = plans[i];
+        const cgs_solve_opts *o = &opts[i];
+        if (!p) { set_error("null plan in batch"); return CGS_ERR_BAD_ARG; }
+        if (p->device != plans[0]->device) { set_error("batch plans must share a device"); return CGS_ERR_BAD_ARG; }
+        for (int j = 0; j < i; ++j)
+            if (plans[j] == p) { set_error("a plan appears twice in the batch"); return CGS_ERR_BAD_ARG; }
+        const bool codeare = o->mode == CGS_MODE_CODEARE;
+        CGS_TRY(check_ready(p, codeare || o->weighted, true));
+        if (o->cgiter < 1 || o->cgiter > 100000 || o->ftiter < 0) { set_error("bad iteration counts"); return CGS_ERR_BAD_ARG; }
+    }
+    cgs_batch *b = new cgs_batch();
+    b->device = plans[0]->device;
+    cudaSetDevice(b->device);
+    cgs_status r = CGS_OK;
+    if (stream) b->stream = (cudaStream_t)stream;
+    else if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess) b->own_stream = true;
+    else r = CGS_ERR_CUDA;
+    if (r == CGS_OK && (cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)) r = CGS_ERR_CUDA;
+    if (r == CGS_OK && cudaMallocHost(&b->host_sc, sizeof(CGScalars) * count) != cudaSuccess) r = CGS_ERR_OOM;
+    cudaStream_t st = b->stream;
+    // Toeplitz kernels first: building one invalidates the plan's graphs
+    for (int i = 0; i < count && r == CGS_OK; ++i) {
+        cgs_plan *p = plans[i];
+        const cgs_solve_opts &o = opts[i];
+        if (o.mode != CGS_MODE_CODEARE && o.toeplitz) {
+            const int wtd = (o.weighted && p->have_w) ? 1 : 0;
+            if (!p->toep_valid || p->toep_weighted != wtd) r = build_toeplitz(p, wtd, st);
+        }
+    }
+    cudaGraph_t g = nullptr;
+    if (r == CGS_OK && cudaGraphCreate(&g, 0) != cudaSuccess) r = CGS_ERR_CUDA;
+    for (int i = 0; i < count && r == CGS_OK; ++i) {
+        cgs_solve_opts o = opts[i];
+        if (o.mode == CGS_MODE_CODEARE) o.toeplitz = 0;
+        int64_t kp = 0, kb = 0;
+        r = append_solve(plans[i], &o, g, true, st, &kp, &kb);
+        b->plans.push_back(plans[i]);
+        b->opts.push_back(o);
+        b->kpro.push_back(kp);
+        b->kbody.push_back(kb);
+    }
+    if (r == CGS_OK && cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) {
+        set_error("cudaGraphInstantiate of the batch graph failed");
+        r = CGS_ERR_CUDA;
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (r != CGS_OK) { b->exec = nullptr; cgs_batch_destroy(b); return r; }
+    for (cgs_plan *p : b->plans) b->gens.push_back(p->gen);
+    *out = b;
+    return CGS_OK;
+}
+
+cgs_status cgs_batch_solve(cgs_batch *b, const float *const *y, float *const *x, cgs_solve_report *reports,
+                           double *seconds)
+{
+    if (!b || !y || !x) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    const int count = (int)b->plans.size();
+    for (int i = 0; i < count; ++i) {
+        if (!y[i] || !x[i]) { set_error("null data pointer in batch"); return CGS_ERR_BAD_ARG; }
+        if (b->plans[i]->gen != b->gens[i]) {
+            set_error("a plan of the batch changed after the batch was built");
+            return CGS_ERR_STATE;
+        }
+    }
+    CGS_CUDA(cudaSetDevice(b->device));
+    cudaStream_t st = b->stream;
+    for (int i = 0; i < count; ++i) CGS_TRY(ks_in(b->plans[i], y[i], st));
+    CGS_CUDA(cudaEventRecord(b->ev0, st));
+    CGS_CUDA(cudaGraphLaunch(b->exec, st));
+    CGS_CUDA(cudaEventRecord(b->ev1, st));
+    for (int i = 0; i < count; ++i)
+        CGS_CUDA(cudaMemcpyAsync(&b->host_sc[i], b->plans[i]->sc, sizeof(CGScalars), cudaMemcpyDeviceToHost, st));
+    for (int i = 0; i < count; ++i) CGS_TRY(image_out(b->plans[i], b->plans[i]->vX, x[i], st));
+    CGS_CUDA(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    CGS_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    if (seconds) *seconds = ms * 1e-3;
+    cgs_status result = CGS_OK;
+    for (int i = 0; i < count; ++i) {
+        const CGScalars &h = b->host_sc[i];
+        const bool codeare = b->opts[i].mode == CGS_MODE_CODEARE;
+        count_launch((int)(b->kpro[i] + (int64_t)h.iter * b->kbody[i]));
+        if (h.nan_flag) result = CGS_ERR_NAN;
+        if (reports) {
+            cgs_solve_report *rep = &reports[i];
+            std::memset(rep, 0, sizeof(*rep));
+            rep->fallback_at = -1;
+            const int nh = std::min(256, h.iter + 1);
+            for (int k = 0; k < nh; ++k) rep->res_hist[k] = h.hist[k];
+            rep->res_first = h.hist[0];
+            const double ratio = h.rn / h.xn;
+            rep->res_last = codeare ? ratio : std::sqrt(ratio);
+            if (!codeare && h.iter < 256) rep->res_hist[h.iter] = rep->res_last;
+            rep->iterations = h.iter;
+            rep->seconds = ms * 1e-3;
+        }
+    }
+    if (result == CGS_ERR_NAN) set_error("NaN in a batch solve");
+    return result;
 }
 
 }  // extern "C"

@@ -562,6 +562,28 @@ cgs_status launch_fcg_kernels(int which, FCGScalars *fs, float2 *x, float2 *r, f
     return CGS_OK;
 }
 
+__global__ void cg_init_kernel(CGScalars *sc, double lambda, double tol, int maxit, int sqrt_mode)
+{
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) sc->hist[i] = 0.0;
+    if (threadIdx.x == 0) {
+        sc->rn = sc->xn = sc->rno = sc->pq = sc->ts = sc->beta = 0.0;
+        sc->lambda = lambda;
+        sc->done = 0;
+        sc->tol = tol;
+        sc->iter = 0;
+        sc->maxit = maxit;
+        sc->sqrt_mode = sqrt_mode;
+        sc->nan_flag = 0;
+    }
+}
+
+cgs_status launch_cg_init(CGScalars *sc, double lambda, double tol, int maxit, int sqrt_mode, cudaStream_t st)
+{
+    cg_init_kernel<<<1, 256, 0, st>>>(sc, lambda, tol, maxit, sqrt_mode);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
 cgs_status launch_cg_check(CGScalars *sc, cudaGraphConditionalHandle h, cudaStream_t st)
 {
     cg_check_kernel<<<1, 1, 0, st>>>(sc, h);

@@ -149,6 +149,15 @@ def spiral2d(ninter: int, nsamp: int, density_exp: float = 1.5, turns: float = 1
     return _clip_k(np.concatenate(out, axis=0))
 
 
+def spiral_weights(k: np.ndarray, ninter: int) -> np.ndarray:
+    """density compensation for interleaved spirals: the area |k x dk/dt| swept
+    per sample, scaled to a maximum of 0.5 (the ramp's maximum)"""
+    kk = k.astype(np.float64).reshape(ninter, -1, 2)
+    g = np.gradient(kk, axis=1)
+    w = np.abs(kk[..., 0] * g[..., 1] - kk[..., 1] * g[..., 0]).ravel()
+    return (0.5 * w / max(float(w.max()), 1e-30)).astype(np.float32)
+
+
 def kooshball3d(nspokes: int, nsamp: int) -> np.ndarray:
     """3-D radial spokes with directions on a Fibonacci hemisphere."""
     i = np.arange(nspokes, dtype=np.float64)
@@ -189,6 +198,28 @@ def config1():
     return dict(name="cfg1_nufft_256_32c_ga403x512", shape=(N, N), image=phantom(N),
                 sens=coils2d(N, nc), k=k, w=ramp_weights(k), alpha=2.0, m=4,
                 seed=SEED_BASE + 1)
+
+
+def config2(count: int = 64, seed: int = SEED_BASE + 2):
+    """Batched uneven CG-SENSE: per problem N in 96..320 (step 32), NC in
+    {4, 8, 16, 32}, golden-angle radial 32..400 spokes x 512; every fourth
+    problem a variable-density spiral (16 interleaves x 4096, exponent 1.5).
+    Shepp-Logan images, sigma=2, m=4, 15 CG iterations, 1e-3 noise."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        N = int(rng.choice(np.arange(96, 321, 32)))
+        nc = int(rng.choice([4, 8, 16, 32]))
+        if i % 4 == 3:
+            k = spiral2d(16, 4096, density_exp=1.5)
+            w, kind = spiral_weights(k, 16), "spiral16x4096"
+        else:
+            spokes = int(rng.integers(32, 401))
+            k = radial2d(spokes, 512, golden=True)
+            w, kind = ramp_weights(k), "radial%dx512" % spokes
+        out.append(dict(name="cfg2_%02d_%d_%dc_%s" % (i, N, nc, kind), shape=(N, N), N=N, nc=nc, kind=kind,
+                        k=k, w=w, alpha=2.0, m=4, cgiter=15, noise=1e-3, seed=seed + 1000 * i))
+    return out
 
 
 def small_config(N=32, nc=4, nspokes=24, nsamp=64, alpha=2.0, m=4, golden=True, seed=7):

@@ -169,6 +169,46 @@ cgs_status cgs_net_gradients(cgs_net *net, const float *x, const float *target, 
 cgs_status cgs_net_train_step(cgs_net *net, const float *x, const float *target, int B, int H, int W,
                               float lr, float *loss, void *stream);
 
+/* Batched solves (no reference counterpart; codeare runs one CGSENSE module
+ * per process): one CUDA graph holds the solves of `count` plans as
+ * independent branches, each a device-driven CG loop (opts[i] as in
+ * cgs_solve, cgiter >= 1), so uneven problems of any size, coil count and
+ * trajectory run concurrently from a single graph launch.  A plan may belong
+ * to one batch at a time and must not be used elsewhere while the batch
+ * solves; changing its k-space, weights or tuning afterwards makes
+ * cgs_batch_solve return CGS_ERR_STATE (build a new batch). */
+typedef struct cgs_batch cgs_batch;
+cgs_status cgs_batch_create(cgs_batch **out, cgs_plan *const *plans, const cgs_solve_opts *opts, int count,
+                            void *stream);
+/* y[i]: plan i's samples (M x NC complex, host or device); x[i]: its image.
+ * reports (nullable) gets one report per plan; seconds (nullable) the device
+ * time of the graph launch. */
+cgs_status cgs_batch_solve(cgs_batch *b, const float *const *y, float *const *x, cgs_solve_report *reports,
+                           double *seconds);
+cgs_status cgs_batch_destroy(cgs_batch *b);
+
+/* Gridding work decomposition of a plan (no reference counterpart: NFFT3
+ * has no tunable bins).  0 in a field means the built-in default. */
+typedef struct {
+    int tile;          /* 2-D interpolation bin side in grid points (8, 16, 32; default 16) */
+    int work_slice;    /* most nodes per interpolation work item (default 1024) */
+    int spread_chunk;  /* most nodes per spreading work item (default 2x the mean patch list, 128..1024) */
+    int interp_coils;  /* coils per interpolation CTA: 1, 4, 8 or 16 (default 8, fewer for fewer coils) */
+    int spread_coils;  /* coils per spreading warp: 1, 2, 4, 8, 16 or 32 (default: coils, at most 32) */
+} cgs_tuning;
+
+cgs_status cgs_get_tuning(const cgs_plan *plan, cgs_tuning *out);
+/* Applies `t`; a change of tile, work_slice or spread_chunk re-bins the
+ * trajectory (the k-space and weights already set are kept). */
+cgs_status cgs_set_tuning(cgs_plan *plan, const cgs_tuning *t);
+/* Autotuner: times the plan's own interpolation and spreading launches on
+ * scratch data for each candidate decomposition (tile x work_slice x
+ * interp_coils, spread_chunk x spread_coils), applies the fastest and returns
+ * it with its interpolation + spreading time in milliseconds.  Needs the
+ * k-space; leaves the plan's data and the Toeplitz kernel to be rebuilt on
+ * their next use.  2-D plans only. */
+cgs_status cgs_autotune(cgs_plan *plan, cgs_tuning *chosen, double *ms, void *stream);
+
 /* Flexible CG-SENSE with the learned preconditioner (no reference
  * counterpart): standard-mode normal equations (E^H W E + lambda) x = b with
  * z = d . net(d . r) as a variable preconditioner, d = D^-1/2 the exact

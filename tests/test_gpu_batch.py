@@ -1,0 +1,186 @@
+"""Gridding tuning, the autotuner and batched graph solves (uneven problems in
+one CUDA graph launch) against per-plan solves and the FP64 oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-300))
+
+
+def make_plan(N, nc, k, w, m=4, alpha=2.0):
+    from codeare_gb300 import capi, synth
+    p = capi.Plan((N, N), k.shape[0], ncoils=nc, m=m, alpha=alpha)
+    p.set_kspace(k)
+    p.set_weights(w)
+    S = synth.coils2d(N, nc)
+    p.set_sensitivities(S)
+    return p, S
+
+
+def data_for(p, N, nc, M, seed):
+    from codeare_gb300 import synth
+    y = np.zeros((nc, M), np.complex64)
+    p.sense_trafo(np.ascontiguousarray(synth.phantom(N)), y)
+    return synth.add_noise(y, 1e-3, seed=seed)
+
+
+def nfft_pair(p, N, nc, M, seed=0):
+    rng = np.random.default_rng(seed)
+    fh = (rng.standard_normal((nc, N, N)) + 1j * rng.standard_normal((nc, N, N))).astype(np.complex64)
+    f = np.zeros((nc, M), np.complex64)
+    img = np.zeros((nc, N, N), np.complex64)
+    p.nfft_trafo(fh, f)
+    p.nfft_adjoint(f, img)
+    return f, img
+
+
+def test_tuning_changes_decomposition_not_results(gpu):
+    from codeare_gb300 import capi, synth
+    N, nc = 64, 8
+    k = synth.radial2d(48, 128, golden=True)
+    p, _ = make_plan(N, nc, k, synth.ramp_weights(k))
+    f0, a0 = nfft_pair(p, N, nc, k.shape[0])
+    assert p.tuning() == dict(tile=0, work_slice=0, spread_chunk=0, interp_coils=0, spread_coils=0)
+    for t in [dict(tile=8, work_slice=256, spread_chunk=64, interp_coils=4, spread_coils=2),
+              dict(tile=32, work_slice=2048, spread_chunk=1024, interp_coils=16, spread_coils=8),
+              dict(tile=16, work_slice=100, spread_chunk=0, interp_coils=1, spread_coils=1)]:
+        p.set_tuning(**t)
+        assert p.tuning() == t
+        f1, a1 = nfft_pair(p, N, nc, k.shape[0])
+        # interpolation sums each node's taps in a fixed order: identical bits
+        assert np.array_equal(f1, f0)
+        # spreading sums split patches in another grouping: rounding only
+        assert rel(a1, a0) < 1e-6
+    with pytest.raises(capi.CgsError):
+        p.set_tuning(tile=12)
+    with pytest.raises(capi.CgsError):
+        p.set_tuning(interp_coils=3)
+    p.close()
+
+
+def test_autotune_picks_valid_decomposition(gpu):
+    from codeare_gb300 import synth
+    N, nc = 128, 16
+    k = synth.radial2d(96, 256, golden=True)
+    p, _ = make_plan(N, nc, k, synth.ramp_weights(k))
+    f0, a0 = nfft_pair(p, N, nc, k.shape[0], seed=3)
+    t, ms = p.autotune()
+    assert ms > 0
+    assert t["tile"] in (8, 16, 32) and t["interp_coils"] in (1, 4, 8, 16)
+    assert t["spread_coils"] in (1, 2, 4, 8, 16) and t["work_slice"] in (512, 1024, 2048)
+    assert p.tuning() == t
+    f1, a1 = nfft_pair(p, N, nc, k.shape[0], seed=3)
+    assert np.array_equal(f1, f0)
+    assert rel(a1, a0) < 1e-6
+    p.close()
+
+
+def test_new_trajectory_rebuilds_the_solve_graph(gpu):
+    """A cached solve graph holds the work lists by address: setting a new
+    trajectory must rebuild it (same answer as a fresh plan)."""
+    from codeare_gb300 import synth
+    import codeare_gb300 as cg
+    N, nc = 48, 4
+    k1 = synth.radial2d(40, 96, golden=True)
+    k2 = synth.radial2d(40, 96, golden=False)
+    p, _ = make_plan(N, nc, k1, synth.ramp_weights(k1))
+    y = data_for(p, N, nc, k1.shape[0], seed=1)
+    x = np.zeros((N, N), np.complex64)
+    p.solve(y, x, mode=cg.MODE_STANDARD, cgiter=8, cgeps=0.0, lam=0.0, toeplitz=True)
+    p.set_kspace(k2)
+    p.set_weights(synth.ramp_weights(k2))
+    p.solve(y, x, mode=cg.MODE_STANDARD, cgiter=8, cgeps=0.0, lam=0.0, toeplitz=True)
+    q, _ = make_plan(N, nc, k2, synth.ramp_weights(k2))
+    xq = np.zeros_like(x)
+    q.solve(y, xq, mode=cg.MODE_STANDARD, cgiter=8, cgeps=0.0, lam=0.0, toeplitz=True)
+    assert np.array_equal(x, xq)
+    p.close()
+    q.close()
+
+
+def uneven_problems():
+    from codeare_gb300 import synth
+    spec = [(48, 4, "radial", 40), (64, 8, "spiral", 0), (96, 4, "radial", 64), (32, 16, "radial", 24),
+            (80, 8, "radial", 56), (64, 32, "spiral", 0)]
+    out = []
+    for i, (N, nc, kind, sp) in enumerate(spec):
+        if kind == "spiral":
+            k = synth.spiral2d(8, 512)
+            w = synth.spiral_weights(k, 8)
+        else:
+            k = synth.radial2d(sp, 2 * N, golden=True)
+            w = synth.ramp_weights(k)
+        out.append((N, nc, k, w))
+    return out
+
+
+def test_batch_matches_per_plan_solves(gpu):
+    """Mixed modes in one graph: codeare CGLS (CGNR E^H), standard mode with the
+    NFFT pair and with the Toeplitz embedding.  Same kernels on the same data:
+    the batch must reproduce each plan's own solve."""
+    from codeare_gb300 import capi
+    import codeare_gb300 as cg
+    probs = uneven_problems()
+    plans, ys, opts = [], [], []
+    for i, (N, nc, k, w) in enumerate(probs):
+        p, _ = make_plan(N, nc, k, w)
+        plans.append(p)
+        ys.append(data_for(p, N, nc, k.shape[0], seed=10 + i))
+        if i % 3 == 0:
+            opts.append(capi.solve_opts(mode=cg.MODE_CODEARE, cgiter=15, cgeps=0.0, lam=5e-2))
+        elif i % 3 == 1:
+            opts.append(capi.solve_opts(mode=cg.MODE_STANDARD, cgiter=15, cgeps=0.0, lam=1e-2))
+        else:
+            opts.append(capi.solve_opts(mode=cg.MODE_STANDARD, cgiter=15, cgeps=0.0, lam=1e-2, toeplitz=True))
+    singles = []
+    for p, y, o, (N, *_r) in zip(plans, ys, opts, probs):
+        x = np.zeros((N, N), np.complex64)
+        p.solve(y, x, mode=o.mode, cgiter=o.cgiter, cgeps=o.cgeps, lam=o.lam, ftiter=o.ftiter, fteps=o.fteps,
+                weighted=bool(o.weighted), toeplitz=bool(o.toeplitz))
+        singles.append(x)
+    b = capi.Batch(plans, opts)
+    xs = [np.zeros((N, N), np.complex64) for (N, *_r) in probs]
+    reps, sec = b.solve(ys, xs)
+    assert sec > 0
+    for x, s, r in zip(xs, singles, reps):
+        assert r["iterations"] == 15
+        assert rel(x, s) < 1e-6
+    # a second launch of the same graph gives the same images
+    xs2 = [np.zeros_like(x) for x in xs]
+    b.solve(ys, xs2)
+    for x, x2 in zip(xs, xs2):
+        assert np.array_equal(x, x2)
+    # changing a member plan invalidates the batch
+    plans[1].set_weights(probs[1][3] * 2)
+    with pytest.raises(capi.CgsError):
+        b.solve(ys, xs2)
+    b.close()
+    for p in plans:
+        p.close()
+
+
+def test_batch_parity_with_oracle(gpu, oracle):
+    """codeare-mode CGLS, 15 iterations, through the batch: within 1e-4 of the
+    FP64 oracle of the reference semantics for two uneven problems."""
+    from codeare_gb300 import capi
+    import codeare_gb300 as cg
+    probs = uneven_problems()[:2]
+    plans, ys, sens = [], [], []
+    for i, (N, nc, k, w) in enumerate(probs):
+        p, S = make_plan(N, nc, k, w)
+        plans.append(p)
+        sens.append(S)
+        ys.append(data_for(p, N, nc, k.shape[0], seed=20 + i))
+    b = capi.Batch(plans, capi.solve_opts(mode=cg.MODE_CODEARE, cgiter=15, cgeps=1e-7, lam=5e-2))
+    xs = [np.zeros((N, N), np.complex64) for (N, *_r) in probs]
+    b.solve(ys, xs)
+    for (N, nc, k, w), S, y, x in zip(probs, sens, ys, xs):
+        s = oracle.Sense(S, k, w=w, m=4, alpha=2.0)
+        xo, _ = s.cgls_codeare(y, cgiter=15, cgeps=1e-7, lam=5e-2)
+        assert rel(x, xo) < 1e-4
+    b.close()
+    for p in plans:
+        p.close()
