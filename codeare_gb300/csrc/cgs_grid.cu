@@ -229,15 +229,7 @@ spread_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSe
     }
 }
 
-// ---------------------------------------------------------------------------
-// Output-stationary 2-D spreading.  Lane l of a warp owns grid point
-// (py0 + l/8, px0 + l%8) of a 4 x 8 patch and accumulates CC coils in
-// registers while the warp walks the patch's node list; every node value is
-// one uniform (broadcast) load per coil, no atomics anywhere.  A crowded patch
-// is split into several work items whose partial sums land in `partial` and
-// are added in slot order by patch_reduce_kernel, so results are bitwise
-// reproducible.
-// ---------------------------------------------------------------------------
+// window weights and wrapped footprint starts of every node (once per trajectory)
 __global__ void node_weights_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
                                     int2 *__restrict__ nodeU, float *__restrict__ nodeW)
 {
@@ -253,70 +245,149 @@ __global__ void node_weights_kernel(const __grid_constant__ GridGeom g, const __
     }
 }
 
-// Per-warp staging in shared memory of a batch of 32 list entries: lane l
-// fetches entry l's node weights, values and density weight with independent
-// loads, so one global round trip serves 32 entries; the accumulation loop
-// then reads only shared memory (broadcasts and conflict-free rows).  The
-// value rows are padded to a 16-byte multiple so two coils come per load.
-template <int CC> struct SpreadRow { static constexpr int v = CC + ((CC & 1) ? 1 : 2); };
+// ---------------------------------------------------------------------------
+// Output-stationary 2-D spreading.  A warp owns a PH x PW patch of grid
+// points: its 32 lanes form G = 32 / (PH PW) coil groups, lane l serves point
+// l mod (PH PW) for the group's CPL coils, accumulated in registers, while
+// the warp walks the patch's node list.  Batches of kSpreadBatch list entries
+// (node values of the warp's CC = G CPL coils, window weights, footprint
+// start, density weight) are staged in shared memory by cp.async, double
+// buffered, so the next batch streams in while the current one is summed;
+// each node value reaches its group by a broadcast load.  Two FP32 lanes of a
+// complex accumulator update with one paired FMA (fma.rn.f32x2, the same
+// rounding as two fmaf).  No atomics anywhere: a crowded patch is split into
+// several work items whose partial sums land in `partial` and are added in
+// slot order by patch_reduce_kernel, so results are bitwise reproducible.
+// ---------------------------------------------------------------------------
+constexpr int kSpreadBatch = 8;
 
-template <int CC>
-__host__ __device__ __forceinline__ size_t spread_patch_smem_per_warp(int taps)
+__device__ __forceinline__ void cp_async4(void *dst, const void *src)
 {
-    return (size_t)32 * ((2 * taps + 1) * sizeof(float) + SpreadRow<CC>::v * sizeof(float2) + sizeof(int2) +
-                         sizeof(float));
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst, const void *src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// acc + w * v on both FP32 lanes of a complex value
+__device__ __forceinline__ float2 ffma2(float2 w, float2 v, float2 acc)
+{
+    unsigned long long r;
+    const unsigned long long a = *reinterpret_cast<const unsigned long long *>(&w);
+    const unsigned long long b = *reinterpret_cast<const unsigned long long *>(&v);
+    const unsigned long long c = *reinterpret_cast<const unsigned long long *>(&acc);
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return *reinterpret_cast<float2 *>(&r);
 }
 
-template <int CC>
-__global__ void __launch_bounds__(256)
+template <int PH, int PW, int CPL>
+struct SpreadShape {
+    static constexpr int NPT = PH * PW;                        // points per patch
+    static constexpr int G = 32 / NPT;                         // coil groups per warp
+    static constexpr int CC = G * CPL;                         // coils per warp
+    static constexpr int GS = (CPL % 2 == 0) ? CPL + 2 : CPL;  // group stride (float2): groups 16 B apart in banks
+    static constexpr int VR = G * GS;                          // staged value row per entry (float2)
+    static_assert(NPT * G == 32, "a patch must tile the warp");
+    // one staging buffer: values, weights, footprint starts, density weights
+    __host__ __device__ static size_t buf_bytes(int taps)
+    {
+        return (size_t)kSpreadBatch * (VR * sizeof(float2) + 2 * taps * sizeof(float) + sizeof(int2) + sizeof(float));
+    }
+};
+
+template <int PH, int PW, int CPL>
+__global__ void __launch_bounds__(256, 3)
 spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
                     const float2 *__restrict__ ks, const float *__restrict__ dens, int weighted,
                     float2 *__restrict__ grid)
 {
+    using S = SpreadShape<PH, PW, CPL>;
     extern __shared__ float4 smem4[];
-    constexpr int RS = SpreadRow<CC>::v;                  // value row stride (float2)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wi = blockIdx.x * 8 + warp;
     if (wi >= ps.nwork) return;
     const int taps = 2 * g.m + 2;
-    const int WS = 2 * taps + 1;                          // padded weight row (conflict-free fill)
-    char *base = reinterpret_cast<char *>(smem4) + warp * spread_patch_smem_per_warp<CC>(taps);
-    float2 *sv = reinterpret_cast<float2 *>(base);        // [32][RS]
-    float *sw = reinterpret_cast<float *>(sv + 32 * RS);  // [32][WS]
-    int2 *su = reinterpret_cast<int2 *>(sw + 32 * WS);    // [32]
-    float *sd = reinterpret_cast<float *>(su + 32);       // [32]
-    const int c0 = blockIdx.y * CC;
-    const int ccn = min(CC, g.nc - c0);
+    const int WS = 2 * taps;                               // weights per entry (a multiple of 4)
+    const size_t bb = S::buf_bytes(taps);
+    char *wbase = reinterpret_cast<char *>(smem4) + (size_t)warp * 2 * bb;
+    const int c0 = blockIdx.y * S::CC;
+    const int ccn = min(S::CC, g.nc - c0);
+    const bool v16 = ((g.nc & 1) == 0);                    // node rows 16-byte aligned: two coils per copy
     const int4 wk = ps.work[wi];
     const int n0 = g.n[0], n1 = g.n[1];
-    const int py = (wk.x / ps.npx) * kPatchH + (lane >> 3);
-    const int px = (wk.x % ps.npx) * kPatchW + (lane & 7);
+    const int pt = lane % S::NPT, cg = lane / S::NPT;
+    const int py = (wk.x / ps.npx) * PH + pt / PW;
+    const int px = (wk.x % ps.npx) * PW + pt % PW;
     const bool inside = (py < n0) && (px < n1);
-    const bool wide = (n0 >= taps) && (n1 >= taps);       // no footprint wraps onto itself
-    float ax[CC], ay[CC];
-#pragma unroll
-    for (int c = 0; c < CC; ++c) { ax[c] = 0.f; ay[c] = 0.f; }
-    const int end = wk.y + wk.z;
-    for (int e0 = wk.y; e0 < end; e0 += 32) {
-        const int cnt = min(32, end - e0);
-        // ---- stage: lane l fetches entry e0 + l ----
+    const bool wide = (n0 >= taps) && (n1 >= taps);        // no footprint wraps onto itself
+
+    auto buffers = [&](int buf, float2 *&sv, float *&sw, int2 *&su, float *&sd) {
+        char *b = wbase + (size_t)buf * bb;
+        sv = reinterpret_cast<float2 *>(b);
+        sw = reinterpret_cast<float *>(sv + kSpreadBatch * S::VR);
+        su = reinterpret_cast<int2 *>(sw + kSpreadBatch * WS);
+        sd = reinterpret_cast<float *>(su + kSpreadBatch);
+    };
+    // queue the copies of entries [e0, e0 + cnt) into buffer `buf`
+    auto issue = [&](int e0, int cnt, int buf) {
+        float2 *sv; float *sw; int2 *su; float *sd;
+        buffers(buf, sv, sw, su, sd);
+        const int s_l = (lane < cnt) ? ps.entries[e0 + lane] : 0;
         if (lane < cnt) {
-            const int s = ps.entries[e0 + lane];
-            su[lane] = ps.nodeU[s];
-            sd[lane] = weighted ? dens[s] : 1.f;
-            const float2 *W2 = reinterpret_cast<const float2 *>(ps.nodeW + (size_t)s * 2 * taps);
-            for (int q = 0; q < taps; ++q) {
-                const float2 w = W2[q];
-                sw[lane * WS + 2 * q] = w.x;
-                sw[lane * WS + 2 * q + 1] = w.y;
-            }
-            const float2 *v = ks + (size_t)s * g.nc + c0;
-#pragma unroll
-            for (int c = 0; c < CC; ++c)
-                sv[lane * RS + c] = (c < ccn) ? v[c] : make_float2(0.f, 0.f);
+            cp_async8(&su[lane], &ps.nodeU[s_l]);
+            if (weighted) cp_async4(&sd[lane], &dens[s_l]);
+            else sd[lane] = 1.f;
+            const float *W = ps.nodeW + (size_t)s_l * WS;
+            for (int q = 0; q < WS; q += 4) cp_async16(&sw[lane * WS + q], W + q);
         }
+        for (int j = 0; j < cnt; ++j) {
+            const int s = __shfl_sync(0xffffffffu, s_l, j);
+            const float2 *v = ks + (size_t)s * g.nc + c0;
+            float2 *dv = sv + j * S::VR;
+            if (v16 && (S::CC % 2 == 0)) {
+                const int c = 2 * lane;
+                if (c < S::CC) {
+                    float2 *d = dv + (c / CPL) * S::GS + (c % CPL);
+                    if (c + 1 < ccn) cp_async16(d, v + c);
+                    else if (c < ccn) { cp_async8(d, v + c); d[1] = make_float2(0.f, 0.f); }
+                    else { d[0] = make_float2(0.f, 0.f); d[1] = make_float2(0.f, 0.f); }
+                }
+            } else {
+                for (int c = lane; c < S::CC; c += 32) {
+                    float2 *d = dv + (c / CPL) * S::GS + (c % CPL);
+                    if (c < ccn) cp_async8(d, v + c);
+                    else *d = make_float2(0.f, 0.f);
+                }
+            }
+        }
+        cp_async_commit();
+    };
+
+    float2 acc[CPL];
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) acc[k] = make_float2(0.f, 0.f);
+    const int end = wk.y + wk.z;
+    int e0 = wk.y, cnt = min(kSpreadBatch, end - e0), buf = 0;
+    issue(e0, cnt, 0);
+    while (true) {
+        const int e1 = e0 + cnt;
+        const int cnt1 = min(kSpreadBatch, end - e1);
+        if (cnt1 > 0) { issue(e1, cnt1, buf ^ 1); cp_async_wait<1>(); }
+        else cp_async_wait<0>();
         __syncwarp();
-        // ---- accumulate ----
+        float2 *sv; float *sw; int2 *su; float *sd;
+        buffers(buf, sv, sw, su, sd);
         for (int i = 0; i < cnt; ++i) {
             const int2 u = su[i];
             float w = 0.f;
@@ -334,49 +405,50 @@ spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ 
                 }
                 w = wy * wx * sd[i];
             }
-            if constexpr ((CC & 1) == 0) {
-                const float4 *v = reinterpret_cast<const float4 *>(sv + i * RS);
+            const float2 ww = make_float2(w, w);
+            const float2 *vr = sv + i * S::VR + cg * S::GS;
+            if constexpr (CPL % 2 == 0) {
+                const float4 *v4 = reinterpret_cast<const float4 *>(vr);
 #pragma unroll
-                for (int c = 0; c < CC / 2; ++c) {
-                    const float4 q = v[c];
-                    ax[2 * c] = fmaf(w, q.x, ax[2 * c]); ay[2 * c] = fmaf(w, q.y, ay[2 * c]);
-                    ax[2 * c + 1] = fmaf(w, q.z, ax[2 * c + 1]); ay[2 * c + 1] = fmaf(w, q.w, ay[2 * c + 1]);
+                for (int k = 0; k < CPL / 2; ++k) {
+                    const float4 q = v4[k];
+                    acc[2 * k] = ffma2(ww, make_float2(q.x, q.y), acc[2 * k]);
+                    acc[2 * k + 1] = ffma2(ww, make_float2(q.z, q.w), acc[2 * k + 1]);
                 }
             } else {
-                const float2 *v = sv + i * RS;
 #pragma unroll
-                for (int c = 0; c < CC; ++c) {
-                    const float2 q = v[c];
-                    ax[c] = fmaf(w, q.x, ax[c]); ay[c] = fmaf(w, q.y, ay[c]);
-                }
+                for (int k = 0; k < CPL; ++k) acc[k] = ffma2(ww, vr[k], acc[k]);
             }
         }
         __syncwarp();
+        if (cnt1 <= 0) break;
+        e0 = e1; cnt = cnt1; buf ^= 1;
     }
     if (!inside) return;
-    float2 *dst = (wk.w < 0) ? grid + ((size_t)py * n1 + px) * g.nc + c0
-                             : ps.partial + ((size_t)wk.w * 32 + lane) * g.nc + c0;
+    const int cb = c0 + cg * CPL;                          // first coil of this lane's group
+    float2 *dst = (wk.w < 0) ? grid + ((size_t)py * n1 + px) * g.nc + cb
+                             : ps.partial + ((size_t)wk.w * S::NPT + pt) * g.nc + cb;
 #pragma unroll
-    for (int c = 0; c < CC; ++c)
-        if (c < ccn) dst[c] = make_float2(ax[c], ay[c]);
+    for (int k = 0; k < CPL; ++k)
+        if (cg * CPL + k < ccn) dst[k] = acc[k];
 }
 
 // sum the partial slots of split patches in slot order and store them
 __global__ void patch_reduce_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
                                     float2 *__restrict__ grid)
 {
-    const int nc = g.nc;
-    const int64_t total = (int64_t)ps.nmulti * 32 * nc;
+    const int nc = g.nc, npt = ps.ph * ps.pw;
+    const int64_t total = (int64_t)ps.nmulti * npt * nc;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
         const int c = (int)(e % nc);
-        const int lane = (int)((e / nc) % 32);
-        const int4 mu = ps.multi[e / ((int64_t)32 * nc)];
-        const int py = (mu.x / ps.npx) * kPatchH + (lane >> 3);
-        const int px = (mu.x % ps.npx) * kPatchW + (lane & 7);
+        const int pt = (int)((e / nc) % npt);
+        const int4 mu = ps.multi[e / ((int64_t)npt * nc)];
+        const int py = (mu.x / ps.npx) * ps.ph + pt / ps.pw;
+        const int px = (mu.x % ps.npx) * ps.pw + pt % ps.pw;
         if (py >= g.n[0] || px >= g.n[1]) continue;
         float sx = 0.f, sy = 0.f;
         for (int k = 0; k < mu.z; ++k) {
-            const float2 v = ps.partial[((size_t)(mu.y + k) * 32 + lane) * nc + c];
+            const float2 v = ps.partial[((size_t)(mu.y + k) * npt + pt) * nc + c];
             sx += v.x; sy += v.y;
         }
         grid[((size_t)py * g.n[1] + px) * nc + c] = make_float2(sx, sy);
@@ -550,31 +622,43 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
                                int weighted, float2 *grid, cudaStream_t st)
 {
     if (ps.nwork == 0) return CGS_OK;
-    const int CC = g.scc > 0 ? g.scc
-                             : (g.nc >= 32 ? 32 : (g.nc >= 16 ? 16 : (g.nc >= 8 ? 8 : (g.nc >= 4 ? 4 : (g.nc >= 2 ? 2 : 1)))));
     const int taps = 2 * g.m + 2;
     if (taps > kMaxTaps) { set_error("m too large"); return CGS_ERR_BAD_ARG; }
+    // coils per warp: the next power of two >= coils (at most 32), or the tuned value
+    int CC = 1;
+    if (ps.pw == 8) {
+        CC = 1;
+    } else {
+        CC = 2;
+        while (CC < g.nc && CC < 32) CC *= 2;
+        if (g.scc > 0) CC = g.scc < 2 ? 2 : g.scc;
+    }
     dim3 grd((ps.nwork + 7) / 8, (g.nc + CC - 1) / CC);
     prof_begin(PROF_SPREAD, st);
-#define CGS_SP(CCV)                                                                                        \
-    do {                                                                                                 \
-        const size_t sm = 8 * spread_patch_smem_per_warp<CCV>(taps);                                     \
-        CGS_CUDA(cudaFuncSetAttribute(spread_patch_kernel<CCV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                      (int)sm));                                                          \
-        spread_patch_kernel<CCV><<<grd, 256, sm, st>>>(g, ps, ks, dens, weighted, grid);                   \
+#define CGS_SP(PHV, PWV, CPLV)                                                                              \
+    do {                                                                                                  \
+        const size_t sm = 8 * 2 * SpreadShape<PHV, PWV, CPLV>::buf_bytes(taps);                           \
+        CGS_CUDA(cudaFuncSetAttribute(spread_patch_kernel<PHV, PWV, CPLV>,                                 \
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));             \
+        spread_patch_kernel<PHV, PWV, CPLV><<<grd, 256, sm, st>>>(g, ps, ks, dens, weighted, grid);        \
     } while (0)
-    switch (CC) {
-        case 32: CGS_SP(32); break;
-        case 16: CGS_SP(16); break;
-        case 8: CGS_SP(8); break;
-        case 4: CGS_SP(4); break;
-        case 2: CGS_SP(2); break;
-        default: CGS_SP(1); break;
+    if (ps.pw == 8) {
+        if (ps.ph != 4) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
+        CGS_SP(4, 8, 1);
+    } else {
+        if (ps.ph != 4 || ps.pw != 4) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
+        switch (CC) {
+            case 32: CGS_SP(4, 4, 16); break;
+            case 16: CGS_SP(4, 4, 8); break;
+            case 8: CGS_SP(4, 4, 4); break;
+            case 4: CGS_SP(4, 4, 2); break;
+            default: CGS_SP(4, 4, 1); break;
+        }
     }
 #undef CGS_SP
     CGS_LAUNCH_CHECK();
     if (ps.nmulti > 0) {
-        const int64_t total = (int64_t)ps.nmulti * 32 * g.nc;
+        const int64_t total = (int64_t)ps.nmulti * ps.ph * ps.pw * g.nc;
         const int64_t blocks = std::min<int64_t>((total + 255) / 256, 152 * 16);
         patch_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, ps, grid);
         CGS_LAUNCH_CHECK();

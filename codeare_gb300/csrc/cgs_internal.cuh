@@ -145,18 +145,20 @@ struct NodeSet {
     const float *nodeW; // 2-D: per node [2][2m+2] window weights (nullable)
 };
 
-// Output-stationary 2-D spreading: one warp per work item over a PH x PW patch
-// of grid points (lane = point), FP32 accumulators for a coil chunk in
-// registers, walking the list of nodes whose footprint covers the patch.
-constexpr int kPatchH = 4, kPatchW = 8;
+// Output-stationary 2-D spreading: one warp per work item over a ph x pw patch
+// of grid points (32 / (ph pw) coil groups of lanes, lane = point within its
+// group), FP32 accumulators for the group's coils in registers, walking the
+// list of nodes whose footprint covers the patch.  Patches are 4 x 4 (two coil
+// groups) for several coils and 4 x 8 (one group) for a single coil.
 struct PatchSet {
+    int ph, pw;            // patch rows and columns
     int npx;               // patches per grid row
     int nwork;             // work items
     const int *entries;    // node (sorted index) lists, patch after patch
     const int4 *work;      // {patch, first entry, count, partial slot or -1}
     const int2 *nodeU;     // per node: wrapped footprint start (u0, u1)
     const float *nodeW;    // per node: [2][2m+2] window weights
-    float2 *partial;       // [slot][32 points][nc] partial sums of split patches
+    float2 *partial;       // [slot][ph pw points][nc] partial sums of split patches
     int nmulti;            // patches split into several slots
     const int4 *multi;     // {patch, first slot, slots, 0}
 };

@@ -426,7 +426,7 @@ void apply_tiles(cgs_plan *p)
     g.scc = p->tune.spread_coils;
 }
 
-// Per 4 x 8 patch of the 2-D grid, the sorted indices of the nodes whose
+// Per 4 x 4 patch (4 x 8 for one coil) of the 2-D grid, the sorted indices of the nodes whose
 // footprint (2m+2 taps per axis, wrapped) covers any point of the patch; work
 // items of at most `chunk` nodes, crowded patches spread over several partial
 // slots; node weights precomputed on the device.  `cc` holds each node's
@@ -434,6 +434,7 @@ void apply_tiles(cgs_plan *p)
 cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
 {
     const int n0 = p->n[0], n1 = p->n[1], m = p->m, taps = 2 * m + 2;
+    const int kPatchH = 4, kPatchW = p->nc > 1 ? 4 : 8;
     const int npy = (n0 + kPatchH - 1) / kPatchH, npx = (n1 + kPatchW - 1) / kPatchW;
     const int64_t P = (int64_t)npy * npx, M = p->M;
     std::vector<int> perm(M);
@@ -500,7 +501,7 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     CGS_TRY(dev_alloc(&p->pentries, entries.size()));
     CGS_TRY(dev_alloc(&p->pwork, work.size()));
     CGS_TRY(dev_alloc(&p->pmulti, std::max<size_t>(1, multi.size())));
-    CGS_TRY(dev_alloc(&p->ppartial, (size_t)std::max(slots, 1) * 32 * p->nc));
+    CGS_TRY(dev_alloc(&p->ppartial, (size_t)std::max(slots, 1) * kPatchH * kPatchW * p->nc));
     CGS_CUDA(cudaMemcpy(p->pentries, entries.data(), sizeof(int) * entries.size(), cudaMemcpyHostToDevice));
     CGS_CUDA(cudaMemcpy(p->pwork, work.data(), sizeof(int4) * work.size(), cudaMemcpyHostToDevice));
     if (!multi.empty())
@@ -509,6 +510,8 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     CGS_TRY(launch_node_weights(p->geom, ns, p->nodeU, p->nodeW, p->stream));
     CGS_CUDA(cudaStreamSynchronize(p->stream));
     PatchSet &ps = p->pset;
+    ps.ph = kPatchH;
+    ps.pw = kPatchW;
     ps.npx = npx;
     ps.nwork = (int)work.size();
     ps.entries = p->pentries;
