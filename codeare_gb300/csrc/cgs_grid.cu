@@ -457,17 +457,20 @@ __global__ void patch_reduce_kernel(const __grid_constant__ GridGeom g, const __
 
 // ---------------------------------------------------------------------------
 // 2-D interpolation with the coil index on the lanes.  A CTA stages the padded
-// (T+2m+1)^2 tile of CC coils ([point][coil], coil innermost); a group of CC
-// lanes serves one node, so every tap is one conflict-free read of CC
-// consecutive complex values, and the node's 2 x TAPS weights (precomputed
-// once per trajectory) sit in registers.
+// (T+2m+1)^2 tile of CC coils ([point][coil], coil innermost); a group of
+// CC / CPL lanes serves one node, each lane CPL consecutive coils, so every
+// tap is one read of CC consecutive complex values (for CC = 16, CPL = 2: one
+// full 128-byte bank row per node, conflict-free), and the node's 2 x TAPS
+// weights (precomputed once per trajectory) sit in registers.  The complex
+// multiply-adds are paired FP32 FMAs (the rounding of two fmaf).
 // ---------------------------------------------------------------------------
-template <int TAPS, int CC>
+template <int TAPS, int CC, int CPL>
 __global__ void __launch_bounds__(256)
 interp2_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
                const int2 *__restrict__ nodeU, const float *__restrict__ nodeW,
                const float2 *__restrict__ grid, float2 *__restrict__ ks)
 {
+    static_assert(CC % CPL == 0 && 32 % (CC / CPL) == 0, "coil lanes must tile the warp");
     extern __shared__ float4 smem4[];
     float2 *tile = reinterpret_cast<float2 *>(smem4);
     const int E = g.T + TAPS - 1;
@@ -493,8 +496,9 @@ interp2_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeS
             if (e0 + u * 256 < tot) tile[e0 + u * 256] = v[u];
     }
     __syncthreads();
-    constexpr int NPW = 32 / CC;           // nodes served by one warp at a time
-    const int lane = threadIdx.x & 31, c = lane % CC, slot = lane / CC;
+    constexpr int LPN = CC / CPL;          // lanes per node
+    constexpr int NPW = 32 / LPN;          // nodes served by one warp at a time
+    const int lane = threadIdx.x & 31, cl = lane % LPN, slot = lane / LPN;
     const int warp = threadIdx.x >> 5;
     for (int i = warp * NPW + slot; i < wk.z; i += 8 * NPW) {
         const int64_t s = (int64_t)wk.y + i;
@@ -504,19 +508,369 @@ interp2_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeS
         float w0[TAPS], w1[TAPS];
 #pragma unroll
         for (int q = 0; q < TAPS; ++q) { w0[q] = W[q]; w1[q] = W[TAPS + q]; }
-        float ax = 0.f, ay = 0.f;
+        float2 acc[CPL];
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) acc[k] = make_float2(0.f, 0.f);
 #pragma unroll
         for (int a = 0; a < TAPS; ++a) {
-            const float2 *row = tile + ((y0 + a) * E + x0) * CC + c;
-            float rx = 0.f, ry = 0.f;
+            const float2 *row = tile + ((y0 + a) * E + x0) * CC + cl * CPL;
+            float2 r[CPL];
+#pragma unroll
+            for (int k = 0; k < CPL; ++k) r[k] = make_float2(0.f, 0.f);
 #pragma unroll
             for (int b = 0; b < TAPS; ++b) {
-                const float2 v = row[b * CC];
-                rx = fmaf(w1[b], v.x, rx); ry = fmaf(w1[b], v.y, ry);
+                const float2 wb = make_float2(w1[b], w1[b]);
+                if constexpr (CPL == 2) {
+                    const float4 q = *reinterpret_cast<const float4 *>(row + b * CC);
+                    r[0] = ffma2(wb, make_float2(q.x, q.y), r[0]);
+                    r[1] = ffma2(wb, make_float2(q.z, q.w), r[1]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < CPL; ++k) r[k] = ffma2(wb, row[b * CC + k], r[k]);
+                }
             }
-            ax = fmaf(w0[a], rx, ax); ay = fmaf(w0[a], ry, ay);
+            const float2 wa = make_float2(w0[a], w0[a]);
+#pragma unroll
+            for (int k = 0; k < CPL; ++k) acc[k] = ffma2(wa, r[k], acc[k]);
         }
-        if (c < ccn) ks[s * g.nc + c0 + c] = make_float2(ax, ay);
+#pragma unroll
+        for (int k = 0; k < CPL; ++k)
+            if (cl * CPL + k < ccn) ks[s * g.nc + c0 + cl * CPL + k] = acc[k];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 3-D gridding, one warp per node.  A CTA owns a bin of footprint starts (T^3)
+// and its padded E^3 tile (E = T + 2m + 1) for CC coils in shared memory,
+// stored as planes of real and imaginary parts, [coil][part][z][y][x] with an
+// x pitch PX >= E chosen on the host so that the TAPS x (32 / TAPS) points a
+// warp touches in one step fall in distinct banks.  A warp takes one node at
+// a time: its lanes evaluate the node's 3 x TAPS window weights (one per
+// lane), then lane (row, x) of every y-step walks the TAPS z-planes of its
+// (y, x) column with the z weights in registers.
+//   interpolation: each lane accumulates its taps, then a warp reduction;
+//   spreading: shared-memory atomics into the tile (conflict-free within a
+//   step; other warps may hit the same point), then one atomic flush of the
+//   tile into the grid per work item.
+// ---------------------------------------------------------------------------
+template <bool SPREAD, int TAPS, int CC>
+__global__ void __launch_bounds__(256)
+grid3_warp_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
+                  const float2 *__restrict__ in, int weighted, float2 *__restrict__ out, int PX)
+{
+    constexpr int RPI = 32 / TAPS;                     // x-rows per step
+    constexpr int NSTEP = (TAPS + RPI - 1) / RPI;      // steps over the y taps
+    extern __shared__ float4 smem4[];
+    const int E = g.T + TAPS - 1;
+    const int EE = E * E * E;
+    const int plane = E * E * PX;                      // floats per (coil, part) plane
+    const int4 wk = ns.work[blockIdx.x];
+    const int c0 = blockIdx.y * CC;
+    const int ccn = min(CC, g.nc - c0);
+    const int org2 = (wk.x % g.nt[2]) * g.T;
+    const int org1 = ((wk.x / g.nt[2]) % g.nt[1]) * g.T;
+    const int org0 = (wk.x / (g.nt[2] * g.nt[1])) * g.T;
+    float *tile = reinterpret_cast<float *>(smem4);
+    float *wsm = tile + (size_t)CC * 2 * plane;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float *W = wsm + warp * 3 * TAPS;
+    auto grid_off = [&](int r) {
+        const int lz = r / (E * E), ly = (r / E) % E, lx = r % E;
+        return ((int64_t)wrapi(org0 + lz, g.n[0]) * g.n[1] + wrapi(org1 + ly, g.n[1])) * g.n[2] + wrapi(org2 + lx, g.n[2]);
+    };
+    auto tile_off = [&](int r) {
+        const int lz = r / (E * E), ly = (r / E) % E, lx = r % E;
+        return (lz * E + ly) * PX + lx;
+    };
+
+    // tile: zeros (spreading) or the grid values (interpolation), batches of
+    // kUnroll independent loads per thread in flight
+    constexpr int kUnroll = 8;
+    for (int e0 = threadIdx.x; e0 < EE * CC; e0 += 256 * kUnroll) {
+        float2 v[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const int e = e0 + u * 256;
+            const int cc = e % CC;
+            v[u] = make_float2(0.f, 0.f);
+            if (!SPREAD && e < EE * CC && cc < ccn) v[u] = in[grid_off(e / CC) * g.nc + c0 + cc];
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const int e = e0 + u * 256;
+            if (e < EE * CC) {
+                const int cc = e % CC, t = tile_off(e / CC);
+                tile[(2 * cc) * plane + t] = v[u].x;
+                tile[(2 * cc + 1) * plane + t] = v[u].y;
+            }
+        }
+    }
+    __syncthreads();
+
+    const float mf = (float)g.m;
+    const int ry = lane / TAPS, rx = lane % TAPS;
+    const bool act = ry < RPI;
+    for (int i = warp; i < wk.z; i += 8) {
+        const int64_t s = (int64_t)wk.y + i;
+        const float4 na = ns.nodes[2 * s], nb = ns.nodes[2 * s + 1];
+        const int l0 = wrapi(__float_as_int(nb.x) - g.m, g.n[0]) - org0;
+        const int l1 = wrapi(__float_as_int(nb.y) - g.m, g.n[1]) - org1;
+        const int l2 = wrapi(__float_as_int(nb.z) - g.m, g.n[2]) - org2;
+        for (int e = lane; e < 3 * TAPS; e += 32) {
+            const int t = e / TAPS, q = e % TAPS;
+            const float ft = t == 0 ? na.x : (t == 1 ? na.y : na.z);
+            const float bt = t == 0 ? g.b[0] : (t == 1 ? g.b[1] : g.b[2]);
+            W[e] = kb_phi(ft + mf - (float)q, mf, bt);
+        }
+        __syncwarp();
+        float wz[TAPS];
+#pragma unroll
+        for (int q = 0; q < TAPS; ++q) wz[q] = W[q];
+        const float wx = act ? W[2 * TAPS + rx] : 0.f;
+        float2 v[CC];
+        if (SPREAD) {
+            const float dw = (weighted && ns.w) ? ns.w[s] : 1.f;
+#pragma unroll
+            for (int cc = 0; cc < CC; ++cc) {
+                v[cc] = cc < ccn ? in[s * g.nc + c0 + cc] : make_float2(0.f, 0.f);
+                v[cc].x *= dw; v[cc].y *= dw;
+            }
+        } else {
+#pragma unroll
+            for (int cc = 0; cc < CC; ++cc) v[cc] = make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int st = 0; st < NSTEP; ++st) {
+            const int b = st * RPI + ry;
+            if (act && b < TAPS) {
+                const float wyx = W[TAPS + b] * wx;
+                const int base = (l0 * E + l1 + b) * PX + l2 + rx;
+#pragma unroll
+                for (int a = 0; a < TAPS; ++a) {
+                    const float w = wz[a] * wyx;
+                    const int t = base + a * E * PX;
+#pragma unroll
+                    for (int cc = 0; cc < CC; ++cc) {
+                        float *re = tile + (2 * cc) * plane + t;
+                        float *im = tile + (2 * cc + 1) * plane + t;
+                        if (SPREAD) {
+                            atomicAdd(re, w * v[cc].x);
+                            atomicAdd(im, w * v[cc].y);
+                        } else {
+                            v[cc].x = fmaf(w, *re, v[cc].x);
+                            v[cc].y = fmaf(w, *im, v[cc].y);
+                        }
+                    }
+                }
+            }
+        }
+        if (!SPREAD) {
+#pragma unroll
+            for (int cc = 0; cc < CC; ++cc) {
+                float x = v[cc].x, y = v[cc].y;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    x += __shfl_down_sync(0xffffffffu, x, o);
+                    y += __shfl_down_sync(0xffffffffu, y, o);
+                }
+                if (lane == 0 && cc < ccn) out[s * g.nc + c0 + cc] = make_float2(x, y);
+            }
+        }
+        __syncwarp();
+    }
+    if (!SPREAD) return;
+    __syncthreads();
+    // add the tile to the grid (wrapped)
+    for (int e = threadIdx.x; e < EE * CC; e += 256) {
+        const int cc = e % CC;
+        if (cc >= ccn) continue;
+        const int t = tile_off(e / CC);
+        const float vx = tile[(2 * cc) * plane + t], vy = tile[(2 * cc + 1) * plane + t];
+        if (vx == 0.f && vy == 0.f) continue;
+        float2 *dst = out + grid_off(e / CC) * g.nc + c0 + cc;
+        atomicAdd(&dst->x, vx);
+        atomicAdd(&dst->y, vy);
+    }
+}
+
+// 3-D spreading without atomics in shared memory: the tile's z-planes are
+// dealt round-robin to the CTA's 8 warps, every warp walks every staged node
+// and adds only the node's taps in its own planes (plain read-modify-write:
+// no two warps share a plane, no two lanes of a step share a point).  Batches
+// of kStage3 nodes (window weights, footprint starts, density-weighted
+// values) are staged for the whole CTA; the tile is flushed into the grid
+// with one atomic add per point and coil.
+constexpr int kStage3 = 32;
+
+template <int TAPS, int CC>
+__global__ void __launch_bounds__(256)
+spread3_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
+               const float2 *__restrict__ ks, int weighted, float2 *__restrict__ grid, int PX)
+{
+    constexpr int RPI = 32 / TAPS;
+    constexpr int NSTEP = (TAPS + RPI - 1) / RPI;
+    extern __shared__ float4 smem4[];
+    const int E = g.T + TAPS - 1;
+    const int EE = E * E * E;
+    const int plane = E * E * PX;
+    const int4 wk = ns.work[blockIdx.x];
+    const int c0 = blockIdx.y * CC;
+    const int ccn = min(CC, g.nc - c0);
+    const int org2 = (wk.x % g.nt[2]) * g.T;
+    const int org1 = ((wk.x / g.nt[2]) % g.nt[1]) * g.T;
+    const int org0 = (wk.x / (g.nt[2] * g.nt[1])) * g.T;
+    float *tile = reinterpret_cast<float *>(smem4);
+    float *sW = tile + (size_t)CC * 2 * plane;                   // [kStage3][3 TAPS]
+    float2 *sV = reinterpret_cast<float2 *>(sW + kStage3 * 3 * TAPS);  // [kStage3][CC]
+    int *sL = reinterpret_cast<int *>(sV + kStage3 * CC);        // [kStage3][3]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int e = threadIdx.x; e < CC * 2 * plane; e += 256) tile[e] = 0.f;
+
+    const float mf = (float)g.m;
+    const int ry = lane / TAPS, rx = lane % TAPS;
+    const bool act = ry < RPI;
+    for (int j0 = 0; j0 < wk.z; j0 += kStage3) {
+        const int cnt = min(kStage3, wk.z - j0);
+        __syncthreads();   // the previous batch is consumed (and the tile zeroed)
+        for (int e = threadIdx.x; e < cnt * 3 * TAPS; e += 256) {
+            const int j = e / (3 * TAPS), r = e % (3 * TAPS), t = r / TAPS, q = r % TAPS;
+            const int64_t s = (int64_t)wk.y + j0 + j;
+            const float4 na = ns.nodes[2 * s];
+            const float ft = t == 0 ? na.x : (t == 1 ? na.y : na.z);
+            const float bt = t == 0 ? g.b[0] : (t == 1 ? g.b[1] : g.b[2]);
+            sW[e] = kb_phi(ft + mf - (float)q, mf, bt);
+        }
+        for (int e = threadIdx.x; e < cnt * CC; e += 256) {
+            const int j = e / CC, cc = e % CC;
+            const int64_t s = (int64_t)wk.y + j0 + j;
+            float2 v = cc < ccn ? ks[s * g.nc + c0 + cc] : make_float2(0.f, 0.f);
+            const float dw = (weighted && ns.w) ? ns.w[s] : 1.f;
+            v.x *= dw; v.y *= dw;
+            sV[e] = v;
+        }
+        for (int j = threadIdx.x; j < cnt; j += 256) {
+            const int64_t s = (int64_t)wk.y + j0 + j;
+            const float4 nb = ns.nodes[2 * s + 1];
+            sL[3 * j] = wrapi(__float_as_int(nb.x) - g.m, g.n[0]) - org0;
+            sL[3 * j + 1] = wrapi(__float_as_int(nb.y) - g.m, g.n[1]) - org1;
+            sL[3 * j + 2] = wrapi(__float_as_int(nb.z) - g.m, g.n[2]) - org2;
+        }
+        __syncthreads();
+        for (int j = 0; j < cnt; ++j) {
+            const int l0 = sL[3 * j], l1 = sL[3 * j + 1], l2 = sL[3 * j + 2];
+            const float *W = sW + j * 3 * TAPS;
+            const float wx = act ? W[2 * TAPS + rx] : 0.f;
+            float2 v[CC];
+#pragma unroll
+            for (int cc = 0; cc < CC; ++cc) v[cc] = sV[j * CC + cc];
+            // this warp's planes z = l0 + a with z % 8 == warp
+            for (int a = ((warp - l0) % 8 + 8) % 8; a < TAPS; a += 8) {
+                const float wz = W[a];
+#pragma unroll
+                for (int st = 0; st < NSTEP; ++st) {
+                    const int b = st * RPI + ry;
+                    if (act && b < TAPS) {
+                        const float w = wz * W[TAPS + b] * wx;
+                        const int t = ((l0 + a) * E + l1 + b) * PX + l2 + rx;
+#pragma unroll
+                        for (int cc = 0; cc < CC; ++cc) {
+                            float *re = tile + (2 * cc) * plane + t;
+                            float *im = tile + (2 * cc + 1) * plane + t;
+                            *re = fmaf(w, v[cc].x, *re);
+                            *im = fmaf(w, v[cc].y, *im);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < EE * CC; e += 256) {
+        const int cc = e % CC;
+        if (cc >= ccn) continue;
+        const int r = e / CC;
+        const int lz = r / (E * E), ly = (r / E) % E, lx = r % E;
+        const int t = (lz * E + ly) * PX + lx;
+        const float vx = tile[(2 * cc) * plane + t], vy = tile[(2 * cc + 1) * plane + t];
+        if (vx == 0.f && vy == 0.f) continue;
+        const int64_t off = ((int64_t)wrapi(org0 + lz, g.n[0]) * g.n[1] + wrapi(org1 + ly, g.n[1])) * g.n[2] +
+                            wrapi(org2 + lx, g.n[2]);
+        float2 *dst = grid + off * g.nc + c0 + cc;
+        atomicAdd(&dst->x, vx);
+        atomicAdd(&dst->y, vy);
+    }
+}
+
+// x pitch of the 3-D tile planes: the smallest PX >= E for which the
+// (32 / taps) rows x taps points of one warp step fall in distinct banks
+int grid3_pitch(int E, int taps)
+{
+    const int rpi = 32 / taps;
+    for (int px = E; px < E + 32; ++px) {
+        bool used[32] = {false};
+        bool ok = true;
+        for (int r = 0; r < rpi && ok; ++r)
+            for (int x = 0; x < taps && ok; ++x) {
+                const int bank = (r * px + x) % 32;
+                ok = !used[bank];
+                used[bank] = true;
+            }
+        if (ok) return px;
+    }
+    return E;
+}
+
+size_t grid3_smem(int E, int PX, int taps, int CC)
+{
+    // tile planes + the larger of the interpolation per-warp weights and the
+    // spreading node batch (weights, values, footprint starts)
+    const size_t stage = std::max<size_t>((size_t)8 * 3 * taps * sizeof(float),
+                                          (size_t)kStage3 * (3 * taps * sizeof(float) + CC * sizeof(float2) + 3 * sizeof(int)));
+    return (size_t)CC * 2 * E * E * PX * sizeof(float) + stage;
+}
+
+template <bool SPREAD, int TAPS>
+cgs_status launch_grid3_taps(const GridGeom &g, const NodeSet &ns, const float2 *in, int weighted, float2 *out,
+                             cudaStream_t st)
+{
+    const int E = g.T + TAPS - 1;
+    const int PX = grid3_pitch(E, TAPS);
+    const int CC = (g.nc >= 2 && grid3_smem(E, PX, TAPS, 2) <= 110 * 1024) ? 2 : 1;
+    const size_t smem = grid3_smem(E, PX, TAPS, CC);
+    if (smem > 200 * 1024) { set_error("3-D gridding tile does not fit in shared memory"); return CGS_ERR_BAD_ARG; }
+    dim3 grd(ns.nwork, (g.nc + CC - 1) / CC);
+#define CGS_G3(CCV)                                                                                         \
+    do {                                                                                                  \
+        if (SPREAD) {                                                                                     \
+            CGS_CUDA(cudaFuncSetAttribute(spread3_kernel<TAPS, CCV>,                                       \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));       \
+            spread3_kernel<TAPS, CCV><<<grd, 256, smem, st>>>(g, ns, in, weighted, out, PX);               \
+        } else {                                                                                          \
+            CGS_CUDA(cudaFuncSetAttribute(grid3_warp_kernel<false, TAPS, CCV>,                             \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));       \
+            grid3_warp_kernel<false, TAPS, CCV><<<grd, 256, smem, st>>>(g, ns, in, weighted, out, PX);     \
+        }                                                                                                 \
+    } while (0)
+    if (CC == 2) CGS_G3(2);
+    else CGS_G3(1);
+#undef CGS_G3
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+template <bool SPREAD>
+cgs_status launch_grid3(const GridGeom &g, const NodeSet &ns, const float2 *in, int weighted, float2 *out,
+                        cudaStream_t st)
+{
+    switch (2 * g.m + 2) {
+        case 4: return launch_grid3_taps<SPREAD, 4>(g, ns, in, weighted, out, st);
+        case 6: return launch_grid3_taps<SPREAD, 6>(g, ns, in, weighted, out, st);
+        case 8: return launch_grid3_taps<SPREAD, 8>(g, ns, in, weighted, out, st);
+        case 10: return launch_grid3_taps<SPREAD, 10>(g, ns, in, weighted, out, st);
+        case 12: return launch_grid3_taps<SPREAD, 12>(g, ns, in, weighted, out, st);
+        case 14: return launch_grid3_taps<SPREAD, 14>(g, ns, in, weighted, out, st);
+        case 16: return launch_grid3_taps<SPREAD, 16>(g, ns, in, weighted, out, st);
+        default: set_error("m too large for 3-D gridding"); return CGS_ERR_BAD_ARG;
     }
 }
 
@@ -552,16 +906,17 @@ cgs_status launch_interp2_taps(const GridGeom &g, const NodeSet &ns, const float
     const int E = g.T + TAPS - 1;
     const size_t smem = (size_t)E * E * CC * sizeof(float2);
     dim3 grd(ns.nwork, (g.nc + CC - 1) / CC);
-#define CGS_I2(CCV)                                                                                         \
+#define CGS_I2(CCV, CPLV)                                                                                   \
     do {                                                                                                  \
-        CGS_CUDA(cudaFuncSetAttribute(interp2_kernel<TAPS, CCV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                      (int)smem));                                                         \
-        interp2_kernel<TAPS, CCV><<<grd, 256, smem, st>>>(g, ns, ns.nodeU, ns.nodeW, grid, ks);            \
+        CGS_CUDA(cudaFuncSetAttribute(interp2_kernel<TAPS, CCV, CPLV>,                                     \
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));           \
+        interp2_kernel<TAPS, CCV, CPLV><<<grd, 256, smem, st>>>(g, ns, ns.nodeU, ns.nodeW, grid, ks);      \
     } while (0)
-    if (CC == 16) CGS_I2(16);
-    else if (CC == 8) CGS_I2(8);
-    else if (CC == 4) CGS_I2(4);
-    else CGS_I2(1);
+    if (CC == 32) CGS_I2(32, 2);
+    else if (CC == 16) CGS_I2(16, 2);
+    else if (CC == 8) CGS_I2(8, 2);
+    else if (CC == 4) CGS_I2(4, 2);
+    else CGS_I2(1, 1);
 #undef CGS_I2
     CGS_LAUNCH_CHECK();
     return CGS_OK;
@@ -574,8 +929,9 @@ cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *gri
     if (2 * g.m + 2 > kMaxTaps) { set_error("m too large"); return CGS_ERR_BAD_ARG; }
     const int taps = 2 * g.m + 2;
     if (g.d == 2 && ns.nodeU && ns.nodeW && taps <= 10) {
-        // 8 coils per CTA by default: 40 KB tiles leave room for 4 CTAs per SM
-        const int CC = g.icc > 0 ? g.icc : (g.nc >= 8 ? 8 : (g.nc >= 4 ? 4 : 1));
+        // 16 coils per CTA by default: a 46 KB tile (T = 16, m = 4) leaves room
+        // for 4 CTAs per SM, and each node reads one full bank row per tap
+        const int CC = g.icc > 0 ? g.icc : (g.nc >= 16 ? 16 : (g.nc >= 8 ? 8 : (g.nc >= 4 ? 4 : 1)));
         const int E = g.T + taps - 1;
         if ((size_t)E * E * CC * sizeof(float2) <= 200 * 1024) {
             cgs_status r;
@@ -589,6 +945,12 @@ cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *gri
             prof_end(PROF_INTERP, st);
             return r;
         }
+    }
+    if (g.d == 3) {
+        prof_begin(PROF_INTERP, st);
+        const cgs_status r = launch_grid3<false>(g, ns, grid, 0, ks, st);
+        prof_end(PROF_INTERP, st);
+        return r;
     }
     GridCfg c = pick_cfg(g);
     size_t smem = smem_bytes(g, c);
@@ -672,6 +1034,12 @@ cgs_status launch_spread(const GridGeom &g, const NodeSet &ns, const float2 *ks,
 {
     if (ns.nwork == 0 || g.nc == 0) return CGS_OK;
     if (2 * g.m + 2 > kMaxTaps) { set_error("m too large"); return CGS_ERR_BAD_ARG; }
+    if (g.d == 3) {
+        prof_begin(PROF_SPREAD, st);
+        const cgs_status r = launch_grid3<true>(g, ns, ks, weighted, grid, st);
+        prof_end(PROF_SPREAD, st);
+        return r;
+    }
     GridCfg c = pick_cfg(g);
     size_t smem = smem_bytes(g, c);
     if (smem > 200 * 1024) { set_error("gridding tile does not fit in shared memory"); return CGS_ERR_BAD_ARG; }

@@ -1178,7 +1178,7 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
         }
     }
     // work items: bins split into slices of at most kWork nodes
-    const int kWork = p->tune.work_slice > 0 ? p->tune.work_slice : 1024;
+    const int kWork = p->tune.work_slice > 0 ? p->tune.work_slice : 512;
     std::vector<int4> work;
     for (int ti = 0; ti < ntiles; ++ti) {
         for (int s0 = cnt[ti]; s0 < cnt[ti + 1]; s0 += kWork) {
@@ -1186,6 +1186,8 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
             work.push_back(make_int4(ti, s0, c, 0));
         }
     }
+    // longest items first (the crowded k-space centre), so they do not form the tail
+    std::stable_sort(work.begin(), work.end(), [](const int4 &x, const int4 &y) { return x.z > y.z; });
     dev_free(p->work);
     p->work = nullptr;
     CGS_TRY(dev_alloc(&p->work, work.size()));
@@ -1525,7 +1527,7 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
         for (int o : ok) if (v == o) return true;
         return false;
     };
-    if (!in(t->tile, {0, 8, 16, 32}) || !in(t->interp_coils, {0, 1, 4, 8, 16}) ||
+    if (!in(t->tile, {0, 8, 16, 32}) || !in(t->interp_coils, {0, 1, 4, 8, 16, 32}) ||
         !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) ||
         (t->work_slice != 0 && (t->work_slice < 32 || t->work_slice > 65536)) ||
         (t->spread_chunk != 0 && (t->spread_chunk < 32 || t->spread_chunk > 65536))) {
@@ -1575,7 +1577,7 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
         return launch_spread_patch(p->geom, p->pset, p->ksV, p->w, 0, p->grid, st);
     };
     std::vector<int> iccs, sccs;
-    for (int c : {1, 4, 8, 16})
+    for (int c : {1, 4, 8, 16, 32})
         if (c == 1 || c <= p->nc) iccs.push_back(c);
     for (int c : {32, 16, 8, 4, 2, 1})
         if (c <= p->nc && (int)sccs.size() < 3) sccs.push_back(c);
@@ -1585,7 +1587,7 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
     CGS_TRY(fill(p->grid, gridN, 0x9e3779b9u));
     for (int tile : {8, 16, 32}) {
         if (tile > p->n[0] || tile > p->n[1]) continue;
-        cur = best; cur.tile = tile; cur.work_slice = 1024;
+        cur = best; cur.tile = tile; cur.work_slice = 512;
         p->tune = cur;
         CGS_TRY(rebin(p));
         const int E = std::min(tile, std::min(p->n[0], p->n[1])) + 2 * p->m + 1;
@@ -1594,10 +1596,10 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
             p->tune.interp_coils = c;
             apply_tiles(p);
             CGS_TRY(timed(interp, &t));
-            if (t < t_int) { t_int = t; best.tile = tile; best.work_slice = 1024; best.interp_coils = c; }
+            if (t < t_int) { t_int = t; best.tile = tile; best.work_slice = 512; best.interp_coils = c; }
         }
     }
-    for (int slice : {512, 2048}) {
+    for (int slice : {256, 1024}) {
         cur = best; cur.work_slice = slice;
         p->tune = cur;
         CGS_TRY(rebin(p));

@@ -6,6 +6,8 @@
 // complex<float>, src/matrix/linalg/Lapack.hpp:619-624).
 #include "cgs_internal.cuh"
 
+#include <algorithm>
+
 namespace cgs {
 
 namespace {
@@ -43,20 +45,25 @@ __global__ void scatter_ks_kernel(const float2 *__restrict__ ks, const int *__re
     }
 }
 
-// tiled transpose between (nc, P) and (P, nc)
+// tiled transpose between (nc, P) and (P, nc): 32 x 32 tiles, a 1-D grid
+// striding over all tiles (P can exceed the 65535 limit of a grid's y extent)
 __global__ void transpose_kernel(const float2 *__restrict__ a, int64_t rows, int64_t cols,
                                  float2 *__restrict__ out)
 {
     __shared__ float2 t[32][33];
-    const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
-    for (int k = threadIdx.y; k < 32; k += 8) {
-        const int64_t r = r0 + k, c = c0 + threadIdx.x;
-        if (r < rows && c < cols) t[k][threadIdx.x] = a[r * cols + c];
-    }
-    __syncthreads();
-    for (int k = threadIdx.y; k < 32; k += 8) {
-        const int64_t c = c0 + k, r = r0 + threadIdx.x;
-        if (r < rows && c < cols) out[c * rows + r] = t[threadIdx.x][k];
+    const int64_t tr_n = (rows + 31) / 32, tc_n = (cols + 31) / 32;
+    for (int64_t tile = blockIdx.x; tile < tr_n * tc_n; tile += gridDim.x) {
+        const int64_t r0 = (tile / tc_n) * 32, c0 = (tile % tc_n) * 32;
+        for (int k = threadIdx.y; k < 32; k += 8) {
+            const int64_t r = r0 + k, c = c0 + threadIdx.x;
+            if (r < rows && c < cols) t[k][threadIdx.x] = a[r * cols + c];
+        }
+        __syncthreads();
+        for (int k = threadIdx.y; k < 32; k += 8) {
+            const int64_t c = c0 + k, r = r0 + threadIdx.x;
+            if (r < rows && c < cols) out[c * rows + r] = t[threadIdx.x][k];
+        }
+        __syncthreads();
     }
 }
 
@@ -413,8 +420,8 @@ cgs_status launch_to_coil_minor(const float2 *a, int64_t P, int nc, float2 *out,
 {
     // a: (nc rows, P cols) -> out: (P rows, nc cols)
     if (P * nc == 0) return CGS_OK;
-    dim3 grd((unsigned)((P + 31) / 32), (unsigned)((nc + 31) / 32));
-    transpose_kernel<<<grd, dim3(32, 8), 0, st>>>(a, nc, P, out);
+    const int64_t tiles = ((P + 31) / 32) * ((nc + 31) / 32);
+    transpose_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 32), dim3(32, 8), 0, st>>>(a, nc, P, out);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }
@@ -422,8 +429,8 @@ cgs_status launch_to_coil_minor(const float2 *a, int64_t P, int nc, float2 *out,
 cgs_status launch_to_coil_major(const float2 *a, int64_t P, int nc, float2 *out, cudaStream_t st)
 {
     if (P * nc == 0) return CGS_OK;
-    dim3 grd((unsigned)((nc + 31) / 32), (unsigned)((P + 31) / 32));
-    transpose_kernel<<<grd, dim3(32, 8), 0, st>>>(a, P, nc, out);
+    const int64_t tiles = ((P + 31) / 32) * ((nc + 31) / 32);
+    transpose_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 32), dim3(32, 8), 0, st>>>(a, P, nc, out);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }

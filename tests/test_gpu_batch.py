@@ -69,8 +69,8 @@ def test_autotune_picks_valid_decomposition(gpu):
     f0, a0 = nfft_pair(p, N, nc, k.shape[0], seed=3)
     t, ms = p.autotune()
     assert ms > 0
-    assert t["tile"] in (8, 16, 32) and t["interp_coils"] in (1, 4, 8, 16)
-    assert t["spread_coils"] in (1, 2, 4, 8, 16) and t["work_slice"] in (512, 1024, 2048)
+    assert t["tile"] in (8, 16, 32) and t["interp_coils"] in (1, 4, 8, 16, 32)
+    assert t["spread_coils"] in (1, 2, 4, 8, 16) and t["work_slice"] in (256, 512, 1024)
     assert p.tuning() == t
     f1, a1 = nfft_pair(p, N, nc, k.shape[0], seed=3)
     assert np.array_equal(f1, f0)
