@@ -149,6 +149,26 @@ def _stream(s):
     return C.c_void_p(int(s))
 
 
+def _resolve_stream(stream):
+    """Stream for a plan call and whether to wait for the plan's own stream
+    afterwards.  An explicit stream is used as given.  Otherwise torch's current
+    stream is used when it is a real stream, so device tensors are ordered with
+    torch's own work; on the legacy default stream (handle 0) the library runs
+    on the plan's stream and the call waits for it, so a device result is ready
+    for torch when the call returns."""
+    if stream is not None:
+        return _stream(stream), False
+    try:
+        import torch
+        if torch.cuda.is_available() and torch.cuda.is_initialized():
+            h = torch.cuda.current_stream().cuda_stream
+            if h:
+                return C.c_void_p(h), False
+    except ImportError:
+        pass
+    return None, True
+
+
 def kernel_launches() -> int:
     return int(load().cgs_kernel_launches())
 
@@ -174,6 +194,12 @@ def _report(rep):
 
 class Plan:
     """One NFFT / NCSENSE operator on the current CUDA device."""
+
+    def _go(self, fn, *args, stream=None):
+        st, wait = _resolve_stream(stream)
+        _check(fn(self._h, *args, st))
+        if wait:
+            _check(load().cgs_sync(self._h))
 
     def __init__(self, shape, M, ncoils=1, m=1, alpha=1.0):
         L = load()
@@ -216,28 +242,27 @@ class Plan:
 
     # -- operators (out must be preallocated, same memory kind as in) -------
     def nfft_trafo(self, fhat, out, stream=None):
-        _check(load().cgs_nfft_trafo(self._h, _ptr(fhat), _ptr(out), _stream(stream)))
+        self._go(load().cgs_nfft_trafo, _ptr(fhat), _ptr(out), stream=stream)
         return out
 
     def nfft_adjoint(self, f, out, stream=None):
-        _check(load().cgs_nfft_adjoint(self._h, _ptr(f), _ptr(out), _stream(stream)))
+        self._go(load().cgs_nfft_adjoint, _ptr(f), _ptr(out), stream=stream)
         return out
 
     def nfft_itrafo(self, f, out, maxit=3, eps=1e-3, stream=None):
-        _check(load().cgs_nfft_itrafo(self._h, _ptr(f), _ptr(out), int(maxit), float(eps), _stream(stream)))
+        self._go(load().cgs_nfft_itrafo, _ptr(f), _ptr(out), int(maxit), float(eps), stream=stream)
         return out
 
     def sense_trafo(self, x, out, stream=None):
-        _check(load().cgs_sense_trafo(self._h, _ptr(x), _ptr(out), _stream(stream)))
+        self._go(load().cgs_sense_trafo, _ptr(x), _ptr(out), stream=stream)
         return out
 
     def sense_adjoint_codeare(self, y, out, ftiter=3, fteps=1e-3, stream=None):
-        _check(load().cgs_sense_adjoint_codeare(self._h, _ptr(y), _ptr(out), int(ftiter), float(fteps),
-                                                 _stream(stream)))
+        self._go(load().cgs_sense_adjoint_codeare, _ptr(y), _ptr(out), int(ftiter), float(fteps), stream=stream)
         return out
 
     def sense_adjoint(self, y, out, weighted=True, stream=None):
-        _check(load().cgs_sense_adjoint(self._h, _ptr(y), _ptr(out), int(bool(weighted)), _stream(stream)))
+        self._go(load().cgs_sense_adjoint, _ptr(y), _ptr(out), int(bool(weighted)), stream=stream)
         return out
 
     def solve(self, y, out, mode=MODE_CODEARE, cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3,
@@ -245,7 +270,7 @@ class Plan:
         o = SolveOpts(int(mode), int(cgiter), float(cgeps), float(lam), int(ftiter), float(fteps),
                       int(bool(weighted)), int(bool(toeplitz)))
         rep = SolveReport()
-        _check(load().cgs_solve(self._h, _ptr(y), _ptr(out), C.byref(o), C.byref(rep), _stream(stream)))
+        self._go(load().cgs_solve, _ptr(y), _ptr(out), C.byref(o), C.byref(rep), stream=stream)
         return _report(rep)
 
     def tuning(self):
@@ -276,14 +301,13 @@ class Plan:
         o = SolveOpts(MODE_STANDARD, int(cgiter), float(cgeps), float(lam), 0, 0.0, int(bool(weighted)),
                       int(bool(toeplitz)), int(bool(jacobi)))
         rep = SolveReport()
-        _check(load().cgs_solve_fcg(self._h, None if y is None else _ptr(y), None if rhs is None else _ptr(rhs),
-                                    _ptr(out), C.byref(o), None if net is None else net._h, C.byref(rep),
-                                    _stream(stream)))
+        self._go(load().cgs_solve_fcg, None if y is None else _ptr(y), None if rhs is None else _ptr(rhs),
+                 _ptr(out), C.byref(o), None if net is None else net._h, C.byref(rep), stream=stream)
         return _report(rep)
 
     def normal_apply(self, x, out, lam=0.0, weighted=True, toeplitz=True, stream=None):
         o = SolveOpts(MODE_STANDARD, 0, 0.0, float(lam), 0, 0.0, int(bool(weighted)), int(bool(toeplitz)))
-        _check(load().cgs_normal_apply(self._h, _ptr(x), _ptr(out), C.byref(o), _stream(stream)))
+        self._go(load().cgs_normal_apply, _ptr(x), _ptr(out), C.byref(o), stream=stream)
         return out
 
 

@@ -200,6 +200,18 @@ def config1():
                 seed=SEED_BASE + 1)
 
 
+def config3(N: int = 128, nc: int = 16, nspokes: int = 20000, nsamp: int = 256):
+    """3-D kooshball CG-SENSE: 128^3 3-D Shepp-Logan (tabulated intensities),
+    16 Gaussian coils (sigma 0.45 FOV) on a Fibonacci sphere, 20000 spokes x 256
+    samples, density compensation |k|^2 (3-D radial), noise-free data, sigma=2,
+    m=4, standard CG to ||r||/||r0|| = 1e-4 with the Toeplitz-embedded E^H W E.  Smaller
+    arguments give the reduced cases the FP64 oracle can finish."""
+    k = kooshball3d(nspokes, nsamp)
+    w = (ramp_weights(k).astype(np.float64) ** 2).astype(np.float32)
+    return dict(name="cfg3_kooshball_%d_%dc_%dx%d" % (N, nc, nspokes, nsamp), shape=(N, N, N), image=phantom3d(N),
+                sens=coils3d(N, nc), k=k, w=w, alpha=2.0, m=4, cgeps=1e-4, noise=0.0, seed=SEED_BASE + 3)
+
+
 def config2(count: int = 64, seed: int = SEED_BASE + 2):
     """Batched uneven CG-SENSE: per problem N in 96..320 (step 32), NC in
     {4, 8, 16, 32}, golden-angle radial 32..400 spokes x 512; every fourth

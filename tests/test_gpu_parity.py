@@ -257,3 +257,27 @@ def test_standard_cg_toeplitz_3d(gpu, oracle):
     x2 = np.zeros_like(x)
     p.solve(c64(y), x2, mode=gpu.MODE_STANDARD, cgiter=6, cgeps=1e-12, lam=1e-3, weighted=True, toeplitz=False)
     assert rel(x2, xo) < TOL_IMG
+
+
+def test_config3_reduced_toeplitz_cg_matches_oracle(gpu, oracle):
+    """Config 3 at a size the FP64 oracle finishes: 3-D kooshball, |k|^2
+    weights, standard CG with the Toeplitz-embedded E^H W E on the GPU against
+    the oracle's CG on the NFFT pair, same iteration count (8)."""
+    from codeare_gb300 import capi, synth
+    import codeare_gb300 as cg
+    c = synth.config3(N=24, nc=4, nspokes=600, nsamp=48)
+    N, nc = c["shape"][0], c["sens"].shape[0]
+    k, w, S = c["k"], c["w"], c["sens"]
+    s = oracle.Sense(S, k, w=w, m=c["m"], alpha=c["alpha"])
+    y = synth.add_noise(s.trafo(c["image"]), c["noise"], seed=c["seed"])
+    xo, _ = s.cg(y, maxit=8, tol=0.0, lam=0.0, weighted=True)
+    p = capi.Plan((N, N, N), k.shape[0], ncoils=nc, m=c["m"], alpha=c["alpha"])
+    p.set_kspace(k)
+    p.set_weights(w)
+    p.set_sensitivities(np.ascontiguousarray(S))
+    x = np.zeros((N, N, N), np.complex64)
+    r = p.solve(y.astype(np.complex64), x, mode=cg.MODE_STANDARD, cgiter=8, cgeps=0.0, lam=0.0, weighted=True,
+                toeplitz=True)
+    assert r["iterations"] == 8
+    assert rel(x, xo) < 1e-4
+    p.close()
