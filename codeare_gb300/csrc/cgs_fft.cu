@@ -284,6 +284,162 @@ axis_fft_kernel(const __grid_constant__ AxisPass p, int BO, int BI, int64_t nib)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Power-of-two passes with the length N = 2^LOGN and the column count
+// B = 2^LOGB fixed at compile time (N B = 4096 values per CTA, 16 per
+// thread).  Every thread owns one column of the block and the rows
+// r0, r0 + 256/B, ..., so its global addresses are one column base plus a
+// row stride; the Stockham passes (radix 8, then 4 or 2 for the rest) index
+// shared memory with compile-time shifts and masks.  Same fusions as
+// axis_fft_kernel: pad/crop index maps, the image-side load (coil expansion,
+// mask, deapodisation), the deapodising store and the Toeplitz round.
+// ---------------------------------------------------------------------------
+constexpr int kP2Elems = 4096;
+
+template <int LOGN, int LOGB, int LOGR, int LOGNS>
+__device__ __forceinline__ void p2_pass(float2 *buf, const float2 *tw, int sign)
+{
+    constexpr int N = 1 << LOGN, B = 1 << LOGB, P = B + 1, R = 1 << LOGR, NS = 1 << LOGNS;
+    constexpr int NR = N / R;
+    constexpr int NBF = (B * NR) / kThreads;   // butterflies per thread
+    constexpr int STEP = N / (NS * R);         // twiddle index stride
+    static_assert(NBF >= 1 && (B * NR) % kThreads == 0, "block too small for the pass");
+    float2 v[NBF][R];
+#pragma unroll
+    for (int t = 0; t < NBF; ++t) {
+        const int q = threadIdx.x + t * kThreads;
+        const int b = q & (B - 1), j = q >> LOGB, k = j & (NS - 1);
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[t][r] = buf[(j + r * NR) * P + b];
+        if constexpr (NS > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                float2 w = tw[k * r * STEP];
+                if (sign > 0) w.y = -w.y;
+                v[t][r] = cmul(v[t][r], w);
+            }
+        }
+        bfly<R>(v[t], sign, tw, NR);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < NBF; ++t) {
+        const int q = threadIdx.x + t * kThreads;
+        const int b = q & (B - 1), j = q >> LOGB, k = j & (NS - 1);
+        const int base = ((j >> LOGNS) << (LOGNS + LOGR)) + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) buf[(base + r * NS) * P + b] = v[t][r];
+    }
+    __syncthreads();
+}
+
+template <int LOGN, int LOGB, int LOGNS>
+__device__ __forceinline__ void p2_passes(float2 *buf, const float2 *tw, int sign)
+{
+    if constexpr (LOGNS < LOGN) {
+        constexpr int LOGR = (LOGN - LOGNS) >= 3 ? 3 : (LOGN - LOGNS);
+        p2_pass<LOGN, LOGB, LOGR, LOGNS>(buf, tw, sign);
+        p2_passes<LOGN, LOGB, LOGNS + LOGR>(buf, tw, sign);
+    }
+}
+
+template <int LOGN, int LOGB>
+__global__ void __launch_bounds__(kThreads, 4)
+axis_fft_p2_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
+{
+    constexpr int N = 1 << LOGN, B = 1 << LOGB, P = B + 1;
+    constexpr int EPT = (N * B) / kThreads;    // values per thread
+    constexpr int RSTEP = kThreads / B;        // rows between a thread's values
+    static_assert(EPT * RSTEP == N, "rows must tile the transform");
+    extern __shared__ float2 smem[];
+    float2 *tw = smem;                          // [N]
+    float2 *buf = smem + N;                     // [N][P]
+    const int b = threadIdx.x & (B - 1), r0 = threadIdx.x >> LOGB;
+    const int64_t blk = blockIdx.x;
+    const int64_t o = ((blk / nib) << (LOGB - logBI)) + (b >> logBI);
+    const int64_t i = ((blk % nib) << logBI) + (b & ((1 << logBI) - 1));
+    const bool col_ok = (o < p.outer) && (i < p.inner);
+    for (int t = threadIdx.x; t < N; t += kThreads) tw[t] = p.tw[t];
+    float dcol = 1.f;  // outer-dimension deapodisation of this column (fused passes)
+    if (col_ok && (p.load_mode == LOAD_IMAGE || p.store_mode == STORE_DEAPOD)) {
+        if (p.deap_o1) dcol *= p.deap_o1[o % p.o1_len];
+        if (p.deap_o0) dcol *= p.deap_o0[o / p.o1_len];
+    }
+    {
+        float2 v[EPT];
+#pragma unroll
+        for (int u = 0; u < EPT; ++u) {
+            const int pos = r0 + u * RSTEP;
+            v[u] = make_float2(0.f, 0.f);
+            if (!col_ok) continue;
+            const int a = in_pos_to_axis(pos, p.Lin, N, p.in_centred);
+            if (a < 0) continue;
+            const int64_t pix = o * p.Lin + a;
+            if (p.load_mode == LOAD_PLAIN) {
+                v[u] = p.src[pix * p.inner + i];
+            } else {
+                float2 x = p.img_per_coil ? p.img[pix * p.inner + i] : p.img[pix];
+                if (p.sens) x = cmul(x, p.sens[pix * p.inner + i]);
+                float sc = dcol * (p.deap_ax ? p.deap_ax[a] : 1.f);
+                if (p.mask) sc *= p.mask[pix];
+                v[u] = cscale(x, sc);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < EPT; ++u) buf[(r0 + u * RSTEP) * P + b] = v[u];
+    }
+    __syncthreads();
+    p2_passes<LOGN, LOGB, 0>(buf, tw, p.sign);
+    if (p.toep_k) {
+        // pointwise multiply by the real Toeplitz kernel, then transform back
+        const int64_t kstride = p.inner / p.toep_nc;
+        if (i < p.inner) {
+#pragma unroll
+            for (int u = 0; u < EPT; ++u) {
+                const int pos = r0 + u * RSTEP;
+                buf[pos * P + b] = cscale(buf[pos * P + b], p.toep_k[pos * kstride + i / p.toep_nc]);
+            }
+        }
+        __syncthreads();
+        p2_passes<LOGN, LOGB, 0>(buf, tw, +1);
+    }
+    if (!col_ok) return;
+#pragma unroll
+    for (int u = 0; u < EPT; ++u) {
+        const int a = r0 + u * RSTEP;
+        if (a >= p.Lout) continue;
+        const int pos = out_axis_to_pos(a, p.Lout, N, p.out_centred);
+        float2 v = buf[pos * P + b];
+        if (p.store_mode == STORE_DEAPOD) v = cscale(v, dcol * (p.deap_ax ? p.deap_ax[a] : 1.f));
+        p.dst[(o * p.Lout + a) * p.inner + i] = v;
+    }
+}
+
+template <int LOGN>
+cgs_status launch_p2(const AxisPass &p, cudaStream_t st)
+{
+    constexpr int LOGB = (12 - LOGN) < 6 ? (12 - LOGN) : 6;   // N B = 4096 (B <= 64)
+    constexpr int B = 1 << LOGB;
+    static_assert((1 << LOGN) * B == kP2Elems, "4096 values per CTA");
+    int logBI = 0;  // largest power of two <= min(inner, B)
+    while ((1 << (logBI + 1)) <= B && (int64_t)(1 << (logBI + 1)) <= p.inner) ++logBI;
+    const int64_t nib = (p.inner + (1 << logBI) - 1) >> logBI;
+    const int64_t BO = B >> logBI;
+    const int64_t nob = (p.outer + BO - 1) / BO;
+    const int64_t nblocks = nib * nob;
+    if (nblocks > 0x7fffffffLL) { set_error("axis pass grid too large"); return CGS_ERR_BAD_ARG; }
+    const size_t smem = ((size_t)(1 << LOGN) * (B + 2)) * sizeof(float2);
+    static bool attr_set = false;
+    if (!attr_set) {
+        CGS_CUDA(cudaFuncSetAttribute(axis_fft_p2_kernel<LOGN, LOGB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        attr_set = true;
+    }
+    axis_fft_p2_kernel<LOGN, LOGB><<<(unsigned)nblocks, kThreads, smem, st>>>(p, logBI, nib);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
 }  // namespace
 
 cgs_status launch_axis_pass(const AxisPass &p, cudaStream_t st)
@@ -305,6 +461,21 @@ cgs_status launch_axis_pass(const AxisPass &p, cudaStream_t st)
     const size_t smem = ((size_t)n + (size_t)n * (BO * BI + 1)) * sizeof(float2) + (size_t)B * sizeof(float);
     bool mixed = false;
     for (int i = 0; i < p.nfac; ++i) mixed = mixed || (p.fac[i] != 2 && p.fac[i] != 4 && p.fac[i] != 8);
+    if (!mixed && n >= 64 && n <= 1024) {
+        int logn = 0;
+        while ((1 << logn) < n) ++logn;
+        cgs_status r;
+        prof_begin(PROF_FFT, st);
+        switch (logn) {
+            case 6: r = launch_p2<6>(p, st); break;
+            case 7: r = launch_p2<7>(p, st); break;
+            case 8: r = launch_p2<8>(p, st); break;
+            case 9: r = launch_p2<9>(p, st); break;
+            default: r = launch_p2<10>(p, st); break;
+        }
+        prof_end(PROF_FFT, st);
+        return r;
+    }
     static bool attr_set = false;
     if (!attr_set) {
         CGS_CUDA(cudaFuncSetAttribute(axis_fft_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -291,14 +291,15 @@ __device__ __forceinline__ float2 ffma2(float2 w, float2 v, float2 acc)
     return *reinterpret_cast<float2 *>(&r);
 }
 
-template <int PH, int PW, int CPL>
+template <int PH, int PW, int CPL, int BY, int BX>
 struct SpreadShape {
     static constexpr int NPT = PH * PW;                        // points per patch
-    static constexpr int G = 32 / NPT;                         // coil groups per warp
+    static constexpr int L = (PH / BY) * (PW / BX);            // lanes per coil group (BY x BX points each)
+    static constexpr int G = 32 / L;                           // coil groups per warp
     static constexpr int CC = G * CPL;                         // coils per warp
     static constexpr int GS = (CPL % 2 == 0) ? CPL + 2 : CPL;  // group stride (float2): groups 16 B apart in banks
     static constexpr int VR = G * GS;                          // staged value row per entry (float2)
-    static_assert(NPT * G == 32, "a patch must tile the warp");
+    static_assert(L * G == 32 && PH % BY == 0 && PW % BX == 0, "a patch must tile the warp");
     // one staging buffer: values, weights, footprint starts, density weights
     __host__ __device__ static size_t buf_bytes(int taps)
     {
@@ -306,13 +307,14 @@ struct SpreadShape {
     }
 };
 
-template <int PH, int PW, int CPL>
-__global__ void __launch_bounds__(256, 3)
+template <int PH, int PW, int CPL, int BY, int BX>
+__global__ void __launch_bounds__(256, (BY * BX == 1) ? 3 : 2)
 spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
                     const float2 *__restrict__ ks, const float *__restrict__ dens, int weighted,
                     float2 *__restrict__ grid)
 {
-    using S = SpreadShape<PH, PW, CPL>;
+    using S = SpreadShape<PH, PW, CPL, BY, BX>;
+    constexpr int NB = BY * BX;                            // points per lane
     extern __shared__ float4 smem4[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wi = blockIdx.x * 8 + warp;
@@ -326,10 +328,10 @@ spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ 
     const bool v16 = ((g.nc & 1) == 0);                    // node rows 16-byte aligned: two coils per copy
     const int4 wk = ps.work[wi];
     const int n0 = g.n[0], n1 = g.n[1];
-    const int pt = lane % S::NPT, cg = lane / S::NPT;
-    const int py = (wk.x / ps.npx) * PH + pt / PW;
-    const int px = (wk.x % ps.npx) * PW + pt % PW;
-    const bool inside = (py < n0) && (px < n1);
+    const int pt = lane % S::L, cg = lane / S::L;
+    const int by = (pt / (PW / BX)) * BY, bx = (pt % (PW / BX)) * BX;   // block origin in the patch
+    const int py = (wk.x / ps.npx) * PH + by;
+    const int px = (wk.x % ps.npx) * PW + bx;
     const bool wide = (n0 >= taps) && (n1 >= taps);        // no footprint wraps onto itself
 
     auto buffers = [&](int buf, float2 *&sv, float *&sw, int2 *&su, float *&sd) {
@@ -374,9 +376,11 @@ spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ 
         cp_async_commit();
     };
 
-    float2 acc[CPL];
+    float2 acc[NB][CPL];
 #pragma unroll
-    for (int k = 0; k < CPL; ++k) acc[k] = make_float2(0.f, 0.f);
+    for (int q = 0; q < NB; ++q)
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) acc[q][k] = make_float2(0.f, 0.f);
     const int end = wk.y + wk.z;
     int e0 = wk.y, cnt = min(kSpreadBatch, end - e0), buf = 0;
     issue(e0, cnt, 0);
@@ -390,47 +394,73 @@ spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ 
         buffers(buf, sv, sw, su, sd);
         for (int i = 0; i < cnt; ++i) {
             const int2 u = su[i];
-            float w = 0.f;
-            if (inside) {
-                int dy = py - u.x; if (dy < 0) dy += n0;
-                int dx = px - u.y; if (dx < 0) dx += n1;
-                const float *W = sw + i * WS;
-                float wy = 0.f, wx = 0.f;
-                if (wide) {
-                    wy = (dy < taps) ? W[dy] : 0.f;
-                    wx = (dx < taps) ? W[taps + dx] : 0.f;
-                } else {
-                    for (int q = dy; q < taps; q += n0) wy += W[q];
-                    for (int q = dx; q < taps; q += n1) wx += W[taps + q];
+            const float *W = sw + i * WS;
+            const float d = sd[i];
+            float wy[BY], wx[BX];
+#pragma unroll
+            for (int yy = 0; yy < BY; ++yy) {
+                wy[yy] = 0.f;
+                if (py + yy < n0) {
+                    int dy = py + yy - u.x; if (dy < 0) dy += n0;
+                    if (wide) wy[yy] = (dy < taps) ? W[dy] : 0.f;
+                    else for (int q = dy; q < taps; q += n0) wy[yy] += W[q];
                 }
-                w = wy * wx * sd[i];
             }
-            const float2 ww = make_float2(w, w);
+#pragma unroll
+            for (int xx = 0; xx < BX; ++xx) {
+                wx[xx] = 0.f;
+                if (px + xx < n1) {
+                    int dx = px + xx - u.y; if (dx < 0) dx += n1;
+                    if (wide) wx[xx] = (dx < taps) ? W[taps + dx] : 0.f;
+                    else for (int q = dx; q < taps; q += n1) wx[xx] += W[taps + q];
+                }
+            }
+            float2 ww[NB];
+#pragma unroll
+            for (int yy = 0; yy < BY; ++yy)
+#pragma unroll
+                for (int xx = 0; xx < BX; ++xx) {
+                    const float w = wy[yy] * wx[xx] * d;
+                    ww[yy * BX + xx] = make_float2(w, w);
+                }
             const float2 *vr = sv + i * S::VR + cg * S::GS;
             if constexpr (CPL % 2 == 0) {
                 const float4 *v4 = reinterpret_cast<const float4 *>(vr);
 #pragma unroll
                 for (int k = 0; k < CPL / 2; ++k) {
                     const float4 q = v4[k];
-                    acc[2 * k] = ffma2(ww, make_float2(q.x, q.y), acc[2 * k]);
-                    acc[2 * k + 1] = ffma2(ww, make_float2(q.z, q.w), acc[2 * k + 1]);
+#pragma unroll
+                    for (int b = 0; b < NB; ++b) {
+                        acc[b][2 * k] = ffma2(ww[b], make_float2(q.x, q.y), acc[b][2 * k]);
+                        acc[b][2 * k + 1] = ffma2(ww[b], make_float2(q.z, q.w), acc[b][2 * k + 1]);
+                    }
                 }
             } else {
 #pragma unroll
-                for (int k = 0; k < CPL; ++k) acc[k] = ffma2(ww, vr[k], acc[k]);
+                for (int k = 0; k < CPL; ++k) {
+                    const float2 q = vr[k];
+#pragma unroll
+                    for (int b = 0; b < NB; ++b) acc[b][k] = ffma2(ww[b], q, acc[b][k]);
+                }
             }
         }
         __syncwarp();
         if (cnt1 <= 0) break;
         e0 = e1; cnt = cnt1; buf ^= 1;
     }
-    if (!inside) return;
     const int cb = c0 + cg * CPL;                          // first coil of this lane's group
-    float2 *dst = (wk.w < 0) ? grid + ((size_t)py * n1 + px) * g.nc + cb
-                             : ps.partial + ((size_t)wk.w * S::NPT + pt) * g.nc + cb;
 #pragma unroll
-    for (int k = 0; k < CPL; ++k)
-        if (cg * CPL + k < ccn) dst[k] = acc[k];
+    for (int yy = 0; yy < BY; ++yy)
+#pragma unroll
+        for (int xx = 0; xx < BX; ++xx) {
+            if (py + yy >= n0 || px + xx >= n1) continue;
+            const int ppt = (by + yy) * PW + bx + xx;       // point index within the patch
+            float2 *dst = (wk.w < 0) ? grid + ((size_t)(py + yy) * n1 + px + xx) * g.nc + cb
+                                     : ps.partial + ((size_t)wk.w * S::NPT + ppt) * g.nc + cb;
+#pragma unroll
+            for (int k = 0; k < CPL; ++k)
+                if (cg * CPL + k < ccn) dst[k] = acc[yy * BX + xx][k];
+        }
 }
 
 // sum the partial slots of split patches in slot order and store them
@@ -988,33 +1018,40 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
     if (taps > kMaxTaps) { set_error("m too large"); return CGS_ERR_BAD_ARG; }
     // coils per warp: the next power of two >= coils (at most 32), or the tuned value
     int CC = 1;
-    if (ps.pw == 8) {
+    if (ps.pw == 8 && ps.blk == 1) {
         CC = 1;
     } else {
-        CC = 2;
+        const int lo = ps.blk == 4 ? 4 : 2;
+        CC = lo;
         while (CC < g.nc && CC < 32) CC *= 2;
-        if (g.scc > 0) CC = g.scc < 2 ? 2 : g.scc;
+        if (g.scc > 0) CC = g.scc < lo ? lo : g.scc;
     }
     dim3 grd((ps.nwork + 7) / 8, (g.nc + CC - 1) / CC);
     prof_begin(PROF_SPREAD, st);
-#define CGS_SP(PHV, PWV, CPLV)                                                                              \
+#define CGS_SP(PHV, PWV, CPLV, BYV, BXV)                                                                    \
     do {                                                                                                  \
-        const size_t sm = 8 * 2 * SpreadShape<PHV, PWV, CPLV>::buf_bytes(taps);                           \
-        CGS_CUDA(cudaFuncSetAttribute(spread_patch_kernel<PHV, PWV, CPLV>,                                 \
+        const size_t sm = 8 * 2 * SpreadShape<PHV, PWV, CPLV, BYV, BXV>::buf_bytes(taps);                 \
+        CGS_CUDA(cudaFuncSetAttribute(spread_patch_kernel<PHV, PWV, CPLV, BYV, BXV>,                       \
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));             \
-        spread_patch_kernel<PHV, PWV, CPLV><<<grd, 256, sm, st>>>(g, ps, ks, dens, weighted, grid);        \
+        spread_patch_kernel<PHV, PWV, CPLV, BYV, BXV><<<grd, 256, sm, st>>>(g, ps, ks, dens, weighted, grid); \
     } while (0)
-    if (ps.pw == 8) {
-        if (ps.ph != 4) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
-        CGS_SP(4, 8, 1);
-    } else {
-        if (ps.ph != 4 || ps.pw != 4) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
+    if (ps.ph != 4 || (ps.pw != 4 && ps.pw != 8)) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
+    if (ps.pw == 8 && ps.blk == 1) {
+        CGS_SP(4, 8, 1, 1, 1);
+    } else if (ps.pw == 8) {
         switch (CC) {
-            case 32: CGS_SP(4, 4, 16); break;
-            case 16: CGS_SP(4, 4, 8); break;
-            case 8: CGS_SP(4, 4, 4); break;
-            case 4: CGS_SP(4, 4, 2); break;
-            default: CGS_SP(4, 4, 1); break;
+            case 32: CGS_SP(4, 8, 8, 2, 2); break;
+            case 16: CGS_SP(4, 8, 4, 2, 2); break;
+            case 8: CGS_SP(4, 8, 2, 2, 2); break;
+            default: CGS_SP(4, 8, 1, 2, 2); break;
+        }
+    } else {
+        switch (CC) {
+            case 32: CGS_SP(4, 4, 16, 1, 1); break;
+            case 16: CGS_SP(4, 4, 8, 1, 1); break;
+            case 8: CGS_SP(4, 4, 4, 1, 1); break;
+            case 4: CGS_SP(4, 4, 2, 1, 1); break;
+            default: CGS_SP(4, 4, 1, 1, 1); break;
         }
     }
 #undef CGS_SP

@@ -146,12 +146,14 @@ struct NodeSet {
 };
 
 // Output-stationary 2-D spreading: one warp per work item over a ph x pw patch
-// of grid points (32 / (ph pw) coil groups of lanes, lane = point within its
-// group), FP32 accumulators for the group's coils in registers, walking the
-// list of nodes whose footprint covers the patch.  Patches are 4 x 4 (two coil
-// groups) for several coils and 4 x 8 (one group) for a single coil.
+// of grid points, its lanes split into coil groups (lane = one point or a 2 x 2
+// block of points within its group), FP32 accumulators for the group's coils
+// in registers, walking the list of nodes whose footprint covers the patch.
+// Patches are 4 x 4 single points (two groups) for several coils, 4 x 8 of
+// 2 x 2 blocks (four groups) when tuned so, and 4 x 8 single points for one coil.
 struct PatchSet {
     int ph, pw;            // patch rows and columns
+    int blk;               // grid points per lane: 1 (one point) or 4 (a 2 x 2 block)
     int npx;               // patches per grid row
     int nwork;             // work items
     const int *entries;    // node (sorted index) lists, patch after patch

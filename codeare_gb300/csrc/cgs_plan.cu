@@ -417,7 +417,7 @@ cgs_status op_eh(cgs_plan *p, const float2 *ks, int weighted, float2 *x, cudaStr
 void apply_tiles(cgs_plan *p)
 {
     GridGeom &g = p->geom;
-    g.T = (p->d == 2) ? (p->tune.tile > 0 ? p->tune.tile : 16) : 8;
+    g.T = (p->d == 2) ? (p->tune.tile > 0 ? p->tune.tile : 8) : 8;
     for (int t = 0; t < p->d; ++t)
         if (g.T > p->n[t]) g.T = p->n[t];
     for (int t = 0; t < 3; ++t) g.nt[t] = 1;
@@ -434,7 +434,10 @@ void apply_tiles(cgs_plan *p)
 cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
 {
     const int n0 = p->n[0], n1 = p->n[1], m = p->m, taps = 2 * m + 2;
-    const int kPatchH = 4, kPatchW = p->nc > 1 ? 4 : 8;
+    // one coil: 4 x 8 patches, a point per lane; spread_block 4 (4 or more coils): 4 x 8
+    // patches of 2 x 2 blocks, four coil groups; otherwise 4 x 4 patches, two coil groups
+    const int blk = (p->nc >= 4 && p->tune.spread_block == 4) ? 4 : 1;
+    const int kPatchH = 4, kPatchW = (p->nc == 1 || blk == 4) ? 8 : 4;
     const int npy = (n0 + kPatchH - 1) / kPatchH, npx = (n1 + kPatchW - 1) / kPatchW;
     const int64_t P = (int64_t)npy * npx, M = p->M;
     std::vector<int> perm(M);
@@ -512,6 +515,7 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     PatchSet &ps = p->pset;
     ps.ph = kPatchH;
     ps.pw = kPatchW;
+    ps.blk = blk;
     ps.npx = npx;
     ps.nwork = (int)work.size();
     ps.entries = p->pentries;
@@ -1528,7 +1532,7 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
         return false;
     };
     if (!in(t->tile, {0, 8, 16, 32}) || !in(t->interp_coils, {0, 1, 4, 8, 16, 32}) ||
-        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) ||
+        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 4}) ||
         (t->work_slice != 0 && (t->work_slice < 32 || t->work_slice > 65536)) ||
         (t->spread_chunk != 0 && (t->spread_chunk < 32 || t->spread_chunk > 65536))) {
         set_error("tuning value out of range");
@@ -1536,7 +1540,7 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
     }
     CGS_CUDA(cudaSetDevice(p->device));
     const bool bins = t->tile != p->tune.tile || t->work_slice != p->tune.work_slice ||
-                      t->spread_chunk != p->tune.spread_chunk;
+                      t->spread_chunk != p->tune.spread_chunk || t->spread_block != p->tune.spread_block;
     p->tune = *t;
     apply_tiles(p);
     drop_graphs(p);
@@ -1606,17 +1610,21 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
         CGS_TRY(timed(interp, &t));
         if (t < t_int) { t_int = t; best.work_slice = slice; }
     }
-    // spreading: chunk bound and coils per warp
+    // spreading: points per lane, chunk bound and coils per warp
     CGS_TRY(fill(p->ksV, ksN, 0x85ebca6bu));
-    for (int chunk : {0, 128, 256, 512, 1024}) {
-        cur = best; cur.spread_chunk = chunk;
-        p->tune = cur;
-        CGS_TRY(rebin(p));
-        for (int c : sccs) {
-            p->tune.spread_coils = c;
-            apply_tiles(p);
-            CGS_TRY(timed(spread, &t));
-            if (t < t_spr) { t_spr = t; best.spread_chunk = chunk; best.spread_coils = c; }
+    for (int blk : {1, 4}) {
+        if (blk == 4 && p->nc < 4) continue;
+        for (int chunk : {0, 128, 256, 512, 1024}) {
+            cur = best; cur.spread_chunk = chunk; cur.spread_block = blk;
+            p->tune = cur;
+            CGS_TRY(rebin(p));
+            for (int c : sccs) {
+                if (blk == 4 && c < 4) continue;
+                p->tune.spread_coils = c;
+                apply_tiles(p);
+                CGS_TRY(timed(spread, &t));
+                if (t < t_spr) { t_spr = t; best.spread_chunk = chunk; best.spread_coils = c; best.spread_block = blk; }
+            }
         }
     }
     p->tune = best;

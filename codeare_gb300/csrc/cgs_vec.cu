@@ -21,27 +21,56 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 }
 
 // user[c][perm[s]] -> ks[s][c]
+// Caller layout (coil-major, trajectory order) <-> device layout (bin order,
+// coil innermost) through 32 x 32 shared-memory tiles: the device side is
+// read or written in contiguous coil runs, the caller side along 32 sorted
+// positions of one coil, whose trajectory indices perm[s] come in runs (the
+// bin sort is stable, so a spoke's consecutive samples stay together).
 __global__ void gather_ks_kernel(const float2 *__restrict__ user, const int *__restrict__ perm,
                                  int64_t M, int nc, float2 *__restrict__ ks)
 {
-    const int64_t total = M * nc;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t s = e / nc;
-        const int c = (int)(e % nc);
-        ks[e] = user[(int64_t)c * M + perm[s]];
+    __shared__ float2 t[32][33];
+    const int64_t ts_n = (M + 31) / 32, tc_n = (nc + 31) / 32;
+    for (int64_t tile = blockIdx.x; tile < ts_n * tc_n; tile += gridDim.x) {
+        const int64_t s0 = (tile / tc_n) * 32;
+        const int c0 = (int)(tile % tc_n) * 32;
+        const int64_t s = s0 + threadIdx.x;
+        const int64_t j = s < M ? perm[s] : 0;
+        for (int k = threadIdx.y; k < 32; k += 8) {
+            const int c = c0 + k;
+            if (s < M && c < nc) t[k][threadIdx.x] = user[(int64_t)c * M + j];
+        }
+        __syncthreads();
+        for (int k = threadIdx.y; k < 32; k += 8) {
+            const int64_t ss = s0 + k;
+            const int c = c0 + threadIdx.x;
+            if (ss < M && c < nc) ks[ss * nc + c] = t[threadIdx.x][k];
+        }
+        __syncthreads();
     }
 }
 
 __global__ void scatter_ks_kernel(const float2 *__restrict__ ks, const int *__restrict__ perm,
                                   int64_t M, int nc, float2 *__restrict__ user)
 {
-    const int64_t total = M * nc;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t s = e / nc;
-        const int c = (int)(e % nc);
-        user[(int64_t)c * M + perm[s]] = ks[e];
+    __shared__ float2 t[32][33];
+    const int64_t ts_n = (M + 31) / 32, tc_n = (nc + 31) / 32;
+    for (int64_t tile = blockIdx.x; tile < ts_n * tc_n; tile += gridDim.x) {
+        const int64_t s0 = (tile / tc_n) * 32;
+        const int c0 = (int)(tile % tc_n) * 32;
+        for (int k = threadIdx.y; k < 32; k += 8) {
+            const int64_t ss = s0 + k;
+            const int c = c0 + threadIdx.x;
+            if (ss < M && c < nc) t[k][threadIdx.x] = ks[ss * nc + c];
+        }
+        __syncthreads();
+        const int64_t s = s0 + threadIdx.x;
+        const int64_t j = s < M ? perm[s] : 0;
+        for (int k = threadIdx.y; k < 32; k += 8) {
+            const int c = c0 + k;
+            if (s < M && c < nc) user[(int64_t)c * M + j] = t[threadIdx.x][k];
+        }
+        __syncthreads();
     }
 }
 
@@ -402,7 +431,8 @@ cgs_status launch_gather_ks(const float2 *user, const int *perm, int64_t M, int 
                             cudaStream_t st)
 {
     if (M * nc == 0) return CGS_OK;
-    gather_ks_kernel<<<grid_for(M * nc), kThreads, 0, st>>>(user, perm, M, nc, ks);
+    const int64_t tiles = ((M + 31) / 32) * ((nc + 31) / 32);
+    gather_ks_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 32), dim3(32, 8), 0, st>>>(user, perm, M, nc, ks);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }
@@ -411,7 +441,8 @@ cgs_status launch_scatter_ks(const float2 *ks, const int *perm, int64_t M, int n
                              cudaStream_t st)
 {
     if (M * nc == 0) return CGS_OK;
-    scatter_ks_kernel<<<grid_for(M * nc), kThreads, 0, st>>>(ks, perm, M, nc, user);
+    const int64_t tiles = ((M + 31) / 32) * ((nc + 31) / 32);
+    scatter_ks_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 32), dim3(32, 8), 0, st>>>(ks, perm, M, nc, user);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }

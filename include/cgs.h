@@ -190,11 +190,13 @@ cgs_status cgs_batch_destroy(cgs_batch *b);
 /* Gridding work decomposition of a plan (no reference counterpart: NFFT3
  * has no tunable bins).  0 in a field means the built-in default. */
 typedef struct {
-    int tile;          /* 2-D interpolation bin side in grid points (8, 16, 32; default 16) */
+    int tile;          /* 2-D interpolation bin side in grid points (8, 16, 32; default 8) */
     int work_slice;    /* most nodes per interpolation work item (default 512) */
     int spread_chunk;  /* most nodes per spreading work item (default 2x the mean patch list, 128..1024) */
     int interp_coils;  /* coils per interpolation CTA: 1, 4, 8, 16 or 32 (default 16, fewer for fewer coils) */
     int spread_coils;  /* coils per spreading warp: 1, 2, 4, 8, 16 or 32 (default: coils, at most 32) */
+    int spread_block;  /* grid points per spreading lane: 1 (4 x 4 patches) or 4 (2 x 2 blocks on 4 x 8
+                          patches, four coil groups per warp, 4 or more coils); default 1 */
 } cgs_tuning;
 
 cgs_status cgs_get_tuning(const cgs_plan *plan, cgs_tuning *out);
@@ -203,7 +205,7 @@ cgs_status cgs_get_tuning(const cgs_plan *plan, cgs_tuning *out);
 cgs_status cgs_set_tuning(cgs_plan *plan, const cgs_tuning *t);
 /* Autotuner: times the plan's own interpolation and spreading launches on
  * scratch data for each candidate decomposition (tile x work_slice x
- * interp_coils, spread_chunk x spread_coils), applies the fastest and returns
+ * interp_coils, spread_block x spread_chunk x spread_coils), applies the fastest and returns
  * it with its interpolation + spreading time in milliseconds.  Needs the
  * k-space; leaves the plan's data and the Toeplitz kernel to be rebuilt on
  * their next use.  2-D plans only. */
