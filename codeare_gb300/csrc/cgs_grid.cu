@@ -308,7 +308,7 @@ struct SpreadShape {
 };
 
 template <int PH, int PW, int CPL, int BY, int BX>
-__global__ void __launch_bounds__(256, (BY * BX == 1) ? 3 : 2)
+__global__ void __launch_bounds__(256, (BY * BX <= 2) ? 3 : 2)
 spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
                     const float2 *__restrict__ ks, const float *__restrict__ dens, int weighted,
                     float2 *__restrict__ grid)
@@ -1021,7 +1021,7 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
     if (ps.pw == 8 && ps.blk == 1) {
         CC = 1;
     } else {
-        const int lo = ps.blk == 4 ? 4 : 2;
+        const int lo = ps.blk >= 2 ? 4 : 2;
         CC = lo;
         while (CC < g.nc && CC < 32) CC *= 2;
         if (g.scc > 0) CC = g.scc < lo ? lo : g.scc;
@@ -1038,6 +1038,13 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
     if (ps.ph != 4 || (ps.pw != 4 && ps.pw != 8)) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
     if (ps.pw == 8 && ps.blk == 1) {
         CGS_SP(4, 8, 1, 1, 1);
+    } else if (ps.blk == 2) {
+        switch (CC) {
+            case 32: CGS_SP(4, 4, 8, 2, 1); break;
+            case 16: CGS_SP(4, 4, 4, 2, 1); break;
+            case 8: CGS_SP(4, 4, 2, 2, 1); break;
+            default: CGS_SP(4, 4, 1, 2, 1); break;
+        }
     } else if (ps.pw == 8) {
         switch (CC) {
             case 32: CGS_SP(4, 8, 8, 2, 2); break;

@@ -149,11 +149,12 @@ struct NodeSet {
 // of grid points, its lanes split into coil groups (lane = one point or a 2 x 2
 // block of points within its group), FP32 accumulators for the group's coils
 // in registers, walking the list of nodes whose footprint covers the patch.
-// Patches are 4 x 4 single points (two groups) for several coils, 4 x 8 of
-// 2 x 2 blocks (four groups) when tuned so, and 4 x 8 single points for one coil.
+// Patches are 4 x 4 single points (two groups) for several coils, 4 x 4 of
+// 2 x 1 or 4 x 8 of 2 x 2 blocks (four groups) when tuned so, and 4 x 8 single
+// points for one coil.
 struct PatchSet {
     int ph, pw;            // patch rows and columns
-    int blk;               // grid points per lane: 1 (one point) or 4 (a 2 x 2 block)
+    int blk;               // grid points per lane: 1, 2 (a 2 x 1 block) or 4 (a 2 x 2 block)
     int npx;               // patches per grid row
     int nwork;             // work items
     const int *entries;    // node (sorted index) lists, patch after patch

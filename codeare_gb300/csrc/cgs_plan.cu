@@ -434,9 +434,10 @@ void apply_tiles(cgs_plan *p)
 cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
 {
     const int n0 = p->n[0], n1 = p->n[1], m = p->m, taps = 2 * m + 2;
-    // one coil: 4 x 8 patches, a point per lane; spread_block 4 (4 or more coils): 4 x 8
-    // patches of 2 x 2 blocks, four coil groups; otherwise 4 x 4 patches, two coil groups
-    const int blk = (p->nc >= 4 && p->tune.spread_block == 4) ? 4 : 1;
+    // one coil: 4 x 8 patches, a point per lane; with 4 or more coils, spread_block 4:
+    // 4 x 8 patches of 2 x 2 blocks and spread_block 2: 4 x 4 patches of 2 x 1 blocks
+    // (four coil groups); otherwise 4 x 4 patches, a point per lane, two coil groups
+    const int blk = (p->nc >= 4 && (p->tune.spread_block == 4 || p->tune.spread_block == 2)) ? p->tune.spread_block : 1;
     const int kPatchH = 4, kPatchW = (p->nc == 1 || blk == 4) ? 8 : 4;
     const int npy = (n0 + kPatchH - 1) / kPatchH, npx = (n1 + kPatchW - 1) / kPatchW;
     const int64_t P = (int64_t)npy * npx, M = p->M;
@@ -1532,7 +1533,7 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
         return false;
     };
     if (!in(t->tile, {0, 8, 16, 32}) || !in(t->interp_coils, {0, 1, 4, 8, 16, 32}) ||
-        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 4}) ||
+        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 2, 4}) ||
         (t->work_slice != 0 && (t->work_slice < 32 || t->work_slice > 65536)) ||
         (t->spread_chunk != 0 && (t->spread_chunk < 32 || t->spread_chunk > 65536))) {
         set_error("tuning value out of range");
@@ -1612,14 +1613,14 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
     }
     // spreading: points per lane, chunk bound and coils per warp
     CGS_TRY(fill(p->ksV, ksN, 0x85ebca6bu));
-    for (int blk : {1, 4}) {
-        if (blk == 4 && p->nc < 4) continue;
+    for (int blk : {1, 2, 4}) {
+        if (blk > 1 && p->nc < 4) continue;
         for (int chunk : {0, 128, 256, 512, 1024}) {
             cur = best; cur.spread_chunk = chunk; cur.spread_block = blk;
             p->tune = cur;
             CGS_TRY(rebin(p));
             for (int c : sccs) {
-                if (blk == 4 && c < 4) continue;
+                if (blk > 1 && c < 4) continue;
                 p->tune.spread_coils = c;
                 apply_tiles(p);
                 CGS_TRY(timed(spread, &t));
