@@ -11,6 +11,8 @@
 // nfft_trafo / nfft_adjoint (src/matrix/ft/NFFTTraits.hpp:176-204).
 #include "cgs_internal.cuh"
 
+#include <initializer_list>
+
 namespace cgs {
 
 namespace {
@@ -285,30 +287,45 @@ axis_fft_kernel(const __grid_constant__ AxisPass p, int BO, int BI, int64_t nib)
 }
 
 // ---------------------------------------------------------------------------
-// Power-of-two passes with the length N = 2^LOGN and the column count
-// B = 2^LOGB fixed at compile time (N B = 4096 values per CTA, 16 per
-// thread).  Every thread owns one column of the block and the rows
-// r0, r0 + 256/B, ..., so its global addresses are one column base plus a
-// row stride; the Stockham passes (radix 8, then 4 or 2 for the rest) index
-// shared memory with compile-time shifts and masks.  Same fusions as
-// axis_fft_kernel: pad/crop index maps, the image-side load (coil expansion,
-// mask, deapodisation), the deapodising store and the Toeplitz round.
+// Passes with the length N and the column count B = 2^LOGB fixed at compile
+// time (N B <= 4096 values per CTA and a multiple of 256, so every thread
+// holds the same number).  Every thread owns one column of the block and the
+// rows r0, r0 + 256/B, ..., so its global addresses are one column base plus
+// a row stride; the Stockham passes (radix 7, 5, 3 for the odd part of N,
+// then 8, 4, 2) index shared memory with compile-time arithmetic.  Same
+// fusions as axis_fft_kernel: pad/crop index maps, the image-side load (coil
+// expansion, mask, deapodisation), the deapodising store and the Toeplitz
+// round.  Instantiated for the powers of two 64..1024 and the grid sizes with
+// small odd factors that 2N oversampling of N = 48..480 produces.
 // ---------------------------------------------------------------------------
-constexpr int kP2Elems = 4096;
+constexpr int kCtElems = 4096;
 
-template <int LOGN, int LOGB, int LOGR, int LOGNS>
-__device__ __forceinline__ void p2_pass(float2 *buf, const float2 *tw, int sign)
+__host__ __device__ constexpr int ct_next_radix(int rem)
 {
-    constexpr int N = 1 << LOGN, B = 1 << LOGB, P = B + 1, R = 1 << LOGR, NS = 1 << LOGNS;
+    return rem % 7 == 0 ? 7 : rem % 5 == 0 ? 5 : rem % 3 == 0 ? 3 : rem % 8 == 0 ? 8 : rem % 4 == 0 ? 4 : 2;
+}
+
+__host__ __device__ constexpr int ct_logb(int n)
+{
+    int lb = 6;
+    while (lb > 0 && (n << lb) > kCtElems) --lb;
+    return lb;
+}
+
+template <int N, int LOGB, int R, int NS>
+__device__ __forceinline__ void ct_pass(float2 *buf, const float2 *tw, int sign)
+{
+    constexpr int B = 1 << LOGB, P = B + 1;
     constexpr int NR = N / R;
-    constexpr int NBF = (B * NR) / kThreads;   // butterflies per thread
-    constexpr int STEP = N / (NS * R);         // twiddle index stride
-    static_assert(NBF >= 1 && (B * NR) % kThreads == 0, "block too small for the pass");
+    constexpr int TB = B * NR;                           // butterflies in the block
+    constexpr int NBF = (TB + kThreads - 1) / kThreads;  // per thread
+    constexpr int STEP = N / (NS * R);                   // twiddle index stride
     float2 v[NBF][R];
 #pragma unroll
     for (int t = 0; t < NBF; ++t) {
         const int q = threadIdx.x + t * kThreads;
-        const int b = q & (B - 1), j = q >> LOGB, k = j & (NS - 1);
+        if (TB % kThreads != 0 && q >= TB) continue;
+        const int b = q & (B - 1), j = q >> LOGB, k = j % NS;
 #pragma unroll
         for (int r = 0; r < R; ++r) v[t][r] = buf[(j + r * NR) * P + b];
         if constexpr (NS > 1) {
@@ -325,32 +342,33 @@ __device__ __forceinline__ void p2_pass(float2 *buf, const float2 *tw, int sign)
 #pragma unroll
     for (int t = 0; t < NBF; ++t) {
         const int q = threadIdx.x + t * kThreads;
-        const int b = q & (B - 1), j = q >> LOGB, k = j & (NS - 1);
-        const int base = ((j >> LOGNS) << (LOGNS + LOGR)) + k;
+        if (TB % kThreads != 0 && q >= TB) continue;
+        const int b = q & (B - 1), j = q >> LOGB, k = j % NS;
+        const int base = (j / NS) * NS * R + k;
 #pragma unroll
         for (int r = 0; r < R; ++r) buf[(base + r * NS) * P + b] = v[t][r];
     }
     __syncthreads();
 }
 
-template <int LOGN, int LOGB, int LOGNS>
-__device__ __forceinline__ void p2_passes(float2 *buf, const float2 *tw, int sign)
+template <int N, int LOGB, int NS>
+__device__ __forceinline__ void ct_passes(float2 *buf, const float2 *tw, int sign)
 {
-    if constexpr (LOGNS < LOGN) {
-        constexpr int LOGR = (LOGN - LOGNS) >= 3 ? 3 : (LOGN - LOGNS);
-        p2_pass<LOGN, LOGB, LOGR, LOGNS>(buf, tw, sign);
-        p2_passes<LOGN, LOGB, LOGNS + LOGR>(buf, tw, sign);
+    if constexpr (NS < N) {
+        constexpr int R = ct_next_radix(N / NS);
+        ct_pass<N, LOGB, R, NS>(buf, tw, sign);
+        ct_passes<N, LOGB, NS * R>(buf, tw, sign);
     }
 }
 
-template <int LOGN, int LOGB>
-__global__ void __launch_bounds__(kThreads, 4)
-axis_fft_p2_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
+template <int N, int LOGB>
+__global__ void __launch_bounds__(kThreads, ((N & (N - 1)) == 0) ? 4 : 3)
+axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
 {
-    constexpr int N = 1 << LOGN, B = 1 << LOGB, P = B + 1;
+    constexpr int B = 1 << LOGB, P = B + 1;
     constexpr int EPT = (N * B) / kThreads;    // values per thread
     constexpr int RSTEP = kThreads / B;        // rows between a thread's values
-    static_assert(EPT * RSTEP == N, "rows must tile the transform");
+    static_assert((N * B) % kThreads == 0 && EPT * RSTEP == N, "rows must tile the transform");
     extern __shared__ float2 smem[];
     float2 *tw = smem;                          // [N]
     float2 *buf = smem + N;                     // [N][P]
@@ -389,7 +407,7 @@ axis_fft_p2_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
         for (int u = 0; u < EPT; ++u) buf[(r0 + u * RSTEP) * P + b] = v[u];
     }
     __syncthreads();
-    p2_passes<LOGN, LOGB, 0>(buf, tw, p.sign);
+    ct_passes<N, LOGB, 1>(buf, tw, p.sign);
     if (p.toep_k) {
         // pointwise multiply by the real Toeplitz kernel, then transform back
         const int64_t kstride = p.inner / p.toep_nc;
@@ -401,7 +419,7 @@ axis_fft_p2_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
             }
         }
         __syncthreads();
-        p2_passes<LOGN, LOGB, 0>(buf, tw, +1);
+        ct_passes<N, LOGB, 1>(buf, tw, +1);
     }
     if (!col_ok) return;
 #pragma unroll
@@ -415,12 +433,12 @@ axis_fft_p2_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
     }
 }
 
-template <int LOGN>
-cgs_status launch_p2(const AxisPass &p, cudaStream_t st)
+template <int N>
+cgs_status launch_ct(const AxisPass &p, cudaStream_t st)
 {
-    constexpr int LOGB = (12 - LOGN) < 6 ? (12 - LOGN) : 6;   // N B = 4096 (B <= 64)
+    constexpr int LOGB = ct_logb(N);
     constexpr int B = 1 << LOGB;
-    static_assert((1 << LOGN) * B == kP2Elems, "4096 values per CTA");
+    static_assert(N * B <= kCtElems && (N * B) % kThreads == 0, "column block");
     int logBI = 0;  // largest power of two <= min(inner, B)
     while ((1 << (logBI + 1)) <= B && (int64_t)(1 << (logBI + 1)) <= p.inner) ++logBI;
     const int64_t nib = (p.inner + (1 << logBI) - 1) >> logBI;
@@ -428,16 +446,49 @@ cgs_status launch_p2(const AxisPass &p, cudaStream_t st)
     const int64_t nob = (p.outer + BO - 1) / BO;
     const int64_t nblocks = nib * nob;
     if (nblocks > 0x7fffffffLL) { set_error("axis pass grid too large"); return CGS_ERR_BAD_ARG; }
-    const size_t smem = ((size_t)(1 << LOGN) * (B + 2)) * sizeof(float2);
+    const size_t smem = ((size_t)N * (B + 2)) * sizeof(float2);
     static bool attr_set = false;
     if (!attr_set) {
-        CGS_CUDA(cudaFuncSetAttribute(axis_fft_p2_kernel<LOGN, LOGB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CGS_CUDA(cudaFuncSetAttribute(axis_fft_ct_kernel<N, LOGB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
         attr_set = true;
     }
-    axis_fft_p2_kernel<LOGN, LOGB><<<(unsigned)nblocks, kThreads, smem, st>>>(p, logBI, nib);
+    axis_fft_ct_kernel<N, LOGB><<<(unsigned)nblocks, kThreads, smem, st>>>(p, logBI, nib);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
+}
+
+bool ct_supported(int n)
+{
+    for (int c : {64, 96, 128, 160, 192, 224, 256, 288, 320, 384, 448, 512, 576, 640, 768, 896, 960, 1024})
+        if (n == c) return true;
+    return false;
+}
+
+// the compile-time pass for length n (ct_supported(n) must hold)
+cgs_status launch_ct_any(int n, const AxisPass &p, cudaStream_t st)
+{
+    switch (n) {
+        case 64: return launch_ct<64>(p, st);
+        case 96: return launch_ct<96>(p, st);
+        case 128: return launch_ct<128>(p, st);
+        case 160: return launch_ct<160>(p, st);
+        case 192: return launch_ct<192>(p, st);
+        case 224: return launch_ct<224>(p, st);
+        case 256: return launch_ct<256>(p, st);
+        case 288: return launch_ct<288>(p, st);
+        case 320: return launch_ct<320>(p, st);
+        case 384: return launch_ct<384>(p, st);
+        case 448: return launch_ct<448>(p, st);
+        case 512: return launch_ct<512>(p, st);
+        case 576: return launch_ct<576>(p, st);
+        case 640: return launch_ct<640>(p, st);
+        case 768: return launch_ct<768>(p, st);
+        case 896: return launch_ct<896>(p, st);
+        case 960: return launch_ct<960>(p, st);
+        case 1024: return launch_ct<1024>(p, st);
+        default: set_error("no compile-time FFT pass for this length"); return CGS_ERR_BAD_ARG;
+    }
 }
 
 }  // namespace
@@ -461,18 +512,9 @@ cgs_status launch_axis_pass(const AxisPass &p, cudaStream_t st)
     const size_t smem = ((size_t)n + (size_t)n * (BO * BI + 1)) * sizeof(float2) + (size_t)B * sizeof(float);
     bool mixed = false;
     for (int i = 0; i < p.nfac; ++i) mixed = mixed || (p.fac[i] != 2 && p.fac[i] != 4 && p.fac[i] != 8);
-    if (!mixed && n >= 64 && n <= 1024) {
-        int logn = 0;
-        while ((1 << logn) < n) ++logn;
-        cgs_status r;
+    if (ct_supported(n)) {
         prof_begin(PROF_FFT, st);
-        switch (logn) {
-            case 6: r = launch_p2<6>(p, st); break;
-            case 7: r = launch_p2<7>(p, st); break;
-            case 8: r = launch_p2<8>(p, st); break;
-            case 9: r = launch_p2<9>(p, st); break;
-            default: r = launch_p2<10>(p, st); break;
-        }
+        const cgs_status r = launch_ct_any(n, p, st);
         prof_end(PROF_FFT, st);
         return r;
     }

@@ -1616,6 +1616,7 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
     for (int blk : {1, 2, 4}) {
         if (blk > 1 && p->nc < 4) continue;
         for (int chunk : {0, 128, 256, 512, 1024}) {
+            if (blk > 1 && chunk != 0 && chunk != 512) continue;  // block variants: two chunk bounds
             cur = best; cur.spread_chunk = chunk; cur.spread_block = blk;
             p->tune = cur;
             CGS_TRY(rebin(p));

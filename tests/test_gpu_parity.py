@@ -78,9 +78,11 @@ def test_golden_3d_operators(gpu):
     assert rel(img, g["adjoint"]) < TOL_OP
 
 
-@pytest.mark.parametrize("N,nc,alpha,m", [(32, 4, 2.0, 4), (48, 3, 2.0, 4), (40, 2, 1.0, 1), (32, 5, 1.5, 2)])
+@pytest.mark.parametrize("N,nc,alpha,m", [(32, 4, 2.0, 4), (48, 3, 2.0, 4), (40, 2, 1.0, 1), (32, 5, 1.5, 2),
+                                         (96, 2, 2.0, 4), (160, 2, 2.0, 4), (224, 1, 2.0, 4), (288, 1, 2.0, 4)])
 def test_nfft_vs_oracle(gpu, oracle, N, nc, alpha, m):
-    """Non-power-of-two grids (48*2 = 96 = 2^5 3, 40*1.5 = 60) exercise the radix-3/5 passes."""
+    """Non-power-of-two grids exercise the odd radices: 40 and 48 (alpha 1.5 on 32) the runtime-radix
+    passes, 96, 192, 320, 448 and 576 (2^k times 3, 5, 7, 9) the compile-time passes."""
     from codeare_gb300 import synth
     k = synth.radial2d(30, 2 * N, golden=True)
     M = k.shape[0]
