@@ -239,6 +239,13 @@ cgs_status launch_fcg_kernels(int which, FCGScalars *fs, float2 *x, float2 *r, f
                               const float2 *q, float2 *z, int64_t n, cudaGraphConditionalHandle h,
                               cudaStream_t st);
 enum FcgOp { FCG_INIT = 0, FCG_UPDATE_XR = 1, FCG_DECIDE = 2, FCG_SELECT = 3, FCG_BETA = 4, FCG_P = 5, FCG_CHECK = 6 };
+// flexible-CG loop with a fixed preconditioner (mode 0 plain, 1 Jacobi):
+// x, r update and rr (mode 0 also beta and the loop test); z = d^2 r, zr, beta, loop test
+cgs_status launch_fcg_xr_rr(FCGScalars *fs, float2 *x, float2 *r, const float2 *p, const float2 *q, int64_t n,
+                            double *partial, unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st);
+cgs_status launch_fcg_jacobi_z(FCGScalars *fs, float2 *z, const float2 *r, const float *d, int64_t n,
+                               double *partial, unsigned int *ticket, cudaGraphConditionalHandle h,
+                               cudaStream_t st);
 // d[p] = 1/sqrt(sum_c |S[p][c]|^2 * sumw + lambda) from the coil-minor sensitivities
 cgs_status launch_jacobi_scale(const float2 *sens, int64_t P, int nc, const FCGScalars *fs, float *d,
                                cudaStream_t st);
@@ -255,6 +262,14 @@ cgs_status net_apply_image(cgs_net *n, const float2 *r, const double *nrm2, int 
 // iterate, decides whether another update follows, and sets the conditional
 // handle of the enclosing while node accordingly.
 cgs_status launch_cg_check(CGScalars *sc, cudaGraphConditionalHandle h, cudaStream_t st);
+// Fused updates with a deterministic dot (kDotBlocks blocks, partial[kDotBlocks],
+// a ticket that starts at 0 and is reset by the kernel):
+// q += lambda p (lambda nullable), *out = Re <p, q>; nothing when *done
+cgs_status launch_axpy_dot(float2 *q, const float2 *p, const double *lambda, const int *done, int64_t n,
+                           double *partial, unsigned int *ticket, double *out, cudaStream_t st);
+// CG / CGLS: x += ts p, r -= ts q (ts = rn / pq), rno = rn, rn = |r|^2, loop test
+cgs_status launch_cg_xr_rr(float2 *x, float2 *r, const float2 *p, const float2 *q, CGScalars *sc, int64_t n,
+                           double *partial, unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st);
 // resets the loop scalars on the device (a graph-resident replacement for the host upload)
 cgs_status launch_cg_init(CGScalars *sc, double lambda, double tol, int maxit, int sqrt_mode, cudaStream_t st);
 // q += lambda * p ; then pq = Re<p,q> is computed by coldot

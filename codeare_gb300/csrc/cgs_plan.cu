@@ -202,6 +202,8 @@ struct cgs_plan {
     double *partial = nullptr, *dots = nullptr;  // dots: 8 arrays of NC
     int *active = nullptr;
     CGScalars *sc = nullptr;
+    double *fpart = nullptr;        // per-block partials of the fused update-and-dot kernels
+    unsigned int *ftick = nullptr;  // their completion ticket (zero between launches)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // flexible CG state and graph
     float2 *vB = nullptr, *vZ = nullptr, *vO = nullptr, *vT = nullptr;
@@ -684,7 +686,9 @@ cgs_status op_ehe_toeplitz(cgs_plan *p, const float2 *x, float2 *out, cudaStream
 }
 
 // One CG-SENSE iteration (either mode) on the plan's buffers.
-cgs_status cg_iteration(cgs_plan *p, const cgs_solve_opts *o, cudaStream_t st)
+// One CG-SENSE iteration (either mode) on the plan's buffers, ending with the
+// loop test that sets the graph condition h.
+cgs_status cg_iteration(cgs_plan *p, const cgs_solve_opts *o, cudaGraphConditionalHandle h, cudaStream_t st)
 {
     const int64_t Nt = p->Nt;
     if (o->mode == CGS_MODE_CODEARE) {
@@ -696,12 +700,10 @@ cgs_status cg_iteration(cgs_plan *p, const cgs_solve_opts *o, cudaStream_t st)
         CGS_TRY(op_forward(p, p->vP, 0, nullptr, p->ksV, st));
         CGS_TRY(op_eh(p, p->ksV, o->weighted, p->vQ, st));
     }
-    CGS_TRY(launch_add_scaled(p->vQ, p->vP, p->sc, Nt, st));
-    CGS_TRY(launch_coldot(p->vP, p->vQ, nullptr, Nt, 1, p->partial, p->scal(), st));
-    CGS_TRY(launch_scalar_op(p->sc, p->scal(), 1, st));
-    CGS_TRY(launch_cg_update_xr(p->vX, p->vR, p->vP, p->vQ, p->sc, Nt, st));
-    CGS_TRY(launch_coldot(p->vR, p->vR, nullptr, Nt, 1, p->partial, p->scal(), st));
-    CGS_TRY(launch_scalar_op(p->sc, p->scal(), 2, st));
+    // q += lambda p, pq = Re <p, q>
+    CGS_TRY(launch_axpy_dot(p->vQ, p->vP, &p->sc->lambda, &p->sc->done, Nt, p->fpart, p->ftick, &p->sc->pq, st));
+    // x += ts p, r -= ts q, rn = |r|^2, loop test
+    CGS_TRY(launch_cg_xr_rr(p->vX, p->vR, p->vP, p->vQ, p->sc, Nt, p->fpart, p->ftick, h, st));
     return launch_cg_update_p(p->vP, p->vR, p->sc, Nt, st);
 }
 
@@ -769,8 +771,7 @@ cgs_status append_solve(cgs_plan *p, const cgs_solve_opts *o, cudaGraph_t g, boo
     if (r == CGS_OK && cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
         r = CGS_ERR_CUDA;
     if (r == CGS_OK) {
-        cgs_status q = cg_iteration(p, o, st);
-        if (q == CGS_OK) q = launch_cg_check(p->sc, h, st);
+        cgs_status q = cg_iteration(p, o, h, st);
         cudaGraph_t bb = body;
         if (cudaStreamEndCapture(st, &bb) != cudaSuccess && q == CGS_OK) q = CGS_ERR_CUDA;
         r = q;
@@ -799,7 +800,8 @@ cgs_status build_solve_graph(cgs_plan *p, const cgs_solve_opts *o, cudaStream_t 
     return CGS_OK;
 }
 
-// q = (E^H W E + lambda) p on the device buffers (lambda from the scalars)
+// q = (E^H W E + lambda) p on the device buffers (lambda from the scalars;
+// with sc null only E^H W E p)
 cgs_status op_normal(cgs_plan *p, const float2 *x, float2 *q, int toeplitz, int weighted, CGScalars *sc,
                      cudaStream_t st)
 {
@@ -809,7 +811,7 @@ cgs_status op_normal(cgs_plan *p, const float2 *x, float2 *q, int toeplitz, int 
         CGS_TRY(op_forward(p, x, 0, nullptr, p->ksV, st));
         CGS_TRY(op_eh(p, p->ksV, weighted, q, st));
     }
-    return launch_add_scaled(q, x, sc, p->Nt, st);
+    return sc ? launch_add_scaled(q, x, sc, p->Nt, st) : CGS_OK;  // null sc: the caller adds lambda x
 }
 
 cgs_status fcg_alloc(cgs_plan *p)
@@ -902,7 +904,20 @@ cgs_status build_fcg_graph(cgs_plan *p, int from_data, int toeplitz, int weighte
     if (r == CGS_OK && cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess)
         r = CGS_ERR_CUDA;
     if (r == CGS_OK) {
-        cgs_status q = op_normal(p, p->vP, p->vQ, toeplitz, weighted, &fs->cg, st);
+        cgs_status q = CGS_OK;
+        if (mode < 2) {
+            // fixed preconditioner: fused updates, Fletcher-Reeves beta
+            q = op_normal(p, p->vP, p->vQ, toeplitz, weighted, nullptr, st);
+            if (q == CGS_OK) q = launch_axpy_dot(p->vQ, p->vP, &fs->cg.lambda, nullptr, Nt, p->fpart, p->ftick, &fs->pq, st);
+            if (q == CGS_OK) q = launch_fcg_xr_rr(fs, p->vX, p->vR, p->vP, p->vQ, Nt, p->fpart, p->ftick, h, st);
+            if (q == CGS_OK && mode == 1)
+                q = launch_fcg_jacobi_z(fs, p->vZ, p->vR, p->dscale, Nt, p->fpart, p->ftick, h, st);
+            if (q == CGS_OK) q = K(FCG_P, h);
+            cudaGraph_t bb = body;
+            if (cudaStreamEndCapture(st, &bb) != cudaSuccess && q == CGS_OK) q = CGS_ERR_CUDA;
+            r = q;
+        } else {
+        q = op_normal(p, p->vP, p->vQ, toeplitz, weighted, &fs->cg, st);
         if (q == CGS_OK) q = launch_coldot(p->vP, p->vQ, nullptr, Nt, 1, p->partial, &fs->pq, st);
         if (q == CGS_OK) q = K(FCG_UPDATE_XR, h);
         if (q == CGS_OK) q = launch_coldot(p->vR, p->vR, nullptr, Nt, 1, p->partial, &fs->rr, st);
@@ -916,6 +931,7 @@ cgs_status build_fcg_graph(cgs_plan *p, int from_data, int toeplitz, int weighte
         cudaGraph_t bb = body;
         if (cudaStreamEndCapture(st, &bb) != cudaSuccess && q == CGS_OK) q = CGS_ERR_CUDA;
         r = q;
+        }
     }
     p->fg_kbody = cgs_kernel_launches() - c1;
     count_launch((int)-(cgs_kernel_launches() - c0));
@@ -1077,6 +1093,13 @@ cgs_status cgs_plan_create(cgs_plan **out, const cgs_plan_desc *desc)
     ALLOC(p->dots, 8 * nc + 8);
     ALLOC(p->active, nc);
     ALLOC(p->sc, 1);
+    ALLOC(p->fpart, (size_t)dot_blocks());
+    ALLOC(p->ftick, 1);
+    if (cudaMemset(p->ftick, 0, sizeof(unsigned int)) != cudaSuccess) {
+        cgs_plan_destroy(p);
+        set_error("cudaMemset failed");
+        return CGS_ERR_CUDA;
+    }
     ALLOC(p->nodes, (size_t)M * (p->d == 2 ? 1 : 2));
     ALLOC(p->perm, M);
     ALLOC(p->w, M);
@@ -1093,7 +1116,7 @@ cgs_status cgs_plan_destroy(cgs_plan *p)
     void *bufs[] = {p->tw[0], p->tw[1], p->tw[2], p->deap[0], p->deap[1], p->deap[2], p->nodes, p->perm,
                     p->w, p->work, p->nodeU, p->nodeW, p->pentries, p->pwork, p->pmulti, p->ppartial, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
                     p->cF, p->cP, p->cZ, p->vX, p->vR, p->vP, p->vQ, p->ioA, p->ioB, p->partial, p->dots,
-                    p->active, p->sc};
+                    p->active, p->sc, p->fpart, p->ftick};
     for (void *b : bufs) dev_free(b);
     for (void *b : {(void *)p->tw2[0], (void *)p->tw2[1], (void *)p->tw2[2], (void *)p->toepK, (void *)p->tA,
                     (void *)p->tB}) dev_free(b);

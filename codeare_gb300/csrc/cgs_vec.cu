@@ -247,7 +247,9 @@ __global__ void cg_update_p_kernel(float2 *__restrict__ p, const float2 *__restr
     }
 }
 
-__global__ void cg_check_kernel(CGScalars *sc, cudaGraphConditionalHandle h)
+// loop test of the CG-SENSE solvers on the device: records the residual
+// measure, sets done; returns whether another iteration runs
+__device__ unsigned int cg_check_logic(CGScalars *sc)
 {
     unsigned int go = 0;
     if (!sc->done) {
@@ -266,7 +268,99 @@ __global__ void cg_check_kernel(CGScalars *sc, cudaGraphConditionalHandle h)
             else { sc->iter += 1; go = 1; }
         }
     }
-    cudaGraphSetConditional(h, go);
+    return go;
+}
+
+__global__ void cg_check_kernel(CGScalars *sc, cudaGraphConditionalHandle h)
+{
+    cudaGraphSetConditional(h, cg_check_logic(sc));
+}
+
+// ---- fused vector updates with a dot product --------------------------------
+// Each block reduces its share in a fixed tree into partial[block]; the last
+// block to finish (an atomic ticket) adds the partials in block order, so the
+// value does not depend on scheduling, writes it and runs the loop's scalar
+// step.  The grid is always kDotBlocks blocks.
+__device__ __forceinline__ double block_reduce(double v, double *sred)
+{
+    __syncthreads();
+    sred[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = kThreads / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sred[threadIdx.x] += sred[threadIdx.x + s];
+        __syncthreads();
+    }
+    return sred[0];
+}
+
+// true in every thread of the last block, which then holds the total in *tot
+__device__ __forceinline__ bool finish_reduce(double v, double *partial, unsigned int *ticket, double *tot)
+{
+    __shared__ double sred[kThreads];
+    __shared__ bool last;
+    const double bs = block_reduce(v, sred);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = bs;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double sum = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += kThreads) sum += ((volatile double *)partial)[b];
+    const double t = block_reduce(sum, sred);
+    if (threadIdx.x == 0) *ticket = 0u;
+    *tot = t;
+    return true;
+}
+
+// q += lambda p (lambda nullable: no update), *out = Re <p, q>; skipped when *done
+__global__ void __launch_bounds__(kThreads)
+axpy_dot_kernel(float2 *__restrict__ q, const float2 *__restrict__ p, const double *lambda, const int *done,
+                int64_t n, double *partial, unsigned int *ticket, double *out)
+{
+    if (done && *done) return;
+    const float l = lambda ? (float)*lambda : 0.f;
+    double acc = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        float2 a = q[e];
+        const float2 b = p[e];
+        if (lambda) {
+            a.x = fmaf(l, b.x, a.x); a.y = fmaf(l, b.y, a.y);
+            q[e] = a;
+        }
+        acc += (double)fmaf(b.x, a.x, b.y * a.y);
+    }
+    double t;
+    if (finish_reduce(acc, partial, ticket, &t) && threadIdx.x == 0) *out = t;
+}
+
+// CG / CGLS: ts = rn / pq; x += ts p; r -= ts q; rno = rn, rn = |r|^2; loop test
+__global__ void __launch_bounds__(kThreads)
+cg_xr_rr_kernel(float2 *__restrict__ x, float2 *__restrict__ r, const float2 *__restrict__ p,
+                const float2 *__restrict__ q, CGScalars *sc, int64_t n, double *partial, unsigned int *ticket,
+                cudaGraphConditionalHandle h)
+{
+    if (sc->done) return;
+    const double tsd = sc->rn / sc->pq;
+    const float ts = (float)tsd;
+    double acc = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const float2 pv = p[e], qv = q[e];
+        float2 xv = x[e], rv = r[e];
+        xv.x = fmaf(ts, pv.x, xv.x); xv.y = fmaf(ts, pv.y, xv.y);
+        rv.x = fmaf(-ts, qv.x, rv.x); rv.y = fmaf(-ts, qv.y, rv.y);
+        x[e] = xv; r[e] = rv;
+        acc += (double)fmaf(rv.x, rv.x, rv.y * rv.y);
+    }
+    double t;
+    if (finish_reduce(acc, partial, ticket, &t) && threadIdx.x == 0) {
+        sc->ts = tsd;
+        sc->rno = sc->rn;
+        sc->rn = t;
+        cudaGraphSetConditional(h, cg_check_logic(sc));
+    }
 }
 
 // ---- flexible CG ----------------------------------------------------------
@@ -344,11 +438,10 @@ __global__ void fcg_p_kernel(const FCGScalars *fs, float2 *__restrict__ p, const
 }
 
 // residual check ||r|| / ||r0|| as the plain standard-mode loop
-__global__ void fcg_check_kernel(FCGScalars *fs, cudaGraphConditionalHandle h)
+__device__ unsigned int fcg_check_logic(FCGScalars *fs)
 {
     CGScalars *sc = &fs->cg;
     unsigned int go = 0;
-    fs->use_r = 0;
     if (!sc->done) {
         if (sc->iter >= sc->maxit) {
             sc->done = 1;
@@ -363,7 +456,70 @@ __global__ void fcg_check_kernel(FCGScalars *fs, cudaGraphConditionalHandle h)
             else { sc->iter += 1; go = 1; }
         }
     }
-    cudaGraphSetConditional(h, go);
+    return go;
+}
+
+__global__ void fcg_check_kernel(FCGScalars *fs, cudaGraphConditionalHandle h)
+{
+    fs->use_r = 0;
+    cudaGraphSetConditional(h, fcg_check_logic(fs));
+}
+
+// plain (mode 0) and Jacobi (mode 1) loops, where z = M r with a fixed M:
+// a = rz / pq; x += a p; r -= a q; rr = |r|^2.  Mode 0 (z = r) also takes the
+// Fletcher-Reeves beta = rr / rz here and runs the loop test.
+__global__ void __launch_bounds__(kThreads)
+fcg_xr_rr_kernel(FCGScalars *fs, float2 *__restrict__ x, float2 *__restrict__ r, const float2 *__restrict__ p,
+                 const float2 *__restrict__ q, int64_t n, double *partial, unsigned int *ticket,
+                 cudaGraphConditionalHandle h)
+{
+    const float a = (float)(fs->rz / fs->pq);
+    double acc = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const float2 pv = p[e], qv = q[e], rv = r[e];
+        float2 xv = x[e];
+        xv.x = fmaf(a, pv.x, xv.x); xv.y = fmaf(a, pv.y, xv.y);
+        x[e] = xv;
+        const float2 rn = make_float2(fmaf(-a, qv.x, rv.x), fmaf(-a, qv.y, rv.y));
+        r[e] = rn;
+        acc += (double)fmaf(rn.x, rn.x, rn.y * rn.y);
+    }
+    double t;
+    if (finish_reduce(acc, partial, ticket, &t) && threadIdx.x == 0) {
+        fs->rr = t;
+        if (fs->mode == 0) {
+            fs->zr = t;
+            fs->beta = t / fs->rz;
+            fs->rz = t;
+            fs->use_r = 1;
+            cudaGraphSetConditional(h, fcg_check_logic(fs));
+        }
+    }
+}
+
+// Jacobi loop: z = d^2 . r, zr = Re <z, r>, Fletcher-Reeves beta = zr / rz, loop test
+__global__ void __launch_bounds__(kThreads)
+fcg_jacobi_z_kernel(FCGScalars *fs, float2 *__restrict__ z, const float2 *__restrict__ r,
+                    const float *__restrict__ d, int64_t n, double *partial, unsigned int *ticket,
+                    cudaGraphConditionalHandle h)
+{
+    double acc = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        float f = d[e];
+        f *= f;
+        const float2 rv = r[e];
+        const float2 zv = make_float2(rv.x * f, rv.y * f);
+        z[e] = zv;
+        acc += (double)fmaf(zv.x, rv.x, zv.y * rv.y);
+    }
+    double t;
+    if (finish_reduce(acc, partial, ticket, &t) && threadIdx.x == 0) {
+        fs->zr = t;
+        fs->beta = t / fs->rz;
+        fs->rz = t;
+        fs->use_r = 0;
+        cudaGraphSetConditional(h, fcg_check_logic(fs));
+    }
 }
 
 // op 0: rn = xn = *src; 1: pq = *src; 2: rno = rn, rn = *src
@@ -462,6 +618,39 @@ cgs_status launch_to_coil_major(const float2 *a, int64_t P, int nc, float2 *out,
     if (P * nc == 0) return CGS_OK;
     const int64_t tiles = ((P + 31) / 32) * ((nc + 31) / 32);
     transpose_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 32), dim3(32, 8), 0, st>>>(a, P, nc, out);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_axpy_dot(float2 *q, const float2 *p, const double *lambda, const int *done, int64_t n,
+                           double *partial, unsigned int *ticket, double *out, cudaStream_t st)
+{
+    axpy_dot_kernel<<<kDotBlocks, kThreads, 0, st>>>(q, p, lambda, done, n, partial, ticket, out);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_cg_xr_rr(float2 *x, float2 *r, const float2 *p, const float2 *q, CGScalars *sc, int64_t n,
+                           double *partial, unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st)
+{
+    cg_xr_rr_kernel<<<kDotBlocks, kThreads, 0, st>>>(x, r, p, q, sc, n, partial, ticket, h);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_fcg_xr_rr(FCGScalars *fs, float2 *x, float2 *r, const float2 *p, const float2 *q, int64_t n,
+                            double *partial, unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st)
+{
+    fcg_xr_rr_kernel<<<kDotBlocks, kThreads, 0, st>>>(fs, x, r, p, q, n, partial, ticket, h);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_fcg_jacobi_z(FCGScalars *fs, float2 *z, const float2 *r, const float *d, int64_t n,
+                               double *partial, unsigned int *ticket, cudaGraphConditionalHandle h,
+                               cudaStream_t st)
+{
+    fcg_jacobi_z_kernel<<<kDotBlocks, kThreads, 0, st>>>(fs, z, r, d, n, partial, ticket, h);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }
