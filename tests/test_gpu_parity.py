@@ -187,6 +187,44 @@ def test_device_pointers_match_host(gpu):
     assert rel(yd.cpu().numpy(), yh) < 1e-6
 
 
+def test_pinned_host_buffers_match_pageable(gpu):
+    """Pinned host buffers (asynchronous copies) must give the results of
+    pageable buffers, and the host output must be complete on return."""
+    import torch
+    from codeare_gb300 import synth
+    import codeare_gb300 as cg
+    cfg = synth.small_config(N=32, nc=4)
+    k, M = cfg["k"], cfg["k"].shape[0]
+    p = make_plan(gpu, (32, 32), k, 4, 4, 2.0, w=cfg["w"], S=cfg["sens"])
+
+    def pinned(shape):
+        return torch.zeros(shape, dtype=torch.complex64).pin_memory().numpy()
+
+    rng = np.random.default_rng(5)
+    fh = c64(rng.standard_normal((4, 32, 32)) + 1j * rng.standard_normal((4, 32, 32)))
+    f_pg, f_pn = np.zeros((4, M), np.complex64), pinned((4, M))
+    fh_pn = pinned((4, 32, 32))
+    fh_pn[...] = fh
+    p.nfft_trafo(fh, f_pg)
+    p.nfft_trafo(fh_pn, f_pn)
+    assert np.array_equal(f_pg, f_pn)
+    a_pg, a_pn = np.zeros((4, 32, 32), np.complex64), pinned((4, 32, 32))
+    p.nfft_adjoint(f_pg, a_pg)
+    p.nfft_adjoint(f_pn, a_pn)
+    assert np.array_equal(a_pg, a_pn)
+    x = c64(cfg["image"])
+    y_pg, y_pn = np.zeros((4, M), np.complex64), pinned((4, M))
+    p.sense_trafo(x, y_pg)
+    x_pn = pinned((32, 32))
+    x_pn[...] = x
+    p.sense_trafo(x_pn, y_pn)
+    assert np.array_equal(y_pg, y_pn)
+    s_pg, s_pn = np.zeros((32, 32), np.complex64), pinned((32, 32))
+    p.solve(y_pg, s_pg, mode=cg.MODE_STANDARD, cgiter=5, cgeps=0.0, lam=0.0)
+    p.solve(y_pn, s_pn, mode=cg.MODE_STANDARD, cgiter=5, cgeps=0.0, lam=0.0)
+    assert np.array_equal(s_pg, s_pn)
+
+
 def test_bad_arguments_return_errors(gpu):
     from codeare_gb300 import capi
     with pytest.raises(capi.CgsError) as e:
