@@ -75,16 +75,19 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
 HOST = os.path.join(HERE, "host")
 PLUGIN = os.path.join(LIBDIR, "CGSENSE.so")
 PLUGIN_NUFFT = os.path.join(LIBDIR, "NuFFT.so")
+PLUGIN_ESTSENS = os.path.join(LIBDIR, "EstimateSensitivities.so")
 DRIVER = os.path.join(LIBDIR, "cgsense_run")
 
 
 def build_host(force: bool = False) -> str:
-    """The C++ drop-in layer: CGSENSE.so and NuFFT.so (ReconStrategy plugins
-    over libcgs.so) and cgsense_run (a dlopen host that drives a plugin)."""
-    srcs = [os.path.join(HOST, f) for f in ("CGSENSE.cpp", "cgsense_run.cpp", "NuFFT.cpp")]
+    """The C++ drop-in layer: CGSENSE.so, NuFFT.so and EstimateSensitivities.so
+    (ReconStrategy plugins over libcgs.so) and cgsense_run (a dlopen host that
+    drives a plugin)."""
+    srcs = [os.path.join(HOST, f) for f in ("CGSENSE.cpp", "cgsense_run.cpp", "NuFFT.cpp",
+                                            "EstimateSensitivities.cpp")]
     hdrs = [os.path.join(HOST, "codeare", f) for f in os.listdir(os.path.join(HOST, "codeare"))]
     newest = max(os.path.getmtime(f) for f in srcs + hdrs + [LIB])
-    outs = (PLUGIN, DRIVER, PLUGIN_NUFFT)
+    outs = (PLUGIN, DRIVER, PLUGIN_NUFFT, PLUGIN_ESTSENS)
     if not force and all(os.path.exists(o) for o in outs) and min(os.path.getmtime(o) for o in outs) >= newest:
         return PLUGIN
     common = ["g++", "-O2", "-std=c++17", "-Wall", "-I" + HOST, "-I" + os.path.join(ROOT, "include")]
@@ -93,6 +96,8 @@ def build_host(force: bool = False) -> str:
                   "-Wl,-rpath,$ORIGIN"],
         common + [srcs[1], "-o", DRIVER + ".tmp", "-ldl", "-rdynamic"],
         common + ["-fPIC", "-shared", srcs[2], "-o", PLUGIN_NUFFT + ".tmp", "-L" + LIBDIR, "-lcgs",
+                  "-Wl,-rpath,$ORIGIN"],
+        common + ["-fPIC", "-shared", srcs[3], "-o", PLUGIN_ESTSENS + ".tmp", "-L" + LIBDIR, "-lcgs",
                   "-Wl,-rpath,$ORIGIN"],
     ]
     for cmd in cmds:

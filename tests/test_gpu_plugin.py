@@ -99,3 +99,54 @@ def test_nufft_plugin_matches_reference_semantics(gpu, oracle, tmp_path):
     img = cgsm.read(str(out))["img"]
     assert img.shape == (N, N)
     assert rel(img, ref) < TOL_IMG, r.stdout
+
+
+def golden_radial_from_raster(raster, nk, nv, golden_deg=111.246117975):
+    """The EstimateSensitivities trajectory: the raster spoke linearly
+    interpolated to 10x its samples and cut to nk, rotated by v golden angles,
+    scaled to |k| <= 1/2, +0.5 wrapped to -0.5; (M, 2) with row order
+    (sample fastest, then volume), columns (kx, ky) as codeare's kspace rows."""
+    n = raster.shape[0]
+    xi = np.linspace(0.0, 1.0, n)
+    XI = np.linspace(0.0, 1.0, 10 * n)[:nk]
+    kx = np.interp(XI, xi, raster[:, 0].astype(np.float64))
+    ky = np.interp(XI, xi, raster[:, 1].astype(np.float64))
+    spoke = kx + 1j * ky
+    k = np.concatenate([spoke * np.exp(1j * np.deg2rad(v * golden_deg)) for v in range(nv)])
+    k = k / (2.0 * np.abs(k).max())
+    out = np.stack([k.real, k.imag], axis=1)
+    out[out >= 0.5] -= 1.0
+    return out.astype(np.float32)
+
+
+def test_estimate_sensitivities_matches_oracle(gpu, oracle, tmp_path):
+    """EstimateSensitivities.so (src/modules/EstimateSensitivities.cpp:53-182):
+    golden-angle spokes from a raster trajectory and the per-coil inverse NFFT
+    (unit weights, 3 CGNR steps) of 1e6-scaled data, against the FP64 oracle's
+    inverse NFFT on the same nodes."""
+    from codeare_gb300 import build, cgsm, synth
+    build.build()
+    N, nc, nk, nv, n = 48, 4, 96, 40, 12
+    raster = np.stack([np.linspace(-1.0, 1.0, n), np.zeros(n)], axis=1).astype(np.float32)
+    k = golden_radial_from_raster(raster, nk, nv)
+    M = k.shape[0]
+    S = synth.coils2d(N, nc)
+    img = synth.phantom(N)
+    P = oracle.NFFT((N, N), M, m=2, alpha=2.0)
+    P.set_x(k)
+    y = np.stack([P.trafo(S[c] * img) for c in range(nc)]).astype(np.complex64)   # (nc, M)
+    meas = np.ascontiguousarray(y.reshape(nc, nv, nk).transpose(1, 0, 2))        # codeare (nk, nc, nv)
+    sync = raster.reshape(-1)                                                    # (2n) interleaved (kx, ky)
+    inp, out, xml = tmp_path / "in.cgsm", tmp_path / "out.cgsm", tmp_path / "cfg.xml"
+    cgsm.write(str(inp), {"meas": meas, "sync": sync.astype(np.float32)})
+    xml.write_text('<EstimateSensitivities ftalpha="2.0" ftm="2" nk="%d" nl="1" cart_3rd_dim="0" '
+                   'image_size="%d %d" ftiter="3"/>\n' % (nk, N, N))
+    r = subprocess.run([build.DRIVER, build.PLUGIN_ESTSENS, str(xml), str(inp), str(out), "sensitivities"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    sens = cgsm.read(str(out))["sensitivities"]
+    assert sens.shape == (nc, N, N)
+    what = oracle.damp_mask((N, N))
+    w = np.ones(M, np.float32)
+    ref = np.stack([P.itrafo(y[c].astype(np.complex128) * 1e6, w, what, maxit=3, eps=7e-4)[0] for c in range(nc)])
+    assert rel(sens, ref) < TOL_IMG, r.stdout
