@@ -312,10 +312,27 @@ __host__ __device__ constexpr int ct_logb(int n)
     return lb;
 }
 
+// Shared-memory slot of (row, column): rows of B values with no padding; for
+// B <= 8 (a row fills at most half the banks) one spare row after every 8, so
+// that both consecutive rows and rows 8 apart (the first pass writes stride
+// R = 8) fall in different bank groups.
+template <int LOGB>
+__device__ __forceinline__ int ct_slot(int row, int b)
+{
+    if constexpr (LOGB <= 3) return ((row + (row >> 3)) << LOGB) + b;
+    else return (row << LOGB) + b;
+}
+
+template <int N, int LOGB>
+__host__ __device__ constexpr int ct_rows()
+{
+    return LOGB <= 3 ? N + (N + 7) / 8 : N;
+}
+
 template <int N, int LOGB, int R, int NS>
 __device__ __forceinline__ void ct_pass(float2 *buf, const float2 *tw, int sign)
 {
-    constexpr int B = 1 << LOGB, P = B + 1;
+    constexpr int B = 1 << LOGB;
     constexpr int NR = N / R;
     constexpr int TB = B * NR;                           // butterflies in the block
     constexpr int NBF = (TB + kThreads - 1) / kThreads;  // per thread
@@ -327,7 +344,7 @@ __device__ __forceinline__ void ct_pass(float2 *buf, const float2 *tw, int sign)
         if (TB % kThreads != 0 && q >= TB) continue;
         const int b = q & (B - 1), j = q >> LOGB, k = j % NS;
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[t][r] = buf[(j + r * NR) * P + b];
+        for (int r = 0; r < R; ++r) v[t][r] = buf[ct_slot<LOGB>(j + r * NR, b)];
         if constexpr (NS > 1) {
 #pragma unroll
             for (int r = 1; r < R; ++r) {
@@ -346,7 +363,7 @@ __device__ __forceinline__ void ct_pass(float2 *buf, const float2 *tw, int sign)
         const int b = q & (B - 1), j = q >> LOGB, k = j % NS;
         const int base = (j / NS) * NS * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) buf[(base + r * NS) * P + b] = v[t][r];
+        for (int r = 0; r < R; ++r) buf[ct_slot<LOGB>(base + r * NS, b)] = v[t][r];
     }
     __syncthreads();
 }
@@ -365,13 +382,13 @@ template <int N, int LOGB>
 __global__ void __launch_bounds__(kThreads, ((N & (N - 1)) == 0) ? 4 : 3)
 axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
 {
-    constexpr int B = 1 << LOGB, P = B + 1;
+    constexpr int B = 1 << LOGB;
     constexpr int EPT = (N * B) / kThreads;    // values per thread
     constexpr int RSTEP = kThreads / B;        // rows between a thread's values
     static_assert((N * B) % kThreads == 0 && EPT * RSTEP == N, "rows must tile the transform");
     extern __shared__ float2 smem[];
     float2 *tw = smem;                          // [N]
-    float2 *buf = smem + N;                     // [N][P]
+    float2 *buf = smem + N;                     // [rows][B], see ct_slot
     const int b = threadIdx.x & (B - 1), r0 = threadIdx.x >> LOGB;
     const int64_t blk = blockIdx.x;
     const int64_t o = ((blk / nib) << (LOGB - logBI)) + (b >> logBI);
@@ -404,7 +421,7 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
             }
         }
 #pragma unroll
-        for (int u = 0; u < EPT; ++u) buf[(r0 + u * RSTEP) * P + b] = v[u];
+        for (int u = 0; u < EPT; ++u) buf[ct_slot<LOGB>(r0 + u * RSTEP, b)] = v[u];
     }
     __syncthreads();
     ct_passes<N, LOGB, 1>(buf, tw, p.sign);
@@ -415,7 +432,7 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
 #pragma unroll
             for (int u = 0; u < EPT; ++u) {
                 const int pos = r0 + u * RSTEP;
-                buf[pos * P + b] = cscale(buf[pos * P + b], p.toep_k[pos * kstride + i / p.toep_nc]);
+                buf[ct_slot<LOGB>(pos, b)] = cscale(buf[ct_slot<LOGB>(pos, b)], p.toep_k[pos * kstride + i / p.toep_nc]);
             }
         }
         __syncthreads();
@@ -427,7 +444,7 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
         const int a = r0 + u * RSTEP;
         if (a >= p.Lout) continue;
         const int pos = out_axis_to_pos(a, p.Lout, N, p.out_centred);
-        float2 v = buf[pos * P + b];
+        float2 v = buf[ct_slot<LOGB>(pos, b)];
         if (p.store_mode == STORE_DEAPOD) v = cscale(v, dcol * (p.deap_ax ? p.deap_ax[a] : 1.f));
         p.dst[(o * p.Lout + a) * p.inner + i] = v;
     }
@@ -446,7 +463,7 @@ cgs_status launch_ct(const AxisPass &p, cudaStream_t st)
     const int64_t nob = (p.outer + BO - 1) / BO;
     const int64_t nblocks = nib * nob;
     if (nblocks > 0x7fffffffLL) { set_error("axis pass grid too large"); return CGS_ERR_BAD_ARG; }
-    const size_t smem = ((size_t)N * (B + 2)) * sizeof(float2);
+    const size_t smem = ((size_t)N + (size_t)ct_rows<N, LOGB>() * B) * sizeof(float2);
     static bool attr_set = false;
     if (!attr_set) {
         CGS_CUDA(cudaFuncSetAttribute(axis_fft_ct_kernel<N, LOGB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
