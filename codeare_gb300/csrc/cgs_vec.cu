@@ -134,14 +134,23 @@ coldot_partial_kernel(const float2 *__restrict__ a, const float2 *__restrict__ b
     }
 }
 
-__global__ void coldot_final_kernel(const double *__restrict__ partial, int nblk, int nc,
-                                    double *__restrict__ out)
+// one block per column: a fixed strided split of the block partials and a
+// fixed tree (deterministic; a single thread per column would serialise on
+// the load latency of nblk dependent adds)
+__global__ void __launch_bounds__(kThreads)
+coldot_final_kernel(const double *__restrict__ partial, int nblk, int nc, double *__restrict__ out)
 {
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        double s = 0.0;
-        for (int b = 0; b < nblk; ++b) s += partial[(int64_t)b * nc + c];
-        out[c] = s;
+    __shared__ double sred[kThreads];
+    const int c = blockIdx.x;
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += kThreads) s += partial[(int64_t)b * nc + c];
+    sred[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = kThreads / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) sred[threadIdx.x] += sred[threadIdx.x + h];
+        __syncthreads();
     }
+    if (threadIdx.x == 0) out[c] = sred[0];
 }
 
 __global__ void cgnr_scalars_kernel(int mode, int nc, double eps, int *active, const double *dot_r,
@@ -661,7 +670,7 @@ cgs_status launch_coldot(const float2 *a, const float2 *b, const float *wr, int6
     coldot_partial_kernel<<<kDotBlocks, kThreads, kThreads * sizeof(double), st>>>(a, b, wr, rows, nc,
                                                                                   partial);
     CGS_LAUNCH_CHECK();
-    coldot_final_kernel<<<(nc + 127) / 128, 128, 0, st>>>(partial, kDotBlocks, nc, out);
+    coldot_final_kernel<<<nc, kThreads, 0, st>>>(partial, kDotBlocks, nc, out);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }
