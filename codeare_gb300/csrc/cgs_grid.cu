@@ -1020,6 +1020,10 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
     int CC = 1;
     if (ps.pw == 8 && ps.blk == 1) {
         CC = 1;
+    } else if (ps.blk == 8) {
+        CC = 2;
+        while (CC < g.nc && CC < 16) CC *= 2;
+        if (g.scc > 0) CC = g.scc < 2 ? 2 : (g.scc > 16 ? 16 : g.scc);
     } else {
         const int lo = ps.blk >= 2 ? 4 : 2;
         CC = lo;
@@ -1038,6 +1042,13 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
     if (ps.ph != 4 || (ps.pw != 4 && ps.pw != 8)) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
     if (ps.pw == 8 && ps.blk == 1) {
         CGS_SP(4, 8, 1, 1, 1);
+    } else if (ps.blk == 8) {
+        switch (CC) {
+            case 16: CGS_SP(4, 8, 16, 1, 1); break;
+            case 8: CGS_SP(4, 8, 8, 1, 1); break;
+            case 4: CGS_SP(4, 8, 4, 1, 1); break;
+            default: CGS_SP(4, 8, 2, 1, 1); break;
+        }
     } else if (ps.blk == 2) {
         switch (CC) {
             case 32: CGS_SP(4, 4, 8, 2, 1); break;

@@ -154,7 +154,7 @@ struct NodeSet {
 // points for one coil.
 struct PatchSet {
     int ph, pw;            // patch rows and columns
-    int blk;               // grid points per lane: 1, 2 (a 2 x 1 block) or 4 (a 2 x 2 block)
+    int blk;               // 1: a point per lane; 2, 4: 2 x 1, 2 x 2 blocks; 8: 4 x 8 patch, one coil group
     int npx;               // patches per grid row
     int nwork;             // work items
     const int *entries;    // node (sorted index) lists, patch after patch

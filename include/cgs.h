@@ -195,9 +195,10 @@ typedef struct {
     int spread_chunk;  /* most nodes per spreading work item (default 2x the mean patch list, 128..1024) */
     int interp_coils;  /* coils per interpolation CTA: 1, 4, 8, 16 or 32 (default 16, fewer for fewer coils) */
     int spread_coils;  /* coils per spreading warp: 1, 2, 4, 8, 16 or 32 (default: coils, at most 32) */
-    int spread_block;  /* grid points per spreading lane: 1 (4 x 4 patches), 2 (2 x 1 blocks on 4 x 4
-                          patches) or 4 (2 x 2 blocks on 4 x 8 patches); blocks need 4 or more coils
-                          and put four coil groups in a warp; default 1 */
+    int spread_block;  /* spreading lanes: 1 (a point each on 4 x 4 patches, two coil groups),
+                          2 / 4 (2 x 1 / 2 x 2 blocks, four coil groups, 4 or more coils),
+                          8 (a point each on 4 x 8 patches, one coil group, 2..16 coils);
+                          default 1 */
 } cgs_tuning;
 
 cgs_status cgs_get_tuning(const cgs_plan *plan, cgs_tuning *out);

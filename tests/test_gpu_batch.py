@@ -49,7 +49,8 @@ def test_tuning_changes_decomposition_not_results(gpu):
               dict(tile=32, work_slice=2048, spread_chunk=1024, interp_coils=16, spread_coils=8, spread_block=4),
               dict(tile=16, work_slice=100, spread_chunk=0, interp_coils=1, spread_coils=1, spread_block=0),
               dict(tile=8, work_slice=512, spread_chunk=128, interp_coils=8, spread_coils=4, spread_block=4),
-              dict(tile=8, work_slice=512, spread_chunk=0, interp_coils=16, spread_coils=8, spread_block=2)]:
+              dict(tile=8, work_slice=512, spread_chunk=0, interp_coils=16, spread_coils=8, spread_block=2),
+              dict(tile=8, work_slice=512, spread_chunk=256, interp_coils=8, spread_coils=8, spread_block=8)]:
         p.set_tuning(**t)
         assert p.tuning() == t
         f1, a1 = nfft_pair(p, N, nc, k.shape[0])
@@ -74,7 +75,7 @@ def test_autotune_picks_valid_decomposition(gpu):
     assert ms > 0
     assert t["tile"] in (8, 16, 32) and t["interp_coils"] in (1, 4, 8, 16, 32)
     assert t["spread_coils"] in (1, 2, 4, 8, 16) and t["work_slice"] in (256, 512, 1024)
-    assert t["spread_block"] in (1, 2, 4)
+    assert t["spread_block"] in (1, 2, 4, 8)
     assert p.tuning() == t
     f1, a1 = nfft_pair(p, N, nc, k.shape[0], seed=3)
     assert np.array_equal(f1, f0)
