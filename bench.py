@@ -190,6 +190,7 @@ def cgsense_section(cpu_too: bool):
     p.set_kspace(k)
     p.set_weights(w)
     p.set_sensitivities(S)
+    p.autotune()
     y = np.zeros((nc, M), np.complex64)
     p.sense_trafo(np.ascontiguousarray(c["image"]), y)
     y = synth.add_noise(y, c["noise"], seed=c["seed"])

@@ -262,6 +262,13 @@ cgs_status net_apply_image(cgs_net *n, const float2 *r, const double *nrm2, int 
 // iterate, decides whether another update follows, and sets the conditional
 // handle of the enclosing while node accordingly.
 cgs_status launch_cg_check(CGScalars *sc, cudaGraphConditionalHandle h, cudaStream_t st);
+// One fused per-coil step of the batched CGNR inverse NFFT (see cgs_vec.cu):
+// mode 1 dot_v and alpha, mode 2 the image and k-space updates with dot_r and
+// the early-exit flags, mode 3 dz_new and beta.  dots6 = [dot_r, dot_z, dot_v,
+// dz_new, alpha, beta] of nc each; partial holds dot_blocks() x nc doubles.
+cgs_status launch_cgnr_fused(int mode, int64_t rows, int nc, const float *wr, float2 *vec, const float2 *other,
+                             float2 *img, const float2 *imgp, const float *mask, int64_t img_rows, double *partial,
+                             unsigned int *ticket, double *dots6, int *active, double eps, cudaStream_t st);
 // Fused updates with a deterministic dot (kDotBlocks blocks, partial[kDotBlocks],
 // a ticket that starts at 0 and is reset by the kernel):
 // q += lambda p (lambda nullable), *out = Re <p, q>; nothing when *done

@@ -381,20 +381,23 @@ cgs_status op_itrafo(cgs_plan *p, const float2 *ksIn, int maxit, double eps, cud
     CGS_CUDA(cudaMemcpyAsync(p->cP, p->cZ, sizeof(float2) * Nt * nc, cudaMemcpyDeviceToDevice, st));
     CGS_TRY(launch_coldot(p->cZ, p->cZ, p->mask, Nt, nc, p->partial, p->dot_z(), st));
     CGS_CUDA(cudaMemsetAsync(p->active, 0x01, sizeof(int) * nc, st));
-    for (int l = 0; l < maxit; ++l) {
+    // Per step: A p (masked), alpha; f += alpha p, r -= alpha A p, dot_r and the
+    // early-exit flag of the next step; A^H W r, beta; p = z + beta p.  The
+    // reductions and their scalar steps are fused into three kernels (a coil
+    // leaving after this step's update only skips the beta and p of this step,
+    // which no later step reads).
+    if (maxit > 0)
         CGS_TRY(launch_cgnr_scalars(0, nc, eps, p->active, p->dot_r(), p->dot_z(), p->dot_v(),
                                     p->dz_new(), p->alpha_c(), p->beta_c(), st));
+    for (int l = 0; l < maxit; ++l) {
         CGS_TRY(op_forward(p, p->cP, 1, p->mask, p->ksV, st));
-        CGS_TRY(launch_coldot(p->ksV, p->ksV, w, M, nc, p->partial, p->dot_v(), st));
-        CGS_TRY(launch_cgnr_scalars(1, nc, eps, p->active, p->dot_r(), p->dot_z(), p->dot_v(),
-                                    p->dz_new(), p->alpha_c(), p->beta_c(), st));
-        CGS_TRY(launch_axpy_cols(p->cF, p->alpha_c(), 1.0, p->mask, p->cP, Nt, nc, st));
-        CGS_TRY(launch_axpy_cols(p->ksR, p->alpha_c(), -1.0, nullptr, p->ksV, M, nc, st));
-        CGS_TRY(launch_coldot(p->ksR, p->ksR, w, M, nc, p->partial, p->dot_r(), st));
+        CGS_TRY(launch_cgnr_fused(1, M, nc, w, p->ksV, nullptr, nullptr, nullptr, nullptr, 0, p->partial, p->ftick,
+                                  p->dots, p->active, eps, st));
+        CGS_TRY(launch_cgnr_fused(2, M, nc, w, p->ksR, p->ksV, p->cF, p->cP, p->mask, Nt, p->partial, p->ftick,
+                                  p->dots, p->active, eps, st));
         CGS_TRY(op_adjoint(p, p->ksR, 1, p->cZ, st));
-        CGS_TRY(launch_coldot(p->cZ, p->cZ, p->mask, Nt, nc, p->partial, p->dz_new(), st));
-        CGS_TRY(launch_cgnr_scalars(2, nc, eps, p->active, p->dot_r(), p->dot_z(), p->dot_v(),
-                                    p->dz_new(), p->alpha_c(), p->beta_c(), st));
+        CGS_TRY(launch_cgnr_fused(3, Nt, nc, p->mask, p->cZ, nullptr, nullptr, nullptr, nullptr, 0, p->partial,
+                                  p->ftick, p->dots, p->active, eps, st));
         CGS_TRY(launch_xpby_cols(p->cP, p->cZ, p->beta_c(), p->active, Nt, nc, st));
     }
     return CGS_OK;
@@ -482,7 +485,7 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     // work items: a chunk bound that keeps every warp's list short
     const int64_t avg = std::max<int64_t>(1, E / std::max<int64_t>(P, 1));
     const int chunk = p->tune.spread_chunk > 0 ? p->tune.spread_chunk
-                                               : (int)std::min<int64_t>(1024, std::max<int64_t>(128, 2 * avg));
+                                               : (int)std::min<int64_t>(1024, std::max<int64_t>(64, 2 * avg));
     std::vector<int4> work, multi;
     int slots = 0;
     for (int64_t q = 0; q < P; ++q) {
@@ -1629,7 +1632,7 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
             if (t < t_int) { t_int = t; best.tile = tile; best.work_slice = 512; best.interp_coils = c; }
         }
     }
-    for (int slice : {256, 1024}) {
+    for (int slice : {128, 256, 1024}) {
         cur = best; cur.work_slice = slice;
         p->tune = cur;
         CGS_TRY(rebin(p));
@@ -1641,7 +1644,7 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
     for (int blk : {1, 2, 4, 8}) {
         if ((blk == 2 || blk == 4) && p->nc < 4) continue;
         if (blk == 8 && (p->nc < 2 || p->nc > 16)) continue;
-        for (int chunk : {0, 128, 256, 512, 1024}) {
+        for (int chunk : {0, 64, 128, 256, 512, 1024}) {
             if (blk > 1 && chunk != 0 && chunk != 512) continue;  // block variants: two chunk bounds
             cur = best; cur.spread_chunk = chunk; cur.spread_block = blk;
             p->tune = cur;

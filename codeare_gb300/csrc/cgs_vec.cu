@@ -173,6 +173,120 @@ __global__ void cgnr_scalars_kernel(int mode, int nc, double eps, int *active, c
     }
 }
 
+// ---- fused per-coil steps of the batched CGNR inverse NFFT ------------------
+// Per-column weighted squared norms of a [rows][nc] array, reduced in a fixed
+// order: per block (thread column c = t % ncl, row lanes t / ncl, then the
+// lanes in order) into partial[block][c]; the last block to finish (atomic
+// ticket) adds the block partials per column in block order, one warp per
+// column, and runs the scalar step of its coil.
+//   MODE 1: dot_v = |ksV|_w^2;  alpha = active ? dot_z / dot_v : 0
+//   MODE 2: img += alpha mask imgp (image side, no norm); vec -= alpha other;
+//           dot_r = |vec|_w^2; active &= !(dot_r < eps)
+//   MODE 3: dz_new = |cZ|_mask^2; beta = active ? dz_new / dot_z : 0, dot_z = dz_new
+struct CgnrArgs {
+    int64_t rows;
+    int nc;
+    const float *wr;       // row weights of the norm (nullable)
+    float2 *vec;           // the array whose column norms are taken (MODE 2 updates it)
+    const float2 *other;   // MODE 2: vec -= alpha * other
+    float2 *img;           // MODE 2: image estimate [img_rows][nc]
+    const float2 *imgp;    // MODE 2: search direction
+    const float *mask;     // MODE 2: damping mask per image row
+    int64_t img_rows;
+    double *partial;       // [gridDim.x][nc]
+    unsigned int *ticket;
+    double *dot_r, *dot_z, *dot_v, *dz_new, *alpha, *beta;
+    int *active;
+    double eps;
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) cgnr_fused_kernel(CgnrArgs a)
+{
+    __shared__ double sred[kThreads];
+    __shared__ bool last;
+    const int nc = a.nc, t = threadIdx.x;
+    if (MODE == 2) {
+        const int64_t total = a.img_rows * nc;
+        for (int64_t e = blockIdx.x * (int64_t)blockDim.x + t; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t r = e / nc;
+            const int c = (int)(e % nc);
+            const double al = a.alpha[c];
+            if (al == 0.0) continue;
+            float sc = (float)al;
+            if (a.mask) sc *= a.mask[r];
+            const float2 v = a.imgp[e];
+            float2 y = a.img[e];
+            y.x = fmaf(sc, v.x, y.x); y.y = fmaf(sc, v.y, y.y);
+            a.img[e] = y;
+        }
+    }
+    const int64_t per = (a.rows + gridDim.x - 1) / gridDim.x;
+    const int64_t rbeg = (int64_t)blockIdx.x * per;
+    const int64_t rend = min(a.rows, rbeg + per);
+    const int ncl = nc < kThreads ? nc : kThreads;
+    const int lanes = kThreads / ncl;
+    const int lr = t / ncl;
+    for (int cb = 0; cb < nc; cb += ncl) {
+        const int c = cb + t % ncl;
+        double acc = 0.0;
+        if (lr < lanes && c < nc) {
+            const float ms = (MODE == 2) ? (float)(-a.alpha[c]) : 0.f;
+            for (int64_t r = rbeg + lr; r < rend; r += lanes) {
+                float2 x = a.vec[r * nc + c];
+                if (MODE == 2 && ms != 0.f) {
+                    const float2 o = a.other[r * nc + c];
+                    x.x = fmaf(ms, o.x, x.x); x.y = fmaf(ms, o.y, x.y);
+                    a.vec[r * nc + c] = x;
+                }
+                double dv = (double)fmaf(x.x, x.x, x.y * x.y);
+                if (a.wr) dv *= (double)a.wr[r];
+                acc += dv;
+            }
+        }
+        sred[t] = (lr < lanes) ? acc : 0.0;
+        __syncthreads();
+        if (t < ncl) {
+            double sum = 0.0;
+            for (int l = 0; l < lanes; ++l) sum += sred[l * ncl + t];
+            if (cb + t < nc) a.partial[(int64_t)blockIdx.x * nc + cb + t] = sum;
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        __threadfence();
+        last = atomicAdd(a.ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int warp = t >> 5, lane = t & 31;
+    for (int c = warp; c < nc; c += kThreads / 32) {
+        double sum = 0.0;
+        for (int b = lane; b < (int)gridDim.x; b += 32) sum += ((volatile double *)a.partial)[(int64_t)b * nc + c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+        if (lane == 0) {
+            if (MODE == 1) {
+                a.dot_v[c] = sum;
+                a.alpha[c] = a.active[c] ? a.dot_z[c] / sum : 0.0;
+            } else if (MODE == 2) {
+                a.dot_r[c] = sum;
+                a.active[c] = a.active[c] && !(sum < a.eps);
+            } else {
+                a.dz_new[c] = sum;
+                if (a.active[c]) {
+                    a.beta[c] = sum / a.dot_z[c];
+                    a.dot_z[c] = sum;
+                } else {
+                    a.beta[c] = 0.0;
+                }
+            }
+        }
+    }
+    if (t == 0) *a.ticket = 0u;
+}
+
 __global__ void axpy_cols_kernel(float2 *__restrict__ x, const double *__restrict__ alpha, double sgn,
                                  const float *__restrict__ mask, const float2 *__restrict__ p,
                                  int64_t rows, int nc)
@@ -660,6 +774,24 @@ cgs_status launch_fcg_jacobi_z(FCGScalars *fs, float2 *z, const float2 *r, const
                                cudaStream_t st)
 {
     fcg_jacobi_z_kernel<<<kDotBlocks, kThreads, 0, st>>>(fs, z, r, d, n, partial, ticket, h);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_cgnr_fused(int mode, int64_t rows, int nc, const float *wr, float2 *vec, const float2 *other,
+                             float2 *img, const float2 *imgp, const float *mask, int64_t img_rows, double *partial,
+                             unsigned int *ticket, double *dots6, int *active, double eps, cudaStream_t st)
+{
+    CgnrArgs a;
+    a.rows = rows; a.nc = nc; a.wr = wr; a.vec = vec; a.other = other;
+    a.img = img; a.imgp = imgp; a.mask = mask; a.img_rows = img_rows;
+    a.partial = partial; a.ticket = ticket;
+    a.dot_r = dots6; a.dot_z = dots6 + nc; a.dot_v = dots6 + 2 * nc; a.dz_new = dots6 + 3 * nc;
+    a.alpha = dots6 + 4 * nc; a.beta = dots6 + 5 * nc;
+    a.active = active; a.eps = eps;
+    if (mode == 1) cgnr_fused_kernel<1><<<kDotBlocks, kThreads, 0, st>>>(a);
+    else if (mode == 2) cgnr_fused_kernel<2><<<kDotBlocks, kThreads, 0, st>>>(a);
+    else cgnr_fused_kernel<3><<<kDotBlocks, kThreads, 0, st>>>(a);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }

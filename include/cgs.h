@@ -192,7 +192,7 @@ cgs_status cgs_batch_destroy(cgs_batch *b);
 typedef struct {
     int tile;          /* 2-D interpolation bin side in grid points (8, 16, 32; default 8) */
     int work_slice;    /* most nodes per interpolation work item (default 512) */
-    int spread_chunk;  /* most nodes per spreading work item (default 2x the mean patch list, 128..1024) */
+    int spread_chunk;  /* most nodes per spreading work item (default 2x the mean patch list, 64..1024) */
     int interp_coils;  /* coils per interpolation CTA: 1, 4, 8, 16 or 32 (default 16, fewer for fewer coils) */
     int spread_coils;  /* coils per spreading warp: 1, 2, 4, 8, 16 or 32 (default: coils, at most 32) */
     int spread_block;  /* spreading lanes: 1 (a point each on 4 x 4 patches, two coil groups),

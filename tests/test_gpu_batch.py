@@ -74,7 +74,7 @@ def test_autotune_picks_valid_decomposition(gpu):
     t, ms = p.autotune()
     assert ms > 0
     assert t["tile"] in (8, 16, 32) and t["interp_coils"] in (1, 4, 8, 16, 32)
-    assert t["spread_coils"] in (1, 2, 4, 8, 16) and t["work_slice"] in (256, 512, 1024)
+    assert t["spread_coils"] in (1, 2, 4, 8, 16) and t["work_slice"] in (128, 256, 512, 1024)
     assert t["spread_block"] in (1, 2, 4, 8)
     assert p.tuning() == t
     f1, a1 = nfft_pair(p, N, nc, k.shape[0], seed=3)
