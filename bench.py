@@ -373,7 +373,7 @@ def run_ours(args):
     plan = cg.Plan((N, N), M, ncoils=NC, m=M_KB, alpha=SIGMA)
     plan.set_kspace(k)
     # the library's autotuner picks the gridding bins and coil blocks (untimed set-up)
-    tuning, _ = plan.autotune()
+    tuning = plan.autotune()[0] if not args.no_autotune else plan.tuning()
     # a dedicated stream: torch's default stream has handle 0, which the C ABI
     # reads as "the plan's own stream"
     stream = torch.cuda.Stream()
@@ -524,6 +524,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default gridding decomposition (profiling runs: no candidate launches)")
     ap.add_argument("--no-cgsense", action="store_true", help="skip the config-0, 2, 3 and 4 CG-SENSE sections")
     args = ap.parse_args()
     if args.impl == "reference":
