@@ -307,7 +307,8 @@ struct SpreadShape {
     }
 };
 
-template <int PH, int PW, int CPL, int BY, int BX>
+// TAPS > 0 fixes the footprint width at compile time (0: 2m + 2 at run time)
+template <int PH, int PW, int CPL, int BY, int BX, int TAPS = 0>
 __global__ void __launch_bounds__(256, (BY * BX <= 2) ? 3 : 2)
 spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
                     const float2 *__restrict__ ks, const float *__restrict__ dens, int weighted,
@@ -319,7 +320,7 @@ spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wi = blockIdx.x * 8 + warp;
     if (wi >= ps.nwork) return;
-    const int taps = 2 * g.m + 2;
+    const int taps = TAPS > 0 ? TAPS : 2 * g.m + 2;
     const int WS = 2 * taps;                               // weights per entry (a multiple of 4)
     const size_t bb = S::buf_bytes(taps);
     char *wbase = reinterpret_cast<char *>(smem4) + (size_t)warp * 2 * bb;
@@ -1032,12 +1033,19 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
     }
     dim3 grd((ps.nwork + 7) / 8, (g.nc + CC - 1) / CC);
     prof_begin(PROF_SPREAD, st);
-#define CGS_SP(PHV, PWV, CPLV, BYV, BXV)                                                                    \
+#define CGS_SPT(PHV, PWV, CPLV, BYV, BXV, TV)                                                               \
     do {                                                                                                  \
         const size_t sm = 8 * 2 * SpreadShape<PHV, PWV, CPLV, BYV, BXV>::buf_bytes(taps);                 \
-        CGS_CUDA(cudaFuncSetAttribute(spread_patch_kernel<PHV, PWV, CPLV, BYV, BXV>,                       \
+        CGS_CUDA(cudaFuncSetAttribute(spread_patch_kernel<PHV, PWV, CPLV, BYV, BXV, TV>,                   \
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));             \
-        spread_patch_kernel<PHV, PWV, CPLV, BYV, BXV><<<grd, 256, sm, st>>>(g, ps, ks, dens, weighted, grid); \
+        spread_patch_kernel<PHV, PWV, CPLV, BYV, BXV, TV><<<grd, 256, sm, st>>>(g, ps, ks, dens, weighted, grid); \
+    } while (0)
+#define CGS_SP(PHV, PWV, CPLV, BYV, BXV) CGS_SPT(PHV, PWV, CPLV, BYV, BXV, 0)
+    // the common footprint (m = 4) with one point per lane on 4 x 4 patches: compile-time taps
+#define CGS_SP1(CPLV)                                           \
+    do {                                                        \
+        if (taps == 10) CGS_SPT(4, 4, CPLV, 1, 1, 10);          \
+        else CGS_SP(4, 4, CPLV, 1, 1);                          \
     } while (0)
     if (ps.ph != 4 || (ps.pw != 4 && ps.pw != 8)) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
     if (ps.pw == 8 && ps.blk == 1) {
@@ -1065,14 +1073,16 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
         }
     } else {
         switch (CC) {
-            case 32: CGS_SP(4, 4, 16, 1, 1); break;
-            case 16: CGS_SP(4, 4, 8, 1, 1); break;
-            case 8: CGS_SP(4, 4, 4, 1, 1); break;
-            case 4: CGS_SP(4, 4, 2, 1, 1); break;
-            default: CGS_SP(4, 4, 1, 1, 1); break;
+            case 32: CGS_SP1(16); break;
+            case 16: CGS_SP1(8); break;
+            case 8: CGS_SP1(4); break;
+            case 4: CGS_SP1(2); break;
+            default: CGS_SP1(1); break;
         }
     }
+#undef CGS_SP1
 #undef CGS_SP
+#undef CGS_SPT
     CGS_LAUNCH_CHECK();
     if (ps.nmulti > 0) {
         const int64_t total = (int64_t)ps.nmulti * ps.ph * ps.pw * g.nc;
