@@ -46,6 +46,7 @@ def _deps_mtime() -> float:
 def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> str:
     os.makedirs(OBJDIR, exist_ok=True)
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime() and not extra:
+        build_host()
         return LIB
     extra = list(extra or [])
     cc = nvcc()

@@ -3,11 +3,19 @@
 // src/core/Loader.hpp.in:46-118, src/core/ReconContext.cpp:44-51) and drives
 // Init / Prepare / Process / Finalise on workspace matrices read from a file.
 //
-//   cgsense_run <plugin.so> <config.xml> <in.cgsm> <out.cgsm> [output names...]
+//   cgsense_run <plugin.so> <config.xml> <inputs> <output> [output names...]
+//
+// <inputs> is a .cgsm container, or codeare .cod files named for the
+// workspace: "sensitivities=s.cod,kspace=k.cod,...".  <output> is a .cgsm
+// container, or a .cod file when exactly one output name is given.
 //
 // The .cgsm container holds named matrices: "CGSM" u32 count, then per entry
 // u32 name length, name bytes, u32 type (0 float, 1 complex float), u32 ndims,
-// u64 dims[ndims] (codeare order, first index fastest), raw data.
+// u64 dims[ndims] (codeare order, first index fastest), raw data.  A .cod file
+// (src/matrix/io/CODFile.hpp:103-190) holds one matrix: i32 type (0 float,
+// 1 double, 2 complex float, 3 complex double), u64 ndims, u64 dims[ndims],
+// f32 resolutions[ndims], u64 name length, name, data, then a 32-character
+// delimiter.  Double data is converted to single precision.
 #include <dlfcn.h>
 
 #include <cstdint>
@@ -52,6 +60,102 @@ static bool read_cgsm(const char *path, Workspace &ws)
     return true;
 }
 
+static const char kCodDelimiter[] = "543f562189f1e82beb9c177f89f67822";
+
+static bool read_cod(const std::string &path, const std::string &name, Workspace &ws)
+{
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return false;
+    int32_t dt = -1;
+    uint64_t nd = 0, nlen = 0;
+    f.read((char *)&dt, 4);
+    f.read((char *)&nd, 8);
+    if (!f || nd == 0 || nd > 16) return false;
+    std::vector<size_t> dims(nd);
+    size_t count = 1;
+    for (uint64_t i = 0; i < nd; ++i) { uint64_t d; f.read((char *)&d, 8); dims[i] = (size_t)d; count *= (size_t)d; }
+    std::vector<float> res(nd);
+    f.read((char *)res.data(), 4 * nd);
+    f.read((char *)&nlen, 8);
+    if (!f || nlen > 4096) return false;
+    std::string stored(nlen, '\0');
+    f.read(&stored[0], (std::streamsize)nlen);
+    if (dt == 0 || dt == 1) {
+        Matrix<float> &m = ws.AddMatrix<float>(name);
+        m = Matrix<float>(dims);
+        if (dt == 0) {
+            f.read((char *)m.Ptr(), count * sizeof(float));
+        } else {
+            std::vector<double> b(count);
+            f.read((char *)b.data(), count * sizeof(double));
+            for (size_t i = 0; i < count; ++i) m.Ptr()[i] = (float)b[i];
+        }
+    } else if (dt == 2 || dt == 3) {
+        Matrix<cxfl> &m = ws.AddMatrix<cxfl>(name);
+        m = Matrix<cxfl>(dims);
+        if (dt == 2) {
+            f.read((char *)m.Ptr(), count * sizeof(cxfl));
+        } else {
+            std::vector<double> b(2 * count);
+            f.read((char *)b.data(), 2 * count * sizeof(double));
+            for (size_t i = 0; i < count; ++i) m.Ptr()[i] = cxfl((float)b[2 * i], (float)b[2 * i + 1]);
+        }
+    } else {
+        return false;
+    }
+    return (bool)f;
+}
+
+static bool write_cod(const char *path, Workspace &ws, const std::string &name)
+{
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return false;
+    auto header = [&](int32_t dt, const std::vector<size_t> &dims) {
+        const uint64_t nd = dims.size(), nlen = name.size();
+        f.write((const char *)&dt, 4);
+        f.write((const char *)&nd, 8);
+        for (size_t d : dims) { const uint64_t v = d; f.write((const char *)&v, 8); }
+        for (size_t i = 0; i < dims.size(); ++i) { const float r = 1.f; f.write((const char *)&r, 4); }
+        f.write((const char *)&nlen, 8);
+        f.write(name.data(), (std::streamsize)nlen);
+    };
+    if (ws.Exists<cxfl>(name) == codeare::OK) {
+        const Matrix<cxfl> &m = ws.Get<cxfl>(name);
+        header(2, m.Dim());
+        f.write((const char *)m.Ptr(), m.Size() * sizeof(cxfl));
+    } else if (ws.Exists<float>(name) == codeare::OK) {
+        const Matrix<float> &m = ws.Get<float>(name);
+        header(0, m.Dim());
+        f.write((const char *)m.Ptr(), m.Size() * sizeof(float));
+    } else {
+        return false;
+    }
+    f.write(kCodDelimiter, 32);
+    return (bool)f;
+}
+
+static bool ends_with(const std::string &s, const char *suf)
+{
+    const size_t n = std::strlen(suf);
+    return s.size() >= n && s.compare(s.size() - n, n, suf) == 0;
+}
+
+// "name=file.cod,name=file.cod,..."
+static bool read_cod_list(const std::string &spec, Workspace &ws)
+{
+    std::stringstream ss(spec);
+    std::string item;
+    while (std::getline(ss, item, ',')) {
+        const size_t eq = item.find('=');
+        if (eq == std::string::npos || eq == 0) return false;
+        if (!read_cod(item.substr(eq + 1), item.substr(0, eq), ws)) {
+            std::fprintf(stderr, "cannot read %s\n", item.substr(eq + 1).c_str());
+            return false;
+        }
+    }
+    return true;
+}
+
 static bool write_cgsm(const char *path, Workspace &ws, const std::vector<std::string> &names)
 {
     std::ofstream f(path, std::ios::binary);
@@ -75,7 +179,8 @@ static bool write_cgsm(const char *path, Workspace &ws, const std::vector<std::s
 int main(int argc, char **argv)
 {
     if (argc < 5) {
-        std::fprintf(stderr, "usage: %s plugin.so config.xml in.cgsm out.cgsm [outputs...]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s plugin.so config.xml in.cgsm|name=f.cod,... out.cgsm|out.cod [outputs...]\n",
+                     argv[0]);
         return 2;
     }
     std::ifstream cf(argv[2]);
@@ -83,7 +188,17 @@ int main(int argc, char **argv)
     ss << cf.rdbuf();
     const std::string xml = ss.str();
     Workspace &ws = Workspace::Instance();
-    if (!read_cgsm(argv[3], ws)) { std::fprintf(stderr, "cannot read %s\n", argv[3]); return 3; }
+    const std::string in(argv[3]);
+    const bool cod_in = in.find('=') != std::string::npos;
+    if (cod_in ? !read_cod_list(in, ws) : !read_cgsm(argv[3], ws)) {
+        std::fprintf(stderr, "cannot read %s\n", argv[3]);
+        return 3;
+    }
+    const bool cod_out = ends_with(argv[4], ".cod");
+    if (cod_out && argc > 6) {
+        std::fprintf(stderr, "a .cod output holds one matrix\n");
+        return 2;
+    }
     void *h = dlopen(argv[1], RTLD_NOW);
     if (!h) { std::fprintf(stderr, "dlopen: %s\n", dlerror()); return 4; }
     create_t *create = (create_t *)dlsym(h, "create");
@@ -107,7 +222,8 @@ int main(int argc, char **argv)
     std::vector<std::string> outs;
     for (int i = 5; i < argc; ++i) outs.push_back(argv[i]);
     if (outs.empty()) outs.push_back("image");
-    if (e == codeare::OK && !write_cgsm(argv[4], ws, outs)) e = codeare::FILE_WRITE_FAILED;
+    if (e == codeare::OK && !(cod_out ? write_cod(argv[4], ws, outs[0]) : write_cgsm(argv[4], ws, outs)))
+        e = codeare::FILE_WRITE_FAILED;
     destroy(rs);
     ws.Clear();  // entries the plugin added carry deleters that live in the plugin
     dlclose(h);

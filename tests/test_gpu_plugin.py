@@ -150,3 +150,32 @@ def test_estimate_sensitivities_matches_oracle(gpu, oracle, tmp_path):
     w = np.ones(M, np.float32)
     ref = np.stack([P.itrafo(y[c].astype(np.complex128) * 1e6, w, what, maxit=3, eps=7e-4)[0] for c in range(nc)])
     assert rel(sens, ref) < TOL_IMG, r.stdout
+
+
+def test_plugin_from_cod_files(gpu, tmp_path):
+    """The same CGSENSE run fed from codeare .cod files (double-precision
+    weights, converted on read) and writing a .cod image gives the image of
+    the container-fed run."""
+    from codeare_gb300 import build, cod, synth
+    cfg = synth.small_config(N=32, nc=4, nspokes=32, nsamp=64, alpha=2.0, m=4)
+    k, w, S = cfg["k"], cfg["w"], cfg["sens"]
+    from oracle import oracle as O
+    y = synth.add_noise(O.Sense(S, k, w=w, m=4, alpha=2.0).trafo(cfg["image"]), 1e-3, seed=5)
+    mats = {"sensitivities": S, "kspace": k, "weights": w, "signals": y.astype(np.complex64)}
+    attrs = {"nk": k.shape[0], "lambda": 0.05, "m": 4, "alpha": 2.0, "cgeps": 1e-6, "cgmaxit": 8,
+             "ftmaxit": 3, "fteps": 0.001, "noise": 0, "testcase": 0, "threads": 1, "verbose": 0}
+    ref, _ = run_plugin(tmp_path, mats, attrs)
+    files = []
+    for name, a in mats.items():
+        a = np.asarray(a)
+        a = a.astype(np.complex64 if np.iscomplexobj(a) else (np.float64 if name == "weights" else np.float32))
+        p = tmp_path / (name + ".cod")
+        cod.write(str(p), a, name)
+        files.append("%s=%s" % (name, p))
+    out = tmp_path / "image.cod"
+    r = subprocess.run([build.DRIVER, build.PLUGIN, str(tmp_path / "cfg.xml"), ",".join(files), str(out), "image"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    img, name, _ = cod.read(str(out))
+    assert name == "image" and img.dtype == np.complex64 and img.shape == ref.shape
+    assert np.array_equal(img, ref)
