@@ -5,6 +5,6 @@ include/cgs.h); `capi` binds it.  There is no CPU fallback: using an operator
 without the built library raises.
 """
 from . import capi, synth  # noqa: F401
-from .capi import Plan, CgsError, MODE_CODEARE, MODE_STANDARD, kernel_launches  # noqa: F401
+from .capi import Plan, CS, CgsError, MODE_CODEARE, MODE_STANDARD, kernel_launches  # noqa: F401
 
-__all__ = ["capi", "synth", "Plan", "CgsError", "MODE_CODEARE", "MODE_STANDARD", "kernel_launches"]
+__all__ = ["capi", "synth", "Plan", "CS", "CgsError", "MODE_CODEARE", "MODE_STANDARD", "kernel_launches"]

@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
            "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 
-SOURCES = ["cgs_fft.cu", "cgs_grid.cu", "cgs_vec.cu", "cgs_plan.cu", "cgs_static.cu", "cgs_cnn.cu"]
+SOURCES = ["cgs_fft.cu", "cgs_grid.cu", "cgs_vec.cu", "cgs_plan.cu", "cgs_static.cu", "cgs_cnn.cu", "cgs_cs.cu"]
 
 
 def nvcc() -> str:

@@ -29,7 +29,7 @@ EXPORTED = [
     "cgs_net_num_params", "cgs_net_create", "cgs_net_destroy", "cgs_net_set_weights", "cgs_net_get_weights",
     "cgs_net_forward", "cgs_net_gradients", "cgs_net_train_step", "cgs_solve_fcg", "cgs_normal_apply",
     "cgs_get_tuning", "cgs_set_tuning", "cgs_autotune", "cgs_batch_create", "cgs_batch_solve",
-    "cgs_batch_destroy",
+    "cgs_batch_destroy", "cgs_cs_create", "cgs_cs_destroy", "cgs_cs_adjoint", "cgs_cs_df", "cgs_cs_obj",
 ]
 PROFILE_CATEGORIES = ("fft", "interp", "spread")
 
@@ -56,6 +56,21 @@ class Tuning(C.Structure):
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class CsOpts(C.Structure):
+    _fields_ = [("cgiter", C.c_int), ("cgeps", C.c_double), ("lambda_", C.c_double), ("ftiter", C.c_int),
+                ("fteps", C.c_double), ("nlopt", C.c_int), ("csiter", C.c_int), ("nliter", C.c_int),
+                ("lsiter", C.c_int), ("lsa", C.c_float), ("lsb", C.c_float), ("cgconv", C.c_float),
+                ("parallel_linesearch", C.c_int), ("tvw", C.c_float * 2), ("tvdims", (C.c_int * 3) * 2),
+                ("ntvdims", C.c_int * 2), ("xfmw", C.c_float), ("l1", C.c_float), ("pnorm", C.c_float),
+                ("wl_family", C.c_int), ("wl_member", C.c_int)]
+
+
+class CsReport(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("ls_index", C.c_int * 256), ("rmse", C.c_double * 256),
+                ("solves", C.c_int), ("solve_iterations", C.c_int), ("tvw_used", C.c_float * 2),
+                ("seconds", C.c_double)]
 
 
 class CgsError(RuntimeError):
@@ -115,6 +130,11 @@ def load(path: str = LIB_PATH):
     L.cgs_net_forward.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp]
     L.cgs_net_gradients.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
     L.cgs_net_train_step.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_float, vp, vp]
+    L.cgs_cs_create.argtypes = [C.POINTER(vp), vp, C.POINTER(CsOpts)]
+    L.cgs_cs_destroy.argtypes = [vp]
+    L.cgs_cs_adjoint.argtypes = [vp, vp, vp, C.POINTER(CsReport), vp]
+    L.cgs_cs_df.argtypes = [vp, vp, vp, vp, vp]
+    L.cgs_cs_obj.argtypes = [vp, vp, vp, vp, C.c_float, C.POINTER(C.c_double), C.POINTER(C.c_double), vp]
     for name in EXPORTED:
         if name not in ("cgs_kernel_launches", "cgs_last_error", "cgs_profile_enable",
                         "cgs_profile_collect", "cgs_net_num_params"):
@@ -309,6 +329,69 @@ class Plan:
         o = SolveOpts(MODE_STANDARD, 0, 0.0, float(lam), 0, 0.0, int(bool(weighted)), int(bool(toeplitz)))
         self._go(load().cgs_normal_apply, _ptr(x), _ptr(out), C.byref(o), stream=stream)
         return out
+
+
+class CS:
+    """Compressed sensing over a plan's NCSENSE operator (codeare's CS_XSENSE
+    with ft = 3, minimised by NLCG).  The plan needs k-space, weights and
+    sensitivities and must not be used elsewhere while a CS call runs.
+    tvdims: per TV term the list of TV'ed axes in codeare order (None: all)."""
+
+    def __init__(self, plan, tvw=(0.0, 0.0), tvdims=(None, None), xfmw=0.0, l1=0.0, pnorm=0.0, nlopt=0,
+                 csiter=1, nliter=4, lsiter=8, lsa=0.01, lsb=0.6, cgconv=1e-4, parallel_linesearch=False,
+                 cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3, wl_family=-1, wl_member=0):
+        o = CsOpts()
+        o.cgiter, o.cgeps, o.lambda_, o.ftiter, o.fteps = int(cgiter), float(cgeps), float(lam), int(ftiter), float(fteps)
+        o.nlopt, o.csiter, o.nliter, o.lsiter = int(nlopt), int(csiter), int(nliter), int(lsiter)
+        o.lsa, o.lsb, o.cgconv = float(lsa), float(lsb), float(cgconv)
+        o.parallel_linesearch = int(bool(parallel_linesearch))
+        for i in range(2):
+            o.tvw[i] = float(tvw[i])
+            dims = list(tvdims[i] or [])[:3]
+            o.ntvdims[i] = len(dims)
+            for j, v in enumerate(dims):
+                o.tvdims[i][j] = int(v)
+        o.xfmw, o.l1, o.pnorm = float(xfmw), float(l1), float(pnorm)
+        o.wl_family, o.wl_member = int(wl_family), int(wl_member)
+        self.plan = plan
+        h = C.c_void_p()
+        _check(load().cgs_cs_create(C.byref(h), plan._h, C.byref(o)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().cgs_cs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _go(self, fn, *args, stream=None):
+        st, wait = _resolve_stream(stream)
+        _check(fn(self._h, *args, st))
+        if wait:
+            _check(load().cgs_sync(self.plan._h))
+
+    def adjoint(self, y, out, stream=None):
+        rep = CsReport()
+        self._go(load().cgs_cs_adjoint, _ptr(y), _ptr(out), C.byref(rep), stream=stream)
+        n = min(256, rep.iterations)
+        return dict(iterations=rep.iterations, ls_index=[rep.ls_index[i] for i in range(n)],
+                    rmse=[rep.rmse[i] for i in range(n)], solves=rep.solves,
+                    solve_iterations=rep.solve_iterations, tvw_used=(rep.tvw_used[0], rep.tvw_used[1]),
+                    seconds=rep.seconds)
+
+    def df(self, y, x, out, stream=None):
+        self._go(load().cgs_cs_df, _ptr(y), _ptr(x), _ptr(out), stream=stream)
+        return out
+
+    def obj(self, y, x, dx, t, stream=None):
+        o, r = C.c_double(), C.c_double()
+        self._go(load().cgs_cs_obj, _ptr(y), _ptr(x), _ptr(dx), float(t), C.byref(o), C.byref(r), stream=stream)
+        return o.value, r.value
 
 
 class Net:

@@ -299,4 +299,43 @@ cgs_status launch_intensity(const float2 *sens_cm, int64_t P, int nc, float *I, 
 // x *= real scale (elementwise, single image)
 cgs_status launch_scale_real(float2 *x, const float *s, int64_t n, cudaStream_t st);
 
+// ---------------------------------------------------------------------------
+// Compressed sensing over the NCSENSE operator (cgs_cs.cu)
+// ---------------------------------------------------------------------------
+constexpr int kCsSteps = 16;   // trial step sizes per objective pass
+constexpr int kCsBlocks = 304; // reduction grid (2 blocks per SM)
+// Penalty terms on a codeare-ordered image (axis 0 fastest).  tvmode: 0 off,
+// 1 TV2D, 2 TV3D over all axes, 3 TV3D over the third axis only.
+struct CsTerms {
+    int D0, D1, D2;
+    int tvmode[2];
+    float tvw[2];
+    float xfmw, l1, pnorm;
+};
+struct CsSteps {
+    float t[kCsSteps];
+    int n;
+};
+// out[0..15]: data term per step over the k-space arrays (ffdbx = ksA,
+// ffdbg = ksB, data = ksY); out[16..31]: TV and L1 terms per step.
+// partial holds 2 * kCsBlocks * kCsSteps doubles.
+cgs_status launch_cs_obj(const float2 *ksA, const float2 *ksB, const float2 *ksY, int64_t nks, const float2 *x,
+                         const float2 *dx, const CsTerms &terms, const CsSteps &steps, double *partial, double *out,
+                         cudaStream_t st);
+// out2 = (Re, Im) sum conj(a) b
+cgs_status launch_cs_dot(const float2 *a, const float2 *b, int64_t n, double *partial, double *out2,
+                         cudaStream_t st);
+cgs_status launch_cs_nnz(const float2 *a, int64_t n, double *partial, double *out, cudaStream_t st);
+// *out = bits of max |x| (a float)
+cgs_status launch_cs_absmax(const float2 *x, int64_t n, unsigned int *out, cudaStream_t st);
+// g = 2 ehr + the L1 and TV gradients at x
+cgs_status launch_cs_grad(const float2 *x, const float2 *ehr, const CsTerms &terms, float2 *g, cudaStream_t st);
+cgs_status launch_cs_axpy(float2 *x, const float2 *dx, float t, int64_t n, cudaStream_t st);
+// dx = -g1 + dx * (*g1sq / *g0sq); dx = -g1 when g0sq is null
+cgs_status launch_cs_dir(float2 *dx, const float2 *g1, const double *g1sq, const double *g0sq, int64_t n,
+                         cudaStream_t st);
+cgs_status launch_cs_sub(float2 *out, const float2 *a, const float2 *b, int64_t n, cudaStream_t st);
+// acc[0] += sc->iter; acc[1] |= sc->nan_flag
+cgs_status launch_cs_tally(const CGScalars *sc, int *acc, cudaStream_t st);
+
 }  // namespace cgs

@@ -1808,3 +1808,339 @@ cgs_status cgs_batch_solve(cgs_batch *b, const float *const *y, float *const *x,
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Compressed sensing over the NCSENSE operator (CS_XSENSE with ft = 3)
+// ===========================================================================
+struct cgs_cs {
+    cgs_plan *p = nullptr;
+    cgs_cs_opts o{};
+    CsTerms tm{};
+    cgs_solve_opts so{};
+    // image vectors (codeare order) and k-space vectors (the plan's sorted layout)
+    float2 *x = nullptr, *g0 = nullptr, *g1 = nullptr, *dx = nullptr;
+    float2 *ksData = nullptr, *ksE = nullptr, *ksG = nullptr;
+    double *partial = nullptr;   // 2 * kCsBlocks * kCsSteps
+    double *sums = nullptr;      // [0..31] objective per step, [32..47] dots, [48] nnz
+    unsigned int *amax = nullptr;
+    int *tally = nullptr;        // solve iterations, NaN flag
+    double *hsums = nullptr;     // pinned copy of sums
+    int solves = 0;
+    double ndnz = 0.0;
+};
+
+namespace {
+
+// slots in cgs_cs::sums
+constexpr int kSumDots = 2 * kCsSteps;  // (re, im) pairs: g0.dx, dx.dx, x.x, gsq[0], gsq[1]
+constexpr int kDotG0Dx = kSumDots, kDotDx = kSumDots + 2, kDotX = kSumDots + 4, kDotGsq = kSumDots + 6;
+constexpr int kSumNnz = kSumDots + 10;
+constexpr int kSumCount = kSumNnz + 1;
+
+// codeare CGLS from p->ksY into p->vX, on the device only (the loop scalars
+// stay there; cs_tally adds its iterations and NaN flag)
+cgs_status cs_solve(cgs_cs *c, cudaStream_t st)
+{
+    cgs_plan *p = c->p;
+    const cgs_solve_opts *o = &c->so;
+    c->solves++;
+    if (o->cgiter == 0) return op_eh_codeare(p, p->ksY, o->ftiter, o->fteps, p->vX, st);  // CGLS.hpp:32-33
+    const bool same = p->solve_exec && p->sg_mode == CGS_MODE_CODEARE && p->sg_toep == 0 &&
+                      p->sg_weighted == o->weighted && p->sg_ftiter == o->ftiter && p->sg_fteps == o->fteps;
+    if (!same) CGS_TRY(build_solve_graph(p, o, st));
+    CGScalars init{};
+    init.lambda = o->lambda;
+    init.tol = o->cgeps;
+    init.maxit = o->cgiter;
+    init.sqrt_mode = 0;
+    CGS_CUDA(cudaMemcpyAsync(p->sc, &init, sizeof(init), cudaMemcpyHostToDevice, st));
+    CGS_CUDA(cudaGraphLaunch(p->solve_exec, st));
+    count_launch((int)p->sg_kpro);
+    return launch_cs_tally(p->sc, c->tally, st);
+}
+
+// g = df(x) (CS_XSENSE.hpp:223-232); leaves E x in ksE for the next Update
+cgs_status cs_df(cgs_cs *c, const float2 *x, float2 *g, cudaStream_t st)
+{
+    cgs_plan *p = c->p;
+    const int64_t nks = p->M * p->nc;
+    CGS_TRY(op_forward(p, x, 0, nullptr, c->ksE, st));
+    CGS_TRY(launch_cs_sub(p->ksY, c->ksE, c->ksData, nks, st));
+    CGS_TRY(cs_solve(c, st));
+    return launch_cs_grad(x, p->vX, c->tm, g, st);
+}
+
+cgs_status cs_read(cgs_cs *c, cudaStream_t st)
+{
+    CGS_CUDA(cudaMemcpyAsync(c->hsums, c->sums, sizeof(double) * kSumCount, cudaMemcpyDeviceToHost, st));
+    CGS_CUDA(cudaStreamSynchronize(st));
+    return CGS_OK;
+}
+
+// one NLCG minimisation of x in place (NLCG.hpp:84-125)
+cgs_status cs_minimise(cgs_cs *c, cgs_cs_report *rep, cudaStream_t st)
+{
+    cgs_plan *p = c->p;
+    const cgs_cs_opts &o = c->o;
+    const int64_t Nt = p->Nt, nks = p->M * p->nc;
+    float t0 = 1.f, t = 1.f;
+    int cur = 0;  // which gsq slot holds |g0|^2
+    CGS_TRY(launch_cs_dot(c->x, c->x, Nt, c->partial, c->sums + kDotX, st));
+    CGS_TRY(cs_df(c, c->x, c->g0, st));
+    CGS_TRY(launch_cs_dot(c->g0, c->g0, Nt, c->partial, c->sums + kDotGsq, st));
+    CGS_TRY(launch_cs_dir(c->dx, c->g0, nullptr, nullptr, Nt, st));
+    double xn = -1.0;
+    for (int k = 0; k < o.nliter; ++k) {
+        // Update(dx): ffdbx = E x is in ksE from the last df, ffdbg = E dx
+        CGS_TRY(op_forward(p, c->dx, 0, nullptr, c->ksG, st));
+        CGS_TRY(launch_cs_dot(c->g0, c->dx, Nt, c->partial, c->sums + kDotG0Dx, st));
+        // f0 and the line search (NLCG.hpp:42-54), kCsSteps - 1 candidates per pass
+        int li = o.lsiter;
+        double rmse = 0.0, f0 = 0.0, g0dx = 0.0;
+        const float tprev = t;
+        for (int base = 0; base < o.lsiter && li == o.lsiter; base += kCsSteps - 1) {
+            CsSteps steps{};
+            steps.t[0] = 0.f;
+            steps.n = 1;
+            for (int i = base; i < o.lsiter && steps.n < kCsSteps; ++i)
+                steps.t[steps.n++] = (float)((double)t0 * std::pow((double)o.lsb, (double)(i + 1)));
+            CGS_TRY(launch_cs_obj(c->ksE, c->ksG, c->ksData, nks, c->x, c->dx, c->tm, steps, c->partial, c->sums, st));
+            CGS_TRY(cs_read(c, st));
+            if (xn < 0.0) xn = std::sqrt(c->hsums[kDotX]);
+            const double *h = c->hsums;
+            f0 = h[0] + h[kCsSteps];
+            g0dx = std::hypot(h[kDotG0Dx], h[kDotG0Dx + 1]);
+            rmse = std::sqrt(h[0] / c->ndnz);
+            for (int j = 1; j < steps.n; ++j) {
+                const double tj = steps.t[j];
+                const double f1 = h[j] + h[kCsSteps + j];
+                const double lim = f0 - (double)o.lsa * (o.parallel_linesearch ? (double)tprev : tj) * g0dx;
+                if (f1 <= lim) {
+                    li = base + j - 1;
+                    t = steps.t[j];
+                    rmse = std::sqrt(h[j] / c->ndnz);
+                    break;
+                }
+            }
+            if (li == o.lsiter && steps.n > 1) rmse = std::sqrt(h[steps.n - 1] / c->ndnz);
+        }
+        if (rep && rep->iterations < 256) {
+            rep->ls_index[rep->iterations] = li;
+            rep->rmse[rep->iterations] = rmse;
+        }
+        if (rep) rep->iterations++;
+        if (li == o.lsiter) return CGS_OK;  // "Reached max line search, exiting"
+        if (li > 2) t0 *= o.lsb;
+        else if (li < 1) t0 /= o.lsb;
+        CGS_TRY(launch_cs_axpy(c->x, c->dx, t, Nt, st));
+        CGS_TRY(cs_df(c, c->x, c->g1, st));
+        double *gsq0 = c->sums + kDotGsq + 2 * cur, *gsq1 = c->sums + kDotGsq + 2 * (1 - cur);
+        CGS_TRY(launch_cs_dot(c->g1, c->g1, Nt, c->partial, gsq1, st));
+        CGS_TRY(launch_cs_dir(c->dx, c->g1, gsq1, gsq0, Nt, st));
+        std::swap(c->g0, c->g1);
+        cur = 1 - cur;
+        CGS_TRY(launch_cs_dot(c->dx, c->dx, Nt, c->partial, c->sums + kDotDx, st));
+        CGS_TRY(cs_read(c, st));
+        if (std::sqrt(c->hsums[kDotDx]) / xn < (double)o.cgconv) break;
+    }
+    return CGS_OK;
+}
+
+cgs_status cs_data_in(cgs_cs *c, const float *y, cudaStream_t st)
+{
+    cgs_plan *p = c->p;
+    const void *src;
+    CGS_TRY(stage_in(y, sizeof(float2) * p->M * p->nc, p->ioA, &src, st));
+    CGS_TRY(launch_gather_ks((const float2 *)src, p->perm, p->M, p->nc, c->ksData, st));
+    CGS_TRY(launch_cs_nnz(c->ksData, p->M * p->nc, c->partial, c->sums + kSumNnz, st));
+    CGS_TRY(cs_read(c, st));
+    c->ndnz = c->hsums[kSumNnz];
+    return CGS_OK;
+}
+
+cgs_status cs_image_in(cgs_plan *p, const float *src, float2 *dst, cudaStream_t st)
+{
+    CGS_CUDA(cudaMemcpyAsync(dst, src, sizeof(float2) * p->Nt,
+                             is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    return CGS_OK;
+}
+
+// TVOP::Trafo's choice of operator (TVOP.hpp:277-295) for a rank-d image
+int cs_tv_mode(int d, const int *dims, int nd)
+{
+    if (d == 2 && (nd == 0 || (nd >= 2 && dims[0] == 1 && dims[1] == 1))) return 1;
+    if (d == 3 && (nd == 0 || (nd >= 3 && dims[0] == 1 && dims[1] == 1 && dims[2] == 1))) return 2;
+    if (d == 3 && nd >= 3 && dims[0] == 0 && dims[1] == 0 && dims[2] == 1) return 3;
+    return -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+cgs_status cgs_cs_create(cgs_cs **out, cgs_plan *p, const cgs_cs_opts *o)
+{
+    if (!out || !o) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    *out = nullptr;
+    CGS_TRY(check_ready(p, true, true));
+    if (o->nlopt != 0 && o->nlopt != 2) { set_error("nlopt: only 0 (NLCG) and 2 (Split Bregman)"); return CGS_ERR_BAD_ARG; }
+    if (o->wl_family != -1) { set_error("wl_family: only -1 (no wavelet) is supported"); return CGS_ERR_BAD_ARG; }
+    if (o->cgiter < 0 || o->ftiter < 0 || o->csiter < 0 || o->nliter < 0 || o->lsiter < 0) {
+        set_error("negative iteration count");
+        return CGS_ERR_BAD_ARG;
+    }
+    CsTerms tm{};
+    // codeare order: axis 0 is the plan's fastest axis
+    tm.D0 = p->N[p->d - 1];
+    tm.D1 = p->d >= 2 ? p->N[p->d - 2] : 1;
+    tm.D2 = p->d >= 3 ? p->N[p->d - 3] : 1;
+    for (int i = 0; i < 2; ++i) {
+        tm.tvw[i] = o->tvw[i];
+        if (o->tvw[i] == 0.f) continue;
+        const int nd = std::max(0, std::min(3, o->ntvdims[i]));
+        tm.tvmode[i] = cs_tv_mode(p->d, o->tvdims[i], nd);
+        if (tm.tvmode[i] < 0) { set_error("no TV operator for these image axes"); return CGS_ERR_BAD_ARG; }
+        if (tm.tvmode[i] != 3 && tm.D0 != tm.D1) { set_error("TV over axes 0 and 1 needs a square image"); return CGS_ERR_BAD_ARG; }
+        if (tm.tvmode[i] == 3 && tm.D2 < 2) { set_error("TV over axis 2 needs at least 2 slices"); return CGS_ERR_BAD_ARG; }
+    }
+    tm.xfmw = o->xfmw;
+    tm.l1 = o->l1;
+    tm.pnorm = o->pnorm;
+    cgs_cs *c = new cgs_cs;
+    c->p = p;
+    c->o = *o;
+    c->tm = tm;
+    c->so.mode = CGS_MODE_CODEARE;
+    c->so.cgiter = o->cgiter;
+    c->so.cgeps = o->cgeps;
+    c->so.lambda = o->lambda;
+    c->so.ftiter = o->ftiter;
+    c->so.fteps = o->fteps;
+    c->so.weighted = 1;
+    const int64_t Nt = p->Nt, nks = p->M * p->nc;
+    cgs_status r = CGS_OK;
+    if (r == CGS_OK) r = dev_alloc(&c->x, Nt);
+    if (r == CGS_OK) r = dev_alloc(&c->g0, Nt);
+    if (r == CGS_OK) r = dev_alloc(&c->g1, Nt);
+    if (r == CGS_OK) r = dev_alloc(&c->dx, Nt);
+    if (r == CGS_OK) r = dev_alloc(&c->ksData, nks);
+    if (r == CGS_OK) r = dev_alloc(&c->ksE, nks);
+    if (r == CGS_OK) r = dev_alloc(&c->ksG, nks);
+    if (r == CGS_OK) r = dev_alloc(&c->partial, (size_t)2 * kCsBlocks * kCsSteps);
+    if (r == CGS_OK) r = dev_alloc(&c->sums, kSumCount);
+    if (r == CGS_OK) r = dev_alloc(&c->amax, 1);
+    if (r == CGS_OK) r = dev_alloc(&c->tally, 2);
+    if (r == CGS_OK && cudaMallocHost((void **)&c->hsums, sizeof(double) * kSumCount) != cudaSuccess) {
+        set_error("cudaMallocHost failed");
+        r = CGS_ERR_OOM;
+    }
+    if (r == CGS_OK && cudaMemset(c->sums, 0, sizeof(double) * kSumCount) != cudaSuccess) r = CGS_ERR_CUDA;
+    if (r != CGS_OK) {
+        cgs_cs_destroy(c);
+        return r;
+    }
+    *out = c;
+    return CGS_OK;
+}
+
+cgs_status cgs_cs_destroy(cgs_cs *c)
+{
+    if (!c) return CGS_OK;
+    cudaSetDevice(c->p->device);
+    cudaStreamSynchronize(c->p->stream);
+    for (void *q : {(void *)c->x, (void *)c->g0, (void *)c->g1, (void *)c->dx, (void *)c->ksData, (void *)c->ksE,
+                    (void *)c->ksG, (void *)c->partial, (void *)c->sums, (void *)c->amax, (void *)c->tally})
+        dev_free(q);
+    if (c->hsums) cudaFreeHost(c->hsums);
+    delete c;
+    return CGS_OK;
+}
+
+cgs_status cgs_cs_adjoint(cgs_cs *c, const float *y, float *x, cgs_cs_report *rep, void *stream)
+{
+    if (!c || !y || !x) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    cgs_plan *p = c->p;
+    CGS_TRY(check_ready(p, true, true));
+    cudaStream_t st = pick_stream(p, stream);
+    if (rep) std::memset(rep, 0, sizeof(*rep));
+    CGS_CUDA(cudaEventRecord(p->ev0, st));
+    c->solves = 0;
+    CGS_CUDA(cudaMemsetAsync(c->tally, 0, 2 * sizeof(int), st));
+    CGS_TRY(cs_data_in(c, y, st));
+    // x0 = ft ->* data, the CG-SENSE solve (CS_XSENSE.hpp:293-297)
+    CGS_CUDA(cudaMemcpyAsync(p->ksY, c->ksData, sizeof(float2) * p->M * p->nc, cudaMemcpyDeviceToDevice, st));
+    CGS_TRY(cs_solve(c, st));
+    CGS_CUDA(cudaMemcpyAsync(c->x, p->vX, sizeof(float2) * p->Nt, cudaMemcpyDeviceToDevice, st));
+    // TV weights *= max |x0| (CS_XSENSE.hpp:303-305; cumulative over calls, as the reference's)
+    CGS_TRY(launch_cs_absmax(c->x, p->Nt, c->amax, st));
+    unsigned int bits = 0;
+    CGS_CUDA(cudaMemcpyAsync(&bits, c->amax, sizeof(bits), cudaMemcpyDeviceToHost, st));
+    CGS_CUDA(cudaStreamSynchronize(st));
+    float ma;
+    std::memcpy(&ma, &bits, sizeof(ma));
+    for (int i = 0; i < 2; ++i) c->tm.tvw[i] *= ma;
+    if (c->o.nlopt == 0)
+        for (int i = 0; i < c->o.csiter; ++i) CGS_TRY(cs_minimise(c, rep, st));
+    CGS_CUDA(cudaEventRecord(p->ev1, st));
+    CGS_TRY(image_out(p, c->x, x, st));
+    int tally[2] = {0, 0};
+    CGS_CUDA(cudaMemcpyAsync(tally, c->tally, sizeof(tally), cudaMemcpyDeviceToHost, st));
+    CGS_CUDA(cudaStreamSynchronize(st));
+    count_launch((int)((int64_t)tally[0] * p->sg_kbody));
+    if (rep) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+        rep->seconds = ms * 1e-3;
+        rep->solves = c->solves;
+        rep->solve_iterations = tally[0];
+        rep->tvw_used[0] = c->tm.tvw[0];
+        rep->tvw_used[1] = c->tm.tvw[1];
+    }
+    if (tally[1]) { set_error("NaN in a CG-SENSE solve"); return CGS_ERR_NAN; }
+    return CGS_OK;
+}
+
+cgs_status cgs_cs_df(cgs_cs *c, const float *y, const float *x, float *g, void *stream)
+{
+    if (!c || !y || !x || !g) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    cgs_plan *p = c->p;
+    CGS_TRY(check_ready(p, true, true));
+    cudaStream_t st = pick_stream(p, stream);
+    c->solves = 0;
+    CGS_CUDA(cudaMemsetAsync(c->tally, 0, 2 * sizeof(int), st));
+    CGS_TRY(cs_data_in(c, y, st));
+    CGS_TRY(cs_image_in(p, x, c->x, st));
+    CGS_TRY(cs_df(c, c->x, c->g0, st));
+    CGS_TRY(image_out(p, c->g0, g, st));
+    int tally[2] = {0, 0};
+    CGS_CUDA(cudaMemcpyAsync(tally, c->tally, sizeof(tally), cudaMemcpyDeviceToHost, st));
+    CGS_CUDA(cudaStreamSynchronize(st));
+    count_launch((int)((int64_t)tally[0] * p->sg_kbody));
+    if (tally[1]) { set_error("NaN in a CG-SENSE solve"); return CGS_ERR_NAN; }
+    return CGS_OK;
+}
+
+cgs_status cgs_cs_obj(cgs_cs *c, const float *y, const float *x, const float *dx, float t, double *obj,
+                      double *rmse, void *stream)
+{
+    if (!c || !y || !x || !dx || !obj) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    cgs_plan *p = c->p;
+    CGS_TRY(check_ready(p, true, true));
+    cudaStream_t st = pick_stream(p, stream);
+    CGS_TRY(cs_data_in(c, y, st));
+    CGS_TRY(cs_image_in(p, x, c->x, st));
+    CGS_TRY(cs_image_in(p, dx, c->dx, st));
+    CGS_TRY(op_forward(p, c->x, 0, nullptr, c->ksE, st));
+    CGS_TRY(op_forward(p, c->dx, 0, nullptr, c->ksG, st));
+    CsSteps steps{};
+    steps.t[0] = t;
+    steps.n = 1;
+    CGS_TRY(launch_cs_obj(c->ksE, c->ksG, c->ksData, p->M * p->nc, c->x, c->dx, c->tm, steps, c->partial, c->sums,
+                          st));
+    CGS_TRY(cs_read(c, st));
+    *obj = c->hsums[0] + c->hsums[kCsSteps];
+    if (rmse) *rmse = std::sqrt(c->hsums[0] / c->ndnz);
+    return CGS_OK;
+}
+
+}  // extern "C"

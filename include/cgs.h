@@ -271,6 +271,65 @@ void cgs_profile_collect(double *ms, int64_t *count);
 /* Text of the last error on this thread ("" if none). */
 const char *cgs_last_error(void);
 
+/* ------------------------------------------------------------------------
+ * Compressed sensing over the NCSENSE operator: codeare's CS_XSENSE with
+ * ft = 3 (src/matrix/ft/CS_XSENSE.hpp:73-140), its TV and L1 penalties
+ * (TVOP.hpp, CS_XSENSE.hpp:329-405) and the NLCG minimiser
+ * (src/optimisation/NLCG.hpp:42-125), as the CompressedSensing module
+ * configures them (src/modules/CompressedSensing.cpp:86-136).  A handle
+ * borrows a plan that has k-space, weights and sensitivities; the plan must
+ * not be used by anyone else while a CS call runs.
+ * ------------------------------------------------------------------------ */
+typedef struct cgs_cs cgs_cs;
+
+typedef struct {
+    /* the NCSENSE inverse (ft ->*): codeare CGLS (keys cgmaxit, cgeps,
+     * lambda, ftmaxit, fteps) */
+    int cgiter;
+    double cgeps, lambda;
+    int ftiter;
+    double fteps;
+    /* minimiser: nlopt 0 = NLCG, 2 = Split Bregman (the reference's is
+     * empty: the result is the CGLS image); 1 (L-BFGS) is not supported */
+    int nlopt, csiter, nliter, lsiter;
+    float lsa, lsb, cgconv;
+    int parallel_linesearch;   /* the reference's parallel rule (NLCG.hpp:56-80) */
+    /* objective: TV weights (scaled by max |x0| in every cgs_cs_adjoint, as
+     * the reference's mutable _tvw), TV'ed axes per term (codeare order;
+     * ntvdims 0 = every axis), L1 weight, smoothing l1, p-norm */
+    float tvw[2];
+    int tvdims[2][3], ntvdims[2];
+    float xfmw, l1, pnorm;
+    int wl_family, wl_member;  /* wavelet: only -1 (none) is supported */
+} cgs_cs_opts;
+
+typedef struct {
+    int iterations;            /* NLCG iterations over all repetitions */
+    int ls_index[256];         /* accepted line-search index per iteration
+                                  (lsiter when the search gave up) */
+    double rmse[256];          /* sqrt(data term / nnz(data)) per iteration */
+    int solves;                /* CGLS solves run */
+    int solve_iterations;      /* their CG iterations */
+    float tvw_used[2];         /* TV weights after the scaling */
+    double seconds;
+} cgs_cs_report;
+
+cgs_status cgs_cs_create(cgs_cs **cs, cgs_plan *plan, const cgs_cs_opts *opts);
+cgs_status cgs_cs_destroy(cgs_cs *cs);
+
+/* x = CS reconstruction of data y ((M, NC) complex): CS_XSENSE::Adjoint /
+ * operator->* (CS_XSENSE.hpp:283-322). */
+cgs_status cgs_cs_adjoint(cgs_cs *cs, const float *y, float *x, cgs_cs_report *report, void *stream);
+
+/* g = gradient of the objective at x for data y (CS_XSENSE::df,
+ * CS_XSENSE.hpp:223-232), with the current TV weights. */
+cgs_status cgs_cs_df(cgs_cs *cs, const float *y, const float *x, float *g, void *stream);
+
+/* Objective at x + t dx for data y (CS_XSENSE::obj after df(x) and
+ * Update(dx), CS_XSENSE.hpp:197-221); *rmse = sqrt(data term / nnz(y)). */
+cgs_status cgs_cs_obj(cgs_cs *cs, const float *y, const float *x, const float *dx, float t, double *obj,
+                      double *rmse, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,199 @@
+"""FP64 restatement of codeare's compressed sensing over the NCSENSE operator.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/ as the checker of the CUDA
+path, never by the product package.
+
+PARITY UNPINNED: the reference ships no test or golden vector for its CS
+code; this restates the reference's source line by line, in FP64, on top of
+the NCSENSE restatement in oracle.py.
+
+  TV operators        src/matrix/TVOP.hpp:37-64 (TV2D), 81-131 (TV3D, all
+                      axes), 134-166 (TV3D, third axis), 277-318 (dispatch)
+  CS objective        src/matrix/ft/CS_XSENSE.hpp:197-255 (obj, df, Update),
+                      279-322 (Adjoint), 329-414 (Obj, TV, XFM, dObj, dXFM, dTV)
+  NLCG                src/optimisation/NLCG.hpp:42-125
+  module keys         src/modules/CompressedSensing.cpp:86-136
+
+Images are numpy arrays in C order, so the codeare (D0, D1[, D2]) image is
+the array of shape ([D2,] D1, D0); the TV code works on its transpose, which
+indexes like codeare's Matrix.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def tv_mode(ndim: int, dims) -> str:
+    """TVOP::Trafo's choice of operator (TVOP.hpp:277-295)."""
+    dims = list(dims or [])
+    if ndim == 2 and (not dims or (len(dims) >= 2 and dims[0] == 1 and dims[1] == 1)):
+        return "2d"
+    if ndim == 3 and (not dims or (len(dims) >= 3 and dims[:3] == [1, 1, 1])):
+        return "3d"
+    if ndim == 3 and len(dims) >= 3 and dims[:3] == [0, 0, 1]:
+        return "z"
+    raise ValueError("no TV operator for %d-D images over axes %s" % (ndim, dims))
+
+
+def tv_fwd(c, mode):
+    """Forward differences of the codeare-ordered image c."""
+    if mode == "2d":  # TVOP.hpp:39-50
+        r = np.zeros(c.shape + (2,), c.dtype)
+        r[:-1, :, 0] = c[1:, :] - c[:-1, :]
+        r[:, :-1, 1] = c[:, 1:] - c[:, :-1]
+        return r
+    if mode == "3d":  # TVOP.hpp:83-99: the third loop writes component 1 again
+        r = np.zeros(c.shape + (3,), c.dtype)
+        r[:-1, :, :, 0] = c[1:] - c[:-1]
+        r[:, :-1, :, 1] = c[:, 1:, :] - c[:, :-1, :]
+        r[:, :, :-1, 1] = c[:, :, 1:] - c[:, :, :-1]
+        return r
+    if mode == "z":  # TVOP.hpp:135-144
+        r = np.zeros_like(c)
+        r[:, :, :-1] = c[:, :, 1:] - c[:, :, :-1]
+        return r
+    raise ValueError(mode)
+
+
+def tv_adj(A, mode):
+    """The reference's adjoints: interior ranges only for 2d/3d (their border
+    rows stay zero), a complete adjoint for z."""
+    if mode == "2d":  # TVOP.hpp:52-63 (square images)
+        M, N = A.shape[0], A.shape[1]
+        r = np.zeros((M, N), A.dtype)
+        r[1:N - 1, :] = A[0:N - 2, :, 0] - A[1:N - 1, :, 0]
+        r[:, 1:M - 1] += A[:, 0:M - 2, 1] - A[:, 1:M - 1, 1]
+        return r
+    if mode == "3d":  # TVOP.hpp:101-118
+        M, N, L = A.shape[0], A.shape[1], A.shape[2]
+        r = np.zeros((M, N, L), A.dtype)
+        r[1:N - 1, :, :] = A[0:N - 2, :, :, 0] - A[1:N - 1, :, :, 0]
+        r[:, 1:M - 1, :] += A[:, 0:M - 2, :, 1] - A[:, 1:M - 1, :, 1]
+        r[:, :, 1:L - 1] += A[:, :, 0:L - 2, 2] - A[:, :, 1:L - 1, 2]
+        return r
+    if mode == "z":  # TVOP.hpp:146-165
+        L = A.shape[2]
+        r = np.zeros_like(A)
+        r[:, :, 1:L - 1] = A[:, :, 0:L - 2] - A[:, :, 1:L - 1]
+        r[:, :, 0] = -A[:, :, 0]
+        r[:, :, L - 1] = A[:, :, L - 2]
+        return r
+    raise ValueError(mode)
+
+
+def _pw(v, l1, e):
+    """(|v|^2 + l1)^e, the reference's om *= conj(om); om += l1; om ^= e."""
+    return (np.abs(v) ** 2 + l1) ** e
+
+
+class CSXSense:
+    """CS_XSENSE<cxfl> with ft = 3 (NCSENSE) and no wavelet."""
+
+    def __init__(self, sense, tvw=(0.0, 0.0), tvdims=(None, None), xfmw=0.0, l1=0.0, pnorm=0.0,
+                 nlopt=0, csiter=1, nliter=4, lsiter=8, lsa=0.01, lsb=0.6, cgconv=1e-4,
+                 parallel_linesearch=False, cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3):
+        self.s = sense
+        self.nd = len(sense.shape)
+        self.tvw = [float(tvw[0]), float(tvw[1])]
+        self.modes = [tv_mode(self.nd, tvdims[0]) if tvw[0] else None,
+                      tv_mode(self.nd, tvdims[1]) if tvw[1] else None]
+        self.xfmw, self.l1, self.p = float(xfmw), float(l1), float(pnorm)
+        self.nlopt, self.csiter, self.nliter, self.lsiter = nlopt, csiter, nliter, lsiter
+        self.lsa, self.lsb, self.cgconv, self.pls = float(lsa), float(lsb), float(cgconv), parallel_linesearch
+        self.solve = dict(cgiter=cgiter, cgeps=cgeps, lam=lam, ftiter=ftiter, fteps=fteps)
+        self.log = []
+
+    # the NCSENSE operator: * and ->*
+    def E(self, x):
+        return self.s.trafo(x)
+
+    def Einv(self, y):
+        return self.s.cgls_codeare(y, **self.solve)[0]
+
+    def _c(self, x):  # codeare-ordered view
+        return np.asarray(x).T
+
+    def set_data(self, y):
+        self.data = np.asarray(y, np.complex128).reshape(self.s.nc, -1)
+        self.ndnz = float(np.count_nonzero(self.data))
+
+    # CS_XSENSE.hpp:223-232
+    def df(self, x):
+        self.wx = x
+        g = 2.0 * self.Einv(self.E(x) - self.data)  # dObj, :367-372
+        if self.xfmw:  # dXFM, :383-385
+            g = g + self.xfmw * (x * _pw(x, self.l1, 0.5 * self.p - 1.0))
+        for i in range(2):
+            if self.tvw[i]:  # dTV, :395-405
+                d = tv_fwd(self._c(self.wx), self.modes[i])
+                G = self.p * (d * _pw(d, self.l1, 0.5 * self.p - 1.0))
+                g = g + self.tvw[i] * tv_adj(G, self.modes[i]).T
+        return g
+
+    # CS_XSENSE.hpp:234-255
+    def update(self, dx):
+        self.ffdbx = self.E(self.wx)
+        self.ffdbg = self.E(dx)
+        self.ttdbx = [tv_fwd(self._c(self.wx), m) if m else None for m in self.modes]
+        self.ttdbg = [tv_fwd(self._c(dx), m) if m else None for m in self.modes]
+
+    # CS_XSENSE.hpp:197-221, 329-365
+    def obj(self, x, dx, t):
+        om = self.ffdbx + t * self.ffdbg if t > 0 else self.ffdbx
+        o = float(np.sum(np.abs(om - self.data) ** 2))
+        rmse = np.sqrt(o / self.ndnz)
+        for i in range(2):
+            if self.tvw[i]:
+                u = self.ttdbx[i] + t * self.ttdbg[i] if t > 0 else self.ttdbx[i]
+                o += self.tvw[i] * float(np.sum(_pw(u, self.l1, 0.5 * self.p)))
+        if self.xfmw:
+            u = x + t * dx if t > 0 else x
+            o += self.xfmw * float(np.sum(_pw(u, self.l1, 0.5 * self.p)))
+        return o, rmse
+
+    # NLCG.hpp:84-125 (the sequential line search, :42-54; with
+    # parallel_linesearch the test uses the previous step t, :56-80, and a
+    # search that accepts nothing reports the last trial's rmse here, where
+    # the reference reads rmses[-1])
+    def minimise(self, x):
+        t0, t = 1.0, 1.0
+        xn = np.linalg.norm(x)
+        g0 = self.df(x)
+        dx = -g0
+        for k in range(self.nliter):
+            self.update(dx)
+            f0, rmse = self.obj(x, dx, 0.0)
+            g0dx = abs(np.vdot(g0, dx))
+            li, tprev = self.lsiter, t
+            for i in range(self.lsiter):
+                ti = t0 * self.lsb ** (i + 1)
+                f1, rmse = self.obj(x, dx, ti)  # rmse is an output of every obj call
+                if f1 <= f0 - self.lsa * (tprev if self.pls else ti) * g0dx:
+                    li, t = i, ti
+                    break
+            self.log.append((li, rmse))
+            if li == self.lsiter:
+                return x
+            if li > 2:
+                t0 *= self.lsb
+            elif li < 1:
+                t0 /= self.lsb
+            x = x + dx * t
+            g1 = self.df(x)
+            bk = np.vdot(g1, g1).real / np.vdot(g0, g0).real
+            g0 = g1
+            dx = -g1 + dx * bk
+            if np.linalg.norm(dx) / xn < self.cgconv:
+                break
+        return x
+
+    # CS_XSENSE.hpp:283-322
+    def adjoint(self, y):
+        self.set_data(y)
+        x = self.Einv(self.data)
+        ma = float(np.abs(x).max())
+        self.tvw = [w * ma for w in self.tvw]
+        for _ in range(self.csiter):
+            if self.nlopt == 0:
+                x = self.minimise(x)
+        return x
