@@ -160,6 +160,8 @@ public:
     virtual Matrix<T> operator->*(const MatrixType<T> &m) const { return Adjoint(m); }
 
     size_t KSpaceSize() const { return m_nk; }
+    const std::vector<size_t> &ImageSize() const { return m_imsz; }
+    cgs_plan *Plan() const { return m_plan; }  // the operator's plan (for callers that build on it)
     const cgs_solve_report &LastReport() const { return m_last; }
 
     virtual std::ostream &Print(std::ostream &os) const

@@ -31,8 +31,9 @@ def test_plugin_exports_reconstrategy_factories():
     import ctypes
     from codeare_gb300 import build
     build.build()
-    P = ctypes.CDLL(build.PLUGIN)
-    assert hasattr(P, "create") and hasattr(P, "destroy")
+    for so in (build.PLUGIN, build.PLUGIN_NUFFT, build.PLUGIN_ESTSENS, build.PLUGIN_CS):
+        P = ctypes.CDLL(so)
+        assert hasattr(P, "create") and hasattr(P, "destroy"), so
     assert os.access(build.DRIVER, os.X_OK)
 
 

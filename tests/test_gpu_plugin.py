@@ -179,3 +179,33 @@ def test_plugin_from_cod_files(gpu, tmp_path):
     img, name, _ = cod.read(str(out))
     assert name == "image" and img.dtype == np.complex64 and img.shape == ref.shape
     assert np.array_equal(img, ref)
+
+
+def test_compressed_sensing_plugin_matches_oracle(gpu, tmp_path):
+    """CompressedSensing.so with ft = 3 through the plugin host: the keys of
+    src/modules/CompressedSensing.cpp:31-136, compared with the FP64
+    restatement of CS_XSENSE + NLCG."""
+    from codeare_gb300 import build, cgsm, synth
+    from oracle import oracle as O, cs
+    cfg = synth.small_config(N=32, nc=4, nspokes=32, nsamp=64, alpha=1.0, m=1)
+    k, w, S = cfg["k"], cfg["w"], cfg["sens"]
+    s = O.Sense(S, k, w=w, m=1, alpha=1.0)
+    y = synth.add_noise(s.trafo(cfg["image"]), 1e-3, seed=4)
+    o = cs.CSXSense(s, tvw=(2e-3, 0.0), xfmw=5e-3, l1=1e-15, pnorm=1.0, csiter=2, nliter=4, lsiter=10,
+                    lsa=1e-3, lsb=0.6, cgconv=1e-5, cgiter=6, cgeps=1e-7, lam=5e-2, ftiter=3, fteps=1e-3)
+    xo = o.adjoint(y)
+    attrs = {"ftdims": "32 32", "ft": 3, "test_case": 0, "noise": 0, "verbose": 1, "nk": k.shape[0],
+             "ftmaxit": 3, "fteps": 1e-3, "cgmaxit": 6, "cgeps": 1e-7, "lambda": 5e-2, "ftalpha": 1.0,
+             "cart_3rd_dim": 0, "threads": 1, "nlopt": 0, "parallel_linesearch": 0, "tvw1": 2e-3, "tvw2": 0,
+             "tv1": "1 1", "xfmw": 5e-3, "l1": 1e-15, "lsa": 1e-3, "lsb": 0.6, "pnorm": 1, "wl_family": -1,
+             "wl_member": 0, "csiter": 2, "cgiter": 4, "cgconv": 1e-5, "lsiter": 10}
+    inp, out, xml = tmp_path / "in.cgsm", tmp_path / "out.cgsm", tmp_path / "cfg.xml"
+    cgsm.write(str(inp), {"sensitivities": S, "kspace": k, "weights": w, "data": y.astype(np.complex64)})
+    xml.write_text("<CompressedSensing " + " ".join('%s="%s"' % kv for kv in attrs.items()) + "/>\n")
+    r = subprocess.run([build.DRIVER, build.PLUGIN_CS, str(xml), str(inp), str(out), "im_dc"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    img = cgsm.read(str(out))["im_dc"]
+    assert img.shape == (32, 32)
+    assert rel(img, xo) < 2e-3, r.stdout
+    assert "%d NLCG iterations" % len(o.log) in r.stdout
