@@ -30,6 +30,7 @@ EXPORTED = [
     "cgs_net_forward", "cgs_net_gradients", "cgs_net_train_step", "cgs_solve_fcg", "cgs_normal_apply",
     "cgs_get_tuning", "cgs_set_tuning", "cgs_autotune", "cgs_batch_create", "cgs_batch_solve",
     "cgs_batch_destroy", "cgs_cs_create", "cgs_cs_destroy", "cgs_cs_adjoint", "cgs_cs_df", "cgs_cs_obj",
+    "cgs_cs_wavelet",
 ]
 PROFILE_CATEGORIES = ("fft", "interp", "spread")
 
@@ -135,6 +136,7 @@ def load(path: str = LIB_PATH):
     L.cgs_cs_adjoint.argtypes = [vp, vp, vp, C.POINTER(CsReport), vp]
     L.cgs_cs_df.argtypes = [vp, vp, vp, vp, vp]
     L.cgs_cs_obj.argtypes = [vp, vp, vp, vp, C.c_float, C.POINTER(C.c_double), C.POINTER(C.c_double), vp]
+    L.cgs_cs_wavelet.argtypes = [vp, vp, vp, C.c_int, vp]
     for name in EXPORTED:
         if name not in ("cgs_kernel_launches", "cgs_last_error", "cgs_profile_enable",
                         "cgs_profile_collect", "cgs_net_num_params"):
@@ -383,6 +385,11 @@ class CS:
                     rmse=[rep.rmse[i] for i in range(n)], solves=rep.solves,
                     solve_iterations=rep.solve_iterations, tvw_used=(rep.tvw_used[0], rep.tvw_used[1]),
                     seconds=rep.seconds)
+
+    def wavelet(self, x, out, inverse=False, stream=None):
+        """out = W x (or W^-1 x), the handle's wavelet transform"""
+        self._go(load().cgs_cs_wavelet, _ptr(x), _ptr(out), int(bool(inverse)), stream=stream)
+        return out
 
     def df(self, y, x, out, stream=None):
         self._go(load().cgs_cs_df, _ptr(y), _ptr(x), _ptr(out), stream=stream)

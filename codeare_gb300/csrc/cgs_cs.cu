@@ -139,8 +139,11 @@ __global__ void __launch_bounds__(kT) cs_obj_ks_kernel(const float2 *__restrict_
 
 // TV and L1 terms per step (CS_XSENSE.hpp:337-365): for each TV term
 // tvw * sum (|TV x + t TV dx|^2 + l1)^(p/2) over every component (zeros
-// included), and xfmw * sum (|x + t dx|^2 + l1)^(p/2)
+// included), and xfmw * sum (|lx + t ldx|^2 + l1)^(p/2).  With a wavelet
+// transform x, dx are the images and lx, ldx the NLCG variables (wavelet
+// coefficients); without one they are the same arrays.
 __global__ void __launch_bounds__(kT) cs_obj_img_kernel(const float2 *__restrict__ x, const float2 *__restrict__ dx,
+                                                        const float2 *__restrict__ lx, const float2 *__restrict__ ldx,
                                                         CsTerms g, CsSteps st, double *__restrict__ partial)
 {
     double acc[kCsSteps];
@@ -169,7 +172,7 @@ __global__ void __launch_bounds__(kT) cs_obj_img_kernel(const float2 *__restrict
             }
         }
         if (g.xfmw != 0.f) {
-            const float2 u = x[q], v = dx[q];
+            const float2 u = lx[q], v = ldx[q];
 #pragma unroll
             for (int k = 0; k < kCsSteps; ++k) {
                 if (k < st.n) {
@@ -266,6 +269,93 @@ __global__ void __launch_bounds__(kT) cs_grad_kernel(const float2 *__restrict__ 
     }
 }
 
+// g += xfmw x (|x|^2 + l1)^(p/2-1) (dXFM, CS_XSENSE.hpp:383-385)
+__global__ void __launch_bounds__(kT) cs_l1grad_kernel(float2 *__restrict__ g, const float2 *__restrict__ x,
+                                                       CsTerms t, int64_t n)
+{
+    for (int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT) {
+        const float2 u = x[i];
+        const float f = pw(u, t.l1, 0.5f * t.pnorm - 1.0f);
+        float2 r = g[i];
+        r.x += t.xfmw * (u.x * f);
+        r.y += t.xfmw * (u.y * f);
+        g[i] = r;
+    }
+}
+
+// One pass of the periodic wavelet transform along one axis of the n x n
+// top-left block of an ld x ld image (DWT.hpp:354-418 per level; filters
+// along a line DWT.hpp:644-740): coefficient k < n/2 of a line is
+// sum_h lo[h] s[(2k + h) mod n], coefficient n/2 + i is
+// sum_h hi[h] s[(2i + 1 - h) mod n].  Thread per output value; axis 1 maps
+// consecutive threads to consecutive columns so both axes coalesce.
+__global__ void __launch_bounds__(kT) dwt_down_kernel(const float2 *__restrict__ src, float2 *__restrict__ dst,
+                                                      int ld, int n, int axis, DwtFilt f)
+{
+    const int64_t total = (int64_t)n * n;
+    for (int64_t t = (int64_t)blockIdx.x * kT + threadIdx.x; t < total; t += (int64_t)gridDim.x * kT) {
+        int line, k;
+        if (axis == 0) { line = (int)(t / n); k = (int)(t % n); }
+        else { k = (int)(t / n); line = (int)(t % n); }
+        const int64_t base = axis == 0 ? (int64_t)line * ld : line;
+        const int64_t step = axis == 0 ? 1 : ld;
+        float2 s = make_float2(0.f, 0.f);
+        if (k < n / 2) {
+            for (int h = 0; h < f.fl; ++h) {
+                int j = 2 * k + h;
+                j %= n;
+                const float2 v = src[base + j * step];
+                s.x += f.lo[h] * v.x;
+                s.y += f.lo[h] * v.y;
+            }
+        } else {
+            const int i = k - n / 2;
+            for (int h = 0; h < f.fl; ++h) {
+                int j = (2 * i + 1 - h) % n;
+                if (j < 0) j += n;
+                const float2 v = src[base + j * step];
+                s.x += f.hi[h] * v.x;
+                s.y += f.hi[h] * v.y;
+            }
+        }
+        dst[base + (int64_t)k * step] = s;
+    }
+}
+
+// One inverse pass along one axis of the n2 x n2 top-left block (n2 = 2 *
+// half; DWT.hpp:756-823 per level, DWT.hpp:1046-1180 along a line):
+// out[2i + e] = sum_h lo[2h + e] low[(i - h) mod half]
+//             + sum_h hi[2h + 1 - e] high[(i + h) mod half]
+__global__ void __launch_bounds__(kT) dwt_up_kernel(const float2 *__restrict__ src, float2 *__restrict__ dst,
+                                                    int ld, int n2, int axis, DwtFilt f)
+{
+    const int64_t total = (int64_t)n2 * n2;
+    const int half = n2 / 2, m2 = f.fl / 2;
+    for (int64_t t = (int64_t)blockIdx.x * kT + threadIdx.x; t < total; t += (int64_t)gridDim.x * kT) {
+        int line, m;
+        if (axis == 0) { line = (int)(t / n2); m = (int)(t % n2); }
+        else { m = (int)(t / n2); line = (int)(t % n2); }
+        const int64_t base = axis == 0 ? (int64_t)line * ld : line;
+        const int64_t step = axis == 0 ? 1 : ld;
+        const int i = m >> 1, e = m & 1;
+        float2 lo = make_float2(0.f, 0.f), hi = make_float2(0.f, 0.f);
+        for (int h = 0; h < m2; ++h) {
+            int j = (i - h) % half;
+            if (j < 0) j += half;
+            const float2 v = src[base + (int64_t)j * step];
+            lo.x += f.lo[2 * h + e] * v.x;
+            lo.y += f.lo[2 * h + e] * v.y;
+        }
+        for (int h = 0; h < m2; ++h) {
+            const int j = (i + h) % half;
+            const float2 v = src[base + (int64_t)(half + j) * step];
+            hi.x += f.hi[2 * h + 1 - e] * v.x;
+            hi.y += f.hi[2 * h + 1 - e] * v.y;
+        }
+        dst[base + (int64_t)m * step] = make_float2(lo.x + hi.x, lo.y + hi.y);
+    }
+}
+
 __global__ void __launch_bounds__(kT) cs_axpy_kernel(float2 *__restrict__ x, const float2 *__restrict__ dx, float t,
                                                      int64_t n)
 {
@@ -318,8 +408,8 @@ int grid_for(int64_t n)
 }  // namespace
 
 cgs_status launch_cs_obj(const float2 *ksA, const float2 *ksB, const float2 *ksY, int64_t nks, const float2 *x,
-                         const float2 *dx, const CsTerms &terms, const CsSteps &steps, double *partial, double *out,
-                         cudaStream_t st)
+                         const float2 *dx, const float2 *lx, const float2 *ldx, const CsTerms &terms,
+                         const CsSteps &steps, double *partial, double *out, cudaStream_t st)
 {
     const int gk = grid_for(nks);
     cs_obj_ks_kernel<<<gk, kT, 0, st>>>(ksA, ksB, ksY, nks, steps, partial);
@@ -329,7 +419,7 @@ cgs_status launch_cs_obj(const float2 *ksA, const float2 *ksB, const float2 *ksY
     const int64_t nimg = (int64_t)terms.D0 * terms.D1 * terms.D2;
     const int gi = grid_for(nimg);
     double *pimg = partial + (int64_t)kCsBlocks * kCsSteps;
-    cs_obj_img_kernel<<<gi, kT, 0, st>>>(x, dx, terms, steps, pimg);
+    cs_obj_img_kernel<<<gi, kT, 0, st>>>(x, dx, lx, ldx, terms, steps, pimg);
     CGS_LAUNCH_CHECK();
     cs_colsum_kernel<<<kCsSteps, kT, 0, st>>>(pimg, gi, kCsSteps, out + kCsSteps);
     CGS_LAUNCH_CHECK();
@@ -369,6 +459,25 @@ cgs_status launch_cs_grad(const float2 *x, const float2 *ehr, const CsTerms &ter
 {
     const int64_t n = (int64_t)terms.D0 * terms.D1 * terms.D2;
     cs_grad_kernel<<<grid_for(n), kT, 0, st>>>(x, ehr, terms, g);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_cs_l1grad(float2 *g, const float2 *x, const CsTerms &terms, int64_t n, cudaStream_t st)
+{
+    cs_l1grad_kernel<<<grid_for(n), kT, 0, st>>>(g, x, terms, n);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_dwt_pass(const float2 *src, float2 *dst, int ld, int n, int axis, int inverse, const DwtFilt &f,
+                           cudaStream_t st)
+{
+    const int64_t total = (int64_t)n * n;
+    const int64_t b = (total + kT - 1) / kT;
+    const int grid = (int)(b < 4 * kCsBlocks ? b : 4 * kCsBlocks);
+    if (inverse) dwt_up_kernel<<<grid, kT, 0, st>>>(src, dst, ld, n, axis, f);
+    else dwt_down_kernel<<<grid, kT, 0, st>>>(src, dst, ld, n, axis, f);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }

@@ -316,12 +316,24 @@ struct CsSteps {
     float t[kCsSteps];
     int n;
 };
+// wavelet decomposition filters (high[i] = (-1)^i low[i]), at most 8 taps
+struct DwtFilt {
+    float lo[8], hi[8];
+    int fl;
+};
 // out[0..15]: data term per step over the k-space arrays (ffdbx = ksA,
-// ffdbg = ksB, data = ksY); out[16..31]: TV and L1 terms per step.
-// partial holds 2 * kCsBlocks * kCsSteps doubles.
+// ffdbg = ksB, data = ksY); out[16..31]: TV terms of the images x, dx and
+// L1 terms of lx, ldx per step.  partial holds 2 * kCsBlocks * kCsSteps doubles.
 cgs_status launch_cs_obj(const float2 *ksA, const float2 *ksB, const float2 *ksY, int64_t nks, const float2 *x,
-                         const float2 *dx, const CsTerms &terms, const CsSteps &steps, double *partial, double *out,
-                         cudaStream_t st);
+                         const float2 *dx, const float2 *lx, const float2 *ldx, const CsTerms &terms,
+                         const CsSteps &steps, double *partial, double *out, cudaStream_t st);
+// g += the L1 gradient at x
+cgs_status launch_cs_l1grad(float2 *g, const float2 *x, const CsTerms &terms, int64_t n, cudaStream_t st);
+// one wavelet pass along `axis` of the top-left n x n block of an ld x ld
+// image: decomposition (inverse 0) or reconstruction (inverse 1); src and
+// dst must differ
+cgs_status launch_dwt_pass(const float2 *src, float2 *dst, int ld, int n, int axis, int inverse, const DwtFilt &f,
+                           cudaStream_t st);
 // out2 = (Re, Im) sum conj(a) b
 cgs_status launch_cs_dot(const float2 *a, const float2 *b, int64_t n, double *partial, double *out2,
                          cudaStream_t st);

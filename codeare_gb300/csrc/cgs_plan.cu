@@ -15,6 +15,7 @@
 #include <initializer_list>
 #include <atomic>
 #include <chrono>
+#include <complex>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -1814,6 +1815,7 @@ cgs_status cgs_batch_solve(cgs_batch *b, const float *const *y, float *const *x,
 // ===========================================================================
 struct cgs_cs {
     cgs_plan *p = nullptr;
+    int device = 0;  // the plan's device (destroy must not touch the plan, which may be gone)
     cgs_cs_opts o{};
     CsTerms tm{};
     cgs_solve_opts so{};
@@ -1827,6 +1829,12 @@ struct cgs_cs {
     double *hsums = nullptr;     // pinned copy of sums
     int solves = 0;
     double ndnz = 0.0;
+    // wavelet transform (the NLCG variable is the coefficient array when on)
+    bool dwt = false;
+    int dwt_levels = 0;
+    DwtFilt filt{};
+    float2 *wx = nullptr, *wdx = nullptr, *wtmp = nullptr, *wu = nullptr;
+    const float2 *wxp = nullptr;  // image of the last df's x (x itself without a wavelet)
 };
 
 namespace {
@@ -1859,15 +1867,56 @@ cgs_status cs_solve(cgs_cs *c, cudaStream_t st)
     return launch_cs_tally(p->sc, c->tally, st);
 }
 
-// g = df(x) (CS_XSENSE.hpp:223-232); leaves E x in ksE for the next Update
+// out = W in (inverse 0) or W^-1 in (inverse 1), the reference's DWT
+// operator * and ->* (DWT.hpp:354-418, 756-823); a copy without a wavelet
+cgs_status cs_dwt(cgs_cs *c, const float2 *in, float2 *out, int inverse, cudaStream_t st)
+{
+    cgs_plan *p = c->p;
+    if (in != out) CGS_CUDA(cudaMemcpyAsync(out, in, sizeof(float2) * p->Nt, cudaMemcpyDeviceToDevice, st));
+    if (!c->dwt) return CGS_OK;
+    const int S = c->tm.D0;
+    if (!inverse) {
+        int n = S;
+        for (int l = 0; l < c->dwt_levels; ++l, n /= 2) {
+            CGS_TRY(launch_dwt_pass(out, c->wtmp, S, n, 0, 0, c->filt, st));
+            CGS_TRY(launch_dwt_pass(c->wtmp, out, S, n, 1, 0, c->filt, st));
+        }
+    } else {
+        int n = S >> c->dwt_levels;
+        for (int l = 0; l < c->dwt_levels; ++l, n *= 2) {
+            CGS_TRY(launch_dwt_pass(out, c->wtmp, S, 2 * n, 1, 1, c->filt, st));
+            CGS_TRY(launch_dwt_pass(c->wtmp, out, S, 2 * n, 0, 1, c->filt, st));
+        }
+    }
+    return CGS_OK;
+}
+
+// g = df(x) (CS_XSENSE.hpp:223-232); leaves E wx in ksE and wx in wxp for
+// the next Update and objective
 cgs_status cs_df(cgs_cs *c, const float2 *x, float2 *g, cudaStream_t st)
 {
     cgs_plan *p = c->p;
     const int64_t nks = p->M * p->nc;
-    CGS_TRY(op_forward(p, x, 0, nullptr, c->ksE, st));
+    if (c->dwt) CGS_TRY(cs_dwt(c, x, c->wx, 1, st));
+    c->wxp = c->dwt ? c->wx : x;
+    CGS_TRY(op_forward(p, c->wxp, 0, nullptr, c->ksE, st));
     CGS_TRY(launch_cs_sub(p->ksY, c->ksE, c->ksData, nks, st));
     CGS_TRY(cs_solve(c, st));
-    return launch_cs_grad(x, p->vX, c->tm, g, st);
+    if (!c->dwt) return launch_cs_grad(x, p->vX, c->tm, g, st);
+    // W (2 ehr + TV terms of wx) + the L1 term of the coefficients
+    CsTerms img = c->tm;
+    img.xfmw = 0.f;
+    CGS_TRY(launch_cs_grad(c->wxp, p->vX, img, c->wu, st));
+    CGS_TRY(cs_dwt(c, c->wu, g, 0, st));
+    return c->tm.xfmw != 0.f ? launch_cs_l1grad(g, x, c->tm, p->Nt, st) : CGS_OK;
+}
+
+// Update(dx): ffdbg = E W^-1 dx (CS_XSENSE.hpp:234-236); returns the image of dx
+cgs_status cs_update(cgs_cs *c, const float2 *dx, const float2 **wdxp, cudaStream_t st)
+{
+    if (c->dwt) CGS_TRY(cs_dwt(c, dx, c->wdx, 1, st));
+    *wdxp = c->dwt ? c->wdx : dx;
+    return op_forward(c->p, *wdxp, 0, nullptr, c->ksG, st);
 }
 
 cgs_status cs_read(cgs_cs *c, cudaStream_t st)
@@ -1891,8 +1940,9 @@ cgs_status cs_minimise(cgs_cs *c, cgs_cs_report *rep, cudaStream_t st)
     CGS_TRY(launch_cs_dir(c->dx, c->g0, nullptr, nullptr, Nt, st));
     double xn = -1.0;
     for (int k = 0; k < o.nliter; ++k) {
-        // Update(dx): ffdbx = E x is in ksE from the last df, ffdbg = E dx
-        CGS_TRY(op_forward(p, c->dx, 0, nullptr, c->ksG, st));
+        // Update(dx): ffdbx = E wx is in ksE from the last df, ffdbg = E wdx
+        const float2 *wdxp = nullptr;
+        CGS_TRY(cs_update(c, c->dx, &wdxp, st));
         CGS_TRY(launch_cs_dot(c->g0, c->dx, Nt, c->partial, c->sums + kDotG0Dx, st));
         // f0 and the line search (NLCG.hpp:42-54), kCsSteps - 1 candidates per pass
         int li = o.lsiter;
@@ -1904,7 +1954,8 @@ cgs_status cs_minimise(cgs_cs *c, cgs_cs_report *rep, cudaStream_t st)
             steps.n = 1;
             for (int i = base; i < o.lsiter && steps.n < kCsSteps; ++i)
                 steps.t[steps.n++] = (float)((double)t0 * std::pow((double)o.lsb, (double)(i + 1)));
-            CGS_TRY(launch_cs_obj(c->ksE, c->ksG, c->ksData, nks, c->x, c->dx, c->tm, steps, c->partial, c->sums, st));
+            CGS_TRY(launch_cs_obj(c->ksE, c->ksG, c->ksData, nks, c->wxp, wdxp, c->x, c->dx, c->tm, steps,
+                                  c->partial, c->sums, st));
             CGS_TRY(cs_read(c, st));
             if (xn < 0.0) xn = std::sqrt(c->hsums[kDotX]);
             const double *h = c->hsums;
@@ -1965,6 +2016,65 @@ cgs_status cs_image_in(cgs_plan *p, const float *src, float2 *dst, cudaStream_t 
     return CGS_OK;
 }
 
+// Minimum-phase Daubechies low-pass filter with p = taps / 2 vanishing
+// moments (I. Daubechies, Comm. Pure Appl. Math. 41 (1988) 909-996), by
+// spectral factorisation: the roots y_k of P(y) = sum_k C(p-1+k, k) y^k
+// (Durand-Kerner iteration), each mapped to the root w_k of
+// w + 1/w = 2 - 4 y_k outside the unit circle; h(w) = (1 + w)^p prod (w - w_k)
+// in ascending powers, scaled to sum sqrt(2).  p = 1 is the Haar filter.
+std::vector<double> daubechies(int taps)
+{
+    typedef std::complex<double> cd;
+    const int p = taps / 2, deg = p - 1;
+    std::vector<cd> poly(1, cd(1.0, 0.0));
+    auto mul = [&](cd a0, cd a1) {  // poly *= a0 + a1 w
+        std::vector<cd> r(poly.size() + 1, cd(0.0, 0.0));
+        for (size_t i = 0; i < poly.size(); ++i) {
+            r[i] += poly[i] * a0;
+            r[i + 1] += poly[i] * a1;
+        }
+        poly.swap(r);
+    };
+    for (int i = 0; i < p; ++i) mul(cd(1.0, 0.0), cd(1.0, 0.0));
+    if (deg > 0) {
+        std::vector<double> c(p);
+        for (int k = 0; k < p; ++k) {
+            double b = 1.0;  // C(p-1+k, k)
+            for (int j = 1; j <= k; ++j) b = b * (p - 1 + j) / j;
+            c[k] = b;
+        }
+        auto eval = [&](cd x) {  // monic P
+            cd v(0.0, 0.0);
+            for (int k = deg; k >= 0; --k) v = v * x + c[k] / c[deg];
+            return v;
+        };
+        std::vector<cd> z(deg);
+        for (int i = 0; i < deg; ++i) z[i] = std::pow(cd(0.4, 0.9), i);
+        for (int it = 0; it < 1000; ++it) {
+            double delta = 0.0;
+            for (int i = 0; i < deg; ++i) {
+                cd den(1.0, 0.0);
+                for (int j = 0; j < deg; ++j)
+                    if (j != i) den *= z[i] - z[j];
+                const cd step = eval(z[i]) / den;
+                z[i] -= step;
+                delta = std::max(delta, std::abs(step));
+            }
+            if (delta < 1e-16) break;
+        }
+        for (const cd &y : z) {
+            const cd b = 2.0 - 4.0 * y, q = std::sqrt(b * b - 4.0);
+            const cd w1 = 0.5 * (b + q), w2 = 0.5 * (b - q);
+            mul(-(std::abs(w1) > std::abs(w2) ? w1 : w2), cd(1.0, 0.0));
+        }
+    }
+    std::vector<double> h(poly.size());
+    double sum = 0.0;
+    for (size_t i = 0; i < h.size(); ++i) sum += (h[i] = poly[i].real());
+    for (double &v : h) v *= std::sqrt(2.0) / sum;
+    return h;
+}
+
 // TVOP::Trafo's choice of operator (TVOP.hpp:277-295) for a rank-d image
 int cs_tv_mode(int d, const int *dims, int nd)
 {
@@ -1984,7 +2094,13 @@ cgs_status cgs_cs_create(cgs_cs **out, cgs_plan *p, const cgs_cs_opts *o)
     *out = nullptr;
     CGS_TRY(check_ready(p, true, true));
     if (o->nlopt != 0 && o->nlopt != 2) { set_error("nlopt: only 0 (NLCG) and 2 (Split Bregman)"); return CGS_ERR_BAD_ARG; }
-    if (o->wl_family != -1) { set_error("wl_family: only -1 (no wavelet) is supported"); return CGS_ERR_BAD_ARG; }
+    // the reference initialises filters for Daubechies 4 / 8 and Haar 2 only (Wavelet.hpp:165-200)
+    const bool dwt = o->wl_family > -1 && o->wl_family <= 5;
+    if (dwt && !((o->wl_family == 0 && (o->wl_member == 4 || o->wl_member == 8)) ||
+                 (o->wl_family == 2 && o->wl_member == 2))) {
+        set_error("wavelet: families 0 (members 4, 8) and 2 (member 2) have filters");
+        return CGS_ERR_BAD_ARG;
+    }
     if (o->cgiter < 0 || o->ftiter < 0 || o->csiter < 0 || o->nliter < 0 || o->lsiter < 0) {
         set_error("negative iteration count");
         return CGS_ERR_BAD_ARG;
@@ -2006,10 +2122,33 @@ cgs_status cgs_cs_create(cgs_cs **out, cgs_plan *p, const cgs_cs_opts *o)
     tm.xfmw = o->xfmw;
     tm.l1 = o->l1;
     tm.pnorm = o->pnorm;
+    int levels = 0;
+    if (dwt) {
+        // DWT<T>(N) of CS_XSENSE.hpp:133: a square 2-D transform with dyadic
+        // sides down to 2^4 (WL_SCALE, DWT.hpp:38-40)
+        if (p->d != 2 || tm.D0 != tm.D1 || (tm.D0 & (tm.D0 - 1)) != 0) {
+            set_error("the wavelet transform needs a square 2-D image with dyadic sides");
+            return CGS_ERR_BAD_ARG;
+        }
+        int L = 0;
+        while ((1 << L) < tm.D0) ++L;
+        levels = std::max(0, L - 4);
+    }
     cgs_cs *c = new cgs_cs;
     c->p = p;
+    c->device = p->device;
     c->o = *o;
     c->tm = tm;
+    c->dwt = dwt;
+    c->dwt_levels = levels;
+    if (dwt) {
+        const std::vector<double> h = daubechies(o->wl_member);
+        c->filt.fl = (int)h.size();
+        for (int i = 0; i < c->filt.fl; ++i) {
+            c->filt.lo[i] = (float)h[i];
+            c->filt.hi[i] = (float)((i & 1) ? -h[i] : h[i]);  // mirrorfilt, Wavelet.hpp:12-19
+        }
+    }
     c->so.mode = CGS_MODE_CODEARE;
     c->so.cgiter = o->cgiter;
     c->so.cgeps = o->cgeps;
@@ -2030,6 +2169,10 @@ cgs_status cgs_cs_create(cgs_cs **out, cgs_plan *p, const cgs_cs_opts *o)
     if (r == CGS_OK) r = dev_alloc(&c->sums, kSumCount);
     if (r == CGS_OK) r = dev_alloc(&c->amax, 1);
     if (r == CGS_OK) r = dev_alloc(&c->tally, 2);
+    if (r == CGS_OK && dwt) r = dev_alloc(&c->wx, Nt);
+    if (r == CGS_OK && dwt) r = dev_alloc(&c->wdx, Nt);
+    if (r == CGS_OK && dwt) r = dev_alloc(&c->wtmp, Nt);
+    if (r == CGS_OK && dwt) r = dev_alloc(&c->wu, Nt);
     if (r == CGS_OK && cudaMallocHost((void **)&c->hsums, sizeof(double) * kSumCount) != cudaSuccess) {
         set_error("cudaMallocHost failed");
         r = CGS_ERR_OOM;
@@ -2046,10 +2189,10 @@ cgs_status cgs_cs_create(cgs_cs **out, cgs_plan *p, const cgs_cs_opts *o)
 cgs_status cgs_cs_destroy(cgs_cs *c)
 {
     if (!c) return CGS_OK;
-    cudaSetDevice(c->p->device);
-    cudaStreamSynchronize(c->p->stream);
+    cudaSetDevice(c->device);  // cudaFree waits for work still using the buffers
     for (void *q : {(void *)c->x, (void *)c->g0, (void *)c->g1, (void *)c->dx, (void *)c->ksData, (void *)c->ksE,
-                    (void *)c->ksG, (void *)c->partial, (void *)c->sums, (void *)c->amax, (void *)c->tally})
+                    (void *)c->ksG, (void *)c->partial, (void *)c->sums, (void *)c->amax, (void *)c->tally,
+                    (void *)c->wx, (void *)c->wdx, (void *)c->wtmp, (void *)c->wu})
         dev_free(q);
     if (c->hsums) cudaFreeHost(c->hsums);
     delete c;
@@ -2070,8 +2213,8 @@ cgs_status cgs_cs_adjoint(cgs_cs *c, const float *y, float *x, cgs_cs_report *re
     // x0 = ft ->* data, the CG-SENSE solve (CS_XSENSE.hpp:293-297)
     CGS_CUDA(cudaMemcpyAsync(p->ksY, c->ksData, sizeof(float2) * p->M * p->nc, cudaMemcpyDeviceToDevice, st));
     CGS_TRY(cs_solve(c, st));
-    CGS_CUDA(cudaMemcpyAsync(c->x, p->vX, sizeof(float2) * p->Nt, cudaMemcpyDeviceToDevice, st));
-    // TV weights *= max |x0| (CS_XSENSE.hpp:303-305; cumulative over calls, as the reference's)
+    CGS_TRY(cs_dwt(c, p->vX, c->x, 0, st));  // x = W x0 (CS_XSENSE.hpp:301-302)
+    // TV weights *= max |x| (CS_XSENSE.hpp:303-305; cumulative over calls, as the reference's)
     CGS_TRY(launch_cs_absmax(c->x, p->Nt, c->amax, st));
     unsigned int bits = 0;
     CGS_CUDA(cudaMemcpyAsync(&bits, c->amax, sizeof(bits), cudaMemcpyDeviceToHost, st));
@@ -2081,8 +2224,9 @@ cgs_status cgs_cs_adjoint(cgs_cs *c, const float *y, float *x, cgs_cs_report *re
     for (int i = 0; i < 2; ++i) c->tm.tvw[i] *= ma;
     if (c->o.nlopt == 0)
         for (int i = 0; i < c->o.csiter; ++i) CGS_TRY(cs_minimise(c, rep, st));
+    if (c->dwt) CGS_TRY(cs_dwt(c, c->x, c->wu, 1, st));  // CS_XSENSE.hpp:317-318
     CGS_CUDA(cudaEventRecord(p->ev1, st));
-    CGS_TRY(image_out(p, c->x, x, st));
+    CGS_TRY(image_out(p, c->dwt ? c->wu : c->x, x, st));
     int tally[2] = {0, 0};
     CGS_CUDA(cudaMemcpyAsync(tally, c->tally, sizeof(tally), cudaMemcpyDeviceToHost, st));
     CGS_CUDA(cudaStreamSynchronize(st));
@@ -2120,6 +2264,17 @@ cgs_status cgs_cs_df(cgs_cs *c, const float *y, const float *x, float *g, void *
     return CGS_OK;
 }
 
+cgs_status cgs_cs_wavelet(cgs_cs *c, const float *in, float *out, int inverse, void *stream)
+{
+    if (!c || !in || !out) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    cgs_plan *p = c->p;
+    CGS_TRY(check_ready(p, true, true));
+    cudaStream_t st = pick_stream(p, stream);
+    CGS_TRY(cs_image_in(p, in, c->dx, st));
+    CGS_TRY(cs_dwt(c, c->dx, c->g1, inverse ? 1 : 0, st));
+    return image_out(p, c->g1, out, st);
+}
+
 cgs_status cgs_cs_obj(cgs_cs *c, const float *y, const float *x, const float *dx, float t, double *obj,
                       double *rmse, void *stream)
 {
@@ -2130,13 +2285,16 @@ cgs_status cgs_cs_obj(cgs_cs *c, const float *y, const float *x, const float *dx
     CGS_TRY(cs_data_in(c, y, st));
     CGS_TRY(cs_image_in(p, x, c->x, st));
     CGS_TRY(cs_image_in(p, dx, c->dx, st));
-    CGS_TRY(op_forward(p, c->x, 0, nullptr, c->ksE, st));
-    CGS_TRY(op_forward(p, c->dx, 0, nullptr, c->ksG, st));
+    if (c->dwt) CGS_TRY(cs_dwt(c, c->x, c->wx, 1, st));
+    c->wxp = c->dwt ? c->wx : c->x;
+    CGS_TRY(op_forward(p, c->wxp, 0, nullptr, c->ksE, st));
+    const float2 *wdxp = nullptr;
+    CGS_TRY(cs_update(c, c->dx, &wdxp, st));
     CsSteps steps{};
     steps.t[0] = t;
     steps.n = 1;
-    CGS_TRY(launch_cs_obj(c->ksE, c->ksG, c->ksData, p->M * p->nc, c->x, c->dx, c->tm, steps, c->partial, c->sums,
-                          st));
+    CGS_TRY(launch_cs_obj(c->ksE, c->ksG, c->ksData, p->M * p->nc, c->wxp, wdxp, c->x, c->dx, c->tm, steps,
+                          c->partial, c->sums, st));
     CGS_TRY(cs_read(c, st));
     *obj = c->hsums[0] + c->hsums[kCsSteps];
     if (rmse) *rmse = std::sqrt(c->hsums[0] / c->ndnz);

@@ -300,7 +300,11 @@ typedef struct {
     float tvw[2];
     int tvdims[2][3], ntvdims[2];
     float xfmw, l1, pnorm;
-    int wl_family, wl_member;  /* wavelet: only -1 (none) is supported */
+    /* wavelet (DWT.hpp): -1 none; 0 Daubechies with member 4 or 8 taps, 2
+     * Haar with member 2 (the reference's only initialised filters); the
+     * NLCG variable is then the image's wavelet coefficients.  Needs a
+     * square 2-D image with dyadic sides; levels down to 16 x 16. */
+    int wl_family, wl_member;
 } cgs_cs_opts;
 
 typedef struct {
@@ -315,6 +319,7 @@ typedef struct {
 } cgs_cs_report;
 
 cgs_status cgs_cs_create(cgs_cs **cs, cgs_plan *plan, const cgs_cs_opts *opts);
+/* May be called before or after the plan is destroyed. */
 cgs_status cgs_cs_destroy(cgs_cs *cs);
 
 /* x = CS reconstruction of data y ((M, NC) complex): CS_XSENSE::Adjoint /
@@ -322,8 +327,13 @@ cgs_status cgs_cs_destroy(cgs_cs *cs);
 cgs_status cgs_cs_adjoint(cgs_cs *cs, const float *y, float *x, cgs_cs_report *report, void *stream);
 
 /* g = gradient of the objective at x for data y (CS_XSENSE::df,
- * CS_XSENSE.hpp:223-232), with the current TV weights. */
+ * CS_XSENSE.hpp:223-232), with the current TV weights.  x, g (and dx below)
+ * are wavelet coefficients when the handle has a wavelet. */
 cgs_status cgs_cs_df(cgs_cs *cs, const float *y, const float *x, float *g, void *stream);
+
+/* The handle's wavelet transform: out = W in (DWT::operator*, inverse 0)
+ * or W^-1 in (DWT::operator->*, inverse 1); a copy without a wavelet. */
+cgs_status cgs_cs_wavelet(cgs_cs *cs, const float *in, float *out, int inverse, void *stream);
 
 /* Objective at x + t dx for data y (CS_XSENSE::obj after df(x) and
  * Update(dx), CS_XSENSE.hpp:197-221); *rmse = sqrt(data term / nnz(y)). */

@@ -12,6 +12,9 @@ the NCSENSE restatement in oracle.py.
   CS objective        src/matrix/ft/CS_XSENSE.hpp:197-255 (obj, df, Update),
                       279-322 (Adjoint), 329-414 (Obj, TV, XFM, dObj, dXFM, dTV)
   NLCG                src/optimisation/NLCG.hpp:42-125
+  wavelets            src/matrix/dwt/DWT.hpp:354-418 (forward), 756-823
+                      (inverse), 644-740 and 1046-1180 (filters along a line),
+                      Wavelet.hpp:12-19, 75-190 (filter sets)
   module keys         src/modules/CompressedSensing.cpp:86-136
 
 Images are numpy arrays in C order, so the codeare (D0, D1[, D2]) image is
@@ -81,18 +84,106 @@ def tv_adj(A, mode):
     raise ValueError(mode)
 
 
+# ---------------------------------------------------------------------------
+# periodic orthonormal wavelet transform (src/matrix/dwt/DWT.hpp,
+# Wavelet.hpp): the reference initialises filters for Daubechies 4 and 8
+# taps (family 0) and Haar (family 2, 2 taps) only
+# ---------------------------------------------------------------------------
+def daubechies(taps: int):
+    """Minimum-phase Daubechies low-pass filter with taps/2 vanishing moments,
+    by spectral factorisation of P(y) = sum_k C(p-1+k, k) y^k (Daubechies
+    1988), ordered with the large coefficients first and sum sqrt(2)."""
+    from math import comb
+    p = taps // 2
+    poly = np.array([1.0 + 0j])
+    for _ in range(p):
+        poly = np.convolve(poly, [1.0, 1.0])          # (1 + w)^p, ascending powers
+    if p > 1:
+        for y in np.roots([comb(p - 1 + k, k) for k in range(p)][::-1]):
+            r = np.roots([1.0, -(2.0 - 4.0 * y), 1.0])  # w + 1/w = 2 - 4y
+            poly = np.convolve(poly, [-r[np.argmax(np.abs(r))], 1.0])
+    h = poly.real
+    return h * (np.sqrt(2.0) / h.sum())
+
+
+def wavelet_filters(family: int, member: int):
+    """(low, high) decomposition filters; high[i] = (-1)^i low[i] (Wavelet.hpp:12-19)."""
+    if (family, member) not in ((0, 4), (0, 8), (2, 2)):
+        raise ValueError("no wavelet filters for family %d member %d" % (family, member))
+    lo = daubechies(member)
+    return lo, lo * (-1.0) ** np.arange(lo.size)
+
+
+def _down(b, lo, hi, axis):
+    """DWT::downlo / downhi along one axis of the block (DWT.hpp:644-740)."""
+    b = np.moveaxis(b, axis, 0)
+    n = b.shape[0]
+    i = np.arange(n // 2)
+    low = sum(lo[h] * b[(2 * i + h) % n] for h in range(lo.size))
+    high = sum(hi[h] * b[(2 * i + 1 - h) % n] for h in range(hi.size))
+    return np.moveaxis(np.concatenate([low, high]), 0, axis)
+
+
+def _up(b, lo, hi, axis):
+    """DWT::uplo + uphi along one axis (DWT.hpp:1046-1180), even filter lengths."""
+    b = np.moveaxis(b, axis, 0)
+    n = b.shape[0] // 2
+    low, high = b[:n], b[n:]
+    i = np.arange(n)
+    out = np.zeros_like(b)
+    for e in (0, 1):
+        s = sum(lo[2 * h + e] * low[(i - h) % n] for h in range(lo.size // 2))
+        s = s + sum(hi[2 * h + (1 - e)] * high[(i + h) % n] for h in range(hi.size // 2))
+        out[e::2] = s
+    return np.moveaxis(out, 0, axis)
+
+
+def dwt_levels(side: int, min_level: int = 4):
+    L = int(round(np.log2(side)))
+    if 2 ** L != side:
+        raise ValueError("the wavelet transform needs dyadic sides")
+    return L, min_level
+
+
+def dwt_fwd(c, lo, hi, min_level=4):
+    """DWT::dpwt2 on the codeare-ordered square image c (DWT.hpp:354-418)."""
+    L, _ = dwt_levels(c.shape[0], min_level)
+    r = np.array(c, dtype=np.complex128)
+    n = c.shape[0]
+    for _ in range(L - 1, min_level - 1, -1):
+        r[:n, :n] = _down(r[:n, :n], lo, hi, 0)
+        r[:n, :n] = _down(r[:n, :n], lo, hi, 1)
+        n //= 2
+    return r
+
+
+def dwt_inv(c, lo, hi, min_level=4):
+    """DWT::idpwt2 (DWT.hpp:756-823): coarse to fine, axis 1 then axis 0."""
+    L, _ = dwt_levels(c.shape[0], min_level)
+    r = np.array(c, dtype=np.complex128)
+    n = 2 ** min_level
+    for _ in range(min_level, L):
+        r[:2 * n, :2 * n] = _up(r[:2 * n, :2 * n], lo, hi, 1)
+        r[:2 * n, :2 * n] = _up(r[:2 * n, :2 * n], lo, hi, 0)
+        n *= 2
+    return r
+
+
 def _pw(v, l1, e):
     """(|v|^2 + l1)^e, the reference's om *= conj(om); om += l1; om ^= e."""
     return (np.abs(v) ** 2 + l1) ** e
 
 
 class CSXSense:
-    """CS_XSENSE<cxfl> with ft = 3 (NCSENSE) and no wavelet."""
+    """CS_XSENSE<cxfl> with ft = 3 (NCSENSE); with wl_family >= 0 the NLCG
+    variable is the image's wavelet coefficients (CS_XSENSE.hpp:131-134)."""
 
     def __init__(self, sense, tvw=(0.0, 0.0), tvdims=(None, None), xfmw=0.0, l1=0.0, pnorm=0.0,
                  nlopt=0, csiter=1, nliter=4, lsiter=8, lsa=0.01, lsb=0.6, cgconv=1e-4,
-                 parallel_linesearch=False, cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3):
+                 parallel_linesearch=False, cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3,
+                 wl_family=-1, wl_member=0):
         self.s = sense
+        self.filt = wavelet_filters(wl_family, wl_member) if wl_family > -1 else None
         self.nd = len(sense.shape)
         self.tvw = [float(tvw[0]), float(tvw[1])]
         self.modes = [tv_mode(self.nd, tvdims[0]) if tvw[0] else None,
@@ -113,29 +204,37 @@ class CSXSense:
     def _c(self, x):  # codeare-ordered view
         return np.asarray(x).T
 
+    # the wavelet operator: * (forward) and ->* (inverse); identity without one
+    def W(self, x):
+        return x if self.filt is None else dwt_fwd(self._c(x), *self.filt).T
+
+    def Winv(self, x):
+        return x if self.filt is None else dwt_inv(self._c(x), *self.filt).T
+
     def set_data(self, y):
         self.data = np.asarray(y, np.complex128).reshape(self.s.nc, -1)
         self.ndnz = float(np.count_nonzero(self.data))
 
     # CS_XSENSE.hpp:223-232
     def df(self, x):
-        self.wx = x
-        g = 2.0 * self.Einv(self.E(x) - self.data)  # dObj, :367-372
+        self.wx = self.Winv(x)
+        g = 2.0 * self.W(self.Einv(self.E(self.wx) - self.data))  # dObj, :367-372
         if self.xfmw:  # dXFM, :383-385
             g = g + self.xfmw * (x * _pw(x, self.l1, 0.5 * self.p - 1.0))
         for i in range(2):
             if self.tvw[i]:  # dTV, :395-405
                 d = tv_fwd(self._c(self.wx), self.modes[i])
                 G = self.p * (d * _pw(d, self.l1, 0.5 * self.p - 1.0))
-                g = g + self.tvw[i] * tv_adj(G, self.modes[i]).T
+                g = g + self.tvw[i] * self.W(tv_adj(G, self.modes[i]).T)
         return g
 
     # CS_XSENSE.hpp:234-255
     def update(self, dx):
+        wdx = self.Winv(dx)
         self.ffdbx = self.E(self.wx)
-        self.ffdbg = self.E(dx)
+        self.ffdbg = self.E(wdx)
         self.ttdbx = [tv_fwd(self._c(self.wx), m) if m else None for m in self.modes]
-        self.ttdbg = [tv_fwd(self._c(dx), m) if m else None for m in self.modes]
+        self.ttdbg = [tv_fwd(self._c(wdx), m) if m else None for m in self.modes]
 
     # CS_XSENSE.hpp:197-221, 329-365
     def obj(self, x, dx, t):
@@ -190,10 +289,10 @@ class CSXSense:
     # CS_XSENSE.hpp:283-322
     def adjoint(self, y):
         self.set_data(y)
-        x = self.Einv(self.data)
+        x = self.W(self.Einv(self.data))
         ma = float(np.abs(x).max())
         self.tvw = [w * ma for w in self.tvw]
         for _ in range(self.csiter):
             if self.nlopt == 0:
                 x = self.minimise(x)
-        return x
+        return self.Winv(x)

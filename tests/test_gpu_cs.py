@@ -135,8 +135,85 @@ def test_split_bregman_is_the_cgls_image(gpu):
 def test_cs_rejects_unsupported_settings(gpu):
     s, p, y, _ = setup_2d(gpu)
     with pytest.raises(gpu.capi.CgsError):
-        gpu.CS(p, nlopt=1)           # L-BFGS
-    with pytest.raises(gpu.capi.CgsError):
-        gpu.CS(p, wl_family=0)       # wavelet transform
+        gpu.CS(p, nlopt=1)                        # L-BFGS
+    for fam, mem in ((0, 6), (1, 4), (2, 4), (4, 2)):
+        with pytest.raises(gpu.capi.CgsError):    # wavelets without filters in the reference
+            gpu.CS(p, wl_family=fam, wl_member=mem)
     with pytest.raises(gpu.capi.CgsError):
         gpu.CS(p, tvw=(1e-3, 0.0), tvdims=([0, 0, 1], None))  # third-axis TV on a 2-D image
+    s3, p3, y3 = setup_3d(gpu)
+    with pytest.raises(gpu.capi.CgsError):
+        gpu.CS(p3, wl_family=0, wl_member=4)      # the reference's DWT is 2-D
+
+
+WAVELETS = [(0, 4), (0, 8), (2, 2)]
+
+
+@pytest.mark.parametrize("fam,mem", WAVELETS)
+@pytest.mark.parametrize("N", [32, 64])
+def test_wavelet_transform_matches_oracle(gpu, fam, mem, N):
+    """DWT::operator* and ->* (DWT.hpp:354-418, 756-823): forward and inverse
+    against the FP64 restatement; the inverse undoes the forward."""
+    from oracle import cs
+    s, p, y, _ = setup_2d(gpu, N=N, nc=2)
+    g = gpu.CS(p, wl_family=fam, wl_member=mem, **SOLVE)
+    x = rand_img((N, N), 11)
+    w = np.zeros_like(x)
+    g.wavelet(x, w)
+    lo, hi = cs.wavelet_filters(fam, mem)
+    wo = cs.dwt_fwd(x.T, lo, hi).T
+    assert rel(w, wo) < 2e-6
+    xi = np.zeros_like(x)
+    g.wavelet(w, xi, inverse=True)
+    assert rel(xi, cs.dwt_inv(w.T, lo, hi).T) < 2e-6
+    assert rel(xi, x) < 4e-6
+
+
+# With a wavelet each side forms the image W^-1 x itself, the GPU in FP32.
+# For p = 1 the TV factor d / sqrt(|d|^2 + l1) has slope 1/sqrt(l1) at d = 0,
+# so at l1 = 1e-15 the FP32 rounding noise of the image (~1e-8 in flat
+# regions) alone moves the FP64 gradient by several percent -- the
+# reference's FP32 code is as sensitive.  These cases use l1 = 1e-6, where
+# the same noise moves it by ~4e-6.
+L1_WAVELET = 1e-6
+
+
+@pytest.mark.parametrize("fam,mem", WAVELETS)
+def test_cs_obj_and_df_wavelet(gpu, fam, mem):
+    """With a wavelet the NLCG variable is the coefficient array: the data and
+    TV terms act on its inverse transform, the L1 term on the coefficients."""
+    from oracle import cs
+    s, p, y, _ = setup_2d(gpu, N=64, nc=2)
+    terms = dict(tvw=(2e-3, 0.0), xfmw=5e-3, l1=L1_WAVELET, pnorm=1.0, wl_family=fam, wl_member=mem)
+    o = cs.CSXSense(s, **terms, **SOLVE)
+    g = gpu.CS(p, **terms, **SOLVE)
+    x0 = np.zeros((64, 64), np.complex64)
+    p.solve(y, x0, cgiter=SOLVE["cgiter"], cgeps=SOLVE["cgeps"], lam=SOLVE["lam"])
+    w0 = c64(o.W(x0))
+    dx = rand_img((64, 64), 3, scale=0.1 * float(np.abs(w0).max()))
+    o.set_data(y)
+    go = o.df(w0)
+    gg = np.zeros_like(w0)
+    g.df(y, w0, gg)
+    assert rel(gg, go) < TOL_GRAD
+    o.update(dx)
+    for t in (0.0, 0.36):
+        fo, ro = o.obj(w0, dx, t)
+        fg, rg = g.obj(y, w0, dx, t)
+        assert abs(fg - fo) <= TOL_OBJ * abs(fo), (t, fg, fo)
+
+
+def test_cs_reconstruction_wavelet_matches_oracle(gpu):
+    """The reference's example settings (Daubechies 4, TV and L1 weights,
+    p = 1; l1 as above): same line-search path and image as the FP64
+    restatement."""
+    from oracle import cs
+    s, p, y, _ = setup_2d(gpu, N=64, nc=4)
+    kw = dict(tvw=(2e-3, 0.0), xfmw=5e-3, l1=L1_WAVELET, pnorm=1.0, csiter=2, nliter=4, lsiter=10, lsa=1e-3,
+              lsb=0.6, cgconv=1e-5, wl_family=0, wl_member=4, **SOLVE)
+    o = cs.CSXSense(s, **kw)
+    xo = o.adjoint(y)
+    x = np.zeros((64, 64), np.complex64)
+    rep = gpu.CS(p, **kw).adjoint(y, x)
+    assert rep["ls_index"] == [li for li, _ in o.log]
+    assert rel(x, xo) < TOL_IMG

@@ -184,3 +184,43 @@ def test_cnn_oracle_gradients_match_finite_differences():
         wm[i] -= eps
         fd = (cnn.gradients(wp, x, t)[0] - cnn.gradients(wm, x, t)[0]) / (2 * eps)
         assert abs(fd - g[i]) < 1e-6 * max(1.0, abs(g[i])) + 1e-9
+
+
+def test_wavelet_filters_and_transform():
+    """The oracle's Daubechies filters are orthonormal with taps/2 vanishing
+    moments, and its periodic transform is orthogonal (inverse = adjoint)."""
+    from oracle import cs
+    for taps in (2, 4, 8):
+        h = cs.daubechies(taps)
+        assert abs(h.sum() - np.sqrt(2.0)) < 1e-12
+        for m in range(taps // 2):
+            assert abs(np.dot(h[:taps - 2 * m], h[2 * m:]) - (m == 0)) < 1e-12
+        g = h * (-1.0) ** np.arange(taps)
+        for q in range(taps // 2):
+            assert abs(np.dot(g, np.arange(taps, dtype=float) ** q)) < 1e-9
+    assert h[0] > h[-1] > -0.02  # large coefficients first (Wavelet.hpp:142-153 ordering)
+    lo, hi = cs.wavelet_filters(0, 8)
+    rng = np.random.default_rng(0)
+    c = rng.standard_normal((64, 64)) + 1j * rng.standard_normal((64, 64))
+    d = rng.standard_normal((64, 64)) + 1j * rng.standard_normal((64, 64))
+    assert np.abs(cs.dwt_inv(cs.dwt_fwd(c, lo, hi), lo, hi) - c).max() < 1e-12
+    assert abs(np.vdot(d, cs.dwt_fwd(c, lo, hi)) - np.vdot(cs.dwt_inv(d, lo, hi), c)) < 1e-9
+
+
+def test_tv_operators():
+    """The third-axis TV adjoint is exact; the 2-D adjoint leaves the border
+    rows of each component out (TVOP.hpp:52-63)."""
+    from oracle import cs
+    rng = np.random.default_rng(1)
+    c = rng.standard_normal((6, 6, 5)) + 1j * rng.standard_normal((6, 6, 5))
+    A = rng.standard_normal((6, 6, 5)) + 1j * rng.standard_normal((6, 6, 5))
+    assert abs(np.vdot(A, cs.tv_fwd(c, "z")) - np.vdot(cs.tv_adj(A, "z"), c)) < 1e-10
+    c2 = c[:, :, 0]
+    A2 = np.zeros((6, 6, 2), complex)
+    A2[2, 3, 0] = 1.0
+    r = cs.tv_adj(A2, "2d")
+    assert r[2, 3] == -1.0 and r[3, 3] == 1.0 and np.count_nonzero(r) == 2
+    A2[:] = 0
+    A2[0, 3, 0] = 1.0  # border row: the reference's adjoint drops the -1 at index 0
+    assert np.count_nonzero(cs.tv_adj(A2, "2d")) == 1
+    assert cs.tv_fwd(c2, "2d").shape == (6, 6, 2)
