@@ -37,7 +37,7 @@ PROFILE_CATEGORIES = ("fft", "interp", "spread")
 
 class PlanDesc(C.Structure):
     _fields_ = [("rank", C.c_int), ("N", C.c_int * 3), ("alpha", C.c_double), ("m", C.c_int),
-                ("M", C.c_int64), ("ncoils", C.c_int)]
+                ("M", C.c_int64), ("ncoils", C.c_int), ("frames", C.c_int)]
 
 
 class SolveOpts(C.Structure):
@@ -215,7 +215,9 @@ def _report(rep):
 
 
 class Plan:
-    """One NFFT / NCSENSE operator on the current CUDA device."""
+    """One NFFT / NCSENSE operator on the current CUDA device.  With frames > 1
+    it is NCSENSE's dim4 batch: `shape` and `M` are per frame, k-space is
+    (F, M, d), signals (F, NC, M) and images (F, *shape) (C order)."""
 
     def _go(self, fn, *args, stream=None):
         st, wait = _resolve_stream(stream)
@@ -223,14 +225,15 @@ class Plan:
         if wait:
             _check(load().cgs_sync(self._h))
 
-    def __init__(self, shape, M, ncoils=1, m=1, alpha=1.0):
+    def __init__(self, shape, M, ncoils=1, m=1, alpha=1.0, frames=1):
         L = load()
         self.shape = tuple(int(s) for s in shape)
         self.d = len(self.shape)
         self.M = int(M)
         self.nc = int(ncoils)
+        self.frames = int(frames)
         desc = PlanDesc(self.d, (C.c_int * 3)(*self.shape, *([1] * (3 - self.d))), float(alpha), int(m),
-                        self.M, self.nc)
+                        self.M, self.nc, self.frames)
         h = C.c_void_p()
         _check(L.cgs_plan_create(C.byref(h), C.byref(desc)))
         self._h = h

@@ -150,6 +150,14 @@ using namespace cgs;
 
 struct cgs_plan {
     int d = 0, N[3] = {1, 1, 1}, n[3] = {1, 1, 1}, m = 1, nc = 1;
+    // frames (NCSENSE dim4 x dim5, NCSENSE.hpp:141-166): F child plans with one
+    // trajectory each and the same sensitivities and weights.  The parent's
+    // vectors stack the frames (image Nt = F * Ntf, k-space M = F * Mf nodes,
+    // frame-major); the operator building blocks run per child on the parent's
+    // stream, so the CG machinery above them is unchanged.
+    int F = 1;
+    int64_t Mf = 0, Ntf = 0;
+    std::vector<cgs_plan *> fr;
     double alpha = 1.0;
     int64_t M = 0, Nt = 1, ntot = 1;
     int device = 0;
@@ -292,6 +300,12 @@ AxisPass base_pass(cgs_plan *p, int t)
 cgs_status op_forward(cgs_plan *p, const float2 *src_img, int per_coil, const float *mask, float2 *ks,
                       cudaStream_t st)
 {
+    if (p->F > 1) {
+        for (int f = 0; f < p->F; ++f)
+            CGS_TRY(op_forward(p->fr[f], src_img + (per_coil ? f * p->Ntf * p->nc : f * p->Ntf), per_coil, mask,
+                               ks + f * p->Mf * p->nc, st));
+        return CGS_OK;
+    }
     const int d = p->d, nc = p->nc;
     // pass over the fastest image axis (t = d-1), from the image side
     {
@@ -331,6 +345,11 @@ cgs_status op_forward(cgs_plan *p, const float2 *src_img, int per_coil, const fl
 // adjoint NFFT of all coils into coil-minor per-coil images (deapodised)
 cgs_status op_adjoint(cgs_plan *p, const float2 *ks, int weighted, float2 *out, cudaStream_t st)
 {
+    if (p->F > 1) {
+        for (int f = 0; f < p->F; ++f)
+            CGS_TRY(op_adjoint(p->fr[f], ks + f * p->Mf * p->nc, weighted, out + f * p->Ntf * p->nc, st));
+        return CGS_OK;
+    }
     const int d = p->d, nc = p->nc;
     NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW};
     if (d == 2) {
@@ -408,6 +427,11 @@ cgs_status op_itrafo(cgs_plan *p, const float2 *ksIn, int maxit, double eps, cud
 cgs_status op_eh_codeare(cgs_plan *p, const float2 *ks, int ftiter, double fteps, float2 *x,
                          cudaStream_t st)
 {
+    if (p->F > 1) {  // per frame (NCSENSE.hpp:254-266)
+        for (int f = 0; f < p->F; ++f)
+            CGS_TRY(op_eh_codeare(p->fr[f], ks + f * p->Mf * p->nc, ftiter, fteps, x + f * p->Ntf, st));
+        return CGS_OK;
+    }
     CGS_TRY(op_itrafo(p, ks, ftiter, fteps, st));
     return launch_coil_combine(p->cF, p->sens, p->imap, p->Nt, p->nc, x, st);
 }
@@ -415,6 +439,11 @@ cgs_status op_eh_codeare(cgs_plan *p, const float2 *ks, int ftiter, double fteps
 // true E^H W: x = sum conj(S) . A^H (w ks)
 cgs_status op_eh(cgs_plan *p, const float2 *ks, int weighted, float2 *x, cudaStream_t st)
 {
+    if (p->F > 1) {
+        for (int f = 0; f < p->F; ++f)
+            CGS_TRY(op_eh(p->fr[f], ks + f * p->Mf * p->nc, weighted, x + f * p->Ntf, st));
+        return CGS_OK;
+    }
     CGS_TRY(op_adjoint(p, ks, weighted, p->cF, st));
     return launch_coil_combine(p->cF, p->sens, nullptr, p->Nt, p->nc, x, st);
 }
@@ -1003,6 +1032,51 @@ cgs_status cgs_plan_create(cgs_plan **out, const cgs_plan_desc *desc)
 {
     if (!out || !desc) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
     *out = nullptr;
+    if (desc->frames < 0 || desc->frames > 4096) { set_error("frames must be 0..4096"); return CGS_ERR_BAD_ARG; }
+    if (desc->frames > 1) {
+        // one child plan per frame; the parent holds the stacked vectors only
+        cgs_plan_desc one = *desc;
+        one.frames = 1;
+        cgs_plan *p = new cgs_plan();
+        p->F = desc->frames;
+        cgs_status st = CGS_OK;
+        for (int f = 0; f < p->F && st == CGS_OK; ++f) {
+            cgs_plan *c = nullptr;
+            st = cgs_plan_create(&c, &one);
+            if (st == CGS_OK) p->fr.push_back(c);
+        }
+        if (st != CGS_OK) { cgs_plan_destroy(p); return st; }
+        const cgs_plan *c0 = p->fr[0];
+        p->d = c0->d; p->m = c0->m; p->nc = c0->nc; p->alpha = c0->alpha; p->device = c0->device;
+        for (int t = 0; t < 3; ++t) { p->N[t] = c0->N[t]; p->n[t] = c0->n[t]; }
+        p->geom = c0->geom;
+        p->tune = c0->tune;
+        p->Mf = c0->M; p->Ntf = c0->Nt;
+        p->M = p->F * p->Mf; p->Nt = p->F * p->Ntf; p->ntot = c0->ntot;
+        const int64_t nc = p->nc, M = p->M, Nt = p->Nt;
+#define ALLOCF(ptr, cnt) do { st = dev_alloc(&(ptr), (cnt)); if (st != CGS_OK) { cgs_plan_destroy(p); return st; } } while (0)
+        if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            cgs_plan_destroy(p); set_error("stream creation failed"); return CGS_ERR_CUDA;
+        }
+        cudaEventCreate(&p->ev0);
+        cudaEventCreate(&p->ev1);
+        ALLOCF(p->ksY, M * nc); ALLOCF(p->ksV, M * nc);
+        ALLOCF(p->vX, Nt); ALLOCF(p->vR, Nt); ALLOCF(p->vP, Nt); ALLOCF(p->vQ, Nt);
+        ALLOCF(p->ioA, std::max(Nt, M * nc)); ALLOCF(p->ioB, std::max(Nt, M * nc));
+        ALLOCF(p->partial, (size_t)dot_blocks() * std::max<int64_t>(nc, 1));
+        ALLOCF(p->dots, 8 * nc + 8);
+        ALLOCF(p->sc, 1);
+        ALLOCF(p->fpart, (size_t)dot_blocks());
+        ALLOCF(p->ftick, 1);
+#undef ALLOCF
+        if (cudaMemset(p->ftick, 0, sizeof(unsigned int)) != cudaSuccess) {
+            cgs_plan_destroy(p);
+            set_error("cudaMemset failed");
+            return CGS_ERR_CUDA;
+        }
+        *out = p;
+        return CGS_OK;
+    }
     if (desc->rank != 2 && desc->rank != 3) { set_error("rank must be 2 or 3"); return CGS_ERR_BAD_ARG; }
     if (desc->ncoils < 1 || desc->M < 1 || desc->m < 0 || desc->m > 8 || !(desc->alpha >= 1.0)) {
         set_error("bad ncoils / M / m / alpha");
@@ -1119,6 +1193,7 @@ cgs_status cgs_plan_destroy(cgs_plan *p)
     if (!p) return CGS_OK;
     cudaSetDevice(p->device);
     if (p->stream) cudaStreamSynchronize(p->stream);
+    for (cgs_plan *c : p->fr) cgs_plan_destroy(c);
     void *bufs[] = {p->tw[0], p->tw[1], p->tw[2], p->deap[0], p->deap[1], p->deap[2], p->nodes, p->perm,
                     p->w, p->work, p->nodeU, p->nodeW, p->pentries, p->pwork, p->pmulti, p->ppartial, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
                     p->cF, p->cP, p->cZ, p->vX, p->vR, p->vP, p->vQ, p->ioA, p->ioB, p->partial, p->dots,
@@ -1154,6 +1229,13 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
 {
     if (!p || !k_in) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
     CGS_CUDA(cudaSetDevice(p->device));
+    if (p->F > 1) {  // frame f takes k[:, :, f] (NCSENSE.hpp:213-223)
+        drop_graphs(p);
+        p->have_k = p->have_w = false;
+        for (int f = 0; f < p->F; ++f) CGS_TRY(cgs_set_kspace(p->fr[f], k_in + (int64_t)f * p->d * p->Mf));
+        p->have_k = true;
+        return CGS_OK;
+    }
     const int d = p->d;
     const int64_t M = p->M;
     std::vector<float> k((size_t)M * d);
@@ -1243,6 +1325,12 @@ cgs_status cgs_set_weights(cgs_plan *p, const float *w_in)
     if (!p || !w_in) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
     if (!p->have_k) { set_error("set k-space before weights (NFFT.hpp:281-296 needs the nodes)"); return CGS_ERR_STATE; }
     CGS_CUDA(cudaSetDevice(p->device));
+    if (p->F > 1) {  // the same weights for every frame (NCSENSE.hpp:244-248)
+        drop_graphs(p);
+        for (int f = 0; f < p->F; ++f) CGS_TRY(cgs_set_weights(p->fr[f], w_in));
+        p->have_w = true;
+        return CGS_OK;
+    }
     const int64_t M = p->M;
     std::vector<float> w(M), ws(M);
     std::vector<int> perm(M);
@@ -1262,6 +1350,11 @@ cgs_status cgs_set_sensitivities(cgs_plan *p, const float *s_in)
 {
     if (!p || !s_in) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
     CGS_CUDA(cudaSetDevice(p->device));
+    if (p->F > 1) {
+        for (int f = 0; f < p->F; ++f) CGS_TRY(cgs_set_sensitivities(p->fr[f], s_in));
+        p->have_s = true;
+        return CGS_OK;
+    }
     cudaStream_t st = p->stream;
     const void *src;
     CGS_TRY(stage_in(s_in, sizeof(float2) * p->Nt * p->nc, p->ioA, &src, st));
@@ -1285,6 +1378,11 @@ cgs_status cgs_nfft_trafo(cgs_plan *p, const float *fhat, float *f, void *stream
     CGS_TRY(check_ready(p, false, false));
     if (!fhat || !f) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
     cudaStream_t st = pick_stream(p, stream);
+    if (p->F > 1) {
+        for (int q = 0; q < p->F; ++q)
+            CGS_TRY(cgs_nfft_trafo(p->fr[q], fhat + 2 * q * p->Ntf * p->nc, f + 2 * q * p->Mf * p->nc, st));
+        return CGS_OK;
+    }
     const void *src;
     CGS_TRY(stage_in(fhat, sizeof(float2) * p->Nt * p->nc, p->ioA, &src, st));
     CGS_TRY(launch_to_coil_minor((const float2 *)src, p->Nt, p->nc, p->cF, st));
@@ -1299,12 +1397,20 @@ cgs_status cgs_nfft_trafo(cgs_plan *p, const float *fhat, float *f, void *stream
     return CGS_OK;
 }
 
-static cgs_status ks_in(cgs_plan *p, const float *y, cudaStream_t st)
+// caller k-space (coil-major, trajectory order; frames stacked) -> sorted layout
+static cgs_status gather_ks(cgs_plan *p, const float *y, float2 *dst, cudaStream_t st)
 {
     const void *src;
     CGS_TRY(stage_in(y, sizeof(float2) * p->M * p->nc, p->ioA, &src, st));
-    return launch_gather_ks((const float2 *)src, p->perm, p->M, p->nc, p->ksY, st);
+    if (p->F == 1) return launch_gather_ks((const float2 *)src, p->perm, p->M, p->nc, dst, st);
+    for (int f = 0; f < p->F; ++f) {
+        const int64_t off = f * p->Mf * p->nc;
+        CGS_TRY(launch_gather_ks((const float2 *)src + off, p->fr[f]->perm, p->Mf, p->nc, dst + off, st));
+    }
+    return CGS_OK;
 }
+
+static cgs_status ks_in(cgs_plan *p, const float *y, cudaStream_t st) { return gather_ks(p, y, p->ksY, st); }
 
 static cgs_status coil_images_out(cgs_plan *p, const float2 *cm, float *out, cudaStream_t st)
 {
@@ -1335,6 +1441,11 @@ cgs_status cgs_nfft_adjoint(cgs_plan *p, const float *f, float *fhat, void *stre
     CGS_TRY(check_ready(p, false, false));
     if (!fhat || !f) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
     cudaStream_t st = pick_stream(p, stream);
+    if (p->F > 1) {
+        for (int q = 0; q < p->F; ++q)
+            CGS_TRY(cgs_nfft_adjoint(p->fr[q], f + 2 * q * p->Mf * p->nc, fhat + 2 * q * p->Ntf * p->nc, st));
+        return CGS_OK;
+    }
     CGS_TRY(ks_in(p, f, st));
     CGS_TRY(op_adjoint(p, p->ksY, 0, p->cF, st));
     return coil_images_out(p, p->cF, fhat, st);
@@ -1345,6 +1456,12 @@ cgs_status cgs_nfft_itrafo(cgs_plan *p, const float *f, float *fhat, int maxit, 
     CGS_TRY(check_ready(p, true, false));
     if (!fhat || !f || maxit < 0) { set_error("bad argument"); return CGS_ERR_BAD_ARG; }
     cudaStream_t st = pick_stream(p, stream);
+    if (p->F > 1) {
+        for (int q = 0; q < p->F; ++q)
+            CGS_TRY(cgs_nfft_itrafo(p->fr[q], f + 2 * q * p->Mf * p->nc, fhat + 2 * q * p->Ntf * p->nc, maxit, eps,
+                                    st));
+        return CGS_OK;
+    }
     CGS_TRY(ks_in(p, f, st));
     CGS_TRY(op_itrafo(p, p->ksY, maxit, eps, st));
     return coil_images_out(p, p->cF, fhat, st);
@@ -1360,7 +1477,14 @@ cgs_status cgs_sense_trafo(cgs_plan *p, const float *x, float *y, void *stream)
     CGS_TRY(op_forward(p, (const float2 *)src, 0, nullptr, p->ksV, st));
     const bool dev = is_device_ptr(y);
     float2 *dst = dev ? (float2 *)y : p->ioB;
-    CGS_TRY(launch_scatter_ks(p->ksV, p->perm, p->M, p->nc, dst, st));
+    if (p->F == 1) {
+        CGS_TRY(launch_scatter_ks(p->ksV, p->perm, p->M, p->nc, dst, st));
+    } else {
+        for (int f = 0; f < p->F; ++f) {
+            const int64_t off = f * p->Mf * p->nc;
+            CGS_TRY(launch_scatter_ks(p->ksV + off, p->fr[f]->perm, p->Mf, p->nc, dst + off, st));
+        }
+    }
     if (!dev) {
         CGS_CUDA(cudaMemcpyAsync(y, dst, sizeof(float2) * p->M * p->nc, cudaMemcpyDeviceToHost, st));
         CGS_CUDA(cudaStreamSynchronize(st));
@@ -1396,6 +1520,7 @@ cgs_status cgs_solve(cgs_plan *p, const float *y, float *x, const cgs_solve_opts
     const bool codeare = (o->mode == CGS_MODE_CODEARE);
     CGS_TRY(check_ready(p, codeare || o->weighted, true));
     if (!x || !y || o->cgiter < 0 || o->ftiter < 0) { set_error("bad argument"); return CGS_ERR_BAD_ARG; }
+    if (p->F > 1 && !codeare && o->toeplitz) { set_error("the Toeplitz operator is not built for frames"); return CGS_ERR_BAD_ARG; }
     cudaStream_t st = pick_stream(p, stream);
     const int64_t Nt = p->Nt;
     if (rep) { std::memset(rep, 0, sizeof(*rep)); rep->fallback_at = -1; }
@@ -1457,6 +1582,7 @@ cgs_status cgs_normal_apply(cgs_plan *p, const float *x, float *out, const cgs_s
     if (!o) { set_error("null options"); return CGS_ERR_BAD_ARG; }
     CGS_TRY(check_ready(p, o->weighted != 0, true));
     if (!x || !out) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    if (p->F > 1 && o->toeplitz) { set_error("the Toeplitz operator is not built for frames"); return CGS_ERR_BAD_ARG; }
     cudaStream_t st = pick_stream(p, stream);
     if (o->toeplitz) {
         const int wtd = (o->weighted && p->have_w) ? 1 : 0;
@@ -1480,6 +1606,7 @@ cgs_status cgs_solve_fcg(cgs_plan *p, const float *y, const float *rhs, float *x
     CGS_TRY(check_ready(p, o->weighted != 0, true));
     if (!x || (!y && !rhs) || o->cgiter < 0) { set_error("bad argument"); return CGS_ERR_BAD_ARG; }
     if (p->d != 2) { set_error("the learned preconditioner is 2-D"); return CGS_ERR_BAD_ARG; }
+    if (p->F > 1) { set_error("flexible CG is not built for frames"); return CGS_ERR_BAD_ARG; }
     cudaStream_t st = pick_stream(p, stream);
     if (rep) std::memset(rep, 0, sizeof(*rep));
     CGS_TRY(fcg_alloc(p));
@@ -1540,7 +1667,7 @@ cgs_status cgs_solve_fcg(cgs_plan *p, const float *y, const float *rhs, float *x
 cgs_status cgs_get_tuning(const cgs_plan *p, cgs_tuning *out)
 {
     if (!p || !out) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
-    *out = p->tune;
+    *out = p->F > 1 ? p->fr[0]->tune : p->tune;
     return CGS_OK;
 }
 
@@ -1569,6 +1696,12 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
         return CGS_ERR_BAD_ARG;
     }
     CGS_CUDA(cudaSetDevice(p->device));
+    if (p->F > 1) {
+        drop_graphs(p);
+        for (int f = 0; f < p->F; ++f) CGS_TRY(cgs_set_tuning(p->fr[f], t));
+        p->tune = *t;
+        return CGS_OK;
+    }
     const bool bins = t->tile != p->tune.tile || t->work_slice != p->tune.work_slice ||
                       t->spread_chunk != p->tune.spread_chunk || t->spread_block != p->tune.spread_block;
     p->tune = *t;
@@ -1583,6 +1716,13 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
     if (!p) { set_error("null plan"); return CGS_ERR_BAD_ARG; }
     if (!p->have_k) { set_error("autotune needs the k-space"); return CGS_ERR_STATE; }
     if (p->d != 2) { set_error("the autotuner covers 2-D plans"); return CGS_ERR_BAD_ARG; }
+    if (p->F > 1) {  // frames share the geometry: tune the first, apply to all
+        cgs_tuning t{};
+        CGS_TRY(cgs_autotune(p->fr[0], &t, ms, stream));
+        CGS_TRY(cgs_set_tuning(p, &t));
+        if (chosen) *chosen = t;
+        return CGS_OK;
+    }
     CGS_CUDA(cudaSetDevice(p->device));
     cudaStream_t st = pick_stream(p, stream);
     const int64_t gridN = p->ntot * p->nc, ksN = p->M * p->nc;
@@ -1709,6 +1849,7 @@ cgs_status cgs_batch_create(cgs_batch **out, cgs_plan *const *plans, const cgs_s
         cgs_plan *p = plans[i];
         const cgs_solve_opts *o = &opts[i];
         if (!p) { set_error("null plan in batch"); return CGS_ERR_BAD_ARG; }
+        if (p->F > 1) { set_error("batches take single-frame plans"); return CGS_ERR_BAD_ARG; }
         if (p->device != plans[0]->device) { set_error("batch plans must share a device"); return CGS_ERR_BAD_ARG; }
         for (int j = 0; j < i; ++j)
             if (plans[j] == p) { set_error("a plan appears twice in the batch"); return CGS_ERR_BAD_ARG; }
@@ -2000,9 +2141,7 @@ cgs_status cs_minimise(cgs_cs *c, cgs_cs_report *rep, cudaStream_t st)
 cgs_status cs_data_in(cgs_cs *c, const float *y, cudaStream_t st)
 {
     cgs_plan *p = c->p;
-    const void *src;
-    CGS_TRY(stage_in(y, sizeof(float2) * p->M * p->nc, p->ioA, &src, st));
-    CGS_TRY(launch_gather_ks((const float2 *)src, p->perm, p->M, p->nc, c->ksData, st));
+    CGS_TRY(gather_ks(p, y, c->ksData, st));
     CGS_TRY(launch_cs_nnz(c->ksData, p->M * p->nc, c->partial, c->sums + kSumNnz, st));
     CGS_TRY(cs_read(c, st));
     c->ndnz = c->hsums[kSumNnz];
@@ -2105,16 +2244,19 @@ cgs_status cgs_cs_create(cgs_cs **out, cgs_plan *p, const cgs_cs_opts *o)
         set_error("negative iteration count");
         return CGS_ERR_BAD_ARG;
     }
+    if (p->F > 1 && p->d != 2) { set_error("CS over frames takes 2-D frames"); return CGS_ERR_BAD_ARG; }
     CsTerms tm{};
-    // codeare order: axis 0 is the plan's fastest axis
+    // codeare order: axis 0 is the plan's fastest axis; frames are the third
+    // axis of the image (the dim4 image (N, N, nt), NCSENSE.hpp:173-180)
+    const int rank = p->F > 1 ? 3 : p->d;
     tm.D0 = p->N[p->d - 1];
-    tm.D1 = p->d >= 2 ? p->N[p->d - 2] : 1;
-    tm.D2 = p->d >= 3 ? p->N[p->d - 3] : 1;
+    tm.D1 = p->N[p->d - 2];
+    tm.D2 = p->F > 1 ? p->F : (p->d >= 3 ? p->N[p->d - 3] : 1);
     for (int i = 0; i < 2; ++i) {
         tm.tvw[i] = o->tvw[i];
         if (o->tvw[i] == 0.f) continue;
         const int nd = std::max(0, std::min(3, o->ntvdims[i]));
-        tm.tvmode[i] = cs_tv_mode(p->d, o->tvdims[i], nd);
+        tm.tvmode[i] = cs_tv_mode(rank, o->tvdims[i], nd);
         if (tm.tvmode[i] < 0) { set_error("no TV operator for these image axes"); return CGS_ERR_BAD_ARG; }
         if (tm.tvmode[i] != 3 && tm.D0 != tm.D1) { set_error("TV over axes 0 and 1 needs a square image"); return CGS_ERR_BAD_ARG; }
         if (tm.tvmode[i] == 3 && tm.D2 < 2) { set_error("TV over axis 2 needs at least 2 slices"); return CGS_ERR_BAD_ARG; }
@@ -2126,7 +2268,7 @@ cgs_status cgs_cs_create(cgs_cs **out, cgs_plan *p, const cgs_cs_opts *o)
     if (dwt) {
         // DWT<T>(N) of CS_XSENSE.hpp:133: a square 2-D transform with dyadic
         // sides down to 2^4 (WL_SCALE, DWT.hpp:38-40)
-        if (p->d != 2 || tm.D0 != tm.D1 || (tm.D0 & (tm.D0 - 1)) != 0) {
+        if (rank != 2 || tm.D0 != tm.D1 || (tm.D0 & (tm.D0 - 1)) != 0) {
             set_error("the wavelet transform needs a square 2-D image with dyadic sides");
             return CGS_ERR_BAD_ARG;
         }

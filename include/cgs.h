@@ -55,6 +55,12 @@ typedef struct {
     int m;           /* Kaiser-Bessel cut-off (reference default 1)        */
     int64_t M;       /* k-space nodes per coil ("nk")                      */
     int ncoils;      /* NC; 1 for a plain NFFT                             */
+    int frames;      /* 0 or 1: one trajectory.  F > 1: NCSENSE's dim4 x dim5
+                        batch (NCSENSE.hpp:141-166, 204-348): F frames with a
+                        trajectory of M nodes each (k-space (d, M, F)) and the
+                        same sensitivities and weights; images (N^d, F),
+                        signals (M, NC, F); solves and CS run over the
+                        stacked frames.  Not for Toeplitz, FCG or batches. */
 } cgs_plan_desc;
 
 /* Create / destroy.  Allocates all device scratch up front. */

@@ -212,7 +212,7 @@ class CSXSense:
         return x if self.filt is None else dwt_inv(self._c(x), *self.filt).T
 
     def set_data(self, y):
-        self.data = np.asarray(y, np.complex128).reshape(self.s.nc, -1)
+        self.data = np.asarray(y, np.complex128).reshape(self.s.data_shape)
         self.ndnz = float(np.count_nonzero(self.data))
 
     # CS_XSENSE.hpp:223-232

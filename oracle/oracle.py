@@ -220,6 +220,7 @@ class Sense:
         self.w = None if w is None else _f64(w).reshape(self.M)
         self.what = damp_mask(self.shape)
         self.I = intensity_map(self.S)
+        self.data_shape = (self.nc, self.M)
         self.threads = _threads(threads)
 
     def _S(self):
@@ -269,6 +270,51 @@ class Sense:
                                float(lam), int(maxit), float(tol), _d(y.view(np.float64)),
                                _d(x.view(np.float64)), _d(res), self.threads)
         return x, res[:n + 1]
+
+
+class FramesSense:
+    """NCSENSE with dim4 (x dim5) frames (NCSENSE.hpp:141-166, 204-348): frame
+    f has its own trajectory ks[f]; every frame shares the sensitivities and
+    the weights.  Images (F, *shape), data (F, NC, M); CGLS (CGLS.hpp:30-59)
+    runs over the stacked frames."""
+
+    def __init__(self, S, ks, w=None, m=1, alpha=1.0, threads=0):
+        self.frames = [Sense(S, k, w=w, m=m, alpha=alpha, threads=threads) for k in ks]
+        s0 = self.frames[0]
+        self.F, self.nc, self.M = len(self.frames), s0.nc, s0.M
+        self.shape = (self.F,) + tuple(s0.shape)
+        self.data_shape = (self.F, self.nc, self.M)
+
+    def trafo(self, x):
+        x = np.asarray(x).reshape(self.shape)
+        return np.stack([s.trafo(x[f]) for f, s in enumerate(self.frames)])
+
+    def adjoint_codeare(self, y, ftiter=3, fteps=1e-3):
+        y = np.asarray(y).reshape(self.data_shape)
+        return np.stack([s.adjoint_codeare(y[f], ftiter, fteps) for f, s in enumerate(self.frames)])
+
+    def cgls_codeare(self, y, cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3):
+        """CGLS.hpp:30-59 in FP64 over the stacked frames"""
+        A = lambda v: self.adjoint_codeare(v, ftiter, fteps)
+        p = A(y)
+        if cgiter == 0:
+            return p, np.zeros(0)
+        r = p.copy()
+        rn = xn = float(np.vdot(r, p).real)
+        x = np.zeros_like(p)
+        res = []
+        for _ in range(cgiter):
+            q = rn / xn
+            res.append(q)
+            if np.isnan(q) or q <= cgeps:
+                break
+            q = A(self.trafo(p)) + lam * p
+            ts = rn / float(np.vdot(p, q).real)
+            x += ts * p
+            r -= ts * q
+            rno, rn = rn, float(np.vdot(r, r).real)
+            p = r + (rn / rno) * p
+        return x, np.array(res)
 
 
 # ---------------------------------------------------------------------------
