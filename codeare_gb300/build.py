@@ -78,18 +78,19 @@ PLUGIN = os.path.join(LIBDIR, "CGSENSE.so")
 PLUGIN_NUFFT = os.path.join(LIBDIR, "NuFFT.so")
 PLUGIN_ESTSENS = os.path.join(LIBDIR, "EstimateSensitivities.so")
 PLUGIN_CS = os.path.join(LIBDIR, "CompressedSensing.so")
+PLUGIN_GRASP = os.path.join(LIBDIR, "GRASP.so")
 DRIVER = os.path.join(LIBDIR, "cgsense_run")
 
 
 def build_host(force: bool = False) -> str:
-    """The C++ drop-in layer: CGSENSE.so, NuFFT.so, EstimateSensitivities.so and
-    CompressedSensing.so (ReconStrategy plugins over libcgs.so) and cgsense_run
-    (a dlopen host that drives a plugin)."""
+    """The C++ drop-in layer: CGSENSE.so, NuFFT.so, EstimateSensitivities.so,
+    CompressedSensing.so and GRASP.so (ReconStrategy plugins over libcgs.so)
+    and cgsense_run (a dlopen host that drives a plugin)."""
     srcs = [os.path.join(HOST, f) for f in ("CGSENSE.cpp", "cgsense_run.cpp", "NuFFT.cpp",
-                                            "EstimateSensitivities.cpp", "CompressedSensing.cpp")]
+                                            "EstimateSensitivities.cpp", "CompressedSensing.cpp", "GRASP.cpp")]
     hdrs = [os.path.join(HOST, "codeare", f) for f in os.listdir(os.path.join(HOST, "codeare"))]
     newest = max(os.path.getmtime(f) for f in srcs + hdrs + [LIB])
-    outs = (PLUGIN, DRIVER, PLUGIN_NUFFT, PLUGIN_ESTSENS, PLUGIN_CS)
+    outs = (PLUGIN, DRIVER, PLUGIN_NUFFT, PLUGIN_ESTSENS, PLUGIN_CS, PLUGIN_GRASP)
     if not force and all(os.path.exists(o) for o in outs) and min(os.path.getmtime(o) for o in outs) >= newest:
         return PLUGIN
     common = ["g++", "-O2", "-std=c++17", "-Wall", "-I" + HOST, "-I" + os.path.join(ROOT, "include")]
@@ -102,6 +103,8 @@ def build_host(force: bool = False) -> str:
         common + ["-fPIC", "-shared", srcs[3], "-o", PLUGIN_ESTSENS + ".tmp", "-L" + LIBDIR, "-lcgs",
                   "-Wl,-rpath,$ORIGIN"],
         common + ["-fPIC", "-shared", srcs[4], "-o", PLUGIN_CS + ".tmp", "-L" + LIBDIR, "-lcgs",
+                  "-Wl,-rpath,$ORIGIN"],
+        common + ["-fPIC", "-shared", srcs[5], "-o", PLUGIN_GRASP + ".tmp", "-L" + LIBDIR, "-lcgs",
                   "-Wl,-rpath,$ORIGIN"],
     ]
     for cmd in cmds:

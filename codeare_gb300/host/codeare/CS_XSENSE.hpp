@@ -73,7 +73,7 @@ public:
 
     virtual Matrix<T> Adjoint(const MatrixType<T> &m) const
     {
-        Matrix<T> out(m_ft.ImageSize());
+        Matrix<T> out(m_ft.image_dims());
         m_rep = cgs_cs_report{};
         cgs_host::check(cgs_cs_adjoint(handle(), reinterpret_cast<const float *>(m.Ptr()),
                                        reinterpret_cast<float *>(out.Ptr()), &m_rep, nullptr),
@@ -85,7 +85,7 @@ public:
     // gradient of the objective at x for data y (CS_XSENSE::df with data = y)
     Matrix<T> df(const Matrix<T> &y, const Matrix<T> &x) const
     {
-        Matrix<T> g(m_ft.ImageSize());
+        Matrix<T> g(m_ft.image_dims());
         cgs_host::check(cgs_cs_df(handle(), reinterpret_cast<const float *>(y.Ptr()),
                                   reinterpret_cast<const float *>(x.Ptr()), reinterpret_cast<float *>(g.Ptr()),
                                   nullptr),

@@ -13,10 +13,13 @@
 //                                                          (NCSENSE.hpp:251-301)
 //   Adjoint / ->*       the full CG-SENSE solve            (NCSENSE.hpp:408-436)
 //
+// dim4 / dim5 (NCSENSE.hpp:141-166, 204-348): dim4 x dim5 frames, each with
+// its own trajectory (k-space (d, nk, dim4[, dim5])) and the shared
+// sensitivities and weights; images (N.., dim4[, dim5]), signals
+// (nk, NC, dim4[, dim5]); the CG-SENSE solve runs over the stacked frames.
 // The whole solve runs on the GPU (libcgs.so cgs_solve); unlike the
 // reference's CGLS member, no residual history survives between solves.
-// Not supported (the constructor throws): nmany / dim4 / dim5 batches and a
-// Cartesian third dimension.
+// Not supported (the constructor throws): a Cartesian third dimension.
 #pragma once
 
 #include <cstdio>
@@ -56,8 +59,8 @@ public:
         m_weighted = try_to_fetch<int>(params, "weighted", 1);
         if (try_to_fetch<bool>(params, "3rd_dim_cart", false))
             throw std::invalid_argument("NCSENSE: a Cartesian third dimension is not supported");
-        if (params.exists("dim4") || params.exists("dim5"))
-            throw std::invalid_argument("NCSENSE: multi-volume batches (dim4/dim5) are not supported");
+        m_dim4 = std::max<size_t>(1, try_to_fetch<size_t>(params, "dim4", 1));
+        m_dim5 = std::max<size_t>(1, try_to_fetch<size_t>(params, "dim5", 1));
         plan();
     }
 
@@ -70,6 +73,7 @@ public:
         this->m_params = o.m_params;
         m_sm = o.m_sm; m_k = o.m_k; m_w = o.m_w;
         m_ftiter = o.m_ftiter; m_fteps = o.m_fteps; m_alpha = o.m_alpha; m_m = o.m_m; m_nk = o.m_nk;
+        m_dim4 = o.m_dim4; m_dim5 = o.m_dim5;
         m_cgiter = o.m_cgiter; m_cgeps = o.m_cgeps; m_lambda = o.m_lambda; m_verbose = o.m_verbose;
         m_mode = o.m_mode; m_weighted = o.m_weighted; m_have_k = o.m_have_k; m_have_w = o.m_have_w;
         if (o.m_plan) {
@@ -99,7 +103,8 @@ public:
 
     virtual void KSpace(const Matrix<RT> &k)
     {
-        if (size(k, 1) != m_nk || size(k, 0) != m_rank) throw NCSENSE_KSPACE_DIMENSIONS;
+        if (size(k, 1) != m_nk || size(k, 0) != m_rank || k.Size() != m_rank * m_nk * frames())
+            throw NCSENSE_KSPACE_DIMENSIONS;
         m_k = k;
         cgs_host::check(cgs_set_kspace(m_plan, k.Ptr()), "cgs_set_kspace");
         m_have_k = true;
@@ -116,7 +121,10 @@ public:
 
     virtual Matrix<T> Trafo(const MatrixType<T> &m) const
     {
-        Matrix<T> out(m_nk, m_nc);
+        std::vector<size_t> od{m_nk, m_nc};  // m_fwd_out (NCSENSE.hpp:173)
+        if (frames() > 1) od.push_back(m_dim4);
+        if (m_dim5 > 1) od.push_back(m_dim5);
+        Matrix<T> out(od);
         cgs_host::check(cgs_sense_trafo(m_plan, reinterpret_cast<const float *>(m.Ptr()),
                                         reinterpret_cast<float *>(out.Ptr()), nullptr), "cgs_sense_trafo");
         return squeeze(out);
@@ -125,7 +133,7 @@ public:
 
     virtual Matrix<T> operator/(const MatrixType<T> &m) const
     {
-        Matrix<T> out(m_imsz);
+        Matrix<T> out(image_dims());
         if (m_mode == CGS_MODE_CODEARE)
             cgs_host::check(cgs_sense_adjoint_codeare(m_plan, reinterpret_cast<const float *>(m.Ptr()),
                                                       reinterpret_cast<float *>(out.Ptr()), (int)m_ftiter,
@@ -139,7 +147,7 @@ public:
 
     virtual Matrix<T> Adjoint(const MatrixType<T> &m) const
     {
-        Matrix<T> out(m_imsz);
+        Matrix<T> out(image_dims());
         cgs_solve_opts o{};
         o.mode = m_mode; o.cgiter = (int)m_cgiter; o.cgeps = m_cgeps; o.lambda = m_lambda;
         o.ftiter = (int)m_ftiter; o.fteps = m_fteps; o.weighted = m_weighted;
@@ -160,6 +168,15 @@ public:
     virtual Matrix<T> operator->*(const MatrixType<T> &m) const { return Adjoint(m); }
 
     size_t KSpaceSize() const { return m_nk; }
+    size_t frames() const { return m_dim4 * m_dim5; }
+    // image dims: N.. plus dim4 (and dim5) when batched (m_bwd_out without NC, NCSENSE.hpp:175-180)
+    std::vector<size_t> image_dims() const
+    {
+        std::vector<size_t> v = m_imsz;
+        if (frames() > 1) v.push_back(m_dim4);
+        if (m_dim5 > 1) v.push_back(m_dim5);
+        return v;
+    }
     const std::vector<size_t> &ImageSize() const { return m_imsz; }
     cgs_plan *Plan() const { return m_plan; }  // the operator's plan (for callers that build on it)
     const cgs_solve_report &LastReport() const { return m_last; }
@@ -188,6 +205,7 @@ private:
         d.m = (int)m_m;
         d.M = (int64_t)m_nk;
         d.ncoils = (int)m_nc;
+        d.frames = (int)frames();
         cgs_host::check(cgs_plan_create(&m_plan, &d), "cgs_plan_create");
         cgs_host::check(cgs_set_sensitivities(m_plan, reinterpret_cast<const float *>(m_sm.Ptr())),
                         "cgs_set_sensitivities");
@@ -204,6 +222,7 @@ private:
         m_plan = o.m_plan; o.m_plan = nullptr;
         m_sm = std::move(o.m_sm); m_k = std::move(o.m_k); m_w = std::move(o.m_w); m_imsz = o.m_imsz;
         m_rank = o.m_rank; m_nc = o.m_nc; m_nk = o.m_nk; m_ftiter = o.m_ftiter; m_m = o.m_m;
+        m_dim4 = o.m_dim4; m_dim5 = o.m_dim5;
         m_cgiter = o.m_cgiter; m_fteps = o.m_fteps; m_alpha = o.m_alpha; m_cgeps = o.m_cgeps;
         m_lambda = o.m_lambda; m_verbose = o.m_verbose; m_have_k = o.m_have_k; m_have_w = o.m_have_w;
         m_mode = o.m_mode; m_weighted = o.m_weighted; m_last = o.m_last;
@@ -213,7 +232,7 @@ private:
     Matrix<T> m_sm;
     Matrix<RT> m_k, m_w;
     std::vector<size_t> m_imsz;
-    size_t m_rank = 2, m_nc = 1, m_nk = 1, m_ftiter = 3, m_m = 1, m_cgiter = 0;
+    size_t m_rank = 2, m_nc = 1, m_nk = 1, m_ftiter = 3, m_m = 1, m_cgiter = 0, m_dim4 = 1, m_dim5 = 1;
     double m_fteps = 1e-3, m_alpha = 1.0;
     RT m_cgeps = 1.0e-6f, m_lambda = 1.0e-6f;
     bool m_verbose = false, m_have_k = false, m_have_w = false;

@@ -31,7 +31,7 @@ def test_plugin_exports_reconstrategy_factories():
     import ctypes
     from codeare_gb300 import build
     build.build()
-    for so in (build.PLUGIN, build.PLUGIN_NUFFT, build.PLUGIN_ESTSENS, build.PLUGIN_CS):
+    for so in (build.PLUGIN, build.PLUGIN_NUFFT, build.PLUGIN_ESTSENS, build.PLUGIN_CS, build.PLUGIN_GRASP):
         P = ctypes.CDLL(so)
         assert hasattr(P, "create") and hasattr(P, "destroy"), so
     assert os.access(build.DRIVER, os.X_OK)

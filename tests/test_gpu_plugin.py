@@ -209,3 +209,55 @@ def test_compressed_sensing_plugin_matches_oracle(gpu, tmp_path):
     assert img.shape == (32, 32)
     assert rel(img, xo) < 2e-3, r.stdout
     assert "%d NLCG iterations" % len(o.log) in r.stdout
+
+
+def grasp_weights(nx, nv):
+    """GRASP.cpp:158-162 with codeare's float linspace (Creators.hpp:573-590)"""
+    def linspace(a, b, n):
+        r = np.full(n, np.float32(a), np.float32)
+        gap = np.float32((np.float32(b) - np.float32(a)) / np.float32(n - 1))
+        for i in range(1, n - 1):
+            r[i] = np.float32(r[i - 1] + gap)
+        r[n - 1] = np.float32(b)
+        return r
+    half = np.concatenate([linspace(1.0, 0.002, nx // 2), linspace(0.002, 1.0, nx // 2)])
+    w = (half.astype(np.float64) ** 0.75).astype(np.float32)
+    return np.tile(w, nv)
+
+
+def test_grasp_plugin_matches_oracle(gpu, tmp_path):
+    """GRASP.so: stack-of-stars data sorted into frames (GRASP.cpp:129-170),
+    one CS over NCSENSE with dim4 = frames per slice inside the margins,
+    against the FP64 restatement slice by slice."""
+    from codeare_gb300 import build, cgsm, synth
+    from oracle import oracle as O, cs
+    N, nc, nz, nx, nt, nv = 32, 3, 3, 64, 4, 10
+    NV = nt * nv + 2                                   # two views past the last frame are dropped
+    k = synth.radial2d(NV, nx, golden=True).reshape(NV, nx, 2).astype(np.float32)
+    sens = np.stack([synth.coils2d(N, nc) * (1.0 + 0.2 * z) for z in range(nz)], axis=1)  # (nc, nz, N, N)
+    w = grasp_weights(nx, nv)
+    ks = list(k[:nt * nv].reshape(nt, nv * nx, 2))
+    rng = np.random.default_rng(3)
+    meas = (rng.standard_normal((nc, nz, NV, nx)) + 1j * rng.standard_normal((nc, nz, NV, nx))).astype(np.complex64)
+    kw = dict(tvw=(0.02, 0.0), tvdims=([0, 0, 1], None), xfmw=0.0, l1=1e-6, pnorm=1.0, csiter=3, nliter=6,
+              lsiter=6, lsa=0.01, lsb=0.6, cgconv=0.0, parallel_linesearch=True, cgiter=0, cgeps=1e-6, lam=1e-9,
+              ftiter=1, fteps=7e-4)
+    expect = {}
+    for z in (1, 2):                                   # margin_top = 1
+        fs = O.FramesSense(sens[:, z], ks, w=w, m=1, alpha=1.0)
+        x = np.stack([synth.phantom(N) * (1.0 + 0.15 * t + 0.1 * z) for t in range(nt)])
+        y = synth.add_noise(fs.trafo(x), 1e-3, seed=10 + z)   # (nt, nc, nv nx)
+        meas[:, z, :nt * nv, :] = y.transpose(1, 0, 2).reshape(nc, nt * nv, nx)
+        expect[z] = cs.CSXSense(fs, **kw).adjoint(meas[:, z, :nt * nv, :].reshape(nc, nt, nv * nx).transpose(1, 0, 2))
+    inp, out, xml = tmp_path / "in.cgsm", tmp_path / "out.cgsm", tmp_path / "cfg.xml"
+    cgsm.write(str(inp), {"meas": meas, "kspace": k, "sensitivities": sens.astype(np.complex64)})
+    attrs = {"ta": 40.0, "frame_duration": 10, "margin_top": 1, "margin_bottom": 0, "tv": "0 0 1", "l1": 1e-6,
+             "verbose": 1}
+    xml.write_text("<GRASP " + " ".join('%s="%s"' % kv for kv in attrs.items()) + "/>\n")
+    r = subprocess.run([build.DRIVER, build.PLUGIN_GRASP, str(xml), str(inp), str(out), "im_xd"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    im = cgsm.read(str(out))["im_xd"]                  # codeare (N, N, nz', nt)
+    assert im.shape == (nt, 2, N, N)
+    for i, z in enumerate((1, 2)):
+        assert rel(im[:, i], expect[z]) < 2e-3, (z, r.stdout)
