@@ -65,7 +65,7 @@ class CsOpts(C.Structure):
                 ("lsiter", C.c_int), ("lsa", C.c_float), ("lsb", C.c_float), ("cgconv", C.c_float),
                 ("parallel_linesearch", C.c_int), ("tvw", C.c_float * 2), ("tvdims", (C.c_int * 3) * 2),
                 ("ntvdims", C.c_int * 2), ("xfmw", C.c_float), ("l1", C.c_float), ("pnorm", C.c_float),
-                ("wl_family", C.c_int), ("wl_member", C.c_int)]
+                ("wl_family", C.c_int), ("wl_member", C.c_int), ("ft", C.c_int)]
 
 
 class CsReport(C.Structure):
@@ -338,13 +338,14 @@ class Plan:
 
 class CS:
     """Compressed sensing over a plan's NCSENSE operator (codeare's CS_XSENSE
-    with ft = 3, minimised by NLCG).  The plan needs k-space, weights and
+    with ft = 3, minimised by NLCG), or with ft = 2 over a single-coil plan's
+    NFFT (its inverse by CGNR with ftiter steps and threshold fteps).  The plan needs k-space, weights and
     sensitivities and must not be used elsewhere while a CS call runs.
     tvdims: per TV term the list of TV'ed axes in codeare order (None: all)."""
 
     def __init__(self, plan, tvw=(0.0, 0.0), tvdims=(None, None), xfmw=0.0, l1=0.0, pnorm=0.0, nlopt=0,
                  csiter=1, nliter=4, lsiter=8, lsa=0.01, lsb=0.6, cgconv=1e-4, parallel_linesearch=False,
-                 cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3, wl_family=-1, wl_member=0):
+                 cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3, wl_family=-1, wl_member=0, ft=3):
         o = CsOpts()
         o.cgiter, o.cgeps, o.lambda_, o.ftiter, o.fteps = int(cgiter), float(cgeps), float(lam), int(ftiter), float(fteps)
         o.nlopt, o.csiter, o.nliter, o.lsiter = int(nlopt), int(csiter), int(nliter), int(lsiter)
@@ -357,7 +358,7 @@ class CS:
             for j, v in enumerate(dims):
                 o.tvdims[i][j] = int(v)
         o.xfmw, o.l1, o.pnorm = float(xfmw), float(l1), float(pnorm)
-        o.wl_family, o.wl_member = int(wl_family), int(wl_member)
+        o.wl_family, o.wl_member, o.ft = int(wl_family), int(wl_member), int(ft)
         self.plan = plan
         h = C.c_void_p()
         _check(load().cgs_cs_create(C.byref(h), plan._h, C.byref(o)))

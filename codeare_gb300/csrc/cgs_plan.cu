@@ -1957,6 +1957,7 @@ cgs_status cgs_batch_solve(cgs_batch *b, const float *const *y, float *const *x,
 struct cgs_cs {
     cgs_plan *p = nullptr;
     int device = 0;  // the plan's device (destroy must not touch the plan, which may be gone)
+    int ft = 3;      // 3 NCSENSE, 2 plain NFFT
     cgs_cs_opts o{};
     CsTerms tm{};
     cgs_solve_opts so{};
@@ -1993,6 +1994,11 @@ cgs_status cs_solve(cgs_cs *c, cudaStream_t st)
     cgs_plan *p = c->p;
     const cgs_solve_opts *o = &c->so;
     c->solves++;
+    if (c->ft == 2) {  // NFFT ->*: the CGNR inverse NFFT of the single coil (NFFT.hpp:370-436)
+        CGS_TRY(op_itrafo(p, p->ksY, o->ftiter, o->fteps, st));
+        CGS_CUDA(cudaMemcpyAsync(p->vX, p->cF, sizeof(float2) * p->Nt, cudaMemcpyDeviceToDevice, st));
+        return CGS_OK;
+    }
     if (o->cgiter == 0) return op_eh_codeare(p, p->ksY, o->ftiter, o->fteps, p->vX, st);  // CGLS.hpp:32-33
     const bool same = p->solve_exec && p->sg_mode == CGS_MODE_CODEARE && p->sg_toep == 0 &&
                       p->sg_weighted == o->weighted && p->sg_ftiter == o->ftiter && p->sg_fteps == o->fteps;
@@ -2032,6 +2038,12 @@ cgs_status cs_dwt(cgs_cs *c, const float2 *in, float2 *out, int inverse, cudaStr
     return CGS_OK;
 }
 
+// the CS operator's forward (ft * x): E of NCSENSE, or the single-coil NFFT
+cgs_status cs_E(cgs_cs *c, const float2 *x, float2 *ks, cudaStream_t st)
+{
+    return op_forward(c->p, x, c->ft == 2 ? 1 : 0, nullptr, ks, st);
+}
+
 // g = df(x) (CS_XSENSE.hpp:223-232); leaves E wx in ksE and wx in wxp for
 // the next Update and objective
 cgs_status cs_df(cgs_cs *c, const float2 *x, float2 *g, cudaStream_t st)
@@ -2040,7 +2052,7 @@ cgs_status cs_df(cgs_cs *c, const float2 *x, float2 *g, cudaStream_t st)
     const int64_t nks = p->M * p->nc;
     if (c->dwt) CGS_TRY(cs_dwt(c, x, c->wx, 1, st));
     c->wxp = c->dwt ? c->wx : x;
-    CGS_TRY(op_forward(p, c->wxp, 0, nullptr, c->ksE, st));
+    CGS_TRY(cs_E(c, c->wxp, c->ksE, st));
     CGS_TRY(launch_cs_sub(p->ksY, c->ksE, c->ksData, nks, st));
     CGS_TRY(cs_solve(c, st));
     if (!c->dwt) return launch_cs_grad(x, p->vX, c->tm, g, st);
@@ -2057,7 +2069,7 @@ cgs_status cs_update(cgs_cs *c, const float2 *dx, const float2 **wdxp, cudaStrea
 {
     if (c->dwt) CGS_TRY(cs_dwt(c, dx, c->wdx, 1, st));
     *wdxp = c->dwt ? c->wdx : dx;
-    return op_forward(c->p, *wdxp, 0, nullptr, c->ksG, st);
+    return cs_E(c, *wdxp, c->ksG, st);
 }
 
 cgs_status cs_read(cgs_cs *c, cudaStream_t st)
@@ -2231,7 +2243,10 @@ cgs_status cgs_cs_create(cgs_cs **out, cgs_plan *p, const cgs_cs_opts *o)
 {
     if (!out || !o) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
     *out = nullptr;
-    CGS_TRY(check_ready(p, true, true));
+    const int ft = o->ft == 0 ? 3 : o->ft;
+    if (ft != 2 && ft != 3) { set_error("ft: 2 (NFFT) or 3 (NCSENSE)"); return CGS_ERR_BAD_ARG; }
+    CGS_TRY(check_ready(p, true, ft == 3));
+    if (ft == 2 && (p->nc != 1 || p->F > 1)) { set_error("ft = 2 takes a single-coil, single-frame plan"); return CGS_ERR_BAD_ARG; }
     if (o->nlopt != 0 && o->nlopt != 2) { set_error("nlopt: only 0 (NLCG) and 2 (Split Bregman)"); return CGS_ERR_BAD_ARG; }
     // the reference initialises filters for Daubechies 4 / 8 and Haar 2 only (Wavelet.hpp:165-200)
     const bool dwt = o->wl_family > -1 && o->wl_family <= 5;
@@ -2279,6 +2294,7 @@ cgs_status cgs_cs_create(cgs_cs **out, cgs_plan *p, const cgs_cs_opts *o)
     cgs_cs *c = new cgs_cs;
     c->p = p;
     c->device = p->device;
+    c->ft = ft;
     c->o = *o;
     c->tm = tm;
     c->dwt = dwt;
@@ -2345,7 +2361,7 @@ cgs_status cgs_cs_adjoint(cgs_cs *c, const float *y, float *x, cgs_cs_report *re
 {
     if (!c || !y || !x) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
     cgs_plan *p = c->p;
-    CGS_TRY(check_ready(p, true, true));
+    CGS_TRY(check_ready(p, true, c->ft == 3));
     cudaStream_t st = pick_stream(p, stream);
     if (rep) std::memset(rep, 0, sizeof(*rep));
     CGS_CUDA(cudaEventRecord(p->ev0, st));
@@ -2390,7 +2406,7 @@ cgs_status cgs_cs_df(cgs_cs *c, const float *y, const float *x, float *g, void *
 {
     if (!c || !y || !x || !g) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
     cgs_plan *p = c->p;
-    CGS_TRY(check_ready(p, true, true));
+    CGS_TRY(check_ready(p, true, c->ft == 3));
     cudaStream_t st = pick_stream(p, stream);
     c->solves = 0;
     CGS_CUDA(cudaMemsetAsync(c->tally, 0, 2 * sizeof(int), st));
@@ -2410,7 +2426,7 @@ cgs_status cgs_cs_wavelet(cgs_cs *c, const float *in, float *out, int inverse, v
 {
     if (!c || !in || !out) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
     cgs_plan *p = c->p;
-    CGS_TRY(check_ready(p, true, true));
+    CGS_TRY(check_ready(p, true, c->ft == 3));
     cudaStream_t st = pick_stream(p, stream);
     CGS_TRY(cs_image_in(p, in, c->dx, st));
     CGS_TRY(cs_dwt(c, c->dx, c->g1, inverse ? 1 : 0, st));
@@ -2422,14 +2438,14 @@ cgs_status cgs_cs_obj(cgs_cs *c, const float *y, const float *x, const float *dx
 {
     if (!c || !y || !x || !dx || !obj) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
     cgs_plan *p = c->p;
-    CGS_TRY(check_ready(p, true, true));
+    CGS_TRY(check_ready(p, true, c->ft == 3));
     cudaStream_t st = pick_stream(p, stream);
     CGS_TRY(cs_data_in(c, y, st));
     CGS_TRY(cs_image_in(p, x, c->x, st));
     CGS_TRY(cs_image_in(p, dx, c->dx, st));
     if (c->dwt) CGS_TRY(cs_dwt(c, c->x, c->wx, 1, st));
     c->wxp = c->dwt ? c->wx : c->x;
-    CGS_TRY(op_forward(p, c->wxp, 0, nullptr, c->ksE, st));
+    CGS_TRY(cs_E(c, c->wxp, c->ksE, st));
     const float2 *wdxp = nullptr;
     CGS_TRY(cs_update(c, c->dx, &wdxp, st));
     CsSteps steps{};

@@ -1,12 +1,13 @@
 // CompressedSensing.cpp -- the compressed-sensing ReconStrategy plugin
 // (CompressedSensing.so), a drop-in for codeare's module of the same name
-// with ft = 3, i.e. CS over the non-Cartesian SENSE operator (reference:
-// src/modules/CompressedSensing.cpp:31-205).
+// with ft = 3 (CS over the non-Cartesian SENSE operator) and ft = 2 (CS over
+// the plain NFFT) (reference: src/modules/CompressedSensing.cpp:31-205).
 //
 // Lifecycle, keys and workspace names are the reference's:
-//   Init     ftdims ("N0 N1 [N2]"), test_case, noise, ft, verbose and for
+//   Init     ftdims ("N0 N1 [N2]"), test_case, noise, ft, verbose; for
 //            ft = 3 the NCSENSE keys nk, ftmaxit, fteps, cgmaxit, cgeps,
-//            lambda, cart_3rd_dim, ftalpha (workspace "sensitivities"), then
+//            lambda, cart_3rd_dim, ftalpha (workspace "sensitivities"); for
+//            ft = 2 the NFFT keys fteps, ftalpha, ftiter, ftm, ftnk; then
 //            the CS keys nlopt, parallel_linesearch, tvw1, tvw2, tv1, xfmw,
 //            l1, lsa, lsb, pnorm, wl_family, wl_member, csiter, cgiter (the
 //            NLCG iterations), cgconv, lsiter
@@ -15,8 +16,8 @@
 //            Shepp-Logan phantom when test_case is set, plus optional noise)
 // The reference reads every key with RHSAttribute, whose value is undefined
 // when the key is absent; here absent keys take CS_XSENSE's own defaults
-// (zero weights and iterations, wl_family -1).  Only ft = 3 is served (the
-// GPU path); test_case needs a 2-D image (the 3-D phantom is not provided);
+// (zero weights and iterations, wl_family -1).  ft = 0 and 1 (Cartesian) are
+// not served; test_case needs a 2-D image (the 3-D phantom is not provided);
 // an optional key seed fixes the noise (the reference seeds from the clock).
 #include <cstdio>
 #include <cstdlib>
@@ -54,26 +55,33 @@ public:
         Attribute("test_case", &m_test_case);
         Attribute("noise", &m_noise);
         Attribute("ft", &m_ft_type);
-        if (m_ft_type != 3) {
-            std::printf("**ERROR - CompressedSensing::Init: ft = %d; this module serves ft = 3 (NCSENSE)\n",
-                        m_ft_type);
+        if (m_ft_type != 3 && m_ft_type != 2) {
+            std::printf("**ERROR - CompressedSensing::Init: ft = %d; this module serves ft = 2 (NFFT) and 3 "
+                        "(NCSENSE)\n", m_ft_type);
             return codeare::UNSUPPORTED_DIMENSION;
         }
         if (m_test_case && m_dim != 2) {
             std::printf("**ERROR - CompressedSensing::Init: test_case needs a 2-D image\n");
             return codeare::UNSUPPORTED_DIMENSION;
         }
-        std::printf("  FFT class: NCSENSE\n");
+        std::printf("  FFT class: %s\n", m_ft_type == 3 ? "NCSENSE" : "NUFFT");
         try {
             Params p;
-            p["sensitivities"] = Get<cxfl>("sensitivities");
             int i = 0; float f = 0.f; bool b = false;
-            if (Attribute("nk", &i) == 0) p["nk"] = (size_t)i;
-            if (Attribute("ftmaxit", &i) == 0) p["ftiter"] = (size_t)i;
-            if (Attribute("fteps", &f) == 0) p["fteps"] = f;
-            if (Attribute("cgmaxit", &i) == 0) p["cgiter"] = (size_t)i;
-            if (Attribute("cgeps", &f) == 0) p["cgeps"] = f;
-            if (Attribute("lambda", &f) == 0) p["lambda"] = f;
+            if (m_ft_type == 3) {  // CompressedSensing.cpp:86-101
+                p["sensitivities"] = Get<cxfl>("sensitivities");
+                if (Attribute("nk", &i) == 0) p["nk"] = (size_t)i;
+                if (Attribute("ftmaxit", &i) == 0) p["ftiter"] = (size_t)i;
+                if (Attribute("fteps", &f) == 0) p["fteps"] = f;
+                if (Attribute("cgmaxit", &i) == 0) p["cgiter"] = (size_t)i;
+                if (Attribute("cgeps", &f) == 0) p["cgeps"] = f;
+                if (Attribute("lambda", &f) == 0) p["lambda"] = f;
+            } else {  // CompressedSensing.cpp:73-85
+                if (Attribute("fteps", &f) == 0) p["epsilon"] = f;
+                if (Attribute("ftiter", &i) == 0) p["maxit"] = (size_t)i;
+                if (Attribute("ftm", &i) == 0) p["m"] = (size_t)i;
+                if (Attribute("ftnk", &i) == 0) p["nk"] = (size_t)i;
+            }
             if (Attribute("cart_3rd_dim", &b) == 0) p["3rd_dim_cart"] = b;
             if (Attribute("ftalpha", &f) == 0) p["alpha"] = f;
             p["imsz"] = m_image_size;

@@ -1,18 +1,19 @@
 // CS_XSENSE.hpp -- compressed sensing over the GB300 NCSENSE operator with
 // the interface of codeare's CS_XSENSE<T> (reference:
-// src/matrix/ft/CS_XSENSE.hpp:47-431) for ft = 3.
+// src/matrix/ft/CS_XSENSE.hpp:47-431) for ft = 3 (NCSENSE) and ft = 2 (NFFT).
 //
 // Params keys as the reference constructor (CS_XSENSE.hpp:73-140) and its
 // NLCG (src/optimisation/NLCG.hpp:33-40): tvw1, tv1, tvw2, tv2, xfmw, l1,
 // pnorm, nlopt, ft, csiter, wl_family, wl_member, nliter, cgconv, lsiter,
 // lsa, lsb, parallel_linesearch, verbose; the NCSENSE keys (sensitivities,
-// nk, ftiter, fteps, cgiter, cgeps, lambda, alpha) build the operator.
+// nk, ftiter, fteps, cgiter, cgeps, lambda, alpha) or the NFFT keys (nk,
+// imsz, m, alpha, maxit, epsilon) build the operator.
 //
 //   Trafo / operator*   E, the NCSENSE forward operator
 //   Adjoint / ->*       the CS reconstruction: x0 = NCSENSE ->* data, TV
 //                       weights scaled by max |x0|, csiter NLCG runs
 //   obj, df             the objective and its gradient (CS_XSENSE.hpp:197-232)
-// Every step runs on the GPU (libcgs.so cgs_cs_*).  Supported: ft = 3;
+// Every step runs on the GPU (libcgs.so cgs_cs_*).  Supported: ft = 3 and 2;
 // nlopt 0 (NLCG) and 2 (Split Bregman, whose Minimise is empty in the
 // reference); wl_family -1 (no wavelet).  Anything else throws, where the
 // reference either throws as well or needs DFT / CSENSE / L-BFGS / DWT.
@@ -22,18 +23,23 @@
 #include <string>
 #include <vector>
 
+#include <memory>
+
 #include "NCSENSE.hpp"
 
 template <class T> class CS_XSENSE : public FT<T> {
     typedef typename TypeTraits<T>::RT RT;
 
 public:
-    explicit CS_XSENSE(const Params &p) : FT<T>(p), m_ft(p)
+    explicit CS_XSENSE(const Params &p) : FT<T>(p)
     {
         const int ft = try_to_fetch<int>(p, "ft", 4);
-        if (ft != 3) throw std::invalid_argument("CS_XSENSE: only ft = 3 (NCSENSE) runs on the GPU");
+        if (ft == 3) m_ncs.reset(new NCSENSE<T>(p));
+        else if (ft == 2) m_nft.reset(new NFFT<T>(p));
+        else throw std::invalid_argument("CS_XSENSE: ft = 2 (NFFT) or 3 (NCSENSE) run on the GPU");
         cgs_cs_opts &o = m_o;
         o = cgs_cs_opts{};
+        o.ft = ft;
         o.tvw[0] = try_to_fetch<float>(p, "tvw1", 0.f);
         o.tvw[1] = try_to_fetch<float>(p, "tvw2", 0.f);
         dims(p, "tv1", 0);
@@ -58,22 +64,26 @@ public:
         o.lambda = try_to_fetch<double>(p, "lambda", 1.0e-6);
         o.ftiter = (int)try_to_fetch<size_t>(p, "ftiter", 3);
         o.fteps = try_to_fetch<double>(p, "fteps", 1.0e-3);
+        if (ft == 2) {  // NFFT::Adjoint's own settings (NFFT.hpp:114-115)
+            o.ftiter = (int)try_to_fetch<size_t>(p, "maxit", 3);
+            o.fteps = try_to_fetch<double>(p, "epsilon", 7.0e-4);
+        }
     }
 
     CS_XSENSE(const CS_XSENSE &) = delete;
     CS_XSENSE &operator=(const CS_XSENSE &) = delete;
     virtual ~CS_XSENSE() { release(); }
 
-    virtual void KSpace(const Matrix<RT> &k) { m_ft.KSpace(k); }
-    virtual void Weights(const Matrix<RT> &w) { m_ft.Weights(w); }
-    virtual void Sensitivities(const Matrix<T> &sm) { m_ft.Sensitivities(sm); }
+    virtual void KSpace(const Matrix<RT> &k) { ft().KSpace(k); }
+    virtual void Weights(const Matrix<RT> &w) { ft().Weights(w); }
+    virtual void Sensitivities(const Matrix<T> &sm) { ft().Sensitivities(sm); }
 
-    virtual Matrix<T> Trafo(const MatrixType<T> &m) const { return m_ft.Trafo(m); }
+    virtual Matrix<T> Trafo(const MatrixType<T> &m) const { return m_ncs ? m_ncs->Trafo(m) : m_nft->Trafo(m); }
     virtual Matrix<T> operator*(const MatrixType<T> &m) const { return Trafo(m); }
 
     virtual Matrix<T> Adjoint(const MatrixType<T> &m) const
     {
-        Matrix<T> out(m_ft.image_dims());
+        Matrix<T> out(image_dims());
         m_rep = cgs_cs_report{};
         cgs_host::check(cgs_cs_adjoint(handle(), reinterpret_cast<const float *>(m.Ptr()),
                                        reinterpret_cast<float *>(out.Ptr()), &m_rep, nullptr),
@@ -85,7 +95,7 @@ public:
     // gradient of the objective at x for data y (CS_XSENSE::df with data = y)
     Matrix<T> df(const Matrix<T> &y, const Matrix<T> &x) const
     {
-        Matrix<T> g(m_ft.image_dims());
+        Matrix<T> g(image_dims());
         cgs_host::check(cgs_cs_df(handle(), reinterpret_cast<const float *>(y.Ptr()),
                                   reinterpret_cast<const float *>(x.Ptr()), reinterpret_cast<float *>(g.Ptr()),
                                   nullptr),
@@ -106,7 +116,7 @@ public:
     }
 
     const cgs_cs_report &LastReport() const { return m_rep; }
-    const NCSENSE<T> &getFT() const { return m_ft; }
+    const FT<T> &getFT() const { return m_ncs ? (const FT<T> &)*m_ncs : (const FT<T> &)*m_nft; }
 
     virtual std::ostream &Print(std::ostream &os) const
     {
@@ -115,7 +125,7 @@ public:
            << ") Pnorm: " << m_o.pnorm << "\n";
         os << "    NLCG iterations: (" << m_o.nliter << ") LS(" << m_o.lsiter << ") conv(" << m_o.cgconv
            << ") lsa(" << m_o.lsa << ") lsb(" << m_o.lsb << ")\n";
-        return m_ft.Print(os);
+        return getFT().Print(os);
     }
 
 private:
@@ -132,7 +142,8 @@ private:
     // created on first use: the plan needs k-space, weights and sensitivities
     cgs_cs *handle() const
     {
-        if (!m_cs) cgs_host::check(cgs_cs_create(&m_cs, m_ft.Plan(), &m_o), "cgs_cs_create");
+        if (!m_cs)
+            cgs_host::check(cgs_cs_create(&m_cs, m_ncs ? m_ncs->Plan() : m_nft->Plan(), &m_o), "cgs_cs_create");
         return m_cs;
     }
 
@@ -142,7 +153,11 @@ private:
         m_cs = nullptr;
     }
 
-    NCSENSE<T> m_ft;
+    FT<T> &ft() { return m_ncs ? (FT<T> &)*m_ncs : (FT<T> &)*m_nft; }
+    std::vector<size_t> image_dims() const { return m_ncs ? m_ncs->image_dims() : m_nft->image_dims(); }
+
+    std::unique_ptr<NCSENSE<T>> m_ncs;
+    std::unique_ptr<NFFT<T>> m_nft;
     cgs_cs_opts m_o{};
     mutable cgs_cs *m_cs = nullptr;
     mutable cgs_cs_report m_rep{};

@@ -141,6 +141,8 @@ public:
 
     size_t Rank() const { return m_N.size(); }
     size_t ImageSize() const { return m_N.empty() ? 0 : m_N[0]; }
+    const std::vector<size_t> &image_dims() const { return m_N; }
+    cgs_plan *Plan() const { return m_plan; }  // the operator's plan (for callers that build on it)
     size_t KSpaceSize() const { return m_M; }
     size_t Maxit() const { return m_maxit; }
     RT Alpha() const { return m_alpha; }

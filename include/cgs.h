@@ -311,6 +311,11 @@ typedef struct {
      * NLCG variable is then the image's wavelet coefficients.  Needs a
      * square 2-D image with dyadic sides; levels down to 16 x 16. */
     int wl_family, wl_member;
+    /* operator (CS_XSENSE.hpp:98-110): 3 (or 0) NCSENSE, whose ->* is the
+     * CGLS above; 2 plain NFFT (a single-coil plan, no sensitivities), whose
+     * ->* is the plan's CGNR inverse NFFT with ftiter steps and threshold
+     * fteps (NFFT.hpp:370-436) */
+    int ft;
 } cgs_cs_opts;
 
 typedef struct {

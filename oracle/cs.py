@@ -169,20 +169,44 @@ def dwt_inv(c, lo, hi, min_level=4):
     return r
 
 
+class NFFTOp:
+    """codeare's NFFT operator as CS_XSENSE uses it with ft = 2: * is the NFFT,
+    ->* its CGNR inverse with the density weights and the damping mask
+    (NFFT.hpp:305-436), one coil."""
+
+    def __init__(self, shape, k, w=None, m=1, alpha=1.0):
+        from . import oracle as O
+        self.shape = tuple(shape)
+        self.M = int(np.asarray(k).size // len(self.shape))
+        self.nfft = O.NFFT(self.shape, self.M, m=m, alpha=alpha)
+        self.nfft.set_x(np.asarray(k, np.float64))
+        self.w = None if w is None else np.asarray(w, np.float64)
+        self.what = O.damp_mask(self.shape)
+        self.nc, self.data_shape = 1, (self.M,)
+
+    def trafo(self, x):
+        return self.nfft.trafo(np.asarray(x, np.complex128).reshape(self.shape))
+
+    def inverse(self, y, maxit, eps):
+        return self.nfft.itrafo(y, self.w, self.what, maxit, eps)[0]
+
+
 def _pw(v, l1, e):
     """(|v|^2 + l1)^e, the reference's om *= conj(om); om += l1; om ^= e."""
     return (np.abs(v) ** 2 + l1) ** e
 
 
 class CSXSense:
-    """CS_XSENSE<cxfl> with ft = 3 (NCSENSE); with wl_family >= 0 the NLCG
+    """CS_XSENSE<cxfl> with ft = 3 (NCSENSE, `sense` an oracle.Sense or
+    FramesSense) or ft = 2 (plain NFFT, `sense` an NFFTOp); with wl_family >= 0 the NLCG
     variable is the image's wavelet coefficients (CS_XSENSE.hpp:131-134)."""
 
     def __init__(self, sense, tvw=(0.0, 0.0), tvdims=(None, None), xfmw=0.0, l1=0.0, pnorm=0.0,
                  nlopt=0, csiter=1, nliter=4, lsiter=8, lsa=0.01, lsb=0.6, cgconv=1e-4,
                  parallel_linesearch=False, cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3,
-                 wl_family=-1, wl_member=0):
+                 wl_family=-1, wl_member=0, ft=3):
         self.s = sense
+        self.ft = ft
         self.filt = wavelet_filters(wl_family, wl_member) if wl_family > -1 else None
         self.nd = len(sense.shape)
         self.tvw = [float(tvw[0]), float(tvw[1])]
@@ -199,6 +223,8 @@ class CSXSense:
         return self.s.trafo(x)
 
     def Einv(self, y):
+        if self.ft == 2:
+            return self.s.inverse(y, self.solve["ftiter"], self.solve["fteps"])
         return self.s.cgls_codeare(y, **self.solve)[0]
 
     def _c(self, x):  # codeare-ordered view

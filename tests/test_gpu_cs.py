@@ -217,3 +217,48 @@ def test_cs_reconstruction_wavelet_matches_oracle(gpu):
     rep = gpu.CS(p, **kw).adjoint(y, x)
     assert rep["ls_index"] == [li for li, _ in o.log]
     assert rel(x, xo) < TOL_IMG
+
+
+def setup_nfft(cg, N=32, m=1, alpha=1.0):
+    """single-coil NFFT data for CS with ft = 2"""
+    from codeare_gb300 import synth
+    from oracle import cs
+    k = synth.radial2d(24, 64, golden=True)
+    w = synth.ramp_weights(k)
+    op = cs.NFFTOp((N, N), k, w=w, m=m, alpha=alpha)
+    y = c64(synth.add_noise(op.trafo(synth.phantom(N)), 1e-3, seed=6))
+    p = cg.Plan((N, N), k.shape[0], ncoils=1, m=m, alpha=alpha)
+    p.set_kspace(np.ascontiguousarray(k, np.float32))
+    p.set_weights(np.ascontiguousarray(w, np.float32))
+    return op, p, y
+
+
+@pytest.mark.parametrize("m,alpha", [(1, 1.0), (4, 2.0)])
+def test_cs_over_nfft_matches_oracle(gpu, m, alpha):
+    """ft = 2 (CompressedSensing.cpp:73-85): E is the single-coil NFFT and its
+    ->* the CGNR inverse NFFT (ftiter steps, threshold fteps)."""
+    from oracle import cs
+    op, p, y = setup_nfft(gpu, m=m, alpha=alpha)
+    kw = dict(tvw=(2e-3, 0.0), xfmw=5e-3, l1=1e-6, pnorm=1.0, csiter=2, nliter=5, lsiter=8, lsa=1e-3, lsb=0.6,
+              cgconv=1e-5, ftiter=3, fteps=7e-4, ft=2)
+    o = cs.CSXSense(op, **kw)
+    g = gpu.CS(p, **kw)
+    x0 = np.zeros((1, 32, 32), np.complex64)
+    p.nfft_itrafo(y, x0, maxit=3, eps=7e-4)
+    x0 = x0[0]
+    o.set_data(y)
+    go = o.df(x0)
+    gg = np.zeros_like(x0)
+    g.df(y, x0, gg)
+    assert rel(gg, go) < TOL_GRAD
+    dx = rand_img((32, 32), 5, scale=0.1 * float(np.abs(x0).max()))
+    o.update(dx)
+    fo, _ = o.obj(x0, dx, 0.36)
+    fg, _ = g.obj(y, x0, dx, 0.36)
+    assert abs(fg - fo) <= TOL_OBJ * abs(fo)
+    o2 = cs.CSXSense(op, **kw)
+    xo = o2.adjoint(y)
+    x = np.zeros_like(x0)
+    rep = gpu.CS(p, **kw).adjoint(y, x)
+    assert rep["ls_index"] == [li for li, _ in o2.log]
+    assert rel(x, xo) < TOL_IMG

@@ -261,3 +261,28 @@ def test_grasp_plugin_matches_oracle(gpu, tmp_path):
     assert im.shape == (nt, 2, N, N)
     for i, z in enumerate((1, 2)):
         assert rel(im[:, i], expect[z]) < 2e-3, (z, r.stdout)
+
+
+def test_compressed_sensing_plugin_nfft(gpu, tmp_path):
+    """CompressedSensing.so with ft = 2: CS over the plain NFFT (the
+    reference's nufft_cs configurations), keys of CompressedSensing.cpp:73-85."""
+    from codeare_gb300 import build, cgsm, synth
+    from oracle import cs
+    k = synth.radial2d(24, 64, golden=True)
+    w = synth.ramp_weights(k)
+    op = cs.NFFTOp((32, 32), k, w=w, m=1, alpha=1.0)
+    y = synth.add_noise(op.trafo(synth.phantom(32)), 1e-3, seed=6).astype(np.complex64)
+    kw = dict(tvw=(2e-3, 0.0), xfmw=5e-3, l1=1e-6, pnorm=1.0, csiter=2, nliter=5, lsiter=8, lsa=1e-3, lsb=0.6,
+              cgconv=1e-5, ftiter=3, fteps=7e-4, ft=2)
+    xo = cs.CSXSense(op, **kw).adjoint(y)
+    attrs = {"ftdims": "32 32", "ft": 2, "test_case": 0, "noise": 0, "verbose": 0, "ftnk": k.shape[0], "ftiter": 3,
+             "fteps": 7e-4, "ftalpha": 1.0, "ftm": 1, "nlopt": 0, "parallel_linesearch": 0, "tvw1": 2e-3, "tvw2": 0,
+             "xfmw": 5e-3, "l1": 1e-6, "lsa": 1e-3, "lsb": 0.6, "pnorm": 1, "wl_family": -1, "wl_member": 0,
+             "csiter": 2, "cgiter": 5, "cgconv": 1e-5, "lsiter": 8}
+    inp, out, xml = tmp_path / "in.cgsm", tmp_path / "out.cgsm", tmp_path / "cfg.xml"
+    cgsm.write(str(inp), {"kspace": k, "weights": w, "data": y})
+    xml.write_text("<CompressedSensing " + " ".join('%s="%s"' % kv for kv in attrs.items()) + "/>\n")
+    r = subprocess.run([build.DRIVER, build.PLUGIN_CS, str(xml), str(inp), str(out), "im_dc"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert rel(cgsm.read(str(out))["im_dc"], xo) < 2e-3, r.stdout
