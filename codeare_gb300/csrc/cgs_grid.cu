@@ -464,6 +464,207 @@ spread_patch_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ 
         }
 }
 
+// ---------------------------------------------------------------------------
+// Spreading on the tensor cores.  A warp owns a 4 x 4 patch and 4 NT coils;
+// each batch of kSpreadBatch = 8 list entries is one k-step of
+// mma.m16n8k8 (TF32 operands, FP32 accumulation):
+//   D[16 points][8 NT cols] += W[16 points][8 entries] V[8 entries][8 NT cols]
+// W holds the entries' window weights at the patch points (wy * wx *
+// density), V their coil values (column 2c and 2c + 1: Re and Im of coil c).
+// Both operands are split into a TF32 value and its TF32 remainder and the
+// products lo*hi, hi*lo, hi*hi are accumulated (the dropped lo*lo is below
+// 2^-22 relative), which keeps the accuracy of FP32 fused multiply-adds.
+// Fragments follow the PTX ISA layout of m16n8k8 .tf32: thread (g = lane/4,
+// t = lane%4) holds A rows g, g+8 x columns t, t+4; B rows t, t+4 x column g;
+// D rows g, g+8 x columns 2t, 2t+1.  Patch point r is row r (row-major 4 x 4),
+// so rows g and g+8 are the same column, two rows apart.
+// ---------------------------------------------------------------------------
+// staged value row in floats: at least 8 NT and 8 or 24 mod 32, so the B
+// loads of entry rows t and t + 4 (t = 0..3) fall in distinct banks
+__host__ __device__ constexpr int spread_mma_row(int nt)
+{
+    int r = 8 * nt;
+    while (r % 32 != 8 && r % 32 != 24) r += 8;
+    return r;
+}
+
+template <int NT> struct SpreadMma {
+    static constexpr int R = spread_mma_row(NT);
+    // one staging buffer: values, window taps, footprint starts, density weights
+    __host__ __device__ static size_t buf_bytes(int taps)
+    {
+        return (size_t)kSpreadBatch * (R * sizeof(float) + 2 * taps * sizeof(float) + sizeof(int2) + sizeof(float));
+    }
+    // per warp: two buffers and the batch's patch weights (8 entries x 4 rows + 4 columns)
+    __host__ __device__ static size_t warp_bytes(int taps) { return 2 * buf_bytes(taps) + kSpreadBatch * 8 * sizeof(float); }
+};
+
+// TF32 split: hi rounded to nearest, lo = x - hi passed as is (the tensor
+// cores read the upper 19 bits of a .tf32 operand, so lo is truncated there)
+__device__ __forceinline__ void tf32_split(float x, uint32_t &hi, uint32_t &lo)
+{
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
+    lo = __float_as_uint(x - __uint_as_float(hi));
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+{
+    asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+template <int NT, int TAPS = 0>
+__global__ void __launch_bounds__(256, 3)
+spread_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
+                  const float2 *__restrict__ ks, const float *__restrict__ dens, int weighted,
+                  float2 *__restrict__ grid)
+{
+    using S = SpreadMma<NT>;
+    constexpr int R = S::R, CC = 4 * NT, CH = 2 * NT;     // coils per warp; 16-byte chunks per entry row
+    extern __shared__ float4 smem4[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wi = blockIdx.x * 8 + warp;
+    if (wi >= ps.nwork) return;
+    const int taps = TAPS > 0 ? TAPS : 2 * g.m + 2;
+    const int WS = 2 * taps;
+    const size_t bb = S::buf_bytes(taps);                  // a multiple of 16 bytes
+    char *wbase = reinterpret_cast<char *>(smem4) + (size_t)warp * S::warp_bytes(taps);
+    float *swt = reinterpret_cast<float *>(wbase + 2 * bb);   // [entry][wy 0..3, wx 0..3]
+    const int c0 = blockIdx.y * CC;
+    const int ccn = min(CC, g.nc - c0);
+    const bool v16 = ((g.nc & 1) == 0);
+    const int4 wk = ps.work[wi];
+    const int n0 = g.n[0], n1 = g.n[1];
+    const int gq = lane >> 2, tq = lane & 3;
+    const int py0 = (wk.x / ps.npx) * 4, px0 = (wk.x % ps.npx) * 4;
+    const bool wide = (n0 >= taps) && (n1 >= taps);
+    // zero both buffers once: padding columns and rows past a short batch stay finite
+    {
+        float4 *z = reinterpret_cast<float4 *>(wbase);
+        const int n16 = (int)(2 * bb / 16);
+        for (int i = lane; i < n16; i += 32) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncwarp();
+    }
+    auto buffers = [&](int buf, float *&sv, float *&sw, int2 *&su, float *&sd) {
+        char *b = wbase + (size_t)buf * bb;
+        sv = reinterpret_cast<float *>(b);
+        sw = sv + kSpreadBatch * R;
+        su = reinterpret_cast<int2 *>(sw + kSpreadBatch * WS);
+        sd = reinterpret_cast<float *>(su + kSpreadBatch);
+    };
+    auto issue = [&](int e0, int cnt, int buf) {
+        float *sv, *sw, *sd; int2 *su;
+        buffers(buf, sv, sw, su, sd);
+        const int s_l = (lane < cnt) ? ps.entries[e0 + lane] : 0;
+        if (lane < cnt) {
+            cp_async8(&su[lane], &ps.nodeU[s_l]);
+            if (weighted) cp_async4(&sd[lane], &dens[s_l]);
+            else sd[lane] = 1.f;
+            const float *W = ps.nodeW + (size_t)s_l * WS;
+            for (int q = 0; q < WS; q += 4) cp_async16(&sw[lane * WS + q], W + q);
+        }
+        if (v16) {
+            // all lanes: chunk ch = entry ch / CH, coils 2 (ch % CH) and 2 (ch % CH) + 1
+#pragma unroll
+            for (int i = 0; i < (kSpreadBatch * CH + 31) / 32; ++i) {
+                const int ch = lane + 32 * i;
+                const int e = ch / CH, c = 2 * (ch % CH);
+                const int s = __shfl_sync(0xffffffffu, s_l, e & (kSpreadBatch - 1));
+                if (ch < kSpreadBatch * CH && e < cnt && c < ccn) {
+                    const float2 *v = ks + (size_t)s * g.nc + c0 + c;
+                    float2 *d = reinterpret_cast<float2 *>(sv + e * R) + c;
+                    if (c + 1 < ccn) cp_async16(d, v);
+                    else cp_async8(d, v);
+                }
+            }
+        } else {
+            for (int j = 0; j < cnt; ++j) {
+                const int s = __shfl_sync(0xffffffffu, s_l, j);
+                const float2 *v = ks + (size_t)s * g.nc + c0;
+                float2 *dv = reinterpret_cast<float2 *>(sv + j * R);
+                for (int c = lane; c < ccn; c += 32) cp_async8(dv + c, v + c);
+            }
+        }
+        cp_async_commit();
+    };
+    // window weight of one axis at offset q from the footprint start
+    auto wgt = [&](const float *W, int q, int n) -> float {
+        if (q < 0) q += n;
+        if (wide) return q < taps ? W[q] : 0.f;
+        float w = 0.f;
+        for (int r = q; r < taps; r += n) w += W[r];
+        return w;
+    };
+
+    float acc[NT][4];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+    const int end = wk.y + wk.z;
+    int e0 = wk.y, cnt = min(kSpreadBatch, end - e0), buf = 0;
+    issue(e0, cnt, 0);
+    while (true) {
+        const int e1 = e0 + cnt;
+        const int cnt1 = min(kSpreadBatch, end - e1);
+        if (cnt1 > 0) { issue(e1, cnt1, buf ^ 1); cp_async_wait<1>(); }
+        else cp_async_wait<0>();
+        __syncwarp();
+        float *sv, *sw, *sd; int2 *su;
+        buffers(buf, sv, sw, su, sd);
+        // the batch's patch weights: lane = (entry e, row/column r); zero past cnt
+        {
+            const int e = lane >> 2, r = lane & 3;
+            float wy = 0.f, wx = 0.f;
+            if (e < cnt) {
+                const int2 u = su[e];
+                const float *W = sw + e * WS;
+                if (py0 + r < n0) wy = wgt(W, py0 + r - u.x, n0);
+                if (px0 + r < n1) wx = wgt(W + taps, px0 + r - u.y, n1) * sd[e];
+            }
+            swt[e * 8 + r] = wy;
+            swt[e * 8 + 4 + r] = wx;
+        }
+        __syncwarp();
+        // A: entries tq and tq + 4 at patch rows gq / 4 and gq / 4 + 2, column gq % 4
+        uint32_t ah[4], al[4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const float *wr = swt + (tq + 4 * h) * 8;
+            const float wx = wr[4 + (gq & 3)];
+            tf32_split(wr[gq >> 2] * wx, ah[2 * h], al[2 * h]);
+            tf32_split(wr[(gq >> 2) + 2] * wx, ah[2 * h + 1], al[2 * h + 1]);
+        }
+        const float *r0 = sv + tq * R + gq, *r1 = sv + (tq + 4) * R + gq;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            uint32_t bh0, bl0, bh1, bl1;
+            tf32_split(r0[8 * t], bh0, bl0);
+            tf32_split(r1[8 * t], bh1, bl1);
+            mma_tf32(acc[t], al, bh0, bh1);
+            mma_tf32(acc[t], ah, bl0, bl1);
+            mma_tf32(acc[t], ah, bh0, bh1);
+        }
+        __syncwarp();
+        if (cnt1 <= 0) break;
+        e0 = e1; cnt = cnt1; buf ^= 1;
+    }
+    const int py = py0 + (gq >> 2), px = px0 + (gq & 3);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int yy = py + 2 * h;
+        if (yy >= n0 || px >= n1) continue;
+        const int ppt = gq + 8 * h;                         // point index within the patch
+        float2 *dst = (wk.w < 0) ? grid + ((size_t)yy * n1 + px) * g.nc + c0
+                                 : ps.partial + ((size_t)wk.w * 16 + ppt) * g.nc + c0;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            const int c = 4 * t + tq;
+            if (c < ccn) dst[c] = make_float2(acc[t][2 * h], acc[t][2 * h + 1]);
+        }
+    }
+}
+
 // sum the partial slots of split patches in slot order and store them
 __global__ void patch_reduce_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
                                     float2 *__restrict__ grid)
@@ -1048,7 +1249,35 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
         else CGS_SP(4, 4, CPLV, 1, 1);                          \
     } while (0)
     if (ps.ph != 4 || (ps.pw != 4 && ps.pw != 8)) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
-    if (ps.pw == 8 && ps.blk == 1) {
+    if (ps.blk == 16) {  // tensor cores: 4 NT coils per warp, 4 x 4 patches
+        if (ps.pw != 4) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
+        const int nt = std::min(8, (2 * g.nc + 7) / 8);
+        dim3 grm((ps.nwork + 7) / 8, (g.nc + 4 * nt - 1) / (4 * nt));
+#define CGS_SPM(NTV, TV)                                                                                 \
+    do {                                                                                                 \
+        const size_t sm = 8 * SpreadMma<NTV>::warp_bytes(taps);                                          \
+        CGS_CUDA(cudaFuncSetAttribute(spread_mma_kernel<NTV, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                      (int)sm));                                                         \
+        spread_mma_kernel<NTV, TV><<<grm, 256, sm, st>>>(g, ps, ks, dens, weighted, grid);               \
+    } while (0)
+#define CGS_SPM1(NTV)                                     \
+    do {                                                  \
+        if (taps == 10) CGS_SPM(NTV, 10);                 \
+        else CGS_SPM(NTV, 0);                             \
+    } while (0)
+        switch (nt) {
+            case 8: CGS_SPM1(8); break;
+            case 7: CGS_SPM1(7); break;
+            case 6: CGS_SPM1(6); break;
+            case 5: CGS_SPM1(5); break;
+            case 4: CGS_SPM1(4); break;
+            case 3: CGS_SPM1(3); break;
+            case 2: CGS_SPM1(2); break;
+            default: CGS_SPM1(1); break;
+        }
+#undef CGS_SPM1
+#undef CGS_SPM
+    } else if (ps.pw == 8 && ps.blk == 1) {
         CGS_SP(4, 8, 1, 1, 1);
     } else if (ps.blk == 8) {
         switch (CC) {

@@ -473,9 +473,11 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     // 4 x 8 patches of 2 x 2 blocks and spread_block 2: 4 x 4 patches of 2 x 1 blocks
     // (four coil groups); spread_block 1: 4 x 4 patches, a point per lane, two coil groups
     // spread_block 8: 4 x 8 patches, one coil group, a point per lane
-    const int tb = p->tune.spread_block != 0 ? p->tune.spread_block : 1;
-    const int blk = p->nc == 1 ? 1 : ((tb == 8 || (p->nc >= 4 && (tb == 4 || tb == 2))) ? tb : 1);
-    const int kPatchH = 4, kPatchW = (p->nc == 1 || blk == 4 || blk == 8) ? 8 : 4;
+    // spread_block 16: 4 x 4 patches on the tensor cores (TF32 split, FP32
+    // accumulation), the default from 4 coils up
+    const int tb = p->tune.spread_block != 0 ? p->tune.spread_block : (p->nc >= 4 ? 16 : 1);
+    const int blk = tb == 16 ? 16 : (p->nc == 1 ? 1 : ((tb == 8 || (p->nc >= 4 && (tb == 4 || tb == 2))) ? tb : 1));
+    const int kPatchH = 4, kPatchW = (blk != 16 && (p->nc == 1 || blk == 4 || blk == 8)) ? 8 : 4;
     const int npy = (n0 + kPatchH - 1) / kPatchH, npx = (n1 + kPatchW - 1) / kPatchW;
     const int64_t P = (int64_t)npy * npx, M = p->M;
     std::vector<int> perm(M);
@@ -1689,7 +1691,7 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
         return false;
     };
     if (!in(t->tile, {0, 8, 16, 32}) || !in(t->interp_coils, {0, 1, 4, 8, 16, 32}) ||
-        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 2, 4, 8}) ||
+        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 2, 4, 8, 16}) ||
         (t->work_slice != 0 && (t->work_slice < 32 || t->work_slice > 65536)) ||
         (t->spread_chunk != 0 && (t->spread_chunk < 32 || t->spread_chunk > 65536))) {
         set_error("tuning value out of range");
@@ -1782,15 +1784,17 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
     }
     // spreading: points per lane, chunk bound and coils per warp
     CGS_TRY(fill(p->ksV, ksN, 0x85ebca6bu));
-    for (int blk : {1, 2, 4, 8}) {
+    for (int blk : {16, 1, 2, 4, 8}) {
         if ((blk == 2 || blk == 4) && p->nc < 4) continue;
         if (blk == 8 && (p->nc < 2 || p->nc > 16)) continue;
         for (int chunk : {0, 64, 128, 256, 512, 1024}) {
-            if (blk > 1 && chunk != 0 && chunk != 512) continue;  // block variants: two chunk bounds
+            if (blk > 1 && blk < 16 && chunk != 0 && chunk != 512) continue;  // block variants: two chunk bounds
+            if (blk == 16 && chunk == 64) continue;
             cur = best; cur.spread_chunk = chunk; cur.spread_block = blk;
             p->tune = cur;
             CGS_TRY(rebin(p));
             for (int c : sccs) {
+                if (blk == 16 && c != sccs.front()) continue;  // the tensor-core kernel sets its own coil width
                 if ((blk == 2 || blk == 4) && c < 4) continue;
                 if (blk == 8 && c > 16) continue;
                 p->tune.spread_coils = c;

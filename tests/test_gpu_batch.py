@@ -50,14 +50,18 @@ def test_tuning_changes_decomposition_not_results(gpu):
               dict(tile=16, work_slice=100, spread_chunk=0, interp_coils=1, spread_coils=1, spread_block=0),
               dict(tile=8, work_slice=512, spread_chunk=128, interp_coils=8, spread_coils=4, spread_block=4),
               dict(tile=8, work_slice=512, spread_chunk=0, interp_coils=16, spread_coils=8, spread_block=2),
-              dict(tile=8, work_slice=512, spread_chunk=256, interp_coils=8, spread_coils=8, spread_block=8)]:
+              dict(tile=8, work_slice=512, spread_chunk=256, interp_coils=8, spread_coils=8, spread_block=8),
+              dict(tile=8, work_slice=512, spread_chunk=0, interp_coils=16, spread_coils=0, spread_block=16),
+              dict(tile=16, work_slice=256, spread_chunk=128, interp_coils=8, spread_coils=0, spread_block=16)]:
         p.set_tuning(**t)
         assert p.tuning() == t
         f1, a1 = nfft_pair(p, N, nc, k.shape[0])
         # interpolation sums each node's taps in a fixed order: identical bits
         assert np.array_equal(f1, f0)
-        # spreading sums split patches in another grouping: rounding only
-        assert rel(a1, a0) < 1e-6
+        # spreading sums split patches in another grouping, and the default
+        # (tensor cores, TF32-split operands) rounds differently from the
+        # CUDA-core variants: rounding only
+        assert rel(a1, a0) < 3e-6
     with pytest.raises(capi.CgsError):
         p.set_tuning(tile=12)
     with pytest.raises(capi.CgsError):
@@ -75,11 +79,11 @@ def test_autotune_picks_valid_decomposition(gpu):
     assert ms > 0
     assert t["tile"] in (8, 16, 32) and t["interp_coils"] in (1, 4, 8, 16, 32)
     assert t["spread_coils"] in (1, 2, 4, 8, 16) and t["work_slice"] in (128, 256, 512, 1024)
-    assert t["spread_block"] in (1, 2, 4, 8)
+    assert t["spread_block"] in (1, 2, 4, 8, 16)
     assert p.tuning() == t
     f1, a1 = nfft_pair(p, N, nc, k.shape[0], seed=3)
     assert np.array_equal(f1, f0)
-    assert rel(a1, a0) < 1e-6
+    assert rel(a1, a0) < 3e-6   # the tuned spreading may round differently from the default
     p.close()
 
 
@@ -189,3 +193,24 @@ def test_batch_parity_with_oracle(gpu, oracle):
     b.close()
     for p in plans:
         p.close()
+
+
+@pytest.mark.parametrize("nc", [1, 3, 12, 20, 40])
+def test_tensor_core_spreading_matches_cuda_cores(gpu, nc):
+    """spread_block 16 (mma.m16n8k8, TF32-split operands) against the CUDA-core
+    spreading for coil counts that leave partial n-tiles and coil chunks, on a
+    grid whose side is not a multiple of the patch (N = 50, n = 100)."""
+    from codeare_gb300 import synth
+    N = 50
+    k = synth.radial2d(40, 100, golden=True)
+    p, _ = make_plan(N, nc, k, synth.ramp_weights(k))
+    rng = np.random.default_rng(nc)
+    f = (rng.standard_normal((nc, k.shape[0])) + 1j * rng.standard_normal((nc, k.shape[0]))).astype(np.complex64)
+    ref = np.zeros((nc, N, N), np.complex64)
+    p.set_tuning(spread_block=1)
+    p.nfft_adjoint(f, ref)
+    p.set_tuning(spread_block=16)
+    out = np.zeros_like(ref)
+    p.nfft_adjoint(f, out)
+    assert rel(out, ref) < 2e-6
+    p.close()
