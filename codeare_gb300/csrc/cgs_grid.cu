@@ -665,6 +665,161 @@ spread_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ Pa
     }
 }
 
+// ---------------------------------------------------------------------------
+// 2-D interpolation on the tensor cores.  Nodes are grouped by the 4 x 4 bin
+// of their footprint start, so the footprints of a bin's nodes lie in one
+// U x U region of the grid (U = 3 + taps).  A warp takes up to 16 nodes of
+// one bin and computes with mma.m16n8k8 over the region's points:
+//   f[16 nodes][8 NT cols] = W[16 nodes][U^2 points] G[U^2 points][8 NT cols]
+// W[j][p] = wy_j[dy] wx_j[dx] for p inside node j's footprint, else 0; G is
+// read from the grid through the read-only path (8 consecutive floats per
+// column group, one 32-byte sector), warps of neighbouring bins sharing it in
+// L1.  Both operands are split into TF32 value and remainder and three
+// products are accumulated in FP32, as in the spreading.
+// ---------------------------------------------------------------------------
+template <int NT, int TAPS> struct InterpMma {
+    static constexpr int U = 3 + TAPS, KP = (U * U + 7) / 8 * 8;
+    // zero-padded window rows: entry 3 + i is tap i, so a region coordinate
+    // minus the footprint offset (in [-3, U]) indexes them without checks
+    static constexpr int PL = U + 4;
+    static constexpr size_t warp_bytes = (size_t)kInterpGroup * 2 * PL * sizeof(float) + (size_t)KP * sizeof(int);
+    static constexpr size_t smem = 8 * warp_bytes;
+};
+
+template <int NT, int TAPS>
+__global__ void __launch_bounds__(256, 2)
+interp_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
+                  const float2 *__restrict__ grid, float2 *__restrict__ ks)
+{
+    using I = InterpMma<NT, TAPS>;
+    constexpr int U = I::U, KP = I::KP, CC = 4 * NT, WS = 2 * TAPS, PL = I::PL;
+    extern __shared__ float4 smem4[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wi = blockIdx.x * 8 + warp;
+    if (wi >= ns.niwork) return;
+    float *wpad = reinterpret_cast<float *>(reinterpret_cast<char *>(smem4) + warp * I::warp_bytes);  // [16][2][PL]
+    int *spt = reinterpret_cast<int *>(wpad + kInterpGroup * 2 * PL);                                // [KP] grid points
+    const int4 wk = ns.iwork[wi];                           // {bin, first, count <= 16, 0}
+    const int c0 = blockIdx.y * CC;
+    const int ccn = min(CC, g.nc - c0);
+    const int n0 = g.n[0], n1 = g.n[1];
+    const int by0 = (wk.x / ns.ibx) * 4, bx0 = (wk.x % ns.ibx) * 4;
+    const int cnt = wk.z;
+    // region points (rows and columns wrap once: n0, n1 >= U); -1 past the region
+    for (int q = lane; q < KP; q += 32) {
+        int pt = -1;
+        if (q < U * U) {
+            int gy = by0 + q / U, gx = bx0 + q % U;
+            if (gy >= n0) gy -= n0;
+            if (gx >= n1) gx -= n1;
+            pt = gy * n1 + gx;
+        }
+        spt[q] = pt;
+    }
+    // the group's padded window rows and footprint offsets (relative to the bin)
+    int s_l = -1, oy_l = 0, ox_l = 0;
+    if (lane < kInterpGroup) {
+        float *wy = wpad + lane * 2 * PL, *wx = wy + PL;
+        if (lane < cnt) {
+            s_l = ns.ilist[wk.y + lane];
+            const int2 u = ns.nodeU[s_l];
+            oy_l = u.x - by0;
+            ox_l = u.y - bx0;
+            const float *W = ns.nodeW + (size_t)s_l * WS;
+            for (int i = 0; i < PL; ++i) {
+                const int t = i - 3;
+                wy[i] = (t >= 0 && t < TAPS) ? W[t] : 0.f;
+                wx[i] = (t >= 0 && t < TAPS) ? W[TAPS + t] : 0.f;
+            }
+        } else {
+            for (int i = 0; i < PL; ++i) wy[i] = wx[i] = 0.f;
+        }
+    }
+    __syncwarp();
+    const int gq = lane >> 2, tq = lane & 3;
+    const int na = gq, nb = gq + 8;
+    const int oya = __shfl_sync(0xffffffffu, oy_l, na), oxa = __shfl_sync(0xffffffffu, ox_l, na);
+    const int oyb = __shfl_sync(0xffffffffu, oy_l, nb), oxb = __shfl_sync(0xffffffffu, ox_l, nb);
+    // row pointers shifted so that [qy] / [qx] is tap qy - oy / qx - ox (zero outside)
+    const float *Wya = wpad + na * 2 * PL + 3 - oya, *Wxa = wpad + na * 2 * PL + PL + 3 - oxa;
+    const float *Wyb = wpad + nb * 2 * PL + 3 - oyb, *Wxb = wpad + nb * 2 * PL + PL + 3 - oxb;
+    const float *gf = reinterpret_cast<const float *>(grid) + (size_t)c0 * 2 + gq;
+    const size_t rs = (size_t)g.nc * 2;                     // floats per grid point
+    float acc[NT][4];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+    const bool full = (ccn == CC);
+    // region coordinates of the thread's two points q0 = k0 + tq and q1 = q0 + 4
+    int qy0 = tq / U, qx0 = tq % U, qy1 = (tq + 4) / U, qx1 = (tq + 4) % U;
+#pragma unroll 2
+    for (int k0 = 0; k0 < KP; k0 += 8) {
+        const int p0 = spt[k0 + tq], p1 = spt[k0 + tq + 4];
+        float b0v[NT], b1v[NT];
+        const float *g0 = gf + (size_t)max(p0, 0) * rs, *g1 = gf + (size_t)max(p1, 0) * rs;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            const bool ok = full || (8 * t + gq < 2 * ccn);
+            b0v[t] = (p0 >= 0 && ok) ? __ldg(g0 + 8 * t) : 0.f;
+            b1v[t] = (p1 >= 0 && ok) ? __ldg(g1 + 8 * t) : 0.f;
+        }
+        uint32_t ah[4], al[4];
+        tf32_split(Wya[qy0] * Wxa[qx0], ah[0], al[0]);
+        tf32_split(Wyb[qy0] * Wxb[qx0], ah[1], al[1]);
+        tf32_split(Wya[qy1] * Wxa[qx1], ah[2], al[2]);
+        tf32_split(Wyb[qy1] * Wxb[qx1], ah[3], al[3]);
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            uint32_t bh0, bl0, bh1, bl1;
+            tf32_split(b0v[t], bh0, bl0);
+            tf32_split(b1v[t], bh1, bl1);
+            mma_tf32(acc[t], al, bh0, bh1);
+            mma_tf32(acc[t], ah, bl0, bl1);
+            mma_tf32(acc[t], ah, bh0, bh1);
+        }
+        qx0 += 8; while (qx0 >= U) { qx0 -= U; ++qy0; }
+        qx1 += 8; while (qx1 >= U) { qx1 -= U; ++qy1; }
+    }
+    // rows gq and gq + 8: nodes na and nb, columns 2 tq, 2 tq + 1 of each n-tile
+    const int sa = __shfl_sync(0xffffffffu, s_l, na), sb = __shfl_sync(0xffffffffu, s_l, nb);
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        const int c = 4 * t + tq;
+        if (c < ccn) {
+            if (na < cnt) ks[(size_t)sa * g.nc + c0 + c] = make_float2(acc[t][0], acc[t][1]);
+            if (nb < cnt) ks[(size_t)sb * g.nc + c0 + c] = make_float2(acc[t][2], acc[t][3]);
+        }
+    }
+}
+
+template <int NT, int TAPS>
+static cgs_status launch_interp_mma_t(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,
+                                      cudaStream_t st)
+{
+    using I = InterpMma<NT, TAPS>;
+    CGS_CUDA(cudaFuncSetAttribute(interp_mma_kernel<NT, TAPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)I::smem));
+    dim3 grd((ns.niwork + 7) / 8, (g.nc + 4 * NT - 1) / (4 * NT));
+    interp_mma_kernel<NT, TAPS><<<grd, 256, I::smem, st>>>(g, ns, grid, ks);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+template <int TAPS>
+static cgs_status launch_interp_mma_taps(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,
+                                         cudaStream_t st)
+{
+    switch (std::min(8, (2 * g.nc + 7) / 8)) {
+        case 8: return launch_interp_mma_t<8, TAPS>(g, ns, grid, ks, st);
+        case 7: return launch_interp_mma_t<7, TAPS>(g, ns, grid, ks, st);
+        case 6: return launch_interp_mma_t<6, TAPS>(g, ns, grid, ks, st);
+        case 5: return launch_interp_mma_t<5, TAPS>(g, ns, grid, ks, st);
+        case 4: return launch_interp_mma_t<4, TAPS>(g, ns, grid, ks, st);
+        case 3: return launch_interp_mma_t<3, TAPS>(g, ns, grid, ks, st);
+        case 2: return launch_interp_mma_t<2, TAPS>(g, ns, grid, ks, st);
+        default: return launch_interp_mma_t<1, TAPS>(g, ns, grid, ks, st);
+    }
+}
+
 // sum the partial slots of split patches in slot order and store them
 __global__ void patch_reduce_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
                                     float2 *__restrict__ grid)
@@ -1160,6 +1315,19 @@ cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *gri
     if (ns.nwork == 0 || g.nc == 0) return CGS_OK;
     if (2 * g.m + 2 > kMaxTaps) { set_error("m too large"); return CGS_ERR_BAD_ARG; }
     const int taps = 2 * g.m + 2;
+    if (g.d == 2 && g.imma && ns.ilist && ns.niwork > 0 && ns.nodeU && ns.nodeW && taps <= 10 &&
+        g.n[0] >= 3 + taps && g.n[1] >= 3 + taps) {
+        cgs_status r;
+        prof_begin(PROF_INTERP, st);
+        switch (taps) {
+            case 4: r = launch_interp_mma_taps<4>(g, ns, grid, ks, st); break;
+            case 6: r = launch_interp_mma_taps<6>(g, ns, grid, ks, st); break;
+            case 8: r = launch_interp_mma_taps<8>(g, ns, grid, ks, st); break;
+            default: r = launch_interp_mma_taps<10>(g, ns, grid, ks, st); break;
+        }
+        prof_end(PROF_INTERP, st);
+        return r;
+    }
     if (g.d == 2 && ns.nodeU && ns.nodeW && taps <= 10) {
         // 16 coils per CTA by default: a 46 KB tile (T = 16, m = 4) leaves room
         // for 4 CTAs per SM, and each node reads one full bank row per tap

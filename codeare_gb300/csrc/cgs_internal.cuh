@@ -132,7 +132,10 @@ struct GridGeom {
     int nc;           // coils (innermost in grid and k-space)
     int icc;          // coils per interpolation CTA (1, 4, 8, 16; 0 = automatic)
     int scc;          // coils per spreading warp (1, 2, 4, 8, 16, 32; 0 = automatic)
+    int imma;         // 2-D interpolation on the tensor cores (needs the NodeSet's bin lists)
 };
+
+constexpr int kInterpGroup = 16;     // tensor-core interpolation: nodes per warp (the m16)
 
 struct NodeSet {
     int64_t M;          // nodes
@@ -143,6 +146,12 @@ struct NodeSet {
     const int4 *work;   // {tile index, first node, node count, 0}
     const int2 *nodeU;  // 2-D: per node wrapped footprint start (nullable)
     const float *nodeW; // 2-D: per node [2][2m+2] window weights (nullable)
+    // 2-D tensor-core interpolation: sorted node indices grouped by the 4 x 4
+    // bin of their footprint start, and work items {bin, first, count, 0}
+    const int *ilist;
+    const int4 *iwork;
+    int niwork;
+    int ibx;            // bins per grid row
 };
 
 // Output-stationary 2-D spreading: one warp per work item over a ph x pw patch

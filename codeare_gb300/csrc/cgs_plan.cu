@@ -183,6 +183,10 @@ struct cgs_plan {
     int4 *pwork = nullptr, *pmulti = nullptr;
     float2 *ppartial = nullptr;
     PatchSet pset{};
+    // 2-D tensor-core interpolation: node lists by 4 x 4 footprint-start bin
+    int *ilist = nullptr;
+    int4 *iwork = nullptr;
+    int niwork = 0, ibx = 0;
 
     // host copies of the trajectory and weights (the Toeplitz kernel is built from them)
     std::vector<float> k_host, w_host;
@@ -338,7 +342,7 @@ cgs_status op_forward(cgs_plan *p, const float2 *src_img, int per_coil, const fl
         b.src = p->t2; b.dst = p->grid;
         CGS_TRY(launch_axis_pass(b, st));
     }
-    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW};
+    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork, p->niwork, p->ibx};
     return launch_interp(p->geom, ns, p->grid, ks, st);
 }
 
@@ -351,7 +355,7 @@ cgs_status op_adjoint(cgs_plan *p, const float2 *ks, int weighted, float2 *out, 
         return CGS_OK;
     }
     const int d = p->d, nc = p->nc;
-    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW};
+    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork, p->niwork, p->ibx};
     if (d == 2) {
         // writes every grid point: no clearing pass
         CGS_TRY(launch_spread_patch(p->geom, p->pset, ks, p->w, weighted && p->w != nullptr, p->grid, st));
@@ -459,6 +463,46 @@ void apply_tiles(cgs_plan *p)
     for (int t = 0; t < p->d; ++t) g.nt[t] = (p->n[t] + g.T - 1) / g.T;
     g.icc = p->tune.interp_coils;
     g.scc = p->tune.spread_coils;
+    const int ib = p->tune.interp_block;
+    g.imma = (p->d == 2 && (ib == 16 || (ib == 0 && p->nc >= 4))) ? 1 : 0;
+}
+
+// Node lists of the 2-D tensor-core interpolation: sorted node indices grouped
+// by the 4 x 4 bin of their wrapped footprint start (the same wrap as the
+// device's node tables), work items (one warp each) of at most kInterpGroup
+// nodes of one bin, in bin order so that neighbouring warps read
+// neighbouring grid regions.  `cc` holds floor(n x) per node in trajectory order.
+cgs_status build_ibins(cgs_plan *p, const std::vector<int> &cc, const std::vector<int> &perm)
+{
+    const int n0 = p->n[0], n1 = p->n[1], m = p->m;
+    const int nby = (n0 + 3) / 4, nbx = (n1 + 3) / 4;
+    const int64_t M = p->M;
+    std::vector<int> bin(M), cnt((size_t)nby * nbx + 1, 0);
+    auto wrap = [](int v, int n) { v %= n; return v < 0 ? v + n : v; };
+    for (int64_t s = 0; s < M; ++s) {
+        const int j = perm[s];
+        const int u0 = wrap(cc[(size_t)j * 2] - m, n0), u1 = wrap(cc[(size_t)j * 2 + 1] - m, n1);
+        bin[s] = (u0 / 4) * nbx + u1 / 4;
+        cnt[bin[s] + 1]++;
+    }
+    for (size_t b = 0; b + 1 < cnt.size(); ++b) cnt[b + 1] += cnt[b];
+    std::vector<int> list(M), fill(cnt.begin(), cnt.end() - 1);
+    for (int64_t s = 0; s < M; ++s) list[fill[bin[s]]++] = (int)s;
+    std::vector<int4> work;
+    for (int b = 0; b < nby * nbx; ++b)
+        for (int s0 = cnt[b]; s0 < cnt[b + 1]; s0 += kInterpGroup)
+            work.push_back(make_int4(b, s0, std::min(kInterpGroup, cnt[b + 1] - s0), 0));
+    dev_free(p->ilist);
+    dev_free(p->iwork);
+    p->ilist = nullptr;
+    p->iwork = nullptr;
+    CGS_TRY(dev_alloc(&p->ilist, (size_t)M));
+    CGS_TRY(dev_alloc(&p->iwork, std::max<size_t>(work.size(), 1)));
+    CGS_CUDA(cudaMemcpy(p->ilist, list.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+    if (!work.empty()) CGS_CUDA(cudaMemcpy(p->iwork, work.data(), sizeof(int4) * work.size(), cudaMemcpyHostToDevice));
+    p->niwork = (int)work.size();
+    p->ibx = nbx;
+    return CGS_OK;
 }
 
 // Per 4 x 4 patch (4 x 8 for one coil) of the 2-D grid, the sorted indices of the nodes whose
@@ -549,7 +593,7 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     CGS_CUDA(cudaMemcpy(p->pwork, work.data(), sizeof(int4) * work.size(), cudaMemcpyHostToDevice));
     if (!multi.empty())
         CGS_CUDA(cudaMemcpy(p->pmulti, multi.data(), sizeof(int4) * multi.size(), cudaMemcpyHostToDevice));
-    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW};
+    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork, p->niwork, p->ibx};
     CGS_TRY(launch_node_weights(p->geom, ns, p->nodeU, p->nodeW, p->stream));
     CGS_CUDA(cudaStreamSynchronize(p->stream));
     PatchSet &ps = p->pset;
@@ -1197,7 +1241,7 @@ cgs_status cgs_plan_destroy(cgs_plan *p)
     if (p->stream) cudaStreamSynchronize(p->stream);
     for (cgs_plan *c : p->fr) cgs_plan_destroy(c);
     void *bufs[] = {p->tw[0], p->tw[1], p->tw[2], p->deap[0], p->deap[1], p->deap[2], p->nodes, p->perm,
-                    p->w, p->work, p->nodeU, p->nodeW, p->pentries, p->pwork, p->pmulti, p->ppartial, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
+                    p->w, p->work, p->nodeU, p->nodeW, p->pentries, p->pwork, p->pmulti, p->ppartial, p->ilist, p->iwork, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
                     p->cF, p->cP, p->cZ, p->vX, p->vR, p->vP, p->vQ, p->ioA, p->ioB, p->partial, p->dots,
                     p->active, p->sc, p->fpart, p->ftick};
     for (void *b : bufs) dev_free(b);
@@ -1313,7 +1357,10 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
     CGS_CUDA(cudaMemcpy(p->work, work.data(), sizeof(int4) * work.size(), cudaMemcpyHostToDevice));
     CGS_CUDA(cudaMemcpy(p->nodes, nodes.data(), sizeof(float4) * nodes.size(), cudaMemcpyHostToDevice));
     CGS_CUDA(cudaMemcpy(p->perm, perm.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
-    if (d == 2) CGS_TRY(build_patches(p, cc));
+    if (d == 2) {
+        CGS_TRY(build_patches(p, cc));
+        CGS_TRY(build_ibins(p, cc, perm));
+    }
     p->k_host = k;
     p->have_k = true;
     // weights (if already given) must follow the new order: reset to "unset"
@@ -1691,7 +1738,7 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
         return false;
     };
     if (!in(t->tile, {0, 8, 16, 32}) || !in(t->interp_coils, {0, 1, 4, 8, 16, 32}) ||
-        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 2, 4, 8, 16}) ||
+        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 2, 4, 8, 16}) || !in(t->interp_block, {0, 1, 16}) ||
         (t->work_slice != 0 && (t->work_slice < 32 || t->work_slice > 65536)) ||
         (t->spread_chunk != 0 && (t->spread_chunk < 32 || t->spread_chunk > 65536))) {
         set_error("tuning value out of range");
@@ -1746,7 +1793,7 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
         return CGS_OK;
     };
     auto interp = [&]() -> cgs_status {
-        NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW};
+        NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork, p->niwork, p->ibx};
         return launch_interp(p->geom, ns, p->grid, p->ksR, st);
     };
     auto spread = [&]() -> cgs_status {
@@ -1759,11 +1806,22 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
         if (c <= p->nc && (int)sccs.size() < 3) sccs.push_back(c);
     cgs_tuning best = p->tune, cur = p->tune;
     double t_int = 1e30, t_spr = 1e30, t = 0.0;
-    // interpolation: bin side and coils per CTA, then the work slice
+    // interpolation: the tensor cores, then CUDA-core bin sides and coils per CTA,
+    // then the work slice
     CGS_TRY(fill(p->grid, gridN, 0x9e3779b9u));
+    bool imma_best = false;
+    {
+        cur = best; cur.interp_block = 16;
+        p->tune = cur;
+        apply_tiles(p);
+        if (p->geom.imma) {
+            CGS_TRY(timed(interp, &t));
+            t_int = t; best.interp_block = 16; imma_best = true;
+        }
+    }
     for (int tile : {8, 16, 32}) {
         if (tile > p->n[0] || tile > p->n[1]) continue;
-        cur = best; cur.tile = tile; cur.work_slice = 512;
+        cur = best; cur.tile = tile; cur.work_slice = 512; cur.interp_block = 1;
         p->tune = cur;
         CGS_TRY(rebin(p));
         const int E = std::min(tile, std::min(p->n[0], p->n[1])) + 2 * p->m + 1;
@@ -1772,10 +1830,14 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
             p->tune.interp_coils = c;
             apply_tiles(p);
             CGS_TRY(timed(interp, &t));
-            if (t < t_int) { t_int = t; best.tile = tile; best.work_slice = 512; best.interp_coils = c; }
+            if (t < t_int) {
+                t_int = t; best.tile = tile; best.work_slice = 512; best.interp_coils = c; best.interp_block = 1;
+                imma_best = false;
+            }
         }
     }
     for (int slice : {128, 256, 1024}) {
+        if (imma_best) break;  // the tensor-core kernel does not use the work slices
         cur = best; cur.work_slice = slice;
         p->tune = cur;
         CGS_TRY(rebin(p));

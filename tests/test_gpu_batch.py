@@ -44,7 +44,7 @@ def test_tuning_changes_decomposition_not_results(gpu):
     p, _ = make_plan(N, nc, k, synth.ramp_weights(k))
     f0, a0 = nfft_pair(p, N, nc, k.shape[0])
     assert p.tuning() == dict(tile=0, work_slice=0, spread_chunk=0, interp_coils=0, spread_coils=0,
-                              spread_block=0)
+                              spread_block=0, interp_block=0)
     for t in [dict(tile=8, work_slice=256, spread_chunk=64, interp_coils=4, spread_coils=2, spread_block=1),
               dict(tile=32, work_slice=2048, spread_chunk=1024, interp_coils=16, spread_coils=8, spread_block=4),
               dict(tile=16, work_slice=100, spread_chunk=0, interp_coils=1, spread_coils=1, spread_block=0),
@@ -52,12 +52,22 @@ def test_tuning_changes_decomposition_not_results(gpu):
               dict(tile=8, work_slice=512, spread_chunk=0, interp_coils=16, spread_coils=8, spread_block=2),
               dict(tile=8, work_slice=512, spread_chunk=256, interp_coils=8, spread_coils=8, spread_block=8),
               dict(tile=8, work_slice=512, spread_chunk=0, interp_coils=16, spread_coils=0, spread_block=16),
-              dict(tile=16, work_slice=256, spread_chunk=128, interp_coils=8, spread_coils=0, spread_block=16)]:
+              dict(tile=16, work_slice=256, spread_chunk=128, interp_coils=8, spread_coils=0, spread_block=16),
+              dict(tile=8, work_slice=256, spread_chunk=0, interp_coils=16, spread_coils=0, spread_block=0,
+                   interp_block=1),
+              dict(tile=32, work_slice=512, spread_chunk=0, interp_coils=4, spread_coils=0, spread_block=0,
+                   interp_block=1)]:
+        t = dict(interp_block=0, **t) if "interp_block" not in t else t
         p.set_tuning(**t)
         assert p.tuning() == t
         f1, a1 = nfft_pair(p, N, nc, k.shape[0])
-        # interpolation sums each node's taps in a fixed order: identical bits
-        assert np.array_equal(f1, f0)
+        if t["interp_block"] == 1:
+            # the CUDA-core interpolation rounds differently from the default
+            # tensor-core one (TF32-split operands)
+            assert rel(f1, f0) < 2e-6
+        else:
+            # the tensor-core interpolation does not depend on the bins: identical bits
+            assert np.array_equal(f1, f0)
         # spreading sums split patches in another grouping, and the default
         # (tensor cores, TF32-split operands) rounds differently from the
         # CUDA-core variants: rounding only
@@ -66,6 +76,8 @@ def test_tuning_changes_decomposition_not_results(gpu):
         p.set_tuning(tile=12)
     with pytest.raises(capi.CgsError):
         p.set_tuning(interp_coils=3)
+    with pytest.raises(capi.CgsError):
+        p.set_tuning(interp_block=2)
     p.close()
 
 
@@ -77,13 +89,15 @@ def test_autotune_picks_valid_decomposition(gpu):
     f0, a0 = nfft_pair(p, N, nc, k.shape[0], seed=3)
     t, ms = p.autotune()
     assert ms > 0
-    assert t["tile"] in (8, 16, 32) and t["interp_coils"] in (1, 4, 8, 16, 32)
-    assert t["spread_coils"] in (1, 2, 4, 8, 16) and t["work_slice"] in (128, 256, 512, 1024)
-    assert t["spread_block"] in (1, 2, 4, 8, 16)
+    # the tensor-core interpolation has no bin side or coils per CTA to tune
+    assert t["interp_block"] == 16 or (t["tile"] in (8, 16, 32) and t["interp_coils"] in (1, 4, 8, 16, 32))
+    assert t["spread_coils"] in (1, 2, 4, 8, 16) and (t["interp_block"] == 16 or t["work_slice"] in (128, 256, 512, 1024))
+    assert t["spread_block"] in (1, 2, 4, 8, 16) and t["interp_block"] in (1, 16)
     assert p.tuning() == t
     f1, a1 = nfft_pair(p, N, nc, k.shape[0], seed=3)
-    assert np.array_equal(f1, f0)
-    assert rel(a1, a0) < 3e-6   # the tuned spreading may round differently from the default
+    # the tuned kernels may round differently from the default ones
+    assert rel(f1, f0) < 3e-6
+    assert rel(a1, a0) < 3e-6
     p.close()
 
 
@@ -212,5 +226,27 @@ def test_tensor_core_spreading_matches_cuda_cores(gpu, nc):
     p.set_tuning(spread_block=16)
     out = np.zeros_like(ref)
     p.nfft_adjoint(f, out)
+    assert rel(out, ref) < 2e-6
+    p.close()
+
+
+@pytest.mark.parametrize("nc,m", [(1, 4), (3, 4), (12, 4), (20, 2), (40, 3), (8, 1)])
+def test_tensor_core_interpolation_matches_cuda_cores(gpu, nc, m):
+    """interp_block 16 (4 x 4 footprint-start bins, mma.m16n8k8 with
+    TF32-split operands) against the CUDA-core interpolation, for coil counts
+    with partial n-tiles and coil chunks, every footprint width, on a grid
+    whose side is not a multiple of the bin (N = 50, n = 100)."""
+    from codeare_gb300 import synth
+    N = 50
+    k = synth.radial2d(40, 100, golden=True)
+    p, _ = make_plan(N, nc, k, synth.ramp_weights(k), m=m)
+    rng = np.random.default_rng(nc)
+    fh = (rng.standard_normal((nc, N, N)) + 1j * rng.standard_normal((nc, N, N))).astype(np.complex64)
+    ref = np.zeros((nc, k.shape[0]), np.complex64)
+    p.set_tuning(interp_block=1)
+    p.nfft_trafo(fh, ref)
+    p.set_tuning(interp_block=16)
+    out = np.zeros_like(ref)
+    p.nfft_trafo(fh, out)
     assert rel(out, ref) < 2e-6
     p.close()
