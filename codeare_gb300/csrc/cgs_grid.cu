@@ -687,7 +687,7 @@ template <int NT, int TAPS> struct InterpMma {
 };
 
 template <int NT, int TAPS>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, 3)
 interp_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
                   const float2 *__restrict__ grid, float2 *__restrict__ ks)
 {
@@ -751,7 +751,7 @@ interp_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ No
     const bool full = (ccn == CC);
     // region coordinates of the thread's two points q0 = k0 + tq and q1 = q0 + 4
     int qy0 = tq / U, qx0 = tq % U, qy1 = (tq + 4) / U, qx1 = (tq + 4) % U;
-#pragma unroll 2
+#pragma unroll 1
     for (int k0 = 0; k0 < KP; k0 += 8) {
         const int p0 = spt[k0 + tq], p1 = spt[k0 + tq + 4];
         float b0v[NT], b1v[NT];
