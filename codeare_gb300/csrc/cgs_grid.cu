@@ -689,7 +689,7 @@ template <int NT, int TAPS> struct InterpMma {
 template <int NT, int TAPS>
 __global__ void __launch_bounds__(256, 3)
 interp_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
-                  const float2 *__restrict__ grid, float2 *__restrict__ ks)
+                  const float2 *__restrict__ grid, float2 *__restrict__ ks, float2 *__restrict__ user)
 {
     using I = InterpMma<NT, TAPS>;
     constexpr int U = I::U, KP = I::KP, CC = 4 * NT, WS = 2 * TAPS, PL = I::PL;
@@ -779,8 +779,24 @@ interp_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ No
         qx0 += 8; while (qx0 >= U) { qx0 -= U; ++qy0; }
         qx1 += 8; while (qx1 >= U) { qx1 -= U; ++qy1; }
     }
-    // rows gq and gq + 8: nodes na and nb, columns 2 tq, 2 tq + 1 of each n-tile
+    // rows gq and gq + 8: nodes na and nb, columns 2 tq, 2 tq + 1 of each n-tile.
+    // With `user`, straight into the caller's layout (coil-major, trajectory
+    // order): a bin's nodes are mostly runs of consecutive trajectory samples,
+    // so each coil row's stores stay close to sector-dense.
     const int sa = __shfl_sync(0xffffffffu, s_l, na), sb = __shfl_sync(0xffffffffu, s_l, nb);
+    if (user) {
+        const int ja = na < cnt ? ns.perm[sa] : 0, jb = nb < cnt ? ns.perm[sb] : 0;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            const int c = 4 * t + tq;
+            if (c < ccn) {
+                float2 *row = user + (size_t)(c0 + c) * ns.M;
+                if (na < cnt) row[ja] = make_float2(acc[t][0], acc[t][1]);
+                if (nb < cnt) row[jb] = make_float2(acc[t][2], acc[t][3]);
+            }
+        }
+        return;
+    }
 #pragma unroll
     for (int t = 0; t < NT; ++t) {
         const int c = 4 * t + tq;
@@ -793,30 +809,30 @@ interp_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ No
 
 template <int NT, int TAPS>
 static cgs_status launch_interp_mma_t(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,
-                                      cudaStream_t st)
+                                      float2 *user, cudaStream_t st)
 {
     using I = InterpMma<NT, TAPS>;
     CGS_CUDA(cudaFuncSetAttribute(interp_mma_kernel<NT, TAPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)I::smem));
     dim3 grd((ns.niwork + 7) / 8, (g.nc + 4 * NT - 1) / (4 * NT));
-    interp_mma_kernel<NT, TAPS><<<grd, 256, I::smem, st>>>(g, ns, grid, ks);
+    interp_mma_kernel<NT, TAPS><<<grd, 256, I::smem, st>>>(g, ns, grid, ks, user);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }
 
 template <int TAPS>
 static cgs_status launch_interp_mma_taps(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,
-                                         cudaStream_t st)
+                                         float2 *user, cudaStream_t st)
 {
     switch (std::min(8, (2 * g.nc + 7) / 8)) {
-        case 8: return launch_interp_mma_t<8, TAPS>(g, ns, grid, ks, st);
-        case 7: return launch_interp_mma_t<7, TAPS>(g, ns, grid, ks, st);
-        case 6: return launch_interp_mma_t<6, TAPS>(g, ns, grid, ks, st);
-        case 5: return launch_interp_mma_t<5, TAPS>(g, ns, grid, ks, st);
-        case 4: return launch_interp_mma_t<4, TAPS>(g, ns, grid, ks, st);
-        case 3: return launch_interp_mma_t<3, TAPS>(g, ns, grid, ks, st);
-        case 2: return launch_interp_mma_t<2, TAPS>(g, ns, grid, ks, st);
-        default: return launch_interp_mma_t<1, TAPS>(g, ns, grid, ks, st);
+        case 8: return launch_interp_mma_t<8, TAPS>(g, ns, grid, ks, user, st);
+        case 7: return launch_interp_mma_t<7, TAPS>(g, ns, grid, ks, user, st);
+        case 6: return launch_interp_mma_t<6, TAPS>(g, ns, grid, ks, user, st);
+        case 5: return launch_interp_mma_t<5, TAPS>(g, ns, grid, ks, user, st);
+        case 4: return launch_interp_mma_t<4, TAPS>(g, ns, grid, ks, user, st);
+        case 3: return launch_interp_mma_t<3, TAPS>(g, ns, grid, ks, user, st);
+        case 2: return launch_interp_mma_t<2, TAPS>(g, ns, grid, ks, user, st);
+        default: return launch_interp_mma_t<1, TAPS>(g, ns, grid, ks, user, st);
     }
 }
 
@@ -1310,22 +1326,25 @@ cgs_status launch_interp2_taps(const GridGeom &g, const NodeSet &ns, const float
 }
 
 cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,
-                         cudaStream_t st)
+                         cudaStream_t st, float2 *user, bool *wrote_user)
 {
+    if (wrote_user) *wrote_user = false;
     if (ns.nwork == 0 || g.nc == 0) return CGS_OK;
     if (2 * g.m + 2 > kMaxTaps) { set_error("m too large"); return CGS_ERR_BAD_ARG; }
     const int taps = 2 * g.m + 2;
     if (g.d == 2 && g.imma && ns.ilist && ns.niwork > 0 && ns.nodeU && ns.nodeW && taps <= 10 &&
         g.n[0] >= 3 + taps && g.n[1] >= 3 + taps) {
         cgs_status r;
+        float2 *u = (user && ns.perm) ? user : nullptr;
         prof_begin(PROF_INTERP, st);
         switch (taps) {
-            case 4: r = launch_interp_mma_taps<4>(g, ns, grid, ks, st); break;
-            case 6: r = launch_interp_mma_taps<6>(g, ns, grid, ks, st); break;
-            case 8: r = launch_interp_mma_taps<8>(g, ns, grid, ks, st); break;
-            default: r = launch_interp_mma_taps<10>(g, ns, grid, ks, st); break;
+            case 4: r = launch_interp_mma_taps<4>(g, ns, grid, ks, u, st); break;
+            case 6: r = launch_interp_mma_taps<6>(g, ns, grid, ks, u, st); break;
+            case 8: r = launch_interp_mma_taps<8>(g, ns, grid, ks, u, st); break;
+            default: r = launch_interp_mma_taps<10>(g, ns, grid, ks, u, st); break;
         }
         prof_end(PROF_INTERP, st);
+        if (r == CGS_OK && wrote_user) *wrote_user = (u != nullptr);
         return r;
     }
     if (g.d == 2 && ns.nodeU && ns.nodeW && taps <= 10) {

@@ -182,8 +182,11 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
                                int weighted, float2 *grid, cudaStream_t st);
 
 // y[s][c] (sorted, coil innermost) = sum over footprint of grid[...][c]
+// With `user` (the caller's layout: coil-major, trajectory order) the
+// tensor-core kernel writes there directly and sets *wrote_user; otherwise
+// the result is in ks and the caller scatters it.
 cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,
-                         cudaStream_t st);
+                         cudaStream_t st, float2 *user = nullptr, bool *wrote_user = nullptr);
 // grid[...][c] += sum_s phi * (w_s if weighted) * ks[s][c]; grid must be zeroed first
 cgs_status launch_spread(const GridGeom &g, const NodeSet &ns, const float2 *ks, int weighted,
                          float2 *grid, cudaStream_t st);

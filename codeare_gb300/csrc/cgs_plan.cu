@@ -300,14 +300,17 @@ AxisPass base_pass(cgs_plan *p, int t)
 }
 
 // forward NFFT of all coils.  src_img: single image (expand with sens) when
-// per_coil == 0, else coil-minor per-coil images.  mask may be null.
+// per_coil == 0, else coil-minor per-coil images.  mask may be null.  With
+// `user` the result goes to the caller's layout (coil-major, trajectory
+// order) instead of ks, by the interpolation itself where it can, else by a
+// scatter after it.
 cgs_status op_forward(cgs_plan *p, const float2 *src_img, int per_coil, const float *mask, float2 *ks,
-                      cudaStream_t st)
+                      cudaStream_t st, float2 *user = nullptr)
 {
     if (p->F > 1) {
         for (int f = 0; f < p->F; ++f)
             CGS_TRY(op_forward(p->fr[f], src_img + (per_coil ? f * p->Ntf * p->nc : f * p->Ntf), per_coil, mask,
-                               ks + f * p->Mf * p->nc, st));
+                               ks + f * p->Mf * p->nc, st, user ? user + f * p->Mf * p->nc : nullptr));
         return CGS_OK;
     }
     const int d = p->d, nc = p->nc;
@@ -343,7 +346,10 @@ cgs_status op_forward(cgs_plan *p, const float2 *src_img, int per_coil, const fl
         CGS_TRY(launch_axis_pass(b, st));
     }
     NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork, p->niwork, p->ibx};
-    return launch_interp(p->geom, ns, p->grid, ks, st);
+    bool direct = false;
+    CGS_TRY(launch_interp(p->geom, ns, p->grid, ks, st, user, &direct));
+    if (user && !direct) CGS_TRY(launch_scatter_ks(ks, p->perm, p->M, p->nc, user, st));
+    return CGS_OK;
 }
 
 // adjoint NFFT of all coils into coil-minor per-coil images (deapodised)
@@ -1435,10 +1441,9 @@ cgs_status cgs_nfft_trafo(cgs_plan *p, const float *fhat, float *f, void *stream
     const void *src;
     CGS_TRY(stage_in(fhat, sizeof(float2) * p->Nt * p->nc, p->ioA, &src, st));
     CGS_TRY(launch_to_coil_minor((const float2 *)src, p->Nt, p->nc, p->cF, st));
-    CGS_TRY(op_forward(p, p->cF, 1, nullptr, p->ksV, st));
     const bool dev = is_device_ptr(f);
     float2 *dst = dev ? (float2 *)f : p->ioB;
-    CGS_TRY(launch_scatter_ks(p->ksV, p->perm, p->M, p->nc, dst, st));
+    CGS_TRY(op_forward(p, p->cF, 1, nullptr, p->ksV, st, dst));
     if (!dev) {
         CGS_CUDA(cudaMemcpyAsync(f, dst, sizeof(float2) * p->M * p->nc, cudaMemcpyDeviceToHost, st));
         CGS_CUDA(cudaStreamSynchronize(st));
@@ -1523,17 +1528,9 @@ cgs_status cgs_sense_trafo(cgs_plan *p, const float *x, float *y, void *stream)
     cudaStream_t st = pick_stream(p, stream);
     const void *src;
     CGS_TRY(stage_in(x, sizeof(float2) * p->Nt, p->ioA, &src, st));
-    CGS_TRY(op_forward(p, (const float2 *)src, 0, nullptr, p->ksV, st));
     const bool dev = is_device_ptr(y);
     float2 *dst = dev ? (float2 *)y : p->ioB;
-    if (p->F == 1) {
-        CGS_TRY(launch_scatter_ks(p->ksV, p->perm, p->M, p->nc, dst, st));
-    } else {
-        for (int f = 0; f < p->F; ++f) {
-            const int64_t off = f * p->Mf * p->nc;
-            CGS_TRY(launch_scatter_ks(p->ksV + off, p->fr[f]->perm, p->Mf, p->nc, dst + off, st));
-        }
-    }
+    CGS_TRY(op_forward(p, (const float2 *)src, 0, nullptr, p->ksV, st, dst));
     if (!dev) {
         CGS_CUDA(cudaMemcpyAsync(y, dst, sizeof(float2) * p->M * p->nc, cudaMemcpyDeviceToHost, st));
         CGS_CUDA(cudaStreamSynchronize(st));
