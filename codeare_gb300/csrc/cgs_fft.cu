@@ -221,7 +221,8 @@ axis_fft_kernel(const __grid_constant__ AxisPass p, int BO, int BI, int64_t nib)
                     if (p.load_mode == LOAD_PLAIN) {
                         v[u] = p.src[pix * p.inner + i];
                     } else {
-                        float2 x = p.img_per_coil ? p.img[pix * p.inner + i] : p.img[pix];
+                        float2 x = p.img_per_coil ? (p.coil_major ? p.img[i * p.coil_major + pix] : p.img[pix * p.inner + i])
+                                                  : p.img[pix];
                         if (p.sens) x = cmul(x, p.sens[pix * p.inner + i]);
                         float sc = dcol[b] * (p.deap_ax ? p.deap_ax[a] : 1.f);
                         if (p.mask) sc *= p.mask[pix];
@@ -282,7 +283,8 @@ axis_fft_kernel(const __grid_constant__ AxisPass p, int BO, int BI, int64_t nib)
         float2 v = src[pos * P + b];
         const int64_t pix = o * p.Lout + a;
         if (p.store_mode == STORE_DEAPOD) v = cscale(v, dcol[b] * (p.deap_ax ? p.deap_ax[a] : 1.f));
-        p.dst[pix * p.inner + i] = v;
+        if (p.coil_major && p.store_mode == STORE_DEAPOD) p.dst[i * p.coil_major + pix] = v;
+        else p.dst[pix * p.inner + i] = v;
     }
 }
 
@@ -413,7 +415,8 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
             if (p.load_mode == LOAD_PLAIN) {
                 v[u] = p.src[pix * p.inner + i];
             } else {
-                float2 x = p.img_per_coil ? p.img[pix * p.inner + i] : p.img[pix];
+                float2 x = p.img_per_coil ? (p.coil_major ? p.img[i * p.coil_major + pix] : p.img[pix * p.inner + i])
+                                          : p.img[pix];
                 if (p.sens) x = cmul(x, p.sens[pix * p.inner + i]);
                 float sc = dcol * (p.deap_ax ? p.deap_ax[a] : 1.f);
                 if (p.mask) sc *= p.mask[pix];
@@ -446,7 +449,8 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
         const int pos = out_axis_to_pos(a, p.Lout, N, p.out_centred);
         float2 v = buf[ct_slot<LOGB>(pos, b)];
         if (p.store_mode == STORE_DEAPOD) v = cscale(v, dcol * (p.deap_ax ? p.deap_ax[a] : 1.f));
-        p.dst[(o * p.Lout + a) * p.inner + i] = v;
+        if (p.coil_major && p.store_mode == STORE_DEAPOD) p.dst[i * p.coil_major + o * p.Lout + a] = v;
+        else p.dst[(o * p.Lout + a) * p.inner + i] = v;
     }
 }
 

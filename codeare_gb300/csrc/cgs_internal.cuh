@@ -101,6 +101,8 @@ struct AxisPass {
     int load_mode, store_mode;
     const float2 *img;     // LOAD_IMAGE: image [outer][Lin] (broadcast) or [outer][Lin][inner]
     int img_per_coil;
+    int64_t coil_major;    // nonzero: the per-coil images of a LOAD_IMAGE pass and the output of a
+                           // STORE_DEAPOD pass are coil-major, img / dst[i * coil_major + pix]
     const float2 *sens;    // [outer][Lin|Lout][inner] sensitivities (coil innermost), nullable
     const float *mask;     // [outer][Lin] real pixel mask (nullable)
     const float *scale;    // STORE_COMBINE: per-pixel real scale (intensity map), nullable

@@ -300,7 +300,8 @@ AxisPass base_pass(cgs_plan *p, int t)
 }
 
 // forward NFFT of all coils.  src_img: single image (expand with sens) when
-// per_coil == 0, else coil-minor per-coil images.  mask may be null.  With
+// per_coil == 0, coil-minor per-coil images when 1, coil-major (the caller's
+// layout) when 2.  mask may be null.  With
 // `user` the result goes to the caller's layout (coil-major, trajectory
 // order) instead of ks, by the interpolation itself where it can, else by a
 // scatter after it.
@@ -321,7 +322,8 @@ cgs_status op_forward(cgs_plan *p, const float2 *src_img, int per_coil, const fl
         for (int t = 0; t < d - 1; ++t) outer *= p->N[t];
         a.outer = outer; a.inner = nc; a.Lin = p->N[d - 1]; a.Lout = p->n[d - 1]; a.sign = -1; a.in_centred = 1;
         a.load_mode = LOAD_IMAGE;
-        a.img = src_img; a.img_per_coil = per_coil;
+        a.img = src_img; a.img_per_coil = per_coil ? 1 : 0;
+        a.coil_major = per_coil == 2 ? p->Nt : 0;
         a.sens = per_coil ? nullptr : p->sens;
         a.mask = mask;
         a.deap_ax = p->deap[d - 1];
@@ -352,12 +354,15 @@ cgs_status op_forward(cgs_plan *p, const float2 *src_img, int per_coil, const fl
     return CGS_OK;
 }
 
-// adjoint NFFT of all coils into coil-minor per-coil images (deapodised)
-cgs_status op_adjoint(cgs_plan *p, const float2 *ks, int weighted, float2 *out, cudaStream_t st)
+// adjoint NFFT of all coils into per-coil images (deapodised): coil-minor,
+// or coil-major (the caller's layout) with coil_major_out
+cgs_status op_adjoint(cgs_plan *p, const float2 *ks, int weighted, float2 *out, cudaStream_t st,
+                      bool coil_major_out = false)
 {
     if (p->F > 1) {
         for (int f = 0; f < p->F; ++f)
-            CGS_TRY(op_adjoint(p->fr[f], ks + f * p->Mf * p->nc, weighted, out + f * p->Ntf * p->nc, st));
+            CGS_TRY(op_adjoint(p->fr[f], ks + f * p->Mf * p->nc, weighted, out + f * p->Ntf * p->nc, st,
+                               coil_major_out));
         return CGS_OK;
     }
     const int d = p->d, nc = p->nc;
@@ -391,6 +396,7 @@ cgs_status op_adjoint(cgs_plan *p, const float2 *ks, int weighted, float2 *out, 
     c.outer = outer; c.inner = nc; c.Lin = p->n[d - 1]; c.Lout = p->N[d - 1]; c.sign = +1; c.out_centred = 1;
     c.src = p->t1; c.dst = out;
     c.store_mode = STORE_DEAPOD;
+    c.coil_major = coil_major_out ? p->Nt : 0;
     c.deap_ax = p->deap[d - 1];
     c.deap_o1 = p->deap[d - 2]; c.o1_len = p->N[d - 2];
     c.deap_o0 = (d == 3) ? p->deap[0] : nullptr;
@@ -1440,10 +1446,9 @@ cgs_status cgs_nfft_trafo(cgs_plan *p, const float *fhat, float *f, void *stream
     }
     const void *src;
     CGS_TRY(stage_in(fhat, sizeof(float2) * p->Nt * p->nc, p->ioA, &src, st));
-    CGS_TRY(launch_to_coil_minor((const float2 *)src, p->Nt, p->nc, p->cF, st));
     const bool dev = is_device_ptr(f);
     float2 *dst = dev ? (float2 *)f : p->ioB;
-    CGS_TRY(op_forward(p, p->cF, 1, nullptr, p->ksV, st, dst));
+    CGS_TRY(op_forward(p, (const float2 *)src, 2, nullptr, p->ksV, st, dst));
     if (!dev) {
         CGS_CUDA(cudaMemcpyAsync(f, dst, sizeof(float2) * p->M * p->nc, cudaMemcpyDeviceToHost, st));
         CGS_CUDA(cudaStreamSynchronize(st));
@@ -1501,8 +1506,15 @@ cgs_status cgs_nfft_adjoint(cgs_plan *p, const float *f, float *fhat, void *stre
         return CGS_OK;
     }
     CGS_TRY(ks_in(p, f, st));
-    CGS_TRY(op_adjoint(p, p->ksY, 0, p->cF, st));
-    return coil_images_out(p, p->cF, fhat, st);
+    // the last FFT pass stores straight into the caller's coil-major layout
+    const bool dev = is_device_ptr(fhat);
+    float2 *dst = dev ? (float2 *)fhat : p->ioB;
+    CGS_TRY(op_adjoint(p, p->ksY, 0, dst, st, true));
+    if (!dev) {
+        CGS_CUDA(cudaMemcpyAsync(fhat, dst, sizeof(float2) * p->Nt * p->nc, cudaMemcpyDeviceToHost, st));
+        CGS_CUDA(cudaStreamSynchronize(st));
+    }
+    return CGS_OK;
 }
 
 cgs_status cgs_nfft_itrafo(cgs_plan *p, const float *f, float *fhat, int maxit, double eps, void *stream)
