@@ -488,15 +488,16 @@ __host__ __device__ constexpr int spread_mma_row(int nt)
     return r;
 }
 
-template <int NT> struct SpreadMma {
+template <int NT, int MT = 1> struct SpreadMma {
     static constexpr int R = spread_mma_row(NT);
+    static constexpr int WPE = 4 * MT + 4;                 // patch weights per entry: 4 MT rows, 4 columns
     // one staging buffer: values, window taps, footprint starts, density weights
     __host__ __device__ static size_t buf_bytes(int taps)
     {
         return (size_t)kSpreadBatch * (R * sizeof(float) + 2 * taps * sizeof(float) + sizeof(int2) + sizeof(float));
     }
-    // per warp: two buffers and the batch's patch weights (8 entries x 4 rows + 4 columns)
-    __host__ __device__ static size_t warp_bytes(int taps) { return 2 * buf_bytes(taps) + kSpreadBatch * 8 * sizeof(float); }
+    // per warp: two buffers and the batch's patch weights
+    __host__ __device__ static size_t warp_bytes(int taps) { return 2 * buf_bytes(taps) + kSpreadBatch * WPE * sizeof(float); }
 };
 
 // TF32 split: hi rounded to nearest, lo = x - hi passed as is (the tensor
@@ -515,13 +516,15 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-template <int NT, int TAPS = 0>
-__global__ void __launch_bounds__(256, 3)
+// MT m-tiles: a (4 MT) x 4 patch, each m-tile four patch rows
+template <int NT, int TAPS = 0, int MT = 1>
+__global__ void __launch_bounds__(256, MT == 1 ? 3 : 2)
 spread_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
                   const float2 *__restrict__ ks, const float *__restrict__ dens, int weighted,
                   float2 *__restrict__ grid)
 {
-    using S = SpreadMma<NT>;
+    using S = SpreadMma<NT, MT>;
+    constexpr int WPE = S::WPE;
     constexpr int R = S::R, CC = 4 * NT, CH = 2 * NT;     // coils per warp; 16-byte chunks per entry row
     extern __shared__ float4 smem4[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -531,14 +534,14 @@ spread_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ Pa
     const int WS = 2 * taps;
     const size_t bb = S::buf_bytes(taps);                  // a multiple of 16 bytes
     char *wbase = reinterpret_cast<char *>(smem4) + (size_t)warp * S::warp_bytes(taps);
-    float *swt = reinterpret_cast<float *>(wbase + 2 * bb);   // [entry][wy 0..3, wx 0..3]
+    float *swt = reinterpret_cast<float *>(wbase + 2 * bb);   // [entry][wy 0..4MT-1, wx 0..3]
     const int c0 = blockIdx.y * CC;
     const int ccn = min(CC, g.nc - c0);
     const bool v16 = ((g.nc & 1) == 0);
     const int4 wk = ps.work[wi];
     const int n0 = g.n[0], n1 = g.n[1];
     const int gq = lane >> 2, tq = lane & 3;
-    const int py0 = (wk.x / ps.npx) * 4, px0 = (wk.x % ps.npx) * 4;
+    const int py0 = (wk.x / ps.npx) * (4 * MT), px0 = (wk.x % ps.npx) * 4;
     const bool wide = (n0 >= taps) && (n1 >= taps);
     // zero both buffers once: padding columns and rows past a short batch stay finite
     {
@@ -598,9 +601,11 @@ spread_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ Pa
         return w;
     };
 
-    float acc[NT][4];
+    float acc[MT][NT][4];
 #pragma unroll
-    for (int t = 0; t < NT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+    for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+        for (int t = 0; t < NT; ++t) acc[mt][t][0] = acc[mt][t][1] = acc[mt][t][2] = acc[mt][t][3] = 0.f;
     const int end = wk.y + wk.z;
     int e0 = wk.y, cnt = min(kSpreadBatch, end - e0), buf = 0;
     issue(e0, cnt, 0);
@@ -612,57 +617,67 @@ spread_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ Pa
         __syncwarp();
         float *sv, *sw, *sd; int2 *su;
         buffers(buf, sv, sw, su, sd);
-        // the batch's patch weights: lane = (entry e, row/column r); zero past cnt
-        {
-            const int e = lane >> 2, r = lane & 3;
-            float wy = 0.f, wx = 0.f;
+        // the batch's patch weights: (entry e, row or column r) per lane; zero past cnt
+#pragma unroll
+        for (int idx = lane; idx < kSpreadBatch * WPE; idx += 32) {
+            const int e = idx / WPE, r = idx % WPE;
+            float w = 0.f;
             if (e < cnt) {
                 const int2 u = su[e];
                 const float *W = sw + e * WS;
-                if (py0 + r < n0) wy = wgt(W, py0 + r - u.x, n0);
-                if (px0 + r < n1) wx = wgt(W + taps, px0 + r - u.y, n1) * sd[e];
+                if (r < 4 * MT) {
+                    if (py0 + r < n0) w = wgt(W, py0 + r - u.x, n0);
+                } else if (px0 + r - 4 * MT < n1) {
+                    w = wgt(W + taps, px0 + r - 4 * MT - u.y, n1) * sd[e];
+                }
             }
-            swt[e * 8 + r] = wy;
-            swt[e * 8 + 4 + r] = wx;
+            swt[idx] = w;
         }
         __syncwarp();
-        // A: entries tq and tq + 4 at patch rows gq / 4 and gq / 4 + 2, column gq % 4
-        uint32_t ah[4], al[4];
+        // A of m-tile mt: entries tq and tq + 4 at patch rows 4 mt + gq / 4 (+ 2), column gq % 4
+        uint32_t ah[MT][4], al[MT][4];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const float *wr = swt + (tq + 4 * h) * 8;
-            const float wx = wr[4 + (gq & 3)];
-            tf32_split(wr[gq >> 2] * wx, ah[2 * h], al[2 * h]);
-            tf32_split(wr[(gq >> 2) + 2] * wx, ah[2 * h + 1], al[2 * h + 1]);
-        }
+        for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const float *wr = swt + (tq + 4 * h) * WPE;
+                const float wx = wr[4 * MT + (gq & 3)];
+                tf32_split(wr[4 * mt + (gq >> 2)] * wx, ah[mt][2 * h], al[mt][2 * h]);
+                tf32_split(wr[4 * mt + (gq >> 2) + 2] * wx, ah[mt][2 * h + 1], al[mt][2 * h + 1]);
+            }
         const float *r0 = sv + tq * R + gq, *r1 = sv + (tq + 4) * R + gq;
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
             uint32_t bh0, bl0, bh1, bl1;
             tf32_split(r0[8 * t], bh0, bl0);
             tf32_split(r1[8 * t], bh1, bl1);
-            mma_tf32(acc[t], al, bh0, bh1);
-            mma_tf32(acc[t], ah, bl0, bl1);
-            mma_tf32(acc[t], ah, bh0, bh1);
+#pragma unroll
+            for (int mt = 0; mt < MT; ++mt) {
+                mma_tf32(acc[mt][t], al[mt], bh0, bh1);
+                mma_tf32(acc[mt][t], ah[mt], bl0, bl1);
+                mma_tf32(acc[mt][t], ah[mt], bh0, bh1);
+            }
         }
         __syncwarp();
         if (cnt1 <= 0) break;
         e0 = e1; cnt = cnt1; buf ^= 1;
     }
-    const int py = py0 + (gq >> 2), px = px0 + (gq & 3);
+    const int px = px0 + (gq & 3);
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int yy = py + 2 * h;
-        if (yy >= n0 || px >= n1) continue;
-        const int ppt = gq + 8 * h;                         // point index within the patch
-        float2 *dst = (wk.w < 0) ? grid + ((size_t)yy * n1 + px) * g.nc + c0
-                                 : ps.partial + ((size_t)wk.w * 16 + ppt) * g.nc + c0;
+    for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
-        for (int t = 0; t < NT; ++t) {
-            const int c = 4 * t + tq;
-            if (c < ccn) dst[c] = make_float2(acc[t][2 * h], acc[t][2 * h + 1]);
+        for (int h = 0; h < 2; ++h) {
+            const int yy = py0 + 4 * mt + (gq >> 2) + 2 * h;
+            if (yy >= n0 || px >= n1) continue;
+            const int ppt = 16 * mt + gq + 8 * h;           // point index within the patch (row-major, 4 wide)
+            float2 *dst = (wk.w < 0) ? grid + ((size_t)yy * n1 + px) * g.nc + c0
+                                     : ps.partial + ((size_t)wk.w * 16 * MT + ppt) * g.nc + c0;
+#pragma unroll
+            for (int t = 0; t < NT; ++t) {
+                const int c = 4 * t + tq;
+                if (c < ccn) dst[c] = make_float2(acc[mt][t][2 * h], acc[mt][t][2 * h + 1]);
+            }
         }
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1435,17 +1450,25 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
         if (taps == 10) CGS_SPT(4, 4, CPLV, 1, 1, 10);          \
         else CGS_SP(4, 4, CPLV, 1, 1);                          \
     } while (0)
-    if (ps.ph != 4 || (ps.pw != 4 && ps.pw != 8)) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
-    if (ps.blk == 16) {  // tensor cores: 4 NT coils per warp, 4 x 4 patches
-        if (ps.pw != 4) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
+    if ((ps.ph != 4 && !(ps.ph == 8 && ps.blk == 32)) || (ps.pw != 4 && ps.pw != 8)) {
+        set_error("unsupported spreading patch");
+        return CGS_ERR_BAD_ARG;
+    }
+    if (ps.blk == 16 || ps.blk == 32) {  // tensor cores: 4 NT coils per warp, 4 x 4 or 8 x 4 patches
+        if (ps.pw != 4 || ps.ph != (ps.blk == 32 ? 8 : 4)) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
         const int nt = std::min(8, (2 * g.nc + 7) / 8);
         dim3 grm((ps.nwork + 7) / 8, (g.nc + 4 * nt - 1) / (4 * nt));
-#define CGS_SPM(NTV, TV)                                                                                 \
+#define CGS_SPMM(NTV, TV, MTV)                                                                           \
     do {                                                                                                 \
-        const size_t sm = 8 * SpreadMma<NTV>::warp_bytes(taps);                                          \
-        CGS_CUDA(cudaFuncSetAttribute(spread_mma_kernel<NTV, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                      (int)sm));                                                         \
-        spread_mma_kernel<NTV, TV><<<grm, 256, sm, st>>>(g, ps, ks, dens, weighted, grid);               \
+        const size_t sm = 8 * SpreadMma<NTV, MTV>::warp_bytes(taps);                                     \
+        CGS_CUDA(cudaFuncSetAttribute(spread_mma_kernel<NTV, TV, MTV>,                                   \
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));            \
+        spread_mma_kernel<NTV, TV, MTV><<<grm, 256, sm, st>>>(g, ps, ks, dens, weighted, grid);          \
+    } while (0)
+#define CGS_SPM(NTV, TV)                                  \
+    do {                                                  \
+        if (ps.blk == 32) CGS_SPMM(NTV, TV, 2);           \
+        else CGS_SPMM(NTV, TV, 1);                        \
     } while (0)
 #define CGS_SPM1(NTV)                                     \
     do {                                                  \
@@ -1464,6 +1487,7 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
         }
 #undef CGS_SPM1
 #undef CGS_SPM
+#undef CGS_SPMM
     } else if (ps.pw == 8 && ps.blk == 1) {
         CGS_SP(4, 8, 1, 1, 1);
     } else if (ps.blk == 8) {

@@ -532,8 +532,10 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     // spread_block 16: 4 x 4 patches on the tensor cores (TF32 split, FP32
     // accumulation), the default from 4 coils up
     const int tb = p->tune.spread_block != 0 ? p->tune.spread_block : (p->nc >= 4 ? 16 : 1);
-    const int blk = tb == 16 ? 16 : (p->nc == 1 ? 1 : ((tb == 8 || (p->nc >= 4 && (tb == 4 || tb == 2))) ? tb : 1));
-    const int kPatchH = 4, kPatchW = (blk != 16 && (p->nc == 1 || blk == 4 || blk == 8)) ? 8 : 4;
+    // spread_block 32: 8 x 4 patches on the tensor cores (two m-tiles per warp)
+    const int blk = (tb == 16 || tb == 32) ? tb : (p->nc == 1 ? 1 : ((tb == 8 || (p->nc >= 4 && (tb == 4 || tb == 2))) ? tb : 1));
+    const bool tensor = (blk == 16 || blk == 32);
+    const int kPatchH = blk == 32 ? 8 : 4, kPatchW = (!tensor && (p->nc == 1 || blk == 4 || blk == 8)) ? 8 : 4;
     const int npy = (n0 + kPatchH - 1) / kPatchH, npx = (n1 + kPatchW - 1) / kPatchW;
     const int64_t P = (int64_t)npy * npx, M = p->M;
     std::vector<int> perm(M);
@@ -1747,7 +1749,7 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
         return false;
     };
     if (!in(t->tile, {0, 8, 16, 32}) || !in(t->interp_coils, {0, 1, 4, 8, 16, 32}) ||
-        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 2, 4, 8, 16}) || !in(t->interp_block, {0, 1, 16}) ||
+        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 2, 4, 8, 16, 32}) || !in(t->interp_block, {0, 1, 16}) ||
         (t->work_slice != 0 && (t->work_slice < 32 || t->work_slice > 65536)) ||
         (t->spread_chunk != 0 && (t->spread_chunk < 32 || t->spread_chunk > 65536))) {
         set_error("tuning value out of range");

@@ -209,11 +209,13 @@ def test_batch_parity_with_oracle(gpu, oracle):
         p.close()
 
 
+@pytest.mark.parametrize("blk", [16, 32])
 @pytest.mark.parametrize("nc", [1, 3, 12, 20, 40])
-def test_tensor_core_spreading_matches_cuda_cores(gpu, nc):
-    """spread_block 16 (mma.m16n8k8, TF32-split operands) against the CUDA-core
-    spreading for coil counts that leave partial n-tiles and coil chunks, on a
-    grid whose side is not a multiple of the patch (N = 50, n = 100)."""
+def test_tensor_core_spreading_matches_cuda_cores(gpu, nc, blk):
+    """spread_block 16 and 32 (4 x 4 and 8 x 4 patches, mma.m16n8k8 with
+    TF32-split operands) against the CUDA-core spreading for coil counts that
+    leave partial n-tiles and coil chunks, on a grid whose side is not a
+    multiple of the patch (N = 50, n = 100)."""
     from codeare_gb300 import synth
     N = 50
     k = synth.radial2d(40, 100, golden=True)
@@ -223,7 +225,7 @@ def test_tensor_core_spreading_matches_cuda_cores(gpu, nc):
     ref = np.zeros((nc, N, N), np.complex64)
     p.set_tuning(spread_block=1)
     p.nfft_adjoint(f, ref)
-    p.set_tuning(spread_block=16)
+    p.set_tuning(spread_block=blk)
     out = np.zeros_like(ref)
     p.nfft_adjoint(f, out)
     assert rel(out, ref) < 2e-6
