@@ -331,6 +331,120 @@ __host__ __device__ constexpr int ct_rows()
     return LOGB <= 3 ? N + (N + 7) / 8 : N;
 }
 
+// Butterfly with the transform direction fixed at compile time (S = -1
+// forward, +1 inverse): no selects between the two directions' constants.
+template <int R, int S>
+__device__ __forceinline__ void ct_bfly(float2 *v, const float2 *tw, int nR)
+{
+    if constexpr (R == 2) {
+        float2 a = v[0], b = v[1];
+        v[0] = cadd(a, b); v[1] = csub(a, b);
+    } else if constexpr (R == 4) {
+        float2 a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+        float2 b0 = cadd(v[1], v[3]), d = csub(v[1], v[3]);
+        float2 b1 = S < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);   // S i d
+        v[0] = cadd(a0, b0); v[2] = csub(a0, b0);
+        v[1] = cadd(a1, b1); v[3] = csub(a1, b1);
+    } else if constexpr (R == 8) {
+        float2 e[4] = {v[0], v[2], v[4], v[6]};
+        float2 o[4] = {v[1], v[3], v[5], v[7]};
+        ct_bfly<4, S>(e, tw, nR);
+        ct_bfly<4, S>(o, tw, nR);
+        const float h = 0.70710678118654752f;
+        float2 o1 = o[1], o2 = o[2], o3 = o[3];
+        if constexpr (S < 0) {   // w8 = (1 - i)/sqrt2
+            o1 = make_float2(h * (o1.x + o1.y), h * (o1.y - o1.x));
+            o2 = make_float2(o2.y, -o2.x);
+            o3 = make_float2(h * (-o3.x + o3.y), h * (-o3.y - o3.x));
+        } else {                 // w8 = (1 + i)/sqrt2
+            o1 = make_float2(h * (o1.x - o1.y), h * (o1.y + o1.x));
+            o2 = make_float2(-o2.y, o2.x);
+            o3 = make_float2(h * (-o3.x - o3.y), h * (-o3.y + o3.x));
+        }
+        v[0] = cadd(e[0], o[0]); v[4] = csub(e[0], o[0]);
+        v[1] = cadd(e[1], o1);   v[5] = csub(e[1], o1);
+        v[2] = cadd(e[2], o2);   v[6] = csub(e[2], o2);
+        v[3] = cadd(e[3], o3);   v[7] = csub(e[3], o3);
+    } else {
+        bfly<R>(v, S, tw, nR);
+    }
+}
+
+// Slot of rows row0 + r * D (r = 0..R-1) as slot(row0) + r * stride when the
+// padding (a spare row after every 8, ct_slot) shifts them uniformly: D a
+// multiple of 8, or D = 1 with row0 a multiple of 8 and R <= 8.  0: no
+// uniform stride (the caller computes each slot).
+template <int LOGB, int D, int R>
+__host__ __device__ constexpr int ct_stride(bool row0_mult8)
+{
+    if constexpr (LOGB > 3) return D << LOGB;
+    else if constexpr (D % 8 == 0) return (D + D / 8) << LOGB;
+    else return (D == 1 && R <= 8 && row0_mult8) ? (1 << LOGB) : 0;
+}
+
+template <int N, int LOGB, int R, int NS, int S>
+__device__ __forceinline__ void ct_pass_s(float2 *buf, const float2 *tw)
+{
+    constexpr int B = 1 << LOGB;
+    constexpr int NR = N / R;
+    constexpr int TB = B * NR;
+    constexpr int NBF = (TB + kThreads - 1) / kThreads;
+    constexpr int STEP = N / (NS * R);
+    constexpr int SL = ct_stride<LOGB, NR, R>(false);         // load rows j + r NR
+    constexpr int SS = ct_stride<LOGB, NS, R>(NS == 1 && R == 8);  // store rows base + r NS (base = 8 j when NS = 1)
+    float2 v[NBF][R];
+#pragma unroll
+    for (int t = 0; t < NBF; ++t) {
+        const int q = threadIdx.x + t * kThreads;
+        if (TB % kThreads != 0 && q >= TB) continue;
+        const int b = q & (B - 1), j = q >> LOGB, k = j % NS;
+        if constexpr (SL > 0) {
+            const float2 *src = buf + ct_slot<LOGB>(j, b);
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[t][r] = src[r * SL];
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[t][r] = buf[ct_slot<LOGB>(j + r * NR, b)];
+        }
+        if constexpr (NS > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                float2 w = tw[k * r * STEP];
+                if constexpr (S > 0) w.y = -w.y;
+                v[t][r] = cmul(v[t][r], w);
+            }
+        }
+        ct_bfly<R, S>(v[t], tw, NR);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < NBF; ++t) {
+        const int q = threadIdx.x + t * kThreads;
+        if (TB % kThreads != 0 && q >= TB) continue;
+        const int b = q & (B - 1), j = q >> LOGB, k = j % NS;
+        const int base = (j / NS) * NS * R + k;
+        if constexpr (SS > 0) {
+            float2 *dst = buf + ct_slot<LOGB>(base, b);
+#pragma unroll
+            for (int r = 0; r < R; ++r) dst[r * SS] = v[t][r];
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) buf[ct_slot<LOGB>(base + r * NS, b)] = v[t][r];
+        }
+    }
+    __syncthreads();
+}
+
+template <int N, int LOGB, int NS, int S>
+__device__ __forceinline__ void ct_passes_s(float2 *buf, const float2 *tw)
+{
+    if constexpr (NS < N) {
+        constexpr int R = ct_next_radix(N / NS);
+        ct_pass_s<N, LOGB, R, NS, S>(buf, tw);
+        ct_passes_s<N, LOGB, NS * R, S>(buf, tw);
+    }
+}
+
 template <int N, int LOGB, int R, int NS>
 __device__ __forceinline__ void ct_pass(float2 *buf, const float2 *tw, int sign)
 {
@@ -380,7 +494,7 @@ __device__ __forceinline__ void ct_passes(float2 *buf, const float2 *tw, int sig
     }
 }
 
-template <int N, int LOGB>
+template <int N, int LOGB, int S>
 __global__ void __launch_bounds__(kThreads, ((N & (N - 1)) == 0) ? 4 : 3)
 axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
 {
@@ -427,7 +541,7 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
         for (int u = 0; u < EPT; ++u) buf[ct_slot<LOGB>(r0 + u * RSTEP, b)] = v[u];
     }
     __syncthreads();
-    ct_passes<N, LOGB, 1>(buf, tw, p.sign);
+    ct_passes_s<N, LOGB, 1, S>(buf, tw);
     if (p.toep_k) {
         // pointwise multiply by the real Toeplitz kernel, then transform back
         const int64_t kstride = p.inner / p.toep_nc;
@@ -439,7 +553,7 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
             }
         }
         __syncthreads();
-        ct_passes<N, LOGB, 1>(buf, tw, +1);
+        ct_passes_s<N, LOGB, 1, +1>(buf, tw);
     }
     if (!col_ok) return;
 #pragma unroll
@@ -470,11 +584,14 @@ cgs_status launch_ct(const AxisPass &p, cudaStream_t st)
     const size_t smem = ((size_t)N + (size_t)ct_rows<N, LOGB>() * B) * sizeof(float2);
     static bool attr_set = false;
     if (!attr_set) {
-        CGS_CUDA(cudaFuncSetAttribute(axis_fft_ct_kernel<N, LOGB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CGS_CUDA(cudaFuncSetAttribute(axis_fft_ct_kernel<N, LOGB, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        CGS_CUDA(cudaFuncSetAttribute(axis_fft_ct_kernel<N, LOGB, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
         attr_set = true;
     }
-    axis_fft_ct_kernel<N, LOGB><<<(unsigned)nblocks, kThreads, smem, st>>>(p, logBI, nib);
+    if (p.sign < 0) axis_fft_ct_kernel<N, LOGB, -1><<<(unsigned)nblocks, kThreads, smem, st>>>(p, logBI, nib);
+    else axis_fft_ct_kernel<N, LOGB, +1><<<(unsigned)nblocks, kThreads, smem, st>>>(p, logBI, nib);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }
