@@ -54,7 +54,7 @@ class SolveReport(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("tile", C.c_int), ("work_slice", C.c_int), ("spread_chunk", C.c_int),
                 ("interp_coils", C.c_int), ("spread_coils", C.c_int), ("spread_block", C.c_int),
-                ("interp_block", C.c_int)]
+                ("interp_block", C.c_int), ("host_chunks", C.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

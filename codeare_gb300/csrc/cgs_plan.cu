@@ -158,6 +158,19 @@ struct cgs_plan {
     int F = 1;
     int64_t Mf = 0, Ntf = 0;
     std::vector<cgs_plan *> fr;
+    // host-buffer pipeline of the per-coil NFFT (one frame): child plans, each
+    // holding a contiguous range of the caller's coil-major coils and sharing
+    // this plan's node tables, so that one chunk's host copies overlap the
+    // other chunks' kernels.  Copies to the device run in order on hc_in,
+    // copies to the host on hc_out, each chunk's kernels on its child's
+    // stream.  Built on the first host-buffer call, dropped whenever the
+    // trajectory, the weights or the tuning change.
+    std::vector<cgs_plan *> hc;
+    std::vector<int> hc_c0;      // first coil of each chunk (hc.size() + 1 entries)
+    cudaStream_t hc_in = nullptr, hc_out = nullptr;
+    cudaEvent_t hc_fork = nullptr, hc_done = nullptr;
+    std::vector<cudaEvent_t> hc_copied, hc_computed;
+    bool shared_nodes = false;   // a coil chunk: the node tables belong to its parent
     double alpha = 1.0;
     int64_t M = 0, Nt = 1, ntot = 1;
     int device = 0;
@@ -182,6 +195,7 @@ struct cgs_plan {
     int *pentries = nullptr;
     int4 *pwork = nullptr, *pmulti = nullptr;
     float2 *ppartial = nullptr;
+    int pslots = 1;  // partial slots of the split patches (at least 1)
     PatchSet pset{};
     // 2-D tensor-core interpolation: node lists by 4 x 4 footprint-start bin
     int *ilist = nullptr;
@@ -305,15 +319,9 @@ AxisPass base_pass(cgs_plan *p, int t)
 // `user` the result goes to the caller's layout (coil-major, trajectory
 // order) instead of ks, by the interpolation itself where it can, else by a
 // scatter after it.
-cgs_status op_forward(cgs_plan *p, const float2 *src_img, int per_coil, const float *mask, float2 *ks,
-                      cudaStream_t st, float2 *user = nullptr)
+// the FFT passes of the forward NFFT (one frame): images -> oversampled grid
+cgs_status op_forward_grid(cgs_plan *p, const float2 *src_img, int per_coil, const float *mask, cudaStream_t st)
 {
-    if (p->F > 1) {
-        for (int f = 0; f < p->F; ++f)
-            CGS_TRY(op_forward(p->fr[f], src_img + (per_coil ? f * p->Ntf * p->nc : f * p->Ntf), per_coil, mask,
-                               ks + f * p->Mf * p->nc, st, user ? user + f * p->Mf * p->nc : nullptr));
-        return CGS_OK;
-    }
     const int d = p->d, nc = p->nc;
     // pass over the fastest image axis (t = d-1), from the image side
     {
@@ -347,34 +355,40 @@ cgs_status op_forward(cgs_plan *p, const float2 *src_img, int per_coil, const fl
         b.src = p->t2; b.dst = p->grid;
         CGS_TRY(launch_axis_pass(b, st));
     }
+    return CGS_OK;
+}
+
+// the interpolation of the forward NFFT: p's nodes from `grid` (any plan's
+// grid of p's geometry) into ks, or into the caller's layout with `user`
+cgs_status op_forward_interp(cgs_plan *p, const float2 *grid, float2 *ks, cudaStream_t st, float2 *user)
+{
     NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork, p->niwork, p->ibx};
     bool direct = false;
-    CGS_TRY(launch_interp(p->geom, ns, p->grid, ks, st, user, &direct));
+    CGS_TRY(launch_interp(p->geom, ns, grid, ks, st, user, &direct));
     if (user && !direct) CGS_TRY(launch_scatter_ks(ks, p->perm, p->M, p->nc, user, st));
     return CGS_OK;
 }
 
-// adjoint NFFT of all coils into per-coil images (deapodised): coil-minor,
-// or coil-major (the caller's layout) with coil_major_out
-cgs_status op_adjoint(cgs_plan *p, const float2 *ks, int weighted, float2 *out, cudaStream_t st,
-                      bool coil_major_out = false)
+cgs_status op_forward(cgs_plan *p, const float2 *src_img, int per_coil, const float *mask, float2 *ks,
+                      cudaStream_t st, float2 *user = nullptr)
 {
     if (p->F > 1) {
         for (int f = 0; f < p->F; ++f)
-            CGS_TRY(op_adjoint(p->fr[f], ks + f * p->Mf * p->nc, weighted, out + f * p->Ntf * p->nc, st,
-                               coil_major_out));
+            CGS_TRY(op_forward(p->fr[f], src_img + (per_coil ? f * p->Ntf * p->nc : f * p->Ntf), per_coil, mask,
+                               ks + f * p->Mf * p->nc, st, user ? user + f * p->Mf * p->nc : nullptr));
         return CGS_OK;
     }
+    CGS_TRY(op_forward_grid(p, src_img, per_coil, mask, st));
+    return op_forward_interp(p, p->grid, ks, st, user);
+}
+
+// the FFT passes of the adjoint NFFT (one frame): p's grid -> per-coil
+// images (deapodised), coil-minor or, with coil_major_out, coil-major
+cgs_status op_adjoint_fft(cgs_plan *p, float2 *out, cudaStream_t st, bool coil_major_out)
+{
     const int d = p->d, nc = p->nc;
-    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork, p->niwork, p->ibx};
-    if (d == 2) {
-        // writes every grid point: no clearing pass
-        CGS_TRY(launch_spread_patch(p->geom, p->pset, ks, p->w, weighted && p->w != nullptr, p->grid, st));
-    } else {
-        CGS_TRY(launch_zero(p->grid, sizeof(float2) * (size_t)p->ntot * nc, st));
-        CGS_TRY(launch_spread(p->geom, ns, ks, weighted && p->w != nullptr, p->grid, st));
-    }
     const float2 *cur = p->grid;
+
     if (d == 3) {
         AxisPass a = base_pass(p, 0);
         a.outer = 1; a.inner = (int64_t)p->n[1] * p->n[2] * nc; a.Lin = p->n[0]; a.Lout = p->N[0]; a.sign = +1; a.out_centred = 1;
@@ -401,6 +415,29 @@ cgs_status op_adjoint(cgs_plan *p, const float2 *ks, int weighted, float2 *out, 
     c.deap_o1 = p->deap[d - 2]; c.o1_len = p->N[d - 2];
     c.deap_o0 = (d == 3) ? p->deap[0] : nullptr;
     return launch_axis_pass(c, st);
+}
+
+// adjoint NFFT of all coils into per-coil images (deapodised): coil-minor,
+// or coil-major (the caller's layout) with coil_major_out
+cgs_status op_adjoint(cgs_plan *p, const float2 *ks, int weighted, float2 *out, cudaStream_t st,
+                      bool coil_major_out = false)
+{
+    if (p->F > 1) {
+        for (int f = 0; f < p->F; ++f)
+            CGS_TRY(op_adjoint(p->fr[f], ks + f * p->Mf * p->nc, weighted, out + f * p->Ntf * p->nc, st,
+                               coil_major_out));
+        return CGS_OK;
+    }
+    const int d = p->d, nc = p->nc;
+    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork, p->niwork, p->ibx};
+    if (d == 2) {
+        // writes every grid point: no clearing pass
+        CGS_TRY(launch_spread_patch(p->geom, p->pset, ks, p->w, weighted && p->w != nullptr, p->grid, st));
+    } else {
+        CGS_TRY(launch_zero(p->grid, sizeof(float2) * (size_t)p->ntot * nc, st));
+        CGS_TRY(launch_spread(p->geom, ns, ks, weighted && p->w != nullptr, p->grid, st));
+    }
+    return op_adjoint_fft(p, out, st, coil_major_out);
 }
 
 // CGNR inverse NFFT per coil (codeare's NFFT::Adjoint) on sorted k-space ksIn
@@ -602,7 +639,8 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     CGS_TRY(dev_alloc(&p->pentries, entries.size()));
     CGS_TRY(dev_alloc(&p->pwork, work.size()));
     CGS_TRY(dev_alloc(&p->pmulti, std::max<size_t>(1, multi.size())));
-    CGS_TRY(dev_alloc(&p->ppartial, (size_t)std::max(slots, 1) * kPatchH * kPatchW * p->nc));
+    p->pslots = std::max(slots, 1);
+    CGS_TRY(dev_alloc(&p->ppartial, (size_t)p->pslots * kPatchH * kPatchW * p->nc));
     CGS_CUDA(cudaMemcpy(p->pentries, entries.data(), sizeof(int) * entries.size(), cudaMemcpyHostToDevice));
     CGS_CUDA(cudaMemcpy(p->pwork, work.data(), sizeof(int4) * work.size(), cudaMemcpyHostToDevice));
     if (!multi.empty())
@@ -1137,6 +1175,7 @@ cgs_status cgs_plan_create(cgs_plan **out, const cgs_plan_desc *desc)
         *out = p;
         return CGS_OK;
     }
+
     if (desc->rank != 2 && desc->rank != 3) { set_error("rank must be 2 or 3"); return CGS_ERR_BAD_ARG; }
     if (desc->ncoils < 1 || desc->M < 1 || desc->m < 0 || desc->m > 8 || !(desc->alpha >= 1.0)) {
         set_error("bad ncoils / M / m / alpha");
@@ -1248,12 +1287,116 @@ cgs_status cgs_plan_create(cgs_plan **out, const cgs_plan_desc *desc)
     return CGS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Coil chunks of the host-buffer per-coil NFFT
+// ---------------------------------------------------------------------------
+static void drop_host_chunks(cgs_plan *p)
+{
+    if (p->hc_in) cudaStreamSynchronize(p->hc_in);
+    if (p->hc_out) cudaStreamSynchronize(p->hc_out);
+    for (cgs_plan *c : p->hc) cgs_plan_destroy(c);
+    p->hc.clear();
+    p->hc_c0.clear();
+    for (cudaEvent_t e : p->hc_copied) cudaEventDestroy(e);
+    for (cudaEvent_t e : p->hc_computed) cudaEventDestroy(e);
+    p->hc_copied.clear();
+    p->hc_computed.clear();
+    for (cudaEvent_t *e : {&p->hc_fork, &p->hc_done})
+        if (*e) { cudaEventDestroy(*e); *e = nullptr; }
+    for (cudaStream_t *s : {&p->hc_in, &p->hc_out})
+        if (*s) { cudaStreamDestroy(*s); *s = nullptr; }
+}
+
+// chunks of a host-buffer call (one frame): the tuning's host_chunks, else 2
+// once the caller's k-space reaches 8 MiB (below that the copies are too
+// short to hide anything behind); at least 4 coils per chunk, so that every
+// chunk grids with the parent's patch shapes and node tables
+static int host_chunk_count(const cgs_plan *p)
+{
+    if (p->F > 1 || p->nc < 8) return 1;
+    int c = p->tune.host_chunks;
+    if (c == 0) c = (p->M * p->nc * (int64_t)sizeof(float2) >= (8 << 20)) ? 2 : 1;
+    return std::max(1, std::min(c, p->nc / 4));
+}
+
+// C child plans with the parent's geometry and decomposition (coil groups
+// left to their defaults), nc / C coils each (the first nc % C chunks one
+// more), reading the parent's node tables; each owns its grids, staging and
+// the partial sums of split spreading patches
+static cgs_status build_host_chunks(cgs_plan *p, int C)
+{
+    if ((int)p->hc.size() == C) return CGS_OK;
+    drop_host_chunks(p);
+    cgs_plan_desc one{};
+    one.rank = p->d;
+    for (int t = 0; t < 3; ++t) one.N[t] = p->N[t];
+    one.alpha = p->alpha;
+    one.m = p->m;
+    one.M = p->M;
+    one.frames = 1;
+    cgs_status st = CGS_OK;
+    p->hc_c0.push_back(0);
+    for (int q = 0; q < C && st == CGS_OK; ++q) {
+        one.ncoils = p->nc / C + (q < p->nc % C ? 1 : 0);
+        cgs_plan *c = nullptr;
+        st = cgs_plan_create(&c, &one);
+        if (st != CGS_OK) break;
+        p->hc.push_back(c);
+        p->hc_c0.push_back(p->hc_c0.back() + one.ncoils);
+        dev_free(c->nodes);
+        dev_free(c->perm);
+        dev_free(c->w);
+        c->shared_nodes = true;
+        c->nodes = p->nodes; c->perm = p->perm; c->w = p->w;
+        c->work = p->work; c->nwork = p->nwork;
+        c->nodeU = p->nodeU; c->nodeW = p->nodeW;
+        c->pentries = p->pentries; c->pwork = p->pwork; c->pmulti = p->pmulti;
+        c->ilist = p->ilist; c->iwork = p->iwork; c->niwork = p->niwork; c->ibx = p->ibx;
+        c->tune = p->tune;
+        c->tune.interp_coils = c->tune.spread_coils = 0;
+        c->tune.host_chunks = 1;
+        apply_tiles(c);
+        c->pset = p->pset;
+        c->pslots = p->pslots;
+        if (p->d == 2) {
+            st = dev_alloc(&c->ppartial, (size_t)p->pslots * p->pset.ph * p->pset.pw * c->nc);
+            c->pset.partial = c->ppartial;
+        }
+        c->have_k = p->have_k;
+        c->have_w = p->have_w;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        const bool ok0 = cudaEventCreateWithFlags(&e0, cudaEventDisableTiming) == cudaSuccess;
+        if (ok0) p->hc_copied.push_back(e0);
+        const bool ok1 = cudaEventCreateWithFlags(&e1, cudaEventDisableTiming) == cudaSuccess;
+        if (ok1) p->hc_computed.push_back(e1);
+        if (st == CGS_OK && (!ok0 || !ok1)) {
+            set_error("event creation failed");
+            st = CGS_ERR_CUDA;
+        }
+    }
+    if (st == CGS_OK && (cudaEventCreateWithFlags(&p->hc_fork, cudaEventDisableTiming) != cudaSuccess ||
+                         cudaEventCreateWithFlags(&p->hc_done, cudaEventDisableTiming) != cudaSuccess ||
+                         cudaStreamCreateWithFlags(&p->hc_in, cudaStreamNonBlocking) != cudaSuccess ||
+                         cudaStreamCreateWithFlags(&p->hc_out, cudaStreamNonBlocking) != cudaSuccess)) {
+        set_error("event or stream creation failed");
+        st = CGS_ERR_CUDA;
+    }
+    if (st != CGS_OK) drop_host_chunks(p);
+    return st;
+}
+
 cgs_status cgs_plan_destroy(cgs_plan *p)
 {
     if (!p) return CGS_OK;
     cudaSetDevice(p->device);
     if (p->stream) cudaStreamSynchronize(p->stream);
     for (cgs_plan *c : p->fr) cgs_plan_destroy(c);
+    drop_host_chunks(p);
+    if (p->shared_nodes) {  // the parent frees these
+        p->nodes = nullptr; p->perm = nullptr; p->w = nullptr; p->work = nullptr;
+        p->nodeU = nullptr; p->nodeW = nullptr; p->pentries = nullptr; p->pwork = nullptr; p->pmulti = nullptr;
+        p->ilist = nullptr; p->iwork = nullptr;
+    }
     void *bufs[] = {p->tw[0], p->tw[1], p->tw[2], p->deap[0], p->deap[1], p->deap[2], p->nodes, p->perm,
                     p->w, p->work, p->nodeU, p->nodeW, p->pentries, p->pwork, p->pmulti, p->ppartial, p->ilist, p->iwork, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
                     p->cF, p->cP, p->cZ, p->vX, p->vR, p->vP, p->vQ, p->ioA, p->ioB, p->partial, p->dots,
@@ -1306,6 +1449,7 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
     }
     p->toep_valid = false;
     drop_graphs(p);
+    drop_host_chunks(p);
     apply_tiles(p);
     const GridGeom &g = p->geom;
     int ntiles = 1;
@@ -1405,6 +1549,7 @@ cgs_status cgs_set_weights(cgs_plan *p, const float *w_in)
     p->w_host = w;
     p->toep_valid = false;
     drop_graphs(p);
+    drop_host_chunks(p);
     p->have_w = true;
     return CGS_OK;
 }
@@ -1435,6 +1580,61 @@ cgs_status cgs_sync(cgs_plan *p)
     return CGS_OK;
 }
 
+// The coil chunks of a host-buffer call.  Chunk q is copied in on hc_in
+// (after chunk q-1), transformed on its child's stream once its copy is in,
+// and copied out on hc_out (after chunk q-1's copy out) once its kernels are
+// done; `st` forks the work and waits for all of it.  `copy_in(q, stream)`
+// issues chunk q's host-to-device copy, `compute(q, stream)` its kernels and
+// `copy_out(q, stream)` its device-to-host copy (each may issue nothing).
+extern "C++" {
+template <class In, class Run, class Out>
+static cgs_status run_host_chunks(cgs_plan *p, cudaStream_t st, bool hout, In copy_in, Run compute, Out copy_out)
+{
+    const size_t C = p->hc.size();
+    CGS_CUDA(cudaEventRecord(p->hc_fork, st));
+    CGS_CUDA(cudaStreamWaitEvent(p->hc_in, p->hc_fork, 0));
+    CGS_CUDA(cudaStreamWaitEvent(p->hc_out, p->hc_fork, 0));
+    for (size_t q = 0; q < C; ++q) {
+        CGS_TRY(copy_in(q, p->hc_in));
+        CGS_CUDA(cudaEventRecord(p->hc_copied[q], p->hc_in));
+    }
+    for (size_t q = 0; q < C; ++q) {
+        cudaStream_t s = p->hc[q]->stream;
+        CGS_CUDA(cudaStreamWaitEvent(s, p->hc_copied[q], 0));
+        CGS_TRY(compute(q, s));
+        CGS_CUDA(cudaEventRecord(p->hc_computed[q], s));
+        CGS_CUDA(cudaStreamWaitEvent(p->hc_out, p->hc_computed[q], 0));
+        CGS_TRY(copy_out(q, p->hc_out));
+    }
+    CGS_CUDA(cudaEventRecord(p->hc_done, p->hc_out));
+    CGS_CUDA(cudaStreamWaitEvent(st, p->hc_done, 0));
+    if (hout) CGS_CUDA(cudaStreamSynchronize(st));
+    return CGS_OK;
+}
+}  // extern "C++"
+
+static cgs_status chunked_trafo(cgs_plan *p, const float *fhat, float *f, bool hin, bool hout, cudaStream_t st)
+{
+    auto src = [&](size_t q) { return (const float2 *)fhat + (int64_t)p->hc_c0[q] * p->Nt; };
+    auto out = [&](size_t q) { return (float2 *)f + (int64_t)p->hc_c0[q] * p->M; };
+    return run_host_chunks(
+        p, st, hout,
+        [&](size_t q, cudaStream_t s) -> cgs_status {
+            cgs_plan *c = p->hc[q];
+            if (hin) CGS_CUDA(cudaMemcpyAsync(c->ioA, src(q), sizeof(float2) * c->nc * p->Nt, cudaMemcpyHostToDevice, s));
+            return CGS_OK;
+        },
+        [&](size_t q, cudaStream_t s) -> cgs_status {
+            cgs_plan *c = p->hc[q];
+            return op_forward(c, hin ? c->ioA : src(q), 2, nullptr, c->ksV, s, hout ? c->ioB : out(q));
+        },
+        [&](size_t q, cudaStream_t s) -> cgs_status {
+            cgs_plan *c = p->hc[q];
+            if (hout) CGS_CUDA(cudaMemcpyAsync(out(q), c->ioB, sizeof(float2) * c->nc * p->M, cudaMemcpyDeviceToHost, s));
+            return CGS_OK;
+        });
+}
+
 // per-coil images (coil-major, caller) -> samples (coil-major, caller)
 cgs_status cgs_nfft_trafo(cgs_plan *p, const float *fhat, float *f, void *stream)
 {
@@ -1445,6 +1645,14 @@ cgs_status cgs_nfft_trafo(cgs_plan *p, const float *fhat, float *f, void *stream
         for (int q = 0; q < p->F; ++q)
             CGS_TRY(cgs_nfft_trafo(p->fr[q], fhat + 2 * q * p->Ntf * p->nc, f + 2 * q * p->Mf * p->nc, st));
         return CGS_OK;
+    }
+    {
+        const bool hin = !is_device_ptr(fhat), hout = !is_device_ptr(f);
+        const int C = host_chunk_count(p);
+        if ((hin || hout) && C > 1) {
+            CGS_TRY(build_host_chunks(p, C));
+            return chunked_trafo(p, fhat, f, hin, hout, st);
+        }
     }
     const void *src;
     CGS_TRY(stage_in(fhat, sizeof(float2) * p->Nt * p->nc, p->ioA, &src, st));
@@ -1497,6 +1705,29 @@ static cgs_status image_out(cgs_plan *p, const float2 *img, float *out, cudaStre
     return CGS_OK;
 }
 
+static cgs_status chunked_adjoint(cgs_plan *p, const float *f, float *fhat, bool hin, bool hout, cudaStream_t st)
+{
+    auto src = [&](size_t q) { return (const float2 *)f + (int64_t)p->hc_c0[q] * p->M; };
+    auto out = [&](size_t q) { return (float2 *)fhat + (int64_t)p->hc_c0[q] * p->Nt; };
+    return run_host_chunks(
+        p, st, hout,
+        [&](size_t q, cudaStream_t s) -> cgs_status {
+            cgs_plan *c = p->hc[q];
+            if (hin) CGS_CUDA(cudaMemcpyAsync(c->ioA, src(q), sizeof(float2) * c->nc * p->M, cudaMemcpyHostToDevice, s));
+            return CGS_OK;
+        },
+        [&](size_t q, cudaStream_t s) -> cgs_status {
+            cgs_plan *c = p->hc[q];
+            CGS_TRY(launch_gather_ks(hin ? c->ioA : src(q), c->perm, c->M, c->nc, c->ksY, s));
+            return op_adjoint(c, c->ksY, 0, hout ? c->ioB : out(q), s, true);
+        },
+        [&](size_t q, cudaStream_t s) -> cgs_status {
+            cgs_plan *c = p->hc[q];
+            if (hout) CGS_CUDA(cudaMemcpyAsync(out(q), c->ioB, sizeof(float2) * c->nc * p->Nt, cudaMemcpyDeviceToHost, s));
+            return CGS_OK;
+        });
+}
+
 cgs_status cgs_nfft_adjoint(cgs_plan *p, const float *f, float *fhat, void *stream)
 {
     CGS_TRY(check_ready(p, false, false));
@@ -1506,6 +1737,14 @@ cgs_status cgs_nfft_adjoint(cgs_plan *p, const float *f, float *fhat, void *stre
         for (int q = 0; q < p->F; ++q)
             CGS_TRY(cgs_nfft_adjoint(p->fr[q], f + 2 * q * p->Mf * p->nc, fhat + 2 * q * p->Ntf * p->nc, st));
         return CGS_OK;
+    }
+    {
+        const bool hin = !is_device_ptr(f), hout = !is_device_ptr(fhat);
+        const int C = host_chunk_count(p);
+        if ((hin || hout) && C > 1) {
+            CGS_TRY(build_host_chunks(p, C));
+            return chunked_adjoint(p, f, fhat, hin, hout, st);
+        }
     }
     CGS_TRY(ks_in(p, f, st));
     // the last FFT pass stores straight into the caller's coil-major layout
@@ -1751,7 +1990,8 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
     if (!in(t->tile, {0, 8, 16, 32}) || !in(t->interp_coils, {0, 1, 4, 8, 16, 32}) ||
         !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 2, 4, 8, 16, 32}) || !in(t->interp_block, {0, 1, 16}) ||
         (t->work_slice != 0 && (t->work_slice < 32 || t->work_slice > 65536)) ||
-        (t->spread_chunk != 0 && (t->spread_chunk < 32 || t->spread_chunk > 65536))) {
+        (t->spread_chunk != 0 && (t->spread_chunk < 32 || t->spread_chunk > 65536)) ||
+        t->host_chunks < 0 || t->host_chunks > 32) {
         set_error("tuning value out of range");
         return CGS_ERR_BAD_ARG;
     }
@@ -1767,6 +2007,7 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
     p->tune = *t;
     apply_tiles(p);
     drop_graphs(p);
+    drop_host_chunks(p);
     if (bins) CGS_TRY(rebin(p));
     return CGS_OK;
 }

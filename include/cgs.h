@@ -211,6 +211,13 @@ typedef struct {
                           cores (16 nodes of a 4 x 4 footprint-start bin per warp,
                           TF32-split operands, FP32 accumulation); default 16 from 4
                           coils for m <= 4, else 1 */
+    int host_chunks;   /* cgs_nfft_trafo / cgs_nfft_adjoint with a host input or output
+                          (one frame): the coils are split into this many contiguous
+                          chunks, each run by a child plan (sharing the plan's node
+                          tables) on its own stream, so one chunk's host copies
+                          overlap another's kernels; 1 = one pass; default 2 when
+                          the k-space holds 8 MiB or more, else 1; at least 4 coils
+                          per chunk (no chunks below 8 coils).  Up to 32. */
 } cgs_tuning;
 
 cgs_status cgs_get_tuning(const cgs_plan *plan, cgs_tuning *out);

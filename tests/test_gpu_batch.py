@@ -44,7 +44,7 @@ def test_tuning_changes_decomposition_not_results(gpu):
     p, _ = make_plan(N, nc, k, synth.ramp_weights(k))
     f0, a0 = nfft_pair(p, N, nc, k.shape[0])
     assert p.tuning() == dict(tile=0, work_slice=0, spread_chunk=0, interp_coils=0, spread_coils=0,
-                              spread_block=0, interp_block=0)
+                              spread_block=0, interp_block=0, host_chunks=0)
     for t in [dict(tile=8, work_slice=256, spread_chunk=64, interp_coils=4, spread_coils=2, spread_block=1),
               dict(tile=32, work_slice=2048, spread_chunk=1024, interp_coils=16, spread_coils=8, spread_block=4),
               dict(tile=16, work_slice=100, spread_chunk=0, interp_coils=1, spread_coils=1, spread_block=0),
@@ -58,6 +58,7 @@ def test_tuning_changes_decomposition_not_results(gpu):
               dict(tile=32, work_slice=512, spread_chunk=0, interp_coils=4, spread_coils=0, spread_block=0,
                    interp_block=1)]:
         t = dict(interp_block=0, **t) if "interp_block" not in t else t
+        t = dict(host_chunks=0, **t)
         p.set_tuning(**t)
         assert p.tuning() == t
         f1, a1 = nfft_pair(p, N, nc, k.shape[0])
@@ -252,3 +253,83 @@ def test_tensor_core_interpolation_matches_cuda_cores(gpu, nc, m):
     p.nfft_trafo(fh, out)
     assert rel(out, ref) < 2e-6
     p.close()
+
+
+@pytest.mark.parametrize("nc,chunks", [(8, 2), (10, 3), (16, 4), (16, 0), (32, 0)])
+def test_host_buffer_coil_chunks_match_device_path(gpu, nc, chunks):
+    """Host-buffer NFFT calls split the coils into chunks run by child plans
+    (sharing the plan's node tables) on their own streams, host copies
+    overlapping kernels; every combination of host and device buffers gives
+    what the one-pass device path gives.  The 32-coil case is large enough for
+    the default (2 chunks); 10 coils in 3 chunks run as 2 (4 coils at least)."""
+    import torch
+    from codeare_gb300 import synth
+    N = 256 if nc == 32 else 64
+    k = synth.radial2d(403, 512, golden=True) if nc == 32 else synth.radial2d(48, 128, golden=True)
+    M = k.shape[0]
+    p, _ = make_plan(N, nc, k, synth.ramp_weights(k))
+    rng = np.random.default_rng(5)
+    fh = (rng.standard_normal((nc, N, N)) + 1j * rng.standard_normal((nc, N, N))).astype(np.complex64)
+    y = (rng.standard_normal((nc, M)) + 1j * rng.standard_normal((nc, M))).astype(np.complex64)
+    dev = torch.device("cuda:0")
+    fh_d, y_d = torch.from_numpy(fh).to(dev), torch.from_numpy(y).to(dev)
+    f_d = torch.zeros((nc, M), dtype=torch.complex64, device=dev)
+    a_d = torch.zeros((nc, N, N), dtype=torch.complex64, device=dev)
+    p.nfft_trafo(fh_d, f_d)
+    p.nfft_adjoint(y_d, a_d)
+    torch.cuda.synchronize()
+    f_ref, a_ref = f_d.cpu().numpy(), a_d.cpu().numpy()
+    p.set_tuning(host_chunks=chunks)
+    assert p.tuning()["host_chunks"] == chunks
+    for it in range(2):  # the second call reuses the chunk plans
+        f = np.zeros((nc, M), np.complex64)
+        a = np.zeros((nc, N, N), np.complex64)
+        p.nfft_trafo(fh, f)
+        p.nfft_adjoint(y, a)
+        assert rel(f, f_ref) < 1e-6 and rel(a, a_ref) < 1e-6
+    # host in, device out and device in, host out
+    f_d.zero_(); a_d.zero_()
+    p.nfft_trafo(fh, f_d)
+    p.nfft_adjoint(y, a_d)
+    torch.cuda.synchronize()
+    assert rel(f_d.cpu().numpy(), f_ref) < 1e-6 and rel(a_d.cpu().numpy(), a_ref) < 1e-6
+    f = np.zeros((nc, M), np.complex64)
+    a = np.zeros((nc, N, N), np.complex64)
+    p.nfft_trafo(fh_d, f)
+    p.nfft_adjoint(y_d, a)
+    assert rel(f, f_ref) < 1e-6 and rel(a, a_ref) < 1e-6
+    # a new trajectory drops the chunk plans; the next host call rebuilds them
+    k2 = np.ascontiguousarray(k[::-1])
+    p.set_kspace(k2)
+    f2 = np.zeros((nc, M), np.complex64)
+    p.nfft_trafo(fh, f2)
+    assert rel(f2[:, ::-1], f_ref) < 1e-6
+    with pytest.raises(gpu.CgsError):
+        p.set_tuning(host_chunks=33)
+
+
+def test_host_buffer_coil_chunks_3d(gpu):
+    """The 3-D per-coil NFFT through coil chunks (8 coils in 2) against the
+    one-pass device path."""
+    import torch
+    from codeare_gb300 import capi, synth
+    N, nc = 24, 8
+    k = synth.kooshball3d(300, 48)
+    M = k.shape[0]
+    p = capi.Plan((N, N, N), M, ncoils=nc, m=4, alpha=2.0)
+    p.set_kspace(k)
+    rng = np.random.default_rng(6)
+    fh = (rng.standard_normal((nc, N, N, N)) + 1j * rng.standard_normal((nc, N, N, N))).astype(np.complex64)
+    y = (rng.standard_normal((nc, M)) + 1j * rng.standard_normal((nc, M))).astype(np.complex64)
+    dev = torch.device("cuda:0")
+    f_d = torch.zeros((nc, M), dtype=torch.complex64, device=dev)
+    a_d = torch.zeros((nc, N, N, N), dtype=torch.complex64, device=dev)
+    p.nfft_trafo(torch.from_numpy(fh).to(dev), f_d)
+    p.nfft_adjoint(torch.from_numpy(y).to(dev), a_d)
+    torch.cuda.synchronize()
+    p.set_tuning(host_chunks=2)
+    f = np.zeros((nc, M), np.complex64)
+    a = np.zeros((nc, N, N, N), np.complex64)
+    p.nfft_trafo(fh, f)
+    p.nfft_adjoint(y, a)
+    assert rel(f, f_d.cpu().numpy()) < 1e-6 and rel(a, a_d.cpu().numpy()) < 1e-6
