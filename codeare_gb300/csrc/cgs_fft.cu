@@ -517,23 +517,37 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
         if (p.deap_o0) dcol *= p.deap_o0[o / p.o1_len];
     }
     {
+        // a thread's values differ only in the axis index a: the column's base
+        // pointers and strides are set once, the load mode is branched on once
         float2 v[EPT];
 #pragma unroll
-        for (int u = 0; u < EPT; ++u) {
-            const int pos = r0 + u * RSTEP;
-            v[u] = make_float2(0.f, 0.f);
-            if (!col_ok) continue;
-            const int a = in_pos_to_axis(pos, p.Lin, N, p.in_centred);
-            if (a < 0) continue;
-            const int64_t pix = o * p.Lin + a;
-            if (p.load_mode == LOAD_PLAIN) {
-                v[u] = p.src[pix * p.inner + i];
-            } else {
-                float2 x = p.img_per_coil ? (p.coil_major ? p.img[i * p.coil_major + pix] : p.img[pix * p.inner + i])
-                                          : p.img[pix];
-                if (p.sens) x = cmul(x, p.sens[pix * p.inner + i]);
-                float sc = dcol * (p.deap_ax ? p.deap_ax[a] : 1.f);
-                if (p.mask) sc *= p.mask[pix];
+        for (int u = 0; u < EPT; ++u) v[u] = make_float2(0.f, 0.f);
+        if (col_ok && p.load_mode == LOAD_PLAIN) {
+            const float2 *src = p.src + (o * p.Lin) * p.inner + i;
+            const int64_t sst = p.inner;
+#pragma unroll
+            for (int u = 0; u < EPT; ++u) {
+                const int a = in_pos_to_axis(r0 + u * RSTEP, p.Lin, N, p.in_centred);
+                if (a >= 0) v[u] = src[a * sst];
+            }
+        } else if (col_ok) {
+            const bool cm = p.img_per_coil && p.coil_major;
+            const float2 *img = !p.img_per_coil ? p.img + o * p.Lin
+                                : cm ? p.img + i * p.coil_major + o * p.Lin
+                                     : p.img + (o * p.Lin) * p.inner + i;
+            const int64_t ist = (p.img_per_coil && !cm) ? p.inner : 1;
+            const float2 *sens = p.sens ? p.sens + (o * p.Lin) * p.inner + i : nullptr;
+            const float *mask = p.mask ? p.mask + o * p.Lin : nullptr;
+            const float *dax = p.deap_ax;
+            const int64_t inner = p.inner;
+#pragma unroll
+            for (int u = 0; u < EPT; ++u) {
+                const int a = in_pos_to_axis(r0 + u * RSTEP, p.Lin, N, p.in_centred);
+                if (a < 0) continue;
+                float2 x = img[a * ist];
+                if (sens) x = cmul(x, sens[a * inner]);
+                float sc = dax ? dcol * dax[a] : dcol;
+                if (mask) sc *= mask[a];
                 v[u] = cscale(x, sc);
             }
         }
@@ -556,15 +570,19 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
         ct_passes_s<N, LOGB, 1, +1>(buf, tw);
     }
     if (!col_ok) return;
+    const bool dp = p.store_mode == STORE_DEAPOD;
+    const bool cm = dp && p.coil_major;
+    float2 *dst = cm ? p.dst + i * p.coil_major + o * p.Lout : p.dst + (o * p.Lout) * p.inner + i;
+    const int64_t dstr = cm ? 1 : p.inner;
+    const float *dax = dp ? p.deap_ax : nullptr;
 #pragma unroll
     for (int u = 0; u < EPT; ++u) {
         const int a = r0 + u * RSTEP;
         if (a >= p.Lout) continue;
         const int pos = out_axis_to_pos(a, p.Lout, N, p.out_centred);
         float2 v = buf[ct_slot<LOGB>(pos, b)];
-        if (p.store_mode == STORE_DEAPOD) v = cscale(v, dcol * (p.deap_ax ? p.deap_ax[a] : 1.f));
-        if (p.coil_major && p.store_mode == STORE_DEAPOD) p.dst[i * p.coil_major + o * p.Lout + a] = v;
-        else p.dst[(o * p.Lout + a) * p.inner + i] = v;
+        if (dp) v = cscale(v, dax ? dcol * dax[a] : dcol);
+        dst[a * dstr] = v;
     }
 }
 
