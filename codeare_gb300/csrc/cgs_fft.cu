@@ -435,6 +435,102 @@ __device__ __forceinline__ void ct_pass_s(float2 *buf, const float2 *tw)
     __syncthreads();
 }
 
+// A pass whose butterfly inputs (IN) or outputs (OUT) stay in the thread's
+// registers instead of shared memory.  Butterfly t of a thread covers rows
+// j + r N/R with j = r0 + t RSTEP, the rows the thread loads from and stores
+// to global memory (r0 + u RSTEP): register u = t + r NBF.  IN holds for the
+// first pass (NS = 1), OUT for the last (NS R = N), where the stored row of
+// butterfly output r is j + r NS = j + r N/R as well.
+template <int N, int LOGB, int R, int NS, int S, bool IN, bool OUT, int EPT>
+__device__ __forceinline__ void ct_pass_r(float2 *buf, const float2 *tw, float2 (&reg)[EPT])
+{
+    constexpr int B = 1 << LOGB;
+    constexpr int NR = N / R;
+    constexpr int TB = B * NR;
+    constexpr int NBF = (TB + kThreads - 1) / kThreads;
+    constexpr int STEP = N / (NS * R);
+    constexpr int SL = ct_stride<LOGB, NR, R>(false);
+    constexpr int SS = ct_stride<LOGB, NS, R>(NS == 1 && R == 8);
+    static_assert(!(IN || OUT) || (TB % kThreads == 0 && NBF * R == EPT), "register pass layout");
+    static_assert(!IN || NS == 1, "registers in: the first pass only");
+    static_assert(!OUT || NS * R == N, "registers out: the last pass only");
+    float2 v[NBF][R];
+#pragma unroll
+    for (int t = 0; t < NBF; ++t) {
+        const int q = threadIdx.x + t * kThreads;
+        if (TB % kThreads != 0 && q >= TB) continue;
+        const int b = q & (B - 1), j = q >> LOGB, k = j % NS;
+        if constexpr (IN) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[t][r] = reg[t + r * NBF];
+        } else if constexpr (SL > 0) {
+            const float2 *src = buf + ct_slot<LOGB>(j, b);
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[t][r] = src[r * SL];
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[t][r] = buf[ct_slot<LOGB>(j + r * NR, b)];
+        }
+        if constexpr (NS > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                float2 w = tw[k * r * STEP];
+                if constexpr (S > 0) w.y = -w.y;
+                v[t][r] = cmul(v[t][r], w);
+            }
+        }
+        ct_bfly<R, S>(v[t], tw, NR);
+    }
+    if constexpr (OUT) {
+#pragma unroll
+        for (int t = 0; t < NBF; ++t)
+#pragma unroll
+            for (int r = 0; r < R; ++r) reg[t + r * NBF] = v[t][r];
+        return;
+    }
+    if constexpr (!IN) __syncthreads();  // this pass's reads are done before the in-place stores
+#pragma unroll
+    for (int t = 0; t < NBF; ++t) {
+        const int q = threadIdx.x + t * kThreads;
+        if (TB % kThreads != 0 && q >= TB) continue;
+        const int b = q & (B - 1), j = q >> LOGB, k = j % NS;
+        const int base = (j / NS) * NS * R + k;
+        if constexpr (SS > 0) {
+            float2 *dst = buf + ct_slot<LOGB>(base, b);
+#pragma unroll
+            for (int r = 0; r < R; ++r) dst[r * SS] = v[t][r];
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) buf[ct_slot<LOGB>(base + r * NS, b)] = v[t][r];
+        }
+    }
+    __syncthreads();
+}
+
+template <int N, int LOGB, int NS, int S, bool IN, bool OUT, int EPT>
+__device__ __forceinline__ void ct_passes_r(float2 *buf, const float2 *tw, float2 (&reg)[EPT])
+{
+    if constexpr (NS < N) {
+        constexpr int R = ct_next_radix(N / NS);
+        ct_pass_r<N, LOGB, R, NS, S, IN && NS == 1, OUT && NS * R == N, EPT>(buf, tw, reg);
+        ct_passes_r<N, LOGB, NS * R, S, IN, OUT, EPT>(buf, tw, reg);
+    }
+}
+
+// whether the first and last passes can keep their data in registers (every
+// thread holds whole butterflies: B N / R a multiple of the block size)
+template <int N, int LOGB, int NS = 1>
+__host__ __device__ constexpr bool ct_reg_ok()
+{
+    if constexpr (NS >= N) {
+        return true;
+    } else {
+        constexpr int R = ct_next_radix(N / NS);
+        constexpr bool edge = NS == 1 || NS * R == N;
+        return (!edge || (((N / R) << LOGB) % kThreads == 0)) && ct_reg_ok<N, LOGB, NS * R>();
+    }
+}
+
 template <int N, int LOGB, int NS, int S>
 __device__ __forceinline__ void ct_passes_s(float2 *buf, const float2 *tw)
 {
@@ -551,11 +647,36 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
                 v[u] = cscale(x, sc);
             }
         }
+        if constexpr (ct_reg_ok<N, LOGB>()) {
+            // the first pass takes its inputs from these registers; without a
+            // centred (cropping) store or a Toeplitz round the last pass leaves
+            // its outputs in them, in the order the store wants
+            if (!p.toep_k && !p.out_centred) {
+                ct_passes_r<N, LOGB, 1, S, true, true, EPT>(buf, tw, v);
+                if (!col_ok) return;
+                const bool dp = p.store_mode == STORE_DEAPOD;
+                const bool cm = dp && p.coil_major;
+                float2 *dst = cm ? p.dst + i * p.coil_major + o * p.Lout : p.dst + (o * p.Lout) * p.inner + i;
+                const int64_t dstr = cm ? 1 : p.inner;
+                const float *dax = dp ? p.deap_ax : nullptr;
 #pragma unroll
-        for (int u = 0; u < EPT; ++u) buf[ct_slot<LOGB>(r0 + u * RSTEP, b)] = v[u];
+                for (int u = 0; u < EPT; ++u) {
+                    const int a = r0 + u * RSTEP;
+                    if (a >= p.Lout) continue;
+                    float2 x = v[u];
+                    if (dp) x = cscale(x, dax ? dcol * dax[a] : dcol);
+                    dst[a * dstr] = x;
+                }
+                return;
+            }
+            ct_passes_r<N, LOGB, 1, S, true, false, EPT>(buf, tw, v);
+        } else {
+#pragma unroll
+            for (int u = 0; u < EPT; ++u) buf[ct_slot<LOGB>(r0 + u * RSTEP, b)] = v[u];
+            __syncthreads();
+            ct_passes_s<N, LOGB, 1, S>(buf, tw);
+        }
     }
-    __syncthreads();
-    ct_passes_s<N, LOGB, 1, S>(buf, tw);
     if (p.toep_k) {
         // pointwise multiply by the real Toeplitz kernel, then transform back
         const int64_t kstride = p.inner / p.toep_nc;
