@@ -9,6 +9,8 @@
 // mask and the deapodisation 1/phihut (NFFT3's PRE_PHI_HUT step), and the last
 // inverse pass fuses the deapodisation: the FFT-side work of the reference's
 // nfft_trafo / nfft_adjoint (src/matrix/ft/NFFTTraits.hpp:176-204).
+#include <type_traits>
+
 #include "cgs_internal.cuh"
 
 #include <initializer_list>
@@ -648,10 +650,14 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
             }
         }
         if constexpr (ct_reg_ok<N, LOGB>()) {
-            // the first pass takes its inputs from these registers; without a
-            // centred (cropping) store or a Toeplitz round the last pass leaves
-            // its outputs in them, in the order the store wants
-            if (!p.toep_k && !p.out_centred) {
+            // The first pass takes its inputs from these registers.  Without a
+            // Toeplitz round the last pass leaves its outputs in them: row
+            // r0 + u RSTEP in v[u], which is what an uncentred store wants; a
+            // centred crop to Lout = N/2 (twofold oversampling) stores row
+            // a + 3N/4 (a < N/4) or a - N/4 at a = r0 + u RSTEP, which is
+            // v[(u + 3 EPT/4) mod EPT] of the same thread.
+            const bool rot_ok = (EPT % 4 == 0) && 2 * p.Lout == N;
+            if (!p.toep_k && (!p.out_centred || rot_ok)) {
                 ct_passes_r<N, LOGB, 1, S, true, true, EPT>(buf, tw, v);
                 if (!col_ok) return;
                 const bool dp = p.store_mode == STORE_DEAPOD;
@@ -659,14 +665,19 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
                 float2 *dst = cm ? p.dst + i * p.coil_major + o * p.Lout : p.dst + (o * p.Lout) * p.inner + i;
                 const int64_t dstr = cm ? 1 : p.inner;
                 const float *dax = dp ? p.deap_ax : nullptr;
+                auto store = [&](auto rot) {
+                    constexpr int ROT = decltype(rot)::value;
 #pragma unroll
-                for (int u = 0; u < EPT; ++u) {
-                    const int a = r0 + u * RSTEP;
-                    if (a >= p.Lout) continue;
-                    float2 x = v[u];
-                    if (dp) x = cscale(x, dax ? dcol * dax[a] : dcol);
-                    dst[a * dstr] = x;
-                }
+                    for (int u = 0; u < EPT; ++u) {
+                        const int a = r0 + u * RSTEP;
+                        if (a >= p.Lout) continue;
+                        float2 x = v[(u + ROT) % EPT];
+                        if (dp) x = cscale(x, dax ? dcol * dax[a] : dcol);
+                        dst[a * dstr] = x;
+                    }
+                };
+                if (p.out_centred) store(std::integral_constant<int, (3 * EPT / 4) % EPT>{});
+                else store(std::integral_constant<int, 0>{});
                 return;
             }
             ct_passes_r<N, LOGB, 1, S, true, false, EPT>(buf, tw, v);
