@@ -197,7 +197,9 @@ cgs_status launch_spread(const GridGeom &g, const NodeSet &ns, const float2 *ks,
 // vector kernels (cgs_vec.cu)
 // ---------------------------------------------------------------------------
 // user (NC, M) coil-major unsorted  <->  ks[s][c] sorted coil-minor
-cgs_status launch_gather_ks(const float2 *user, const int *perm, int64_t M, int nc, float2 *ks,
+// (gather: iperm[j] = sorted position of trajectory node j; scatter: perm[s] =
+// trajectory node at sorted position s)
+cgs_status launch_gather_ks(const float2 *user, const int *iperm, int64_t M, int nc, float2 *ks,
                             cudaStream_t st);
 cgs_status launch_scatter_ks(const float2 *ks, const int *perm, int64_t M, int nc, float2 *user,
                              cudaStream_t st);

@@ -184,7 +184,8 @@ struct cgs_plan {
     // trajectory
     bool have_k = false, have_w = false, have_s = false;
     float4 *nodes = nullptr;
-    int *perm = nullptr;
+    int *perm = nullptr;   // trajectory node at each sorted position
+    int *iperm = nullptr;  // sorted position of each trajectory node
     float *w = nullptr;
     int4 *work = nullptr;
     int nwork = 0;
@@ -1281,6 +1282,7 @@ cgs_status cgs_plan_create(cgs_plan **out, const cgs_plan_desc *desc)
     }
     ALLOC(p->nodes, (size_t)M * (p->d == 2 ? 1 : 2));
     ALLOC(p->perm, M);
+    ALLOC(p->iperm, M);
     ALLOC(p->w, M);
 #undef ALLOC
     *out = p;
@@ -1347,7 +1349,8 @@ static cgs_status build_host_chunks(cgs_plan *p, int C)
         dev_free(c->perm);
         dev_free(c->w);
         c->shared_nodes = true;
-        c->nodes = p->nodes; c->perm = p->perm; c->w = p->w;
+        dev_free(c->iperm);
+        c->nodes = p->nodes; c->perm = p->perm; c->iperm = p->iperm; c->w = p->w;
         c->work = p->work; c->nwork = p->nwork;
         c->nodeU = p->nodeU; c->nodeW = p->nodeW;
         c->pentries = p->pentries; c->pwork = p->pwork; c->pmulti = p->pmulti;
@@ -1393,11 +1396,11 @@ cgs_status cgs_plan_destroy(cgs_plan *p)
     for (cgs_plan *c : p->fr) cgs_plan_destroy(c);
     drop_host_chunks(p);
     if (p->shared_nodes) {  // the parent frees these
-        p->nodes = nullptr; p->perm = nullptr; p->w = nullptr; p->work = nullptr;
+        p->nodes = nullptr; p->perm = nullptr; p->iperm = nullptr; p->w = nullptr; p->work = nullptr;
         p->nodeU = nullptr; p->nodeW = nullptr; p->pentries = nullptr; p->pwork = nullptr; p->pmulti = nullptr;
         p->ilist = nullptr; p->iwork = nullptr;
     }
-    void *bufs[] = {p->tw[0], p->tw[1], p->tw[2], p->deap[0], p->deap[1], p->deap[2], p->nodes, p->perm,
+    void *bufs[] = {p->tw[0], p->tw[1], p->tw[2], p->deap[0], p->deap[1], p->deap[2], p->nodes, p->perm, p->iperm,
                     p->w, p->work, p->nodeU, p->nodeW, p->pentries, p->pwork, p->pmulti, p->ppartial, p->ilist, p->iwork, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
                     p->cF, p->cP, p->cZ, p->vX, p->vR, p->vP, p->vQ, p->ioA, p->ioB, p->partial, p->dots,
                     p->active, p->sc, p->fpart, p->ftick};
@@ -1515,6 +1518,11 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
     CGS_CUDA(cudaMemcpy(p->work, work.data(), sizeof(int4) * work.size(), cudaMemcpyHostToDevice));
     CGS_CUDA(cudaMemcpy(p->nodes, nodes.data(), sizeof(float4) * nodes.size(), cudaMemcpyHostToDevice));
     CGS_CUDA(cudaMemcpy(p->perm, perm.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+    {
+        std::vector<int> iperm(M);
+        for (int64_t q = 0; q < M; ++q) iperm[perm[q]] = (int)q;
+        CGS_CUDA(cudaMemcpy(p->iperm, iperm.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
+    }
     if (d == 2) {
         CGS_TRY(build_patches(p, cc));
         CGS_TRY(build_ibins(p, cc, perm));
@@ -1671,10 +1679,10 @@ static cgs_status gather_ks(cgs_plan *p, const float *y, float2 *dst, cudaStream
 {
     const void *src;
     CGS_TRY(stage_in(y, sizeof(float2) * p->M * p->nc, p->ioA, &src, st));
-    if (p->F == 1) return launch_gather_ks((const float2 *)src, p->perm, p->M, p->nc, dst, st);
+    if (p->F == 1) return launch_gather_ks((const float2 *)src, p->iperm, p->M, p->nc, dst, st);
     for (int f = 0; f < p->F; ++f) {
         const int64_t off = f * p->Mf * p->nc;
-        CGS_TRY(launch_gather_ks((const float2 *)src + off, p->fr[f]->perm, p->Mf, p->nc, dst + off, st));
+        CGS_TRY(launch_gather_ks((const float2 *)src + off, p->fr[f]->iperm, p->Mf, p->nc, dst + off, st));
     }
     return CGS_OK;
 }
@@ -1718,7 +1726,7 @@ static cgs_status chunked_adjoint(cgs_plan *p, const float *f, float *fhat, bool
         },
         [&](size_t q, cudaStream_t s) -> cgs_status {
             cgs_plan *c = p->hc[q];
-            CGS_TRY(launch_gather_ks(hin ? c->ioA : src(q), c->perm, c->M, c->nc, c->ksY, s));
+            CGS_TRY(launch_gather_ks(hin ? c->ioA : src(q), c->iperm, c->M, c->nc, c->ksY, s));
             return op_adjoint(c, c->ksY, 0, hout ? c->ioB : out(q), s, true);
         },
         [&](size_t q, cudaStream_t s) -> cgs_status {

@@ -26,25 +26,27 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 // read or written in contiguous coil runs, the caller side along 32 sorted
 // positions of one coil, whose trajectory indices perm[s] come in runs (the
 // bin sort is stable, so a spoke's consecutive samples stay together).
-__global__ void gather_ks_kernel(const float2 *__restrict__ user, const int *__restrict__ perm,
+__global__ void gather_ks_kernel(const float2 *__restrict__ user, const int *__restrict__ iperm,
                                  int64_t M, int nc, float2 *__restrict__ ks)
 {
+    // 32 x 32 tiles of (coil, node in trajectory order): read along the
+    // trajectory (coalesced), written as one contiguous run of the tile's
+    // coils per node at the node's sorted position
     __shared__ float2 t[32][33];
-    const int64_t ts_n = (M + 31) / 32, tc_n = (nc + 31) / 32;
-    for (int64_t tile = blockIdx.x; tile < ts_n * tc_n; tile += gridDim.x) {
-        const int64_t s0 = (tile / tc_n) * 32;
+    const int64_t tj_n = (M + 31) / 32, tc_n = (nc + 31) / 32;
+    for (int64_t tile = blockIdx.x; tile < tj_n * tc_n; tile += gridDim.x) {
+        const int64_t j0 = (tile / tc_n) * 32;
         const int c0 = (int)(tile % tc_n) * 32;
-        const int64_t s = s0 + threadIdx.x;
-        const int64_t j = s < M ? perm[s] : 0;
+        const int64_t j = j0 + threadIdx.x;
         for (int k = threadIdx.y; k < 32; k += 8) {
             const int c = c0 + k;
-            if (s < M && c < nc) t[k][threadIdx.x] = user[(int64_t)c * M + j];
+            if (j < M && c < nc) t[k][threadIdx.x] = user[(int64_t)c * M + j];
         }
         __syncthreads();
         for (int k = threadIdx.y; k < 32; k += 8) {
-            const int64_t ss = s0 + k;
+            const int64_t jj = j0 + k;
             const int c = c0 + threadIdx.x;
-            if (ss < M && c < nc) ks[ss * nc + c] = t[threadIdx.x][k];
+            if (jj < M && c < nc) ks[(int64_t)iperm[jj] * nc + c] = t[threadIdx.x][k];
         }
         __syncthreads();
     }
@@ -706,12 +708,12 @@ unsigned grid_for(int64_t n)
 
 int dot_blocks() { return kDotBlocks; }
 
-cgs_status launch_gather_ks(const float2 *user, const int *perm, int64_t M, int nc, float2 *ks,
+cgs_status launch_gather_ks(const float2 *user, const int *iperm, int64_t M, int nc, float2 *ks,
                             cudaStream_t st)
 {
     if (M * nc == 0) return CGS_OK;
     const int64_t tiles = ((M + 31) / 32) * ((nc + 31) / 32);
-    gather_ks_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 32), dim3(32, 8), 0, st>>>(user, perm, M, nc, ks);
+    gather_ks_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 32), dim3(32, 8), 0, st>>>(user, iperm, M, nc, ks);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }
