@@ -657,6 +657,9 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
             // a + 3N/4 (a < N/4) or a - N/4 at a = r0 + u RSTEP, which is
             // v[(u + 3 EPT/4) mod EPT] of the same thread.
             const bool rot_ok = (EPT % 4 == 0) && 2 * p.Lout == N;
+            // the twiddle table is complete before any butterfly reads it (the
+            // radix 3, 5 and 7 butterflies take their roots from it)
+            __syncthreads();
             if (!p.toep_k && (!p.out_centred || rot_ok)) {
                 ct_passes_r<N, LOGB, 1, S, true, true, EPT>(buf, tw, v);
                 if (!col_ok) return;
