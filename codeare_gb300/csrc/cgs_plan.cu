@@ -148,6 +148,21 @@ __global__ void toep_real_kernel(const float2 *K, float *out, int64_t tot, float
 
 using namespace cgs;
 
+// Coil chunks of a host-buffer per-coil NFFT call: child plans, each holding
+// a contiguous range of the caller's coil-major coils and sharing the parent's
+// node tables, so that one chunk's host copies overlap the other chunks'
+// kernels.  Copies to the device run in order on `in`, copies to the host on
+// `out`, each chunk's kernels on its child's stream.  Built on the first
+// host-buffer call, dropped whenever the trajectory, the weights or the tuning
+// change.
+struct HostChunks {
+    std::vector<cgs_plan *> plans;
+    std::vector<int> c0;  // first coil of each chunk (plans.size() + 1 entries)
+    cudaStream_t in = nullptr, out = nullptr;
+    cudaEvent_t fork = nullptr, done = nullptr;
+    std::vector<cudaEvent_t> copied, computed;
+};
+
 struct cgs_plan {
     int d = 0, N[3] = {1, 1, 1}, n[3] = {1, 1, 1}, m = 1, nc = 1;
     // frames (NCSENSE dim4 x dim5, NCSENSE.hpp:141-166): F child plans with one
@@ -158,18 +173,9 @@ struct cgs_plan {
     int F = 1;
     int64_t Mf = 0, Ntf = 0;
     std::vector<cgs_plan *> fr;
-    // host-buffer pipeline of the per-coil NFFT (one frame): child plans, each
-    // holding a contiguous range of the caller's coil-major coils and sharing
-    // this plan's node tables, so that one chunk's host copies overlap the
-    // other chunks' kernels.  Copies to the device run in order on hc_in,
-    // copies to the host on hc_out, each chunk's kernels on its child's
-    // stream.  Built on the first host-buffer call, dropped whenever the
-    // trajectory, the weights or the tuning change.
-    std::vector<cgs_plan *> hc;
-    std::vector<int> hc_c0;      // first coil of each chunk (hc.size() + 1 entries)
-    cudaStream_t hc_in = nullptr, hc_out = nullptr;
-    cudaEvent_t hc_fork = nullptr, hc_done = nullptr;
-    std::vector<cudaEvent_t> hc_copied, hc_computed;
+    // host-buffer pipeline of the per-coil NFFT (one frame): one chunk set for
+    // the forward and one for the adjoint (their best chunk counts differ)
+    HostChunks hcf, hca;
     bool shared_nodes = false;   // a coil chunk: the node tables belong to its parent
     double alpha = 1.0;
     int64_t M = 0, Nt = 1, ntot = 1;
@@ -1292,32 +1298,40 @@ cgs_status cgs_plan_create(cgs_plan **out, const cgs_plan_desc *desc)
 // ---------------------------------------------------------------------------
 // Coil chunks of the host-buffer per-coil NFFT
 // ---------------------------------------------------------------------------
-static void drop_host_chunks(cgs_plan *p)
+static void drop_chunk_set(HostChunks &h)
 {
-    if (p->hc_in) cudaStreamSynchronize(p->hc_in);
-    if (p->hc_out) cudaStreamSynchronize(p->hc_out);
-    for (cgs_plan *c : p->hc) cgs_plan_destroy(c);
-    p->hc.clear();
-    p->hc_c0.clear();
-    for (cudaEvent_t e : p->hc_copied) cudaEventDestroy(e);
-    for (cudaEvent_t e : p->hc_computed) cudaEventDestroy(e);
-    p->hc_copied.clear();
-    p->hc_computed.clear();
-    for (cudaEvent_t *e : {&p->hc_fork, &p->hc_done})
+    if (h.in) cudaStreamSynchronize(h.in);
+    if (h.out) cudaStreamSynchronize(h.out);
+    for (cgs_plan *c : h.plans) cgs_plan_destroy(c);
+    h.plans.clear();
+    h.c0.clear();
+    for (cudaEvent_t e : h.copied) cudaEventDestroy(e);
+    for (cudaEvent_t e : h.computed) cudaEventDestroy(e);
+    h.copied.clear();
+    h.computed.clear();
+    for (cudaEvent_t *e : {&h.fork, &h.done})
         if (*e) { cudaEventDestroy(*e); *e = nullptr; }
-    for (cudaStream_t *s : {&p->hc_in, &p->hc_out})
-        if (*s) { cudaStreamDestroy(*s); *s = nullptr; }
+    for (cudaStream_t *st : {&h.in, &h.out})
+        if (*st) { cudaStreamDestroy(*st); *st = nullptr; }
 }
 
-// chunks of a host-buffer call (one frame): the tuning's host_chunks, else 2
-// once the caller's k-space reaches 8 MiB (below that the copies are too
-// short to hide anything behind); at least 4 coils per chunk, so that every
-// chunk grids with the parent's patch shapes and node tables
-static int host_chunk_count(const cgs_plan *p)
+static void drop_host_chunks(cgs_plan *p)
+{
+    drop_chunk_set(p->hcf);
+    drop_chunk_set(p->hca);
+}
+
+// chunks of a host-buffer call (one frame, 8 coils or more): the tuning's
+// host_chunks, else, once the caller's k-space reaches 8 MiB (below that the
+// copies are too short to hide anything behind), 4 for the forward and 2 for
+// the adjoint, whose spreading loses more to smaller coil counts; at least 4
+// coils per chunk, so that every chunk grids with the parent's patch shapes
+// and node tables
+static int host_chunk_count(const cgs_plan *p, bool adjoint)
 {
     if (p->F > 1 || p->nc < 8) return 1;
     int c = p->tune.host_chunks;
-    if (c == 0) c = (p->M * p->nc * (int64_t)sizeof(float2) >= (8 << 20)) ? 2 : 1;
+    if (c == 0) c = (p->M * p->nc * (int64_t)sizeof(float2) >= (8 << 20)) ? (adjoint ? 2 : 4) : 1;
     return std::max(1, std::min(c, p->nc / 4));
 }
 
@@ -1325,10 +1339,10 @@ static int host_chunk_count(const cgs_plan *p)
 // left to their defaults), nc / C coils each (the first nc % C chunks one
 // more), reading the parent's node tables; each owns its grids, staging and
 // the partial sums of split spreading patches
-static cgs_status build_host_chunks(cgs_plan *p, int C)
+static cgs_status build_host_chunks(cgs_plan *p, HostChunks &h, int C)
 {
-    if ((int)p->hc.size() == C) return CGS_OK;
-    drop_host_chunks(p);
+    if ((int)h.plans.size() == C) return CGS_OK;
+    drop_chunk_set(h);
     cgs_plan_desc one{};
     one.rank = p->d;
     for (int t = 0; t < 3; ++t) one.N[t] = p->N[t];
@@ -1337,14 +1351,14 @@ static cgs_status build_host_chunks(cgs_plan *p, int C)
     one.M = p->M;
     one.frames = 1;
     cgs_status st = CGS_OK;
-    p->hc_c0.push_back(0);
+    h.c0.push_back(0);
     for (int q = 0; q < C && st == CGS_OK; ++q) {
         one.ncoils = p->nc / C + (q < p->nc % C ? 1 : 0);
         cgs_plan *c = nullptr;
         st = cgs_plan_create(&c, &one);
         if (st != CGS_OK) break;
-        p->hc.push_back(c);
-        p->hc_c0.push_back(p->hc_c0.back() + one.ncoils);
+        h.plans.push_back(c);
+        h.c0.push_back(h.c0.back() + one.ncoils);
         dev_free(c->nodes);
         dev_free(c->perm);
         dev_free(c->w);
@@ -1369,22 +1383,22 @@ static cgs_status build_host_chunks(cgs_plan *p, int C)
         c->have_w = p->have_w;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         const bool ok0 = cudaEventCreateWithFlags(&e0, cudaEventDisableTiming) == cudaSuccess;
-        if (ok0) p->hc_copied.push_back(e0);
+        if (ok0) h.copied.push_back(e0);
         const bool ok1 = cudaEventCreateWithFlags(&e1, cudaEventDisableTiming) == cudaSuccess;
-        if (ok1) p->hc_computed.push_back(e1);
+        if (ok1) h.computed.push_back(e1);
         if (st == CGS_OK && (!ok0 || !ok1)) {
             set_error("event creation failed");
             st = CGS_ERR_CUDA;
         }
     }
-    if (st == CGS_OK && (cudaEventCreateWithFlags(&p->hc_fork, cudaEventDisableTiming) != cudaSuccess ||
-                         cudaEventCreateWithFlags(&p->hc_done, cudaEventDisableTiming) != cudaSuccess ||
-                         cudaStreamCreateWithFlags(&p->hc_in, cudaStreamNonBlocking) != cudaSuccess ||
-                         cudaStreamCreateWithFlags(&p->hc_out, cudaStreamNonBlocking) != cudaSuccess)) {
+    if (st == CGS_OK && (cudaEventCreateWithFlags(&h.fork, cudaEventDisableTiming) != cudaSuccess ||
+                         cudaEventCreateWithFlags(&h.done, cudaEventDisableTiming) != cudaSuccess ||
+                         cudaStreamCreateWithFlags(&h.in, cudaStreamNonBlocking) != cudaSuccess ||
+                         cudaStreamCreateWithFlags(&h.out, cudaStreamNonBlocking) != cudaSuccess)) {
         set_error("event or stream creation failed");
         st = CGS_ERR_CUDA;
     }
-    if (st != CGS_OK) drop_host_chunks(p);
+    if (st != CGS_OK) drop_chunk_set(h);
     return st;
 }
 
@@ -1588,34 +1602,34 @@ cgs_status cgs_sync(cgs_plan *p)
     return CGS_OK;
 }
 
-// The coil chunks of a host-buffer call.  Chunk q is copied in on hc_in
+// The coil chunks of a host-buffer call.  Chunk q is copied in on h.in
 // (after chunk q-1), transformed on its child's stream once its copy is in,
-// and copied out on hc_out (after chunk q-1's copy out) once its kernels are
+// and copied out on h.out (after chunk q-1's copy out) once its kernels are
 // done; `st` forks the work and waits for all of it.  `copy_in(q, stream)`
 // issues chunk q's host-to-device copy, `compute(q, stream)` its kernels and
 // `copy_out(q, stream)` its device-to-host copy (each may issue nothing).
 extern "C++" {
 template <class In, class Run, class Out>
-static cgs_status run_host_chunks(cgs_plan *p, cudaStream_t st, bool hout, In copy_in, Run compute, Out copy_out)
+static cgs_status run_host_chunks(HostChunks &h, cudaStream_t st, bool hout, In copy_in, Run compute, Out copy_out)
 {
-    const size_t C = p->hc.size();
-    CGS_CUDA(cudaEventRecord(p->hc_fork, st));
-    CGS_CUDA(cudaStreamWaitEvent(p->hc_in, p->hc_fork, 0));
-    CGS_CUDA(cudaStreamWaitEvent(p->hc_out, p->hc_fork, 0));
+    const size_t C = h.plans.size();
+    CGS_CUDA(cudaEventRecord(h.fork, st));
+    CGS_CUDA(cudaStreamWaitEvent(h.in, h.fork, 0));
+    CGS_CUDA(cudaStreamWaitEvent(h.out, h.fork, 0));
     for (size_t q = 0; q < C; ++q) {
-        CGS_TRY(copy_in(q, p->hc_in));
-        CGS_CUDA(cudaEventRecord(p->hc_copied[q], p->hc_in));
+        CGS_TRY(copy_in(q, h.in));
+        CGS_CUDA(cudaEventRecord(h.copied[q], h.in));
     }
     for (size_t q = 0; q < C; ++q) {
-        cudaStream_t s = p->hc[q]->stream;
-        CGS_CUDA(cudaStreamWaitEvent(s, p->hc_copied[q], 0));
+        cudaStream_t s = h.plans[q]->stream;
+        CGS_CUDA(cudaStreamWaitEvent(s, h.copied[q], 0));
         CGS_TRY(compute(q, s));
-        CGS_CUDA(cudaEventRecord(p->hc_computed[q], s));
-        CGS_CUDA(cudaStreamWaitEvent(p->hc_out, p->hc_computed[q], 0));
-        CGS_TRY(copy_out(q, p->hc_out));
+        CGS_CUDA(cudaEventRecord(h.computed[q], s));
+        CGS_CUDA(cudaStreamWaitEvent(h.out, h.computed[q], 0));
+        CGS_TRY(copy_out(q, h.out));
     }
-    CGS_CUDA(cudaEventRecord(p->hc_done, p->hc_out));
-    CGS_CUDA(cudaStreamWaitEvent(st, p->hc_done, 0));
+    CGS_CUDA(cudaEventRecord(h.done, h.out));
+    CGS_CUDA(cudaStreamWaitEvent(st, h.done, 0));
     if (hout) CGS_CUDA(cudaStreamSynchronize(st));
     return CGS_OK;
 }
@@ -1623,21 +1637,22 @@ static cgs_status run_host_chunks(cgs_plan *p, cudaStream_t st, bool hout, In co
 
 static cgs_status chunked_trafo(cgs_plan *p, const float *fhat, float *f, bool hin, bool hout, cudaStream_t st)
 {
-    auto src = [&](size_t q) { return (const float2 *)fhat + (int64_t)p->hc_c0[q] * p->Nt; };
-    auto out = [&](size_t q) { return (float2 *)f + (int64_t)p->hc_c0[q] * p->M; };
+    HostChunks &h = p->hcf;
+    auto src = [&](size_t q) { return (const float2 *)fhat + (int64_t)h.c0[q] * p->Nt; };
+    auto out = [&](size_t q) { return (float2 *)f + (int64_t)h.c0[q] * p->M; };
     return run_host_chunks(
-        p, st, hout,
+        h, st, hout,
         [&](size_t q, cudaStream_t s) -> cgs_status {
-            cgs_plan *c = p->hc[q];
+            cgs_plan *c = h.plans[q];
             if (hin) CGS_CUDA(cudaMemcpyAsync(c->ioA, src(q), sizeof(float2) * c->nc * p->Nt, cudaMemcpyHostToDevice, s));
             return CGS_OK;
         },
         [&](size_t q, cudaStream_t s) -> cgs_status {
-            cgs_plan *c = p->hc[q];
+            cgs_plan *c = h.plans[q];
             return op_forward(c, hin ? c->ioA : src(q), 2, nullptr, c->ksV, s, hout ? c->ioB : out(q));
         },
         [&](size_t q, cudaStream_t s) -> cgs_status {
-            cgs_plan *c = p->hc[q];
+            cgs_plan *c = h.plans[q];
             if (hout) CGS_CUDA(cudaMemcpyAsync(out(q), c->ioB, sizeof(float2) * c->nc * p->M, cudaMemcpyDeviceToHost, s));
             return CGS_OK;
         });
@@ -1656,9 +1671,9 @@ cgs_status cgs_nfft_trafo(cgs_plan *p, const float *fhat, float *f, void *stream
     }
     {
         const bool hin = !is_device_ptr(fhat), hout = !is_device_ptr(f);
-        const int C = host_chunk_count(p);
+        const int C = host_chunk_count(p, false);
         if ((hin || hout) && C > 1) {
-            CGS_TRY(build_host_chunks(p, C));
+            CGS_TRY(build_host_chunks(p, p->hcf, C));
             return chunked_trafo(p, fhat, f, hin, hout, st);
         }
     }
@@ -1715,22 +1730,23 @@ static cgs_status image_out(cgs_plan *p, const float2 *img, float *out, cudaStre
 
 static cgs_status chunked_adjoint(cgs_plan *p, const float *f, float *fhat, bool hin, bool hout, cudaStream_t st)
 {
-    auto src = [&](size_t q) { return (const float2 *)f + (int64_t)p->hc_c0[q] * p->M; };
-    auto out = [&](size_t q) { return (float2 *)fhat + (int64_t)p->hc_c0[q] * p->Nt; };
+    HostChunks &h = p->hca;
+    auto src = [&](size_t q) { return (const float2 *)f + (int64_t)h.c0[q] * p->M; };
+    auto out = [&](size_t q) { return (float2 *)fhat + (int64_t)h.c0[q] * p->Nt; };
     return run_host_chunks(
-        p, st, hout,
+        h, st, hout,
         [&](size_t q, cudaStream_t s) -> cgs_status {
-            cgs_plan *c = p->hc[q];
+            cgs_plan *c = h.plans[q];
             if (hin) CGS_CUDA(cudaMemcpyAsync(c->ioA, src(q), sizeof(float2) * c->nc * p->M, cudaMemcpyHostToDevice, s));
             return CGS_OK;
         },
         [&](size_t q, cudaStream_t s) -> cgs_status {
-            cgs_plan *c = p->hc[q];
+            cgs_plan *c = h.plans[q];
             CGS_TRY(launch_gather_ks(hin ? c->ioA : src(q), c->iperm, c->M, c->nc, c->ksY, s));
             return op_adjoint(c, c->ksY, 0, hout ? c->ioB : out(q), s, true);
         },
         [&](size_t q, cudaStream_t s) -> cgs_status {
-            cgs_plan *c = p->hc[q];
+            cgs_plan *c = h.plans[q];
             if (hout) CGS_CUDA(cudaMemcpyAsync(out(q), c->ioB, sizeof(float2) * c->nc * p->Nt, cudaMemcpyDeviceToHost, s));
             return CGS_OK;
         });
@@ -1748,9 +1764,9 @@ cgs_status cgs_nfft_adjoint(cgs_plan *p, const float *f, float *fhat, void *stre
     }
     {
         const bool hin = !is_device_ptr(f), hout = !is_device_ptr(fhat);
-        const int C = host_chunk_count(p);
+        const int C = host_chunk_count(p, true);
         if ((hin || hout) && C > 1) {
-            CGS_TRY(build_host_chunks(p, C));
+            CGS_TRY(build_host_chunks(p, p->hca, C));
             return chunked_adjoint(p, f, fhat, hin, hout, st);
         }
     }

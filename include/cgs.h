@@ -215,9 +215,10 @@ typedef struct {
                           (one frame): the coils are split into this many contiguous
                           chunks, each run by a child plan (sharing the plan's node
                           tables) on its own stream, so one chunk's host copies
-                          overlap another's kernels; 1 = one pass; default 2 when
-                          the k-space holds 8 MiB or more, else 1; at least 4 coils
-                          per chunk (no chunks below 8 coils).  Up to 32. */
+                          overlap another's kernels; 1 = one pass; default, when
+                          the k-space holds 8 MiB or more, 4 chunks for the forward
+                          and 2 for the adjoint, else 1; at least 4 coils per chunk
+                          (no chunks below 8 coils).  Up to 32. */
 } cgs_tuning;
 
 cgs_status cgs_get_tuning(const cgs_plan *plan, cgs_tuning *out);
