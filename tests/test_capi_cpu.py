@@ -62,3 +62,49 @@ def test_phantom_values():
     assert np.all(p.imag == 0)
     p3 = synth.phantom3d(32)
     assert p3.shape == (32, 32, 32) and p3.max().real <= 2.0 + 1e-6
+
+
+def header_struct_fields(name):
+    """(field, C type, array length) of `typedef struct {...} name;` in include/cgs.h, in order"""
+    txt = open(os.path.join(ROOT, "include", "cgs.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    m = re.search(r"typedef struct \{([^}]*)\}\s*" + name + r"\s*;", txt)
+    assert m, name
+    fields = []
+    for decl in m.group(1).split(";"):
+        decl = " ".join(decl.split())
+        if not decl:
+            continue
+        t, rest = re.match(r"((?:unsigned )?[a-z_0-9]+)\s+(.*)", decl).groups()
+        for var in rest.split(","):
+            v = re.match(r"\s*([A-Za-z_0-9]+)((?:\[\d+\])*)", var)
+            dims = [int(d) for d in re.findall(r"\[(\d+)\]", v.group(2))]
+            fields.append((v.group(1), t, dims))
+    return fields
+
+
+def test_ctypes_structures_mirror_the_header():
+    """Every ctypes structure of the Python binding lists the header's fields
+    in the header's order with the same C types (a missing field would shift
+    every later one across the boundary)."""
+    import ctypes as C
+    from codeare_gb300 import capi
+    ctype = {"int": C.c_int, "double": C.c_double, "float": C.c_float, "int64_t": C.c_int64}
+    pairs = [(capi.PlanDesc, "cgs_plan_desc"), (capi.SolveOpts, "cgs_solve_opts"),
+             (capi.SolveReport, "cgs_solve_report"), (capi.Tuning, "cgs_tuning"),
+             (capi.CsOpts, "cgs_cs_opts"), (capi.CsReport, "cgs_cs_report")]
+    for cls, name in pairs:
+        hdr = header_struct_fields(name)
+        py = cls._fields_
+        assert len(py) == len(hdr), (name, [f for f, _ in py], [f for f, _, _ in hdr])
+        for (pf, pt), (hf, ht, dims) in zip(py, hdr):
+            # `lambda` is a Python keyword: the binding spells it lam or lambda_
+            assert {"lam": "lambda"}.get(pf, pf.rstrip("_")) == hf, (name, pf, hf)
+            want = ctype[ht]
+            for d in reversed(dims):
+                want = want * d
+            assert C.sizeof(pt) == C.sizeof(want), (name, hf)
+            base = pt
+            while hasattr(base, "_type_") and hasattr(base, "_length_"):
+                base = base._type_
+            assert base == ctype[ht], (name, hf, base, ht)
