@@ -9,6 +9,7 @@
 // mask and the deapodisation 1/phihut (NFFT3's PRE_PHI_HUT step), and the last
 // inverse pass fuses the deapodisation: the FFT-side work of the reference's
 // nfft_trafo / nfft_adjoint (src/matrix/ft/NFFTTraits.hpp:176-204).
+#include <atomic>
 #include <type_traits>
 
 #include "cgs_internal.cuh"
@@ -20,6 +21,23 @@ namespace cgs {
 namespace {
 
 constexpr int kThreads = 256;
+
+// Kernel attributes hold per device: `devs` has bit d set once device d's
+// attributes are set (a process may drive plans on several devices, from
+// several threads).
+inline bool attr_needed(const std::atomic<uint64_t> &devs)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return !(devs.load(std::memory_order_acquire) & (1ull << (dev & 63)));
+}
+
+inline void attr_done(std::atomic<uint64_t> &devs)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    devs.fetch_or(1ull << (dev & 63), std::memory_order_release);
+}
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
@@ -735,13 +753,13 @@ cgs_status launch_ct(const AxisPass &p, cudaStream_t st)
     const int64_t nblocks = nib * nob;
     if (nblocks > 0x7fffffffLL) { set_error("axis pass grid too large"); return CGS_ERR_BAD_ARG; }
     const size_t smem = ((size_t)N + (size_t)ct_rows<N, LOGB>() * B) * sizeof(float2);
-    static bool attr_set = false;
-    if (!attr_set) {
+    static std::atomic<uint64_t> attr_devs{0};
+    if (attr_needed(attr_devs)) {
         CGS_CUDA(cudaFuncSetAttribute(axis_fft_ct_kernel<N, LOGB, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
         CGS_CUDA(cudaFuncSetAttribute(axis_fft_ct_kernel<N, LOGB, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-        attr_set = true;
+        attr_done(attr_devs);
     }
     if (p.sign < 0) axis_fft_ct_kernel<N, LOGB, -1><<<(unsigned)nblocks, kThreads, smem, st>>>(p, logBI, nib);
     else axis_fft_ct_kernel<N, LOGB, +1><<<(unsigned)nblocks, kThreads, smem, st>>>(p, logBI, nib);
@@ -809,13 +827,13 @@ cgs_status launch_axis_pass(const AxisPass &p, cudaStream_t st)
         prof_end(PROF_FFT, st);
         return r;
     }
-    static bool attr_set = false;
-    if (!attr_set) {
+    static std::atomic<uint64_t> attr_devs{0};
+    if (attr_needed(attr_devs)) {
         CGS_CUDA(cudaFuncSetAttribute(axis_fft_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       110 * 1024));
         CGS_CUDA(cudaFuncSetAttribute(axis_fft_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       110 * 1024));
-        attr_set = true;
+        attr_done(attr_devs);
     }
     const int64_t nblocks = nib * nob;
     if (nblocks > 0x7fffffffLL) { set_error("axis pass grid too large"); return CGS_ERR_BAD_ARG; }
