@@ -161,6 +161,7 @@ struct HostChunks {
     cudaStream_t in = nullptr, out = nullptr;
     cudaEvent_t fork = nullptr, done = nullptr;
     std::vector<cudaEvent_t> copied, computed;
+    bool sens = false;    // the children hold their coils of the parent's sensitivities
 };
 
 struct cgs_plan {
@@ -1309,6 +1310,7 @@ static void drop_chunk_set(HostChunks &h)
     for (cudaEvent_t e : h.computed) cudaEventDestroy(e);
     h.copied.clear();
     h.computed.clear();
+    h.sens = false;
     for (cudaEvent_t *e : {&h.fork, &h.done})
         if (*e) { cudaEventDestroy(*e); *e = nullptr; }
     for (cudaStream_t *st : {&h.in, &h.out})
@@ -1400,6 +1402,21 @@ static cgs_status build_host_chunks(cgs_plan *p, HostChunks &h, int C)
     }
     if (st != CGS_OK) drop_chunk_set(h);
     return st;
+}
+
+// each chunk's coils of the parent's sensitivities ([p][NC] -> [p][nq])
+static cgs_status chunk_sensitivities(cgs_plan *p, HostChunks &h)
+{
+    if (h.sens) return CGS_OK;
+    for (size_t q = 0; q < h.plans.size(); ++q) {
+        cgs_plan *c = h.plans[q];
+        CGS_CUDA(cudaMemcpy2DAsync(c->sens, sizeof(float2) * c->nc, p->sens + h.c0[q], sizeof(float2) * p->nc,
+                                   sizeof(float2) * c->nc, p->Nt, cudaMemcpyDeviceToDevice, p->stream));
+        c->have_s = true;
+    }
+    CGS_CUDA(cudaStreamSynchronize(p->stream));
+    h.sens = true;
+    return CGS_OK;
 }
 
 cgs_status cgs_plan_destroy(cgs_plan *p)
@@ -1587,6 +1604,7 @@ cgs_status cgs_set_sensitivities(cgs_plan *p, const float *s_in)
     }
     cudaStream_t st = p->stream;
     const void *src;
+    p->hcf.sens = p->hca.sens = false;  // the chunks copy the new maps on their next use
     CGS_TRY(stage_in(s_in, sizeof(float2) * p->Nt * p->nc, p->ioA, &src, st));
     CGS_TRY(launch_to_coil_minor((const float2 *)src, p->Nt, p->nc, p->sens, st));
     CGS_TRY(launch_intensity(p->sens, p->Nt, p->nc, p->imap, st));
@@ -1798,6 +1816,27 @@ cgs_status cgs_nfft_itrafo(cgs_plan *p, const float *f, float *fhat, int maxit, 
     return coil_images_out(p, p->cF, fhat, st);
 }
 
+// SENSE forward into the caller's host k-space by coil chunks: the image is
+// staged once on `st`, each chunk expands it with its coils' sensitivities
+// and interpolates while the previous chunk's samples go to the host.
+static cgs_status chunked_sense_trafo(cgs_plan *p, const float2 *xs, float *y, cudaStream_t st)
+{
+    HostChunks &h = p->hcf;
+    auto out = [&](size_t q) { return (float2 *)y + (int64_t)h.c0[q] * p->M; };
+    return run_host_chunks(
+        h, st, true,
+        [&](size_t, cudaStream_t) -> cgs_status { return CGS_OK; },
+        [&](size_t q, cudaStream_t s) -> cgs_status {
+            cgs_plan *c = h.plans[q];
+            return op_forward(c, xs, 0, nullptr, c->ksV, s, c->ioB);
+        },
+        [&](size_t q, cudaStream_t s) -> cgs_status {
+            cgs_plan *c = h.plans[q];
+            CGS_CUDA(cudaMemcpyAsync(out(q), c->ioB, sizeof(float2) * c->nc * p->M, cudaMemcpyDeviceToHost, s));
+            return CGS_OK;
+        });
+}
+
 cgs_status cgs_sense_trafo(cgs_plan *p, const float *x, float *y, void *stream)
 {
     CGS_TRY(check_ready(p, false, true));
@@ -1805,6 +1844,14 @@ cgs_status cgs_sense_trafo(cgs_plan *p, const float *x, float *y, void *stream)
     cudaStream_t st = pick_stream(p, stream);
     const void *src;
     CGS_TRY(stage_in(x, sizeof(float2) * p->Nt, p->ioA, &src, st));
+    if (!is_device_ptr(y)) {
+        const int C = host_chunk_count(p, false);
+        if (C > 1) {
+            CGS_TRY(build_host_chunks(p, p->hcf, C));
+            CGS_TRY(chunk_sensitivities(p, p->hcf));
+            return chunked_sense_trafo(p, (const float2 *)src, y, st);
+        }
+    }
     const bool dev = is_device_ptr(y);
     float2 *dst = dev ? (float2 *)y : p->ioB;
     CGS_TRY(op_forward(p, (const float2 *)src, 0, nullptr, p->ksV, st, dst));

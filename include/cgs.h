@@ -211,8 +211,9 @@ typedef struct {
                           cores (16 nodes of a 4 x 4 footprint-start bin per warp,
                           TF32-split operands, FP32 accumulation); default 16 from 4
                           coils for m <= 4, else 1 */
-    int host_chunks;   /* cgs_nfft_trafo / cgs_nfft_adjoint with a host input or output
-                          (one frame): the coils are split into this many contiguous
+    int host_chunks;   /* cgs_nfft_trafo / cgs_nfft_adjoint with a host input or output,
+                          cgs_sense_trafo with a host output (one frame): the coils
+                          are split into this many contiguous
                           chunks, each run by a child plan (sharing the plan's node
                           tables) on its own stream, so one chunk's host copies
                           overlap another's kernels; 1 = one pass; default, when

@@ -348,3 +348,35 @@ def test_mixed_radix_passes_repeat_bit_for_bit(gpu, N):
     for _ in range(6):
         f1, a1 = nfft_pair(p, N, nc, k.shape[0], seed=3)
         assert np.array_equal(f1, f0) and np.array_equal(a1, a0)
+
+
+def test_host_buffer_sense_trafo_coil_chunks(gpu):
+    """E x into a host k-space through coil chunks (each chunk's coils of the
+    sensitivities copied to its child) against the one-pass device path, also
+    after the sensitivities change."""
+    import torch
+    from codeare_gb300 import capi, synth
+    N, nc = 64, 16
+    k = synth.radial2d(48, 128, golden=True)
+    M = k.shape[0]
+    p, S = make_plan(N, nc, k, synth.ramp_weights(k))
+    x = synth.phantom(N).astype(np.complex64)
+    dev = torch.device("cuda:0")
+
+    def device_path():
+        y_d = torch.zeros((nc, M), dtype=torch.complex64, device=dev)
+        p.sense_trafo(torch.from_numpy(x).to(dev), y_d)
+        torch.cuda.synchronize()
+        return y_d.cpu().numpy()
+
+    y_ref = device_path()
+    p.set_tuning(host_chunks=4)
+    y = np.zeros((nc, M), np.complex64)
+    p.sense_trafo(x, y)
+    assert rel(y, y_ref) < 1e-6
+    S2 = np.ascontiguousarray(np.conj(S) * 0.5, np.complex64)
+    p.set_sensitivities(S2)
+    y2_ref = device_path()
+    y2 = np.zeros((nc, M), np.complex64)
+    p.sense_trafo(x, y2)
+    assert rel(y2, y2_ref) < 1e-6 and rel(y2, y_ref) > 1e-2
