@@ -1626,6 +1626,9 @@ cgs_status cgs_sync(cgs_plan *p)
 // done; `st` forks the work and waits for all of it.  `copy_in(q, stream)`
 // issues chunk q's host-to-device copy, `compute(q, stream)` its kernels and
 // `copy_out(q, stream)` its device-to-host copy (each may issue nothing).
+// Every chunk's kernels are queued before the first copy out: a copy with
+// pageable host memory returns only once it is done (to pageable memory) or
+// staged (from it), and the kernels queued before it keep the GPU busy.
 extern "C++" {
 template <class In, class Run, class Out>
 static cgs_status run_host_chunks(HostChunks &h, cudaStream_t st, bool hout, In copy_in, Run compute, Out copy_out)
@@ -1637,12 +1640,12 @@ static cgs_status run_host_chunks(HostChunks &h, cudaStream_t st, bool hout, In 
     for (size_t q = 0; q < C; ++q) {
         CGS_TRY(copy_in(q, h.in));
         CGS_CUDA(cudaEventRecord(h.copied[q], h.in));
-    }
-    for (size_t q = 0; q < C; ++q) {
         cudaStream_t s = h.plans[q]->stream;
         CGS_CUDA(cudaStreamWaitEvent(s, h.copied[q], 0));
         CGS_TRY(compute(q, s));
         CGS_CUDA(cudaEventRecord(h.computed[q], s));
+    }
+    for (size_t q = 0; q < C; ++q) {
         CGS_CUDA(cudaStreamWaitEvent(h.out, h.computed[q], 0));
         CGS_TRY(copy_out(q, h.out));
     }
