@@ -170,14 +170,6 @@ __device__ __forceinline__ int out_axis_to_pos(int a, int Lout, int n, int centr
     return a < h ? n - h + a : a - h;
 }
 
-__device__ __forceinline__ float deapod(const AxisPass &p, int64_t o, int a)
-{
-    float d = p.deap_ax ? p.deap_ax[a] : 1.f;
-    if (p.deap_o1) d *= p.deap_o1[o % p.o1_len];
-    if (p.deap_o0) d *= p.deap_o0[o / p.o1_len];
-    return d;
-}
-
 // MIXED = false: radices 8/4/2 only, every size a power of two, index math by
 // shifts; MIXED = true: also radices 3/5/7 with general division
 template <bool MIXED>

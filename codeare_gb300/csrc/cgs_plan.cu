@@ -1895,7 +1895,6 @@ cgs_status cgs_solve(cgs_plan *p, const float *y, float *x, const cgs_solve_opts
     if (!x || !y || o->cgiter < 0 || o->ftiter < 0) { set_error("bad argument"); return CGS_ERR_BAD_ARG; }
     if (p->F > 1 && !codeare && o->toeplitz) { set_error("the Toeplitz operator is not built for frames"); return CGS_ERR_BAD_ARG; }
     cudaStream_t st = pick_stream(p, stream);
-    const int64_t Nt = p->Nt;
     if (rep) { std::memset(rep, 0, sizeof(*rep)); rep->fallback_at = -1; }
     if (!codeare && o->toeplitz) {
         const int wtd = (o->weighted && p->have_w) ? 1 : 0;

@@ -15,17 +15,13 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kDotBlocks = 304;  // 2 x 152 SMs
 
-__device__ __forceinline__ float2 cmul(float2 a, float2 b)
-{
-    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-
-// user[c][perm[s]] -> ks[s][c]
 // Caller layout (coil-major, trajectory order) <-> device layout (bin order,
-// coil innermost) through 32 x 32 shared-memory tiles: the device side is
-// read or written in contiguous coil runs, the caller side along 32 sorted
-// positions of one coil, whose trajectory indices perm[s] come in runs (the
-// bin sort is stable, so a spoke's consecutive samples stay together).
+// coil innermost) through 32 x 32 shared-memory tiles.  The gather
+// (user[c][j] -> ks[iperm[j]][c]) reads 32 consecutive trajectory nodes of a
+// coil and writes each node's run of coils at its sorted position; the
+// scatter (ks[s][c] -> user[c][perm[s]]) reads contiguous coil runs and
+// writes 32 sorted positions of a coil, whose trajectory indices come in runs
+// (the bin sort is stable, so a spoke's consecutive samples stay together).
 __global__ void gather_ks_kernel(const float2 *__restrict__ user, const int *__restrict__ iperm,
                                  int64_t M, int nc, float2 *__restrict__ ks)
 {
