@@ -509,6 +509,8 @@ def run_ours(args):
         traffic = tj.get(dom)
     except Exception:
         pass
+    for v in per_kernel.values():  # each kernel against the same HBM denominator
+        v["frac_of_hbm"] = v["GBps"] / hbm
     roofline = None
     if dom:
         a = per_kernel[dom]["GBps"]
