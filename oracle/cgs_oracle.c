@@ -197,6 +197,11 @@ typedef struct {
     double *phihut_inv[3]; /* 1/phihut(k) for k = -N/2 .. N/2-1 */
     double *x;             /* M*d */
     size_t Ntot, ntot;
+    /* per node and dimension, the 2m+2 window values and wrapped grid indices,
+     * computed once per trajectory as NFFT3's PRE_PSI does for codeare's plans
+     * (src/matrix/ft/NFFTTraits.hpp:68-69); NULL when they would exceed 1 GiB */
+    double *psi;
+    int *psi_idx;
 } orc_nfft;
 
 orc_nfft *orc_nfft_create(int d, const int *N, const int *n, int m, long M)
@@ -222,16 +227,13 @@ void orc_nfft_destroy(orc_nfft *p)
     if (!p) return;
     for (int t = 0; t < p->d; ++t) free(p->phihut_inv[t]);
     free(p->x);
+    free(p->psi);
+    free(p->psi_idx);
     free(p);
 }
 
-void orc_nfft_set_x(orc_nfft *p, const double *x)
-{
-    memcpy(p->x, x, sizeof(double) * (size_t)p->M * (size_t)p->d);
-}
-
-/* tap positions and weights of node j along dimension t */
-static void node_taps(const orc_nfft *p, long j, int t, int *idx, double *w)
+/* tap positions and weights of node j along dimension t, evaluated */
+static void node_taps_eval(const orc_nfft *p, long j, int t, int *idx, double *w)
 {
     const int n = p->n[t], m = p->m;
     const double nx = (double)n * p->x[(size_t)j * p->d + t];
@@ -242,6 +244,39 @@ static void node_taps(const orc_nfft *p, long j, int t, int *idx, double *w)
         long q = l % n; if (q < 0) q += n;
         idx[i] = (int)q;
     }
+}
+
+void orc_nfft_set_x(orc_nfft *p, const double *x)
+{
+    memcpy(p->x, x, sizeof(double) * (size_t)p->M * (size_t)p->d);
+    free(p->psi); free(p->psi_idx);
+    p->psi = NULL; p->psi_idx = NULL;
+    const size_t T = (size_t)(2 * p->m + 2), cnt = (size_t)p->M * (size_t)p->d * T;
+    if (cnt * (sizeof(double) + sizeof(int)) > ((size_t)1 << 30)) return;
+    p->psi = (double *)malloc(sizeof(double) * (cnt > 0 ? cnt : 1));
+    p->psi_idx = (int *)malloc(sizeof(int) * (cnt > 0 ? cnt : 1));
+    if (!p->psi || !p->psi_idx) { free(p->psi); free(p->psi_idx); p->psi = NULL; p->psi_idx = NULL; return; }
+#pragma omp parallel for schedule(static)
+    for (long j = 0; j < p->M; ++j)
+        for (int t = 0; t < p->d; ++t) {
+            const size_t o = ((size_t)j * (size_t)p->d + (size_t)t) * T;
+            node_taps_eval(p, j, t, p->psi_idx + o, p->psi + o);
+        }
+}
+
+/* tap positions and weights of node j along dimension t: the precomputed
+ * tables, or evaluated into the caller's buffers */
+static void node_taps(const orc_nfft *p, long j, int t, const int **idx, const double **w, int *ib, double *wb)
+{
+    if (p->psi) {
+        const size_t o = ((size_t)j * (size_t)p->d + (size_t)t) * (size_t)(2 * p->m + 2);
+        *idx = p->psi_idx + o;
+        *w = p->psi + o;
+        return;
+    }
+    node_taps_eval(p, j, t, ib, wb);
+    *idx = ib;
+    *w = wb;
 }
 
 static void unravel(size_t flat, int d, const int *dims, int *out)
@@ -275,9 +310,10 @@ void orc_nfft_trafo(const orc_nfft *p, const double *fhat_in, double *f_out)
     }
     fft_nd(g, p->d, p->n, -1);
     const int T = 2 * p->m + 2;
-    int idx[3][64]; double w[3][64];
+    int ib[3][64]; double wb[3][64];
+    const int *idx[3]; const double *w[3];
     for (long j = 0; j < p->M; ++j) {
-        for (int t = 0; t < p->d; ++t) node_taps(p, j, t, idx[t], w[t]);
+        for (int t = 0; t < p->d; ++t) node_taps(p, j, t, &idx[t], &w[t], ib[t], wb[t]);
         cplx acc = 0;
         if (p->d == 1) {
             for (int a = 0; a < T; ++a) acc += g[idx[0][a]] * w[0][a];
@@ -312,9 +348,10 @@ void orc_nfft_adjoint(const orc_nfft *p, const double *f_in, double *fhat_out)
     cplx *fhat = (cplx *)fhat_out;
     cplx *g = (cplx *)calloc(p->ntot, sizeof(cplx));
     const int T = 2 * p->m + 2;
-    int idx[3][64]; double w[3][64];
+    int ib[3][64]; double wb[3][64];
+    const int *idx[3]; const double *w[3];
     for (long j = 0; j < p->M; ++j) {
-        for (int t = 0; t < p->d; ++t) node_taps(p, j, t, idx[t], w[t]);
+        for (int t = 0; t < p->d; ++t) node_taps(p, j, t, &idx[t], &w[t], ib[t], wb[t]);
         const cplx fj = f[j];
         if (p->d == 1) {
             for (int a = 0; a < T; ++a) g[idx[0][a]] += fj * w[0][a];
