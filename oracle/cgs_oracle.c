@@ -123,7 +123,7 @@ static void fft_exec(const fftplan *p, cplx *x, cplx *work, int sign)
             const int k = j % Ns;
             for (int r = 0; r < R; ++r) {
                 cplx a = src[j + r * nR];
-                int t = (int)(((int64_t)k * r * step) % n);
+                const int t = k * r * step;  /* < Ns R step = n */
                 cplx w = (sign < 0) ? p->tw[t] : conj(p->tw[t]);
                 v[r] = a * w;
             }
@@ -166,14 +166,20 @@ static void fft_nd(cplx *a, int d, const int *n, int sign)
         for (int u = 0; u < t; ++u) outer *= (size_t)n[u];
         const int L = n[t];
         fftplan p; fft_plan_init(&p, L);
-        cplx *line = (cplx *)malloc(sizeof(cplx) * (size_t)L * 2);
-        cplx *work = line + L;
+        /* up to CB adjacent columns are gathered per pass, so every strided
+         * row access reads CB consecutive values instead of one */
+        enum { CB = 8 };
+        cplx *line = (cplx *)malloc(sizeof(cplx) * (size_t)L * (CB + 1));
+        cplx *work = line + (size_t)L * CB;
         for (size_t o = 0; o < outer; ++o)
-            for (size_t i = 0; i < inner; ++i) {
-                cplx *base = a + o * (size_t)L * inner + i;
-                for (int l = 0; l < L; ++l) line[l] = base[(size_t)l * inner];
-                fft_exec(&p, line, work, sign);
-                for (int l = 0; l < L; ++l) base[(size_t)l * inner] = line[l];
+            for (size_t i0 = 0; i0 < inner; i0 += CB) {
+                const int cb = (int)((inner - i0) < CB ? (inner - i0) : CB);
+                cplx *base = a + o * (size_t)L * inner + i0;
+                for (int l = 0; l < L; ++l)
+                    for (int c = 0; c < cb; ++c) line[(size_t)c * L + l] = base[(size_t)l * inner + c];
+                for (int c = 0; c < cb; ++c) fft_exec(&p, line + (size_t)c * L, work, sign);
+                for (int l = 0; l < L; ++l)
+                    for (int c = 0; c < cb; ++c) base[(size_t)l * inner + c] = line[(size_t)c * L + l];
             }
         free(line);
         fft_plan_free(&p);
