@@ -16,7 +16,8 @@ deapodise/pad, FFT, interpolation; spreading, FFT, crop/deapodise) / time.
 C ABI, L2 flushed before each timed step); `e2e` is the same metric through
 the C ABI with pinned HOST buffers, host<->device copies inside the timed
 region.  The reference arm times the FP64 CPU restatement of the reference's
-NFFT3 path (oracle/, the reference itself cannot be built: see the design doc).
+NFFT3 path (oracle/): the reference itself needs NFFT3, FFTW, Boost and its
+CMake build, none of which this image has.
 """
 from __future__ import annotations
 
