@@ -1,7 +1,7 @@
 """FP64 restatement of codeare's compressed sensing over the NCSENSE operator.
 
-TEST INFRASTRUCTURE ONLY: imported by tests/ as the checker of the CUDA
-path, never by the product package.
+TEST INFRASTRUCTURE ONLY: imported by tests/, which compare the CUDA path
+against it; never by the product package.
 
 PARITY UNPINNED: the reference ships no test or golden vector for its CS
 code; this restates the reference's source line by line, in FP64, on top of
