@@ -1,5 +1,5 @@
 #!/usr/bin/env python
-"""Benchmark of the NuFFT operator on the config-1 workload.
+"""Benchmark of the NuFFT operator on the 256^2, 32-coil golden-angle radial workload.
 
 Workload (one "step"): the per-coil NFFT forward (32 coil images -> k-space)
 followed by the per-coil adjoint (k-space -> 32 coil images) of a 256^2 image,
@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 METRIC = "NuFFT GB/s (per-coil NFFT forward + adjoint)"
 UNIT = "GB/s"
 N, NC, SPOKES, SAMPLES, SIGMA, M_KB = 256, 32, 403, 512, 2.0, 4
-WORKLOAD = ("config 1: NuFFT forward+adjoint, 256^2 image x 32 coils, golden-angle radial "
+WORKLOAD = ("NuFFT forward+adjoint, 256^2 image x 32 coils, golden-angle radial "
             "403x512 (M=206336), sigma=2 (512^2 grid), KB m=4")
 
 
@@ -174,7 +174,7 @@ def run_reference(args):
 
 
 def cgsense_section(cpu_too: bool):
-    """Config 0: 128^2 Shepp-Logan, 8 coils, 96 uniform spokes x 256, sigma=2, m=4.
+    """CG-SENSE on 128^2 Shepp-Logan, 8 coils, 96 uniform spokes x 256, sigma=2, m=4.
     Times (GPU, inputs already on the device through the C ABI):
       - codeare mode (CGLS over the CGNR-based E^H), 10 iterations, lambda = 5e-2;
       - standard mode (true adjoint) to ||r||/||r0|| = 1e-4, with E^H W E applied by the
@@ -183,7 +183,7 @@ def cgsense_section(cpu_too: bool):
     import torch
     import codeare_gb300 as cg
     from codeare_gb300 import synth
-    c = synth.config0()
+    c = synth.radial2d_128_8coils()
     N, nc = c["shape"][0], c["sens"].shape[0]
     k, w, S = c["k"], c["w"], c["sens"]
     M = k.shape[0]
@@ -197,7 +197,7 @@ def cgsense_section(cpu_too: bool):
     y = synth.add_noise(y, c["noise"], seed=c["seed"])
     yd = torch.from_numpy(y).cuda()
     xd = torch.zeros((N, N), dtype=torch.complex64, device="cuda")
-    out = {"workload": "config 0: 128^2, 8 coils, 96x256 uniform radial, sigma=2, m=4, 1e-3 noise"}
+    out = {"workload": "128^2, 8 coils, 96x256 uniform radial, sigma=2, m=4, 1e-3 noise"}
 
     def timed(**kw):
         p.solve(yd, xd, **kw)  # warm-up (and Toeplitz kernel build)
@@ -233,7 +233,7 @@ def cgsense_section(cpu_too: bool):
 
 def cs_section(cpu_too: bool):
     """Compressed sensing over NCSENSE (the CompressedSensing module, ft = 3) on
-    the config-0 input: 128^2, 8 coils, 96x256 uniform spokes, sigma=2, m=4,
+    the 128^2 radial input: 128^2, 8 coils, 96x256 uniform spokes, sigma=2, m=4,
     with the reference's example CS settings (csiter 2, 8 NLCG iterations,
     10 line-search steps, lsa 0.01, lsb 0.6, TV 0.002, L1 0.005, p = 1,
     l1 1e-15, Daubechies 4) and a 10-iteration codeare CGLS inside every
@@ -244,7 +244,7 @@ def cs_section(cpu_too: bool):
     import torch
     import codeare_gb300 as cg
     from codeare_gb300 import synth
-    c = synth.config0()
+    c = synth.radial2d_128_8coils()
     N, nc = c["shape"][0], c["sens"].shape[0]
     k, w, S = c["k"], c["w"], c["sens"]
     M = k.shape[0]
@@ -273,7 +273,7 @@ def cs_section(cpu_too: bool):
         if best is None or wall < best[0]:
             best = (wall, rep)
     wall, rep = best
-    out = {"workload": "CompressedSensing ft=3 on config 0 (128^2, 8 coils, 96x256 radial, sigma=2, m=4), "
+    out = {"workload": "CompressedSensing ft=3 on the 128^2 radial case (128^2, 8 coils, 96x256 radial, sigma=2, m=4), "
                        "reference example settings, Daubechies 4",
            "wall_ms": wall * 1e3, "device_ms": rep["seconds"] * 1e3, "nlcg_iterations": rep["iterations"],
            "solves": rep["solves"], "cg_iterations": rep["solve_iterations"],
@@ -296,14 +296,14 @@ def cs_section(cpu_too: bool):
 
 
 def batch_section():
-    """Config 2: 64 uneven CG-SENSE problems (N 96..320, 4-32 coils, radial and
+    """Batch of 64 uneven CG-SENSE problems (N 96..320, 4-32 coils, radial and
     spiral trajectories), codeare-mode CGLS with 15 iterations each, as one
     graph launch (cgs_batch) and as 64 consecutive per-plan solves; the
     autotuner runs on every plan first."""
     import torch
     import codeare_gb300 as cg
     from codeare_gb300 import capi, synth
-    probs = synth.config2()
+    probs = synth.uneven_batch()
     t0 = time.perf_counter()
     plans, ys, xs = [], [], []
     for c in probs:
@@ -333,7 +333,7 @@ def batch_section():
     b.solve(ys, xs)
     t_batch = min(b.solve(ys, xs)[1] for _ in range(3))
     b.close()
-    out = {"workload": "config 2: 64 problems, N 96..320, 4/8/16/32 coils, golden-angle radial 32..400 x 512 "
+    out = {"workload": "64 uneven problems, N 96..320, 4/8/16/32 coils, golden-angle radial 32..400 x 512 "
                        "or VD spiral 16 x 4096, codeare CGLS 15 iterations (lambda 5e-2, 3 inner steps)",
            "problems": len(plans), "coil_samples": int(sum(c["k"].shape[0] * c["nc"] for c in probs)),
            "batch_ms": t_batch * 1e3, "sequential_ms": t_seq * 1e3, "problems_per_s": len(plans) / t_batch,
@@ -343,15 +343,15 @@ def batch_section():
     return out
 
 
-def config3_section():
-    """Config 3: 3-D kooshball CG-SENSE, 128^3, 16 coils, 20000 x 256 spokes,
+def kooshball_section():
+    """3-D kooshball CG-SENSE, 128^3, 16 coils, 20000 x 256 spokes,
     standard CG with the Toeplitz-embedded E^H W E (256^3 FFTs) to
     ||r||/||r0|| = 1e-4.  Reports the one-off costs (binning, E^H y, the
     Toeplitz kernel) apart from the iterations."""
     import torch
     import codeare_gb300 as cg
     from codeare_gb300 import capi, synth
-    c = synth.config3()
+    c = synth.kooshball3d_128_16coils()
     N, nc = c["shape"][0], c["sens"].shape[0]
     k = c["k"]
     M = k.shape[0]
@@ -383,7 +383,7 @@ def config3_section():
             best = r
     p.close()
     it = best["iterations"]
-    return {"workload": "config 3: 128^3, 16 coils, kooshball 20000 x 256, |k|^2 weights, sigma=2, m=4, "
+    return {"workload": "3-D kooshball 128^3, 16 coils, kooshball 20000 x 256, |k|^2 weights, sigma=2, m=4, "
                         "Toeplitz 256^3, standard CG to 1e-4",
             "M": M, "plan_s": t_plan, "eh_y_ms": t_eh * 1e3, "toeplitz_build_and_first_solve_ms": t_first * 1e3,
             "iterations": it, "res_last": best["res_last"], "solve_ms": best["seconds"] * 1e3,
@@ -391,7 +391,7 @@ def config3_section():
 
 
 def learned_section():
-    """Config 4: learned-preconditioned flexible CG against plain GPU CG (and
+    """Learned-preconditioned flexible CG against plain GPU CG (and
     Jacobi CG) to relative residual 1e-4 on a held-out 256^2, 16-coil
     golden-angle problem, with each image's error against the converged plain
     solve.  Uses the committed trained weights; null when they are absent."""
@@ -401,7 +401,7 @@ def learned_section():
         return None
     r = learned.compare(net, seed=777)
     net.close()
-    r["workload"] = ("config 4: 256^2, 16 coils, golden-angle radial x 512, random-ellipse phantom, "
+    r["workload"] = ("learned preconditioner: 256^2, 16 coils, golden-angle radial x 512, random-ellipse phantom, "
                      "Toeplitz E^H W E, lambda = 1e-3 mean diagonal, to ||r||/||r0|| = 1e-4")
     r["speedup_vs_plain"] = r["plain"]["ms"] / r["learned"]["ms"]
     return r
@@ -558,14 +558,14 @@ def run_ours(args):
     cgs_part = None
     learned_part = None
     batch_part = None
-    cfg3_part = None
+    kooshball_part = None
     cs_part = None
     if rank == 0 and not args.no_cgsense:
         cgs_part = cgsense_section(cpu_too=(ws == 1 and not args.no_cpu))
         cs_part = cs_section(cpu_too=(ws == 1 and not args.no_cpu))
         learned_part = learned_section()
         batch_part = batch_section()
-        cfg3_part = config3_section()
+        kooshball_part = kooshball_section()
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -577,7 +577,7 @@ def run_ours(args):
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "roofline": roofline, "kernels": per_kernel, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clk, "gpu_launches": launches, "cgsense": cgs_part, "learned_fcg": learned_part,
-            "batch": batch_part, "config3": cfg3_part, "compressed_sensing": cs_part,
+            "batch": batch_part, "kooshball3d": kooshball_part, "compressed_sensing": cs_part,
         }
         print(json.dumps(line))
     if ws > 1:
@@ -595,7 +595,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default gridding decomposition (profiling runs: no candidate launches)")
-    ap.add_argument("--no-cgsense", action="store_true", help="skip the config-0, 2, 3 and 4 CG-SENSE sections and the CS section")
+    ap.add_argument("--no-cgsense", action="store_true", help="skip the CG-SENSE, batch, kooshball, learned-preconditioner and CS sections")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

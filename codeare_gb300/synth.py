@@ -182,25 +182,25 @@ def add_noise(y: np.ndarray, rel: float, seed: int) -> np.ndarray:
     return (y + s * n).astype(np.complex64)
 
 
-def config0():
+def radial2d_128_8coils():
     """128^2 Shepp-Logan, 8 coils, 96 uniform spokes x 256, sigma=2, m=4, 10 CG iterations."""
     N, nc = 128, 8
     k = radial2d(96, 256)
-    return dict(name="cfg0_radial2d_128_8c", shape=(N, N), image=phantom(N), sens=coils2d(N, nc),
+    return dict(name="radial2d_128_8c", shape=(N, N), image=phantom(N), sens=coils2d(N, nc),
                 k=k, w=ramp_weights(k), alpha=2.0, m=4, cgiter=10, cgeps=1e-6,
                 noise=1e-3, seed=SEED_BASE + 0)
 
 
-def config1():
+def radial2d_256_32coils():
     """NuFFT operator alone: 256^2, 32 coils, golden-angle 403 x 512, sigma=2, m=4."""
     N, nc = 256, 32
     k = radial2d(403, 512, golden=True)
-    return dict(name="cfg1_nufft_256_32c_ga403x512", shape=(N, N), image=phantom(N),
+    return dict(name="nufft_256_32c_ga403x512", shape=(N, N), image=phantom(N),
                 sens=coils2d(N, nc), k=k, w=ramp_weights(k), alpha=2.0, m=4,
                 seed=SEED_BASE + 1)
 
 
-def config3(N: int = 128, nc: int = 16, nspokes: int = 20000, nsamp: int = 256):
+def kooshball3d_128_16coils(N: int = 128, nc: int = 16, nspokes: int = 20000, nsamp: int = 256):
     """3-D kooshball CG-SENSE: 128^3 3-D Shepp-Logan (tabulated intensities),
     16 Gaussian coils (sigma 0.45 FOV) on a Fibonacci sphere, 20000 spokes x 256
     samples, density compensation |k|^2 (3-D radial), noise-free data, sigma=2,
@@ -208,11 +208,11 @@ def config3(N: int = 128, nc: int = 16, nspokes: int = 20000, nsamp: int = 256):
     arguments give the reduced cases the FP64 oracle can finish."""
     k = kooshball3d(nspokes, nsamp)
     w = (ramp_weights(k).astype(np.float64) ** 2).astype(np.float32)
-    return dict(name="cfg3_kooshball_%d_%dc_%dx%d" % (N, nc, nspokes, nsamp), shape=(N, N, N), image=phantom3d(N),
+    return dict(name="kooshball_%d_%dc_%dx%d" % (N, nc, nspokes, nsamp), shape=(N, N, N), image=phantom3d(N),
                 sens=coils3d(N, nc), k=k, w=w, alpha=2.0, m=4, cgeps=1e-4, noise=0.0, seed=SEED_BASE + 3)
 
 
-def config2(count: int = 64, seed: int = SEED_BASE + 2):
+def uneven_batch(count: int = 64, seed: int = SEED_BASE + 2):
     """Batched uneven CG-SENSE: per problem N in 96..320 (step 32), NC in
     {4, 8, 16, 32}, golden-angle radial 32..400 spokes x 512; every fourth
     problem a variable-density spiral (16 interleaves x 4096, exponent 1.5).
@@ -229,7 +229,7 @@ def config2(count: int = 64, seed: int = SEED_BASE + 2):
             spokes = int(rng.integers(32, 401))
             k = radial2d(spokes, 512, golden=True)
             w, kind = ramp_weights(k), "radial%dx512" % spokes
-        out.append(dict(name="cfg2_%02d_%d_%dc_%s" % (i, N, nc, kind), shape=(N, N), N=N, nc=nc, kind=kind,
+        out.append(dict(name="uneven_%02d_%d_%dc_%s" % (i, N, nc, kind), shape=(N, N), N=N, nc=nc, kind=kind,
                         k=k, w=w, alpha=2.0, m=4, cgiter=15, noise=1e-3, seed=seed + 1000 * i))
     return out
 

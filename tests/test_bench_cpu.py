@@ -8,7 +8,7 @@ import sys
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def test_byte_model_config1():
+def test_byte_model_256_32coils():
     sys.path.insert(0, ROOT)
     import bench
     b = bench.algorithmic_bytes(256, 512, 403 * 512, 2, 32)

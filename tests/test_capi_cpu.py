@@ -39,11 +39,11 @@ def test_plugin_exports_reconstrategy_factories():
 
 def test_synthetic_configs_shapes_and_ranges():
     from codeare_gb300 import synth
-    c0 = synth.config0()
+    c0 = synth.radial2d_128_8coils()
     assert c0["k"].shape == (96 * 256, 2) and c0["k"].dtype == np.float32
     assert c0["sens"].shape == (8, 128, 128)
     assert np.all(c0["k"] >= -0.5) and np.all(c0["k"] < 0.5)
-    c1 = synth.config1()
+    c1 = synth.radial2d_256_32coils()
     assert c1["k"].shape == (403 * 512, 2)
     assert c1["sens"].shape == (32, 256, 256)
     k3 = synth.kooshball3d(100, 64)

@@ -102,7 +102,7 @@ def test_nfft_vs_oracle(gpu, oracle, N, nc, alpha, m):
     assert rel(img, ref) < TOL_OP
 
 
-def test_ndft_4096_points_config1_size(gpu, oracle):
+def test_ndft_4096_points_256_32coils_size(gpu, oracle):
     """256^2 image, sigma=2, m=4: FP32 NFFT vs FP64 direct NDFT on 4096 seeded random nodes."""
     rng = np.random.default_rng(20261204)
     N = 256
@@ -120,11 +120,11 @@ def test_ndft_4096_points_config1_size(gpu, oracle):
     assert rel(img[0], refa) < 1e-5
 
 
-def test_config1_properties_full_size(gpu):
-    """Full config-1 size (256^2, 32 coils, 403x512 golden-angle): adjointness and
+def test_nufft_256_32coils_properties_full_size(gpu):
+    """Full size (256^2, 32 coils, 403x512 golden-angle): adjointness and
     linearity, which hold at any size."""
     from codeare_gb300 import synth
-    cfg = synth.config1()
+    cfg = synth.radial2d_256_32coils()
     k = cfg["k"]
     M, nc, N = k.shape[0], 32, 256
     rng = np.random.default_rng(5)
@@ -299,13 +299,13 @@ def test_standard_cg_toeplitz_3d(gpu, oracle):
     assert rel(x2, xo) < TOL_IMG
 
 
-def test_config3_reduced_toeplitz_cg_matches_oracle(gpu, oracle):
-    """Config 3 at a size the FP64 oracle finishes: 3-D kooshball, |k|^2
+def test_kooshball_reduced_toeplitz_cg_matches_oracle(gpu, oracle):
+    """The 3-D kooshball case at a size the FP64 oracle finishes: |k|^2
     weights, standard CG with the Toeplitz-embedded E^H W E on the GPU against
     the oracle's CG on the NFFT pair, same iteration count (8)."""
     from codeare_gb300 import capi, synth
     import codeare_gb300 as cg
-    c = synth.config3(N=24, nc=4, nspokes=600, nsamp=48)
+    c = synth.kooshball3d_128_16coils(N=24, nc=4, nspokes=600, nsamp=48)
     N, nc = c["shape"][0], c["sens"].shape[0]
     k, w, S = c["k"], c["w"], c["sens"]
     s = oracle.Sense(S, k, w=w, m=c["m"], alpha=c["alpha"])
