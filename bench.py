@@ -130,18 +130,65 @@ def dist_setup():
     return ws, rank, local
 
 
-def cpu_nfft_step_time(k, fh, threads, reps=1):
-    """FP64 CPU restatement of the reference's per-coil NFFT3 trafo+adjoint."""
-    from oracle import oracle as O
-    O.build()
-    P = O.NFFT((N, N), k.shape[0], m=M_KB, alpha=SIGMA)
-    P.set_x(k.astype(np.float64))
-    fh64 = fh.astype(np.complex128)
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        f = P.trafo_batch(fh64, threads=threads)
-        P.adjoint_batch(f, threads=threads)
-    return (time.perf_counter() - t0) / reps
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo) and core count."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                name = ln.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not name:
+        try:
+            for ln in open("/proc/cpuinfo"):
+                if ln.lower().startswith(("model name", "cpu model")):
+                    name = ln.split(":", 1)[1].strip()
+                    break
+        except Exception:
+            pass
+    return {"model": name or "unknown", "nproc": os.cpu_count() or 1}
+
+
+class CpuNfftStep:
+    """FP64 CPU restatement of the reference's per-coil NFFT3 trafo+adjoint
+    (oracle/), one coil per host thread as NCSENSE runs one plan per thread.
+    The window values are precomputed once per trajectory (NFFT3's PRE_PSI,
+    which codeare sets) outside the timed call."""
+
+    def __init__(self, k, fh, threads):
+        from oracle import oracle as O
+        O.build()
+        self.P = O.NFFT((N, N), k.shape[0], m=M_KB, alpha=SIGMA)
+        self.P.set_x(k.astype(np.float64))
+        self.fh64 = fh.astype(np.complex128)
+        self.threads = threads
+
+    def __call__(self):
+        t0 = time.perf_counter()
+        f = self.P.trafo_batch(self.fh64, threads=self.threads)
+        self.P.adjoint_batch(f, threads=self.threads)
+        return time.perf_counter() - t0
+
+
+def cpu_baseline_leg(k, fh, warmup=1, runs=5):
+    """The CPU baseline protocol: all 32 coils, `warmup` untimed steps, then the
+    median of `runs` timed steps, with the host's core count and CPU model."""
+    cpu = cpu_model()
+    threads = cpu["nproc"]
+    step = CpuNfftStep(k, fh, threads)
+    for _ in range(warmup):
+        step()
+    times = [step() for _ in range(runs)]
+    t = statistics.median(times)
+    b = algorithmic_bytes(N, int(N * SIGMA), k.shape[0], 2, fh.shape[0])["step"]
+    return {"value": b / t / 1e9, "unit": UNIT, "cores": threads, "kind": "port", "cpu_model": cpu["model"],
+            "seconds": t, "runs_s": times,
+            "sample": "all %d coils, one forward+adjoint per run, %d warm-up + median of %d; one coil per "
+                      "thread; FP64 C restatement of the NFFT3 path with the project's own FFT (the "
+                      "reference needs NFFT3/FFTW/Boost, absent here)" % (fh.shape[0], warmup, runs)}
 
 
 def run_reference(args):
@@ -149,28 +196,34 @@ def run_reference(args):
     if rank != 0:
         return 0
     k, fh = workload_data()
-    threads = os.cpu_count() or 1
-    nc_s = min(NC, max(1, threads))  # one coil per host thread per step
-    sample = fh[:nc_s]
-    b = algorithmic_bytes(N, int(N * SIGMA), k.shape[0], 2, nc_s)["step"]
+    cpu = cpu_model()
+    threads = cpu["nproc"]
+    step = CpuNfftStep(k, fh, threads)      # every step: all 32 coils, as the GPU arm
+    b = algorithmic_bytes(N, int(N * SIGMA), k.shape[0], 2, NC)["step"]
     for _ in range(args.warmup):
-        cpu_nfft_step_time(k, sample, threads)
-    times = [cpu_nfft_step_time(k, sample, threads) for _ in range(args.steps)]
+        step()
+    times = [step() for _ in range(args.steps)]
     t = sum(times) / len(times)
     v = b / t / 1e9
     line = {
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)", "impl": "reference",
-        "config": {"workload": WORKLOAD, "sample_coils_per_step": nc_s},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "%d of 32 coils per step (one per host thread), full trajectory; "
+        "config": {"workload": WORKLOAD, "N": N, "n": int(N * SIGMA), "M": int(k.shape[0]), "ncoils": NC,
+                   "m": M_KB, "alg_bytes_per_step": b},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "cpu_model": cpu["model"],
+                         "sample": "all 32 coils per step, one forward+adjoint, one coil per host thread; "
                                    "FP64 C restatement of the NFFT3 path with the project's own FFT "
-                                   "(the reference needs NFFT3/FFTW/Boost, absent here)" % nc_s},
+                                   "(the reference needs NFFT3/FFTW/Boost, absent here)"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
+
+
+def rel_l2(a, b):
+    a = np.ravel(np.asarray(a)); b = np.ravel(np.asarray(b))
+    return float(np.linalg.norm(a - b) / max(float(np.linalg.norm(b)), 1e-300))
 
 
 def cgsense_section(cpu_too: bool):
@@ -215,17 +268,35 @@ def cgsense_section(cpu_too: bool):
                 "res_last": rep["res_last"]}
 
     out["codeare_10it"] = timed(mode=cg.MODE_CODEARE, cgiter=10, cgeps=1e-7, lam=5e-2, ftiter=3, fteps=1e-3)
-    out["standard_to_1e-4_nfft"] = timed(mode=cg.MODE_STANDARD, cgiter=200, cgeps=1e-4, lam=0.0, weighted=True)
-    out["standard_to_1e-4_toeplitz"] = timed(mode=cg.MODE_STANDARD, cgiter=200, cgeps=1e-4, lam=0.0,
+    x_codeare = xd.cpu().numpy()
+    # standard mode to ||r||/||r0|| = 1e-4 (the cap is far above the ~250 iterations it takes)
+    out["standard_to_1e-4_nfft"] = timed(mode=cg.MODE_STANDARD, cgiter=1000, cgeps=1e-4, lam=0.0, weighted=True)
+    out["standard_to_1e-4_toeplitz"] = timed(mode=cg.MODE_STANDARD, cgiter=1000, cgeps=1e-4, lam=0.0,
                                              weighted=True, toeplitz=True)
+    x_std = xd.cpu().numpy()
+    for key in ("standard_to_1e-4_nfft", "standard_to_1e-4_toeplitz"):
+        out[key]["reached_1e-4"] = bool(out[key]["res_last"] <= 1e-4)
+    p.solve(yd, xd, mode=cg.MODE_STANDARD, cgiter=20, cgeps=0.0, lam=0.0, weighted=True, toeplitz=True)
+    x_std20 = xd.cpu().numpy()
     p.close()
+    # the FP64 oracle on the same data, at the same iteration counts
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    s = O.Sense(S, k, w=w, m=c["m"], alpha=c["alpha"], threads=threads)
+    t0 = time.perf_counter()
+    xo, _ = s.cgls_codeare(y, cgiter=10, cgeps=1e-7, lam=5e-2, ftiter=3, fteps=1e-3)
+    t = time.perf_counter() - t0
+    out["codeare_10it"]["rel_l2_vs_oracle"] = rel_l2(x_codeare, xo)
+    it = out["standard_to_1e-4_toeplitz"]["iterations"]
+    xs, _ = s.cg(y, maxit=20, tol=0.0, lam=0.0, weighted=True)
+    out["standard_to_1e-4_toeplitz"]["rel_l2_vs_oracle_20it"] = rel_l2(x_std20, xs)
+    xs, _ = s.cg(y, maxit=it, tol=0.0, lam=0.0, weighted=True)
+    out["standard_to_1e-4_toeplitz"]["rel_l2_vs_oracle_same_iterations"] = rel_l2(x_std, xs)
+    out["standard_to_1e-4_toeplitz"]["note"] = (
+        "lambda 0 is ill-conditioned (ramp weight 0 at the k-space centre): FP32 and FP64 CG drift apart "
+        "(~1e-3 by 40 iterations) and reach 1e-4 along different paths, so the oracle error is also given at "
+        "20 iterations")
     if cpu_too:
-        from oracle import oracle as O
-        threads = os.cpu_count() or 1
-        s = O.Sense(S, k, w=w, m=c["m"], alpha=c["alpha"], threads=threads)
-        t0 = time.perf_counter()
-        s.cgls_codeare(y, cgiter=10, cgeps=1e-7, lam=5e-2, ftiter=3, fteps=1e-3)
-        t = time.perf_counter() - t0
         out["cpu_codeare_10it"] = {"wall_ms": t * 1e3, "cores": threads, "kind": "port",
                                    "note": "FP64 oracle restatement, one coil per thread"}
     return out
@@ -333,11 +404,22 @@ def batch_section():
     b.solve(ys, xs)
     t_batch = min(b.solve(ys, xs)[1] for _ in range(3))
     b.close()
+    # the FP64 oracle on four of the problems (the smallest, a spiral among them), same data and iterations
+    from oracle import oracle as O
+    cost = sorted(range(len(probs)), key=lambda i: probs[i]["nc"] * probs[i]["k"].shape[0])
+    check = cost[:3] + [next(i for i in cost if probs[i]["kind"].startswith("spiral"))]
+    errs = {}
+    for i in dict.fromkeys(check):
+        c = probs[i]
+        s = O.Sense(synth.coils2d(c["N"], c["nc"]), c["k"], w=c["w"], m=c["m"], alpha=c["alpha"])
+        xo, _ = s.cgls_codeare(ys[i].cpu().numpy(), cgiter=15, cgeps=0.0, lam=5e-2)
+        errs[c["name"]] = rel_l2(xs[i].cpu().numpy(), xo)
     out = {"workload": "64 uneven problems, N 96..320, 4/8/16/32 coils, golden-angle radial 32..400 x 512 "
                        "or VD spiral 16 x 4096, codeare CGLS 15 iterations (lambda 5e-2, 3 inner steps)",
            "problems": len(plans), "coil_samples": int(sum(c["k"].shape[0] * c["nc"] for c in probs)),
            "batch_ms": t_batch * 1e3, "sequential_ms": t_seq * 1e3, "problems_per_s": len(plans) / t_batch,
-           "setup_s": t_setup, "autotune_s": t_tune}
+           "setup_s": t_setup, "autotune_s": t_tune, "rel_l2_vs_oracle": errs,
+           "rel_l2_vs_oracle_max": max(errs.values())}
     for p in plans:
         p.close()
     return out
@@ -371,6 +453,25 @@ def kooshball_section():
     p.sense_adjoint(y, x, weighted=True)
     torch.cuda.synchronize()
     t_eh = time.perf_counter() - t0
+    # per-kernel CUDA-event times of one E (interpolation) and one E^H W (spreading), 16 coils
+    capi.profile_enable(True)
+    yk = torch.empty_like(y)
+    for _ in range(2):
+        p.sense_trafo(x, yk)
+        p.sense_adjoint(y, x, weighted=True)
+    torch.cuda.synchronize()
+    prof = capi.profile_collect()
+    capi.profile_enable(False)
+    n3 = 2 * N
+    kern = {}
+    for cat, (ms, cnt) in prof.items():
+        if cnt:
+            kern[cat] = {"launches": cnt, "avg_ms": ms / cnt}
+    gbytes = (M * 3 * 4 + nc * M * 8 + nc * n3 ** 3 * 8)     # coordinates, samples, grid
+    for cat in ("interp", "spread"):
+        if cat in kern:
+            kern[cat]["alg_GBps"] = gbytes / (kern[cat]["avg_ms"] * 1e-3) / 1e9
+            kern[cat]["tap_coil_macs_per_s"] = M * nc * 1000.0 / (kern[cat]["avg_ms"] * 1e-3)
     kw = dict(mode=cg.MODE_STANDARD, cgeps=c["cgeps"], lam=0.0, weighted=True, toeplitz=True)
     t0 = time.perf_counter()
     p.solve(y, x, cgiter=1, **kw)   # builds the Toeplitz kernel
@@ -383,11 +484,44 @@ def kooshball_section():
             best = r
     p.close()
     it = best["iterations"]
-    return {"workload": "3-D kooshball 128^3, 16 coils, kooshball 20000 x 256, |k|^2 weights, sigma=2, m=4, "
-                        "Toeplitz 256^3, standard CG to 1e-4",
-            "M": M, "plan_s": t_plan, "eh_y_ms": t_eh * 1e3, "toeplitz_build_and_first_solve_ms": t_first * 1e3,
-            "iterations": it, "res_last": best["res_last"], "solve_ms": best["seconds"] * 1e3,
-            "ms_per_iteration": (best["seconds"] - t_eh) * 1e3 / max(it, 1)}
+    out = {"workload": "3-D kooshball 128^3, 16 coils, kooshball 20000 x 256, |k|^2 weights, sigma=2, m=4, "
+                       "Toeplitz 256^3, standard CG to 1e-4",
+           "M": M, "plan_s": t_plan, "eh_y_ms": t_eh * 1e3, "toeplitz_build_and_first_solve_ms": t_first * 1e3,
+           "iterations": it, "res_last": best["res_last"], "solve_ms": best["seconds"] * 1e3,
+           "ms_per_iteration": (best["seconds"] - t_eh) * 1e3 / max(it, 1), "kernels": kern}
+    out["downsample_64"] = kooshball64_check()
+    return out
+
+
+def kooshball64_check():
+    """The 64^3 downsample of the kooshball workload against the FP64 oracle's
+    CG solution committed in tests/golden/kooshball64.npz (the data y is
+    recomputed with the oracle's FP64 forward operator): the same iteration
+    count, standard CG with the Toeplitz-embedded E^H W E on 128^3 FFTs."""
+    import torch
+    import codeare_gb300 as cg
+    from codeare_gb300 import capi, synth
+    from oracle import oracle as O
+    path = os.path.join(ROOT, "tests", "golden", "kooshball64.npz")
+    if not os.path.exists(path):
+        return None
+    g = np.load(path)
+    c = synth.kooshball3d_64_downsample()
+    it = int(g["iterations"])
+    s = O.Sense(c["sens"], c["k"], w=c["w"], m=c["m"], alpha=c["alpha"])
+    y = np.ascontiguousarray(s.trafo(c["image"]), dtype=np.complex64)
+    p = capi.Plan(c["shape"], c["k"].shape[0], ncoils=c["sens"].shape[0], m=c["m"], alpha=c["alpha"])
+    p.set_kspace(c["k"])
+    p.set_weights(c["w"])
+    p.set_sensitivities(np.ascontiguousarray(c["sens"]))
+    yd = torch.from_numpy(y).cuda()
+    xd = torch.zeros(c["shape"], dtype=torch.complex64, device="cuda")
+    kw = dict(mode=cg.MODE_STANDARD, cgiter=it, cgeps=0.0, lam=0.0, weighted=True, toeplitz=True)
+    p.solve(yd, xd, **kw)
+    rep = p.solve(yd, xd, **kw)
+    p.close()
+    return {"workload": "64^3 downsample: 16 coils, kooshball 5000 x 128, Toeplitz 128^3", "iterations": it,
+            "solve_ms": rep["seconds"] * 1e3, "rel_l2_vs_oracle": rel_l2(xd.cpu().numpy(), g["x"])}
 
 
 def learned_section():
@@ -546,13 +680,7 @@ def run_ours(args):
     # ---- CPU baseline (rank 0, N = 1): bounded sample, one coil per host thread
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        nc_s = min(NC, threads)
-        t_cpu = cpu_nfft_step_time(k, fh[:nc_s], threads)
-        b = algorithmic_bytes(N, n, M, 2, nc_s)["step"]
-        cpu = {"value": b / t_cpu / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "%d of 32 coils, one forward+adjoint, one coil per thread; FP64 C restatement of "
-                         "the NFFT3 path (own FFT; FFTW absent)" % nc_s, "seconds": t_cpu}
+        cpu = cpu_baseline_leg(k, fh)
 
     plan.close()
     cgs_part = None

@@ -500,11 +500,18 @@ template <int NT, int MT = 1> struct SpreadMma {
     __host__ __device__ static size_t warp_bytes(int taps) { return 2 * buf_bytes(taps) + kSpreadBatch * WPE * sizeof(float); }
 };
 
-// TF32 split: hi rounded to nearest, lo = x - hi passed as is (the tensor
-// cores read the upper 19 bits of a .tf32 operand, so lo is truncated there)
+// TF32 split: hi = x rounded to the nearest TF32 value (half a TF32 unit,
+// bit 12, added to the magnitude bits, then the 13 low mantissa bits
+// cleared), lo = x - hi (exact in FP32, |lo| <= 2^-11 |x|, either sign)
+// passed as is; the tensor cores read the upper 19 bits of a .tf32 operand,
+// so lo loses its low bits there and hi*hi + hi*lo + lo*hi carries ~2^-21
+// relative error per product, without bias because lo takes both signs
+// (a truncated hi would give lo the sign of x and bias every product low).
+// Two full-rate integer ops instead of a rounding conversion keep the split
+// off the conversion pipe.
 __device__ __forceinline__ void tf32_split(float x, uint32_t &hi, uint32_t &lo)
 {
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
+    hi = (__float_as_uint(x) + 0x1000u) & 0xffffe000u;
     lo = __float_as_uint(x - __uint_as_float(hi));
 }
 
@@ -958,6 +965,468 @@ interp2_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeS
 }
 
 // ---------------------------------------------------------------------------
+// 3-D gridding on the tensor cores (taps <= 10, every grid side >= 3 + taps).
+//
+// Node tables (once per trajectory): the wrapped footprint start of every
+// node and its 3 x taps window weights, zero padded to kW3 floats (128 B, so
+// one node's row is eight 16-byte copies).
+//
+// Spreading is output-stationary over 4 x 4 x 4 patches of grid points.  A
+// warp owns one patch as four m-tiles (its z-planes, 16 (y, x) points each)
+// and NT n-tiles of 8 float columns (4 NT coils), and walks the list of nodes
+// whose footprint covers the patch in batches of 8 entries, each batch one
+// mma.m16n8k8 k-step per (m-tile, n-tile):
+//   D[plane z][16 points][8 NT cols] += W[16 points][8 entries] V[8 entries][8 NT cols],
+//   W = wz(entry, z) wy(entry, y) (wx(entry, x) density(entry)).
+// Entries (values, window rows, starts, density weights) are staged by
+// cp.async, double buffered, as in the 2-D kernel; the B fragments and the
+// (y, x) weight products are formed once per batch and shared by the four
+// planes.  Operands are split into TF32 value and remainder, three products
+// accumulate in FP32.  Crowded patches are split into partial slots that
+// patch_reduce3_kernel adds in slot order: no atomics, reproducible results.
+//
+// Interpolation groups up to 16 nodes of one 4 x 4 x 4 footprint-start bin
+// per warp; their footprints lie in one U^3 region (U = 3 + taps) and
+//   f[16 nodes][8 NT cols] = W[16 nodes][U^3 points] G[U^3 points][8 NT cols]
+// runs over the region 8 points per k-step, W = wz wy wx from zero-padded
+// window rows (no bounds checks), G read through L1 (8 consecutive floats per
+// column group, one 32-byte sector).
+// ---------------------------------------------------------------------------
+__global__ void node_weights3_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
+                                     int4 *__restrict__ nodeU3, float *__restrict__ nodeW)
+{
+    const int taps = 2 * g.m + 2;
+    const float mf = (float)g.m;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < ns.M; s += (int64_t)gridDim.x * blockDim.x) {
+        float frac[3]; int c[3];
+        node_read<3>(ns.nodes, s, frac, c);
+        nodeU3[s] = make_int4(wrapi(c[0] - g.m, g.n[0]), wrapi(c[1] - g.m, g.n[1]), wrapi(c[2] - g.m, g.n[2]), 0);
+        float *w = nodeW + s * kW3;
+        for (int i = 0; i < kW3; ++i) {
+            const int t = i / taps, q = i % taps;
+            w[i] = (t < 3) ? kb_phi(frac[t] + mf - (float)q, mf, g.b[t]) : 0.f;
+        }
+    }
+}
+
+template <int NT> struct Spread3Mma {
+    static constexpr int R = spread_mma_row(NT);
+    // one staging buffer: values, window rows, footprint starts, density weights (a multiple of 16 B)
+    static constexpr size_t buf_bytes =
+        (size_t)kSpreadBatch * (R * sizeof(float) + kW3 * sizeof(float) + sizeof(int4) + sizeof(float));
+    // per warp: two buffers and the batch's patch weights (4 wz, 4 wy, 4 wx per entry)
+    static constexpr size_t warp_bytes = 2 * buf_bytes + (size_t)kSpreadBatch * 12 * sizeof(float);
+};
+
+template <int NT, int TAPS>
+__global__ void __launch_bounds__(256, 2)
+spread3_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
+                   const float2 *__restrict__ ks, const float *__restrict__ dens, int weighted,
+                   float2 *__restrict__ grid)
+{
+    using S = Spread3Mma<NT>;
+    constexpr int R = S::R, CC = 4 * NT, CH = 2 * NT;
+    extern __shared__ float4 smem4[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wi = blockIdx.x * 8 + warp;
+    if (wi >= ps.nwork) return;
+    char *wbase = reinterpret_cast<char *>(smem4) + (size_t)warp * S::warp_bytes;
+    float *swt = reinterpret_cast<float *>(wbase + 2 * S::buf_bytes);   // [entry][wz 0..3 | wy 0..3 | wx 0..3]
+    const int c0 = blockIdx.y * CC;
+    const int ccn = min(CC, g.nc - c0);
+    const bool v16 = ((g.nc & 1) == 0);
+    const int4 wk = ps.work[wi];
+    const int n0 = g.n[0], n1 = g.n[1], n2 = g.n[2];
+    const int gq = lane >> 2, tq = lane & 3;
+    const int yr = gq >> 2, xc = gq & 3;
+    const int pz0 = (wk.x / (ps.npx * ps.npy)) * 4, py0 = ((wk.x / ps.npx) % ps.npy) * 4, px0 = (wk.x % ps.npx) * 4;
+    float acc[4][NT][4];
+#pragma unroll
+    for (int mt = 0; mt < 4; ++mt)
+#pragma unroll
+        for (int t = 0; t < NT; ++t) acc[mt][t][0] = acc[mt][t][1] = acc[mt][t][2] = acc[mt][t][3] = 0.f;
+    if (wk.z > 0) {
+        {   // zero both buffers once: padding columns and rows past a short batch stay finite
+            float4 *z = reinterpret_cast<float4 *>(wbase);
+            const int n16 = (int)(2 * S::buf_bytes / 16);
+            for (int i = lane; i < n16; i += 32) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            __syncwarp();
+        }
+        auto buffers = [&](int buf, float *&sv, float *&sw, int4 *&su, float *&sd) {
+            char *b = wbase + (size_t)buf * S::buf_bytes;
+            sv = reinterpret_cast<float *>(b);
+            sw = sv + kSpreadBatch * R;
+            su = reinterpret_cast<int4 *>(sw + kSpreadBatch * kW3);
+            sd = reinterpret_cast<float *>(su + kSpreadBatch);
+        };
+        auto issue = [&](int e0, int cnt, int buf) {
+            float *sv, *sw, *sd; int4 *su;
+            buffers(buf, sv, sw, su, sd);
+            const int s_l = (lane < cnt) ? ps.entries[e0 + lane] : 0;
+            if (lane < cnt) {
+                cp_async16(&su[lane], &ps.nodeU3[s_l]);
+                if (weighted) cp_async4(&sd[lane], &dens[s_l]);
+                else sd[lane] = 1.f;
+            }
+            // window rows: 8 entries x 8 chunks of 16 bytes
+#pragma unroll
+            for (int i = 0; i < (kSpreadBatch * (kW3 / 4)) / 32; ++i) {
+                const int ch = lane + 32 * i;
+                const int e = ch / (kW3 / 4), q = ch % (kW3 / 4);
+                const int s = __shfl_sync(0xffffffffu, s_l, e);
+                if (e < cnt) cp_async16(sw + e * kW3 + 4 * q, ps.nodeW + (size_t)s * kW3 + 4 * q);
+            }
+            if (v16) {
+#pragma unroll
+                for (int i = 0; i < (kSpreadBatch * CH + 31) / 32; ++i) {
+                    const int ch = lane + 32 * i;
+                    const int e = ch / CH, c = 2 * (ch % CH);
+                    const int s = __shfl_sync(0xffffffffu, s_l, e & (kSpreadBatch - 1));
+                    if (ch < kSpreadBatch * CH && e < cnt && c < ccn) {
+                        const float2 *v = ks + (size_t)s * g.nc + c0 + c;
+                        float2 *d = reinterpret_cast<float2 *>(sv + e * R) + c;
+                        if (c + 1 < ccn) cp_async16(d, v);
+                        else cp_async8(d, v);
+                    }
+                }
+            } else {
+                for (int j = 0; j < cnt; ++j) {
+                    const int s = __shfl_sync(0xffffffffu, s_l, j);
+                    const float2 *v = ks + (size_t)s * g.nc + c0;
+                    float2 *dv = reinterpret_cast<float2 *>(sv + j * R);
+                    for (int c = lane; c < ccn; c += 32) cp_async8(dv + c, v + c);
+                }
+            }
+            cp_async_commit();
+        };
+        const int end = wk.y + wk.z;
+        int e0 = wk.y, cnt = min(kSpreadBatch, end - e0), buf = 0;
+        issue(e0, cnt, 0);
+        while (true) {
+            const int e1 = e0 + cnt;
+            const int cnt1 = min(kSpreadBatch, end - e1);
+            if (cnt1 > 0) { issue(e1, cnt1, buf ^ 1); cp_async_wait<1>(); }
+            else cp_async_wait<0>();
+            __syncwarp();
+            float *sv, *sw, *sd; int4 *su;
+            buffers(buf, sv, sw, su, sd);
+            // the batch's patch weights: entry e, axis a (z, y, x), offset r in the patch; zero past cnt
+#pragma unroll
+            for (int i = 0; i < (kSpreadBatch * 12) / 32; ++i) {
+                const int idx = lane + 32 * i;
+                const int e = idx / 12, a = (idx % 12) >> 2, r = idx & 3;
+                float w = 0.f;
+                if (e < cnt) {
+                    const int4 u = su[e];
+                    const int pa = (a == 0 ? pz0 : (a == 1 ? py0 : px0)) + r;
+                    const int na = a == 0 ? n0 : (a == 1 ? n1 : n2);
+                    if (pa < na) {
+                        int q = pa - (a == 0 ? u.x : (a == 1 ? u.y : u.z));
+                        if (q < 0) q += na;
+                        w = q < TAPS ? sw[e * kW3 + a * TAPS + q] : 0.f;
+                        if (a == 2) w *= sd[e];
+                    }
+                }
+                swt[idx] = w;
+            }
+            __syncwarp();
+            const float *we0 = swt + tq * 12, *we1 = swt + (tq + 4) * 12;
+            // rows gq and gq + 8 of an m-tile: points (y, x) = (yr, xc) and (yr + 2, xc)
+            const float wyx00 = we0[4 + yr] * we0[8 + xc], wyx01 = we0[6 + yr] * we0[8 + xc];
+            const float wyx10 = we1[4 + yr] * we1[8 + xc], wyx11 = we1[6 + yr] * we1[8 + xc];
+            uint32_t bh0[NT], bl0[NT], bh1[NT], bl1[NT];
+            const float *r0 = sv + tq * R + gq, *r1 = sv + (tq + 4) * R + gq;
+#pragma unroll
+            for (int t = 0; t < NT; ++t) {
+                tf32_split(r0[8 * t], bh0[t], bl0[t]);
+                tf32_split(r1[8 * t], bh1[t], bl1[t]);
+            }
+#pragma unroll
+            for (int mt = 0; mt < 4; ++mt) {
+                uint32_t ah[4], al[4];
+                const float z0 = we0[mt], z1 = we1[mt];
+                tf32_split(z0 * wyx00, ah[0], al[0]);
+                tf32_split(z0 * wyx01, ah[1], al[1]);
+                tf32_split(z1 * wyx10, ah[2], al[2]);
+                tf32_split(z1 * wyx11, ah[3], al[3]);
+#pragma unroll
+                for (int t = 0; t < NT; ++t) {
+                    mma_tf32(acc[mt][t], al, bh0[t], bh1[t]);
+                    mma_tf32(acc[mt][t], ah, bl0[t], bl1[t]);
+                    mma_tf32(acc[mt][t], ah, bh0[t], bh1[t]);
+                }
+            }
+            __syncwarp();
+            if (cnt1 <= 0) break;
+            e0 = e1; cnt = cnt1; buf ^= 1;
+        }
+    }
+    const int xx = px0 + xc;
+#pragma unroll
+    for (int mt = 0; mt < 4; ++mt)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int zz = pz0 + mt, yy = py0 + yr + 2 * h;
+            if (zz >= n0 || yy >= n1 || xx >= n2) continue;
+            const int ppt = 16 * mt + gq + 8 * h;            // point index within the patch (z, y, x row-major)
+            float2 *dst = (wk.w < 0) ? grid + (((size_t)zz * n1 + yy) * n2 + xx) * g.nc + c0
+                                     : ps.partial + ((size_t)wk.w * 64 + ppt) * g.nc + c0;
+#pragma unroll
+            for (int t = 0; t < NT; ++t) {
+                const int c = 4 * t + tq;
+                if (c < ccn) dst[c] = make_float2(acc[mt][t][2 * h], acc[mt][t][2 * h + 1]);
+            }
+        }
+}
+
+// sum the partial slots of split 3-D patches in slot order and store them
+__global__ void patch_reduce3_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
+                                     float2 *__restrict__ grid)
+{
+    const int nc = g.nc;
+    const int64_t total = (int64_t)ps.nmulti * 64 * nc;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(e % nc);
+        const int pt = (int)((e / nc) % 64);
+        const int4 mu = ps.multi[e / ((int64_t)64 * nc)];
+        const int z = (mu.x / (ps.npx * ps.npy)) * 4 + pt / 16;
+        const int y = ((mu.x / ps.npx) % ps.npy) * 4 + (pt / 4) % 4;
+        const int x = (mu.x % ps.npx) * 4 + pt % 4;
+        if (z >= g.n[0] || y >= g.n[1] || x >= g.n[2]) continue;
+        float sx = 0.f, sy = 0.f;
+        for (int k = 0; k < mu.z; ++k) {
+            const float2 v = ps.partial[((size_t)(mu.y + k) * 64 + pt) * nc + c];
+            sx += v.x; sy += v.y;
+        }
+        grid[(((size_t)z * g.n[1] + y) * g.n[2] + x) * nc + c] = make_float2(sx, sy);
+    }
+}
+
+template <int NT, int TAPS> struct Interp3Mma {
+    static constexpr int U = 3 + TAPS, UU = U * U, KP = (U * U * U + 7) / 8 * 8, NK = KP / 8;
+    // zero-padded window rows per axis: entry 3 + i is tap i, so a region
+    // coordinate in [0, U] minus the node's offset (0..3) indexes them unchecked
+    static constexpr int PL = U + 4;
+    static constexpr int R = spread_mma_row(NT);   // staged point row (floats): conflict-free B reads
+    static constexpr int S = 4;                    // cp.async stages of 8 points each
+    static constexpr size_t stage_bytes = (size_t)8 * R * sizeof(float);
+    static constexpr size_t warp_bytes =
+        (S * stage_bytes + (size_t)kInterpGroup * 3 * PL * sizeof(float) + (size_t)(UU + U) * sizeof(int) + 15) / 16 * 16;
+    static constexpr size_t smem = 8 * warp_bytes;
+};
+
+template <int NT, int TAPS>
+__global__ void __launch_bounds__(256, 2)
+interp3_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
+                   const float2 *__restrict__ grid, float2 *__restrict__ ks)
+{
+    using I = Interp3Mma<NT, TAPS>;
+    constexpr int U = I::U, UU = I::UU, NK = I::NK, CC = 4 * NT, PL = I::PL, R = I::R, S = I::S;
+    constexpr int CH = 2 * NT, NCH = 8 * CH, NI = (NCH + 31) / 32;   // 16-byte chunks per point / per k-step
+    extern __shared__ float4 smem4[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wi = blockIdx.x * 8 + warp;
+    if (wi >= ns.niwork) return;
+    char *wbase = reinterpret_cast<char *>(smem4) + warp * I::warp_bytes;
+    float *sbase = reinterpret_cast<float *>(wbase);                          // [S][8 points][R]
+    float *wpad = reinterpret_cast<float *>(wbase + S * I::stage_bytes);     // [16][3][PL]
+    int *roff = reinterpret_cast<int *>(wpad + kInterpGroup * 3 * PL);       // [U z][U y] first point of each region row
+    int *xoff = roff + UU;                                                    // [U] wrapped x
+    const int4 wk = ns.iwork[wi];                          // {bin, first, count <= 16, 0}
+    const int c0 = blockIdx.y * CC;
+    const int ccn = min(CC, g.nc - c0);
+    const bool v16 = ((g.nc & 1) == 0);
+    const int n0 = g.n[0], n1 = g.n[1], n2 = g.n[2];
+    const int z0 = (wk.x / (ns.ibx * ns.iby)) * 4, y0 = ((wk.x / ns.ibx) % ns.iby) * 4, x0 = (wk.x % ns.ibx) * 4;
+    const int cnt = wk.z;
+    {   // zero the stages once: columns past the coils and points past the region stay finite
+        float4 *z = reinterpret_cast<float4 *>(sbase);
+        for (int i = lane; i < (int)(S * I::stage_bytes / 16); i += 32) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    // region rows and columns wrap at most once (every side >= U)
+    for (int q = lane; q < UU; q += 32) {
+        int gz = z0 + q / U, gy = y0 + q % U;
+        if (gz >= n0) gz -= n0;
+        if (gy >= n1) gy -= n1;
+        roff[q] = (gz * n1 + gy) * n2;
+    }
+    if (lane < U) {
+        int gx = x0 + lane;
+        if (gx >= n2) gx -= n2;
+        xoff[lane] = gx;
+    }
+    // the group's padded window rows and footprint offsets within the bin (0..3)
+    int s_l = -1, oz_l = 0, oy_l = 0, ox_l = 0;
+    if (lane < kInterpGroup) {
+        float *wr = wpad + lane * 3 * PL;
+        if (lane < cnt) {
+            s_l = ns.ilist[wk.y + lane];
+            const int4 u = ns.nodeU3[s_l];
+            oz_l = u.x - z0; oy_l = u.y - y0; ox_l = u.z - x0;
+            const float *W = ns.nodeW + (size_t)s_l * kW3;
+            for (int i = 0; i < PL; ++i) {
+                const int t = i - 3;
+                const bool in = (t >= 0 && t < TAPS);
+                wr[i] = in ? W[t] : 0.f;
+                wr[PL + i] = in ? W[TAPS + t] : 0.f;
+                wr[2 * PL + i] = in ? W[2 * TAPS + t] : 0.f;
+            }
+        } else {
+            for (int i = 0; i < 3 * PL; ++i) wr[i] = 0.f;
+        }
+    }
+    __syncwarp();
+    // staging: chunk ch of a k-step is point ch / CH, coils 2 (ch % CH) and 2 (ch % CH) + 1;
+    // this lane's chunks keep their point slot, so their region coordinates advance by 8 per k-step
+    int cz[NI], cy[NI], cx[NI];
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+        const int ch = lane + 32 * i;
+        const int q = ch < NCH ? ch / CH : 0;
+        cz[i] = q / UU; cy[i] = (q / U) % U; cx[i] = q % U;
+    }
+    const float2 *gsrc = grid + c0;
+    auto issue = [&](int stage) {
+        float *sb = sbase + stage * 8 * R;
+#pragma unroll
+        for (int i = 0; i < NI; ++i) {
+            const int ch = lane + 32 * i;
+            if (ch < NCH) {
+                const int pi = ch / CH, c = 2 * (ch % CH);
+                if (cz[i] < U && c < ccn) {
+                    const float2 *src = gsrc + (size_t)(roff[cz[i] * U + cy[i]] + xoff[cx[i]]) * g.nc + c;
+                    float2 *dst = reinterpret_cast<float2 *>(sb + pi * R) + c;
+                    if (v16 && c + 1 < ccn) {
+                        cp_async16(dst, src);
+                    } else {
+                        cp_async8(dst, src);
+                        if (c + 1 < ccn) cp_async8(dst + 1, src + 1);
+                    }
+                }
+                cx[i] += 8;
+                while (cx[i] >= U) { cx[i] -= U; if (++cy[i] == U) { cy[i] = 0; ++cz[i]; } }
+            }
+        }
+        cp_async_commit();
+    };
+    const int gq = lane >> 2, tq = lane & 3;
+    const int na = gq, nb = gq + 8;
+    const int oza = __shfl_sync(0xffffffffu, oz_l, na), oya = __shfl_sync(0xffffffffu, oy_l, na),
+              oxa = __shfl_sync(0xffffffffu, ox_l, na);
+    const int ozb = __shfl_sync(0xffffffffu, oz_l, nb), oyb = __shfl_sync(0xffffffffu, oy_l, nb),
+              oxb = __shfl_sync(0xffffffffu, ox_l, nb);
+    // row pointers shifted so that [q] is tap q - offset (zero outside)
+    const float *Wza = wpad + na * 3 * PL + 3 - oza, *Wya = wpad + na * 3 * PL + PL + 3 - oya,
+                *Wxa = wpad + na * 3 * PL + 2 * PL + 3 - oxa;
+    const float *Wzb = wpad + nb * 3 * PL + 3 - ozb, *Wyb = wpad + nb * 3 * PL + PL + 3 - oyb,
+                *Wxb = wpad + nb * 3 * PL + 2 * PL + 3 - oxb;
+    float acc[NT][4];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+    // region coordinates of the thread's two A points q0 = 8 k + tq and q1 = q0 + 4
+    int qz0 = tq / UU, qy0 = (tq / U) % U, qx0 = tq % U;
+    int qz1 = (tq + 4) / UU, qy1 = ((tq + 4) / U) % U, qx1 = (tq + 4) % U;
+    __syncwarp();   // zeroed stages and the row tables before the first copies
+#pragma unroll
+    for (int st = 0; st < S - 1; ++st) {
+        if (st < NK) issue(st);
+        else cp_async_commit();
+    }
+#pragma unroll 1
+    for (int k = 0; k < NK; ++k) {
+        if (k + S - 1 < NK) issue((k + S - 1) % S);
+        else cp_async_commit();
+        cp_async_wait<S - 1>();
+        __syncwarp();
+        const float *sb = sbase + (k % S) * 8 * R;
+        uint32_t ah[4], al[4];
+        tf32_split(Wza[qz0] * (Wya[qy0] * Wxa[qx0]), ah[0], al[0]);
+        tf32_split(Wzb[qz0] * (Wyb[qy0] * Wxb[qx0]), ah[1], al[1]);
+        tf32_split(Wza[qz1] * (Wya[qy1] * Wxa[qx1]), ah[2], al[2]);
+        tf32_split(Wzb[qz1] * (Wyb[qy1] * Wxb[qx1]), ah[3], al[3]);
+        const float *r0 = sb + tq * R + gq, *r1 = sb + (tq + 4) * R + gq;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            uint32_t bh0, bl0, bh1, bl1;
+            tf32_split(r0[8 * t], bh0, bl0);
+            tf32_split(r1[8 * t], bh1, bl1);
+            mma_tf32(acc[t], al, bh0, bh1);
+            mma_tf32(acc[t], ah, bl0, bl1);
+            mma_tf32(acc[t], ah, bh0, bh1);
+        }
+        qx0 += 8; while (qx0 >= U) { qx0 -= U; if (++qy0 == U) { qy0 = 0; ++qz0; } }
+        qx1 += 8; while (qx1 >= U) { qx1 -= U; if (++qy1 == U) { qy1 = 0; ++qz1; } }
+        __syncwarp();   // every lane is done with this stage before it is refilled
+    }
+    cp_async_wait<0>();
+    // rows gq and gq + 8: nodes na and nb, columns 2 tq, 2 tq + 1 of each n-tile
+    const int sa = __shfl_sync(0xffffffffu, s_l, na), sb_ = __shfl_sync(0xffffffffu, s_l, nb);
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        const int c = 4 * t + tq;
+        if (c < ccn) {
+            if (na < cnt) ks[(size_t)sa * g.nc + c0 + c] = make_float2(acc[t][0], acc[t][1]);
+            if (nb < cnt) ks[(size_t)sb_ * g.nc + c0 + c] = make_float2(acc[t][2], acc[t][3]);
+        }
+    }
+}
+
+template <int NT, int TAPS>
+static cgs_status launch_interp3_mma_t(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,
+                                       cudaStream_t st)
+{
+    using I = Interp3Mma<NT, TAPS>;
+    CGS_CUDA(cudaFuncSetAttribute(interp3_mma_kernel<NT, TAPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)I::smem));
+    dim3 grd((ns.niwork + 7) / 8, (g.nc + 4 * NT - 1) / (4 * NT));
+    interp3_mma_kernel<NT, TAPS><<<grd, 256, I::smem, st>>>(g, ns, grid, ks);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+template <int TAPS>
+static cgs_status launch_interp3_mma_taps(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,
+                                          cudaStream_t st)
+{
+    switch (std::min(8, (2 * g.nc + 7) / 8)) {
+        case 8: return launch_interp3_mma_t<8, TAPS>(g, ns, grid, ks, st);
+        case 7: return launch_interp3_mma_t<7, TAPS>(g, ns, grid, ks, st);
+        case 6: return launch_interp3_mma_t<6, TAPS>(g, ns, grid, ks, st);
+        case 5: return launch_interp3_mma_t<5, TAPS>(g, ns, grid, ks, st);
+        case 4: return launch_interp3_mma_t<4, TAPS>(g, ns, grid, ks, st);
+        case 3: return launch_interp3_mma_t<3, TAPS>(g, ns, grid, ks, st);
+        case 2: return launch_interp3_mma_t<2, TAPS>(g, ns, grid, ks, st);
+        default: return launch_interp3_mma_t<1, TAPS>(g, ns, grid, ks, st);
+    }
+}
+
+template <int NT, int TAPS>
+static cgs_status launch_spread3_mma_t(const GridGeom &g, const PatchSet &ps, const float2 *ks, const float *dens,
+                                       int weighted, float2 *grid, cudaStream_t st)
+{
+    using S = Spread3Mma<NT>;
+    const size_t sm = 8 * S::warp_bytes;
+    CGS_CUDA(cudaFuncSetAttribute(spread3_mma_kernel<NT, TAPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    dim3 grd((ps.nwork + 7) / 8, (g.nc + 4 * NT - 1) / (4 * NT));
+    spread3_mma_kernel<NT, TAPS><<<grd, 256, sm, st>>>(g, ps, ks, dens, weighted, grid);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+template <int TAPS>
+static cgs_status launch_spread3_mma_taps(const GridGeom &g, const PatchSet &ps, const float2 *ks, const float *dens,
+                                          int weighted, float2 *grid, cudaStream_t st)
+{
+    // at most 16 coils per warp: four m-tiles of 4 NT accumulators each
+    switch (std::min(4, (2 * g.nc + 7) / 8)) {
+        case 4: return launch_spread3_mma_t<4, TAPS>(g, ps, ks, dens, weighted, grid, st);
+        case 3: return launch_spread3_mma_t<3, TAPS>(g, ps, ks, dens, weighted, grid, st);
+        case 2: return launch_spread3_mma_t<2, TAPS>(g, ps, ks, dens, weighted, grid, st);
+        default: return launch_spread3_mma_t<1, TAPS>(g, ps, ks, dens, weighted, grid, st);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // 3-D gridding, one warp per node.  A CTA owns a bin of footprint starts (T^3)
 // and its padded E^3 tile (E = T + 2m + 1) for CC coils in shared memory,
 // stored as planes of real and imaginary parts, [coil][part][z][y][x] with an
@@ -1380,6 +1849,18 @@ cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *gri
             return r;
         }
     }
+    if (g.d == 3 && g.imma && grid3_mma_ok(g) && ns.ilist && ns.nodeU3 && ns.nodeW && ns.niwork > 0) {
+        cgs_status r;
+        prof_begin(PROF_INTERP, st);
+        switch (taps) {
+            case 4: r = launch_interp3_mma_taps<4>(g, ns, grid, ks, st); break;
+            case 6: r = launch_interp3_mma_taps<6>(g, ns, grid, ks, st); break;
+            case 8: r = launch_interp3_mma_taps<8>(g, ns, grid, ks, st); break;
+            default: r = launch_interp3_mma_taps<10>(g, ns, grid, ks, st); break;
+        }
+        prof_end(PROF_INTERP, st);
+        return r;
+    }
     if (g.d == 3) {
         prof_begin(PROF_INTERP, st);
         const cgs_status r = launch_grid3<false>(g, ns, grid, 0, ks, st);
@@ -1412,6 +1893,48 @@ cgs_status launch_node_weights(const GridGeom &g, const NodeSet &ns, int2 *nodeU
     node_weights_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, ns, nodeU, nodeW);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
+}
+
+bool grid3_mma_ok(const GridGeom &g)
+{
+    const int taps = 2 * g.m + 2;
+    return g.d == 3 && taps <= 10 && g.n[0] >= 3 + taps && g.n[1] >= 3 + taps && g.n[2] >= 3 + taps;
+}
+
+cgs_status launch_node_weights3(const GridGeom &g, const NodeSet &ns, int4 *nodeU3, float *nodeW,
+                                cudaStream_t st)
+{
+    if (!grid3_mma_ok(g)) { set_error("3-D node tables need taps <= 10 and every side >= 3 + taps"); return CGS_ERR_BAD_ARG; }
+    if (ns.M == 0) return CGS_OK;
+    const int64_t blocks = std::min<int64_t>((ns.M + 255) / 256, 152 * 16);
+    node_weights3_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, ns, nodeU3, nodeW);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_spread_patch3(const GridGeom &g, const PatchSet &ps, const float2 *ks, const float *dens,
+                                int weighted, float2 *grid, cudaStream_t st)
+{
+    if (ps.nwork == 0 || g.nc == 0) return CGS_OK;
+    if (!grid3_mma_ok(g) || ps.pd != 4 || !ps.nodeU3) { set_error("3-D patch lists missing"); return CGS_ERR_BAD_ARG; }
+    cgs_status r;
+    prof_begin(PROF_SPREAD, st);
+    switch (2 * g.m + 2) {
+        case 4: r = launch_spread3_mma_taps<4>(g, ps, ks, dens, weighted, grid, st); break;
+        case 6: r = launch_spread3_mma_taps<6>(g, ps, ks, dens, weighted, grid, st); break;
+        case 8: r = launch_spread3_mma_taps<8>(g, ps, ks, dens, weighted, grid, st); break;
+        default: r = launch_spread3_mma_taps<10>(g, ps, ks, dens, weighted, grid, st); break;
+    }
+    if (r == CGS_OK && ps.nmulti > 0) {
+        const int64_t total = (int64_t)ps.nmulti * 64 * g.nc;
+        const int64_t blocks = std::min<int64_t>((total + 255) / 256, 152 * 16);
+        patch_reduce3_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, ps, grid);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) { set_error(std::string("kernel launch: ") + cudaGetErrorString(e)); r = CGS_ERR_CUDA; }
+        else count_launch();
+    }
+    prof_end(PROF_SPREAD, st);
+    return r;
 }
 
 cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const float2 *ks, const float *dens,

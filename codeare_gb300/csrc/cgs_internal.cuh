@@ -154,7 +154,13 @@ struct NodeSet {
     const int4 *iwork;
     int niwork;
     int ibx;            // bins per grid row
+    // 3-D tensor-core gridding: per node its wrapped footprint start
+    // {u0, u1, u2, 0}; nodeW then holds kW3 window weights per node (3 x taps,
+    // zero padded), and ilist / iwork group the nodes by 4 x 4 x 4 start bin
+    const int4 *nodeU3;
+    int iby;            // 3-D: bins per grid column (bins per plane = iby * ibx)
 };
+constexpr int kW3 = 32;  // floats per node in the 3-D window table
 
 // Output-stationary 2-D spreading: one warp per work item over a ph x pw patch
 // of grid points, its lanes split into coil groups (lane = one point or a 2 x 2
@@ -175,6 +181,11 @@ struct PatchSet {
     float2 *partial;       // [slot][ph pw points][nc] partial sums of split patches
     int nmulti;            // patches split into several slots
     const int4 *multi;     // {patch, first slot, slots, 0}
+    // 3-D (pd = 4): 4 x 4 x 4 patches, npy patches per grid column; node
+    // starts in nodeU3 and kW3 window weights per node in nodeW; partial
+    // slots hold 64 points each
+    int pd, npy;
+    const int4 *nodeU3;
 };
 // node weights and footprint starts from the node records (once per trajectory)
 cgs_status launch_node_weights(const GridGeom &g, const NodeSet &ns, int2 *nodeU, float *nodeW,
@@ -182,6 +193,15 @@ cgs_status launch_node_weights(const GridGeom &g, const NodeSet &ns, int2 *nodeU
 // grid[...][c] = sum_s phi * (w_s if weighted) * ks[s][c]; writes every grid point
 cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const float2 *ks, const float *dens,
                                int weighted, float2 *grid, cudaStream_t st);
+
+// 3-D node tables: wrapped footprint starts and kW3 window weights per node
+cgs_status launch_node_weights3(const GridGeom &g, const NodeSet &ns, int4 *nodeU3, float *nodeW,
+                                cudaStream_t st);
+// 3-D output-stationary spreading over 4 x 4 x 4 patches (writes every grid point)
+cgs_status launch_spread_patch3(const GridGeom &g, const PatchSet &ps, const float2 *ks, const float *dens,
+                                int weighted, float2 *grid, cudaStream_t st);
+// whether the 3-D tensor-core gridding covers this geometry (taps <= 10, every side >= 3 + taps)
+bool grid3_mma_ok(const GridGeom &g);
 
 // y[s][c] (sorted, coil innermost) = sum over footprint of grid[...][c]
 // With `user` (the caller's layout: coil-major, trajectory order) the

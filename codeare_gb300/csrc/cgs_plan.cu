@@ -12,6 +12,7 @@
 #include "cgs_internal.cuh"
 
 #include <algorithm>
+#include <thread>
 #include <initializer_list>
 #include <atomic>
 #include <chrono>
@@ -209,6 +210,11 @@ struct cgs_plan {
     int *ilist = nullptr;
     int4 *iwork = nullptr;
     int niwork = 0, ibx = 0;
+    // 3-D tensor-core gridding: wrapped footprint starts per node (nodeW then
+    // holds kW3 window weights per node, ilist / iwork the 4 x 4 x 4 bins,
+    // pentries / pwork / pmulti the 4 x 4 x 4 patch lists)
+    int4 *nodeU3 = nullptr;
+    int iby = 0;
 
     // host copies of the trajectory and weights (the Toeplitz kernel is built from them)
     std::vector<float> k_host, w_host;
@@ -282,6 +288,14 @@ cgs_status dev_alloc(T **p, size_t count)
 void dev_free(void *p)
 {
     if (p) cudaFree(p);
+}
+
+// the gridding kernels' view of a plan's node tables
+NodeSet node_set(const cgs_plan *p)
+{
+    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork,
+               p->niwork, p->ibx, p->nodeU3, p->iby};
+    return ns;
 }
 
 bool is_device_ptr(const void *p)
@@ -370,7 +384,7 @@ cgs_status op_forward_grid(cgs_plan *p, const float2 *src_img, int per_coil, con
 // grid of p's geometry) into ks, or into the caller's layout with `user`
 cgs_status op_forward_interp(cgs_plan *p, const float2 *grid, float2 *ks, cudaStream_t st, float2 *user)
 {
-    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork, p->niwork, p->ibx};
+    NodeSet ns = node_set(p);
     bool direct = false;
     CGS_TRY(launch_interp(p->geom, ns, grid, ks, st, user, &direct));
     if (user && !direct) CGS_TRY(launch_scatter_ks(ks, p->perm, p->M, p->nc, user, st));
@@ -437,10 +451,13 @@ cgs_status op_adjoint(cgs_plan *p, const float2 *ks, int weighted, float2 *out, 
         return CGS_OK;
     }
     const int d = p->d, nc = p->nc;
-    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork, p->niwork, p->ibx};
+    NodeSet ns = node_set(p);
     if (d == 2) {
         // writes every grid point: no clearing pass
         CGS_TRY(launch_spread_patch(p->geom, p->pset, ks, p->w, weighted && p->w != nullptr, p->grid, st));
+    } else if (p->pset.pd == 4) {
+        // 3-D patches on the tensor cores: also writes every grid point
+        CGS_TRY(launch_spread_patch3(p->geom, p->pset, ks, p->w, weighted && p->w != nullptr, p->grid, st));
     } else {
         CGS_TRY(launch_zero(p->grid, sizeof(float2) * (size_t)p->ntot * nc, st));
         CGS_TRY(launch_spread(p->geom, ns, ks, weighted && p->w != nullptr, p->grid, st));
@@ -522,6 +539,7 @@ void apply_tiles(cgs_plan *p)
     g.scc = p->tune.spread_coils;
     const int ib = p->tune.interp_block;
     g.imma = (p->d == 2 && (ib == 16 || (ib == 0 && p->nc >= 4))) ? 1 : 0;
+    if (p->d == 3) g.imma = (ib != 1 && grid3_mma_ok(g)) ? 1 : 0;
 }
 
 // Node lists of the 2-D tensor-core interpolation: sorted node indices grouped
@@ -653,7 +671,7 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     CGS_CUDA(cudaMemcpy(p->pwork, work.data(), sizeof(int4) * work.size(), cudaMemcpyHostToDevice));
     if (!multi.empty())
         CGS_CUDA(cudaMemcpy(p->pmulti, multi.data(), sizeof(int4) * multi.size(), cudaMemcpyHostToDevice));
-    NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork, p->niwork, p->ibx};
+    NodeSet ns = node_set(p);
     CGS_TRY(launch_node_weights(p->geom, ns, p->nodeU, p->nodeW, p->stream));
     CGS_CUDA(cudaStreamSynchronize(p->stream));
     PatchSet &ps = p->pset;
@@ -669,6 +687,178 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     ps.partial = p->ppartial;
     ps.nmulti = (int)multi.size();
     ps.multi = p->pmulti;
+    return CGS_OK;
+}
+
+// 3-D tensor-core gridding (taps <= 10, every side >= 3 + taps): the node
+// tables, the interpolation bins (nodes grouped by the 4 x 4 x 4 bin of their
+// wrapped footprint start, work items of at most kInterpGroup nodes) and,
+// unless spread_block 1 asks for the CUDA-core kernel, the spreading patch
+// lists (per 4 x 4 x 4 patch the sorted indices of the nodes whose footprint
+// covers it; work items of at most `chunk` entries, crowded patches spread
+// over partial slots; a patch without nodes still gets an item, which writes
+// its zeros).  `cc` holds floor(n x) per node in trajectory order, `perm` the
+// trajectory node of each sorted position.
+cgs_status build_grid3(cgs_plan *p, const std::vector<int> &cc, const std::vector<int> &perm)
+{
+    const int n0 = p->n[0], n1 = p->n[1], n2 = p->n[2], m = p->m, taps = 2 * m + 2;
+    const int64_t M = p->M;
+    auto wrap = [](int v, int n) { v %= n; return v < 0 ? v + n : v; };
+    for (void *b : {(void *)p->nodeU3, (void *)p->nodeW, (void *)p->ilist, (void *)p->iwork, (void *)p->pentries,
+                    (void *)p->pwork, (void *)p->pmulti, (void *)p->ppartial}) dev_free(b);
+    p->nodeU3 = nullptr; p->nodeW = nullptr; p->ilist = nullptr; p->iwork = nullptr;
+    p->pentries = nullptr; p->pwork = nullptr; p->pmulti = nullptr; p->ppartial = nullptr;
+    p->niwork = 0;
+    p->pset = PatchSet{};
+    p->pslots = 1;
+    std::vector<int> u((size_t)M * 3);
+    for (int64_t s = 0; s < M; ++s) {
+        const int j = perm[s];
+        for (int t = 0; t < 3; ++t) u[(size_t)s * 3 + t] = wrap(cc[(size_t)j * 3 + t] - m, p->n[t]);
+    }
+    CGS_TRY(dev_alloc(&p->nodeU3, (size_t)M));
+    CGS_TRY(dev_alloc(&p->nodeW, (size_t)M * kW3));
+    {
+        NodeSet ns = node_set(p);
+        CGS_TRY(launch_node_weights3(p->geom, ns, p->nodeU3, p->nodeW, p->stream));
+    }
+    // interpolation bins
+    const int nbz = (n0 + 3) / 4, nby = (n1 + 3) / 4, nbx = (n2 + 3) / 4;
+    const int64_t NB = (int64_t)nbz * nby * nbx;
+    {
+        std::vector<int64_t> cnt(NB + 1, 0);
+        std::vector<int> bin(M);
+        for (int64_t s = 0; s < M; ++s) {
+            const int *us = &u[(size_t)s * 3];
+            bin[s] = (int)(((int64_t)(us[0] / 4) * nby + us[1] / 4) * nbx + us[2] / 4);
+            cnt[bin[s] + 1]++;
+        }
+        for (int64_t b = 0; b < NB; ++b) cnt[b + 1] += cnt[b];
+        std::vector<int> list(M > 0 ? M : 1);
+        std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+        for (int64_t s = 0; s < M; ++s) list[fill[bin[s]]++] = (int)s;
+        std::vector<int4> work;
+        for (int64_t b = 0; b < NB; ++b)
+            for (int64_t s0 = cnt[b]; s0 < cnt[b + 1]; s0 += kInterpGroup)
+                work.push_back(make_int4((int)b, (int)s0, (int)std::min<int64_t>(kInterpGroup, cnt[b + 1] - s0), 0));
+        CGS_TRY(dev_alloc(&p->ilist, list.size()));
+        CGS_TRY(dev_alloc(&p->iwork, std::max<size_t>(work.size(), 1)));
+        CGS_CUDA(cudaMemcpy(p->ilist, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
+        if (!work.empty())
+            CGS_CUDA(cudaMemcpy(p->iwork, work.data(), sizeof(int4) * work.size(), cudaMemcpyHostToDevice));
+        p->niwork = (int)work.size();
+        p->ibx = nbx;
+        p->iby = nby;
+    }
+    if (p->tune.spread_block != 1) {
+        // patches of the axis covering [u, u + taps) (mod n), each once
+        auto axis_patches = [taps](int uu, int n, int *out) {
+            int k = 0;
+            for (int i = 0; i < taps; ++i) {
+                const int q = ((uu + i) % n) / 4;
+                bool seen = false;
+                for (int j = 0; j < k; ++j) seen = seen || (out[j] == q);
+                if (!seen) out[k++] = q;
+            }
+            return k;
+        };
+        const int64_t P = NB;  // patches have the bins' shape
+        // nodes split into contiguous ranges, one host thread each: per-thread
+        // counts, then each thread fills its own positions, so every list
+        // keeps the sorted node order whatever the thread count
+        const int nth = (int)std::max<int64_t>(1, std::min<int64_t>({16, (int64_t)std::thread::hardware_concurrency(),
+                                                                      M / 65536 + 1}));
+        std::vector<std::vector<int64_t>> tcnt(nth, std::vector<int64_t>(P, 0));
+        auto walk = [&](int th, auto &&visit) {
+            const int64_t s0 = M * th / nth, s1 = M * (th + 1) / nth;
+            int pz[16], py[16], px[16];
+            for (int64_t s = s0; s < s1; ++s) {
+                const int *us = &u[(size_t)s * 3];
+                const int kz = axis_patches(us[0], n0, pz), ky = axis_patches(us[1], n1, py),
+                          kx = axis_patches(us[2], n2, px);
+                for (int a = 0; a < kz; ++a)
+                    for (int b = 0; b < ky; ++b) {
+                        const int64_t row = ((int64_t)pz[a] * nby + py[b]) * nbx;
+                        for (int c = 0; c < kx; ++c) visit(row + px[c], s);
+                    }
+            }
+        };
+        auto parallel = [&](auto &&body) {
+            std::vector<std::thread> ts;
+            for (int th = 1; th < nth; ++th) ts.emplace_back(body, th);
+            body(0);
+            for (auto &t : ts) t.join();
+        };
+        parallel([&](int th) {
+            int64_t *c = tcnt[th].data();
+            walk(th, [c](int64_t q, int64_t) { c[q]++; });
+        });
+        std::vector<int64_t> cnt(P + 1, 0);
+        for (int64_t q = 0; q < P; ++q) {
+            int64_t sum = 0;
+            for (int th = 0; th < nth; ++th) sum += tcnt[th][q];
+            cnt[q + 1] = cnt[q] + sum;
+        }
+        const int64_t E = cnt[P];
+        if (E > 0x7fffffffLL) { set_error("3-D patch lists too long"); return CGS_ERR_BAD_ARG; }
+        // per-thread start positions within each patch's list
+        for (int64_t q = 0; q < P; ++q) {
+            int64_t pos = cnt[q];
+            for (int th = 0; th < nth; ++th) {
+                const int64_t c = tcnt[th][q];
+                tcnt[th][q] = pos;
+                pos += c;
+            }
+        }
+        std::vector<int> entries(E > 0 ? E : 1);
+        parallel([&](int th) {
+            int64_t *f = tcnt[th].data();
+            int *e = entries.data();
+            walk(th, [f, e](int64_t q, int64_t s) { e[f[q]++] = (int)s; });
+        });
+        const int64_t avg = std::max<int64_t>(1, E / std::max<int64_t>(P, 1));
+        const int chunk = p->tune.spread_chunk > 0 ? p->tune.spread_chunk
+                                                   : (int)std::min<int64_t>(2048, std::max<int64_t>(64, 2 * avg));
+        std::vector<int4> work, multi;
+        int slots = 0;
+        for (int64_t q = 0; q < P; ++q) {
+            const int64_t a = cnt[q], c = cnt[q + 1] - cnt[q];
+            const int64_t nch = std::max<int64_t>(1, (c + chunk - 1) / chunk);
+            if (nch == 1) {
+                work.push_back(make_int4((int)q, (int)a, (int)c, -1));
+            } else {
+                multi.push_back(make_int4((int)q, slots, (int)nch, 0));
+                for (int64_t k = 0; k < nch; ++k) {
+                    const int64_t b = a + k * chunk;
+                    work.push_back(make_int4((int)q, (int)b, (int)std::min<int64_t>(chunk, a + c - b), slots++));
+                }
+            }
+        }
+        std::stable_sort(work.begin(), work.end(), [](const int4 &x, const int4 &y) { return x.z > y.z; });
+        CGS_TRY(dev_alloc(&p->pentries, entries.size()));
+        CGS_TRY(dev_alloc(&p->pwork, std::max<size_t>(work.size(), 1)));
+        CGS_TRY(dev_alloc(&p->pmulti, std::max<size_t>(1, multi.size())));
+        p->pslots = std::max(slots, 1);
+        CGS_TRY(dev_alloc(&p->ppartial, (size_t)p->pslots * 64 * p->nc));
+        CGS_CUDA(cudaMemcpy(p->pentries, entries.data(), sizeof(int) * entries.size(), cudaMemcpyHostToDevice));
+        if (!work.empty())
+            CGS_CUDA(cudaMemcpy(p->pwork, work.data(), sizeof(int4) * work.size(), cudaMemcpyHostToDevice));
+        if (!multi.empty())
+            CGS_CUDA(cudaMemcpy(p->pmulti, multi.data(), sizeof(int4) * multi.size(), cudaMemcpyHostToDevice));
+        PatchSet &ps = p->pset;
+        ps.ph = 4; ps.pw = 4; ps.pd = 4; ps.blk = 16;
+        ps.npx = nbx; ps.npy = nby;
+        ps.nwork = (int)work.size();
+        ps.entries = p->pentries;
+        ps.work = p->pwork;
+        ps.nodeU = nullptr;
+        ps.nodeW = p->nodeW;
+        ps.nodeU3 = p->nodeU3;
+        ps.partial = p->ppartial;
+        ps.nmulti = (int)multi.size();
+        ps.multi = p->pmulti;
+    }
+    CGS_CUDA(cudaStreamSynchronize(p->stream));
     return CGS_OK;
 }
 
@@ -738,7 +928,15 @@ cgs_status build_toeplitz(cgs_plan *p, int weighted, cudaStream_t st)
     cgs_plan *sub = nullptr;
     CGS_TRY(cgs_plan_create(&sub, &sd));
     float2 *wc = nullptr, *T = nullptr;
-    cgs_status r = cgs_set_kspace(sub, p->k_host.data());
+    cgs_status r = CGS_OK;
+    if (d == 3) {
+        // one spreading pass: the CUDA-core kernel, which needs no patch lists
+        cgs_tuning once{};
+        once.spread_block = 1;
+        once.interp_block = 1;
+        r = cgs_set_tuning(sub, &once);
+    }
+    if (r == CGS_OK) r = cgs_set_kspace(sub, p->k_host.data());
     if (r == CGS_OK) r = dev_alloc(&wc, (size_t)p->M);
     if (r == CGS_OK) r = dev_alloc(&T, (size_t)T2);
     if (r == CGS_OK) {
@@ -1371,6 +1569,7 @@ static cgs_status build_host_chunks(cgs_plan *p, HostChunks &h, int C)
         c->nodeU = p->nodeU; c->nodeW = p->nodeW;
         c->pentries = p->pentries; c->pwork = p->pwork; c->pmulti = p->pmulti;
         c->ilist = p->ilist; c->iwork = p->iwork; c->niwork = p->niwork; c->ibx = p->ibx;
+        c->nodeU3 = p->nodeU3; c->iby = p->iby;
         c->tune = p->tune;
         c->tune.interp_coils = c->tune.spread_coils = 0;
         c->tune.host_chunks = 1;
@@ -1379,6 +1578,9 @@ static cgs_status build_host_chunks(cgs_plan *p, HostChunks &h, int C)
         c->pslots = p->pslots;
         if (p->d == 2) {
             st = dev_alloc(&c->ppartial, (size_t)p->pslots * p->pset.ph * p->pset.pw * c->nc);
+            c->pset.partial = c->ppartial;
+        } else if (p->pset.pd == 4) {
+            st = dev_alloc(&c->ppartial, (size_t)p->pslots * 64 * c->nc);
             c->pset.partial = c->ppartial;
         }
         c->have_k = p->have_k;
@@ -1429,10 +1631,10 @@ cgs_status cgs_plan_destroy(cgs_plan *p)
     if (p->shared_nodes) {  // the parent frees these
         p->nodes = nullptr; p->perm = nullptr; p->iperm = nullptr; p->w = nullptr; p->work = nullptr;
         p->nodeU = nullptr; p->nodeW = nullptr; p->pentries = nullptr; p->pwork = nullptr; p->pmulti = nullptr;
-        p->ilist = nullptr; p->iwork = nullptr;
+        p->ilist = nullptr; p->iwork = nullptr; p->nodeU3 = nullptr;
     }
     void *bufs[] = {p->tw[0], p->tw[1], p->tw[2], p->deap[0], p->deap[1], p->deap[2], p->nodes, p->perm, p->iperm,
-                    p->w, p->work, p->nodeU, p->nodeW, p->pentries, p->pwork, p->pmulti, p->ppartial, p->ilist, p->iwork, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
+                    p->w, p->work, p->nodeU, p->nodeW, p->pentries, p->pwork, p->pmulti, p->ppartial, p->ilist, p->iwork, p->nodeU3, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
                     p->cF, p->cP, p->cZ, p->vX, p->vR, p->vP, p->vQ, p->ioA, p->ioB, p->partial, p->dots,
                     p->active, p->sc, p->fpart, p->ftick};
     for (void *b : bufs) dev_free(b);
@@ -1557,6 +1759,15 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
     if (d == 2) {
         CGS_TRY(build_patches(p, cc));
         CGS_TRY(build_ibins(p, cc, perm));
+    } else if (grid3_mma_ok(p->geom) && !(p->tune.spread_block == 1 && p->tune.interp_block == 1)) {
+        CGS_TRY(build_grid3(p, cc, perm));
+    } else {
+        for (void *b : {(void *)p->nodeU3, (void *)p->nodeW, (void *)p->ilist, (void *)p->iwork, (void *)p->pentries,
+                        (void *)p->pwork, (void *)p->pmulti, (void *)p->ppartial}) dev_free(b);
+        p->nodeU3 = nullptr; p->nodeW = nullptr; p->ilist = nullptr; p->iwork = nullptr;
+        p->pentries = nullptr; p->pwork = nullptr; p->pmulti = nullptr; p->ppartial = nullptr;
+        p->niwork = 0;
+        p->pset = PatchSet{};
     }
     p->k_host = k;
     p->have_k = true;
@@ -2076,7 +2287,8 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
         return CGS_OK;
     }
     const bool bins = t->tile != p->tune.tile || t->work_slice != p->tune.work_slice ||
-                      t->spread_chunk != p->tune.spread_chunk || t->spread_block != p->tune.spread_block;
+                      t->spread_chunk != p->tune.spread_chunk || t->spread_block != p->tune.spread_block ||
+                      (p->d == 3 && t->interp_block != p->tune.interp_block);
     p->tune = *t;
     apply_tiles(p);
     drop_graphs(p);
@@ -2118,7 +2330,7 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
         return CGS_OK;
     };
     auto interp = [&]() -> cgs_status {
-        NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork, p->niwork, p->ibx};
+        NodeSet ns = node_set(p);
         return launch_interp(p->geom, ns, p->grid, p->ksR, st);
     };
     auto spread = [&]() -> cgs_status {

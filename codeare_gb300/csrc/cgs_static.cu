@@ -20,7 +20,12 @@
 //     without ordering) race and corrupt each other's results;
 //   * the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture.
+//     before any stream capture.  The address is kept for the life of the
+//     process: a cudaDeviceReset unloads the module, and calls on that device
+//     after a reset are not supported;
+//   * a node outside [-0.5, 0.5) in either coordinate gets NaN in f (the plan
+//     entry points reject such a trajectory with an error instead; this call
+//     does not read k on the host).
 // Nothing here sorts the nodes (sorting needs a plan), so the interpolation
 // reads the grid per node straight from global memory / L2.
 #include "cgs_internal.cuh"
@@ -38,9 +43,11 @@ static __device__ __align__(256) float2 g_static_scratch[kStaticElems];
 
 std::mutex g_static_mu;
 float2 *g_static_ptr[kMaxDevices] = {};
+int g_static_sms[kMaxDevices] = {};
 
-// once per device, with the device current: the array's device address
-cgs_status static_scratch(float2 **out)
+// once per device, with the device current: the array's device address and
+// the device's SM count (it sizes the interpolation grid)
+cgs_status static_scratch(float2 **out, int *sms)
 {
     int dev = 0;
     CGS_CUDA(cudaGetDevice(&dev));
@@ -53,9 +60,17 @@ cgs_status static_scratch(float2 **out)
             set_error(std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(e));
             return CGS_ERR_CUDA;
         }
+        int nsm = 0;
+        e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess || nsm <= 0) {
+            set_error(std::string("cudaDeviceGetAttribute(SM count): ") + cudaGetErrorString(e));
+            return CGS_ERR_CUDA;
+        }
         g_static_ptr[dev] = (float2 *)p;
+        g_static_sms[dev] = nsm;
     }
     *out = g_static_ptr[dev];
+    *sms = g_static_sms[dev];
     return CGS_OK;
 }
 
@@ -159,6 +174,10 @@ extern "C" cgs_status cgs_nfft2d_trafo_noalloc(int N, double alpha, int m, int64
         set_error("cgs_nfft2d_trafo_noalloc: need even N >= 2, alpha >= 1, 0 <= m <= 8, M >= 0");
         return CGS_ERR_BAD_ARG;
     }
+    if (!(alpha * (double)N <= 2048.0)) {  // also catches alpha = inf before the cast below
+        set_error("cgs_nfft2d_trafo_noalloc: oversampled size ceil(alpha*N) must be at most 2048");
+        return CGS_ERR_BAD_ARG;
+    }
     const int n = (int)std::ceil(alpha * N);
     const int64_t need = (int64_t)N * n + (int64_t)n * n + 2 * (int64_t)n + N;
     if (need > kStaticElems) {
@@ -178,7 +197,8 @@ extern "C" cgs_status cgs_nfft2d_trafo_noalloc(int N, double alpha, int m, int64
         return CGS_ERR_BAD_ARG;
     }
     float2 *s = nullptr;
-    CGS_TRY(static_scratch(&s));
+    int sms = 0;
+    CGS_TRY(static_scratch(&s, &sms));
     cudaStream_t st = (cudaStream_t)stream;
     float2 *t1 = s;                                  // [N][n]  rows transformed along x
     float2 *grid = t1 + (int64_t)N * n;              // [n][n]
@@ -200,7 +220,7 @@ extern "C" cgs_status cgs_nfft2d_trafo_noalloc(int N, double alpha, int m, int64
     y.outer = 1; y.inner = n; y.Lin = N; y.Lout = n;
     y.src = t1; y.dst = grid;
     CGS_TRY(launch_axis_pass(y, st));
-    const int64_t blocks = std::min<int64_t>((M + 255) / 256, 152 * 8);
+    const int64_t blocks = std::min<int64_t>((M + 255) / 256, (int64_t)sms * 8);
     static_interp_kernel<<<(unsigned)blocks, 256, 0, st>>>(k, M, grid, n, m, (float)b,
                                                           reinterpret_cast<float2 *>(f));
     CGS_LAUNCH_CHECK();

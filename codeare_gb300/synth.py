@@ -212,6 +212,13 @@ def kooshball3d_128_16coils(N: int = 128, nc: int = 16, nspokes: int = 20000, ns
                 sens=coils3d(N, nc), k=k, w=w, alpha=2.0, m=4, cgeps=1e-4, noise=0.0, seed=SEED_BASE + 3)
 
 
+def kooshball3d_64_downsample():
+    """The 64^3 downsample of the 128^3 kooshball workload: every length halved
+    (64^3 phantom, 5000 spokes x 128 samples, the same spokes per N^2 and the
+    same 2x readout oversampling), 16 coils, |k|^2 weights, sigma=2, m=4."""
+    return kooshball3d_128_16coils(N=64, nc=16, nspokes=5000, nsamp=128)
+
+
 def uneven_batch(count: int = 64, seed: int = SEED_BASE + 2):
     """Batched uneven CG-SENSE: per problem N in 96..320 (step 32), NC in
     {4, 8, 16, 32}, golden-angle radial 32..400 spokes x 512; every fourth

@@ -275,7 +275,11 @@ int64_t cgs_kernel_launches(void);
  * sizes return CGS_ERR_BAD_ARG.  k (M x 2 floats), fhat (N x N complex) and
  * f (M complex) must be device pointers.  All calls share the array, so
  * calls that overlap on the GPU race; the first call on a device resolves
- * the array's address and should come before any stream capture. */
+ * the array's address and should come before any stream capture.  The
+ * address is kept until exit, so a cudaDeviceReset invalidates it: do not
+ * call this again on a device that was reset.  k is not read on the host:
+ * a node outside [-0.5, 0.5) in either coordinate gets NaN in f and the call
+ * still returns CGS_OK (the plan entry points reject such a trajectory). */
 cgs_status cgs_nfft2d_trafo_noalloc(int N, double alpha, int m, int64_t M, const float *k,
                                     const float *fhat, float *f, void *stream);
 
