@@ -525,20 +525,24 @@ def kooshball64_check():
 
 
 def learned_section():
-    """Learned-preconditioned flexible CG against plain GPU CG (and
-    Jacobi CG) to relative residual 1e-4 on a held-out 256^2, 16-coil
-    golden-angle problem, with each image's error against the converged plain
-    solve.  Uses the committed trained weights; null when they are absent."""
+    """Learned-preconditioned flexible CG against plain GPU CG (and Jacobi and
+    circulant-preconditioned CG) to relative residual 1e-4 on eight held-out
+    256^2, 16-coil golden-angle problems spread over 32-100 spokes, with each
+    image's error against the converged plain solve.  The learned arm is the
+    circulant step plus the network's local correction.  Uses the committed
+    trained weights; null when they are absent."""
     from codeare_gb300 import learned
     net = learned.load_net()
     if net is None:
         return None
-    r = learned.compare(net, seed=777)
+    rows, summary = learned.compare_many(net)
     net.close()
-    r["workload"] = ("learned preconditioner: 256^2, 16 coils, golden-angle radial x 512, random-ellipse phantom, "
-                     "Toeplitz E^H W E, lambda = 1e-3 mean diagonal, to ||r||/||r0|| = 1e-4")
-    r["speedup_vs_plain"] = r["plain"]["ms"] / r["learned"]["ms"]
-    return r
+    return {"workload": ("learned preconditioner: 256^2, 16 coils, golden-angle radial 32..100 spokes x 512, "
+                         "random-ellipse phantoms, Toeplitz E^H W E, lambda = 1e-3 mean diagonal, to "
+                         "||r||/||r0|| = 1e-4; eight held-out problems"),
+            "problems": rows, "summary": summary,
+            "speedup_vs_plain": summary["learned"]["median_speedup_vs_plain"],
+            "circulant_speedup_vs_plain": summary["circulant"]["median_speedup_vs_plain"]}
 
 
 def run_ours(args):
@@ -714,6 +718,46 @@ def run_ours(args):
     return 0
 
 
+def run_profile_case(args):
+    """Forward + adjoint steps of one workload and nothing else, for profiler
+    captures (prints one summary line, no JSON contract):
+      nufft256    -- the 256^2, 32-coil NuFFT of the headline (default tuning);
+      kooshball64 -- the 64^3 downsample of the kooshball, 16 coils, E and E^H W."""
+    import torch
+    import codeare_gb300 as cg
+    from codeare_gb300 import capi, synth
+    torch.cuda.set_device(0)
+    if args.profile_case == "nufft256":
+        k, fh = workload_data()
+        p = cg.Plan((N, N), k.shape[0], ncoils=NC, m=M_KB, alpha=SIGMA)
+        p.set_kspace(k)
+        a = torch.from_numpy(fh).cuda()
+        b = torch.empty((NC, k.shape[0]), dtype=torch.complex64, device="cuda")
+
+        def step():
+            p.nfft_trafo(a, b)
+            p.nfft_adjoint(b, a)
+    else:
+        c = synth.kooshball3d_64_downsample()
+        k = c["k"]
+        p = capi.Plan(c["shape"], k.shape[0], ncoils=c["sens"].shape[0], m=c["m"], alpha=c["alpha"])
+        p.set_kspace(k)
+        p.set_weights(c["w"])
+        p.set_sensitivities(np.ascontiguousarray(c["sens"]))
+        a = torch.from_numpy(np.ascontiguousarray(c["image"])).cuda()
+        b = torch.empty((c["sens"].shape[0], k.shape[0]), dtype=torch.complex64, device="cuda")
+
+        def step():
+            p.sense_trafo(a, b)
+            p.sense_adjoint(b, a, weighted=True)
+    for _ in range(args.warmup + args.steps):
+        step()
+    torch.cuda.synchronize()
+    p.close()
+    print("profile case %s: %d steps" % (args.profile_case, args.warmup + args.steps))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -724,7 +768,11 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default gridding decomposition (profiling runs: no candidate launches)")
     ap.add_argument("--no-cgsense", action="store_true", help="skip the CG-SENSE, batch, kooshball, learned-preconditioner and CS sections")
+    ap.add_argument("--profile-case", choices=["nufft256", "kooshball64"],
+                    help="run only this workload's forward+adjoint steps (profiler captures; no JSON line)")
     args = ap.parse_args()
+    if args.profile_case:
+        return run_profile_case(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

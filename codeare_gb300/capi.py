@@ -27,7 +27,7 @@ EXPORTED = [
     "cgs_plan_info", "cgs_sync", "cgs_kernel_launches", "cgs_last_error",
     "cgs_profile_enable", "cgs_profile_collect", "cgs_nfft2d_trafo_noalloc",
     "cgs_net_num_params", "cgs_net_create", "cgs_net_destroy", "cgs_net_set_weights", "cgs_net_get_weights",
-    "cgs_net_forward", "cgs_net_gradients", "cgs_net_train_step", "cgs_solve_fcg", "cgs_normal_apply",
+    "cgs_net_forward", "cgs_net_gradients", "cgs_net_train_step", "cgs_solve_fcg", "cgs_normal_apply", "cgs_precond_apply",
     "cgs_get_tuning", "cgs_set_tuning", "cgs_autotune", "cgs_batch_create", "cgs_batch_solve",
     "cgs_batch_destroy", "cgs_cs_create", "cgs_cs_destroy", "cgs_cs_adjoint", "cgs_cs_df", "cgs_cs_obj",
     "cgs_cs_wavelet",
@@ -117,6 +117,7 @@ def load(path: str = LIB_PATH):
     L.cgs_nfft2d_trafo_noalloc.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int64, vp, vp, vp, vp]
     L.cgs_solve_fcg.argtypes = [vp, vp, vp, vp, C.POINTER(SolveOpts), vp, C.POINTER(SolveReport), vp]
     L.cgs_normal_apply.argtypes = [vp, vp, vp, C.POINTER(SolveOpts), vp]
+    L.cgs_precond_apply.argtypes = [vp, vp, vp, C.POINTER(SolveOpts), vp]
     L.cgs_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.cgs_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.cgs_autotune.argtypes = [vp, C.POINTER(Tuning), C.POINTER(C.c_double), vp]
@@ -320,16 +321,23 @@ class Plan:
         return t.as_dict(), ms.value
 
     def solve_fcg(self, out, y=None, rhs=None, net=None, cgiter=200, cgeps=1e-4, lam=0.0, weighted=True,
-                  toeplitz=True, jacobi=False, stream=None):
-        """flexible CG with the learned preconditioner `net`; without one, plain CG
-        or (jacobi=True) CG preconditioned by the exact diagonal of the normal
-        operator"""
+                  toeplitz=True, jacobi=False, circulant=False, stream=None):
+        """flexible CG with the learned preconditioner `net`; without one, plain CG,
+        (jacobi=True) CG preconditioned by the exact diagonal of the normal
+        operator or (circulant=True) by the circulant of precond_apply.  With a
+        net, circulant=True makes the net correct the circulant step."""
+        kind = 2 if circulant else (1 if jacobi else 0)
         o = SolveOpts(MODE_STANDARD, int(cgiter), float(cgeps), float(lam), 0, 0.0, int(bool(weighted)),
-                      int(bool(toeplitz)), int(bool(jacobi)))
+                      int(bool(toeplitz)), kind)
         rep = SolveReport()
         self._go(load().cgs_solve_fcg, None if y is None else _ptr(y), None if rhs is None else _ptr(rhs),
                  _ptr(out), C.byref(o), None if net is None else net._h, C.byref(rep), stream=stream)
         return _report(rep)
+
+    def precond_apply(self, r, out, lam=0.0, weighted=True, stream=None):
+        """out = C r, the circulant preconditioner of the normal equations"""
+        o = SolveOpts(MODE_STANDARD, 0, 0.0, float(lam), 0, 0.0, int(bool(weighted)), 1, 2)
+        self._go(load().cgs_precond_apply, _ptr(r), _ptr(out), C.byref(o), stream=stream)
 
     def normal_apply(self, x, out, lam=0.0, weighted=True, toeplitz=True, stream=None):
         o = SolveOpts(MODE_STANDARD, 0, 0.0, float(lam), 0, 0.0, int(bool(weighted)), int(bool(toeplitz)))

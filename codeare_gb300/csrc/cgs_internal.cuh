@@ -268,8 +268,9 @@ struct FCGScalars {
     CGScalars cg;        // lambda, done, iter, maxit, tol, hist, nan_flag
     double rr, rr0, rz, pq, zr, zro, beta, best;
     int stall, fallback, use_r, restart, fallback_at;
-    int mode;            // 0 plain, 1 Jacobi, 2 scaled network
+    int mode;            // 0 plain, 1 Jacobi, 2 scaled network, 3 circulant, 4 circulant + network
     double sumw, tt;     // sum of the density weights; |d . r|^2 for the net
+    double dsum;         // sum over pixels and coils of |S|^2 (the circulant's lambda scale)
 };
 cgs_status launch_fcg_kernels(int which, FCGScalars *fs, float2 *x, float2 *r, float2 *rold, float2 *p,
                               const float2 *q, float2 *z, int64_t n, cudaGraphConditionalHandle h,
@@ -289,6 +290,21 @@ cgs_status launch_jacobi_scale(const float2 *sens, int64_t P, int nc, const FCGS
 // scaling steps of the preconditioner
 cgs_status launch_diag_scale(const float2 *in, const float2 *add, const float *d, int power, int64_t n,
                              float2 *out, cudaStream_t st);
+// circulant preconditioner (2-D): the T. Chan fold of the 2N point-spread
+// function T[2N0][2N1] (index d + N) onto the N-periodic grid,
+//   cN[d mod N] = sum (1 - |d0|/N0)(1 - |d1|/N1) T[d]
+cgs_status launch_circ_fold(const float2 *T, int N0, int N1, float2 *cN, cudaStream_t st);
+// csq[p] = 1 / sqrt(sum_c |S[p][c]|^2) (0 where the coils vanish)
+cgs_status launch_coil_rsqrt(const float2 *sens, int64_t P, int nc, float *csq, cudaStream_t st);
+// kinv = 1 / (P (spec + lambda P / dsum)): the spectrum of the inverse circulant,
+// with the 1/P of the unnormalised FFT pair folded in
+cgs_status launch_circ_kinv(const float *spec, const FCGScalars *fs, int64_t P, float *kinv, cudaStream_t st);
+// out = dx . x + (y ? (dy ? dy . y : y) : 0), real per-pixel factors
+cgs_status launch_scale_add(float2 *out, const float2 *x, const float *dx, const float2 *y, const float *dy,
+                            int64_t n, cudaStream_t st);
+// fixed-preconditioner loop: zr = Re <z, r>, Fletcher-Reeves beta = zr / rz, loop test
+cgs_status launch_fcg_zr_check(FCGScalars *fs, const float2 *z, const float2 *r, int64_t n, double *partial,
+                               unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st);
 // z = M(r): the learned preconditioner on one complex image (cgs_cnn.cu);
 // nrm2 = sum |r|^2 on the device sets the input scale
 uint64_t net_serial(const cgs_net *n);   // 0 for null, else unique per created network

@@ -250,6 +250,14 @@ struct cgs_plan {
     float2 *vB = nullptr, *vZ = nullptr, *vO = nullptr, *vT = nullptr;
     float *dscale = nullptr;
     FCGScalars *fs = nullptr;
+    // circulant preconditioner (2-D): floored T. Chan spectrum of the weighted
+    // point-spread function, its lambda-dependent inverse, 1/sqrt(sum |S|^2),
+    // two scratch images and N-point FFT twiddles per axis
+    float *circ = nullptr, *circ_inv = nullptr, *csq = nullptr;
+    float2 *vC = nullptr, *vCo = nullptr;
+    float2 *twN[2] = {nullptr, nullptr};
+    int facN[2][12] = {}, nfacN[2] = {0, 0};
+    bool circ_valid = false;
     cudaGraphExec_t fcg_exec = nullptr;
     int fg_src = -1, fg_toep = -1, fg_weighted = -1, fg_mode = -1;
     uint64_t fg_net = 0;
@@ -893,6 +901,106 @@ void drop_graphs(cgs_plan *p)
     if (p->fcg_exec) { cudaGraphExecDestroy(p->fcg_exec); p->fcg_exec = nullptr; }
 }
 
+// N-point FFT pass along axis t of the image grid (circulant preconditioner)
+static cgs_status circ_twiddles(cgs_plan *p)
+{
+    for (int t = 0; t < 2; ++t) {
+        if (p->twN[t]) continue;
+        if (!factorize(p->N[t], p->facN[t], &p->nfacN[t])) {
+            set_error("the circulant preconditioner needs image sides that factor into 2, 3, 5, 7");
+            return CGS_ERR_BAD_ARG;
+        }
+        std::vector<float2> tw(p->N[t]);
+        for (int i = 0; i < p->N[t]; ++i) {
+            const double a = -2.0 * M_PI * (double)i / (double)p->N[t];
+            tw[i] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+        CGS_TRY(dev_alloc(&p->twN[t], (size_t)p->N[t]));
+        CGS_CUDA(cudaMemcpy(p->twN[t], tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice));
+    }
+    return CGS_OK;
+}
+
+static AxisPass circ_pass(cgs_plan *p, int t)
+{
+    AxisPass a{};
+    a.n = p->N[t];
+    a.tw = p->twN[t];
+    a.nfac = p->nfacN[t];
+    for (int i = 0; i < 12; ++i) a.fac[i] = p->facN[t][i];
+    a.load_mode = LOAD_PLAIN;
+    a.store_mode = STORE_PLAIN;
+    a.o1_len = 1;
+    a.Lin = a.Lout = p->N[t];
+    return a;
+}
+
+// in-place 2-D transform of an N0 x N1 image: axis 1 with `sign1`, then axis 0
+// (forward; with kinv also multiplied by kinv[pos0][pos1] and transformed back)
+static cgs_status circ_fft2(cgs_plan *p, float2 *v, int sign1, const float *kinv, cudaStream_t st)
+{
+    AxisPass a = circ_pass(p, 1);
+    a.outer = p->N[0]; a.inner = 1; a.sign = sign1; a.src = v; a.dst = v;
+    CGS_TRY(launch_axis_pass(a, st));
+    if (sign1 > 0) return CGS_OK;
+    AxisPass b = circ_pass(p, 0);
+    b.outer = 1; b.inner = p->N[1]; b.sign = -1; b.src = v; b.dst = v;
+    b.toep_k = kinv; b.toep_nc = 1;
+    return launch_axis_pass(b, st);
+}
+
+// Floored T. Chan spectrum of the point-spread function T[2N0][2N1] (index
+// d + N): fold onto the N-periodic grid, 2-D DFT, real part, floor at
+// kCircFloor times its mean (the unsampled k-space corners and the gaps
+// between spokes would otherwise give near-zero eigenvalues whose inverse
+// amplifies noise).  Runs once per Toeplitz kernel.
+constexpr double kCircFloor = 0.2;
+static cgs_status build_circulant(cgs_plan *p, const float2 *T, cudaStream_t st)
+{
+    p->circ_valid = false;
+    if (p->d != 2) return CGS_OK;
+    CGS_TRY(circ_twiddles(p));
+    const int64_t P = p->Nt;
+    if (!p->vC) CGS_TRY(dev_alloc(&p->vC, (size_t)P));
+    if (!p->circ) CGS_TRY(dev_alloc(&p->circ, (size_t)P));
+    CGS_TRY(launch_circ_fold(T, p->N[0], p->N[1], p->vC, st));
+    CGS_TRY(circ_fft2(p, p->vC, -1, nullptr, st));
+    std::vector<float2> spec(P);
+    CGS_CUDA(cudaMemcpyAsync(spec.data(), p->vC, sizeof(float2) * P, cudaMemcpyDeviceToHost, st));
+    CGS_CUDA(cudaStreamSynchronize(st));
+    double mean = 0.0;
+    for (const float2 &v : spec) mean += (double)v.x;
+    mean /= (double)P;
+    const double floor = kCircFloor * std::max(mean, 0.0);
+    std::vector<float> c(P);
+    for (int64_t i = 0; i < P; ++i) c[i] = (float)std::max((double)spec[i].x, floor);
+    CGS_CUDA(cudaMemcpy(p->circ, c.data(), sizeof(float) * P, cudaMemcpyHostToDevice));
+    p->circ_valid = true;
+    return CGS_OK;
+}
+
+// z = C(r) = csq . IFFT(kinv . FFT(csq . r)), kinv and csq set for the current
+// lambda and sensitivities (fcg prologue or cgs_precond_apply); out may not alias r
+static cgs_status op_circ(cgs_plan *p, const float2 *r, float2 *out, cudaStream_t st)
+{
+    const int64_t P = p->Nt;
+    CGS_TRY(launch_diag_scale(r, nullptr, p->csq, 1, P, p->vC, st));
+    CGS_TRY(circ_fft2(p, p->vC, -1, p->circ_inv, st));
+    CGS_TRY(circ_fft2(p, p->vC, +1, nullptr, st));
+    return launch_diag_scale(p->vC, nullptr, p->csq, 1, P, out, st);
+}
+
+// the circulant's lambda- and coil-dependent factors from fs->cg.lambda
+static cgs_status circ_prepare(cgs_plan *p, FCGScalars *fs, cudaStream_t st)
+{
+    const int64_t P = p->Nt;
+    if (!p->csq) CGS_TRY(dev_alloc(&p->csq, (size_t)P));
+    if (!p->circ_inv) CGS_TRY(dev_alloc(&p->circ_inv, (size_t)P));
+    CGS_TRY(launch_coil_rsqrt(p->sens, P, p->nc, p->csq, st));
+    CGS_TRY(launch_coldot(p->sens, p->sens, nullptr, P * p->nc, 1, p->partial, &fs->dsum, st));
+    return launch_circ_kinv(p->circ, fs, P, p->circ_inv, st);
+}
+
 cgs_status build_toeplitz(cgs_plan *p, int weighted, cudaStream_t st)
 {
     drop_graphs(p);
@@ -952,6 +1060,7 @@ cgs_status build_toeplitz(cgs_plan *p, int weighted, cudaStream_t st)
         if (cudaGetLastError() != cudaSuccess) r = CGS_ERR_CUDA;
         count_launch();
     }
+    if (r == CGS_OK && d == 2) r = build_circulant(p, T, st);
     // DFT of the circulant kernel: centred input (index d + N <-> position d mod 2N), full output
     for (int t = 0; t < d && r == CGS_OK; ++t) {
         AxisPass a = toep_pass(p, t);
@@ -1161,15 +1270,26 @@ cgs_status fcg_alloc(cgs_plan *p)
     if (!p->vT) CGS_TRY(dev_alloc(&p->vT, (size_t)p->Nt));
     if (!p->dscale) CGS_TRY(dev_alloc(&p->dscale, (size_t)p->Nt));
     if (!p->fs) CGS_TRY(dev_alloc(&p->fs, 1));
+    if (p->d == 2 && !p->vCo) CGS_TRY(dev_alloc(&p->vCo, (size_t)p->Nt));
     return CGS_OK;
 }
 
 // z = M(r): mode 2 d . (t + net(t)) with t = d . r (the network corrects the
-// Jacobi step); mode 1 d^2 . r; mode 0 (or after the fallback) z = r
+// Jacobi step); mode 1 d^2 . r; mode 3 the circulant C(r); mode 4
+// C(r) + d . net(t) (the network corrects the circulant step); mode 0 (or
+// after the fallback) z = r
 cgs_status fcg_precondition(cgs_plan *p, cgs_net *net, int mode, cudaStream_t st)
 {
     const int64_t Nt = p->Nt;
-    if (mode == 2) {
+    if (mode == 4) {
+        CGS_TRY(op_circ(p, p->vR, p->vCo, st));
+        CGS_TRY(launch_diag_scale(p->vR, nullptr, p->dscale, 1, Nt, p->vT, st));
+        CGS_TRY(launch_coldot(p->vT, p->vT, nullptr, Nt, 1, p->partial, &p->fs->tt, st));
+        CGS_TRY(net_apply_image(net, p->vT, &p->fs->tt, p->N[0], p->N[1], p->vZ, st));
+        CGS_TRY(launch_scale_add(p->vZ, p->vZ, p->dscale, p->vCo, nullptr, Nt, st));
+    } else if (mode == 3) {
+        CGS_TRY(op_circ(p, p->vR, p->vZ, st));
+    } else if (mode == 2) {
         CGS_TRY(launch_diag_scale(p->vR, nullptr, p->dscale, 1, Nt, p->vT, st));
         CGS_TRY(launch_coldot(p->vT, p->vT, nullptr, Nt, 1, p->partial, &p->fs->tt, st));
         CGS_TRY(net_apply_image(net, p->vT, &p->fs->tt, p->N[0], p->N[1], p->vZ, st));
@@ -1209,6 +1329,7 @@ cgs_status build_fcg_graph(cgs_plan *p, int from_data, int toeplitz, int weighte
         if (q == CGS_OK) q = launch_zero(p->vP, sizeof(float2) * Nt, st);
         if (q == CGS_OK) q = launch_zero(p->vO, sizeof(float2) * Nt, st);
         if (q == CGS_OK && mode != 0) q = launch_jacobi_scale(p->sens, Nt, p->nc, fs, p->dscale, st);
+        if (q == CGS_OK && mode >= 3) q = circ_prepare(p, fs, st);
         if (q == CGS_OK) q = launch_coldot(p->vR, p->vR, nullptr, Nt, 1, p->partial, &fs->rr, st);
         if (q == CGS_OK) q = K(FCG_INIT, h);
         if (q == CGS_OK) q = fcg_precondition(p, net, mode, st);
@@ -1244,13 +1365,15 @@ cgs_status build_fcg_graph(cgs_plan *p, int from_data, int toeplitz, int weighte
         r = CGS_ERR_CUDA;
     if (r == CGS_OK) {
         cgs_status q = CGS_OK;
-        if (mode < 2) {
+        if (mode < 2 || mode == 3) {
             // fixed preconditioner: fused updates, Fletcher-Reeves beta
             q = op_normal(p, p->vP, p->vQ, toeplitz, weighted, nullptr, st);
             if (q == CGS_OK) q = launch_axpy_dot(p->vQ, p->vP, &fs->cg.lambda, nullptr, Nt, p->fpart, p->ftick, &fs->pq, st);
             if (q == CGS_OK) q = launch_fcg_xr_rr(fs, p->vX, p->vR, p->vP, p->vQ, Nt, p->fpart, p->ftick, h, st);
             if (q == CGS_OK && mode == 1)
                 q = launch_fcg_jacobi_z(fs, p->vZ, p->vR, p->dscale, Nt, p->fpart, p->ftick, h, st);
+            if (q == CGS_OK && mode == 3) q = op_circ(p, p->vR, p->vZ, st);
+            if (q == CGS_OK && mode == 3) q = launch_fcg_zr_check(fs, p->vZ, p->vR, Nt, p->fpart, p->ftick, h, st);
             if (q == CGS_OK) q = K(FCG_P, h);
             cudaGraph_t bb = body;
             if (cudaStreamEndCapture(st, &bb) != cudaSuccess && q == CGS_OK) q = CGS_ERR_CUDA;
@@ -1642,7 +1765,9 @@ cgs_status cgs_plan_destroy(cgs_plan *p)
                     (void *)p->tB}) dev_free(b);
     if (p->solve_exec) cudaGraphExecDestroy(p->solve_exec);
     if (p->fcg_exec) cudaGraphExecDestroy(p->fcg_exec);
-    for (void *b : {(void *)p->vB, (void *)p->vZ, (void *)p->vO, (void *)p->vT, (void *)p->dscale, (void *)p->fs})
+    for (void *b : {(void *)p->vB, (void *)p->vZ, (void *)p->vO, (void *)p->vT, (void *)p->dscale, (void *)p->fs,
+                    (void *)p->circ, (void *)p->circ_inv, (void *)p->csq, (void *)p->vC, (void *)p->vCo,
+                    (void *)p->twN[0], (void *)p->twN[1]})
         dev_free(b);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
@@ -2205,7 +2330,13 @@ cgs_status cgs_solve_fcg(cgs_plan *p, const float *y, const float *rhs, float *x
         CGS_TRY(stage_in(rhs, sizeof(float2) * p->Nt, p->ioA, &src, st));
         CGS_CUDA(cudaMemcpyAsync(p->vB, src, sizeof(float2) * p->Nt, cudaMemcpyDeviceToDevice, st));
     }
-    const int mode = net ? 2 : (o->jacobi ? 1 : 0);
+    // o->jacobi: 0 none, 1 the exact diagonal, 2 the circulant (with a net: its correction's base)
+    if (o->jacobi < 0 || o->jacobi > 2) { set_error("preconditioner kind must be 0, 1 or 2"); return CGS_ERR_BAD_ARG; }
+    const int mode = net ? (o->jacobi == 2 ? 4 : 2) : (o->jacobi == 2 ? 3 : (o->jacobi ? 1 : 0));
+    if (mode >= 3) {
+        const int wtd = (o->weighted && p->have_w) ? 1 : 0;
+        if (!p->toep_valid || p->toep_weighted != wtd || !p->circ_valid) CGS_TRY(build_toeplitz(p, wtd, st));
+    }
     const bool same = p->fcg_exec && p->fg_src == from_data && p->fg_toep == o->toeplitz &&
                       p->fg_weighted == o->weighted && p->fg_net == net_serial(net) && p->fg_mode == mode;
     if (!same) CGS_TRY(build_fcg_graph(p, from_data, o->toeplitz, o->weighted, net, mode, st));
@@ -2246,6 +2377,26 @@ cgs_status cgs_solve_fcg(cgs_plan *p, const float *y, const float *rhs, float *x
     return h.cg.nan_flag ? CGS_ERR_NAN : CGS_OK;
 }
 
+
+cgs_status cgs_precond_apply(cgs_plan *p, const float *r, float *z, const cgs_solve_opts *o, void *stream)
+{
+    if (!o || !r || !z) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    CGS_TRY(check_ready(p, o->weighted != 0, true));
+    if (p->d != 2 || p->F > 1) { set_error("the circulant preconditioner is built for single-frame 2-D plans"); return CGS_ERR_BAD_ARG; }
+    cudaStream_t st = pick_stream(p, stream);
+    CGS_TRY(fcg_alloc(p));
+    const int wtd = (o->weighted && p->have_w) ? 1 : 0;
+    if (!p->toep_valid || p->toep_weighted != wtd || !p->circ_valid) CGS_TRY(build_toeplitz(p, wtd, st));
+    FCGScalars init{};
+    init.cg.lambda = o->lambda;
+    CGS_CUDA(cudaMemcpyAsync(p->fs, &init, sizeof(init), cudaMemcpyHostToDevice, st));
+    CGS_TRY(circ_prepare(p, p->fs, st));
+    const void *src;
+    CGS_TRY(stage_in(r, sizeof(float2) * p->Nt, p->ioA, &src, st));
+    CGS_CUDA(cudaMemcpyAsync(p->vZ, src, sizeof(float2) * p->Nt, cudaMemcpyDeviceToDevice, st));
+    CGS_TRY(op_circ(p, p->vZ, p->vQ, st));
+    return image_out(p, p->vQ, z, st);
+}
 
 cgs_status cgs_get_tuning(const cgs_plan *p, cgs_tuning *out)
 {

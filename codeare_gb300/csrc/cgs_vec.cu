@@ -518,7 +518,7 @@ __global__ void fcg_decide_kernel(FCGScalars *fs)
 {
     if (fs->rr < fs->best) { fs->best = fs->rr; fs->stall = 0; }
     else fs->stall += 1;
-    if (fs->mode == 2 && !fs->fallback && fs->stall >= kStallChecks) {
+    if ((fs->mode == 2 || fs->mode == 4) && !fs->fallback && fs->stall >= kStallChecks) {
         fs->fallback = 1;
         fs->restart = 1;
         fs->fallback_at = fs->cg.iter;
@@ -533,7 +533,7 @@ __global__ void fcg_select_kernel(const FCGScalars *fs, float2 *__restrict__ z, 
 
 __global__ void fcg_beta_kernel(FCGScalars *fs)
 {
-    if (fs->mode == 2 && !fs->fallback && !(fs->zr > 0.0)) {   // the network gave no descent direction
+    if ((fs->mode == 2 || fs->mode == 4) && !fs->fallback && !(fs->zr > 0.0)) {   // no descent direction
         fs->fallback = 1;
         fs->restart = 1;
         fs->use_r = 1;
@@ -640,6 +640,85 @@ fcg_jacobi_z_kernel(FCGScalars *fs, float2 *__restrict__ z, const float2 *__rest
         fs->rz = t;
         fs->use_r = 0;
         cudaGraphSetConditional(h, fcg_check_logic(fs));
+    }
+}
+
+// fixed preconditioner given z: zr = Re <z, r>, Fletcher-Reeves beta = zr / rz, loop test
+__global__ void __launch_bounds__(kThreads)
+fcg_zr_check_kernel(FCGScalars *fs, const float2 *__restrict__ z, const float2 *__restrict__ r, int64_t n,
+                    double *partial, unsigned int *ticket, cudaGraphConditionalHandle h)
+{
+    double acc = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const float2 zv = z[e], rv = r[e];
+        acc += (double)fmaf(zv.x, rv.x, zv.y * rv.y);
+    }
+    double t;
+    if (finish_reduce(acc, partial, ticket, &t) && threadIdx.x == 0) {
+        fs->zr = t;
+        fs->beta = t / fs->rz;
+        fs->rz = t;
+        fs->use_r = 0;
+        cudaGraphSetConditional(h, fcg_check_logic(fs));
+    }
+}
+
+// T. Chan fold of the 2N point-spread function onto the N-periodic grid
+__global__ void circ_fold_kernel(const float2 *__restrict__ T, int N0, int N1, float2 *__restrict__ cN)
+{
+    const int64_t P = (int64_t)N0 * N1;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < P; e += (int64_t)gridDim.x * blockDim.x) {
+        const int i0 = (int)(e / N1), i1 = (int)(e % N1);
+        float sx = 0.f, sy = 0.f;
+        for (int a = 0; a < 2; ++a) {
+            const int j0 = i0 + a * N0;                   // index in T, offset d0 = j0 - N0
+            const float w0 = fmaxf(0.f, 1.f - fabsf((float)(j0 - N0)) / (float)N0);
+            for (int b = 0; b < 2; ++b) {
+                const int j1 = i1 + b * N1;
+                const float w = w0 * fmaxf(0.f, 1.f - fabsf((float)(j1 - N1)) / (float)N1);
+                const float2 v = T[(int64_t)j0 * (2 * N1) + j1];
+                sx = fmaf(w, v.x, sx); sy = fmaf(w, v.y, sy);
+            }
+        }
+        cN[e] = make_float2(sx, sy);
+    }
+}
+
+__global__ void coil_rsqrt_kernel(const float2 *__restrict__ S, int64_t P, int nc, float *__restrict__ csq)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int c = 0; c < nc; ++c) {
+            const float2 v = S[p * nc + c];
+            s += (double)v.x * v.x + (double)v.y * v.y;
+        }
+        csq[p] = s > 0.0 ? (float)(1.0 / sqrt(s)) : 0.f;
+    }
+}
+
+__global__ void circ_kinv_kernel(const float *__restrict__ spec, const FCGScalars *fs, int64_t P,
+                                 float *__restrict__ kinv)
+{
+    const double mu = fs->dsum > 0.0 ? fs->cg.lambda * (double)P / fs->dsum : 0.0;   // lambda / mean sum|S|^2
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < P; e += (int64_t)gridDim.x * blockDim.x) {
+        const double den = (double)P * ((double)spec[e] + mu);
+        kinv[e] = den > 0.0 ? (float)(1.0 / den) : 0.f;
+    }
+}
+
+__global__ void scale_add_kernel(float2 *out, const float2 *x, const float *__restrict__ dx, const float2 *y,
+                                 const float *__restrict__ dy, int64_t n)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const float a = dx ? dx[e] : 1.f;
+        float2 v = x[e];
+        v.x *= a; v.y *= a;
+        if (y) {
+            const float b = dy ? dy[e] : 1.f;
+            const float2 u = y[e];
+            v.x = fmaf(b, u.x, v.x); v.y = fmaf(b, u.y, v.y);
+        }
+        out[e] = v;
     }
 }
 
@@ -907,6 +986,43 @@ cgs_status launch_diag_scale(const float2 *in, const float2 *add, const float *d
                              float2 *out, cudaStream_t st)
 {
     diag_scale_kernel<<<grid_for(n), kThreads, 0, st>>>(in, add, d, power, n, out);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_fcg_zr_check(FCGScalars *fs, const float2 *z, const float2 *r, int64_t n, double *partial,
+                               unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st)
+{
+    fcg_zr_check_kernel<<<kDotBlocks, kThreads, 0, st>>>(fs, z, r, n, partial, ticket, h);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_circ_fold(const float2 *T, int N0, int N1, float2 *cN, cudaStream_t st)
+{
+    circ_fold_kernel<<<grid_for((int64_t)N0 * N1), kThreads, 0, st>>>(T, N0, N1, cN);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_coil_rsqrt(const float2 *sens, int64_t P, int nc, float *csq, cudaStream_t st)
+{
+    coil_rsqrt_kernel<<<grid_for(P), kThreads, 0, st>>>(sens, P, nc, csq);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_circ_kinv(const float *spec, const FCGScalars *fs, int64_t P, float *kinv, cudaStream_t st)
+{
+    circ_kinv_kernel<<<grid_for(P), kThreads, 0, st>>>(spec, fs, P, kinv);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_scale_add(float2 *out, const float2 *x, const float *dx, const float2 *y, const float *dy,
+                            int64_t n, cudaStream_t st)
+{
+    scale_add_kernel<<<grid_for(n), kThreads, 0, st>>>(out, x, dx, y, dy, n);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }

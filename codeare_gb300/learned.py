@@ -8,11 +8,15 @@ complex intensities.  The normal equations are the standard-mode ones,
 Training pairs (residual r, correction e): r is a plain-CG residual
 b - A x_k at a random iteration k of a random problem, e = CG_20(A, r) is the
 20-iteration plain-CG solution of A e = r from zero.  The preconditioner is
-z = d . (t + net(t)), t = d . r, with d = diag(A)^-1/2 (exact: sum_c |S_c|^2
-sum_j w_j + lambda): the network corrects the Jacobi step on the unit-diagonal
-system d A d, so its pairs are (t, e / d - t), both divided by the RMS of t (the network is positively
-homogeneous, so the scale is exact) and stored as [H][W][2] float.  The
-network is include/cgs.h's cgs_net_*; cgs_solve_fcg applies the scaling.
+z = C r + d . net(t), t = d . r, with d = diag(A)^-1/2 (exact: sum_c |S_c|^2
+sum_j w_j + lambda) and C the circulant of cgs_precond_apply (a global step:
+the inverse of the floored T. Chan spectrum of the point-spread function,
+between coil-energy scalings).  The network corrects the circulant step
+locally, so its pairs are (t, (e - C r) / d), both divided by the RMS of t
+(the network is positively homogeneous, so the scale is exact) and stored as
+[H][W][2] float.  With base="jacobi" the older form z = d . (t + net(t))
+(pairs (t, e / d - t)) is trained instead.  The network is include/cgs.h's
+cgs_net_*; cgs_solve_fcg applies the scaling.
 
 All compute runs in libcgs.so; torch only holds device buffers and slices
 random training crops.
@@ -84,9 +88,13 @@ class Problem:
         self.plan.sense_adjoint(self.y_d, b, weighted=True)
         self.b = b
 
-    def solve(self, x, rhs=None, net=None, cgiter=500, cgeps=1e-4, jacobi=False):
+    def solve(self, x, rhs=None, net=None, cgiter=500, cgeps=1e-4, jacobi=False, circulant=False):
         return self.plan.solve_fcg(x, rhs=self.b if rhs is None else rhs, net=net, cgiter=cgiter, cgeps=cgeps,
-                                   lam=self.lam, weighted=True, toeplitz=True, jacobi=jacobi)
+                                   lam=self.lam, weighted=True, toeplitz=True, jacobi=jacobi,
+                                   circulant=circulant)
+
+    def precond(self, r, out):
+        return self.plan.precond_apply(r, out, lam=self.lam, weighted=True)
 
     def apply(self, x, out):
         return self.plan.normal_apply(x, out, lam=self.lam, weighted=True, toeplitz=True)
@@ -102,9 +110,9 @@ def as_channels(z):
 
 
 def generate_pairs(n_pairs: int, seed: int = 20261207, per_problem: int = 8, N: int = 256, nc: int = 16,
-                   k_max: int = 60, corr_iters: int = 20, log=None):
-    """(t = d . residual, correction / d - t) pairs on the GPU, each divided by the
-    RMS of t."""
+                   k_max: int = 60, corr_iters: int = 20, base: str = "circulant", log=None):
+    """(t = d . residual, (correction - C residual) / d) pairs on the GPU (with
+    base="jacobi": (t, correction / d - t)), each divided by the RMS of t."""
     import torch
     X = torch.empty((n_pairs, N, N, 2), dtype=torch.float32, device="cuda")
     T = torch.empty_like(X)
@@ -128,11 +136,17 @@ def generate_pairs(n_pairs: int, seed: int = 20261207, per_problem: int = 8, N: 
                 pr.solve(x, cgiter=kk, cgeps=0.0)
                 pr.apply(x, Ax)
                 r = pr.b - Ax
-            pr.solve(e, rhs=r.contiguous(), cgiter=corr_iters, cgeps=0.0)
+            r = r.contiguous()
+            pr.solve(e, rhs=r, cgiter=corr_iters, cgeps=0.0)
             rs = r * pr.d
             s = torch.sqrt(torch.mean(torch.view_as_real(rs) ** 2)).clamp_min(1e-30)
             X[i] = as_channels(rs / s)
-            T[i] = as_channels((e / pr.d - rs) / s)
+            if base == "circulant":
+                cr = torch.zeros_like(r)
+                pr.precond(r, cr)
+                T[i] = as_channels((e - cr) / pr.d / s)
+            else:
+                T[i] = as_channels((e / pr.d - rs) / s)
             i += 1
         pr.close()
         if log and prob_id % 16 == 0:
@@ -196,20 +210,21 @@ def load_net(path: str = WEIGHTS_FILE):
     return net
 
 
-def compare(net, seed: int, cgeps: float = 1e-4, ref_eps: float = 1e-6, repeats: int = 2):
-    """Plain CG, Jacobi-preconditioned CG and learned flexible CG on one held-out
-    problem to relative residual `cgeps` (the second of `repeats` timed solves
-    is kept: the first builds the solve graph), each image's relative L2 error
-    against the plain solve converged to `ref_eps`."""
+def compare(net, seed: int, cgeps: float = 1e-4, ref_eps: float = 1e-6, repeats: int = 2, spokes=None):
+    """Plain CG, Jacobi-preconditioned CG, circulant-preconditioned CG and
+    learned flexible CG (the circulant step plus the network's correction) on
+    one held-out problem to relative residual `cgeps` (the second of `repeats`
+    timed solves is kept: the first builds the solve graph), each image's
+    relative L2 error against the plain solve converged to `ref_eps`."""
     import torch
-    pr = Problem(seed)
+    pr = Problem(seed, spokes=spokes)
     N = pr.N
     ref = torch.zeros((N, N), dtype=torch.complex64, device="cuda")
     pr.solve(ref, cgiter=2000, cgeps=ref_eps)
     out = {"seed": seed, "spokes": pr.spokes}
-    arms = [("plain", {}), ("jacobi", {"jacobi": True})]
+    arms = [("plain", {}), ("jacobi", {"jacobi": True}), ("circulant", {"circulant": True})]
     if net is not None:
-        arms.append(("learned", {"net": net}))
+        arms.append(("learned", {"net": net, "circulant": True}))
     for name, kw in arms:
         x = torch.zeros_like(ref)
         for _ in range(repeats):
@@ -219,6 +234,25 @@ def compare(net, seed: int, cgeps: float = 1e-4, ref_eps: float = 1e-6, repeats:
                      "fallback_at": rep["fallback_at"], "image_err": err}
     pr.close()
     return out
+
+
+HELD_OUT = [(9001, 32), (9002, 40), (9003, 50), (9004, 60), (9005, 70), (9006, 80), (9007, 90), (9008, 100)]
+
+
+def compare_many(net, problems=HELD_OUT, cgeps: float = 1e-4):
+    """compare() over held-out problems spread over 32-100 spokes; per arm the
+    median speed-up against plain CG and the worst image error."""
+    rows = [compare(net, seed, cgeps=cgeps, spokes=sp) for seed, sp in problems]
+    arms = [a for a in ("jacobi", "circulant", "learned") if a in rows[0]]
+    summary = {}
+    for a in arms:
+        sp = [r["plain"]["ms"] / r[a]["ms"] for r in rows]
+        it = [r["plain"]["iterations"] / max(1, r[a]["iterations"]) for r in rows]
+        summary[a] = {"median_speedup_vs_plain": float(np.median(sp)), "min_speedup": float(np.min(sp)),
+                      "median_iteration_ratio": float(np.median(it)),
+                      "max_image_err": float(max(r[a]["image_err"] for r in rows))}
+    summary["plain_max_image_err"] = float(max(r["plain"]["image_err"] for r in rows))
+    return rows, summary
 
 
 def main(argv=None):
@@ -249,8 +283,10 @@ def main(argv=None):
     save_weights(a.out, net.weights(), "pairs=%d steps=%d lr=%g rel_loss=%.4f" % (a.pairs, a.steps, a.lr,
                                                                                    last / ms))
     del X, T
-    for seed in (777, 778):
-        log(str(compare(net, seed)))
+    rows, summary = compare_many(net)
+    for r in rows:
+        log(str(r))
+    log(str(summary))
 
 
 if __name__ == "__main__":

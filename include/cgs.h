@@ -130,9 +130,11 @@ typedef struct {
                           (2N-grid FFT convolution with the weighted point-spread
                           function, computed once per trajectory and weights);
                           no reference counterpart                            */
-    int jacobi;        /* cgs_solve_fcg without a net: precondition with the exact
-                          diagonal D of E^H W E + lambda (D^-1 r); no reference
-                          counterpart                                        */
+    int jacobi;        /* cgs_solve_fcg preconditioner kind (no reference
+                          counterpart): 0 none; 1 the exact diagonal D of
+                          E^H W E + lambda (D^-1 r); 2 the circulant C (see
+                          cgs_precond_apply), with a net the base that the net
+                          corrects                                            */
 } cgs_solve_opts;
 
 typedef struct {
@@ -242,12 +244,25 @@ cgs_status cgs_autotune(cgs_plan *plan, cgs_tuning *chosen, double *ms, void *st
  * to plain CG (restarted) once the residual stalls for three iterations or the
  * network gives <r, z> <= 0.  Stops at ||r||/||r0|| <= cgeps.  The right-hand
  * side is b = E^H W y from k-space data y, or the image `rhs` when y is NULL.
- * net == NULL runs the same loop as plain CG (Polak-Ribiere beta), or Jacobi
- * preconditioned CG when opts->jacobi is set.  The plan's
+ * net == NULL runs the same loop as plain CG (Polak-Ribiere beta), or
+ * preconditioned CG with the exact diagonal (opts->jacobi 1) or the circulant
+ * of cgs_precond_apply (opts->jacobi 2).  With a net and opts->jacobi 2 the
+ * preconditioner is z = C r + d . net(d . r): the network corrects the
+ * circulant step instead of the diagonal one.  The plan's
  * image must be 2-D and fit the net's maximum image size. */
 cgs_status cgs_solve_fcg(cgs_plan *plan, const float *y, const float *rhs, float *x,
                          const cgs_solve_opts *opts, cgs_net *net, cgs_solve_report *report,
                          void *stream);
+
+/* Circulant preconditioner of the standard-mode normal equations (no
+ * reference counterpart): z = C r with
+ *   C = Q F^-1 diag(1 / (c + lambda / mean(sum_c |S_c|^2))) F Q,  Q = diag(1 / sqrt(sum_c |S_c|^2)),
+ * F the 2-D DFT on the N x N image and c the T. Chan spectrum of the
+ * weighted point-spread function (the Toeplitz kernel of cgs_solve's
+ * toeplitz option, folded onto the N-periodic grid), floored at 0.2 of its
+ * mean.  lambda and the weighting come from opts.  2-D single-frame plans
+ * with k-space, sensitivities and (if weighted) weights set. */
+cgs_status cgs_precond_apply(cgs_plan *plan, const float *r, float *z, const cgs_solve_opts *opts, void *stream);
 
 /* out = (E^H W E + lambda) x for an image x (Toeplitz or NFFT pair as opts say). */
 cgs_status cgs_normal_apply(cgs_plan *plan, const float *x, float *out, const cgs_solve_opts *opts,

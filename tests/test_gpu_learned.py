@@ -78,23 +78,31 @@ def test_cnn_training_reduces_loss(gpu):
 
 
 def test_learned_preconditioner_against_plain_cg(gpu):
-    """What the trained network gains over the method without it, on a held-out
-    256^2, 16-coil problem: plain CG, Jacobi CG (the network's skip path alone)
-    and learned flexible CG to relative residual 1e-4.  Every arm must reach the
-    tolerance (plain CG is the fallback) and land within 5x plain CG's
-    final-image error against the converged plain solve; the iteration and time
-    ratios are printed, not asserted."""
+    """What the circulant and the trained network gain over plain CG, on three
+    held-out 256^2, 16-coil problems (32, 60 and 100 golden-angle spokes) to
+    relative residual 1e-4: plain CG, Jacobi CG, circulant-preconditioned CG
+    and learned flexible CG (the circulant step plus the network's local
+    correction, plain CG as the fallback).  Every arm must reach the
+    tolerance; the circulant must need at least 1.3x fewer iterations than
+    plain CG with an image error no worse than 1.5x plain's; the learned arm
+    must land within 5x plain CG's final-image error against the converged
+    plain solve.  The measured ratios are printed: the 3x wall-clock target of
+    the learned arm is not reached (median 0.28x over eight problems, the
+    circulant alone 1.06x, in the bench line)."""
     from codeare_gb300 import capi, learned
     net = learned.load_net()
     if net is None:
         X, T = learned.generate_pairs(256, per_problem=8)
         net = capi.Net(max_batch=32, max_h=256, max_w=256)
         learned.train(net, X, T, steps=300)
-    r = learned.compare(net, seed=777)
-    for arm in ("plain", "jacobi", "learned"):
-        assert r[arm]["res"] <= 1e-4, r
-        assert r[arm]["image_err"] <= 5 * r["plain"]["image_err"] + 1e-4, r
-    print("learned vs plain: iterations %d vs %d, time %.1f ms vs %.1f ms (x%.2f), jacobi %d its" % (
-        r["learned"]["iterations"], r["plain"]["iterations"], r["learned"]["ms"], r["plain"]["ms"],
-        r["plain"]["ms"] / r["learned"]["ms"], r["jacobi"]["iterations"]))
+    rows, summary = learned.compare_many(net, problems=[(9001, 32), (9004, 60), (9008, 100)])
     net.close()
+    for r in rows:
+        for arm in ("plain", "jacobi", "circulant", "learned"):
+            assert r[arm]["res"] <= 1e-4, r
+        assert r["learned"]["image_err"] <= 5 * r["plain"]["image_err"] + 1e-4, r
+        assert r["circulant"]["image_err"] <= 1.5 * r["plain"]["image_err"], r
+    assert summary["circulant"]["median_iteration_ratio"] >= 1.3, summary
+    print("speed-up vs plain CG (median): circulant x%.2f (iterations x%.2f), learned x%.2f (iterations x%.2f)" % (
+        summary["circulant"]["median_speedup_vs_plain"], summary["circulant"]["median_iteration_ratio"],
+        summary["learned"]["median_speedup_vs_plain"], summary["learned"]["median_iteration_ratio"]))
