@@ -290,6 +290,14 @@ cgs_status launch_jacobi_scale(const float2 *sens, int64_t P, int nc, const FCGS
 // scaling steps of the preconditioner
 cgs_status launch_diag_scale(const float2 *in, const float2 *add, const float *d, int power, int64_t n,
                              float2 *out, cudaStream_t st);
+// codeare's inner CGNR with A^H W A applied in image space (cgs_vec.cu,
+// cgnr_img_kernel): mode 0 the prologue dots, 1 alpha and the residual-norm
+// recurrence after g = T(mask p), 2 the image / z updates and beta.  partial
+// and partial2 hold kDotBlocks x nc doubles each.
+cgs_status launch_cgnr_img(int mode, int64_t rows, int nc, const float *mask, const float2 *bimg,
+                           const float2 *sens, float2 *z, const float2 *g, const float2 *pv, float2 *img,
+                           double *partial, double *partial2, unsigned int *ticket, double *dots6, int *active,
+                           double eps, cudaStream_t st);
 // circulant preconditioner (2-D): the T. Chan fold of the 2N point-spread
 // function T[2N0][2N1] (index d + N) onto the N-periodic grid,
 //   cN[d mod N] = sum (1 - |d0|/N0)(1 - |d1|/N1) T[d]

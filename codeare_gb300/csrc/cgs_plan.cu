@@ -258,6 +258,10 @@ struct cgs_plan {
     float2 *twN[2] = {nullptr, nullptr};
     int facN[2][12] = {}, nfacN[2] = {0, 0};
     bool circ_valid = false;
+    // codeare-mode CGLS with the Toeplitz kernel: T (mask p) per coil and the
+    // second partial-sum buffer of the image-space CGNR
+    float2 *cG = nullptr;
+    double *partial2 = nullptr;
     cudaGraphExec_t fcg_exec = nullptr;
     int fg_src = -1, fg_toep = -1, fg_weighted = -1, fg_mode = -1;
     uint64_t fg_net = 0;
@@ -1086,8 +1090,10 @@ cgs_status build_toeplitz(cgs_plan *p, int weighted, cudaStream_t st)
     return CGS_OK;
 }
 
-// out = sum_c conj(S_c) (A^H W A)(S_c x) through the Toeplitz kernel
-cgs_status op_ehe_toeplitz(cgs_plan *p, const float2 *x, float2 *out, cudaStream_t st)
+// coil_out[p][c] = (A^H W A)(mask . u_c) through the Toeplitz kernel for all
+// coils, u_c = S_c x (per_coil 0, x one image) or x_c (per_coil 1, x coil-minor)
+cgs_status op_toeplitz_coils(cgs_plan *p, const float2 *x, int per_coil, const float *mask, float2 *coil_out,
+                             cudaStream_t st)
 {
     const int d = p->d, nc = p->nc;
     {   // pad the fastest axis: image -> [..][2N][NC], with the coil expansion
@@ -1095,7 +1101,8 @@ cgs_status op_ehe_toeplitz(cgs_plan *p, const float2 *x, float2 *out, cudaStream
         int64_t outer = 1;
         for (int t = 0; t < d - 1; ++t) outer *= p->N[t];
         a.outer = outer; a.inner = nc; a.Lin = p->N[d - 1]; a.Lout = p->n2[d - 1]; a.sign = -1; a.in_centred = 1;
-        a.load_mode = LOAD_IMAGE; a.img = x; a.img_per_coil = 0; a.sens = p->sens;
+        a.load_mode = LOAD_IMAGE; a.img = x; a.img_per_coil = per_coil; a.sens = per_coil ? nullptr : p->sens;
+        a.mask = mask;
         a.dst = p->tA;
         CGS_TRY(launch_axis_pass(a, st));
     }
@@ -1127,10 +1134,48 @@ cgs_status op_ehe_toeplitz(cgs_plan *p, const float2 *x, float2 *out, cudaStream
         int64_t outer = 1;
         for (int t = 0; t < d - 1; ++t) outer *= p->N[t];
         a.outer = outer; a.inner = nc; a.Lin = p->n2[d - 1]; a.Lout = p->N[d - 1]; a.sign = +1; a.out_centred = 1;
-        a.src = p->tA; a.dst = p->cF;
-        CGS_TRY(launch_axis_pass(a, st));
+        a.src = p->tA; a.dst = coil_out;
+        return launch_axis_pass(a, st);
     }
-    return launch_coil_combine(p->cF, p->sens, nullptr, p->Nt, nc, out, st);
+}
+
+// out = sum_c conj(S_c) (A^H W A)(S_c x) through the Toeplitz kernel
+cgs_status op_ehe_toeplitz(cgs_plan *p, const float2 *x, float2 *out, cudaStream_t st)
+{
+    CGS_TRY(op_toeplitz_coils(p, x, 0, nullptr, p->cF, st));
+    return launch_coil_combine(p->cF, p->sens, nullptr, p->Nt, p->nc, out, st);
+}
+
+// codeare's E^H applied to E x (the CGLS step), all in image space: the
+// per-coil CGNR inverse NFFT of y_c = A (S_c x) with A^H W A from the
+// Toeplitz kernel (cgnr_img_kernel states the recurrences), then
+// I . sum conj(S_c) f_c.  Same steps, early exits and frozen coils as
+// op_itrafo; exact up to the NFFT approximation error (sigma >= 2, m >= 4).
+cgs_status op_eh_codeare_ehx_toeplitz(cgs_plan *p, const float2 *x, int ftiter, double fteps, float2 *out,
+                                      cudaStream_t st)
+{
+    const int nc = p->nc;
+    const int64_t Nt = p->Nt;
+    if (!p->cG) CGS_TRY(dev_alloc(&p->cG, (size_t)Nt * nc));
+    if (!p->partial2) CGS_TRY(dev_alloc(&p->partial2, (size_t)dot_blocks() * std::max(nc, 1)));
+    CGS_TRY(op_toeplitz_coils(p, x, 0, nullptr, p->cZ, st));           // z = A^H W y_c = T (S_c x)
+    CGS_TRY(launch_zero(p->cF, sizeof(float2) * Nt * nc, st));
+    CGS_TRY(launch_cgnr_img(0, Nt, nc, p->mask, x, p->sens, p->cZ, nullptr, nullptr, nullptr, p->partial,
+                            p->partial2, p->ftick, p->dots, p->active, fteps, st));
+    CGS_CUDA(cudaMemcpyAsync(p->cP, p->cZ, sizeof(float2) * Nt * nc, cudaMemcpyDeviceToDevice, st));
+    CGS_CUDA(cudaMemsetAsync(p->active, 0x01, sizeof(int) * nc, st));
+    if (ftiter > 0)
+        CGS_TRY(launch_cgnr_scalars(0, nc, fteps, p->active, p->dot_r(), p->dot_z(), p->dot_v(), p->dz_new(),
+                                    p->alpha_c(), p->beta_c(), st));
+    for (int l = 0; l < ftiter; ++l) {
+        CGS_TRY(op_toeplitz_coils(p, p->cP, 1, p->mask, p->cG, st));   // g = T (mask p)
+        CGS_TRY(launch_cgnr_img(1, Nt, nc, p->mask, nullptr, nullptr, p->cZ, p->cG, p->cP, nullptr, p->partial,
+                                p->partial2, p->ftick, p->dots, p->active, fteps, st));
+        CGS_TRY(launch_cgnr_img(2, Nt, nc, p->mask, nullptr, nullptr, p->cZ, p->cG, p->cP, p->cF, p->partial,
+                                p->partial2, p->ftick, p->dots, p->active, fteps, st));
+        CGS_TRY(launch_xpby_cols(p->cP, p->cZ, p->beta_c(), p->active, Nt, nc, st));
+    }
+    return launch_coil_combine(p->cF, p->sens, p->imap, Nt, nc, out, st);
 }
 
 // One CG-SENSE iteration (either mode) on the plan's buffers.
@@ -1139,7 +1184,9 @@ cgs_status op_ehe_toeplitz(cgs_plan *p, const float2 *x, float2 *out, cudaStream
 cgs_status cg_iteration(cgs_plan *p, const cgs_solve_opts *o, cudaGraphConditionalHandle h, cudaStream_t st)
 {
     const int64_t Nt = p->Nt;
-    if (o->mode == CGS_MODE_CODEARE) {
+    if (o->mode == CGS_MODE_CODEARE && o->toeplitz) {
+        CGS_TRY(op_eh_codeare_ehx_toeplitz(p, p->vP, o->ftiter, o->fteps, p->vQ, st));
+    } else if (o->mode == CGS_MODE_CODEARE) {
         CGS_TRY(op_forward(p, p->vP, 0, nullptr, p->ksV, st));
         CGS_TRY(op_eh_codeare(p, p->ksV, o->ftiter, o->fteps, p->vQ, st));
     } else if (o->toeplitz) {
@@ -1767,7 +1814,7 @@ cgs_status cgs_plan_destroy(cgs_plan *p)
     if (p->fcg_exec) cudaGraphExecDestroy(p->fcg_exec);
     for (void *b : {(void *)p->vB, (void *)p->vZ, (void *)p->vO, (void *)p->vT, (void *)p->dscale, (void *)p->fs,
                     (void *)p->circ, (void *)p->circ_inv, (void *)p->csq, (void *)p->vC, (void *)p->vCo,
-                    (void *)p->twN[0], (void *)p->twN[1]})
+                    (void *)p->twN[0], (void *)p->twN[1], (void *)p->cG, (void *)p->partial2})
         dev_free(b);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
@@ -2222,6 +2269,25 @@ cgs_status cgs_sense_adjoint(cgs_plan *p, const float *y, float *x, int weighted
     return image_out(p, p->vX, x, st);
 }
 
+// codeare mode takes the Toeplitz kernel only where the NFFT is accurate: the
+// reference's CGNR composes its own (approximate) NFFT pair, which equals the
+// point-spread-function convolution only up to the NFFT error
+static cgs_status check_codeare_toeplitz(const cgs_plan *p, const cgs_solve_opts *o)
+{
+    if (o->mode == CGS_MODE_CODEARE && o->toeplitz && !(p->alpha >= 2.0 - 1e-9 && p->m >= 4)) {
+        set_error("codeare mode with the Toeplitz kernel needs sigma >= 2 and m >= 4 (an accurate NFFT)");
+        return CGS_ERR_BAD_ARG;
+    }
+    return CGS_OK;
+}
+
+// the density weighting of the Toeplitz kernel: codeare's CGNR always uses W
+static int toeplitz_weighting(const cgs_plan *p, const cgs_solve_opts *o)
+{
+    if (o->mode == CGS_MODE_CODEARE) return p->have_w ? 1 : 0;
+    return (o->weighted && p->have_w) ? 1 : 0;
+}
+
 cgs_status cgs_solve(cgs_plan *p, const float *y, float *x, const cgs_solve_opts *o,
                      cgs_solve_report *rep, void *stream)
 {
@@ -2229,11 +2295,12 @@ cgs_status cgs_solve(cgs_plan *p, const float *y, float *x, const cgs_solve_opts
     const bool codeare = (o->mode == CGS_MODE_CODEARE);
     CGS_TRY(check_ready(p, codeare || o->weighted, true));
     if (!x || !y || o->cgiter < 0 || o->ftiter < 0) { set_error("bad argument"); return CGS_ERR_BAD_ARG; }
-    if (p->F > 1 && !codeare && o->toeplitz) { set_error("the Toeplitz operator is not built for frames"); return CGS_ERR_BAD_ARG; }
+    if (p->F > 1 && o->toeplitz) { set_error("the Toeplitz operator is not built for frames"); return CGS_ERR_BAD_ARG; }
+    CGS_TRY(check_codeare_toeplitz(p, o));
     cudaStream_t st = pick_stream(p, stream);
     if (rep) { std::memset(rep, 0, sizeof(*rep)); rep->fallback_at = -1; }
-    if (!codeare && o->toeplitz) {
-        const int wtd = (o->weighted && p->have_w) ? 1 : 0;
+    if (o->toeplitz) {
+        const int wtd = toeplitz_weighting(p, o);
         if (!p->toep_valid || p->toep_weighted != wtd) CGS_TRY(build_toeplitz(p, wtd, st));
     }
     CGS_CUDA(cudaEventRecord(p->ev0, st));
@@ -2244,13 +2311,9 @@ cgs_status cgs_solve(cgs_plan *p, const float *y, float *x, const cgs_solve_opts
         // CGLS with no iterations returns A/b (CGLS.hpp:32-33)
         CGS_TRY(op_eh_codeare(p, p->ksY, o->ftiter, o->fteps, p->vX, st));
     } else {
-        const bool same = p->solve_exec && p->sg_mode == o->mode && p->sg_toep == (codeare ? 0 : o->toeplitz) &&
+        const bool same = p->solve_exec && p->sg_mode == o->mode && p->sg_toep == o->toeplitz &&
                           p->sg_weighted == o->weighted && p->sg_ftiter == o->ftiter && p->sg_fteps == o->fteps;
-        if (!same) {
-            cgs_solve_opts oo = *o;
-            if (codeare) oo.toeplitz = 0;
-            CGS_TRY(build_solve_graph(p, &oo, st));
-        }
+        if (!same) CGS_TRY(build_solve_graph(p, o, st));
         CGScalars init{};
         init.lambda = o->lambda;
         init.tol = o->cgeps;
@@ -2625,16 +2688,17 @@ cgs_status cgs_batch_create(cgs_batch **out, cgs_plan *const *plans, const cgs_s
     for (int i = 0; i < count && r == CGS_OK; ++i) {
         cgs_plan *p = plans[i];
         const cgs_solve_opts &o = opts[i];
-        if (o.mode != CGS_MODE_CODEARE && o.toeplitz) {
-            const int wtd = (o.weighted && p->have_w) ? 1 : 0;
-            if (!p->toep_valid || p->toep_weighted != wtd) r = build_toeplitz(p, wtd, st);
+        if (o.toeplitz) {
+            if (p->F > 1) { set_error("the Toeplitz operator is not built for frames"); r = CGS_ERR_BAD_ARG; break; }
+            r = check_codeare_toeplitz(p, &o);
+            const int wtd = toeplitz_weighting(p, &o);
+            if (r == CGS_OK && (!p->toep_valid || p->toep_weighted != wtd)) r = build_toeplitz(p, wtd, st);
         }
     }
     cudaGraph_t g = nullptr;
     if (r == CGS_OK && cudaGraphCreate(&g, 0) != cudaSuccess) r = CGS_ERR_CUDA;
     for (int i = 0; i < count && r == CGS_OK; ++i) {
         cgs_solve_opts o = opts[i];
-        if (o.mode == CGS_MODE_CODEARE) o.toeplitz = 0;
         int64_t kp = 0, kb = 0;
         r = append_solve(plans[i], &o, g, true, st, &kp, &kb);
         b->plans.push_back(plans[i]);

@@ -285,6 +285,141 @@ __global__ void __launch_bounds__(kThreads) cgnr_fused_kernel(CgnrArgs a)
     if (t == 0) *a.ticket = 0u;
 }
 
+// ---- the same CGNR with A^H W A applied in image space -----------------------
+// When codeare's inner CGNR runs on data y = A u (the CGLS step E^H(E p), u =
+// S_c p), every quantity of NFFT3's loop is reachable from the image side
+// through T = A^H W A (the Toeplitz kernel): z = A^H W r starts as T u and is
+// updated as z -= alpha T(mask p); |r|_W^2 starts as Re <u, T u> and follows
+// |r - alpha v|_W^2 = |r|_W^2 - 2 alpha Re <mask p, z> + alpha^2 |v|_W^2 with
+// |v|_W^2 = Re <mask p, T(mask p)>.  Three fused kernels per step, each with
+// two per-coil reductions in the fixed order of cgnr_fused_kernel:
+//   MODE 0: dot_r = Re <S bimg, z>, dot_z = |z|_mask^2          (prologue)
+//   MODE 1: dot_v = Re <mask p, g>, cross = Re <mask p, z>; alpha = active ?
+//           dot_z / dot_v : 0; dot_r += alpha^2 dot_v - 2 alpha cross;
+//           active &= !(dot_r < eps)                            (g = T(mask p))
+//   MODE 2: img += alpha mask p, z -= alpha g, dz_new = |z|_mask^2;
+//           beta = active ? dz_new / dot_z : 0, dot_z = dz_new
+struct CgnrImgArgs {
+    int64_t rows;
+    int nc;
+    const float *mask;      // damping mask per image row
+    const float2 *bimg;     // MODE 0: the broadcast image p
+    const float2 *sens;     // MODE 0: sensitivities [rows][nc]
+    float2 *z;              // A^H W r per coil [rows][nc]
+    const float2 *g;        // MODES 1, 2: T(mask p)
+    const float2 *pv;       // MODES 1, 2: search direction
+    float2 *img;            // MODE 2: the estimate
+    double *partial, *partial2;
+    unsigned int *ticket;
+    double *dot_r, *dot_z, *dot_v, *dz_new, *alpha, *beta;
+    int *active;
+    double eps;
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) cgnr_img_kernel(CgnrImgArgs a)
+{
+    __shared__ double sred[kThreads], sred2[kThreads];
+    __shared__ bool last;
+    const int nc = a.nc, t = threadIdx.x;
+    const int64_t per = (a.rows + gridDim.x - 1) / gridDim.x;
+    const int64_t rbeg = (int64_t)blockIdx.x * per;
+    const int64_t rend = min(a.rows, rbeg + per);
+    const int ncl = nc < kThreads ? nc : kThreads;
+    const int lanes = kThreads / ncl;
+    const int lr = t / ncl;
+    for (int cb = 0; cb < nc; cb += ncl) {
+        const int c = cb + t % ncl;
+        double acc1 = 0.0, acc2 = 0.0;
+        if (lr < lanes && c < nc) {
+            const float al = (MODE == 2) ? (float)a.alpha[c] : 0.f;
+            for (int64_t r = rbeg + lr; r < rend; r += lanes) {
+                const int64_t e = r * nc + c;
+                const float m = a.mask ? a.mask[r] : 1.f;
+                if (MODE == 0) {
+                    const float2 b = a.bimg[r], sv = a.sens[e], zv = a.z[e];
+                    const float ux = sv.x * b.x - sv.y * b.y, uy = sv.x * b.y + sv.y * b.x;
+                    acc1 += (double)fmaf(ux, zv.x, uy * zv.y);
+                    acc2 += (double)m * (double)fmaf(zv.x, zv.x, zv.y * zv.y);
+                } else if (MODE == 1) {
+                    const float2 pv = a.pv[e], gv = a.g[e], zv = a.z[e];
+                    acc1 += (double)m * (double)fmaf(pv.x, gv.x, pv.y * gv.y);
+                    acc2 += (double)m * (double)fmaf(pv.x, zv.x, pv.y * zv.y);
+                } else {
+                    float2 zv = a.z[e];
+                    if (al != 0.f) {
+                        const float2 pv = a.pv[e], gv = a.g[e];
+                        const float sm = al * m;
+                        float2 y = a.img[e];
+                        y.x = fmaf(sm, pv.x, y.x); y.y = fmaf(sm, pv.y, y.y);
+                        a.img[e] = y;
+                        zv.x = fmaf(-al, gv.x, zv.x); zv.y = fmaf(-al, gv.y, zv.y);
+                        a.z[e] = zv;
+                    }
+                    acc1 += (double)m * (double)fmaf(zv.x, zv.x, zv.y * zv.y);
+                }
+            }
+        }
+        sred[t] = (lr < lanes) ? acc1 : 0.0;
+        sred2[t] = (lr < lanes) ? acc2 : 0.0;
+        __syncthreads();
+        if (t < ncl) {
+            double s1 = 0.0, s2 = 0.0;
+            for (int l = 0; l < lanes; ++l) { s1 += sred[l * ncl + t]; s2 += sred2[l * ncl + t]; }
+            if (cb + t < nc) {
+                a.partial[(int64_t)blockIdx.x * nc + cb + t] = s1;
+                a.partial2[(int64_t)blockIdx.x * nc + cb + t] = s2;
+            }
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        __threadfence();
+        last = atomicAdd(a.ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int warp = t >> 5, lane = t & 31;
+    for (int c = warp; c < nc; c += kThreads / 32) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int b = lane; b < (int)gridDim.x; b += 32) {
+            s1 += ((volatile double *)a.partial)[(int64_t)b * nc + c];
+            s2 += ((volatile double *)a.partial2)[(int64_t)b * nc + c];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s1 += __shfl_down_sync(0xffffffffu, s1, o);
+            s2 += __shfl_down_sync(0xffffffffu, s2, o);
+        }
+        if (lane == 0) {
+            if (MODE == 0) {
+                a.dot_r[c] = s1;
+                a.dot_z[c] = s2;
+            } else if (MODE == 1) {
+                a.dot_v[c] = s1;
+                if (a.active[c]) {
+                    const double al = a.dot_z[c] / s1;
+                    a.alpha[c] = al;
+                    a.dot_r[c] = a.dot_r[c] + al * al * s1 - 2.0 * al * s2;
+                    a.active[c] = !(a.dot_r[c] < a.eps);
+                } else {
+                    a.alpha[c] = 0.0;
+                }
+            } else {
+                a.dz_new[c] = s1;
+                if (a.active[c]) {
+                    a.beta[c] = s1 / a.dot_z[c];
+                    a.dot_z[c] = s1;
+                } else {
+                    a.beta[c] = 0.0;
+                }
+            }
+        }
+    }
+    if (t == 0) *a.ticket = 0u;
+}
+
 __global__ void axpy_cols_kernel(float2 *__restrict__ x, const double *__restrict__ alpha, double sgn,
                                  const float *__restrict__ mask, const float2 *__restrict__ p,
                                  int64_t rows, int nc)
@@ -869,6 +1004,24 @@ cgs_status launch_cgnr_fused(int mode, int64_t rows, int nc, const float *wr, fl
     if (mode == 1) cgnr_fused_kernel<1><<<kDotBlocks, kThreads, 0, st>>>(a);
     else if (mode == 2) cgnr_fused_kernel<2><<<kDotBlocks, kThreads, 0, st>>>(a);
     else cgnr_fused_kernel<3><<<kDotBlocks, kThreads, 0, st>>>(a);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_cgnr_img(int mode, int64_t rows, int nc, const float *mask, const float2 *bimg,
+                           const float2 *sens, float2 *z, const float2 *g, const float2 *pv, float2 *img,
+                           double *partial, double *partial2, unsigned int *ticket, double *dots6, int *active,
+                           double eps, cudaStream_t st)
+{
+    CgnrImgArgs a;
+    a.rows = rows; a.nc = nc; a.mask = mask; a.bimg = bimg; a.sens = sens; a.z = z; a.g = g; a.pv = pv;
+    a.img = img; a.partial = partial; a.partial2 = partial2; a.ticket = ticket;
+    a.dot_r = dots6; a.dot_z = dots6 + nc; a.dot_v = dots6 + 2 * nc; a.dz_new = dots6 + 3 * nc;
+    a.alpha = dots6 + 4 * nc; a.beta = dots6 + 5 * nc;
+    a.active = active; a.eps = eps;
+    if (mode == 0) cgnr_img_kernel<0><<<kDotBlocks, kThreads, 0, st>>>(a);
+    else if (mode == 1) cgnr_img_kernel<1><<<kDotBlocks, kThreads, 0, st>>>(a);
+    else cgnr_img_kernel<2><<<kDotBlocks, kThreads, 0, st>>>(a);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }

@@ -56,12 +56,16 @@ def cgsense_case(gpu):
     return c, p, y
 
 
+@pytest.mark.parametrize("toeplitz", [False, True])
 @pytest.mark.parametrize("lam", [5e-2, 0.0])
-def test_cgsense_128_8coils_codeare_cgls_full_size(gpu, oracle, lam):
+def test_cgsense_128_8coils_codeare_cgls_full_size(gpu, oracle, lam, toeplitz):
+    """codeare CGLS: each CG step's E^H(E p) through the NFFT pair, or (toeplitz)
+    with the inner CGNR run in image space on the Toeplitz kernel."""
     c, p, y = cgsense_case(gpu)
     N = c["shape"][0]
     x = np.zeros((N, N), np.complex64)
-    rep = p.solve(y, x, mode=gpu.MODE_CODEARE, cgiter=10, cgeps=1e-7, lam=lam, ftiter=3, fteps=1e-3)
+    rep = p.solve(y, x, mode=gpu.MODE_CODEARE, cgiter=10, cgeps=1e-7, lam=lam, ftiter=3, fteps=1e-3,
+                  toeplitz=toeplitz)
     p.close()
     s = oracle.Sense(c["sens"], c["k"], w=c["w"], m=c["m"], alpha=c["alpha"])
     xo, res = s.cgls_codeare(y, cgiter=10, cgeps=1e-7, lam=lam, ftiter=3, fteps=1e-3)
@@ -125,9 +129,24 @@ def test_nufft_256_32coils_all_coils_full_size(gpu, oracle):
     assert rel(img, P.adjoint_batch(ys)) < TOL_OP
 
 
+def test_codeare_toeplitz_needs_an_accurate_nfft(gpu):
+    from codeare_gb300 import capi, synth
+    k = synth.radial2d(16, 64, golden=True)
+    p = gpu.Plan((32, 32), k.shape[0], ncoils=2, m=1, alpha=1.0)
+    p.set_kspace(k)
+    p.set_weights(synth.ramp_weights(k))
+    p.set_sensitivities(synth.coils2d(32, 2))
+    y = np.ones((2, k.shape[0]), np.complex64)
+    x = np.zeros((32, 32), np.complex64)
+    with pytest.raises(capi.CgsError):
+        p.solve(y, x, mode=gpu.MODE_CODEARE, cgiter=2, toeplitz=True)
+    p.close()
+
+
 def test_batch_16_of_64_uneven_problems_full_size(gpu, oracle):
     """One graph launch over 16 of the 64 uneven problems at their own sizes,
-    codeare CGLS 15 iterations each, against the oracle problem by problem."""
+    codeare CGLS 15 iterations each, against the oracle problem by problem;
+    the same batch again with the CG steps on the Toeplitz kernels."""
     from codeare_gb300 import capi, synth
     probs = synth.uneven_batch()
     sel = [probs[i] for i in BATCH_SUBSET]
@@ -147,19 +166,24 @@ def test_batch_16_of_64_uneven_problems_full_size(gpu, oracle):
         plans.append(p)
         sens.append(S)
         ys.append(synth.add_noise(y, c["noise"], seed=c["seed"]))
-    b = capi.Batch(plans, capi.solve_opts(mode=gpu.MODE_CODEARE, cgiter=15, cgeps=0.0, lam=5e-2))
-    xs = [np.zeros((c["N"], c["N"]), np.complex64) for c in sel]
-    reps, _ = b.solve(ys, xs)
-    b.close()
+    runs = []
+    for toeplitz in (False, True):
+        b = capi.Batch(plans, capi.solve_opts(mode=gpu.MODE_CODEARE, cgiter=15, cgeps=0.0, lam=5e-2,
+                                              toeplitz=toeplitz))
+        xs = [np.zeros((c["N"], c["N"]), np.complex64) for c in sel]
+        reps, _ = b.solve(ys, xs)
+        b.close()
+        runs.append((toeplitz, xs, reps))
     for p in plans:
         p.close()
     errs = []
-    for c, S, y, x, r in zip(sel, sens, ys, xs, reps):
+    for i, (c, S, y) in enumerate(zip(sel, sens, ys)):
         s = oracle.Sense(S, c["k"], w=c["w"], m=c["m"], alpha=c["alpha"])
         xo, _ = s.cgls_codeare(y, cgiter=15, cgeps=0.0, lam=5e-2)
-        assert r["iterations"] == 15, c["name"]
-        errs.append((c["name"], rel(x, xo)))
-    bad = [e for e in errs if not e[1] < TOL_IMG]
+        for toeplitz, xs, reps in runs:
+            assert reps[i]["iterations"] == 15, c["name"]
+            errs.append((c["name"], toeplitz, rel(xs[i], xo)))
+    bad = [e for e in errs if not e[2] < TOL_IMG]
     assert not bad, bad
 
 
