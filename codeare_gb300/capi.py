@@ -27,7 +27,7 @@ EXPORTED = [
     "cgs_plan_info", "cgs_sync", "cgs_kernel_launches", "cgs_last_error",
     "cgs_profile_enable", "cgs_profile_collect", "cgs_nfft2d_trafo_noalloc",
     "cgs_net_num_params", "cgs_net_create", "cgs_net_destroy", "cgs_net_set_weights", "cgs_net_get_weights",
-    "cgs_net_forward", "cgs_net_gradients", "cgs_net_train_step", "cgs_solve_fcg", "cgs_normal_apply", "cgs_precond_apply",
+    "cgs_net_forward", "cgs_net_gradients", "cgs_net_train_step", "cgs_solve_fcg", "cgs_normal_apply", "cgs_precond_apply", "cgs_set_frame_sensitivities",
     "cgs_get_tuning", "cgs_set_tuning", "cgs_autotune", "cgs_batch_create", "cgs_batch_solve",
     "cgs_batch_destroy", "cgs_cs_create", "cgs_cs_destroy", "cgs_cs_adjoint", "cgs_cs_df", "cgs_cs_obj",
     "cgs_cs_wavelet",
@@ -118,6 +118,7 @@ def load(path: str = LIB_PATH):
     L.cgs_solve_fcg.argtypes = [vp, vp, vp, vp, C.POINTER(SolveOpts), vp, C.POINTER(SolveReport), vp]
     L.cgs_normal_apply.argtypes = [vp, vp, vp, C.POINTER(SolveOpts), vp]
     L.cgs_precond_apply.argtypes = [vp, vp, vp, C.POINTER(SolveOpts), vp]
+    L.cgs_set_frame_sensitivities.argtypes = [vp, C.c_int, vp]
     L.cgs_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.cgs_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.cgs_autotune.argtypes = [vp, C.POINTER(Tuning), C.POINTER(C.c_double), vp]
@@ -260,6 +261,10 @@ class Plan:
 
     def set_weights(self, w):
         _check(load().cgs_set_weights(self._h, _ptr(w)))
+
+    def set_frame_sensitivities(self, frame, s):
+        """the sensitivities (NC, N..) of one frame of a framed plan"""
+        _check(load().cgs_set_frame_sensitivities(self._h, int(frame), _ptr(s)))
 
     def set_sensitivities(self, s):
         _check(load().cgs_set_sensitivities(self._h, _ptr(s)))

@@ -1996,6 +1996,18 @@ cgs_status cgs_set_sensitivities(cgs_plan *p, const float *s_in)
     return CGS_OK;
 }
 
+cgs_status cgs_set_frame_sensitivities(cgs_plan *p, int frame, const float *s_in)
+{
+    if (!p || !s_in) { set_error("null argument"); return CGS_ERR_BAD_ARG; }
+    if (p->F <= 1 || frame < 0 || frame >= p->F) { set_error("frame index out of range (or not a framed plan)"); return CGS_ERR_BAD_ARG; }
+    CGS_CUDA(cudaSetDevice(p->device));
+    CGS_TRY(cgs_set_sensitivities(p->fr[frame], s_in));
+    bool all = true;
+    for (int f = 0; f < p->F; ++f) all = all && p->fr[f]->have_s;
+    p->have_s = all;
+    return CGS_OK;
+}
+
 cgs_status cgs_sync(cgs_plan *p)
 {
     if (!p) { set_error("null plan"); return CGS_ERR_BAD_ARG; }

@@ -19,7 +19,11 @@
 // (nk, NC, dim4[, dim5]); the CG-SENSE solve runs over the stacked frames.
 // The whole solve runs on the GPU (libcgs.so cgs_solve); unlike the
 // reference's CGLS member, no residual history survives between solves.
-// Not supported (the constructor throws): a Cartesian third dimension.
+// 3rd_dim_cart (NCSENSE.hpp:81-97, 105; NFFT.hpp:100-103): sensitivities
+// (N0, N1, slices, NC), images (N0, N1, slices), signals (nk, slices, NC);
+// every slice is a 2-D problem with the shared trajectory and its own slice of
+// the maps (a frame of the plan), and the CG-SENSE solve runs over the whole
+// stack, as the reference's CGLS does over its (N0, N1, slices) images.
 #pragma once
 
 #include <cstdio>
@@ -57,10 +61,11 @@ public:
             else throw std::invalid_argument("NCSENSE: mode must be codeare or standard");
         }
         m_weighted = try_to_fetch<int>(params, "weighted", 1);
-        if (try_to_fetch<bool>(params, "3rd_dim_cart", false))
-            throw std::invalid_argument("NCSENSE: a Cartesian third dimension is not supported");
+        m_cart = try_to_fetch<bool>(params, "3rd_dim_cart", false);
         m_dim4 = std::max<size_t>(1, try_to_fetch<size_t>(params, "dim4", 1));
         m_dim5 = std::max<size_t>(1, try_to_fetch<size_t>(params, "dim5", 1));
+        if (m_cart && (m_dim4 > 1 || m_dim5 > 1))
+            throw std::invalid_argument("NCSENSE: 3rd_dim_cart with dim4 / dim5 frames is not supported");
         plan();
     }
 
@@ -73,7 +78,7 @@ public:
         this->m_params = o.m_params;
         m_sm = o.m_sm; m_k = o.m_k; m_w = o.m_w;
         m_ftiter = o.m_ftiter; m_fteps = o.m_fteps; m_alpha = o.m_alpha; m_m = o.m_m; m_nk = o.m_nk;
-        m_dim4 = o.m_dim4; m_dim5 = o.m_dim5;
+        m_dim4 = o.m_dim4; m_dim5 = o.m_dim5; m_cart = o.m_cart;
         m_cgiter = o.m_cgiter; m_cgeps = o.m_cgeps; m_lambda = o.m_lambda; m_verbose = o.m_verbose;
         m_mode = o.m_mode; m_weighted = o.m_weighted; m_have_k = o.m_have_k; m_have_w = o.m_have_w;
         if (o.m_plan) {
@@ -97,12 +102,25 @@ public:
     {
         if (sm.Size() != m_sm.Size()) throw std::invalid_argument("NCSENSE: sensitivity size changed");
         m_sm = sm;
-        cgs_host::check(cgs_set_sensitivities(m_plan, reinterpret_cast<const float *>(m_sm.Ptr())),
-                        "cgs_set_sensitivities");
+        set_maps();
     }
 
     virtual void KSpace(const Matrix<RT> &k)
     {
+        if (m_cart) {
+            // one trajectory for every slice (the reference broadcasts it to
+            // each coil's NFFT, NCSENSE.hpp:204-223): one copy per frame
+            if (size(k, 1) != m_nk || size(k, 0) != m_rank || k.Size() != m_rank * m_nk)
+                throw NCSENSE_KSPACE_DIMENSIONS;
+            m_k = k;
+            Matrix<RT> kk(m_rank, m_nk, m_ncart);
+            for (size_t z = 0; z < m_ncart; ++z)
+                std::copy(k.Ptr(), k.Ptr() + k.Size(), kk.Ptr() + z * k.Size());
+            cgs_host::check(cgs_set_kspace(m_plan, kk.Ptr()), "cgs_set_kspace");
+            m_have_k = true;
+            if (m_have_w) cgs_host::check(cgs_set_weights(m_plan, m_w.Ptr()), "cgs_set_weights");
+            return;
+        }
         if (size(k, 1) != m_nk || size(k, 0) != m_rank || k.Size() != m_rank * m_nk * frames())
             throw NCSENSE_KSPACE_DIMENSIONS;
         m_k = k;
@@ -121,6 +139,14 @@ public:
 
     virtual Matrix<T> Trafo(const MatrixType<T> &m) const
     {
+        if (m_cart) {
+            // the plan writes (nk, NC, slice); the reference's m_fwd_out is
+            // (nk, slice, NC) (NCSENSE.hpp:105)
+            Matrix<T> tmp(m_nk, m_nc, m_ncart);
+            cgs_host::check(cgs_sense_trafo(m_plan, reinterpret_cast<const float *>(m.Ptr()),
+                                            reinterpret_cast<float *>(tmp.Ptr()), nullptr), "cgs_sense_trafo");
+            return cart_swap(tmp, m_nc, m_ncart);
+        }
         std::vector<size_t> od{m_nk, m_nc};  // m_fwd_out (NCSENSE.hpp:173)
         if (frames() > 1) od.push_back(m_dim4);
         if (m_dim5 > 1) od.push_back(m_dim5);
@@ -133,13 +159,15 @@ public:
 
     virtual Matrix<T> operator/(const MatrixType<T> &m) const
     {
+        const Matrix<T> mc = m_cart ? plan_order(m) : Matrix<T>();
+        const MatrixType<T> &in = m_cart ? mc : m;
         Matrix<T> out(image_dims());
         if (m_mode == CGS_MODE_CODEARE)
-            cgs_host::check(cgs_sense_adjoint_codeare(m_plan, reinterpret_cast<const float *>(m.Ptr()),
+            cgs_host::check(cgs_sense_adjoint_codeare(m_plan, reinterpret_cast<const float *>(in.Ptr()),
                                                       reinterpret_cast<float *>(out.Ptr()), (int)m_ftiter,
                                                       (double)m_fteps, nullptr), "cgs_sense_adjoint_codeare");
         else
-            cgs_host::check(cgs_sense_adjoint(m_plan, reinterpret_cast<const float *>(m.Ptr()),
+            cgs_host::check(cgs_sense_adjoint(m_plan, reinterpret_cast<const float *>(in.Ptr()),
                                               reinterpret_cast<float *>(out.Ptr()), m_weighted, nullptr),
                             "cgs_sense_adjoint");
         return out;
@@ -147,12 +175,14 @@ public:
 
     virtual Matrix<T> Adjoint(const MatrixType<T> &m) const
     {
+        const Matrix<T> mc = m_cart ? plan_order(m) : Matrix<T>();
+        const MatrixType<T> &in = m_cart ? mc : m;
         Matrix<T> out(image_dims());
         cgs_solve_opts o{};
         o.mode = m_mode; o.cgiter = (int)m_cgiter; o.cgeps = m_cgeps; o.lambda = m_lambda;
         o.ftiter = (int)m_ftiter; o.fteps = m_fteps; o.weighted = m_weighted;
         cgs_solve_report r{};
-        cgs_status s = cgs_solve(m_plan, reinterpret_cast<const float *>(m.Ptr()), reinterpret_cast<float *>(out.Ptr()),
+        cgs_status s = cgs_solve(m_plan, reinterpret_cast<const float *>(in.Ptr()), reinterpret_cast<float *>(out.Ptr()),
                                  &o, &r, nullptr);
         if (s != CGS_OK && s != CGS_ERR_NAN) cgs_host::check(s, "cgs_solve");
         m_last = r;
@@ -168,11 +198,13 @@ public:
     virtual Matrix<T> operator->*(const MatrixType<T> &m) const { return Adjoint(m); }
 
     size_t KSpaceSize() const { return m_nk; }
-    size_t frames() const { return m_dim4 * m_dim5; }
-    // image dims: N.. plus dim4 (and dim5) when batched (m_bwd_out without NC, NCSENSE.hpp:175-180)
+    size_t frames() const { return m_cart ? m_ncart : m_dim4 * m_dim5; }
+    // image dims: N.. plus dim4 (and dim5) when batched (m_bwd_out without NC, NCSENSE.hpp:175-180);
+    // with a Cartesian third dimension N0, N1 and the slices
     std::vector<size_t> image_dims() const
     {
         std::vector<size_t> v = m_imsz;
+        if (m_cart) { v.push_back(m_ncart); return v; }
         if (frames() > 1) v.push_back(m_dim4);
         if (m_dim5 > 1) v.push_back(m_dim5);
         return v;
@@ -196,6 +228,12 @@ private:
         if (nd < 3 || nd > 4) throw std::invalid_argument("NCSENSE: sensitivities must be (N,N[,N],NC)");
         m_rank = nd - 1;
         m_nc = size(m_sm, nd - 1);
+        if (m_cart) {
+            // (N0, N1, slices, NC): 2-D NFFTs per slice (NCSENSE.hpp:89-90)
+            if (nd != 4) throw std::invalid_argument("NCSENSE: 3rd_dim_cart needs sensitivities (N,N,slices,NC)");
+            m_rank = 2;
+            m_ncart = size(m_sm, 2);
+        }
         m_imsz.assign(m_rank, 0);
         for (size_t i = 0; i < m_rank; ++i) m_imsz[i] = size(m_sm, i);
         cgs_plan_desc d{};
@@ -207,8 +245,46 @@ private:
         d.ncoils = (int)m_nc;
         d.frames = (int)frames();
         cgs_host::check(cgs_plan_create(&m_plan, &d), "cgs_plan_create");
-        cgs_host::check(cgs_set_sensitivities(m_plan, reinterpret_cast<const float *>(m_sm.Ptr())),
-                        "cgs_set_sensitivities");
+        set_maps();
+    }
+
+    void set_maps()
+    {
+        if (!m_cart) {
+            cgs_host::check(cgs_set_sensitivities(m_plan, reinterpret_cast<const float *>(m_sm.Ptr())),
+                            "cgs_set_sensitivities");
+            return;
+        }
+        // slice z of every coil: (N0 N1) values at (c * slices + z) * N0 N1
+        const size_t px = m_imsz[0] * m_imsz[1];
+        Matrix<T> sl(m_imsz[0], m_imsz[1], m_nc);
+        for (size_t z = 0; z < m_ncart; ++z) {
+            for (size_t c = 0; c < m_nc; ++c)
+                std::copy(m_sm.Ptr() + (c * m_ncart + z) * px, m_sm.Ptr() + (c * m_ncart + z + 1) * px,
+                          sl.Ptr() + c * px);
+            cgs_host::check(cgs_set_frame_sensitivities(m_plan, (int)z, reinterpret_cast<const float *>(sl.Ptr())),
+                            "cgs_set_frame_sensitivities");
+        }
+    }
+
+    // (a, b, nk) <-> (b, a, nk) in codeare order: swaps the slice and coil axes of signals
+    static Matrix<T> cart_swap(const Matrix<T> &in, size_t a, size_t b)
+    {
+        const size_t nk = size(in, 0);
+        Matrix<T> out(nk, b, a);
+        for (size_t i = 0; i < a; ++i)
+            for (size_t j = 0; j < b; ++j)
+                std::copy(in.Ptr() + (j * a + i) * nk, in.Ptr() + (j * a + i + 1) * nk, out.Ptr() + (i * b + j) * nk);
+        return out;
+    }
+
+    // the caller's signals (nk, slices, NC) in the plan's order (nk, NC, slices)
+    Matrix<T> plan_order(const MatrixType<T> &m) const
+    {
+        if (m.Size() != m_nk * m_ncart * m_nc) throw std::invalid_argument("NCSENSE: signals must be (nk, slices, NC)");
+        Matrix<T> in(m_nk, m_ncart, m_nc);
+        std::copy(m.Ptr(), m.Ptr() + m.Size(), in.Ptr());
+        return cart_swap(in, m_ncart, m_nc);
     }
 
     void release()
@@ -222,7 +298,7 @@ private:
         m_plan = o.m_plan; o.m_plan = nullptr;
         m_sm = std::move(o.m_sm); m_k = std::move(o.m_k); m_w = std::move(o.m_w); m_imsz = o.m_imsz;
         m_rank = o.m_rank; m_nc = o.m_nc; m_nk = o.m_nk; m_ftiter = o.m_ftiter; m_m = o.m_m;
-        m_dim4 = o.m_dim4; m_dim5 = o.m_dim5;
+        m_dim4 = o.m_dim4; m_dim5 = o.m_dim5; m_cart = o.m_cart; m_ncart = o.m_ncart;
         m_cgiter = o.m_cgiter; m_fteps = o.m_fteps; m_alpha = o.m_alpha; m_cgeps = o.m_cgeps;
         m_lambda = o.m_lambda; m_verbose = o.m_verbose; m_have_k = o.m_have_k; m_have_w = o.m_have_w;
         m_mode = o.m_mode; m_weighted = o.m_weighted; m_last = o.m_last;
@@ -232,7 +308,8 @@ private:
     Matrix<T> m_sm;
     Matrix<RT> m_k, m_w;
     std::vector<size_t> m_imsz;
-    size_t m_rank = 2, m_nc = 1, m_nk = 1, m_ftiter = 3, m_m = 1, m_cgiter = 0, m_dim4 = 1, m_dim5 = 1;
+    size_t m_rank = 2, m_nc = 1, m_nk = 1, m_ftiter = 3, m_m = 1, m_cgiter = 0, m_dim4 = 1, m_dim5 = 1, m_ncart = 1;
+    bool m_cart = false;
     double m_fteps = 1e-3, m_alpha = 1.0;
     RT m_cgeps = 1.0e-6f, m_lambda = 1.0e-6f;
     bool m_verbose = false, m_have_k = false, m_have_w = false;

@@ -4,7 +4,7 @@
 // maxit = 3; NFFT.hpp:66-191), KSpace / Weights setters (:258-296), Trafo =
 // forward NFFT (:305-361) and Adjoint = the CGNR inverse NFFT (:370-436).
 // All arithmetic runs in libcgs.so on the GPU through the C ABI.  Not
-// supported (the constructor throws): 3rd_dim_cart, b0 / timing (the
+// supported (the constructor throws): b0 / timing (the
 // off-resonance plan) and pc.
 #pragma once
 
@@ -36,8 +36,15 @@ public:
         m_M = unsigned_cast(p["nk"]);
         if (!p.exists("imsz")) throw std::invalid_argument("NFFT: image dimensions (imsz) need to be specified");
         m_N = p.Get<std::vector<size_t>>("imsz");
-        if (try_to_fetch<bool>(p, "3rd_dim_cart", false))
-            throw std::invalid_argument("NFFT: a Cartesian third dimension is not supported");
+        // Cartesian third dimension (NFFT.hpp:85, 100-103): the last image
+        // dimension is a stack of m_ncart slices, each a 2-D NFFT with the shared
+        // trajectory (the reference leaves the FFT along the stack commented
+        // out, :312-332, :412-432); here the slices are the plan's coils
+        if (try_to_fetch<bool>(p, "3rd_dim_cart", false)) {
+            if (m_N.size() != 3) throw std::invalid_argument("NFFT: 3rd_dim_cart needs a 3-D image size");
+            m_ncart = m_N.back();
+            m_N.pop_back();
+        }
         // off-resonance data only takes effect when its size matches the image
         // (NFFT.hpp:113-140 of the reference warns and ignores it otherwise)
         size_t nimg = 1;
@@ -64,7 +71,7 @@ public:
         release();
         this->m_params = o.m_params;
         m_N = o.m_N; m_M = o.m_M; m_m = o.m_m; m_alpha = o.m_alpha; m_epsilon = o.m_epsilon;
-        m_maxit = o.m_maxit; m_k = o.m_k; m_w = o.m_w;
+        m_maxit = o.m_maxit; m_k = o.m_k; m_w = o.m_w; m_ncart = o.m_ncart;
         m_have_k = o.m_have_k; m_have_w = o.m_have_w;
         if (!m_N.empty()) {
             plan();
@@ -85,6 +92,8 @@ public:
 
     virtual void KSpace(const Matrix<RT> &k)
     {
+        // a per-slice trajectory (rank x nk x slices) only sets a flag in the
+        // reference and never reaches the plan (NFFT.hpp:269-270): not accepted
         if (k.Size() != m_M * m_N.size())
             throw std::invalid_argument("NFFT: k-space must hold rank x nk values");
         m_k = k;
@@ -104,8 +113,8 @@ public:
     virtual Matrix<T> Trafo(const MatrixType<T> &m) const
     {
         need_k();
-        if (m.Size() != image_numel()) throw std::invalid_argument("NFFT::Trafo: image size mismatch");
-        Matrix<T> out(m_M, 1);
+        if (m.Size() != image_numel() * m_ncart) throw std::invalid_argument("NFFT::Trafo: image size mismatch");
+        Matrix<T> out(m_M, m_ncart);
         cgs_host::check(cgs_nfft_trafo(m_plan, reinterpret_cast<const float *>(m.Ptr()),
                                        reinterpret_cast<float *>(out.Ptr()), nullptr), "cgs_nfft_trafo");
         return squeeze(out);
@@ -115,14 +124,14 @@ public:
     virtual Matrix<T> Adjoint(const MatrixType<T> &m) const
     {
         need_k();
-        if (m.Size() != m_M) throw std::invalid_argument("NFFT::Adjoint: sample count mismatch");
+        if (m.Size() != m_M * m_ncart) throw std::invalid_argument("NFFT::Adjoint: sample count mismatch");
         if (!m_have_w) {
             // the reference's solver reads uninitialised weights here; use unit weights
             Matrix<RT> ones(m_M, 1);
             for (auto &v : ones.Container()) v = 1.f;
             const_cast<NFFT *>(this)->Weights(ones);
         }
-        Matrix<T> out(m_N);
+        Matrix<T> out(out_dims());
         cgs_host::check(cgs_nfft_itrafo(m_plan, reinterpret_cast<const float *>(m.Ptr()),
                                         reinterpret_cast<float *>(out.Ptr()), (int)m_maxit, (double)m_epsilon,
                                         nullptr), "cgs_nfft_itrafo");
@@ -133,7 +142,7 @@ public:
     Matrix<T> AdjointTrue(const MatrixType<T> &m) const
     {
         need_k();
-        Matrix<T> out(m_N);
+        Matrix<T> out(out_dims());
         cgs_host::check(cgs_nfft_adjoint(m_plan, reinterpret_cast<const float *>(m.Ptr()),
                                          reinterpret_cast<float *>(out.Ptr()), nullptr), "cgs_nfft_adjoint");
         return out;
@@ -158,6 +167,13 @@ public:
 
 private:
     size_t image_numel() const { size_t p = 1; for (size_t v : m_N) p *= v; return p; }
+    // image dims of the adjoint: N.. plus the Cartesian stack (NFFT.hpp:378-379)
+    std::vector<size_t> out_dims() const
+    {
+        std::vector<size_t> v = m_N;
+        if (m_ncart > 1) v.push_back(m_ncart);
+        return v;
+    }
     void need_k() const { if (!m_have_k) throw std::logic_error("NFFT: k-space not set"); }
 
     void plan()
@@ -169,7 +185,7 @@ private:
         d.alpha = m_alpha;
         d.m = (int)m_m;
         d.M = (int64_t)m_M;
-        d.ncoils = 1;
+        d.ncoils = (int)m_ncart;   // the slices of a Cartesian third dimension, else one
         cgs_host::check(cgs_plan_create(&m_plan, &d), "cgs_plan_create");
     }
 
@@ -183,13 +199,13 @@ private:
     {
         m_plan = o.m_plan; o.m_plan = nullptr;
         m_N = o.m_N; m_M = o.m_M; m_m = o.m_m; m_maxit = o.m_maxit; m_alpha = o.m_alpha;
-        m_epsilon = o.m_epsilon; m_k = std::move(o.m_k); m_w = std::move(o.m_w);
+        m_epsilon = o.m_epsilon; m_k = std::move(o.m_k); m_w = std::move(o.m_w); m_ncart = o.m_ncart;
         m_have_k = o.m_have_k; m_have_w = o.m_have_w;
     }
 
     cgs_plan *m_plan = nullptr;
     std::vector<size_t> m_N;
-    size_t m_M = 0, m_m = 1, m_maxit = 3;
+    size_t m_M = 0, m_m = 1, m_maxit = 3, m_ncart = 1;
     RT m_alpha = 1.f, m_epsilon = 7e-4f;
     Matrix<RT> m_k, m_w;
     bool m_have_k = false, m_have_w = false;

@@ -272,6 +272,13 @@ cgs_status cgs_normal_apply(cgs_plan *plan, const float *x, float *out, const cg
 cgs_status cgs_plan_info(const cgs_plan *plan, int *rank, int *N, int *n, int64_t *M,
                          int *ncoils);
 
+/* Sensitivities of one frame of a framed plan (frames > 1), NC x N.. complex,
+ * coil-major: the maps of a stack of 2-D slices along a Cartesian third axis
+ * (NCSENSE's 3rd_dim_cart, src/matrix/ft/NCSENSE.hpp:81-97, 105: each slice is
+ * a frame with the shared trajectory and its own slice of the 3-D maps).
+ * cgs_set_sensitivities sets the same maps for every frame instead. */
+cgs_status cgs_set_frame_sensitivities(cgs_plan *plan, int frame, const float *sens);
+
 /* Synchronise the plan's stream. */
 cgs_status cgs_sync(cgs_plan *plan);
 

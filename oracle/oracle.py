@@ -276,10 +276,14 @@ class FramesSense:
     """NCSENSE with dim4 (x dim5) frames (NCSENSE.hpp:141-166, 204-348): frame
     f has its own trajectory ks[f]; every frame shares the sensitivities and
     the weights.  Images (F, *shape), data (F, NC, M); CGLS (CGLS.hpp:30-59)
-    runs over the stacked frames."""
+    runs over the stacked frames.  With S a list of per-frame maps it is the
+    3rd_dim_cart stack instead (NCSENSE.hpp:81-97, 105; NFFT.hpp:100-103,
+    335-358, 382-410): every slice a 2-D problem with its own slice of the
+    maps, the CG over the whole stack."""
 
     def __init__(self, S, ks, w=None, m=1, alpha=1.0, threads=0):
-        self.frames = [Sense(S, k, w=w, m=m, alpha=alpha, threads=threads) for k in ks]
+        Ss = list(S) if isinstance(S, (list, tuple)) else [S] * len(ks)
+        self.frames = [Sense(Sf, k, w=w, m=m, alpha=alpha, threads=threads) for Sf, k in zip(Ss, ks)]
         s0 = self.frames[0]
         self.F, self.nc, self.M = len(self.frames), s0.nc, s0.M
         self.shape = (self.F,) + tuple(s0.shape)

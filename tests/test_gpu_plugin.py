@@ -286,3 +286,52 @@ def test_compressed_sensing_plugin_nfft(gpu, tmp_path):
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert rel(cgsm.read(str(out))["im_dc"], xo) < 2e-3, r.stdout
+
+
+def test_plugin_cartesian_third_dimension(gpu, oracle, tmp_path):
+    """CGSENSE with dft_3rd_dim (NCSENSE's 3rd_dim_cart): sensitivities
+    (N, N, slices, NC), signals (nk, slices, NC), one trajectory for every
+    slice; the CGLS over the whole stack against the oracle's slice stack."""
+    from codeare_gb300 import synth
+    N, nz, nc, m, alpha = 32, 3, 4, 4, 2.0
+    k = synth.radial2d(32, 64, golden=True)
+    w = synth.ramp_weights(k)
+    S3 = synth.coils3d(N, nc)[:, N // 2 - 1:N // 2 - 1 + nz]          # (nc, slices, N, N)
+    x3 = synth.phantom3d(N)[N // 2 - 1:N // 2 - 1 + nz]                 # (slices, N, N)
+    fs = oracle.FramesSense([S3[:, z] for z in range(nz)], [k] * nz, w=w, m=m, alpha=alpha)
+    y = synth.add_noise(fs.trafo(x3), 1e-3, seed=6)                      # (slices, nc, nk)
+    xo, _ = fs.cgls_codeare(y, cgiter=8, cgeps=1e-9, lam=5e-2)
+    mats = {"sensitivities": np.ascontiguousarray(S3, dtype=np.complex64), "kspace": k, "weights": w,
+            "signals": np.ascontiguousarray(y.transpose(1, 0, 2), dtype=np.complex64)}
+    attrs = {"nk": k.shape[0], "lambda": 0.05, "m": m, "alpha": alpha, "cgeps": 1e-9, "cgmaxit": 8,
+             "ftmaxit": 3, "fteps": 0.001, "noise": 0, "testcase": 0, "dft_3rd_dim": 1}
+    img, log = run_plugin(tmp_path, mats, attrs)
+    assert img.shape == (nz, N, N)
+    assert rel(img, xo) < TOL_IMG, log
+
+
+def test_nfft_cartesian_third_dimension(gpu, oracle, tmp_path):
+    """NuFFT with dft_3rd_dim (NFFT's 3rd_dim_cart): a stack of 2-D inverse
+    NFFTs over the slices, one trajectory; each slice against the oracle's
+    CGNR (the NuFFT module's 3 steps, epsilon 7e-4)."""
+    from codeare_gb300 import build, cgsm, synth
+    N, nz = 32, 3
+    k = synth.radial2d(24, 64, golden=True)
+    w = synth.ramp_weights(k)
+    rng = np.random.default_rng(12)
+    data = (rng.standard_normal((nz, k.shape[0])) + 1j * rng.standard_normal((nz, k.shape[0]))).astype(np.complex64)
+    P = oracle.NFFT((N, N), k.shape[0], m=1, alpha=1.0)
+    P.set_x(k)
+    what = oracle.damp_mask((N, N))
+    ref = np.stack([P.itrafo(data[z], w, what, 3, 7e-4)[0] for z in range(nz)])
+    build.build()
+    inp, out, xml = tmp_path / "in.cgsm", tmp_path / "out.cgsm", tmp_path / "cfg.xml"
+    cgsm.write(str(inp), {"kspace": k, "weights": w, "data": data})
+    xml.write_text('<NuFFT dim="3" nx="%d" ny="%d" nz="%d" M="%d" shots="1" maxit="3" epsilon="7e-4" '
+                   'dft_3rd_dim="1"/>\n' % (N, N, nz, k.shape[0]))
+    r = subprocess.run([build.DRIVER, build.PLUGIN_NUFFT, str(xml), str(inp), str(out), "img"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    img = cgsm.read(str(out))["img"]
+    assert img.shape == (nz, N, N)
+    assert rel(img, ref) < 2e-5
