@@ -737,11 +737,23 @@ def run_profile_case(args):
     """Forward + adjoint steps of one workload and nothing else, for profiler
     captures (prints one summary line, no JSON contract):
       nufft256    -- the 256^2, 32-coil NuFFT of the headline (default tuning);
-      kooshball64 -- the 64^3 downsample of the kooshball, 16 coils, E and E^H W."""
+      kooshball64 -- the 64^3 downsample of the kooshball, 16 coils, E and E^H W;
+      cnn256      -- the learned preconditioner's network on one 256^2 image."""
     import torch
     import codeare_gb300 as cg
     from codeare_gb300 import capi, synth
     torch.cuda.set_device(0)
+    if args.profile_case == "cnn256":
+        from codeare_gb300 import learned
+        net = learned.load_net() or capi.Net(max_batch=1, max_h=256, max_w=256)
+        x = torch.randn((1, 256, 256, 2), device="cuda")
+        y = torch.empty_like(x)
+        for _ in range(args.warmup + args.steps):
+            net.forward(x, y)
+        torch.cuda.synchronize()
+        net.close()
+        print("profile case cnn256: %d steps" % (args.warmup + args.steps))
+        return 0
     if args.profile_case == "nufft256":
         k, fh = workload_data()
         p = cg.Plan((N, N), k.shape[0], ncoils=NC, m=M_KB, alpha=SIGMA)
@@ -783,7 +795,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default gridding decomposition (profiling runs: no candidate launches)")
     ap.add_argument("--no-cgsense", action="store_true", help="skip the CG-SENSE, batch, kooshball, learned-preconditioner and CS sections")
-    ap.add_argument("--profile-case", choices=["nufft256", "kooshball64"],
+    ap.add_argument("--profile-case", choices=["nufft256", "kooshball64", "cnn256"],
                     help="run only this workload's forward+adjoint steps (profiler captures; no JSON line)")
     args = ap.parse_args()
     if args.profile_case:
