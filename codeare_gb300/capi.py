@@ -27,7 +27,7 @@ EXPORTED = [
     "cgs_plan_info", "cgs_sync", "cgs_kernel_launches", "cgs_last_error",
     "cgs_profile_enable", "cgs_profile_collect", "cgs_nfft2d_trafo_noalloc",
     "cgs_net_num_params", "cgs_net_create", "cgs_net_destroy", "cgs_net_set_weights", "cgs_net_get_weights",
-    "cgs_net_forward", "cgs_net_gradients", "cgs_net_train_step", "cgs_solve_fcg", "cgs_normal_apply", "cgs_precond_apply", "cgs_set_frame_sensitivities",
+    "cgs_net_forward", "cgs_net_gradients", "cgs_net_train_step", "cgs_solve_fcg", "cgs_normal_apply", "cgs_precond_apply", "cgs_set_frame_sensitivities", "cgs_net_set_conv_kernel",
     "cgs_get_tuning", "cgs_set_tuning", "cgs_autotune", "cgs_batch_create", "cgs_batch_solve",
     "cgs_batch_destroy", "cgs_cs_create", "cgs_cs_destroy", "cgs_cs_adjoint", "cgs_cs_df", "cgs_cs_obj",
     "cgs_cs_wavelet",
@@ -119,6 +119,7 @@ def load(path: str = LIB_PATH):
     L.cgs_normal_apply.argtypes = [vp, vp, vp, C.POINTER(SolveOpts), vp]
     L.cgs_precond_apply.argtypes = [vp, vp, vp, C.POINTER(SolveOpts), vp]
     L.cgs_set_frame_sensitivities.argtypes = [vp, C.c_int, vp]
+    L.cgs_net_set_conv_kernel.argtypes = [vp, C.c_int]
     L.cgs_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.cgs_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.cgs_autotune.argtypes = [vp, C.POINTER(Tuning), C.POINTER(C.c_double), vp]
@@ -448,6 +449,10 @@ class Net:
     def set_weights(self, w):
         w = np.ascontiguousarray(w, dtype=np.float32)
         _check(load().cgs_net_set_weights(self._h, _ptr(w)))
+
+    def set_conv_kernel(self, kind):
+        """32 -> 32 layers on tcgen05 (1, default) or mma.sync (0)"""
+        _check(load().cgs_net_set_conv_kernel(self._h, int(kind)))
 
     def forward(self, x, out=None, stream=None):
         B, H, W, _ = x.shape

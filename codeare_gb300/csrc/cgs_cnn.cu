@@ -151,6 +151,173 @@ conv32_mma_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__re
     }
 }
 
+// ---------------------------------------------------------------------------
+// 32 -> 32 convolution on the 5th-generation tensor cores (tcgen05).  A CTA
+// computes an 8 x 16-pixel tile (M = 128 pixels) x 32 output channels (N):
+// one thread issues 18 tcgen05.mma.kind::f16 (BF16 operands, K = 16: 9 taps
+// x 2 channel halves) whose FP32 accumulator lives in 32 TMEM columns, and a
+// tcgen05.commit arrives on an mbarrier when they are done.  Operands sit in
+// shared memory in the canonical K-major layout without swizzle: "core
+// matrices" of 8 rows x 16 bytes (8 BF16 values of K), each 128 contiguous
+// bytes, adjacent core matrices along K `lbo` bytes apart and along M / N
+// `sbo` bytes apart.
+//   A (per tap, 128 pixels x 32 channels): core (m / 8, k / 8) at
+//     (m / 8) * 512 + (k / 8) * 128, so lbo = 128, sbo = 512; k-step j of a
+//     tap starts 256 j bytes in;
+//   B (32 output channels x 288 = 9 taps x 32 input channels): core
+//     (n / 8, k / 8) at (k / 8) * 512 + (n / 8) * 128, so lbo = 512,
+//     sbo = 128; the k-step of (tap t, half j) starts (4 t + 2 j) * 512 in.
+// The threads build A from a halo tile of the input (the im2col of each
+// tap) and B from the weights with ordinary stores, then a proxy fence
+// makes them visible to the tensor cores.  Each warp reads its 32 TMEM lanes
+// (its 32 pixels, 32 channels each) with tcgen05.ld for the epilogue.  The
+// mbarrier wait is bounded: past the limit the CTA sets *err, skips the
+// epilogue and still frees its TMEM.
+// ---------------------------------------------------------------------------
+constexpr int kTcA = 9 * 128 * kC * 2;          // 9 taps of 128 x 32 BF16
+constexpr int kTcB = kC * 9 * kC * 2;           // 32 x 288 BF16
+constexpr int kTcHalo = (kTH + 2) * (kTW + 2) * kC * 2;
+constexpr int kTcSmem = kTcA + kTcB + kTcHalo + 16;
+constexpr uint32_t kTcWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start, leading / stride byte offsets
+// (16-byte units), descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(128, 1)
+conv32_tc05_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__restrict__ Wt,
+                   __nv_bfloat16 *__restrict__ Y, const __nv_bfloat16 *__restrict__ Mask, int H, int W,
+                   int *__restrict__ err)
+{
+    extern __shared__ __align__(128) uint8_t tsm[];
+    uint8_t *sA = tsm;
+    uint8_t *sB = tsm + kTcA;
+    uint8_t *sX = sB + kTcB;                                  // halo tile [10 x 18 px][32 ch]
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(sX + kTcHalo);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int b = blockIdx.z;
+    const int y0 = blockIdx.y * kTH, x0 = blockIdx.x * kTW;
+    const __nv_bfloat16 *Xb = X + (size_t)b * H * W * kC;
+
+    if (warp == 0) {   // 32 TMEM columns: the 128 x 32 FP32 accumulator
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(smem_u32(tslot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
+    // weights: (tap, co, 8-channel chunk) -> core (co / 8, (32 tap + ci) / 8)
+    for (int e = tid; e < 9 * kC * 4; e += 128) {
+        const int q = e & 3, co = (e >> 2) % kC, tap = (e >> 2) / kC;
+        const uint4 v = *reinterpret_cast<const uint4 *>(&Wt[(tap * kC + co) * kC + q * 8]);
+        *reinterpret_cast<uint4 *>(sB + ((tap * 4 + q) * 4 + (co >> 3)) * 128 + (co & 7) * 16) = v;
+    }
+    // input tile with a one-pixel halo, zero outside the image
+    for (int e = tid; e < (kTH + 2) * (kTW + 2) * 4; e += 128) {
+        const int pix = e >> 2, q = e & 3;
+        const int gy = y0 + pix / (kTW + 2) - 1, gx = x0 + pix % (kTW + 2) - 1;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (gy >= 0 && gy < H && gx >= 0 && gx < W)
+            v = *reinterpret_cast<const uint4 *>(&Xb[((size_t)gy * W + gx) * kC + q * 8]);
+        *reinterpret_cast<uint4 *>(sX + pix * 64 + q * 16) = v;
+    }
+    __syncthreads();
+    // im2col: pixel m = tid (row m / 16, column m % 16) of every tap
+    {
+        const int r = tid >> 4, c = tid & 15;
+        uint8_t *dst0 = sA + (tid >> 3) * 512 + (tid & 7) * 16;
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap) {
+            const uint8_t *src = sX + ((r + tap / 3) * (kTW + 2) + c + tap % 3) * 64;
+            uint8_t *dst = dst0 + tap * (128 * kC * 2);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                *reinterpret_cast<uint4 *>(dst + q * 128) = *reinterpret_cast<const uint4 *>(src + q * 16);
+        }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+    if (tid == 0) {
+        // instruction descriptor: D FP32, A and B BF16, both K-major, N = 32, M = 128
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kC >> 3) << 17) | ((128u >> 4) << 24);
+        const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+#pragma unroll 1
+        for (int tap = 0; tap < 9; ++tap)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const uint64_t ad = umma_desc(a0 + tap * (128 * kC * 2) + j * 256, 128, 512);
+                const uint64_t bd = umma_desc(b0 + (tap * 4 + j * 2) * 512, 512, 128);
+                const uint32_t acc = (tap | j) ? 1u : 0u;
+                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                             ::"r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                     ::"r"(smem_u32(mbar)) : "memory");
+    }
+    // bounded wait for the MMAs
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < kTcWaitLimit && !done; ++it)
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}" : "=r"(done) : "r"(smem_u32(mbar)) : "memory");
+    // tcgen05.ld is warp-collective: the whole warp reads, or none of it does
+    done = __all_sync(0xffffffffu, done);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!done) {
+        if (lane == 0) atomicOr(err, 1);
+    } else {
+        float v[32];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                     "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                     "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                     : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]),
+                       "=f"(v[7]), "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]),
+                       "=f"(v[14]), "=f"(v[15]), "=f"(v[16]), "=f"(v[17]), "=f"(v[18]), "=f"(v[19]),
+                       "=f"(v[20]), "=f"(v[21]), "=f"(v[22]), "=f"(v[23]), "=f"(v[24]), "=f"(v[25]),
+                       "=f"(v[26]), "=f"(v[27]), "=f"(v[28]), "=f"(v[29]), "=f"(v[30]), "=f"(v[31])
+                     : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        const int gy = y0 + (tid >> 4), gx = x0 + (tid & 15);
+        if (gy < H && gx < W) {
+            const size_t pix = ((size_t)b * H + gy) * W + gx;
+            __align__(16) __nv_bfloat162 o[kC / 2];
+#pragma unroll
+            for (int c = 0; c < kC; c += 2) {
+                float a = v[c], d = v[c + 1];
+                if (EPI == 0) { a = fmaxf(a, 0.f); d = fmaxf(d, 0.f); }
+                if (EPI == 1) {
+                    const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162 *>(&Mask[pix * kC + c]);
+                    if (!(bf(mk.x) > 0.f)) a = 0.f;
+                    if (!(bf(mk.y) > 0.f)) d = 0.f;
+                }
+                o[c / 2] = __floats2bfloat162_rn(a, d);
+            }
+            uint4 *dst = reinterpret_cast<uint4 *>(&Y[pix * kC]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) dst[q] = reinterpret_cast<const uint4 *>(o)[q];
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem));
+    }
+}
+
 // 2 -> 32 layer (+ReLU): thread per pixel; input fp32 [B][H][W][2]
 __global__ void conv_in_kernel(const float *__restrict__ X, const float *__restrict__ Wf,
                                __nv_bfloat16 *__restrict__ Y, int B, int H, int W)
@@ -377,9 +544,34 @@ struct cgs_net {
     float *loss = nullptr, *scale = nullptr;
     int64_t step = 0;
     uint64_t serial = 0;              // unique per created network (graphs key on it, not the address)
+    int conv_kind = 1;                // 32 -> 32 layers: 1 tcgen05 (default), 0 mma.sync
+    int *err = nullptr;               // set by a tcgen05 layer whose MMA wait ran out
 };
 
 namespace {
+
+// one 32 -> 32 layer with the network's kernel choice; EPI 0 ReLU, 1 the input-gradient mask
+template <int EPI>
+cgs_status conv32(cgs_net *n, const __nv_bfloat16 *x, const __nv_bfloat16 *w, __nv_bfloat16 *y,
+                  const __nv_bfloat16 *mask, int B, int H, int W, cudaStream_t st)
+{
+    dim3 grd((W + kTW - 1) / kTW, (H + kTH - 1) / kTH, B);
+    if (n->conv_kind == 1) {
+        static std::atomic<uint64_t> attr_devs{0};
+        int dev = 0;
+        CGS_CUDA(cudaGetDevice(&dev));
+        const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
+        if (!(attr_devs.load() & bit)) {
+            CGS_CUDA(cudaFuncSetAttribute(conv32_tc05_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+            attr_devs.fetch_or(bit);
+        }
+        conv32_tc05_kernel<EPI><<<grd, 128, kTcSmem, st>>>(x, w, y, mask, H, W, n->err);
+    } else {
+        conv32_mma_kernel<EPI><<<grd, 128, 0, st>>>(x, w, y, mask, H, W);
+    }
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
 
 cgs_status net_refresh_bf16(cgs_net *n, cudaStream_t st)
 {
@@ -395,11 +587,8 @@ cgs_status net_forward_dev(cgs_net *n, int B, int H, int W, cudaStream_t st)
     const int64_t P = (int64_t)B * H * W;
     conv_in_kernel<<<blocks_for(P), 256, 0, st>>>(n->x0, n->w + layer_offset(0), n->act[0], B, H, W);
     CGS_LAUNCH_CHECK();
-    dim3 grd((W + kTW - 1) / kTW, (H + kTH - 1) / kTH, B);
-    for (int l = 1; l <= 3; ++l) {
-        conv32_mma_kernel<0><<<grd, 128, 0, st>>>(n->act[l - 1], n->wb + (l - 1) * 9 * kC * kC, n->act[l], nullptr, H, W);
-        CGS_LAUNCH_CHECK();
-    }
+    for (int l = 1; l <= 3; ++l)
+        CGS_TRY(conv32<0>(n, n->act[l - 1], n->wb + (l - 1) * 9 * kC * kC, n->act[l], nullptr, B, H, W, st));
     conv_out_kernel<<<blocks_for(P), 256, 0, st>>>(n->act[3], n->w + layer_offset(4), n->y5, B, H, W);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
@@ -420,20 +609,33 @@ cgs_status net_backward_dev(cgs_net *n, int B, int H, int W, cudaStream_t st)
     conv_out_back_kernel<<<blocks_for(P), 256, 0, st>>>(n->d5, n->w + layer_offset(4), n->act[3], n->dA, B, H, W);
     CGS_LAUNCH_CHECK();
     // layers 4..2 (32 -> 32): dA holds the gradient at the layer's output (pre-activation)
-    dim3 grd((W + kTW - 1) / kTW, (H + kTH - 1) / kTH, B);
     __nv_bfloat16 *cur = n->dA, *nxt = n->dB;
     for (int l = 3; l >= 1; --l) {
         wgrad_kernel<__nv_bfloat16, __nv_bfloat16, kC, kC><<<wg, 256, 0, st>>>(n->act[l - 1], cur, n->g + layer_offset(l), H, W);
         CGS_LAUNCH_CHECK();
         flip_weights_kernel<<<36, 256, 0, st>>>(n->w + layer_offset(l), n->wflip);
         CGS_LAUNCH_CHECK();
-        conv32_mma_kernel<1><<<grd, 128, 0, st>>>(cur, n->wflip, nxt, n->act[l - 1], H, W);
-        CGS_LAUNCH_CHECK();
+        CGS_TRY(conv32<1>(n, cur, n->wflip, nxt, n->act[l - 1], B, H, W, st));
         __nv_bfloat16 *tmp = cur; cur = nxt; nxt = tmp;
     }
     // layer 1 (2 -> 32): weight gradient only
     wgrad_kernel<float, __nv_bfloat16, 2, kC><<<wg, 256, 0, st>>>(n->x0, cur, n->g + layer_offset(0), H, W);
     CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+std::atomic<uint64_t> g_net_serial{0};
+
+// a tcgen05 layer that gave up waiting for its MMAs sets the flag: report it once
+cgs_status net_check_err(cgs_net *n)
+{
+    int e = 0;
+    CGS_CUDA(cudaMemcpy(&e, n->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        cudaMemset(n->err, 0, sizeof(int));
+        set_error("a tcgen05 convolution timed out waiting for its MMAs");
+        return CGS_ERR_TIMEOUT;
+    }
     return CGS_OK;
 }
 
@@ -473,9 +675,8 @@ int64_t cgs_net_num_params(void) { return kParams; }
 cgs_status cgs_net_create(cgs_net **out, int max_batch, int max_h, int max_w)
 {
     if (!out || max_batch < 1 || max_h < 1 || max_w < 1) { set_error("bad net size"); return CGS_ERR_BAD_ARG; }
-    static std::atomic<uint64_t> next_serial{1};
     cgs_net *n = new cgs_net();
-    n->serial = next_serial++;
+    n->serial = ++g_net_serial;
     n->maxB = max_batch; n->maxH = max_h; n->maxW = max_w;
     const int64_t P = (int64_t)max_batch * max_h * max_w;
     bool ok = true;
@@ -495,9 +696,11 @@ cgs_status cgs_net_create(cgs_net **out, int max_batch, int max_h, int max_w)
     al((void **)&n->dB, sizeof(__nv_bfloat16) * P * kC);
     al((void **)&n->loss, sizeof(float));
     al((void **)&n->scale, sizeof(float));
+    al((void **)&n->err, sizeof(int));
     if (!ok) { cgs_net_destroy(n); set_error("cudaMalloc failed for the network"); return CGS_ERR_OOM; }
     cudaMemset(n->m, 0, sizeof(float) * kParams);
     cudaMemset(n->v, 0, sizeof(float) * kParams);
+    cudaMemset(n->err, 0, sizeof(int));
     // He-style initialisation (fixed seed, host)
     std::vector<float> w(kParams);
     uint64_t s = 0x9e3779b97f4a7c15ull;
@@ -522,7 +725,7 @@ cgs_status cgs_net_destroy(cgs_net *n)
 {
     if (!n) return CGS_OK;
     void *b[] = {n->w, n->g, n->m, n->v, n->wb, n->wflip, n->x0, n->y5, n->d5, n->target, n->act[0], n->act[1],
-                 n->act[2], n->act[3], n->dA, n->dB, n->loss, n->scale};
+                 n->act[2], n->act[3], n->dA, n->dB, n->loss, n->scale, n->err};
     for (void *p : b)
         if (p) cudaFree(p);
     delete n;
@@ -557,6 +760,14 @@ cgs_status cgs_net_forward(cgs_net *n, const float *x, float *y, int B, int H, i
     CGS_TRY(net_forward_dev(n, B, H, W, st));
     CGS_CUDA(cudaMemcpyAsync(y, n->y5, bytes, cudaMemcpyDefault, st));
     CGS_CUDA(cudaStreamSynchronize(st));
+    return net_check_err(n);
+}
+
+cgs_status cgs_net_set_conv_kernel(cgs_net *n, int kind)
+{
+    if (!n || (kind != 0 && kind != 1)) { set_error("conv kernel kind must be 0 (mma.sync) or 1 (tcgen05)"); return CGS_ERR_BAD_ARG; }
+    n->conv_kind = kind;
+    n->serial = ++g_net_serial;   // captured solve graphs hold the kernels by launch: rebuild them
     return CGS_OK;
 }
 
@@ -573,7 +784,7 @@ cgs_status cgs_net_gradients(cgs_net *n, const float *x, const float *target, in
     if (grad) CGS_CUDA(cudaMemcpyAsync(grad, n->g, sizeof(float) * kParams, cudaMemcpyDefault, st));
     if (loss) CGS_CUDA(cudaMemcpyAsync(loss, n->loss, sizeof(float), cudaMemcpyDefault, st));
     CGS_CUDA(cudaStreamSynchronize(st));
-    return CGS_OK;
+    return net_check_err(n);
 }
 
 cgs_status cgs_net_train_step(cgs_net *n, const float *x, const float *target, int B, int H, int W, float lr,

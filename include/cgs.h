@@ -170,6 +170,13 @@ cgs_status cgs_net_destroy(cgs_net *net);
 cgs_status cgs_net_set_weights(cgs_net *net, const float *w);
 cgs_status cgs_net_get_weights(cgs_net *net, float *w);
 cgs_status cgs_net_forward(cgs_net *net, const float *x, float *y, int B, int H, int W, void *stream);
+/* The kernel of the 32 -> 32 layers (forward and input gradients): 1 (the
+ * default) the 5th-generation tensor cores (tcgen05.mma with the accumulator
+ * in tensor memory), 0 the warp-level mma.sync kernel.  Both compute the same
+ * BF16 products with FP32 accumulation.  A tcgen05 layer whose bounded wait
+ * for its MMAs runs out makes the next forward / gradients call return
+ * CGS_ERR_TIMEOUT. */
+cgs_status cgs_net_set_conv_kernel(cgs_net *net, int kind);
 /* mean-squared-error gradients w.r.t. all weights (for checks) */
 cgs_status cgs_net_gradients(cgs_net *net, const float *x, const float *target, int B, int H, int W,
                              float *grad, float *loss, void *stream);

@@ -61,6 +61,34 @@ def test_cnn_forward_and_gradients_match_fp64(gpu):
     net.close()
 
 
+@pytest.mark.parametrize("B,H,W", [(1, 256, 256), (2, 40, 24), (3, 17, 33)])
+def test_tcgen05_layers_match_mma_sync(gpu, B, H, W):
+    """The 32 -> 32 layers on the 5th-generation tensor cores (tcgen05.mma,
+    TMEM accumulator) against the warp-level mma.sync kernel: same BF16
+    products, FP32 accumulation in another order.  Forward outputs and all
+    weight gradients (the input-gradient layers run on the chosen kernel too),
+    on image sizes that leave partial 8 x 16 tiles."""
+    from codeare_gb300 import capi
+    rng = np.random.default_rng(B * 1000 + H + W)
+    x = rng.standard_normal((B, H, W, 2)).astype(np.float32)
+    t = rng.standard_normal((B, H, W, 2)).astype(np.float32)
+    outs = {}
+    for kind in (0, 1):
+        net = capi.Net(max_batch=B, max_h=H, max_w=W)
+        net.set_conv_kernel(kind)
+        y = net.forward(x)
+        loss, g = net.gradients(x, t)
+        outs[kind] = (y, g, loss)
+        net.close()
+    y0, g0, l0 = outs[0]
+    y1, g1, l1 = outs[1]
+    assert np.all(np.isfinite(y1)) and np.all(np.isfinite(g1))
+    # BF16 activations: a different FP32 summation order flips some roundings
+    assert np.linalg.norm(y1 - y0) <= 1e-2 * np.linalg.norm(y0)
+    assert np.linalg.norm(g1 - g0) <= 1e-2 * np.linalg.norm(g0)
+    assert abs(l1 - l0) <= 1e-2 * abs(l0)
+
+
 def test_cnn_training_reduces_loss(gpu):
     """Adam steps on a fixed linear target map (a smoothing of the input)."""
     from codeare_gb300 import capi
