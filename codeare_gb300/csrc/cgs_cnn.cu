@@ -3,11 +3,13 @@
 // layers, no biases, so the map is positively homogeneous: M(c r) = c M(r)
 // for c > 0).  Activations and weights in BF16, accumulation in FP32.
 //
-//   conv32_mma_kernel    32 -> 32 layers on the tensor cores (mma.sync
-//                        m16n8k16 bf16 -> fp32), used for the forward pass and,
-//                        with flipped/transposed weights, for the input
-//                        gradients of the backward pass
-//   conv_in / conv_out   the thin 2 -> 32 and 32 -> 2 layers on CUDA cores
+//   conv32_tc05_kernel   32 -> 32 layers on the 5th-generation tensor cores
+//                        (tcgen05.mma, TMEM accumulator), used for the forward
+//                        pass and, with flipped/transposed weights, for the
+//                        input gradients of the backward pass
+//   conv32_mma_kernel    the same layers with warp-level mma.sync m16n8k16
+//                        (selectable, cgs_net_set_conv_kernel)
+//   conv_in / conv_out_v the thin 2 -> 32 and 32 -> 2 layers on CUDA cores
 //   wgrad_kernel         weight gradients (reduction over pixels, CUDA cores)
 //   adam_kernel          Adam update of the FP32 master weights
 //
@@ -161,23 +163,28 @@ conv32_mma_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__re
 // matrices" of 8 rows x 16 bytes (8 BF16 values of K), each 128 contiguous
 // bytes, adjacent core matrices along K `lbo` bytes apart and along M / N
 // `sbo` bytes apart.
-//   A (per tap, 128 pixels x 32 channels): core (m / 8, k / 8) at
-//     (m / 8) * 512 + (k / 8) * 128, so lbo = 128, sbo = 512; k-step j of a
-//     tap starts 256 j bytes in;
+//   A: the tile's pixels are ordered m = 8 x + y (column-major), and the
+//     input halo tile (10 rows x 18 columns x 32 channels) is stored as
+//     [column][channel group of 8][row][16 bytes] (640 bytes per column).
+//     The 8 rows of a core matrix (pixels y = 0..7 of column x) are then 8
+//     consecutive 16-byte rows of the halo column x + dx starting at row dy,
+//     so the A matrix of tap (dy, dx) is a descriptor into the halo tile
+//     itself: start dx * 640 + dy * 16 (+ 320 for the upper channel half),
+//     lbo = 160 (next channel group), sbo = 640 (next column).  No im2col
+//     copy is made.
 //   B (32 output channels x 288 = 9 taps x 32 input channels): core
 //     (n / 8, k / 8) at (k / 8) * 512 + (n / 8) * 128, so lbo = 512,
 //     sbo = 128; the k-step of (tap t, half j) starts (4 t + 2 j) * 512 in.
-// The threads build A from a halo tile of the input (the im2col of each
-// tap) and B from the weights with ordinary stores, then a proxy fence
-// makes them visible to the tensor cores.  Each warp reads its 32 TMEM lanes
-// (its 32 pixels, 32 channels each) with tcgen05.ld for the epilogue.  The
-// mbarrier wait is bounded: past the limit the CTA sets *err, skips the
-// epilogue and still frees its TMEM.
+// The threads store the halo tile and the weights with ordinary stores, then
+// a proxy fence makes them visible to the tensor cores.  Each warp reads its
+// 32 TMEM lanes (pixels m = 32 w .. 32 w + 31, 32 channels each) with
+// tcgen05.ld for the epilogue.  The mbarrier wait is bounded: past the limit
+// the CTA sets *err, skips the epilogue and still frees its TMEM.
 // ---------------------------------------------------------------------------
-constexpr int kTcA = 9 * 128 * kC * 2;          // 9 taps of 128 x 32 BF16
 constexpr int kTcB = kC * 9 * kC * 2;           // 32 x 288 BF16
-constexpr int kTcHalo = (kTH + 2) * (kTW + 2) * kC * 2;
-constexpr int kTcSmem = kTcA + kTcB + kTcHalo + 16;
+constexpr int kTcCol = 4 * (kTH + 2) * 16;      // one halo column: 4 channel groups x 10 rows x 16 B
+constexpr int kTcHalo = (kTW + 2) * kTcCol;
+constexpr int kTcSmem = kTcB + kTcHalo + 16;
 constexpr uint32_t kTcWaitLimit = 1u << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -194,15 +201,14 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint3
 }
 
 template <int EPI>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128)
 conv32_tc05_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__restrict__ Wt,
                    __nv_bfloat16 *__restrict__ Y, const __nv_bfloat16 *__restrict__ Mask, int H, int W,
                    int *__restrict__ err)
 {
     extern __shared__ __align__(128) uint8_t tsm[];
-    uint8_t *sA = tsm;
-    uint8_t *sB = tsm + kTcA;
-    uint8_t *sX = sB + kTcB;                                  // halo tile [10 x 18 px][32 ch]
+    uint8_t *sB = tsm;
+    uint8_t *sX = sB + kTcB;                                  // halo tile, column-major (see above)
     uint64_t *mbar = reinterpret_cast<uint64_t *>(sX + kTcHalo);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -221,28 +227,16 @@ conv32_tc05_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__r
         const uint4 v = *reinterpret_cast<const uint4 *>(&Wt[(tap * kC + co) * kC + q * 8]);
         *reinterpret_cast<uint4 *>(sB + ((tap * 4 + q) * 4 + (co >> 3)) * 128 + (co & 7) * 16) = v;
     }
-    // input tile with a one-pixel halo, zero outside the image
+    // input tile with a one-pixel halo, zero outside the image: row r, column cx,
+    // channel group q at cx * 640 + q * 160 + r * 16
     for (int e = tid; e < (kTH + 2) * (kTW + 2) * 4; e += 128) {
         const int pix = e >> 2, q = e & 3;
-        const int gy = y0 + pix / (kTW + 2) - 1, gx = x0 + pix % (kTW + 2) - 1;
+        const int r = pix / (kTW + 2), cx = pix % (kTW + 2);
+        const int gy = y0 + r - 1, gx = x0 + cx - 1;
         uint4 v = make_uint4(0, 0, 0, 0);
         if (gy >= 0 && gy < H && gx >= 0 && gx < W)
             v = *reinterpret_cast<const uint4 *>(&Xb[((size_t)gy * W + gx) * kC + q * 8]);
-        *reinterpret_cast<uint4 *>(sX + pix * 64 + q * 16) = v;
-    }
-    __syncthreads();
-    // im2col: pixel m = tid (row m / 16, column m % 16) of every tap
-    {
-        const int r = tid >> 4, c = tid & 15;
-        uint8_t *dst0 = sA + (tid >> 3) * 512 + (tid & 7) * 16;
-#pragma unroll
-        for (int tap = 0; tap < 9; ++tap) {
-            const uint8_t *src = sX + ((r + tap / 3) * (kTW + 2) + c + tap % 3) * 64;
-            uint8_t *dst = dst0 + tap * (128 * kC * 2);
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                *reinterpret_cast<uint4 *>(dst + q * 128) = *reinterpret_cast<const uint4 *>(src + q * 16);
-        }
+        *reinterpret_cast<uint4 *>(sX + cx * kTcCol + q * (kTcCol / 4) + r * 16) = v;
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -252,12 +246,13 @@ conv32_tc05_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__r
     if (tid == 0) {
         // instruction descriptor: D FP32, A and B BF16, both K-major, N = 32, M = 128
         const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kC >> 3) << 17) | ((128u >> 4) << 24);
-        const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+        const uint32_t a0 = smem_u32(sX), b0 = smem_u32(sB);
 #pragma unroll 1
         for (int tap = 0; tap < 9; ++tap)
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
-                const uint64_t ad = umma_desc(a0 + tap * (128 * kC * 2) + j * 256, 128, 512);
+                const int dy = tap / 3, dx = tap % 3;
+                const uint64_t ad = umma_desc(a0 + dx * kTcCol + dy * 16 + j * 2 * (kTcCol / 4), kTcCol / 4, kTcCol);
                 const uint64_t bd = umma_desc(b0 + (tap * 4 + j * 2) * 512, 512, 128);
                 const uint32_t acc = (tap | j) ? 1u : 0u;
                 asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -290,7 +285,8 @@ conv32_tc05_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__r
                        "=f"(v[26]), "=f"(v[27]), "=f"(v[28]), "=f"(v[29]), "=f"(v[30]), "=f"(v[31])
                      : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        const int gy = y0 + (tid >> 4), gx = x0 + (tid & 15);
+        const int m = tid;                                     // TMEM lane = pixel m = 8 x + y
+        const int gy = y0 + (m & 7), gx = x0 + (m >> 3);
         if (gy < H && gx < W) {
             const size_t pix = ((size_t)b * H + gy) * W + gx;
             __align__(16) __nv_bfloat162 o[kC / 2];
@@ -315,6 +311,42 @@ conv32_tc05_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__r
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem));
+    }
+}
+
+// 32 -> 2 layer (linear): thread per pixel, each tap's 32 channels read as
+// four 16-byte vectors; output fp32 [B][H][W][2]
+__global__ void conv_out_v_kernel(const __nv_bfloat16 *__restrict__ X, const float *__restrict__ Wf,
+                                  float *__restrict__ Y, int B, int H, int W)
+{
+    __shared__ float w[9 * 2 * kC];
+    for (int e = threadIdx.x; e < 9 * 2 * kC; e += blockDim.x) w[e] = Wf[e];
+    __syncthreads();
+    const int64_t tot = (int64_t)B * H * W;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < tot; p += (int64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(p % W), y = (int)((p / W) % H);
+        const int64_t base = p - (int64_t)y * W - x;
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap) {
+            const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+            if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
+            const uint4 *xr = reinterpret_cast<const uint4 *>(&X[(base + (int64_t)yy * W + xx) * kC]);
+            const float *w0 = &w[(tap * 2 + 0) * kC], *w1 = &w[(tap * 2 + 1) * kC];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint4 u = __ldg(xr + q);
+                const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const float2 v = __bfloat1622float2(h[c]);
+                    const int ch = q * 8 + 2 * c;
+                    s0 = fmaf(v.x, w0[ch], fmaf(v.y, w0[ch + 1], s0));
+                    s1 = fmaf(v.x, w1[ch], fmaf(v.y, w1[ch + 1], s1));
+                }
+            }
+        }
+        *reinterpret_cast<float2 *>(&Y[p * 2]) = make_float2(s0, s1);
     }
 }
 
@@ -352,35 +384,6 @@ __global__ void conv_in_kernel(const float *__restrict__ X, const float *__restr
         uint4 *dst = reinterpret_cast<uint4 *>(&Y[p * kC]);
 #pragma unroll
         for (int q = 0; q < 4; ++q) dst[q] = reinterpret_cast<const uint4 *>(out)[q];
-    }
-}
-
-// 32 -> 2 layer (linear): thread per pixel; output fp32 [B][H][W][2]
-__global__ void conv_out_kernel(const __nv_bfloat16 *__restrict__ X, const float *__restrict__ Wf,
-                                float *__restrict__ Y, int B, int H, int W)
-{
-    __shared__ float w[9 * 2 * kC];
-    for (int e = threadIdx.x; e < 9 * 2 * kC; e += blockDim.x) w[e] = Wf[e];
-    __syncthreads();
-    const int64_t tot = (int64_t)B * H * W;
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < tot; p += (int64_t)gridDim.x * blockDim.x) {
-        const int x = (int)(p % W), y = (int)((p / W) % H);
-        const int64_t base = p - (int64_t)y * W - x;
-        float s0 = 0.f, s1 = 0.f;
-#pragma unroll
-        for (int tap = 0; tap < 9; ++tap) {
-            const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
-            if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
-            const __nv_bfloat162 *xr = reinterpret_cast<const __nv_bfloat162 *>(&X[(base + (int64_t)yy * W + xx) * kC]);
-            const float *w0 = &w[(tap * 2 + 0) * kC], *w1 = &w[(tap * 2 + 1) * kC];
-#pragma unroll
-            for (int c = 0; c < kC / 2; ++c) {
-                const float2 v = __bfloat1622float2(xr[c]);
-                s0 = fmaf(v.x, w0[2 * c], fmaf(v.y, w0[2 * c + 1], s0));
-                s1 = fmaf(v.x, w1[2 * c], fmaf(v.y, w1[2 * c + 1], s1));
-            }
-        }
-        *reinterpret_cast<float2 *>(&Y[p * 2]) = make_float2(s0, s1);
     }
 }
 
@@ -589,7 +592,7 @@ cgs_status net_forward_dev(cgs_net *n, int B, int H, int W, cudaStream_t st)
     CGS_LAUNCH_CHECK();
     for (int l = 1; l <= 3; ++l)
         CGS_TRY(conv32<0>(n, n->act[l - 1], n->wb + (l - 1) * 9 * kC * kC, n->act[l], nullptr, B, H, W, st));
-    conv_out_kernel<<<blocks_for(P), 256, 0, st>>>(n->act[3], n->w + layer_offset(4), n->y5, B, H, W);
+    conv_out_v_kernel<<<blocks_for(P), 256, 0, st>>>(n->act[3], n->w + layer_offset(4), n->y5, B, H, W);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }
