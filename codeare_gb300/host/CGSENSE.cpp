@@ -63,6 +63,7 @@ public:
         if (const char *a = Configurable::Attribute("alpha")) m_alpha = std::atof(a);
         if (const char *a = Configurable::Attribute("mode")) m_mode = a;
         if (const char *a = Configurable::Attribute("weighted")) m_weighted = std::atoi(a);
+        if (const char *a = Configurable::Attribute("toeplitz")) m_toeplitz = std::atoi(a);
         if (const char *a = Configurable::Attribute("seed")) m_seed = (unsigned)std::atol(a);
         std::printf("... done.\n\n");
         return codeare::OK;
@@ -85,6 +86,7 @@ public:
             if (m_alpha != 1.0) cgp["alpha"] = m_alpha;
             cgp["mode"] = m_mode;
             cgp["weighted"] = m_weighted;
+            cgp["toeplitz"] = m_toeplitz;
             m_ncs = NCSENSE<cxfl>(cgp);
             m_ncs.KSpace(Get<float>("kspace"));
             m_ncs.Weights(Get<float>("weights"));
@@ -138,7 +140,7 @@ private:
     float m_noise = 0.f, m_lambda = 1.0e-6f, m_fteps = 1.0e-3f, m_cgeps = 1.0e-7f;
     double m_alpha = 1.0;
     std::string m_mode = "codeare";
-    int m_weighted = 1;
+    int m_weighted = 1, m_toeplitz = 0;
     unsigned m_seed = 0;
 };
 

@@ -6,7 +6,10 @@
 // alpha = 1, m = 1, cgiter = 0, cgeps = 1e-6, lambda = 1e-6, verbose.  New
 // optional keys: "mode" ("codeare" = the reference's CGLS over its CGNR-based
 // E^H, the default; "standard" = CG on E^H W E + lambda with the true adjoint)
-// and "weighted" (standard mode: use the density weights, default 1).
+// "weighted" (standard mode: use the density weights, default 1) and
+// "toeplitz" (1: every CG step's normal operator through the Toeplitz kernel
+// of the trajectory; codeare mode then runs its inner CGNR in image space and
+// needs alpha >= 2 and m >= 4; default 0).
 //
 //   Trafo / operator*   E: y_c = NFFT(S_c . x)            (NCSENSE.hpp:310-348)
 //   operator/           codeare's E^H (mode codeare) or E^H W (standard)
@@ -61,6 +64,7 @@ public:
             else throw std::invalid_argument("NCSENSE: mode must be codeare or standard");
         }
         m_weighted = try_to_fetch<int>(params, "weighted", 1);
+        m_toeplitz = try_to_fetch<int>(params, "toeplitz", 0);
         m_cart = try_to_fetch<bool>(params, "3rd_dim_cart", false);
         m_dim4 = std::max<size_t>(1, try_to_fetch<size_t>(params, "dim4", 1));
         m_dim5 = std::max<size_t>(1, try_to_fetch<size_t>(params, "dim5", 1));
@@ -80,7 +84,8 @@ public:
         m_ftiter = o.m_ftiter; m_fteps = o.m_fteps; m_alpha = o.m_alpha; m_m = o.m_m; m_nk = o.m_nk;
         m_dim4 = o.m_dim4; m_dim5 = o.m_dim5; m_cart = o.m_cart;
         m_cgiter = o.m_cgiter; m_cgeps = o.m_cgeps; m_lambda = o.m_lambda; m_verbose = o.m_verbose;
-        m_mode = o.m_mode; m_weighted = o.m_weighted; m_have_k = o.m_have_k; m_have_w = o.m_have_w;
+        m_mode = o.m_mode; m_weighted = o.m_weighted; m_toeplitz = o.m_toeplitz; m_have_k = o.m_have_k;
+        m_have_w = o.m_have_w;
         if (o.m_plan) {
             plan();
             if (m_have_k) KSpace(m_k);
@@ -180,7 +185,7 @@ public:
         Matrix<T> out(image_dims());
         cgs_solve_opts o{};
         o.mode = m_mode; o.cgiter = (int)m_cgiter; o.cgeps = m_cgeps; o.lambda = m_lambda;
-        o.ftiter = (int)m_ftiter; o.fteps = m_fteps; o.weighted = m_weighted;
+        o.ftiter = (int)m_ftiter; o.fteps = m_fteps; o.weighted = m_weighted; o.toeplitz = m_toeplitz;
         cgs_solve_report r{};
         cgs_status s = cgs_solve(m_plan, reinterpret_cast<const float *>(in.Ptr()), reinterpret_cast<float *>(out.Ptr()),
                                  &o, &r, nullptr);
@@ -301,7 +306,7 @@ private:
         m_dim4 = o.m_dim4; m_dim5 = o.m_dim5; m_cart = o.m_cart; m_ncart = o.m_ncart;
         m_cgiter = o.m_cgiter; m_fteps = o.m_fteps; m_alpha = o.m_alpha; m_cgeps = o.m_cgeps;
         m_lambda = o.m_lambda; m_verbose = o.m_verbose; m_have_k = o.m_have_k; m_have_w = o.m_have_w;
-        m_mode = o.m_mode; m_weighted = o.m_weighted; m_last = o.m_last;
+        m_mode = o.m_mode; m_weighted = o.m_weighted; m_toeplitz = o.m_toeplitz; m_last = o.m_last;
     }
 
     cgs_plan *m_plan = nullptr;
@@ -313,6 +318,6 @@ private:
     double m_fteps = 1e-3, m_alpha = 1.0;
     RT m_cgeps = 1.0e-6f, m_lambda = 1.0e-6f;
     bool m_verbose = false, m_have_k = false, m_have_w = false;
-    int m_mode = CGS_MODE_CODEARE, m_weighted = 1;
+    int m_mode = CGS_MODE_CODEARE, m_weighted = 1, m_toeplitz = 0;
     mutable cgs_solve_report m_last{};
 };

@@ -129,7 +129,10 @@ typedef struct {
     int toeplitz;      /* standard mode: apply E^H W E by Toeplitz embedding
                           (2N-grid FFT convolution with the weighted point-spread
                           function, computed once per trajectory and weights);
-                          no reference counterpart                            */
+                          codeare mode: run each CG step's inner CGNR in image
+                          space on the same kernel (same steps and early exits
+                          as with the NFFT pair; needs alpha >= 2 and m >= 4,
+                          else CGS_ERR_BAD_ARG); no reference counterpart     */
     int jacobi;        /* cgs_solve_fcg preconditioner kind (no reference
                           counterpart): 0 none; 1 the exact diagonal D of
                           E^H W E + lambda (D^-1 r); 2 the circulant C (see

@@ -47,6 +47,22 @@ def test_plugin_matches_reference_semantics(gpu, oracle, tmp_path, alpha, m):
     assert rel(img, xo) < TOL_IMG, log
 
 
+def test_plugin_toeplitz_key(gpu, oracle, tmp_path):
+    """toeplitz="1": codeare's CGLS with each step's inner CGNR run in image
+    space on the Toeplitz kernel; same result as the NFFT pair (sigma 2, m 4)."""
+    from codeare_gb300 import synth
+    cfg = synth.small_config(N=32, nc=4, nspokes=32, nsamp=64, alpha=2.0, m=4)
+    k, w, S = cfg["k"], cfg["w"], cfg["sens"]
+    s = oracle.Sense(S, k, w=w, m=4, alpha=2.0)
+    y = synth.add_noise(s.trafo(cfg["image"]), 1e-3, seed=4)
+    xo, _ = s.cgls_codeare(y, cgiter=10, cgeps=1e-6, lam=5e-2, ftiter=3, fteps=1e-3)
+    mats = {"sensitivities": S, "kspace": k, "weights": w, "signals": y.astype(np.complex64)}
+    attrs = {"nk": k.shape[0], "lambda": 0.05, "m": 4, "alpha": 2.0, "cgeps": 1e-6, "cgmaxit": 10,
+             "ftmaxit": 3, "fteps": 0.001, "noise": 0, "testcase": 0, "toeplitz": 1}
+    img, log = run_plugin(tmp_path, mats, attrs)
+    assert rel(img, xo) < TOL_IMG, log
+
+
 def test_plugin_testcase_mode(gpu, oracle, tmp_path):
     """testcase=1: the plugin encodes its own Shepp-Logan phantom (CGSENSE.cpp:171-172)."""
     from codeare_gb300 import synth
