@@ -18,6 +18,7 @@
 // convolution is the usual cross-correlation y[p][co] = sum x[p+off][ci] w.
 // No reference counterpart (the reference has no learned component).
 #include "cgs_internal.cuh"
+#include "cgs_tc05.cuh"
 
 #include <atomic>
 
@@ -187,18 +188,7 @@ constexpr int kTcHalo = (kTW + 2) * kTcCol;
 constexpr int kTcSmem = kTcB + kTcHalo + 16;
 constexpr uint32_t kTcWaitLimit = 1u << 22;
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// shared-memory matrix descriptor: start, leading / stride byte offsets
-// (16-byte units), descriptor version 1, no swizzle
-__device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
-{
-    uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
-    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t)1 << 46;
-    return d;
-}
+using tc05::smem_u32;
 
 template <int EPI>
 __global__ void __launch_bounds__(128)
@@ -216,11 +206,8 @@ conv32_tc05_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__r
     const int y0 = blockIdx.y * kTH, x0 = blockIdx.x * kTW;
     const __nv_bfloat16 *Xb = X + (size_t)b * H * W * kC;
 
-    if (warp == 0) {   // 32 TMEM columns: the 128 x 32 FP32 accumulator
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(smem_u32(tslot)));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
-    if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
+    if (warp == 0) tc05::alloc<32>(tslot);   // 32 TMEM columns: the 128 x 32 FP32 accumulator
+    if (tid == 0) tc05::mbar_init(mbar, 1);
     // weights: (tap, co, 8-channel chunk) -> core (co / 8, (32 tap + ci) / 8)
     for (int e = tid; e < 9 * kC * 4; e += 128) {
         const int q = e & 3, co = (e >> 2) % kC, tap = (e >> 2) / kC;
@@ -238,53 +225,36 @@ conv32_tc05_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__r
             v = *reinterpret_cast<const uint4 *>(&Xb[((size_t)gy * W + gx) * kC + q * 8]);
         *reinterpret_cast<uint4 *>(sX + cx * kTcCol + q * (kTcCol / 4) + r * 16) = v;
     }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    tc05::fence_proxy_async();
+    tc05::fence_before();
     __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tc05::fence_after();
     const uint32_t tmem = *tslot;
     if (tid == 0) {
-        // instruction descriptor: D FP32, A and B BF16, both K-major, N = 32, M = 128
-        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kC >> 3) << 17) | ((128u >> 4) << 24);
+        // D FP32, A and B BF16, both K-major, N = 32, M = 128
+        constexpr uint32_t idesc = tc05::idesc_bf16(128, kC);
         const uint32_t a0 = smem_u32(sX), b0 = smem_u32(sB);
 #pragma unroll 1
         for (int tap = 0; tap < 9; ++tap)
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
                 const int dy = tap / 3, dx = tap % 3;
-                const uint64_t ad = umma_desc(a0 + dx * kTcCol + dy * 16 + j * 2 * (kTcCol / 4), kTcCol / 4, kTcCol);
-                const uint64_t bd = umma_desc(b0 + (tap * 4 + j * 2) * 512, 512, 128);
-                const uint32_t acc = (tap | j) ? 1u : 0u;
-                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                             ::"r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+                const uint64_t ad = tc05::desc(a0 + dx * kTcCol + dy * 16 + j * 2 * (kTcCol / 4), kTcCol / 4, kTcCol);
+                const uint64_t bd = tc05::desc(b0 + (tap * 4 + j * 2) * 512, 512, 128);
+                tc05::mma_bf16(tmem, ad, bd, idesc, (tap | j) ? 1u : 0u);
             }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                     ::"r"(smem_u32(mbar)) : "memory");
+        tc05::commit(mbar);
     }
-    // bounded wait for the MMAs
-    uint32_t done = 0;
-    for (uint32_t it = 0; it < kTcWaitLimit && !done; ++it)
-        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
-                     "selp.u32 %0, 1, 0, p;\n\t}" : "=r"(done) : "r"(smem_u32(mbar)) : "memory");
-    // tcgen05.ld is warp-collective: the whole warp reads, or none of it does
-    done = __all_sync(0xffffffffu, done);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // bounded wait for the MMAs; tcgen05.ld is warp-collective: the whole
+    // warp reads, or none of it does
+    const uint32_t done = __all_sync(0xffffffffu, tc05::mbar_wait(mbar, 0, kTcWaitLimit) ? 1u : 0u);
+    tc05::fence_after();
     if (!done) {
         if (lane == 0) atomicOr(err, 1);
     } else {
         float v[32];
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-        asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                     "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                     "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                     : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]),
-                       "=f"(v[7]), "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]),
-                       "=f"(v[14]), "=f"(v[15]), "=f"(v[16]), "=f"(v[17]), "=f"(v[18]), "=f"(v[19]),
-                       "=f"(v[20]), "=f"(v[21]), "=f"(v[22]), "=f"(v[23]), "=f"(v[24]), "=f"(v[25]),
-                       "=f"(v[26]), "=f"(v[27]), "=f"(v[28]), "=f"(v[29]), "=f"(v[30]), "=f"(v[31])
-                     : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        tc05::ld32(tmem + ((uint32_t)(warp * 32) << 16), v);
+        tc05::wait_ld();
         const int m = tid;                                     // TMEM lane = pixel m = 8 x + y
         const int gy = y0 + (m & 7), gx = x0 + (m >> 3);
         if (gy < H && gx < W) {
@@ -306,11 +276,11 @@ conv32_tc05_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__r
             for (int q = 0; q < 4; ++q) dst[q] = reinterpret_cast<const uint4 *>(o)[q];
         }
     }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    tc05::fence_before();
     __syncthreads();
     if (warp == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem));
+        tc05::fence_after();
+        tc05::dealloc<32>(tmem);
     }
 }
 

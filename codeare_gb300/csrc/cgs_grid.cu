@@ -12,6 +12,7 @@
 // work item, so global atomics touch each tile point once instead of once per
 // node and tap.  Grid and k-space data keep the coil index innermost.
 #include "cgs_internal.cuh"
+#include "cgs_tc05.cuh"
 
 #include <algorithm>
 
@@ -685,6 +686,362 @@ spread_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ Pa
                 if (c < ccn) dst[c] = make_float2(acc[mt][t][2 * h], acc[mt][t][2 * h + 1]);
             }
         }
+}
+
+// ---------------------------------------------------------------------------
+// 2-D spreading on the 5th-generation tensor cores (tcgen05), output-
+// stationary over 8 x 16 grid patches (spread_block 64).  A 256-thread CTA
+// owns one work item (a patch, or a slice of a crowded patch's node list) and
+// NCOL / 2 coils: D[128 points][NCOL columns] = W[128][K entries] .
+// V[K entries][NCOL], columns = (coil, re/im), accumulated in FP32 in NCOL
+// tensor-memory columns.  The entries stream in stages of kSpTcKS:
+//   * once per trajectory, spread_tc_weights_kernel stores every stage's
+//     patch weights (8 row and 16 column window values per entry, entries
+//     innermost) and node indices as one contiguous block, so a stage needs
+//     no per-node lookups;
+//   * cp.async brings a stage's weight block three stages ahead and its
+//     k-space values and density weights two stages ahead (rings of four and
+//     three slots, one commit group per kind and stage);
+//   * A = W, TF32-split into hi and lo (tf32_split2), lives in tensor memory
+//     (row m in lane m, entries along the columns): thread m % 128 of warps
+//     m / 32 and m / 32 + 4 (point m = 16 r + c of the patch) multiplies its
+//     row and column weights for 8 of the stage's 16 entries and stores them
+//     with tcgen05.st;
+//   * B = V^T (the values times the density weights), split the same way:
+//     a thread per (coil, 4 entries), stored K-major in shared memory in the
+//     canonical no-swizzle layout (core matrices of 8 rows x 4 values);
+//   * both in one of two stage buffers; a ninth warp waits for a buffer's
+//     "full" mbarrier, issues per K = 8 step lo.hi + hi.lo + hi.hi as three
+//     tcgen05.mma.kind::tf32 and commits them to the buffer's "empty"
+//     mbarrier, while the builders fill the other buffer.
+// Before a buffer is rebuilt its mbarrier is waited on, with a bounded wait:
+// past the limit the CTA sets *ps.err, stores nothing and still frees its
+// tensor memory.  The epilogue reads the accumulator with tcgen05.ld (warps w
+// and w + 4: points 32 (w % 4) .., the lower and the upper half of the
+// columns) and stores each point's coils to the grid, or to the work item's
+// partial slot, reduced in slot order by patch_reduce_kernel as for the other
+// kernels.  Entries past the list end and coils past the chunk are zero in A
+// and B.
+// ---------------------------------------------------------------------------
+constexpr int kSpTcPH = 8, kSpTcPW = 16;     // patch rows and columns: 128 points = the MMA's M
+constexpr int kSpTcKS = 16;                  // entries per stage: two K = 8 steps
+constexpr int kSpTcWPE = kSpTcPH + kSpTcPW;  // patch weights per entry
+constexpr int kSpTcWS = kSpTcKS + 4;         // weight row stride in shared memory (floats), bank-spread
+constexpr int kSpTcThreads = 256;
+constexpr uint32_t kSpTcWait = 1u << 22;     // mbarrier polls before giving up
+
+template <int NCOL> struct SpreadTc {
+    static constexpr int A = 128 * kSpTcKS * 4;        // one of hi / lo
+    static constexpr int B = NCOL * kSpTcKS * 4;
+    static constexpr int LBO_A = 16 * 128;             // next 4 entries: past the 16 point groups
+    static constexpr int LBO_B = (NCOL / 8) * 128;     // next 4 entries: past the NCOL / 8 column groups
+    static constexpr int OPER = 2 * B;                 // B hi, lo (A lives in tensor memory)
+    static constexpr int WSLOT = kSpTcWPE * kSpTcWS * 4 + kSpTcKS * 4;   // weights, node indices
+    static constexpr int VSLOT = kSpTcKS * NCOL * 4 + kSpTcKS * 4;       // values, density weights
+    static constexpr int NW = 4, NV = 3;                                // ring slots
+    static constexpr int SMEM = 2 * OPER + NW * WSLOT + NV * VSLOT + 48;  // + four mbarriers, TMEM slot, flag
+    // tensor memory: the accumulator in columns 0 .. NCOL - 1, then per stage
+    // buffer 16 hi and 16 lo columns of A
+    static constexpr int ACOL = 64;
+    static constexpr int TCOLS = 128;
+};
+
+// x * y on both FP32 lanes (the rounding of two FP32 multiplies)
+__device__ __forceinline__ float2 fmul2(float2 x, float2 y) { return ffma2(x, y, make_float2(0.f, 0.f)); }
+
+// tf32_split on two values; the remainders x - hi with one paired FMA
+__device__ __forceinline__ void tf32_split2(float2 x, uint32_t &h0, uint32_t &h1, uint32_t &l0, uint32_t &l1)
+{
+    h0 = (__float_as_uint(x.x) + 0x1000u) & 0xffffe000u;
+    h1 = (__float_as_uint(x.y) + 0x1000u) & 0xffffe000u;
+    const float2 lo = ffma2(make_float2(-1.f, -1.f), make_float2(__uint_as_float(h0), __uint_as_float(h1)), x);
+    l0 = __float_as_uint(lo.x);
+    l1 = __float_as_uint(lo.y);
+}
+
+// the stage blocks of one work item per CTA: patch weights [24][16] and node
+// indices [16] of entries j * 16 .. j * 16 + 15 of the item's list
+__global__ void spread_tc_weights_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
+                                         float *__restrict__ pw16, int *__restrict__ ps16)
+{
+    const int4 wk = ps.work[blockIdx.x];
+    const int base = ps.pstage[blockIdx.x];
+    const int nst = (wk.z + kSpTcKS - 1) / kSpTcKS;
+    const int n0 = g.n[0], n1 = g.n[1], taps = 2 * g.m + 2;
+    const bool wide = (n0 >= taps) && (n1 >= taps);
+    const int py0 = (wk.x / ps.npx) * kSpTcPH, px0 = (wk.x % ps.npx) * kSpTcPW;
+    auto wgt = [&](const float *W, int q, int n) -> float {
+        if (q < 0) q += n;
+        if (wide) return q < taps ? W[q] : 0.f;
+        float w = 0.f;
+        for (int r = q; r < taps; r += n) w += W[r];
+        return w;
+    };
+    constexpr int PER = kSpTcKS * (kSpTcWPE + 1);
+    for (int idx = threadIdx.x; idx < nst * PER; idx += blockDim.x) {
+        const int j = idx / PER, rem = idx % PER, q = rem / kSpTcKS, e = rem % kSpTcKS;
+        const int ei = j * kSpTcKS + e;
+        const int s = ei < wk.z ? ps.entries[wk.y + ei] : -1;
+        const int64_t blk = (int64_t)base + j;
+        if (q == kSpTcWPE) {
+            ps16[blk * kSpTcKS + e] = s;
+            continue;
+        }
+        float w = 0.f;
+        if (s >= 0) {
+            const int2 u = ps.nodeU[s];
+            const float *W = ps.nodeW + (size_t)s * 2 * taps;
+            if (q < kSpTcPH) {
+                if (py0 + q < n0) w = wgt(W, py0 + q - u.x, n0);
+            } else if (px0 + q - kSpTcPH < n1) {
+                w = wgt(W + taps, px0 + q - kSpTcPH - u.y, n1);
+            }
+        }
+        pw16[(blk * kSpTcWPE + q) * kSpTcKS + e] = w;
+    }
+}
+
+// named barrier 1 over the 256 builder threads (warps 0..7); the second form
+// also returns the OR of `v` over them, the same value in every thread
+__device__ __forceinline__ void builders_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kSpTcThreads) : "memory"); }
+__device__ __forceinline__ bool builders_sync_or(bool v)
+{
+    uint32_t r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 1, %2, p;\n\t"
+                 "selp.u32 %0, 1, 0, q;\n\t}" : "=r"(r) : "r"((uint32_t)v), "n"(kSpTcThreads) : "memory");
+    return r != 0;
+}
+// mbarrier arrive (one count), release at CTA scope
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc05::smem_u32(bar)) : "memory");
+}
+
+template <int NCOL>
+__global__ void __launch_bounds__(kSpTcThreads + 32, 4)
+spread_tc05_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
+                   const float2 *__restrict__ ks, const float *__restrict__ dens, int weighted,
+                   float2 *__restrict__ grid)
+{
+    using S = SpreadTc<NCOL>;
+    constexpr int CC = NCOL / 2;
+    extern __shared__ __align__(128) uint8_t tsm[];
+    uint8_t *wring = tsm + 2 * S::OPER;
+    uint8_t *vring = wring + S::NW * S::WSLOT;
+    uint64_t *full = reinterpret_cast<uint64_t *>(vring + S::NV * S::VSLOT);   // operands of buffer b built
+    uint64_t *empty = full + 2;                                                  // MMAs of buffer b done
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(empty + 2);
+    volatile int *sfail = reinterpret_cast<volatile int *>(tslot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int4 wk = ps.work[blockIdx.x];
+    const int64_t base = ps.pstage[blockIdx.x];
+    const int c0 = blockIdx.y * CC;
+    const int ccn = min(CC, g.nc - c0);
+    const int n0 = g.n[0], n1 = g.n[1];
+    const bool v16 = (g.nc & 1) == 0;
+    const int py0 = (wk.x / ps.npx) * kSpTcPH, px0 = (wk.x % ps.npx) * kSpTcPW;
+    const int nst = (wk.z + kSpTcKS - 1) / kSpTcKS;
+
+    auto wslot = [&](int j) { return reinterpret_cast<float *>(wring + (j % S::NW) * S::WSLOT); };
+    auto vslot = [&](int j) { return reinterpret_cast<float *>(vring + (j % S::NV) * S::VSLOT); };
+    // stage j's weight block (24 rows of 16 entries -> rows kSpTcWS apart) and
+    // node indices: threads 0..99
+    auto fetch_w = [&](int j) {
+        float *d = wslot(j);
+        const int64_t blk = base + j;
+        if (tid < kSpTcWPE * 4) {
+            const int q = tid >> 2, k = tid & 3;
+            cp_async16(d + q * kSpTcWS + 4 * k, ps.pw16 + (blk * kSpTcWPE + q) * kSpTcKS + 4 * k);
+        } else if (tid < kSpTcWPE * 4 + 4) {
+            const int k = tid - kSpTcWPE * 4;
+            cp_async16(d + kSpTcWPE * kSpTcWS + 4 * k, ps.ps16 + blk * kSpTcKS + 4 * k);
+        }
+    };
+    // stage j's values and density weights (its node indices are in
+    // wslot(j)): threads 0..127
+    auto fetch_v = [&](int j) {
+        const int *sidx = reinterpret_cast<const int *>(wslot(j) + kSpTcWPE * kSpTcWS);
+        float *sv = vslot(j), *sd = sv + kSpTcKS * NCOL;
+        if (tid < kSpTcKS) {
+            const int s = sidx[tid];
+            if (s >= 0 && weighted) cp_async4(&sd[tid], &dens[s]);
+            else sd[tid] = 1.f;
+        }
+        if (v16) {                                                  // two coils per 16-byte piece
+            for (int it = tid; it < kSpTcKS * (CC / 2); it += 128) {
+                const int e = it / (CC / 2), q = it % (CC / 2);
+                const int s = sidx[e];
+                float *d = sv + e * NCOL + 4 * q;
+                if (s >= 0 && 2 * q < ccn) cp_async16(d, ks + (size_t)s * g.nc + c0 + 2 * q);
+                else *reinterpret_cast<float4 *>(d) = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        } else {
+            for (int it = tid; it < kSpTcKS * CC; it += 128) {
+                const int e = it / CC, q = it % CC;
+                const int s = sidx[e];
+                float *d = sv + e * NCOL + 2 * q;
+                if (s >= 0 && q < ccn) cp_async8(d, ks + (size_t)s * g.nc + c0 + q);
+                else *reinterpret_cast<float2 *>(d) = make_float2(0.f, 0.f);
+            }
+        }
+    };
+
+    if (warp == kSpTcThreads / 32) tc05::alloc<S::TCOLS>(tslot);
+    if (tid == 0) {
+        for (int k = 0; k < 2; ++k) {
+            tc05::mbar_init(&full[k], 1);
+            tc05::mbar_init(&empty[k], 1);
+        }
+        tc05::fence_mbar_init();
+        *sfail = 0;
+    }
+    tc05::fence_before();
+    __syncthreads();
+    tc05::fence_after();
+    const uint32_t tmem = *tslot;
+
+    if (warp == kSpTcThreads / 32) {
+        // the MMA warp: one thread issues each stage once its operands are built
+        if ((tid & 31) == 0) {
+            constexpr uint32_t idesc = tc05::idesc_tf32(128, NCOL);
+            for (int i = 0; i < nst; ++i) {
+                const int b = i & 1;
+                if (!tc05::mbar_wait(&full[b], (i >> 1) & 1, kSpTcWait)) { *sfail = 1; break; }
+                tc05::fence_after();
+                const uint32_t bh = tc05::smem_u32(tsm + b * S::OPER), bl = bh + S::B;
+                const uint32_t ah = tmem + S::ACOL + 32 * b, al = ah + 16;
+#pragma unroll
+                for (int kk = 0; kk < kSpTcKS / 8; ++kk) {
+                    const uint32_t ob = kk * 2 * S::LBO_B;
+                    const uint64_t dbh = tc05::desc(bh + ob, S::LBO_B, 128), dbl = tc05::desc(bl + ob, S::LBO_B, 128);
+                    tc05::mma_tf32_ta(tmem, al + 8 * kk, dbh, idesc, (i | kk) ? 1u : 0u);
+                    tc05::mma_tf32_ta(tmem, ah + 8 * kk, dbl, idesc, 1u);
+                    tc05::mma_tf32_ta(tmem, ah + 8 * kk, dbh, idesc, 1u);
+                }
+                tc05::commit(&empty[b]);
+            }
+        }
+        __syncwarp();
+    } else {
+        // the builders: prologue, then per stage fetch ahead, build, publish
+        for (int j = 0; j < 3; ++j)
+            if (j < nst) fetch_w(j);
+        cp_async_commit();
+        cp_async_wait<0>();
+        builders_sync();
+        if (nst > 0 && tid < 128) fetch_v(0);
+        cp_async_commit();
+        if (nst > 1 && tid < 128) fetch_v(1);
+        cp_async_commit();
+        cp_async_wait<1>();
+        builders_sync();
+        bool lf = false;      // this thread's bounded wait ran out
+        bool failed = false;  // some builder's did (the same in every builder)
+        for (int i = 0; i < nst; ++i) {
+            const int b = i & 1;
+            uint8_t *bH = tsm + b * S::OPER, *bL = bH + S::B;
+            // the MMAs of stage i - 2 read this operand buffer
+            if (i >= 2 && !tc05::mbar_wait(&empty[b], ((i - 2) >> 1) & 1, kSpTcWait)) lf = true;
+            if (i + 3 < nst) fetch_w(i + 3);
+            cp_async_commit();
+            if (i + 2 < nst && tid < 128) fetch_v(i + 2);
+            cp_async_commit();
+            if (tid >= 128) {
+                // B: the values times the density weights, a thread per (coil, 4 entries)
+                const float *sv = vslot(i), *sd = sv + kSpTcKS * NCOL;
+                for (int it = tid - 128; it < CC * (kSpTcKS / 4); it += 128) {
+                    const int cc = it % CC, kg = it / CC;
+                    uint32_t hr[4], lr[4], hi4[4], li4[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const float d = sd[4 * kg + j];
+                        const float2 v = fmul2(*reinterpret_cast<const float2 *>(sv + (4 * kg + j) * NCOL + 2 * cc),
+                                               make_float2(d, d));
+                        tf32_split2(v, hr[j], hi4[j], lr[j], li4[j]);
+                    }
+                    const int nr = 2 * cc, ni = 2 * cc + 1;
+                    const int offr = kg * S::LBO_B + (nr >> 3) * 128 + (nr & 7) * 16;
+                    const int offi = kg * S::LBO_B + (ni >> 3) * 128 + (ni & 7) * 16;
+                    *reinterpret_cast<uint4 *>(bH + offr) = make_uint4(hr[0], hr[1], hr[2], hr[3]);
+                    *reinterpret_cast<uint4 *>(bL + offr) = make_uint4(lr[0], lr[1], lr[2], lr[3]);
+                    *reinterpret_cast<uint4 *>(bH + offi) = make_uint4(hi4[0], hi4[1], hi4[2], hi4[3]);
+                    *reinterpret_cast<uint4 *>(bL + offi) = make_uint4(li4[0], li4[1], li4[2], li4[3]);
+                }
+            }
+            // A: point m = tid % 128 (row m / 16, column m % 16; tensor-memory
+            // lane m), entries 8 h .. 8 h + 7 for h = tid / 128
+            {
+                const int m = tid & 127, h = tid >> 7;
+                const float *sw = wslot(i);
+                const float4 *wr = reinterpret_cast<const float4 *>(sw + (m >> 4) * kSpTcWS);
+                const float4 *wc = reinterpret_cast<const float4 *>(sw + (kSpTcPH + (m & 15)) * kSpTcWS);
+                uint32_t hv[8], lv[8];
+#pragma unroll
+                for (int t = 0; t < 2; ++t) {
+                    const float4 a = wr[2 * h + t], c = wc[2 * h + t];
+                    tf32_split2(fmul2(make_float2(a.x, a.y), make_float2(c.x, c.y)), hv[4 * t], hv[4 * t + 1],
+                                lv[4 * t], lv[4 * t + 1]);
+                    tf32_split2(fmul2(make_float2(a.z, a.w), make_float2(c.z, c.w)), hv[4 * t + 2], hv[4 * t + 3],
+                                lv[4 * t + 2], lv[4 * t + 3]);
+                }
+                const uint32_t ta = tmem + ((uint32_t)((warp & 3) * 32) << 16) + S::ACOL + 32 * b + 8 * h;
+                tc05::st8(ta, hv);
+                tc05::st8(ta + 16, lv);
+                tc05::wait_st();
+            }
+            // publish: operands to the tensor cores, and the next stage's data
+            // (all groups but the newest landed) to the builders
+            tc05::fence_proxy_async();
+            tc05::fence_before();
+            cp_async_wait<1>();
+            if (builders_sync_or(lf)) { failed = true; break; }
+            if (tid == 0) mbar_arrive(&full[b]);
+        }
+        cp_async_wait<0>();
+        if (nst > 0 && !failed && !tc05::mbar_wait(&empty[(nst - 1) & 1], ((nst - 1) >> 1) & 1, kSpTcWait))
+            failed = true;
+        if (failed) *sfail = 1;
+    }
+    __syncthreads();
+    tc05::fence_after();
+    if (*sfail) {
+        if (tid == 0 && ps.err) *reinterpret_cast<volatile int *>(ps.err) = 1;   // mapped host flag
+    } else if (warp < kSpTcThreads / 32) {
+        constexpr int HC = NCOL / 2;
+        const int m = tid & 127, half = tid >> 7, pr = m >> 4, pc = m & 15;
+        const int py = py0 + pr, px = px0 + pc;
+        float v[HC];
+        if (nst > 0) {
+            const uint32_t ta = tmem + ((uint32_t)((warp & 3) * 32) << 16) + half * HC;
+            if (HC == 32) tc05::ld32(ta, *reinterpret_cast<float(*)[32]>(v));
+            else if (HC == 16) tc05::ld16(ta, *reinterpret_cast<float(*)[16]>(v));
+            else tc05::ld8(ta, *reinterpret_cast<float(*)[8]>(v));
+            tc05::wait_ld();
+        } else {
+#pragma unroll
+            for (int q = 0; q < HC; ++q) v[q] = 0.f;
+        }
+        if (py < n0 && px < n1) {
+            const int cb = half * (CC / 2);               // first coil of this half
+            float2 *dst = (wk.w < 0) ? grid + ((size_t)py * n1 + px) * g.nc + c0 + cb
+                                     : ps.partial + ((size_t)wk.w * (kSpTcPH * kSpTcPW) + m) * g.nc + c0 + cb;
+            if (v16 && ccn == CC) {
+                float4 *d4 = reinterpret_cast<float4 *>(dst);
+#pragma unroll
+                for (int q = 0; q < CC / 4; ++q) d4[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < CC / 2; ++q)
+                    if (cb + q < ccn) dst[q] = make_float2(v[2 * q], v[2 * q + 1]);
+            }
+        }
+    }
+    tc05::fence_before();
+    __syncthreads();
+    if (warp == kSpTcThreads / 32) {
+        tc05::fence_after();
+        tc05::dealloc<S::TCOLS>(tmem);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1937,6 +2294,14 @@ cgs_status launch_spread_patch3(const GridGeom &g, const PatchSet &ps, const flo
     return r;
 }
 
+cgs_status launch_spread_tc_weights(const GridGeom &g, const PatchSet &ps, float *pw16, int *ps16, cudaStream_t st)
+{
+    if (ps.nwork == 0) return CGS_OK;
+    spread_tc_weights_kernel<<<ps.nwork, 256, 0, st>>>(g, ps, pw16, ps16);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
 cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const float2 *ks, const float *dens,
                                int weighted, float2 *grid, cudaStream_t st)
 {
@@ -1973,11 +2338,25 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
         if (taps == 10) CGS_SPT(4, 4, CPLV, 1, 1, 10);          \
         else CGS_SP(4, 4, CPLV, 1, 1);                          \
     } while (0)
-    if ((ps.ph != 4 && !(ps.ph == 8 && ps.blk == 32)) || (ps.pw != 4 && ps.pw != 8)) {
+    if (ps.blk == 64) {   // tcgen05: 8 x 16 patches, 32 coils per CTA (16 or 8 for fewer coils)
+        if (ps.ph != kSpTcPH || ps.pw != kSpTcPW) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
+        const int ncol = g.nc > 8 ? (g.nc > 16 ? 64 : 32) : 16;
+        dim3 grt(ps.nwork, (g.nc + ncol / 2 - 1) / (ncol / 2));
+#define CGS_SPTC(NCV)                                                                                     \
+    do {                                                                                                  \
+        CGS_CUDA(cudaFuncSetAttribute(spread_tc05_kernel<NCV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                      SpreadTc<NCV>::SMEM));                                              \
+        spread_tc05_kernel<NCV><<<grt, kSpTcThreads + 32, SpreadTc<NCV>::SMEM, st>>>(g, ps, ks, dens, weighted, grid); \
+    } while (0)
+        if (!ps.pw16 || !ps.ps16 || !ps.pstage) { set_error("tcgen05 spreading blocks missing"); return CGS_ERR_STATE; }
+        if (ncol == 64) CGS_SPTC(64);
+        else if (ncol == 32) CGS_SPTC(32);
+        else CGS_SPTC(16);
+#undef CGS_SPTC
+    } else if ((ps.ph != 4 && !(ps.ph == 8 && ps.blk == 32)) || (ps.pw != 4 && ps.pw != 8)) {
         set_error("unsupported spreading patch");
         return CGS_ERR_BAD_ARG;
-    }
-    if (ps.blk == 16 || ps.blk == 32) {  // tensor cores: 4 NT coils per warp, 4 x 4 or 8 x 4 patches
+    } else if (ps.blk == 16 || ps.blk == 32) {  // tensor cores: 4 NT coils per warp, 4 x 4 or 8 x 4 patches
         if (ps.pw != 4 || ps.ph != (ps.blk == 32 ? 8 : 4)) { set_error("unsupported spreading patch"); return CGS_ERR_BAD_ARG; }
         const int nt = std::min(8, (2 * g.nc + 7) / 8);
         dim3 grm((ps.nwork + 7) / 8, (g.nc + 4 * nt - 1) / (4 * nt));

@@ -171,7 +171,8 @@ constexpr int kW3 = 32;  // floats per node in the 3-D window table
 // points for one coil.
 struct PatchSet {
     int ph, pw;            // patch rows and columns
-    int blk;               // 1: a point per lane; 2, 4: 2 x 1, 2 x 2 blocks; 8: 4 x 8 patch, one coil group
+    int blk;               // 1: a point per lane; 2, 4: 2 x 1, 2 x 2 blocks; 8: 4 x 8 patch, one coil group;
+                           // 16, 32: mma.sync on 4 x 4, 8 x 4 patches; 64: tcgen05 on 8 x 16 patches
     int npx;               // patches per grid row
     int nwork;             // work items
     const int *entries;    // node (sorted index) lists, patch after patch
@@ -186,6 +187,14 @@ struct PatchSet {
     // slots hold 64 points each
     int pd, npy;
     const int4 *nodeU3;
+    int *err;              // set by a tensor-core kernel whose MMA wait ran out (nullable)
+    // tcgen05 spreading (blk 64): each work item's entries in blocks of 16
+    // from block pstage[item]: the entries' patch weights ([24][16]: 8 row
+    // then 16 column window values, entries innermost) and node indices
+    // ([16], -1 past the list end)
+    const float *pw16;
+    const int *ps16;
+    const int *pstage;
 };
 // node weights and footprint starts from the node records (once per trajectory)
 cgs_status launch_node_weights(const GridGeom &g, const NodeSet &ns, int2 *nodeU, float *nodeW,
@@ -193,6 +202,9 @@ cgs_status launch_node_weights(const GridGeom &g, const NodeSet &ns, int2 *nodeU
 // grid[...][c] = sum_s phi * (w_s if weighted) * ks[s][c]; writes every grid point
 cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const float2 *ks, const float *dens,
                                int weighted, float2 *grid, cudaStream_t st);
+// the tcgen05 spreading's per-block patch weights and node indices (once per
+// trajectory and work list); pw16 / ps16 sized by the blocks of ps.pstage
+cgs_status launch_spread_tc_weights(const GridGeom &g, const PatchSet &ps, float *pw16, int *ps16, cudaStream_t st);
 
 // 3-D node tables: wrapped footprint starts and kW3 window weights per node
 cgs_status launch_node_weights3(const GridGeom &g, const NodeSet &ns, int4 *nodeU3, float *nodeW,

@@ -203,6 +203,9 @@ struct cgs_plan {
     float *nodeW = nullptr;
     int *pentries = nullptr;
     int4 *pwork = nullptr, *pmulti = nullptr;
+    // tcgen05 spreading: per work item, blocks of 16 entries (patch weights, node indices)
+    float *pw16 = nullptr;
+    int *ps16 = nullptr, *pstage = nullptr;
     float2 *ppartial = nullptr;
     int pslots = 1;  // partial slots of the split patches (at least 1)
     PatchSet pset{};
@@ -592,11 +595,14 @@ cgs_status build_ibins(cgs_plan *p, const std::vector<int> &cc, const std::vecto
     return CGS_OK;
 }
 
-// Per 4 x 4 patch (4 x 8 for one coil) of the 2-D grid, the sorted indices of the nodes whose
-// footprint (2m+2 taps per axis, wrapped) covers any point of the patch; work
-// items of at most `chunk` nodes, crowded patches spread over several partial
-// slots; node weights precomputed on the device.  `cc` holds each node's
-// integer grid cell floor(n x) in trajectory order.
+int *tc_flag();
+
+// Per 4 x 4 patch (4 x 8 for one coil, 8 x 4 or 8 x 16 for the tensor-core
+// variants) of the 2-D grid, the sorted indices of the nodes whose footprint
+// (2m+2 taps per axis, wrapped) covers any point of the patch; work items of
+// at most `chunk` nodes, crowded patches spread over several partial slots;
+// node weights precomputed on the device.  `cc` holds each node's integer
+// grid cell floor(n x) in trajectory order.
 cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
 {
     const int n0 = p->n[0], n1 = p->n[1], m = p->m, taps = 2 * m + 2;
@@ -607,10 +613,14 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     // spread_block 16: 4 x 4 patches on the tensor cores (TF32 split, FP32
     // accumulation), the default from 4 coils up
     const int tb = p->tune.spread_block != 0 ? p->tune.spread_block : (p->nc >= 4 ? 16 : 1);
-    // spread_block 32: 8 x 4 patches on the tensor cores (two m-tiles per warp)
-    const int blk = (tb == 16 || tb == 32) ? tb : (p->nc == 1 ? 1 : ((tb == 8 || (p->nc >= 4 && (tb == 4 || tb == 2))) ? tb : 1));
-    const bool tensor = (blk == 16 || blk == 32);
-    const int kPatchH = blk == 32 ? 8 : 4, kPatchW = (!tensor && (p->nc == 1 || blk == 4 || blk == 8)) ? 8 : 4;
+    // spread_block 32: 8 x 4 patches on the tensor cores (two m-tiles per warp);
+    // spread_block 64: 8 x 16 patches on the 5th-generation tensor cores (tcgen05)
+    const int blk = (tb == 16 || tb == 32 || tb == 64)
+                        ? tb
+                        : (p->nc == 1 ? 1 : ((tb == 8 || (p->nc >= 4 && (tb == 4 || tb == 2))) ? tb : 1));
+    const bool tensor = (blk == 16 || blk == 32 || blk == 64);
+    const int kPatchH = (blk == 32 || blk == 64) ? 8 : 4;
+    const int kPatchW = blk == 64 ? 16 : ((!tensor && (p->nc == 1 || blk == 4 || blk == 8)) ? 8 : 4);
     const int npy = (n0 + kPatchH - 1) / kPatchH, npx = (n1 + kPatchW - 1) / kPatchW;
     const int64_t P = (int64_t)npy * npx, M = p->M;
     std::vector<int> perm(M);
@@ -669,9 +679,9 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     // longest lists first, so the long ones do not form the tail
     std::stable_sort(work.begin(), work.end(), [](const int4 &x, const int4 &y) { return x.z > y.z; });
     for (void *b : {(void *)p->nodeU, (void *)p->nodeW, (void *)p->pentries, (void *)p->pwork, (void *)p->pmulti,
-                    (void *)p->ppartial}) dev_free(b);
+                    (void *)p->ppartial, (void *)p->pw16, (void *)p->ps16, (void *)p->pstage}) dev_free(b);
     p->nodeU = nullptr; p->nodeW = nullptr; p->pentries = nullptr; p->pwork = nullptr; p->pmulti = nullptr;
-    p->ppartial = nullptr;
+    p->ppartial = nullptr; p->pw16 = nullptr; p->ps16 = nullptr; p->pstage = nullptr;
     CGS_TRY(dev_alloc(&p->nodeU, M));
     CGS_TRY(dev_alloc(&p->nodeW, (size_t)M * 2 * taps));
     CGS_TRY(dev_alloc(&p->pentries, entries.size()));
@@ -699,6 +709,29 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     ps.partial = p->ppartial;
     ps.nmulti = (int)multi.size();
     ps.multi = p->pmulti;
+    ps.err = tc_flag();
+    ps.pw16 = nullptr; ps.ps16 = nullptr; ps.pstage = nullptr;
+    if (blk == 64) {
+        // the tcgen05 kernel's stage blocks: 16 entries each, per work item in
+        // work order (patch weights computed on the device)
+        std::vector<int> stage(work.size());
+        int64_t blocks = 0;
+        for (size_t t = 0; t < work.size(); ++t) {
+            stage[t] = (int)blocks;
+            blocks += (work[t].z + 15) / 16;
+        }
+        if (blocks > 0x7fffffffLL / 24) { set_error("patch lists too long"); return CGS_ERR_BAD_ARG; }
+        CGS_TRY(dev_alloc(&p->pstage, std::max<size_t>(1, stage.size())));
+        CGS_TRY(dev_alloc(&p->pw16, (size_t)std::max<int64_t>(1, blocks) * 24 * 16));
+        CGS_TRY(dev_alloc(&p->ps16, (size_t)std::max<int64_t>(1, blocks) * 16));
+        if (!stage.empty())
+            CGS_CUDA(cudaMemcpy(p->pstage, stage.data(), sizeof(int) * stage.size(), cudaMemcpyHostToDevice));
+        ps.pstage = p->pstage;
+        CGS_TRY(launch_spread_tc_weights(p->geom, ps, p->pw16, p->ps16, p->stream));
+        CGS_CUDA(cudaStreamSynchronize(p->stream));
+        ps.pw16 = p->pw16;
+        ps.ps16 = p->ps16;
+    }
     return CGS_OK;
 }
 
@@ -717,9 +750,11 @@ cgs_status build_grid3(cgs_plan *p, const std::vector<int> &cc, const std::vecto
     const int64_t M = p->M;
     auto wrap = [](int v, int n) { v %= n; return v < 0 ? v + n : v; };
     for (void *b : {(void *)p->nodeU3, (void *)p->nodeW, (void *)p->ilist, (void *)p->iwork, (void *)p->pentries,
-                    (void *)p->pwork, (void *)p->pmulti, (void *)p->ppartial}) dev_free(b);
+                    (void *)p->pwork, (void *)p->pmulti, (void *)p->ppartial, (void *)p->pw16, (void *)p->ps16,
+                    (void *)p->pstage}) dev_free(b);
     p->nodeU3 = nullptr; p->nodeW = nullptr; p->ilist = nullptr; p->iwork = nullptr;
     p->pentries = nullptr; p->pwork = nullptr; p->pmulti = nullptr; p->ppartial = nullptr;
+    p->pw16 = nullptr; p->ps16 = nullptr; p->pstage = nullptr;
     p->niwork = 0;
     p->pset = PatchSet{};
     p->pslots = 1;
@@ -1455,9 +1490,39 @@ cgs_status build_fcg_graph(cgs_plan *p, int from_data, int toeplitz, int weighte
     return CGS_OK;
 }
 
+// A process-wide flag in mapped pinned host memory (one address for every
+// device) that a tensor-core gridding kernel sets when its bounded MMA wait
+// runs out; the next call that checks it reports CGS_ERR_TIMEOUT once.
+int *g_tc_flag = nullptr;
+std::once_flag g_tc_once;
+
+int *tc_flag()
+{
+    std::call_once(g_tc_once, [] {
+        void *h = nullptr;
+        if (cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable) == cudaSuccess) {
+            *static_cast<volatile int *>(h) = 0;
+            g_tc_flag = static_cast<int *>(h);
+        }
+    });
+    return g_tc_flag;
+}
+
+cgs_status tc_check()
+{
+    volatile int *f = g_tc_flag;
+    if (f && *f) {
+        *f = 0;
+        set_error("a tensor-core gridding kernel timed out waiting for its MMAs; its output is incomplete");
+        return CGS_ERR_TIMEOUT;
+    }
+    return CGS_OK;
+}
+
 cgs_status check_ready(cgs_plan *p, bool need_w, bool need_s)
 {
     if (!p) { set_error("null plan"); return CGS_ERR_BAD_ARG; }
+    CGS_TRY(tc_check());
     if (!p->have_k) { set_error("k-space not set"); return CGS_ERR_STATE; }
     if (need_w && !p->have_w) { set_error("weights not set"); return CGS_ERR_STATE; }
     if (need_s && !p->have_s) { set_error("sensitivities not set"); return CGS_ERR_STATE; }
@@ -1469,7 +1534,7 @@ cgs_status read_scalars(cgs_plan *p, CGScalars *h, cudaStream_t st)
 {
     CGS_CUDA(cudaMemcpyAsync(h, p->sc, sizeof(CGScalars), cudaMemcpyDeviceToHost, st));
     CGS_CUDA(cudaStreamSynchronize(st));
-    return CGS_OK;
+    return tc_check();
 }
 
 }  // namespace
@@ -1738,6 +1803,7 @@ static cgs_status build_host_chunks(cgs_plan *p, HostChunks &h, int C)
         c->work = p->work; c->nwork = p->nwork;
         c->nodeU = p->nodeU; c->nodeW = p->nodeW;
         c->pentries = p->pentries; c->pwork = p->pwork; c->pmulti = p->pmulti;
+        c->pw16 = p->pw16; c->ps16 = p->ps16; c->pstage = p->pstage;
         c->ilist = p->ilist; c->iwork = p->iwork; c->niwork = p->niwork; c->ibx = p->ibx;
         c->nodeU3 = p->nodeU3; c->iby = p->iby;
         c->tune = p->tune;
@@ -1802,9 +1868,10 @@ cgs_status cgs_plan_destroy(cgs_plan *p)
         p->nodes = nullptr; p->perm = nullptr; p->iperm = nullptr; p->w = nullptr; p->work = nullptr;
         p->nodeU = nullptr; p->nodeW = nullptr; p->pentries = nullptr; p->pwork = nullptr; p->pmulti = nullptr;
         p->ilist = nullptr; p->iwork = nullptr; p->nodeU3 = nullptr;
+        p->pw16 = nullptr; p->ps16 = nullptr; p->pstage = nullptr;
     }
     void *bufs[] = {p->tw[0], p->tw[1], p->tw[2], p->deap[0], p->deap[1], p->deap[2], p->nodes, p->perm, p->iperm,
-                    p->w, p->work, p->nodeU, p->nodeW, p->pentries, p->pwork, p->pmulti, p->ppartial, p->ilist, p->iwork, p->nodeU3, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
+                    p->w, p->work, p->nodeU, p->nodeW, p->pentries, p->pwork, p->pmulti, p->ppartial, p->pw16, p->ps16, p->pstage, p->ilist, p->iwork, p->nodeU3, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
                     p->cF, p->cP, p->cZ, p->vX, p->vR, p->vP, p->vQ, p->ioA, p->ioB, p->partial, p->dots,
                     p->active, p->sc, p->fpart, p->ftick};
     for (void *b : bufs) dev_free(b);
@@ -1935,9 +2002,11 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
         CGS_TRY(build_grid3(p, cc, perm));
     } else {
         for (void *b : {(void *)p->nodeU3, (void *)p->nodeW, (void *)p->ilist, (void *)p->iwork, (void *)p->pentries,
-                        (void *)p->pwork, (void *)p->pmulti, (void *)p->ppartial}) dev_free(b);
+                        (void *)p->pwork, (void *)p->pmulti, (void *)p->ppartial, (void *)p->pw16, (void *)p->ps16,
+                        (void *)p->pstage}) dev_free(b);
         p->nodeU3 = nullptr; p->nodeW = nullptr; p->ilist = nullptr; p->iwork = nullptr;
         p->pentries = nullptr; p->pwork = nullptr; p->pmulti = nullptr; p->ppartial = nullptr;
+        p->pw16 = nullptr; p->ps16 = nullptr; p->pstage = nullptr;
         p->niwork = 0;
         p->pset = PatchSet{};
     }
@@ -2498,7 +2567,7 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
         return false;
     };
     if (!in(t->tile, {0, 8, 16, 32}) || !in(t->interp_coils, {0, 1, 4, 8, 16, 32}) ||
-        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 2, 4, 8, 16, 32}) || !in(t->interp_block, {0, 1, 16}) ||
+        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 2, 4, 8, 16, 32, 64}) || !in(t->interp_block, {0, 1, 16}) ||
         (t->work_slice != 0 && (t->work_slice < 32 || t->work_slice > 65536)) ||
         (t->spread_chunk != 0 && (t->spread_chunk < 32 || t->spread_chunk > 65536)) ||
         t->host_chunks < 0 || t->host_chunks > 32) {
@@ -2609,17 +2678,17 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
     }
     // spreading: points per lane, chunk bound and coils per warp
     CGS_TRY(fill(p->ksV, ksN, 0x85ebca6bu));
-    for (int blk : {16, 1, 2, 4, 8}) {
+    for (int blk : {64, 16, 1, 2, 4, 8}) {
         if ((blk == 2 || blk == 4) && p->nc < 4) continue;
         if (blk == 8 && (p->nc < 2 || p->nc > 16)) continue;
         for (int chunk : {0, 64, 128, 256, 512, 1024}) {
             if (blk > 1 && blk < 16 && chunk != 0 && chunk != 512) continue;  // block variants: two chunk bounds
-            if (blk == 16 && chunk == 64) continue;
+            if (blk >= 16 && chunk == 64) continue;
             cur = best; cur.spread_chunk = chunk; cur.spread_block = blk;
             p->tune = cur;
             CGS_TRY(rebin(p));
             for (int c : sccs) {
-                if (blk == 16 && c != sccs.front()) continue;  // the tensor-core kernel sets its own coil width
+                if (blk >= 16 && c != sccs.front()) continue;  // the tensor-core kernels set their own coil width
                 if ((blk == 2 || blk == 4) && c < 4) continue;
                 if (blk == 8 && c > 16) continue;
                 p->tune.spread_coils = c;

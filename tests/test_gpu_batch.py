@@ -53,6 +53,8 @@ def test_tuning_changes_decomposition_not_results(gpu):
               dict(tile=8, work_slice=512, spread_chunk=256, interp_coils=8, spread_coils=8, spread_block=8),
               dict(tile=8, work_slice=512, spread_chunk=0, interp_coils=16, spread_coils=0, spread_block=16),
               dict(tile=16, work_slice=256, spread_chunk=128, interp_coils=8, spread_coils=0, spread_block=16),
+              dict(tile=8, work_slice=512, spread_chunk=0, interp_coils=16, spread_coils=0, spread_block=64),
+              dict(tile=8, work_slice=512, spread_chunk=96, interp_coils=16, spread_coils=0, spread_block=64),
               dict(tile=8, work_slice=256, spread_chunk=0, interp_coils=16, spread_coils=0, spread_block=0,
                    interp_block=1),
               dict(tile=32, work_slice=512, spread_chunk=0, interp_coils=4, spread_coils=0, spread_block=0,
@@ -93,7 +95,7 @@ def test_autotune_picks_valid_decomposition(gpu):
     # the tensor-core interpolation has no bin side or coils per CTA to tune
     assert t["interp_block"] == 16 or (t["tile"] in (8, 16, 32) and t["interp_coils"] in (1, 4, 8, 16, 32))
     assert t["spread_coils"] in (1, 2, 4, 8, 16) and (t["interp_block"] == 16 or t["work_slice"] in (128, 256, 512, 1024))
-    assert t["spread_block"] in (1, 2, 4, 8, 16) and t["interp_block"] in (1, 16)
+    assert t["spread_block"] in (1, 2, 4, 8, 16, 64) and t["interp_block"] in (1, 16)
     assert p.tuning() == t
     f1, a1 = nfft_pair(p, N, nc, k.shape[0], seed=3)
     # the tuned kernels may round differently from the default ones
