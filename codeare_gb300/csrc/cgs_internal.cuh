@@ -134,7 +134,8 @@ struct GridGeom {
     int nc;           // coils (innermost in grid and k-space)
     int icc;          // coils per interpolation CTA (1, 4, 8, 16; 0 = automatic)
     int scc;          // coils per spreading warp (1, 2, 4, 8, 16, 32; 0 = automatic)
-    int imma;         // 2-D interpolation on the tensor cores (needs the NodeSet's bin lists)
+    int imma;         // interpolation on the tensor cores (needs the NodeSet's bin lists): 2-D 1 mma.sync on
+                      // 4 x 4 bins, 2 tcgen05 on 8 x 16 bins; 3-D 1
 };
 
 constexpr int kInterpGroup = 16;     // tensor-core interpolation: nodes per warp (the m16)
@@ -159,6 +160,7 @@ struct NodeSet {
     // zero padded), and ilist / iwork group the nodes by 4 x 4 x 4 start bin
     const int4 *nodeU3;
     int iby;            // 3-D: bins per grid column (bins per plane = iby * ibx)
+    int *err;           // set by a tensor-core kernel whose MMA wait ran out (nullable)
 };
 constexpr int kW3 = 32;  // floats per node in the 3-D window table
 

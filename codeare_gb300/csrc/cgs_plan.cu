@@ -306,10 +306,12 @@ void dev_free(void *p)
 }
 
 // the gridding kernels' view of a plan's node tables
+int *tc_flag();
+
 NodeSet node_set(const cgs_plan *p)
 {
     NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork,
-               p->niwork, p->ibx, p->nodeU3, p->iby};
+               p->niwork, p->ibx, p->nodeU3, p->iby, tc_flag()};
     return ns;
 }
 
@@ -553,26 +555,30 @@ void apply_tiles(cgs_plan *p)
     g.icc = p->tune.interp_coils;
     g.scc = p->tune.spread_coils;
     const int ib = p->tune.interp_block;
-    g.imma = (p->d == 2 && (ib == 16 || (ib == 0 && p->nc >= 4))) ? 1 : 0;
+    g.imma = (p->d == 2 && ib == 64) ? 2 : ((p->d == 2 && (ib == 16 || (ib == 0 && p->nc >= 4))) ? 1 : 0);
     if (p->d == 3) g.imma = (ib != 1 && grid3_mma_ok(g)) ? 1 : 0;
 }
 
 // Node lists of the 2-D tensor-core interpolation: sorted node indices grouped
-// by the 4 x 4 bin of their wrapped footprint start (the same wrap as the
-// device's node tables), work items (one warp each) of at most kInterpGroup
-// nodes of one bin, in bin order so that neighbouring warps read
-// neighbouring grid regions.  `cc` holds floor(n x) per node in trajectory order.
+// by the 4 x 4 bin (8 x 16 for the tcgen05 kernel) of their wrapped footprint
+// start (the same wrap as the device's node tables), work items (one warp, or
+// one CTA for tcgen05) of at most kInterpGroup (128) nodes of one bin, in bin
+// order so that neighbouring work items read neighbouring grid regions.  `cc`
+// holds floor(n x) per node in trajectory order.
 cgs_status build_ibins(cgs_plan *p, const std::vector<int> &cc, const std::vector<int> &perm)
 {
     const int n0 = p->n[0], n1 = p->n[1], m = p->m;
-    const int nby = (n0 + 3) / 4, nbx = (n1 + 3) / 4;
+    // interp_block 64 (tcgen05): 8 x 16 bins, work items of up to 128 nodes
+    const bool tc = p->tune.interp_block == 64;
+    const int bh = tc ? 8 : 4, bw = tc ? 16 : 4, group = tc ? 128 : kInterpGroup;
+    const int nby = (n0 + bh - 1) / bh, nbx = (n1 + bw - 1) / bw;
     const int64_t M = p->M;
     std::vector<int> bin(M), cnt((size_t)nby * nbx + 1, 0);
     auto wrap = [](int v, int n) { v %= n; return v < 0 ? v + n : v; };
     for (int64_t s = 0; s < M; ++s) {
         const int j = perm[s];
         const int u0 = wrap(cc[(size_t)j * 2] - m, n0), u1 = wrap(cc[(size_t)j * 2 + 1] - m, n1);
-        bin[s] = (u0 / 4) * nbx + u1 / 4;
+        bin[s] = (u0 / bh) * nbx + u1 / bw;
         cnt[bin[s] + 1]++;
     }
     for (size_t b = 0; b + 1 < cnt.size(); ++b) cnt[b + 1] += cnt[b];
@@ -580,8 +586,8 @@ cgs_status build_ibins(cgs_plan *p, const std::vector<int> &cc, const std::vecto
     for (int64_t s = 0; s < M; ++s) list[fill[bin[s]]++] = (int)s;
     std::vector<int4> work;
     for (int b = 0; b < nby * nbx; ++b)
-        for (int s0 = cnt[b]; s0 < cnt[b + 1]; s0 += kInterpGroup)
-            work.push_back(make_int4(b, s0, std::min(kInterpGroup, cnt[b + 1] - s0), 0));
+        for (int s0 = cnt[b]; s0 < cnt[b + 1]; s0 += group)
+            work.push_back(make_int4(b, s0, std::min(group, cnt[b + 1] - s0), 0));
     dev_free(p->ilist);
     dev_free(p->iwork);
     p->ilist = nullptr;
@@ -594,8 +600,6 @@ cgs_status build_ibins(cgs_plan *p, const std::vector<int> &cc, const std::vecto
     p->ibx = nbx;
     return CGS_OK;
 }
-
-int *tc_flag();
 
 // Per 4 x 4 patch (4 x 8 for one coil, 8 x 4 or 8 x 16 for the tensor-core
 // variants) of the 2-D grid, the sorted indices of the nodes whose footprint
@@ -2567,7 +2571,7 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
         return false;
     };
     if (!in(t->tile, {0, 8, 16, 32}) || !in(t->interp_coils, {0, 1, 4, 8, 16, 32}) ||
-        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 2, 4, 8, 16, 32, 64}) || !in(t->interp_block, {0, 1, 16}) ||
+        !in(t->spread_coils, {0, 1, 2, 4, 8, 16, 32}) || !in(t->spread_block, {0, 1, 2, 4, 8, 16, 32, 64}) || !in(t->interp_block, {0, 1, 16, 64}) ||
         (t->work_slice != 0 && (t->work_slice < 32 || t->work_slice > 65536)) ||
         (t->spread_chunk != 0 && (t->spread_chunk < 32 || t->spread_chunk > 65536)) ||
         t->host_chunks < 0 || t->host_chunks > 32) {
@@ -2583,7 +2587,7 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
     }
     const bool bins = t->tile != p->tune.tile || t->work_slice != p->tune.work_slice ||
                       t->spread_chunk != p->tune.spread_chunk || t->spread_block != p->tune.spread_block ||
-                      (p->d == 3 && t->interp_block != p->tune.interp_block);
+                      t->interp_block != p->tune.interp_block;
     p->tune = *t;
     apply_tiles(p);
     drop_graphs(p);
@@ -2642,13 +2646,13 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
     // then the work slice
     CGS_TRY(fill(p->grid, gridN, 0x9e3779b9u));
     bool imma_best = false;
-    {
-        cur = best; cur.interp_block = 16;
+    for (int ib : {16, 64}) {   // mma.sync on 4 x 4 bins, tcgen05 on 8 x 16 bins
+        cur = best; cur.interp_block = ib;
         p->tune = cur;
-        apply_tiles(p);
-        if (p->geom.imma) {
+        CGS_TRY(rebin(p));
+        if (p->geom.imma == (ib == 64 ? 2 : 1)) {
             CGS_TRY(timed(interp, &t));
-            t_int = t; best.interp_block = 16; imma_best = true;
+            if (t < t_int) { t_int = t; best.interp_block = ib; imma_best = true; }
         }
     }
     for (int tile : {8, 16, 32}) {

@@ -114,6 +114,30 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32
     return done != 0;
 }
 
+__device__ __forceinline__ uint64_t globaltimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// wait for phase `parity` of *bar to complete; the thread sleeps in
+// try_wait until the phase completes (or the hint's 10 ms pass) instead of
+// spinning, and gives up after `limit_ns` of the global timer; returns false
+// if it gave up
+__device__ __forceinline__ bool mbar_wait_ns(uint64_t *bar, uint32_t parity, uint64_t limit_ns)
+{
+    const uint64_t t0 = globaltimer();
+    while (true) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done) : "r"(smem_u32(bar)), "r"(parity), "r"(10000000u) : "memory");
+        if (done) return true;
+        if (globaltimer() - t0 > limit_ns) return false;
+    }
+}
+
 // 32 consecutive FP32 accumulator columns of this warp's 32 lanes
 // (warp-collective); follow with wait_ld() before using v
 __device__ __forceinline__ void ld32(uint32_t taddr, float (&v)[32])

@@ -223,8 +223,10 @@ typedef struct {
                           accumulator); default 16 from 4 coils, else 1 */
     int interp_block;  /* 2-D interpolation: 1 CUDA cores (tiles of `tile`), 16 tensor
                           cores (16 nodes of a 4 x 4 footprint-start bin per warp,
-                          TF32-split operands, FP32 accumulation); default 16 from 4
-                          coils for m <= 4, else 1 */
+                          TF32-split operands, FP32 accumulation), 64 the 5th-generation
+                          tensor cores (tcgen05.mma kind::tf32, up to 128 nodes of an
+                          8 x 16 footprint-start bin per CTA, the weights in tensor
+                          memory); default 16 from 4 coils for m <= 4, else 1 */
     int host_chunks;   /* cgs_nfft_trafo / cgs_nfft_adjoint with a host input or output,
                           cgs_sense_trafo with a host output (one frame): the coils
                           are split into this many contiguous
