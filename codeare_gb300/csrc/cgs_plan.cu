@@ -615,8 +615,10 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     // (four coil groups); spread_block 1: 4 x 4 patches, a point per lane, two coil groups
     // spread_block 8: 4 x 8 patches, one coil group, a point per lane
     // spread_block 16: 4 x 4 patches on the tensor cores (TF32 split, FP32
-    // accumulation), the default from 4 coils up
-    const int tb = p->tune.spread_block != 0 ? p->tune.spread_block : (p->nc >= 4 ? 16 : 1);
+    // accumulation), the default for 4 to 7 coils; spread_block 64 (tcgen05),
+    // the default from 8 coils up, where its coil-independent weight build
+    // is shared by enough coils
+    const int tb = p->tune.spread_block != 0 ? p->tune.spread_block : (p->nc >= 8 ? 64 : (p->nc >= 4 ? 16 : 1));
     // spread_block 32: 8 x 4 patches on the tensor cores (two m-tiles per warp);
     // spread_block 64: 8 x 16 patches on the 5th-generation tensor cores (tcgen05)
     const int blk = (tb == 16 || tb == 32 || tb == 64)
@@ -663,8 +665,11 @@ cgs_status build_patches(cgs_plan *p, const std::vector<int> &cc)
     }
     // work items: a chunk bound that keeps every warp's list short
     const int64_t avg = std::max<int64_t>(1, E / std::max<int64_t>(P, 1));
+    // the tcgen05 kernel (128-point patches, fixed per-item set-up) prefers
+    // longer items: 3x the mean list, 256..1024
     const int chunk = p->tune.spread_chunk > 0 ? p->tune.spread_chunk
-                                               : (int)std::min<int64_t>(1024, std::max<int64_t>(64, 2 * avg));
+                      : blk == 64 ? (int)std::min<int64_t>(1024, std::max<int64_t>(256, 3 * avg))
+                                  : (int)std::min<int64_t>(1024, std::max<int64_t>(64, 2 * avg));
     std::vector<int4> work, multi;
     int slots = 0;
     for (int64_t q = 0; q < P; ++q) {

@@ -220,7 +220,7 @@ typedef struct {
                           with FP32 accumulation), 32 (8 x 4 patches on the tensor
                           cores), 64 (8 x 16 patches on the 5th-generation tensor
                           cores, tcgen05.mma kind::tf32 with a tensor-memory
-                          accumulator); default 16 from 4 coils, else 1 */
+                          accumulator); default 64 from 8 coils, 16 from 4, else 1 */
     int interp_block;  /* 2-D interpolation: 1 CUDA cores (tiles of `tile`), 16 tensor
                           cores (16 nodes of a 4 x 4 footprint-start bin per warp,
                           TF32-split operands, FP32 accumulation), 64 the 5th-generation
