@@ -516,6 +516,20 @@ __device__ __forceinline__ void tf32_split(float x, uint32_t &hi, uint32_t &lo)
     lo = __float_as_uint(x - __uint_as_float(hi));
 }
 
+// x * y on both FP32 lanes (the rounding of two FP32 multiplies)
+__device__ __forceinline__ float2 fmul2(float2 x, float2 y) { return ffma2(x, y, make_float2(0.f, 0.f)); }
+
+// tf32_split on two values; the remainders x - hi (exact) with one paired
+// FMA, so the result is the same as two tf32_split calls
+__device__ __forceinline__ void tf32_split2(float2 x, uint32_t &h0, uint32_t &h1, uint32_t &l0, uint32_t &l1)
+{
+    h0 = (__float_as_uint(x.x) + 0x1000u) & 0xffffe000u;
+    h1 = (__float_as_uint(x.y) + 0x1000u) & 0xffffe000u;
+    const float2 lo = ffma2(make_float2(-1.f, -1.f), make_float2(__uint_as_float(h0), __uint_as_float(h1)), x);
+    l0 = __float_as_uint(lo.x);
+    l1 = __float_as_uint(lo.y);
+}
+
 __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
 {
     asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -657,8 +671,7 @@ spread_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ Pa
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
             uint32_t bh0, bl0, bh1, bl1;
-            tf32_split(r0[8 * t], bh0, bl0);
-            tf32_split(r1[8 * t], bh1, bl1);
+            tf32_split2(make_float2(r0[8 * t], r1[8 * t]), bh0, bh1, bl0, bl1);
 #pragma unroll
             for (int mt = 0; mt < MT; ++mt) {
                 mma_tf32(acc[mt][t], al[mt], bh0, bh1);
@@ -746,18 +759,6 @@ template <int NCOL> struct SpreadTc {
     static constexpr int TCOLS = 128;
 };
 
-// x * y on both FP32 lanes (the rounding of two FP32 multiplies)
-__device__ __forceinline__ float2 fmul2(float2 x, float2 y) { return ffma2(x, y, make_float2(0.f, 0.f)); }
-
-// tf32_split on two values; the remainders x - hi with one paired FMA
-__device__ __forceinline__ void tf32_split2(float2 x, uint32_t &h0, uint32_t &h1, uint32_t &l0, uint32_t &l1)
-{
-    h0 = (__float_as_uint(x.x) + 0x1000u) & 0xffffe000u;
-    h1 = (__float_as_uint(x.y) + 0x1000u) & 0xffffe000u;
-    const float2 lo = ffma2(make_float2(-1.f, -1.f), make_float2(__uint_as_float(h0), __uint_as_float(h1)), x);
-    l0 = __float_as_uint(lo.x);
-    l1 = __float_as_uint(lo.y);
-}
 
 // the stage blocks of one work item per CTA: patch weights [24][16] and node
 // indices [16] of entries j * 16 .. j * 16 + 15 of the item's list
@@ -1417,8 +1418,7 @@ interp_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ No
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
             uint32_t bh0, bl0, bh1, bl1;
-            tf32_split(b0v[t], bh0, bl0);
-            tf32_split(b1v[t], bh1, bl1);
+            tf32_split2(make_float2(b0v[t], b1v[t]), bh0, bh1, bl0, bl1);
             mma_tf32(acc[t], al, bh0, bh1);
             mma_tf32(acc[t], ah, bl0, bl1);
             mma_tf32(acc[t], ah, bh0, bh1);
@@ -1763,8 +1763,7 @@ spread3_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ P
             const float *r0 = sv + tq * R + gq, *r1 = sv + (tq + 4) * R + gq;
 #pragma unroll
             for (int t = 0; t < NT; ++t) {
-                tf32_split(r0[8 * t], bh0[t], bl0[t]);
-                tf32_split(r1[8 * t], bh1[t], bl1[t]);
+                tf32_split2(make_float2(r0[8 * t], r1[8 * t]), bh0[t], bh1[t], bl0[t], bl1[t]);
             }
 #pragma unroll
             for (int mt = 0; mt < 4; ++mt) {
@@ -1973,8 +1972,7 @@ interp3_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ N
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
             uint32_t bh0, bl0, bh1, bl1;
-            tf32_split(r0[8 * t], bh0, bl0);
-            tf32_split(r1[8 * t], bh1, bl1);
+            tf32_split2(make_float2(r0[8 * t], r1[8 * t]), bh0, bh1, bl0, bl1);
             mma_tf32(acc[t], al, bh0, bh1);
             mma_tf32(acc[t], ah, bl0, bl1);
             mma_tf32(acc[t], ah, bh0, bh1);
