@@ -744,9 +744,7 @@ constexpr int kSpTcThreads = 256;
 constexpr uint64_t kSpTcWaitNs = 1000000000ull;   // a bounded mbarrier wait gives up after 1 s
 
 template <int NCOL> struct SpreadTc {
-    static constexpr int A = 128 * kSpTcKS * 4;        // one of hi / lo
-    static constexpr int B = NCOL * kSpTcKS * 4;
-    static constexpr int LBO_A = 16 * 128;             // next 4 entries: past the 16 point groups
+    static constexpr int B = NCOL * kSpTcKS * 4;        // one of hi / lo
     static constexpr int LBO_B = (NCOL / 8) * 128;     // next 4 entries: past the NCOL / 8 column groups
     static constexpr int OPER = 2 * B;                 // B hi, lo (A lives in tensor memory)
     static constexpr int WSLOT = kSpTcWPE * kSpTcWS * 4 + kSpTcKS * 4;   // weights, node indices
@@ -1041,62 +1039,74 @@ spread_tc05_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ P
 }
 
 // ---------------------------------------------------------------------------
-// 2-D interpolation on the 5th-generation tensor cores (interp_block 64).
-// Nodes are grouped by the 8 x 16 bin of their footprint start, so the
-// footprints of a bin's nodes lie in one UY x UX region of the grid
-// (UY = 7 + taps, UX = 15 + taps).  A CTA of 256 builder threads and an MMA
-// warp takes up to 128 nodes of one bin and NCOL / 2 coils:
-//   f[128 nodes][NCOL columns] = W[128 nodes][K region points] G[K][NCOL]
-// in stages of 16 region points (row-major over the region):
-//   * the tile's nodes: footprint offsets in the bin and window rows padded
-//     with zeros, so that any region coordinate indexes them without checks,
-//     in shared memory for the whole tile;
-//   * A = W in tensor memory, TF32-split (tf32_split2): thread m % 128 of
-//     warps m / 32 and m / 32 + 4 (node m) computes 8 of the stage's 16
-//     weights and stores them with tcgen05.st;
-//   * B = G^T: the stage's grid values (cp.async two stages ahead, a ring of
-//     three slots), split and stored K-major in shared memory as in the
-//     spreading, in one of two stage buffers;
-//   * the MMA warp waits for a buffer's "full" mbarrier, issues lo.hi +
-//     hi.lo + hi.hi per K = 8 step and commits to its "empty" mbarrier.
-// Every wait is bounded; a builder whose wait ran out makes all builders stop
-// (an OR over their barrier), the CTA sets *ns.err, stores nothing and frees
-// its tensor memory.  The epilogue writes each node's coils to the bin-ordered
-// k-space, or with `user` straight into the caller's coil-major layout.
+// 2-D interpolation on the 5th-generation tensor cores (interp_block 64),
+// row by row over the region.  Nodes are grouped by the 8 x 16 bin of their
+// footprint start, so the footprints of a bin's nodes lie in one UY x UX
+// region of the grid (UY = 7 + taps, UX = 15 + taps <= 25).  The window is
+// separable: for up to 128 nodes of a bin and NCOL / 2 coils
+//   D_y[node][col] = sum_x wx_node(x) G[y][x][col]     (tensor cores, per region row y)
+//   f[node][col]   = sum_y wy_node(y) D_y[node][col]   (CUDA cores, FP32)
+// and the A operand Wx[node][x] (x padded to kIsK) is the same for every row:
+// it is built once per tile, TF32-split, into tensor memory.  Per row:
+//   * warps 4..7 bring the row's grid values (cp.async, two rows ahead, a
+//     ring of three slots) and store them TF32-split as B, K-major in the
+//     canonical no-swizzle layout, in one of two shared-memory buffers;
+//   * the MMA warp issues lo.hi + hi.lo + hi.hi per K = 8 step into one of
+//     two tensor-memory accumulators and commits to the row's mbarrier;
+//   * warps 0..3 (thread m: node m) read the accumulator (tcgen05.ld) and
+//     add wy_node(y - oy) times it to their FP32 sums in registers.
+// Every handoff is an mbarrier wait bounded by the global timer; a group of
+// warps whose wait ran out stops together (an OR over its named barrier), the
+// CTA sets *ns.err, stores nothing and frees its tensor memory.  The nodes'
+// sums go to the bin-ordered k-space, or with `user` straight into the
+// caller's coil-major layout.
 // ---------------------------------------------------------------------------
-constexpr int kItBH = 8, kItBW = 16;             // footprint-start bin rows, columns
 constexpr int kItNodes = 128;                    // nodes per tile (the MMA's M)
-constexpr int kItPY = 24, kItPX = 40;            // padded window rows: taps at 7 .., 15 ..
-constexpr int kItRow = kItPY + kItPX + 1;        // floats per node (+1 spreads the banks)
+constexpr int kIsBH = 8, kIsBW = 16;             // footprint-start bin rows, columns
+constexpr int kIsK = 32;                         // region columns padded to the MMA's K
+constexpr int kIsWY = 16;                        // floats per node's y window row in shared memory
 
-template <int NCOL, int TAPS> struct InterpTc {
-    static constexpr int UY = kItBH - 1 + TAPS, UX = kItBW - 1 + TAPS;
-    static constexpr int K = UY * UX, NST = (K + 15) / 16;
-    static constexpr int B = NCOL * 16 * 4;                      // one of hi / lo
-    static constexpr int LBO_B = (NCOL / 8) * 128;
-    static constexpr int VSLOT = 16 * NCOL * 4, NV = 3;
-    static constexpr int ROWS = kItNodes * kItRow * 4;
-    static constexpr int META = kItNodes * 3 * 4;                  // node index, offsets
-    static constexpr int SMEM = 2 * 2 * B + NV * VSLOT + ROWS + META + 48;
-    static constexpr int ACOL = 64, TCOLS = 128;
-    static_assert(UY + 7 <= kItPY + 1 && UX + 15 <= kItPX + 1, "padded window rows too short");
+template <int NCOL, int TAPS> struct InterpSep {
+    static constexpr int UY = kIsBH - 1 + TAPS, UX = kIsBW - 1 + TAPS;
+    static_assert(UX <= kIsK && NCOL <= 32, "region wider than K, or too many columns");
+    static constexpr int B = NCOL * kIsK * 4;                  // one of hi / lo
+    static constexpr int LBO_B = (NCOL / 8) * 128;             // next 4 region columns
+    static constexpr int RAW = kIsK * NCOL * 4, NR = 3;        // one region row's values
+    static constexpr int SMEM = 2 * 2 * B + NR * RAW + kItNodes * kIsWY * 4 + 64;
+    // tensor memory: A hi in columns 0..31, A lo 32..63, the row accumulators
+    // at 64 and 96
+    static constexpr int TCOLS = 128;
 };
+
+// named barriers over 128 threads (ids 1 and 2); the second form returns the
+// OR of `v` over them, the same value in every participating thread
+template <int ID>
+__device__ __forceinline__ void group_sync() { asm volatile("bar.sync %0, 128;" ::"n"(ID) : "memory"); }
+template <int ID>
+__device__ __forceinline__ bool group_sync_or(bool v)
+{
+    uint32_t r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, 128, p;\n\t"
+                 "selp.u32 %0, 1, 0, q;\n\t}" : "=r"(r) : "r"((uint32_t)v), "n"(ID) : "memory");
+    return r != 0;
+}
 
 template <int NCOL, int TAPS>
 __global__ void __launch_bounds__(kSpTcThreads + 32, 3)
-interp_tc05_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
-                   const float2 *__restrict__ grid, float2 *__restrict__ ks, float2 *__restrict__ user)
+interp_sep_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
+                  const float2 *__restrict__ grid, float2 *__restrict__ ks, float2 *__restrict__ user)
 {
-    using I = InterpTc<NCOL, TAPS>;
+    using I = InterpSep<NCOL, TAPS>;
     constexpr int CC = NCOL / 2;
     extern __shared__ __align__(128) uint8_t tsm[];
-    uint8_t *vring = tsm + 2 * 2 * I::B;
-    float *rows = reinterpret_cast<float *>(vring + I::NV * I::VSLOT);
-    int *sidx = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(rows) + I::ROWS);
-    int *soy = sidx + kItNodes, *sox = soy + kItNodes;
-    uint64_t *full = reinterpret_cast<uint64_t *>(sox + kItNodes);
-    uint64_t *empty = full + 2;
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(empty + 2);
+    uint8_t *bbuf = tsm;                                                // [buffer][hi, lo]
+    uint8_t *raw0 = tsm + 4 * I::B;
+    float *wys = reinterpret_cast<float *>(raw0 + I::NR * I::RAW);      // [node][kIsWY]
+    uint64_t *bfull = reinterpret_cast<uint64_t *>(wys + kItNodes * kIsWY);   // B of buffer b built
+    uint64_t *rdone = bfull + 2;                                         // row's MMAs done
+    uint64_t *dempty = rdone + 2;                                        // accumulator read
+    uint64_t *afull = dempty + 2;                                        // A in tensor memory
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(afull + 1);
     volatile int *sfail = reinterpret_cast<volatile int *>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5;
     const int4 wk = ns.iwork[blockIdx.x];                  // {bin, first, count <= 128, 0}
@@ -1104,183 +1114,198 @@ interp_tc05_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ N
     const int ccn = min(CC, g.nc - c0);
     const int n0 = g.n[0], n1 = g.n[1];
     const bool v16 = (g.nc & 1) == 0;
-    const int by0 = (wk.x / ns.ibx) * kItBH, bx0 = (wk.x % ns.ibx) * kItBW;
+    const int by0 = (wk.x / ns.ibx) * kIsBH, bx0 = (wk.x % ns.ibx) * kIsBW;
     const int cnt = wk.z;
-
-    auto vslot = [&](int j) { return reinterpret_cast<float *>(vring + (j % I::NV) * I::VSLOT); };
-    // stage j's grid values: region points 16 j .. 16 j + 15 (threads 0..127)
-    auto fetch_v = [&](int j) {
-        float *sv = vslot(j);
-        const int per = v16 ? CC / 2 : CC;                 // pieces per point
-        for (int it = tid; it < 16 * per; it += 128) {
-            const int e = it / per, q = it % per;
-            const int pt = 16 * j + e;
-            int gy = -1, gx = 0;
-            if (pt < I::K) {
-                gy = by0 + pt / I::UX;
-                gx = bx0 + pt % I::UX;
-                if (gy >= n0) gy -= n0;
-                if (gx >= n1) gx -= n1;
-            }
-            const float2 *src = grid + ((size_t)max(gy, 0) * n1 + gx) * g.nc + c0;
-            if (v16) {
-                float *d = sv + e * NCOL + 4 * q;
-                if (gy >= 0 && 2 * q < ccn) cp_async16(d, src + 2 * q);
-                else *reinterpret_cast<float4 *>(d) = make_float4(0.f, 0.f, 0.f, 0.f);
-            } else {
-                float *d = sv + e * NCOL + 2 * q;
-                if (gy >= 0 && q < ccn) cp_async8(d, src + q);
-                else *reinterpret_cast<float2 *>(d) = make_float2(0.f, 0.f);
-            }
-        }
-    };
 
     if (warp == kSpTcThreads / 32) tc05::alloc<I::TCOLS>(tslot);
     if (tid == 0) {
         for (int k = 0; k < 2; ++k) {
-            tc05::mbar_init(&full[k], 1);
-            tc05::mbar_init(&empty[k], 1);
+            tc05::mbar_init(&bfull[k], 1);
+            tc05::mbar_init(&rdone[k], 1);
+            tc05::mbar_init(&dempty[k], 1);
         }
+        tc05::mbar_init(afull, 1);
         tc05::fence_mbar_init();
         *sfail = 0;
-    }
-    // the tile's nodes: index, offsets in the bin, padded window rows
-    if (tid < kItNodes) {
-        float *wy = rows + tid * kItRow, *wx = wy + kItPY;
-        int sv = -1, oy = 0, ox = 0;
-        if (tid < cnt) {
-            sv = ns.ilist[wk.y + tid];
-            const int2 u = ns.nodeU[sv];
-            oy = u.x - by0;
-            ox = u.y - bx0;
-        }
-        const float *W = ns.nodeW + (size_t)max(sv, 0) * 2 * TAPS;
-        for (int i = 0; i < kItPY; ++i) wy[i] = (sv >= 0 && i >= 7 && i < 7 + TAPS) ? W[i - 7] : 0.f;
-        for (int i = 0; i < kItPX; ++i) wx[i] = (sv >= 0 && i >= 15 && i < 15 + TAPS) ? W[TAPS + i - 15] : 0.f;
-        sidx[tid] = sv;
-        soy[tid] = oy;
-        sox[tid] = ox;
     }
     tc05::fence_before();
     __syncthreads();
     tc05::fence_after();
     const uint32_t tmem = *tslot;
+    float acc[NCOL];
+#pragma unroll
+    for (int c = 0; c < NCOL; ++c) acc[c] = 0.f;
+    int snode = -1;
 
     if (warp == kSpTcThreads / 32) {
+        // the MMA warp: one thread issues each row once A, its B and its accumulator are ready
         if ((tid & 31) == 0) {
             constexpr uint32_t idesc = tc05::idesc_tf32(128, NCOL);
-            for (int i = 0; i < I::NST; ++i) {
-                const int b = i & 1;
-                if (!tc05::mbar_wait_ns(&full[b], (i >> 1) & 1, kSpTcWaitNs)) { *sfail = 1; break; }
+            bool ok = tc05::mbar_wait_ns(afull, 0, kSpTcWaitNs);
+            for (int y = 0; ok && y < I::UY; ++y) {
+                const int b = y & 1;
+                if (!tc05::mbar_wait_ns(&bfull[b], (y >> 1) & 1, kSpTcWaitNs) ||
+                    (y >= 2 && !tc05::mbar_wait_ns(&dempty[b], ((y - 2) >> 1) & 1, kSpTcWaitNs))) {
+                    ok = false;
+                    break;
+                }
                 tc05::fence_after();
-                const uint32_t bh = tc05::smem_u32(tsm + b * 2 * I::B), bl = bh + I::B;
-                const uint32_t ah = tmem + I::ACOL + 32 * b, al = ah + 16;
+                const uint32_t bh = tc05::smem_u32(bbuf + b * 2 * I::B), bl = bh + I::B;
+                const uint32_t d = tmem + 64 + 32 * b;
 #pragma unroll
-                for (int kk = 0; kk < 2; ++kk) {
+                for (int kk = 0; kk < kIsK / 8; ++kk) {
                     const uint32_t ob = kk * 2 * I::LBO_B;
                     const uint64_t dbh = tc05::desc(bh + ob, I::LBO_B, 128), dbl = tc05::desc(bl + ob, I::LBO_B, 128);
-                    tc05::mma_tf32_ta(tmem, al + 8 * kk, dbh, idesc, (i | kk) ? 1u : 0u);
-                    tc05::mma_tf32_ta(tmem, ah + 8 * kk, dbl, idesc, 1u);
-                    tc05::mma_tf32_ta(tmem, ah + 8 * kk, dbh, idesc, 1u);
+                    tc05::mma_tf32_ta(d, tmem + 32 + 8 * kk, dbh, idesc, kk ? 1u : 0u);
+                    tc05::mma_tf32_ta(d, tmem + 8 * kk, dbl, idesc, 1u);
+                    tc05::mma_tf32_ta(d, tmem + 8 * kk, dbh, idesc, 1u);
                 }
-                tc05::commit(&empty[b]);
+                tc05::commit(&rdone[b]);
             }
+            if (!ok) *sfail = 1;
         }
         __syncwarp();
-    } else {
-        const int m = tid & 127, h = tid >> 7;
-        const float *wy = rows + m * kItRow + 7 - soy[m], *wx = rows + m * kItRow + kItPY + 15 - sox[m];
-        if (tid < 128) fetch_v(0);
+    } else if (tid >= kItNodes) {
+        // warps 4..7: each region row's values -> B
+        const int bt = tid - kItNodes;
+        auto raw = [&](int y) { return reinterpret_cast<float *>(raw0 + (y % I::NR) * I::RAW); };
+        // region row y: columns 0 .. kIsK - 1, zero past UX and past the coils
+        auto fetch = [&](int y) {
+            float *sv = raw(y);
+            int gy = by0 + y;
+            if (gy >= n0) gy -= n0;
+            const int per = v16 ? CC / 2 : CC;
+            for (int it = bt; it < kIsK * per; it += kItNodes) {
+                const int x = it / per, q = it % per;
+                int gx = bx0 + x;
+                if (gx >= n1) gx -= n1;
+                const float2 *src = grid + ((size_t)gy * n1 + (x < I::UX ? gx : 0)) * g.nc + c0;
+                if (v16) {
+                    float *d = sv + x * NCOL + 4 * q;
+                    if (x < I::UX && 2 * q < ccn) cp_async16(d, src + 2 * q);
+                    else *reinterpret_cast<float4 *>(d) = make_float4(0.f, 0.f, 0.f, 0.f);
+                } else {
+                    float *d = sv + x * NCOL + 2 * q;
+                    if (x < I::UX && q < ccn) cp_async8(d, src + q);
+                    else *reinterpret_cast<float2 *>(d) = make_float2(0.f, 0.f);
+                }
+            }
+        };
+        fetch(0);
         cp_async_commit();
-        if (tid < 128) fetch_v(1);
+        fetch(1);
         cp_async_commit();
         cp_async_wait<1>();
-        builders_sync();
+        group_sync<1>();
         bool lf = false, failed = false;
-        for (int i = 0; i < I::NST; ++i) {
-            const int b = i & 1;
-            uint8_t *bH = tsm + b * 2 * I::B, *bL = bH + I::B;
-            if (i >= 2 && !tc05::mbar_wait_ns(&empty[b], ((i - 2) >> 1) & 1, kSpTcWaitNs)) lf = true;
-            if (i + 2 < I::NST && tid < 128) fetch_v(i + 2);
+        for (int y = 0; y < I::UY; ++y) {
+            const int b = y & 1;
+            // the MMAs of row y - 2 read this B buffer
+            if (y >= 2 && !tc05::mbar_wait_ns(&rdone[b], ((y - 2) >> 1) & 1, kSpTcWaitNs)) lf = true;
+            if (y + 2 < I::UY) fetch(y + 2);
             cp_async_commit();
-            if (tid >= 128) {
-                // B: a thread per (column, 4 region points): a warp stores 32
-                // consecutive 16-byte rows
-                const float *sv = vslot(i);
-                for (int it = tid - 128; it < NCOL * 4; it += 128) {
-                    const int n = it % NCOL, kg = it / NCOL;
-                    uint32_t h[4], l[4];
-                    tf32_split2(make_float2(sv[(4 * kg) * NCOL + n], sv[(4 * kg + 1) * NCOL + n]), h[0], h[1], l[0], l[1]);
-                    tf32_split2(make_float2(sv[(4 * kg + 2) * NCOL + n], sv[(4 * kg + 3) * NCOL + n]), h[2], h[3], l[2],
-                                l[3]);
-                    const int off = kg * I::LBO_B + (n >> 3) * 128 + (n & 7) * 16;
-                    *reinterpret_cast<uint4 *>(bH + off) = make_uint4(h[0], h[1], h[2], h[3]);
-                    *reinterpret_cast<uint4 *>(bL + off) = make_uint4(l[0], l[1], l[2], l[3]);
-                }
-            }
-            // A: node m, region points 16 i + 8 h .. 16 i + 8 h + 7
-            {
-                const int q0 = 16 * i + 8 * h;
-                int qy = q0 / I::UX, qx = q0 - qy * I::UX;
-                float w[8];
-#pragma unroll
-                for (int t = 0; t < 8; ++t) {
-                    w[t] = (q0 + t < I::K) ? wy[qy] * wx[qx] : 0.f;
-                    if (++qx == I::UX) { qx = 0; ++qy; }
-                }
-                uint32_t hv[8], lv[8];
-#pragma unroll
-                for (int t = 0; t < 8; t += 2)
-                    tf32_split2(make_float2(w[t], w[t + 1]), hv[t], hv[t + 1], lv[t], lv[t + 1]);
-                const uint32_t ta = tmem + ((uint32_t)((warp & 3) * 32) << 16) + I::ACOL + 32 * b + 8 * h;
-                tc05::st8(ta, hv);
-                tc05::st8(ta + 16, lv);
-                tc05::wait_st();
+            const float *sv = raw(y);
+            uint8_t *bH = bbuf + b * 2 * I::B, *bL = bH + I::B;
+            // a thread per (column, 4 region columns): a warp stores 32
+            // consecutive 16-byte rows
+            for (int it = bt; it < NCOL * (kIsK / 4); it += kItNodes) {
+                const int n = it % NCOL, kg = it / NCOL;
+                uint32_t h[4], l[4];
+                tf32_split2(make_float2(sv[(4 * kg) * NCOL + n], sv[(4 * kg + 1) * NCOL + n]), h[0], h[1], l[0], l[1]);
+                tf32_split2(make_float2(sv[(4 * kg + 2) * NCOL + n], sv[(4 * kg + 3) * NCOL + n]), h[2], h[3], l[2], l[3]);
+                const int off = kg * I::LBO_B + (n >> 3) * 128 + (n & 7) * 16;
+                *reinterpret_cast<uint4 *>(bH + off) = make_uint4(h[0], h[1], h[2], h[3]);
+                *reinterpret_cast<uint4 *>(bL + off) = make_uint4(l[0], l[1], l[2], l[3]);
             }
             tc05::fence_proxy_async();
-            tc05::fence_before();
             cp_async_wait<1>();
-            if (builders_sync_or(lf)) { failed = true; break; }
-            if (tid == 0) mbar_arrive(&full[b]);
+            if (group_sync_or<1>(lf)) { failed = true; break; }
+            if (bt == 0) mbar_arrive(&bfull[b]);
         }
         cp_async_wait<0>();
-        if (!failed && !tc05::mbar_wait_ns(&empty[(I::NST - 1) & 1], ((I::NST - 1) >> 1) & 1, kSpTcWaitNs))
-            failed = true;
+        if (failed) *sfail = 1;
+    } else {
+        // warps 0..3: node m = tid
+        const int m = tid;
+        int oy = 0, ox = 0;
+        if (m < cnt) {
+            snode = ns.ilist[wk.y + m];
+            const int2 u = ns.nodeU[snode];
+            oy = u.x - by0;
+            ox = u.y - bx0;
+        }
+        const float *W = ns.nodeW + (size_t)max(snode, 0) * 2 * TAPS;
+        for (int t = 0; t < kIsWY; ++t) wys[m * kIsWY + t] = (snode >= 0 && t < TAPS) ? W[t] : 0.f;
+        // A = Wx: region column x holds tap x - ox of the node's x window
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+#pragma unroll
+        for (int k8 = 0; k8 < kIsK / 8; ++k8) {
+            float w[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int tp = 8 * k8 + t - ox;
+                w[t] = (snode >= 0 && tp >= 0 && tp < TAPS) ? W[TAPS + tp] : 0.f;
+            }
+            uint32_t hv[8], lv[8];
+#pragma unroll
+            for (int t = 0; t < 8; t += 2)
+                tf32_split2(make_float2(w[t], w[t + 1]), hv[t], hv[t + 1], lv[t], lv[t + 1]);
+            tc05::st8(tmem + lane_base + 8 * k8, hv);
+            tc05::st8(tmem + lane_base + 32 + 8 * k8, lv);
+        }
+        tc05::wait_st();
+        tc05::fence_before();
+        group_sync<2>();
+        if (m == 0) mbar_arrive(afull);
+        bool lf = false, failed = false;
+        for (int y = 0; y < I::UY; ++y) {
+            const int b = y & 1;
+            if (!tc05::mbar_wait_ns(&rdone[b], (y >> 1) & 1, kSpTcWaitNs)) lf = true;
+            tc05::fence_after();
+            const int t = y - oy;
+            const float wv = (t >= 0 && t < TAPS) ? wys[m * kIsWY + t] : 0.f;
+            const float2 w2 = make_float2(wv, wv);
+            // 16 accumulator columns at a time (fewer live registers)
+#pragma unroll
+            for (int h = 0; h < NCOL / 16; ++h) {
+                float v[16];
+                tc05::ld16(tmem + lane_base + 64 + 32 * b + 16 * h, v);
+                tc05::wait_ld();
+#pragma unroll
+                for (int c = 0; c < 16; c += 2) {
+                    const float2 r = ffma2(w2, make_float2(v[c], v[c + 1]),
+                                           make_float2(acc[16 * h + c], acc[16 * h + c + 1]));
+                    acc[16 * h + c] = r.x;
+                    acc[16 * h + c + 1] = r.y;
+                }
+            }
+            tc05::fence_before();
+            if (group_sync_or<2>(lf)) { failed = true; break; }
+            if (m == 0) mbar_arrive(&dempty[b]);
+        }
         if (failed) *sfail = 1;
     }
     __syncthreads();
     tc05::fence_after();
     if (*sfail) {
         if (tid == 0 && ns.err) *reinterpret_cast<volatile int *>(ns.err) = 1;   // mapped host flag
-    } else if (warp < kSpTcThreads / 32) {
-        constexpr int HC = NCOL / 2;
-        const int m = tid & 127, half = tid >> 7;
-        float v[HC];
-        const uint32_t ta = tmem + ((uint32_t)((warp & 3) * 32) << 16) + half * HC;
-        if (HC == 32) tc05::ld32(ta, *reinterpret_cast<float(*)[32]>(v));
-        else if (HC == 16) tc05::ld16(ta, *reinterpret_cast<float(*)[16]>(v));
-        else tc05::ld8(ta, *reinterpret_cast<float(*)[8]>(v));
-        tc05::wait_ld();
-        const int sv = sidx[m];
-        if (m < cnt && sv >= 0) {
-            const int cb = half * (CC / 2);
-            if (user) {
-                const int j = ns.perm[sv];
+    } else if (tid < kItNodes && tid < cnt && snode >= 0) {
+        if (user) {
+            const int j = ns.perm[snode];
+#pragma unroll
+            for (int q = 0; q < CC; ++q)
+                if (q < ccn) user[(size_t)(c0 + q) * ns.M + j] = make_float2(acc[2 * q], acc[2 * q + 1]);
+        } else {
+            float2 *dst = ks + (size_t)snode * g.nc + c0;
+            if (v16 && ccn == CC) {
+                float4 *d4 = reinterpret_cast<float4 *>(dst);
 #pragma unroll
                 for (int q = 0; q < CC / 2; ++q)
-                    if (cb + q < ccn) user[(size_t)(c0 + cb + q) * ns.M + j] = make_float2(v[2 * q], v[2 * q + 1]);
+                    d4[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
             } else {
-                float2 *dst = ks + (size_t)sv * g.nc + c0 + cb;
-                if (v16 && ccn == CC) {
-                    float4 *d4 = reinterpret_cast<float4 *>(dst);
 #pragma unroll
-                    for (int q = 0; q < CC / 4; ++q)
-                        d4[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-                } else {
-#pragma unroll
-                    for (int q = 0; q < CC / 2; ++q)
-                        if (cb + q < ccn) dst[q] = make_float2(v[2 * q], v[2 * q + 1]);
-                }
+                for (int q = 0; q < CC; ++q)
+                    if (q < ccn) dst[q] = make_float2(acc[2 * q], acc[2 * q + 1]);
             }
         }
     }
@@ -1296,17 +1321,16 @@ template <int TAPS>
 static cgs_status launch_interp_tc_taps(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,
                                         float2 *user, cudaStream_t st)
 {
-    const int ncol = g.nc > 8 ? (g.nc > 16 ? 64 : 32) : 16;
+    const int ncol = g.nc > 8 ? 32 : 16;
     dim3 grd(ns.niwork, (g.nc + ncol / 2 - 1) / (ncol / 2));
 #define CGS_ITC(NCV)                                                                                        \
     do {                                                                                                    \
-        using IT = InterpTc<NCV, TAPS>;                                                                     \
-        CGS_CUDA(cudaFuncSetAttribute(interp_tc05_kernel<NCV, TAPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+        using IT = InterpSep<NCV, TAPS>;                                                                    \
+        CGS_CUDA(cudaFuncSetAttribute(interp_sep_kernel<NCV, TAPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                       IT::SMEM));                                                           \
-        interp_tc05_kernel<NCV, TAPS><<<grd, kSpTcThreads + 32, IT::SMEM, st>>>(g, ns, grid, ks, user);     \
+        interp_sep_kernel<NCV, TAPS><<<grd, kSpTcThreads + 32, IT::SMEM, st>>>(g, ns, grid, ks, user);      \
     } while (0)
-    if (ncol == 64) CGS_ITC(64);
-    else if (ncol == 32) CGS_ITC(32);
+    if (ncol == 32) CGS_ITC(32);
     else CGS_ITC(16);
 #undef CGS_ITC
     CGS_LAUNCH_CHECK();
@@ -2440,7 +2464,7 @@ cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *gri
     if (2 * g.m + 2 > kMaxTaps) { set_error("m too large"); return CGS_ERR_BAD_ARG; }
     const int taps = 2 * g.m + 2;
     if (g.d == 2 && g.imma == 2 && ns.ilist && ns.niwork > 0 && ns.nodeU && ns.nodeW && taps <= 10 &&
-        g.n[0] >= kItBH - 1 + taps && g.n[1] >= kItBW - 1 + taps) {
+        g.n[0] >= kIsBH - 1 + taps && g.n[1] >= kIsBW - 1 + taps) {
         cgs_status r;
         float2 *u = (user && ns.perm) ? user : nullptr;
         prof_begin(PROF_INTERP, st);

@@ -1,8 +1,10 @@
 """2-D gridding on the 5th-generation tensor cores against the CUDA-core
 kernels and the FP64 oracle: spreading (spread_block 64: tcgen05.mma
 kind::tf32 over 8 x 16 grid patches) and interpolation (interp_block 64: up
-to 128 nodes of an 8 x 16 footprint-start bin per CTA), both with TF32-split
-operands, the weight matrix in tensor memory and FP32 accumulation.
+to 128 nodes of an 8 x 16 footprint-start bin per CTA, one MMA per region
+row with the nodes' x windows as A, the y window applied to the row results),
+both with TF32-split operands, the A matrix in tensor memory and FP32
+accumulation.
 
 The two kernels compute the same 100-tap sums (m = 4) in FP32 in different
 orders, so they agree to FP32 rounding (3e-6 relative, as for the mma.sync
