@@ -28,7 +28,7 @@ EXPORTED = [
     "cgs_profile_enable", "cgs_profile_collect", "cgs_nfft2d_trafo_noalloc",
     "cgs_net_num_params", "cgs_net_create", "cgs_net_destroy", "cgs_net_set_weights", "cgs_net_get_weights",
     "cgs_net_forward", "cgs_net_gradients", "cgs_net_train_step", "cgs_solve_fcg", "cgs_normal_apply", "cgs_precond_apply", "cgs_set_frame_sensitivities", "cgs_net_set_conv_kernel",
-    "cgs_get_tuning", "cgs_set_tuning", "cgs_autotune", "cgs_batch_create", "cgs_batch_solve",
+    "cgs_get_tuning", "cgs_set_tuning", "cgs_autotune", "cgs_autotune_cache", "cgs_batch_create", "cgs_batch_solve",
     "cgs_batch_destroy", "cgs_cs_create", "cgs_cs_destroy", "cgs_cs_adjoint", "cgs_cs_df", "cgs_cs_obj",
     "cgs_cs_wavelet",
 ]
@@ -123,6 +123,7 @@ def load(path: str = LIB_PATH):
     L.cgs_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.cgs_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.cgs_autotune.argtypes = [vp, C.POINTER(Tuning), C.POINTER(C.c_double), vp]
+    L.cgs_autotune_cache.argtypes = [C.c_int]
     L.cgs_batch_create.argtypes = [C.POINTER(vp), C.POINTER(vp), C.POINTER(SolveOpts), C.c_int, vp]
     L.cgs_batch_solve.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(SolveReport),
                                   C.POINTER(C.c_double)]
@@ -197,6 +198,11 @@ def _resolve_stream(stream):
 
 def kernel_launches() -> int:
     return int(load().cgs_kernel_launches())
+
+
+def autotune_cache(mode: int):
+    """cgs_autotune_cache: 0 off (cleared), 1 on (cleared; the default), 2 clear"""
+    _check(load().cgs_autotune_cache(int(mode)))
 
 
 def profile_enable(on: bool = True):

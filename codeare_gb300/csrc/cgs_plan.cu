@@ -19,7 +19,9 @@
 #include <complex>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 
 namespace cgs {
 
@@ -2601,6 +2603,41 @@ cgs_status cgs_set_tuning(cgs_plan *p, const cgs_tuning *t)
     return CGS_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// Autotune results by problem class, process-wide: plans with the same grid,
+// cut-off, coil count and sampling density (nodes per grid point, in steps of
+// 2^(1/4)) share the decomposition measured on the first of them.
+struct TuneKey {
+    int n0, n1, m, nc, dens;
+    bool operator<(const TuneKey &o) const
+    {
+        return std::tie(n0, n1, m, nc, dens) < std::tie(o.n0, o.n1, o.m, o.nc, o.dens);
+    }
+};
+std::mutex g_tune_mx;
+std::map<TuneKey, std::pair<cgs_tuning, double>> g_tune_cache;
+bool g_tune_cache_on = true;
+
+TuneKey tune_key(const cgs_plan *p)
+{
+    const double dens = (double)p->M / ((double)p->n[0] * (double)p->n[1]);
+    return TuneKey{p->n[0], p->n[1], p->m, p->nc, (int)std::lround(4.0 * std::log2(std::max(dens, 1e-12)))};
+}
+}  // namespace
+
+extern "C" {
+
+cgs_status cgs_autotune_cache(int mode)
+{
+    if (mode < 0 || mode > 2) { set_error("autotune cache mode must be 0, 1 or 2"); return CGS_ERR_BAD_ARG; }
+    std::lock_guard<std::mutex> lk(g_tune_mx);
+    g_tune_cache.clear();
+    if (mode != 2) g_tune_cache_on = (mode == 1);
+    return CGS_OK;
+}
+
 cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *stream)
 {
     if (!p) { set_error("null plan"); return CGS_ERR_BAD_ARG; }
@@ -2612,6 +2649,27 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
         CGS_TRY(cgs_set_tuning(p, &t));
         if (chosen) *chosen = t;
         return CGS_OK;
+    }
+    const TuneKey key = tune_key(p);
+    {
+        cgs_tuning t{};
+        double t_ms = 0.0;
+        bool hit = false;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mx);
+            auto it = g_tune_cache.find(key);
+            if (g_tune_cache_on && it != g_tune_cache.end()) {
+                t = it->second.first;
+                t_ms = it->second.second;
+                hit = true;
+            }
+        }
+        if (hit) {
+            CGS_TRY(cgs_set_tuning(p, &t));
+            if (chosen) *chosen = t;
+            if (ms) *ms = t_ms;
+            return CGS_OK;
+        }
     }
     CGS_CUDA(cudaSetDevice(p->device));
     cudaStream_t st = pick_stream(p, stream);
@@ -2712,6 +2770,10 @@ cgs_status cgs_autotune(cgs_plan *p, cgs_tuning *chosen, double *ms, void *strea
     CGS_TRY(rebin(p));
     if (chosen) *chosen = best;
     if (ms) *ms = t_int + t_spr;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mx);
+        if (g_tune_cache_on) g_tune_cache[key] = {best, t_int + t_spr};
+    }
     return CGS_OK;
 }
 

@@ -250,6 +250,14 @@ cgs_status cgs_set_tuning(cgs_plan *plan, const cgs_tuning *t);
  * their next use.  2-D plans only. */
 cgs_status cgs_autotune(cgs_plan *plan, cgs_tuning *chosen, double *ms, void *stream);
 
+/* Autotune cache (no reference counterpart): cgs_autotune keeps, per problem
+ * class (grid, cut-off m, coil count and nodes per grid point in steps of
+ * 2^(1/4)), the decomposition it measured, and applies it to later plans of
+ * the same class without timing again (`ms` then reports the cached time).
+ * Process-wide and thread-safe.  mode 0: off (and cleared), 1: on (and
+ * cleared; the default state is on), 2: clear, keep the current state. */
+cgs_status cgs_autotune_cache(int mode);
+
 /* Flexible CG-SENSE with the learned preconditioner (no reference
  * counterpart): standard-mode normal equations (E^H W E + lambda) x = b with
  * z = d . net(d . r) as a variable preconditioner, d = D^-1/2 the exact

@@ -104,6 +104,37 @@ def test_autotune_picks_valid_decomposition(gpu):
     p.close()
 
 
+def test_autotune_cache_reuses_the_class(gpu):
+    """A second plan of the same class (grid, cut-off, coils, nodes per grid
+    point) takes the first one's decomposition without timing again; with the
+    cache off it is timed."""
+    import time
+    from codeare_gb300 import capi, synth
+    N, nc = 96, 16
+    ka = synth.radial2d(80, 192, golden=True)
+    kb = synth.radial2d(80, 192, golden=False)
+    capi.autotune_cache(1)
+    pa, _ = make_plan(N, nc, ka, synth.ramp_weights(ka))
+    pb, _ = make_plan(N, nc, kb, synth.ramp_weights(kb))
+    t0 = time.perf_counter()
+    ta, ms_a = pa.autotune()
+    t_a = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tb, ms_b = pb.autotune()
+    t_b = time.perf_counter() - t0
+    assert tb == ta and ms_b == ms_a and pb.tuning() == ta
+    assert t_b < 0.5 * t_a
+    f0, a0 = nfft_pair(pb, N, nc, kb.shape[0], seed=2)
+    capi.autotune_cache(0)
+    tc, ms_c = pb.autotune()
+    assert ms_c != ms_a            # timed again
+    f1, a1 = nfft_pair(pb, N, nc, kb.shape[0], seed=2)
+    assert rel(f1, f0) < 3e-6 and rel(a1, a0) < 3e-6
+    capi.autotune_cache(1)
+    pa.close()
+    pb.close()
+
+
 def test_new_trajectory_rebuilds_the_solve_graph(gpu):
     """A cached solve graph holds the work lists by address: setting a new
     trajectory must rebuild it (same answer as a fresh plan)."""
