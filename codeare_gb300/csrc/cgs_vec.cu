@@ -48,6 +48,44 @@ __global__ void gather_ks_kernel(const float2 *__restrict__ user, const int *__r
     }
 }
 
+// The same gather with 16-byte accesses (even M and coil count, 16-byte
+// aligned buffers): tiles of 64 nodes x 32 coils; a warp reads a coil's 64
+// consecutive nodes as 32 float4 (512 contiguous bytes) and writes two
+// nodes' 32-coil runs (2 x 256 bytes) per instruction.
+__global__ void gather_ks_v_kernel(const float2 *__restrict__ user, const int *__restrict__ iperm, int64_t M,
+                                   int nc, float2 *__restrict__ ks)
+{
+    __shared__ float2 t[32][65];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t tj_n = (M + 63) / 64, tc_n = (nc + 31) / 32;
+    for (int64_t tile = blockIdx.x; tile < tj_n * tc_n; tile += gridDim.x) {
+        const int64_t j0 = (tile / tc_n) * 64;
+        const int c0 = (int)(tile % tc_n) * 32;
+        const int64_t j = j0 + 2 * lane;
+#pragma unroll
+        for (int k = warp; k < 32; k += 8) {
+            const int c = c0 + k;
+            if (c < nc && j < M) {
+                const float4 v = *reinterpret_cast<const float4 *>(user + (int64_t)c * M + j);
+                t[k][2 * lane] = make_float2(v.x, v.y);
+                t[k][2 * lane + 1] = make_float2(v.z, v.w);
+            }
+        }
+        __syncthreads();
+        const int q = lane & 15;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int jj = 16 * r + 2 * warp + (lane >> 4);
+            const int c = c0 + 2 * q;
+            if (j0 + jj < M && c < nc) {
+                const float2 a = t[2 * q][jj], b2 = t[2 * q + 1][jj];
+                *reinterpret_cast<float4 *>(ks + (int64_t)iperm[j0 + jj] * nc + c) = make_float4(a.x, a.y, b2.x, b2.y);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void scatter_ks_kernel(const float2 *__restrict__ ks, const int *__restrict__ perm,
                                   int64_t M, int nc, float2 *__restrict__ user)
 {
@@ -922,6 +960,12 @@ cgs_status launch_gather_ks(const float2 *user, const int *iperm, int64_t M, int
                             cudaStream_t st)
 {
     if (M * nc == 0) return CGS_OK;
+    if ((M & 1) == 0 && (nc & 1) == 0 && ((uintptr_t)user & 15) == 0 && ((uintptr_t)ks & 15) == 0) {
+        const int64_t tiles = ((M + 63) / 64) * ((nc + 31) / 32);
+        gather_ks_v_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 16), 256, 0, st>>>(user, iperm, M, nc, ks);
+        CGS_LAUNCH_CHECK();
+        return CGS_OK;
+    }
     const int64_t tiles = ((M + 31) / 32) * ((nc + 31) / 32);
     gather_ks_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 32), dim3(32, 8), 0, st>>>(user, iperm, M, nc, ks);
     CGS_LAUNCH_CHECK();
