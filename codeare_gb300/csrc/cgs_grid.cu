@@ -1507,7 +1507,29 @@ static cgs_status launch_interp_mma_taps(const GridGeom &g, const NodeSet &ns, c
     }
 }
 
-// sum the partial slots of split patches in slot order and store them
+// sum the partial slots of split patches in slot order and store them; with
+// an even coil count two coils per thread (16-byte loads and stores)
+__global__ void patch_reduce2_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
+                                     float2 *__restrict__ grid)
+{
+    const int nh = g.nc / 2, npt = ps.ph * ps.pw;
+    const int64_t total = (int64_t)ps.nmulti * npt * nh;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int c = 2 * (int)(e % nh);
+        const int pt = (int)((e / nh) % npt);
+        const int4 mu = ps.multi[e / ((int64_t)npt * nh)];
+        const int py = (mu.x / ps.npx) * ps.ph + pt / ps.pw;
+        const int px = (mu.x % ps.npx) * ps.pw + pt % ps.pw;
+        if (py >= g.n[0] || px >= g.n[1]) continue;
+        float4 s4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int k = 0; k < mu.z; ++k) {
+            const float4 v = *reinterpret_cast<const float4 *>(&ps.partial[((size_t)(mu.y + k) * npt + pt) * g.nc + c]);
+            s4.x += v.x; s4.y += v.y; s4.z += v.z; s4.w += v.w;
+        }
+        *reinterpret_cast<float4 *>(&grid[((size_t)py * g.n[1] + px) * g.nc + c]) = s4;
+    }
+}
+
 __global__ void patch_reduce_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
                                     float2 *__restrict__ grid)
 {
@@ -2732,9 +2754,11 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
 #undef CGS_SPT
     CGS_LAUNCH_CHECK();
     if (ps.nmulti > 0) {
-        const int64_t total = (int64_t)ps.nmulti * ps.ph * ps.pw * g.nc;
+        const bool v2 = (g.nc % 2) == 0;
+        const int64_t total = (int64_t)ps.nmulti * ps.ph * ps.pw * (v2 ? g.nc / 2 : g.nc);
         const int64_t blocks = std::min<int64_t>((total + 255) / 256, 152 * 16);
-        patch_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, ps, grid);
+        if (v2) patch_reduce2_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, ps, grid);
+        else patch_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, ps, grid);
         CGS_LAUNCH_CHECK();
     }
     prof_end(PROF_SPREAD, st);
