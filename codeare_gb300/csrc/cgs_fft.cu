@@ -630,7 +630,18 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
     const int64_t o = ((blk / nib) << (LOGB - logBI)) + (b >> logBI);
     const int64_t i = ((blk % nib) << logBI) + (b & ((1 << logBI) - 1));
     const bool col_ok = (o < p.outer) && (i < p.inner);
-    for (int t = threadIdx.x; t < N; t += kThreads) tw[t] = p.tw[t];
+    // the twiddle table comes in by cp.async, so the column loads below are
+    // issued without waiting for it (it is waited for before the barrier that
+    // precedes the first butterfly)
+    if constexpr (N % 2 == 0) {
+        for (int t = threadIdx.x; t < N / 2; t += kThreads) {
+            const unsigned d = (unsigned)__cvta_generic_to_shared(tw + 2 * t);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(p.tw + 2 * t) : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    } else {
+        for (int t = threadIdx.x; t < N; t += kThreads) tw[t] = p.tw[t];
+    }
     float dcol = 1.f;  // outer-dimension deapodisation of this column (fused passes)
     if (col_ok && (p.load_mode == LOAD_IMAGE || p.store_mode == STORE_DEAPOD)) {
         if (p.deap_o1) dcol *= p.deap_o1[o % p.o1_len];
@@ -671,6 +682,7 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
                 v[u] = cscale(x, sc);
             }
         }
+        if constexpr (N % 2 == 0) asm volatile("cp.async.wait_group 0;" ::: "memory");
         if constexpr (ct_reg_ok<N, LOGB>()) {
             // The first pass takes its inputs from these registers.  Without a
             // Toeplitz round the last pass leaves its outputs in them: row
