@@ -1364,19 +1364,31 @@ interp_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ No
                   const float2 *__restrict__ grid, float2 *__restrict__ ks, float2 *__restrict__ user)
 {
     using I = InterpMma<NT, TAPS>;
-    constexpr int U = I::U, KP = I::KP, CC = 4 * NT, WS = 2 * TAPS, PL = I::PL;
+    constexpr int U = I::U, KP = I::KP, CC = 4 * NT, PL = I::PL;
     extern __shared__ float4 smem4[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wi = blockIdx.x * 8 + warp;
     if (wi >= ns.niwork) return;
     float *wpad = reinterpret_cast<float *>(reinterpret_cast<char *>(smem4) + warp * I::warp_bytes);  // [16][2][PL]
     int *spt = reinterpret_cast<int *>(wpad + kInterpGroup * 2 * PL);                                // [KP] grid points
+    // the work item's padded window rows ([16][wy, wx][PL]) and node offsets,
+    // precomputed once per trajectory (interp_windows_kernel), come in by
+    // cp.async without waiting on the node list
+    {
+        const float *src = ns.iwin + (size_t)wi * kInterpGroup * 2 * PL;
+        for (int q = lane; q < kInterpGroup * 2 * PL / 4; q += 32) cp_async16(wpad + 4 * q, src + 4 * q);
+        cp_async_commit();
+    }
+    int s_l = -1, oy_l = 0, ox_l = 0;
+    if (lane < kInterpGroup) {
+        const int4 mt = ns.imeta[(size_t)wi * kInterpGroup + lane];
+        s_l = mt.x; oy_l = mt.y; ox_l = mt.z;
+    }
     const int4 wk = ns.iwork[wi];                           // {bin, first, count <= 16, 0}
     const int c0 = blockIdx.y * CC;
     const int ccn = min(CC, g.nc - c0);
     const int n0 = g.n[0], n1 = g.n[1];
     const int by0 = (wk.x / ns.ibx) * 4, bx0 = (wk.x % ns.ibx) * 4;
-    const int cnt = wk.z;
     // region points (rows and columns wrap once: n0, n1 >= U); -1 past the region
     for (int q = lane; q < KP; q += 32) {
         int pt = -1;
@@ -1388,25 +1400,7 @@ interp_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ No
         }
         spt[q] = pt;
     }
-    // the group's padded window rows and footprint offsets (relative to the bin)
-    int s_l = -1, oy_l = 0, ox_l = 0;
-    if (lane < kInterpGroup) {
-        float *wy = wpad + lane * 2 * PL, *wx = wy + PL;
-        if (lane < cnt) {
-            s_l = ns.ilist[wk.y + lane];
-            const int2 u = ns.nodeU[s_l];
-            oy_l = u.x - by0;
-            ox_l = u.y - bx0;
-            const float *W = ns.nodeW + (size_t)s_l * WS;
-            for (int i = 0; i < PL; ++i) {
-                const int t = i - 3;
-                wy[i] = (t >= 0 && t < TAPS) ? W[t] : 0.f;
-                wx[i] = (t >= 0 && t < TAPS) ? W[TAPS + t] : 0.f;
-            }
-        } else {
-            for (int i = 0; i < PL; ++i) wy[i] = wx[i] = 0.f;
-        }
-    }
+    cp_async_wait<0>();
     __syncwarp();
     const int gq = lane >> 2, tq = lane & 3;
     const int na = gq, nb = gq + 8;
@@ -1456,14 +1450,14 @@ interp_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ No
     // so each coil row's stores stay close to sector-dense.
     const int sa = __shfl_sync(0xffffffffu, s_l, na), sb = __shfl_sync(0xffffffffu, s_l, nb);
     if (user) {
-        const int ja = na < cnt ? ns.perm[sa] : 0, jb = nb < cnt ? ns.perm[sb] : 0;
+        const int ja = sa >= 0 ? ns.perm[sa] : 0, jb = sb >= 0 ? ns.perm[sb] : 0;
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
             const int c = 4 * t + tq;
             if (c < ccn) {
                 float2 *row = user + (size_t)(c0 + c) * ns.M;
-                if (na < cnt) row[ja] = make_float2(acc[t][0], acc[t][1]);
-                if (nb < cnt) row[jb] = make_float2(acc[t][2], acc[t][3]);
+                if (sa >= 0) row[ja] = make_float2(acc[t][0], acc[t][1]);
+                if (sb >= 0) row[jb] = make_float2(acc[t][2], acc[t][3]);
             }
         }
         return;
@@ -1472,10 +1466,42 @@ interp_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ No
     for (int t = 0; t < NT; ++t) {
         const int c = 4 * t + tq;
         if (c < ccn) {
-            if (na < cnt) ks[(size_t)sa * g.nc + c0 + c] = make_float2(acc[t][0], acc[t][1]);
-            if (nb < cnt) ks[(size_t)sb * g.nc + c0 + c] = make_float2(acc[t][2], acc[t][3]);
+            if (sa >= 0) ks[(size_t)sa * g.nc + c0 + c] = make_float2(acc[t][0], acc[t][1]);
+            if (sb >= 0) ks[(size_t)sb * g.nc + c0 + c] = make_float2(acc[t][2], acc[t][3]);
         }
     }
+}
+
+// one warp per interpolation work item: the padded window rows and footprint
+// offsets that interp_mma_kernel would build itself, in its shared-memory
+// layout ([16 nodes][wy, wx][PL]) and {node, oy, ox, 0} per node
+template <int TAPS>
+__global__ void interp_windows_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ NodeSet ns,
+                                      float *__restrict__ iwin, int4 *__restrict__ imeta)
+{
+    constexpr int PL = InterpMma<1, TAPS>::PL, WS = 2 * TAPS;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wi = blockIdx.x * 8 + warp;
+    if (wi >= ns.niwork || lane >= kInterpGroup) return;
+    const int4 wk = ns.iwork[wi];
+    const int by0 = (wk.x / ns.ibx) * 4, bx0 = (wk.x % ns.ibx) * 4;
+    float *wy = iwin + ((size_t)wi * kInterpGroup + lane) * 2 * PL, *wx = wy + PL;
+    int sv = -1, oy = 0, ox = 0;
+    if (lane < wk.z) {
+        sv = ns.ilist[wk.y + lane];
+        const int2 u = ns.nodeU[sv];
+        oy = u.x - by0;
+        ox = u.y - bx0;
+        const float *W = ns.nodeW + (size_t)sv * WS;
+        for (int i = 0; i < PL; ++i) {
+            const int t = i - 3;
+            wy[i] = (t >= 0 && t < TAPS) ? W[t] : 0.f;
+            wx[i] = (t >= 0 && t < TAPS) ? W[TAPS + t] : 0.f;
+        }
+    } else {
+        for (int i = 0; i < PL; ++i) wy[i] = wx[i] = 0.f;
+    }
+    imeta[(size_t)wi * kInterpGroup + lane] = make_int4(sv, oy, ox, 0);
 }
 
 template <int NT, int TAPS>
@@ -2478,6 +2504,21 @@ cgs_status launch_interp2_taps(const GridGeom &g, const NodeSet &ns, const float
     return CGS_OK;
 }
 
+cgs_status launch_interp_windows(const GridGeom &g, const NodeSet &ns, float *iwin, int4 *imeta, cudaStream_t st)
+{
+    const int taps = 2 * g.m + 2;
+    if (ns.niwork == 0 || g.d != 2 || taps > 10 || (taps & 1)) return CGS_OK;
+    const unsigned blocks = (unsigned)((ns.niwork + 7) / 8);
+    switch (taps) {
+        case 4: interp_windows_kernel<4><<<blocks, 256, 0, st>>>(g, ns, iwin, imeta); break;
+        case 6: interp_windows_kernel<6><<<blocks, 256, 0, st>>>(g, ns, iwin, imeta); break;
+        case 8: interp_windows_kernel<8><<<blocks, 256, 0, st>>>(g, ns, iwin, imeta); break;
+        default: interp_windows_kernel<10><<<blocks, 256, 0, st>>>(g, ns, iwin, imeta); break;
+    }
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
 cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,
                          cudaStream_t st, float2 *user, bool *wrote_user)
 {
@@ -2500,7 +2541,7 @@ cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *gri
         if (r == CGS_OK && wrote_user) *wrote_user = (u != nullptr);
         return r;
     }
-    if (g.d == 2 && g.imma == 1 && ns.ilist && ns.niwork > 0 && ns.nodeU && ns.nodeW && taps <= 10 &&
+    if (g.d == 2 && g.imma == 1 && ns.ilist && ns.niwork > 0 && ns.iwin && ns.imeta && taps <= 10 &&
         g.n[0] >= 3 + taps && g.n[1] >= 3 + taps) {
         cgs_status r;
         float2 *u = (user && ns.perm) ? user : nullptr;

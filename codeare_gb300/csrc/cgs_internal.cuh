@@ -161,6 +161,11 @@ struct NodeSet {
     const int4 *nodeU3;
     int iby;            // 3-D: bins per grid column (bins per plane = iby * ibx)
     int *err;           // set by a tensor-core kernel whose MMA wait ran out (nullable)
+    // 2-D mma.sync interpolation: per work item its nodes' padded window rows
+    // ([16][2][taps + 7] floats) and {node, footprint offsets in the bin}
+    // (nullable: the kernel then builds them itself)
+    const float *iwin;
+    const int4 *imeta;
 };
 constexpr int kW3 = 32;  // floats per node in the 3-D window table
 
@@ -221,6 +226,8 @@ bool grid3_mma_ok(const GridGeom &g);
 // With `user` (the caller's layout: coil-major, trajectory order) the
 // tensor-core kernel writes there directly and sets *wrote_user; otherwise
 // the result is in ks and the caller scatters it.
+// the 2-D mma.sync interpolation's per-work-item window blocks (once per trajectory)
+cgs_status launch_interp_windows(const GridGeom &g, const NodeSet &ns, float *iwin, int4 *imeta, cudaStream_t st);
 cgs_status launch_interp(const GridGeom &g, const NodeSet &ns, const float2 *grid, float2 *ks,
                          cudaStream_t st, float2 *user = nullptr, bool *wrote_user = nullptr);
 // grid[...][c] += sum_s phi * (w_s if weighted) * ks[s][c]; grid must be zeroed first

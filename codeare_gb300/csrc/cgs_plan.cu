@@ -215,6 +215,9 @@ struct cgs_plan {
     int *ilist = nullptr;
     int4 *iwork = nullptr;
     int niwork = 0, ibx = 0;
+    // mma.sync interpolation: per work item the nodes' padded window rows and offsets
+    float *iwin = nullptr;
+    int4 *imeta = nullptr;
     // 3-D tensor-core gridding: wrapped footprint starts per node (nodeW then
     // holds kW3 window weights per node, ilist / iwork the 4 x 4 x 4 bins,
     // pentries / pwork / pmulti the 4 x 4 x 4 patch lists)
@@ -313,7 +316,7 @@ int *tc_flag();
 NodeSet node_set(const cgs_plan *p)
 {
     NodeSet ns{p->M, p->nodes, p->perm, p->w, p->nwork, p->work, p->nodeU, p->nodeW, p->ilist, p->iwork,
-               p->niwork, p->ibx, p->nodeU3, p->iby, tc_flag()};
+               p->niwork, p->ibx, p->nodeU3, p->iby, tc_flag(), p->iwin, p->imeta};
     return ns;
 }
 
@@ -592,14 +595,26 @@ cgs_status build_ibins(cgs_plan *p, const std::vector<int> &cc, const std::vecto
             work.push_back(make_int4(b, s0, std::min(group, cnt[b + 1] - s0), 0));
     dev_free(p->ilist);
     dev_free(p->iwork);
+    dev_free(p->iwin);
+    dev_free(p->imeta);
     p->ilist = nullptr;
     p->iwork = nullptr;
+    p->iwin = nullptr;
+    p->imeta = nullptr;
     CGS_TRY(dev_alloc(&p->ilist, (size_t)M));
     CGS_TRY(dev_alloc(&p->iwork, std::max<size_t>(work.size(), 1)));
     CGS_CUDA(cudaMemcpy(p->ilist, list.data(), sizeof(int) * M, cudaMemcpyHostToDevice));
     if (!work.empty()) CGS_CUDA(cudaMemcpy(p->iwork, work.data(), sizeof(int4) * work.size(), cudaMemcpyHostToDevice));
     p->niwork = (int)work.size();
     p->ibx = nbx;
+    const int taps = 2 * m + 2;
+    if (!tc && !work.empty() && taps <= 10 && p->nodeU && p->nodeW) {
+        // the mma.sync kernel's window blocks: 16 nodes x 2 rows of taps + 7 floats per item
+        CGS_TRY(dev_alloc(&p->iwin, work.size() * kInterpGroup * 2 * (size_t)(taps + 7)));
+        CGS_TRY(dev_alloc(&p->imeta, work.size() * kInterpGroup));
+        CGS_TRY(launch_interp_windows(p->geom, node_set(p), p->iwin, p->imeta, p->stream));
+        CGS_CUDA(cudaStreamSynchronize(p->stream));
+    }
     return CGS_OK;
 }
 
@@ -760,10 +775,11 @@ cgs_status build_grid3(cgs_plan *p, const std::vector<int> &cc, const std::vecto
     const int n0 = p->n[0], n1 = p->n[1], n2 = p->n[2], m = p->m, taps = 2 * m + 2;
     const int64_t M = p->M;
     auto wrap = [](int v, int n) { v %= n; return v < 0 ? v + n : v; };
-    for (void *b : {(void *)p->nodeU3, (void *)p->nodeW, (void *)p->ilist, (void *)p->iwork, (void *)p->pentries,
+    for (void *b : {(void *)p->iwin, (void *)p->imeta, (void *)p->nodeU3, (void *)p->nodeW, (void *)p->ilist, (void *)p->iwork, (void *)p->pentries,
                     (void *)p->pwork, (void *)p->pmulti, (void *)p->ppartial, (void *)p->pw16, (void *)p->ps16,
                     (void *)p->pstage}) dev_free(b);
     p->nodeU3 = nullptr; p->nodeW = nullptr; p->ilist = nullptr; p->iwork = nullptr;
+    p->iwin = nullptr; p->imeta = nullptr;
     p->pentries = nullptr; p->pwork = nullptr; p->pmulti = nullptr; p->ppartial = nullptr;
     p->pw16 = nullptr; p->ps16 = nullptr; p->pstage = nullptr;
     p->niwork = 0;
@@ -1816,6 +1832,7 @@ static cgs_status build_host_chunks(cgs_plan *p, HostChunks &h, int C)
         c->pentries = p->pentries; c->pwork = p->pwork; c->pmulti = p->pmulti;
         c->pw16 = p->pw16; c->ps16 = p->ps16; c->pstage = p->pstage;
         c->ilist = p->ilist; c->iwork = p->iwork; c->niwork = p->niwork; c->ibx = p->ibx;
+        c->iwin = p->iwin; c->imeta = p->imeta;
         c->nodeU3 = p->nodeU3; c->iby = p->iby;
         c->tune = p->tune;
         c->tune.interp_coils = c->tune.spread_coils = 0;
@@ -1880,9 +1897,10 @@ cgs_status cgs_plan_destroy(cgs_plan *p)
         p->nodeU = nullptr; p->nodeW = nullptr; p->pentries = nullptr; p->pwork = nullptr; p->pmulti = nullptr;
         p->ilist = nullptr; p->iwork = nullptr; p->nodeU3 = nullptr;
         p->pw16 = nullptr; p->ps16 = nullptr; p->pstage = nullptr;
+        p->iwin = nullptr; p->imeta = nullptr;
     }
     void *bufs[] = {p->tw[0], p->tw[1], p->tw[2], p->deap[0], p->deap[1], p->deap[2], p->nodes, p->perm, p->iperm,
-                    p->w, p->work, p->nodeU, p->nodeW, p->pentries, p->pwork, p->pmulti, p->ppartial, p->pw16, p->ps16, p->pstage, p->ilist, p->iwork, p->nodeU3, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
+                    p->w, p->work, p->nodeU, p->nodeW, p->pentries, p->pwork, p->pmulti, p->ppartial, p->pw16, p->ps16, p->pstage, p->ilist, p->iwork, p->iwin, p->imeta, p->nodeU3, p->mask, p->imap, p->sens, p->grid, p->t1, p->t2, p->ksY, p->ksR, p->ksV,
                     p->cF, p->cP, p->cZ, p->vX, p->vR, p->vP, p->vQ, p->ioA, p->ioB, p->partial, p->dots,
                     p->active, p->sc, p->fpart, p->ftick};
     for (void *b : bufs) dev_free(b);
@@ -2012,10 +2030,11 @@ cgs_status cgs_set_kspace(cgs_plan *p, const float *k_in)
     } else if (grid3_mma_ok(p->geom) && !(p->tune.spread_block == 1 && p->tune.interp_block == 1)) {
         CGS_TRY(build_grid3(p, cc, perm));
     } else {
-        for (void *b : {(void *)p->nodeU3, (void *)p->nodeW, (void *)p->ilist, (void *)p->iwork, (void *)p->pentries,
+        for (void *b : {(void *)p->iwin, (void *)p->imeta, (void *)p->nodeU3, (void *)p->nodeW, (void *)p->ilist, (void *)p->iwork, (void *)p->pentries,
                         (void *)p->pwork, (void *)p->pmulti, (void *)p->ppartial, (void *)p->pw16, (void *)p->ps16,
                         (void *)p->pstage}) dev_free(b);
         p->nodeU3 = nullptr; p->nodeW = nullptr; p->ilist = nullptr; p->iwork = nullptr;
+        p->iwin = nullptr; p->imeta = nullptr;
         p->pentries = nullptr; p->pwork = nullptr; p->pmulti = nullptr; p->ppartial = nullptr;
         p->pw16 = nullptr; p->ps16 = nullptr; p->pstage = nullptr;
         p->niwork = 0;
