@@ -642,6 +642,10 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
     } else {
         for (int t = threadIdx.x; t < N; t += kThreads) tw[t] = p.tw[t];
     }
+    // the twiddles are plan constants; everything below uses the previous
+    // kernel's output or buffers it may still read
+    pdl_wait();
+    pdl_trigger();
     float dcol = 1.f;  // outer-dimension deapodisation of this column (fused passes)
     if (col_ok && (p.load_mode == LOAD_IMAGE || p.store_mode == STORE_DEAPOD)) {
         if (p.deap_o1) dcol *= p.deap_o1[o % p.o1_len];
@@ -777,9 +781,8 @@ cgs_status launch_ct(const AxisPass &p, cudaStream_t st)
                                       (int)smem));
         attr_done(attr_devs);
     }
-    if (p.sign < 0) axis_fft_ct_kernel<N, LOGB, -1><<<(unsigned)nblocks, kThreads, smem, st>>>(p, logBI, nib);
-    else axis_fft_ct_kernel<N, LOGB, +1><<<(unsigned)nblocks, kThreads, smem, st>>>(p, logBI, nib);
-    CGS_LAUNCH_CHECK();
+    CGS_CUDA(launch_pdl(p.sign < 0 ? axis_fft_ct_kernel<N, LOGB, -1> : axis_fft_ct_kernel<N, LOGB, +1>,
+                        dim3((unsigned)nblocks), dim3(kThreads), smem, st, p, logBI, nib));
     return CGS_OK;
 }
 

@@ -928,6 +928,10 @@ spread_tc05_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ P
         cp_async_commit();
         cp_async_wait<0>();
         builders_sync();
+        // the weight blocks are plan constants; the samples and the grid are
+        // the previous kernels' data
+        pdl_wait();
+        pdl_trigger();
         if (nst > 0 && tid < 128) fetch_v(0);
         cp_async_commit();
         if (nst > 1 && tid < 128) fetch_v(1);
@@ -1402,6 +1406,10 @@ interp_mma_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ No
     }
     cp_async_wait<0>();
     __syncwarp();
+    // the window blocks and work lists are plan constants; the grid is the
+    // previous kernel's output
+    pdl_wait();
+    pdl_trigger();
     const int gq = lane >> 2, tq = lane & 3;
     const int na = gq, nb = gq + 8;
     const int oya = __shfl_sync(0xffffffffu, oy_l, na), oxa = __shfl_sync(0xffffffffu, ox_l, na);
@@ -1512,8 +1520,7 @@ static cgs_status launch_interp_mma_t(const GridGeom &g, const NodeSet &ns, cons
     CGS_CUDA(cudaFuncSetAttribute(interp_mma_kernel<NT, TAPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)I::smem));
     dim3 grd((ns.niwork + 7) / 8, (g.nc + 4 * NT - 1) / (4 * NT));
-    interp_mma_kernel<NT, TAPS><<<grd, 256, I::smem, st>>>(g, ns, grid, ks, user);
-    CGS_LAUNCH_CHECK();
+    CGS_CUDA(launch_pdl(interp_mma_kernel<NT, TAPS>, grd, dim3(256), I::smem, st, g, ns, grid, ks, user));
     return CGS_OK;
 }
 
@@ -1538,6 +1545,8 @@ static cgs_status launch_interp_mma_taps(const GridGeom &g, const NodeSet &ns, c
 __global__ void patch_reduce2_kernel(const __grid_constant__ GridGeom g, const __grid_constant__ PatchSet ps,
                                      float2 *__restrict__ grid)
 {
+    pdl_wait();
+    pdl_trigger();
     const int nh = g.nc / 2, npt = ps.ph * ps.pw;
     const int64_t total = (int64_t)ps.nmulti * npt * nh;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
@@ -2714,7 +2723,8 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
     do {                                                                                                  \
         CGS_CUDA(cudaFuncSetAttribute(spread_tc05_kernel<NCV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                       SpreadTc<NCV>::SMEM));                                              \
-        spread_tc05_kernel<NCV><<<grt, kSpTcThreads + 32, SpreadTc<NCV>::SMEM, st>>>(g, ps, ks, dens, weighted, grid); \
+        CGS_CUDA(launch_pdl(spread_tc05_kernel<NCV>, grt, dim3(kSpTcThreads + 32), (size_t)SpreadTc<NCV>::SMEM, st, g, ps, \
+                            ks, dens, weighted, grid));                                                   \
     } while (0)
         if (!ps.pw16 || !ps.ps16 || !ps.pstage) { set_error("tcgen05 spreading blocks missing"); return CGS_ERR_STATE; }
         if (ncol == 64) CGS_SPTC(64);
@@ -2798,7 +2808,7 @@ cgs_status launch_spread_patch(const GridGeom &g, const PatchSet &ps, const floa
         const bool v2 = (g.nc % 2) == 0;
         const int64_t total = (int64_t)ps.nmulti * ps.ph * ps.pw * (v2 ? g.nc / 2 : g.nc);
         const int64_t blocks = std::min<int64_t>((total + 255) / 256, 152 * 16);
-        if (v2) patch_reduce2_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, ps, grid);
+        if (v2) CGS_CUDA(launch_pdl(patch_reduce2_kernel, dim3((unsigned)blocks), dim3(256), 0, st, g, ps, grid));
         else patch_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, ps, grid);
         CGS_LAUNCH_CHECK();
     }

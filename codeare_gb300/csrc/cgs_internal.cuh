@@ -121,6 +121,43 @@ struct AxisPass {
 
 cgs_status launch_axis_pass(const AxisPass &p, cudaStream_t st);
 
+// Programmatic dependent launch.  A kernel launched by launch_pdl may start
+// while the previous kernel on the stream finishes: it first does the work
+// that reads only plan constants (twiddles, window tables, work lists, shared
+// and tensor memory set-up), then pdl_wait() before it reads or writes any
+// buffer that earlier work uses (the wait returns once the previous grid has
+// completed and its memory is visible), and pdl_trigger() lets the next such
+// kernel start.  Launched the ordinary way both are no-ops.  Stream capture
+// and the legacy default stream get ordinary launches.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e;
+    if (st == nullptr || cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        kern<<<grid, block, smem, st>>>(args...);
+        e = cudaGetLastError();
+    } else {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = grid;
+        cfg.blockDim = block;
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, kern, args...);
+    }
+    if (e == cudaSuccess) count_launch();   // the library's own launch count, as for CGS_LAUNCH_CHECK
+    return e;
+}
+
 // ---------------------------------------------------------------------------
 // Gridding (KB interpolation / spreading) over tiles of the oversampled grid
 // ---------------------------------------------------------------------------

@@ -56,6 +56,8 @@ __global__ void gather_ks_v_kernel(const float2 *__restrict__ user, const int *_
                                    int nc, float2 *__restrict__ ks)
 {
     __shared__ float2 t[32][65];
+    pdl_wait();
+    pdl_trigger();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t tj_n = (M + 63) / 64, tc_n = (nc + 31) / 32;
     for (int64_t tile = blockIdx.x; tile < tj_n * tc_n; tile += gridDim.x) {
@@ -962,8 +964,8 @@ cgs_status launch_gather_ks(const float2 *user, const int *iperm, int64_t M, int
     if (M * nc == 0) return CGS_OK;
     if ((M & 1) == 0 && (nc & 1) == 0 && ((uintptr_t)user & 15) == 0 && ((uintptr_t)ks & 15) == 0) {
         const int64_t tiles = ((M + 63) / 64) * ((nc + 31) / 32);
-        gather_ks_v_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 16), 256, 0, st>>>(user, iperm, M, nc, ks);
-        CGS_LAUNCH_CHECK();
+        CGS_CUDA(launch_pdl(gather_ks_v_kernel, dim3((unsigned)std::min<int64_t>(tiles, 152 * 16)), dim3(256), 0, st,
+                            user, iperm, M, nc, ks));
         return CGS_OK;
     }
     const int64_t tiles = ((M + 31) / 32) * ((nc + 31) / 32);
