@@ -126,8 +126,13 @@ def test_autotune_cache_reuses_the_class(gpu):
     assert t_b < 0.5 * t_a
     f0, a0 = nfft_pair(pb, N, nc, kb.shape[0], seed=2)
     capi.autotune_cache(0)
+    t0 = time.perf_counter()
     tc, ms_c = pb.autotune()
-    assert ms_c != ms_a            # timed again
+    t_c = time.perf_counter() - t0
+    # timed again: every candidate is rebinned and launched, far slower than
+    # the cache hit (the milliseconds themselves may repeat exactly: the
+    # event timer's resolution is coarse against these small kernels)
+    assert t_c > 2 * t_b and ms_c > 0
     f1, a1 = nfft_pair(pb, N, nc, kb.shape[0], seed=2)
     assert rel(f1, f0) < 3e-6 and rel(a1, a0) < 3e-6
     capi.autotune_cache(1)
