@@ -61,6 +61,16 @@ def algorithmic_bytes(N, n, M, d, nc):
     return b
 
 
+def pruned_fft_bytes(N, n, nc):
+    """Bytes the four 2-D FFT passes of a forward + adjoint step must move
+    when the zero rows of the padded image are neither read nor transformed
+    and the cropped rows are not written: forward along x (N rows: image in,
+    N x n out), forward along y (N x n in, n x n out), inverse along y (n x n
+    in, N x n out), inverse along x (N x n in, image out)."""
+    img, mid, grid = nc * N * N * 8, nc * N * n * 8, nc * n * n * 8
+    return 2 * (img + mid) + 2 * (mid + grid)
+
+
 def workload_data(seed=20261204):
     from codeare_gb300 import synth
     k = synth.radial2d(SPOKES, SAMPLES, golden=True)
@@ -665,6 +675,11 @@ def run_ours(args):
         pass
     for v in per_kernel.values():  # each kernel against the same HBM denominator
         v["frac_of_hbm"] = v["GBps"] / hbm
+    if "fft" in per_kernel:  # the same passes on the bytes a pruned transform must move
+        f = per_kernel["fft"]
+        f["pruned_bytes_per_launch"] = pruned_fft_bytes(N, n, NC) / 4.0
+        f["GBps_pruned"] = f["pruned_bytes_per_launch"] / (f["avg_ms"] * 1e-3) / 1e9
+        f["frac_of_hbm_pruned"] = f["GBps_pruned"] / hbm
     roofline = None
     if dom:
         a = per_kernel[dom]["GBps"]

@@ -18,6 +18,15 @@ def test_byte_model_256_32coils():
     assert b["step"] == 2 * b["interp"] + 2 * b["fft"] + 2 * (img + grid) == 679370752
 
 
+def test_pruned_fft_bytes_256_32coils():
+    """The four passes of a pruned 512^2 transform pair over 32 coils move
+    16.8 + 33.6, 33.6 + 67.1, 67.1 + 33.6 and 33.6 + 16.8 MB."""
+    sys.path.insert(0, ROOT)
+    import bench
+    img, mid, grid = 32 * 256 * 256 * 8, 32 * 256 * 512 * 8, 32 * 512 * 512 * 8
+    assert bench.pruned_fft_bytes(256, 512, 32) == (img + mid) + (mid + grid) + (grid + mid) + (mid + img) == 301989888
+
+
 def test_reference_arm_json_line():
     env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
