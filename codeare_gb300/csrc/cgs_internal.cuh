@@ -333,7 +333,7 @@ struct FCGScalars {
 cgs_status launch_fcg_kernels(int which, FCGScalars *fs, float2 *x, float2 *r, float2 *rold, float2 *p,
                               const float2 *q, float2 *z, int64_t n, cudaGraphConditionalHandle h,
                               cudaStream_t st);
-enum FcgOp { FCG_INIT = 0, FCG_UPDATE_XR = 1, FCG_DECIDE = 2, FCG_SELECT = 3, FCG_BETA = 4, FCG_P = 5, FCG_CHECK = 6 };
+enum FcgOp { FCG_INIT = 0, FCG_SELECT = 3, FCG_BETA = 4, FCG_P = 5, FCG_CHECK = 6 };
 // flexible-CG loop with a fixed preconditioner (mode 0 plain, 1 Jacobi):
 // x, r update and rr (mode 0 also beta and the loop test); z = d^2 r, zr, beta, loop test
 cgs_status launch_fcg_xr_rr(FCGScalars *fs, float2 *x, float2 *r, const float2 *p, const float2 *q, int64_t n,
@@ -368,6 +368,17 @@ cgs_status launch_circ_kinv(const float *spec, const FCGScalars *fs, int64_t P, 
 // out = dx . x + (y ? (dy ? dy . y : y) : 0), real per-pixel factors
 cgs_status launch_scale_add(float2 *out, const float2 *x, const float *dx, const float2 *y, const float *dy,
                             int64_t n, cudaStream_t st);
+// out = d . in and *nrm = sum |out|^2 (partial: dot_blocks() doubles)
+cgs_status launch_diag_scale_nrm(const float2 *in, const float *d, int64_t n, float2 *out, double *partial,
+                                 unsigned int *ticket, double *nrm, cudaStream_t st);
+// flexible-CG loop with a changing preconditioner (modes 2 and 4), two fused
+// steps around z = M(r): x, rold, r update with rr and the stall bookkeeping;
+// then z = r after a fallback, zr and zro (partials in partial_a and partial_b,
+// dot_blocks() each) and the Polak-Ribiere beta
+cgs_status launch_fcg_xr_rr_decide(FCGScalars *fs, float2 *x, float2 *r, float2 *rold, const float2 *p,
+                                   const float2 *q, int64_t n, double *partial, unsigned int *ticket, cudaStream_t st);
+cgs_status launch_fcg_zsel_dots_beta(FCGScalars *fs, float2 *z, const float2 *r, const float2 *rold, int64_t n,
+                                     double *partial_a, double *partial_b, unsigned int *ticket, cudaStream_t st);
 // fixed-preconditioner loop: zr = Re <z, r>, Fletcher-Reeves beta = zr / rz, loop test
 cgs_status launch_fcg_zr_check(FCGScalars *fs, const float2 *z, const float2 *r, int64_t n, double *partial,
                                unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st);

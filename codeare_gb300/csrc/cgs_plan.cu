@@ -1386,26 +1386,26 @@ cgs_status fcg_alloc(cgs_plan *p)
 // z = M(r): mode 2 d . (t + net(t)) with t = d . r (the network corrects the
 // Jacobi step); mode 1 d^2 . r; mode 3 the circulant C(r); mode 4
 // C(r) + d . net(t) (the network corrects the circulant step); mode 0 (or
-// after the fallback) z = r
-cgs_status fcg_precondition(cgs_plan *p, cgs_net *net, int mode, cudaStream_t st)
+// after the fallback) z = r.  Without `select` the caller makes the
+// fallback's z = r itself (the fused loop body does, with its dots).
+cgs_status fcg_precondition(cgs_plan *p, cgs_net *net, int mode, cudaStream_t st, bool select = true)
 {
     const int64_t Nt = p->Nt;
     if (mode == 4) {
         CGS_TRY(op_circ(p, p->vR, p->vCo, st));
-        CGS_TRY(launch_diag_scale(p->vR, nullptr, p->dscale, 1, Nt, p->vT, st));
-        CGS_TRY(launch_coldot(p->vT, p->vT, nullptr, Nt, 1, p->partial, &p->fs->tt, st));
+        CGS_TRY(launch_diag_scale_nrm(p->vR, p->dscale, Nt, p->vT, p->fpart, p->ftick, &p->fs->tt, st));
         CGS_TRY(net_apply_image(net, p->vT, &p->fs->tt, p->N[0], p->N[1], p->vZ, st));
         CGS_TRY(launch_scale_add(p->vZ, p->vZ, p->dscale, p->vCo, nullptr, Nt, st));
     } else if (mode == 3) {
         CGS_TRY(op_circ(p, p->vR, p->vZ, st));
     } else if (mode == 2) {
-        CGS_TRY(launch_diag_scale(p->vR, nullptr, p->dscale, 1, Nt, p->vT, st));
-        CGS_TRY(launch_coldot(p->vT, p->vT, nullptr, Nt, 1, p->partial, &p->fs->tt, st));
+        CGS_TRY(launch_diag_scale_nrm(p->vR, p->dscale, Nt, p->vT, p->fpart, p->ftick, &p->fs->tt, st));
         CGS_TRY(net_apply_image(net, p->vT, &p->fs->tt, p->N[0], p->N[1], p->vZ, st));
         CGS_TRY(launch_diag_scale(p->vZ, p->vT, p->dscale, 1, Nt, p->vZ, st));
     } else if (mode == 1) {
         CGS_TRY(launch_diag_scale(p->vR, nullptr, p->dscale, 2, Nt, p->vZ, st));
     }
+    if (!select) return CGS_OK;
     return launch_fcg_kernels(FCG_SELECT, p->fs, p->vX, p->vR, p->vO, p->vP, p->vQ, p->vZ, Nt,
                               cudaGraphConditionalHandle(), st);
 }
@@ -1488,15 +1488,14 @@ cgs_status build_fcg_graph(cgs_plan *p, int from_data, int toeplitz, int weighte
             if (cudaStreamEndCapture(st, &bb) != cudaSuccess && q == CGS_OK) q = CGS_ERR_CUDA;
             r = q;
         } else {
-        q = op_normal(p, p->vP, p->vQ, toeplitz, weighted, &fs->cg, st);
-        if (q == CGS_OK) q = launch_coldot(p->vP, p->vQ, nullptr, Nt, 1, p->partial, &fs->pq, st);
-        if (q == CGS_OK) q = K(FCG_UPDATE_XR, h);
-        if (q == CGS_OK) q = launch_coldot(p->vR, p->vR, nullptr, Nt, 1, p->partial, &fs->rr, st);
-        if (q == CGS_OK) q = K(FCG_DECIDE, h);
-        if (q == CGS_OK) q = fcg_precondition(p, net, mode, st);
-        if (q == CGS_OK) q = launch_coldot(p->vZ, p->vR, nullptr, Nt, 1, p->partial, &fs->zr, st);
-        if (q == CGS_OK) q = launch_coldot(p->vZ, p->vO, nullptr, Nt, 1, p->partial, &fs->zro, st);
-        if (q == CGS_OK) q = K(FCG_BETA, h);
+        // changing preconditioner: the lambda term with <p, q>, the x / r update
+        // with <r, r> and the stall test, and the fallback's z = r with <z, r>,
+        // <z, r_old> and beta are one kernel each
+        q = op_normal(p, p->vP, p->vQ, toeplitz, weighted, nullptr, st);
+        if (q == CGS_OK) q = launch_axpy_dot(p->vQ, p->vP, &fs->cg.lambda, nullptr, Nt, p->fpart, p->ftick, &fs->pq, st);
+        if (q == CGS_OK) q = launch_fcg_xr_rr_decide(fs, p->vX, p->vR, p->vO, p->vP, p->vQ, Nt, p->fpart, p->ftick, st);
+        if (q == CGS_OK) q = fcg_precondition(p, net, mode, st, false);
+        if (q == CGS_OK) q = launch_fcg_zsel_dots_beta(fs, p->vZ, p->vR, p->vO, Nt, p->fpart, p->partial, p->ftick, st);
         if (q == CGS_OK) q = K(FCG_P, h);
         if (q == CGS_OK) q = K(FCG_CHECK, h);
         cudaGraph_t bb = body;

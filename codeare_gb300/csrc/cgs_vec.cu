@@ -670,26 +670,10 @@ __global__ void fcg_init_kernel(FCGScalars *fs)
     fs->fallback_at = -1;
 }
 
-// alpha = rz / pq; x += alpha p; rold = r; r -= alpha q
-__global__ void fcg_update_xr_kernel(FCGScalars *fs, float2 *__restrict__ x, float2 *__restrict__ r,
-                                     float2 *__restrict__ rold, const float2 *__restrict__ p,
-                                     const float2 *__restrict__ q, int64_t n)
-{
-    const float a = (float)(fs->rz / fs->pq);
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-        const float2 pv = p[e], qv = q[e], rv = r[e];
-        float2 xv = x[e];
-        xv.x = fmaf(a, pv.x, xv.x); xv.y = fmaf(a, pv.y, xv.y);
-        x[e] = xv;
-        rold[e] = rv;
-        r[e] = make_float2(fmaf(-a, qv.x, rv.x), fmaf(-a, qv.y, rv.y));
-    }
-}
-
 // stall bookkeeping on the new residual (network mode only): kStallChecks
 // checks without a new best residual switch to plain CG (restarted)
 constexpr int kStallChecks = 6;
-__global__ void fcg_decide_kernel(FCGScalars *fs)
+__device__ __forceinline__ void fcg_decide_logic(FCGScalars *fs)
 {
     if (fs->rr < fs->best) { fs->best = fs->rr; fs->stall = 0; }
     else fs->stall += 1;
@@ -706,7 +690,8 @@ __global__ void fcg_select_kernel(const FCGScalars *fs, float2 *__restrict__ z, 
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) z[e] = r[e];
 }
 
-__global__ void fcg_beta_kernel(FCGScalars *fs)
+// Polak-Ribiere beta from zr and zro, with the fallback when <z, r> <= 0
+__device__ __forceinline__ void fcg_beta_logic(FCGScalars *fs)
 {
     if ((fs->mode == 2 || fs->mode == 4) && !fs->fallback && !(fs->zr > 0.0)) {   // no descent direction
         fs->fallback = 1;
@@ -719,6 +704,7 @@ __global__ void fcg_beta_kernel(FCGScalars *fs)
     else fs->beta = (fs->zr - fs->zro) / fs->rz;
     fs->rz = zr;
 }
+__global__ void fcg_beta_kernel(FCGScalars *fs) { fcg_beta_logic(fs); }
 
 // p = (use_r ? r : z) + beta p
 __global__ void fcg_p_kernel(const FCGScalars *fs, float2 *__restrict__ p, const float2 *__restrict__ z,
@@ -836,6 +822,98 @@ fcg_zr_check_kernel(FCGScalars *fs, const float2 *__restrict__ z, const float2 *
         fs->use_r = 0;
         cudaGraphSetConditional(h, fcg_check_logic(fs));
     }
+}
+
+// ---- flexible CG with a changing preconditioner (modes 2 and 4), fused ------
+// alpha = rz / pq; x += alpha p; rold = r; r -= alpha q; rr = |r|^2; then the
+// stall bookkeeping (fcg_update_xr + the rr dot + fcg_decide in one kernel)
+__global__ void __launch_bounds__(kThreads)
+fcg_xr_rr_decide_kernel(FCGScalars *fs, float2 *__restrict__ x, float2 *__restrict__ r, float2 *__restrict__ rold,
+                        const float2 *__restrict__ p, const float2 *__restrict__ q, int64_t n, double *partial,
+                        unsigned int *ticket)
+{
+    const float a = (float)(fs->rz / fs->pq);
+    double acc = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const float2 pv = p[e], qv = q[e], rv = r[e];
+        float2 xv = x[e];
+        xv.x = fmaf(a, pv.x, xv.x); xv.y = fmaf(a, pv.y, xv.y);
+        x[e] = xv;
+        rold[e] = rv;
+        const float2 rn = make_float2(fmaf(-a, qv.x, rv.x), fmaf(-a, qv.y, rv.y));
+        r[e] = rn;
+        acc += (double)fmaf(rn.x, rn.x, rn.y * rn.y);
+    }
+    double t;
+    if (finish_reduce(acc, partial, ticket, &t) && threadIdx.x == 0) {
+        fs->rr = t;
+        fcg_decide_logic(fs);
+    }
+}
+
+// z = r where the loop has fallen back (fcg_select's rule), zr = Re <z, r>,
+// zro = Re <z, rold>, then the Polak-Ribiere beta and the no-descent fallback
+// (fcg_beta's rule).  Every block reads fs->fallback before the ticket; only
+// the last block, after every ticket, may change it.  The two block sums go
+// to partial_a and partial_b (kDotBlocks each) and are added in block order.
+__global__ void __launch_bounds__(kThreads)
+fcg_zsel_dots_beta_kernel(FCGScalars *fs, float2 *__restrict__ z, const float2 *__restrict__ r,
+                          const float2 *__restrict__ rold, int64_t n, double *partial_a, double *partial_b,
+                          unsigned int *ticket)
+{
+    __shared__ double sred[kThreads];
+    __shared__ bool last;
+    const bool sel = fs->fallback || fs->mode == 0;
+    double acc_r = 0.0, acc_o = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const float2 rv = r[e], ov = rold[e];
+        float2 zv;
+        if (sel) { zv = rv; z[e] = zv; }
+        else zv = z[e];
+        acc_r += (double)fmaf(zv.x, rv.x, zv.y * rv.y);
+        acc_o += (double)fmaf(zv.x, ov.x, zv.y * ov.y);
+    }
+    const double ba = block_reduce(acc_r, sred);
+    const double bb = block_reduce(acc_o, sred);
+    if (threadIdx.x == 0) {
+        partial_a[blockIdx.x] = ba;
+        partial_b[blockIdx.x] = bb;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double sa = 0.0, sb = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += kThreads) {
+        sa += ((volatile double *)partial_a)[b];
+        sb += ((volatile double *)partial_b)[b];
+    }
+    const double ta = block_reduce(sa, sred);
+    const double tb = block_reduce(sb, sred);
+    if (threadIdx.x == 0) {
+        *ticket = 0u;
+        fs->zr = ta;
+        fs->zro = tb;
+        fcg_beta_logic(fs);
+    }
+}
+
+// out = d . in and *nrm = |out|^2 (the network's input and its scale)
+__global__ void __launch_bounds__(kThreads)
+diag_scale_nrm_kernel(const float2 *__restrict__ in, const float *__restrict__ d, int64_t n, float2 *__restrict__ out,
+                      double *partial, unsigned int *ticket, double *nrm)
+{
+    double acc = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const float f = d[e];
+        const float2 v = in[e];
+        const float2 o = make_float2(v.x * f, v.y * f);
+        out[e] = o;
+        acc += (double)fmaf(o.x, o.x, o.y * o.y);
+    }
+    double t;
+    if (finish_reduce(acc, partial, ticket, &t) && threadIdx.x == 0) *nrm = t;
 }
 
 // T. Chan fold of the 2N point-spread function onto the N-periodic grid
@@ -1197,6 +1275,30 @@ cgs_status launch_fcg_zr_check(FCGScalars *fs, const float2 *z, const float2 *r,
     return CGS_OK;
 }
 
+cgs_status launch_diag_scale_nrm(const float2 *in, const float *d, int64_t n, float2 *out, double *partial,
+                                 unsigned int *ticket, double *nrm, cudaStream_t st)
+{
+    diag_scale_nrm_kernel<<<kDotBlocks, kThreads, 0, st>>>(in, d, n, out, partial, ticket, nrm);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_fcg_xr_rr_decide(FCGScalars *fs, float2 *x, float2 *r, float2 *rold, const float2 *p,
+                                   const float2 *q, int64_t n, double *partial, unsigned int *ticket, cudaStream_t st)
+{
+    fcg_xr_rr_decide_kernel<<<kDotBlocks, kThreads, 0, st>>>(fs, x, r, rold, p, q, n, partial, ticket);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status launch_fcg_zsel_dots_beta(FCGScalars *fs, float2 *z, const float2 *r, const float2 *rold, int64_t n,
+                                     double *partial_a, double *partial_b, unsigned int *ticket, cudaStream_t st)
+{
+    fcg_zsel_dots_beta_kernel<<<kDotBlocks, kThreads, 0, st>>>(fs, z, r, rold, n, partial_a, partial_b, ticket);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
 cgs_status launch_circ_fold(const float2 *T, int N0, int N1, float2 *cN, cudaStream_t st)
 {
     circ_fold_kernel<<<grid_for((int64_t)N0 * N1), kThreads, 0, st>>>(T, N0, N1, cN);
@@ -1232,8 +1334,6 @@ cgs_status launch_fcg_kernels(int which, FCGScalars *fs, float2 *x, float2 *r, f
 {
     switch (which) {
         case FCG_INIT: fcg_init_kernel<<<1, 1, 0, st>>>(fs); break;
-        case FCG_UPDATE_XR: fcg_update_xr_kernel<<<grid_for(n), kThreads, 0, st>>>(fs, x, r, rold, p, q, n); break;
-        case FCG_DECIDE: fcg_decide_kernel<<<1, 1, 0, st>>>(fs); break;
         case FCG_SELECT: fcg_select_kernel<<<grid_for(n), kThreads, 0, st>>>(fs, z, r, n); break;
         case FCG_BETA: fcg_beta_kernel<<<1, 1, 0, st>>>(fs); break;
         case FCG_P: fcg_p_kernel<<<grid_for(n), kThreads, 0, st>>>(fs, p, z, r, n); break;
