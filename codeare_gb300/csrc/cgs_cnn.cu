@@ -492,6 +492,28 @@ __global__ void net_to_img_kernel(const float *__restrict__ y, const float *__re
     }
 }
 
+// z = dsc . (s y) + csq . vc: the network's output back on the image scale,
+// times the pixel scaling, plus the circulant's output csq . vc (the same
+// products and add, in the same order, as net_to_img, the circulant's output
+// scaling and scale_add one after another)
+__global__ void net_combine_kernel(const float *__restrict__ y, const float *__restrict__ scale, int64_t n,
+                                   const float *__restrict__ dsc, const float *__restrict__ csq,
+                                   const float2 *__restrict__ vc, float2 *__restrict__ z)
+{
+    const float s = *scale;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const float2 v = reinterpret_cast<const float2 *>(y)[e];
+        float2 o = make_float2(v.x * s, v.y * s);
+        const float a = dsc[e];
+        o.x *= a; o.y *= a;
+        const float f = csq[e];
+        const float2 c = vc[e];
+        const float2 u = make_float2(c.x * f, c.y * f);
+        o.x = fmaf(1.f, u.x, o.x); o.y = fmaf(1.f, u.y, o.y);
+        z[e] = o;
+    }
+}
+
 unsigned blocks_for(int64_t n)
 {
     int64_t b = (n + 255) / 256;
@@ -636,6 +658,19 @@ cgs_status net_apply_image(cgs_net *n, const float2 *r, const double *nrm2, int 
     CGS_LAUNCH_CHECK();
     CGS_TRY(net_forward_dev(n, 1, H, W, st));
     net_to_img_kernel<<<blocks_for(P), 256, 0, st>>>(n->y5, n->scale, P, z);
+    CGS_LAUNCH_CHECK();
+    return CGS_OK;
+}
+
+cgs_status net_apply_image_combine(cgs_net *n, const float2 *r, const double *nrm2, int H, int W, const float *dsc,
+                                   const float *csq, const float2 *vc, float2 *z, cudaStream_t st)
+{
+    CGS_TRY(net_check(n, 1, H, W));
+    const int64_t P = (int64_t)H * W;
+    img_to_net_kernel<<<blocks_for(P), 256, 0, st>>>(r, nrm2, P, n->x0, n->scale);
+    CGS_LAUNCH_CHECK();
+    CGS_TRY(net_forward_dev(n, 1, H, W, st));
+    net_combine_kernel<<<blocks_for(P), 256, 0, st>>>(n->y5, n->scale, P, dsc, csq, vc, z);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }

@@ -336,8 +336,10 @@ cgs_status launch_fcg_kernels(int which, FCGScalars *fs, float2 *x, float2 *r, f
 enum FcgOp { FCG_INIT = 0, FCG_SELECT = 3, FCG_BETA = 4, FCG_P = 5, FCG_CHECK = 6 };
 // flexible-CG loop with a fixed preconditioner (mode 0 plain, 1 Jacobi):
 // x, r update and rr (mode 0 also beta and the loop test); z = d^2 r, zr, beta, loop test
+// (mode 3: with csq also vc = csq . r, the circulant's input)
 cgs_status launch_fcg_xr_rr(FCGScalars *fs, float2 *x, float2 *r, const float2 *p, const float2 *q, int64_t n,
-                            double *partial, unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st);
+                            double *partial, unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st,
+                            const float *csq = nullptr, float2 *vc = nullptr);
 cgs_status launch_fcg_jacobi_z(FCGScalars *fs, float2 *z, const float2 *r, const float *d, int64_t n,
                                double *partial, unsigned int *ticket, cudaGraphConditionalHandle h,
                                cudaStream_t st);
@@ -375,18 +377,27 @@ cgs_status launch_diag_scale_nrm(const float2 *in, const float *d, int64_t n, fl
 // steps around z = M(r): x, rold, r update with rr and the stall bookkeeping;
 // then z = r after a fallback, zr and zro (partials in partial_a and partial_b,
 // dot_blocks() each) and the Polak-Ribiere beta
+// (with csq also vc = csq . r; with dsc also vt = dsc . r and fs->tt = |vt|^2,
+// whose block sums go to partial_b)
 cgs_status launch_fcg_xr_rr_decide(FCGScalars *fs, float2 *x, float2 *r, float2 *rold, const float2 *p,
-                                   const float2 *q, int64_t n, double *partial, unsigned int *ticket, cudaStream_t st);
+                                   const float2 *q, int64_t n, double *partial, unsigned int *ticket, cudaStream_t st,
+                                   const float *csq = nullptr, float2 *vc = nullptr, const float *dsc = nullptr,
+                                   float2 *vt = nullptr, double *partial_b = nullptr);
 cgs_status launch_fcg_zsel_dots_beta(FCGScalars *fs, float2 *z, const float2 *r, const float2 *rold, int64_t n,
                                      double *partial_a, double *partial_b, unsigned int *ticket, cudaStream_t st);
 // fixed-preconditioner loop: zr = Re <z, r>, Fletcher-Reeves beta = zr / rz, loop test
-cgs_status launch_fcg_zr_check(FCGScalars *fs, const float2 *z, const float2 *r, int64_t n, double *partial,
-                               unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st);
+// (with csq, z = csq . vc is formed and written first: the circulant's output)
+cgs_status launch_fcg_zr_check(FCGScalars *fs, float2 *z, const float2 *r, int64_t n, double *partial,
+                               unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st,
+                               const float *csq = nullptr, const float2 *vc = nullptr);
 // z = M(r): the learned preconditioner on one complex image (cgs_cnn.cu);
 // nrm2 = sum |r|^2 on the device sets the input scale
 uint64_t net_serial(const cgs_net *n);   // 0 for null, else unique per created network
 cgs_status net_apply_image(cgs_net *n, const float2 *r, const double *nrm2, int H, int W, float2 *z,
                            cudaStream_t st);
+// the same with the output step z = dsc . net(r) + csq . vc in one kernel
+cgs_status net_apply_image_combine(cgs_net *n, const float2 *r, const double *nrm2, int H, int W, const float *dsc,
+                                   const float *csq, const float2 *vc, float2 *z, cudaStream_t st);
 // Loop check (one thread): records the residual measure of the current
 // iterate, decides whether another update follows, and sets the conditional
 // handle of the enclosing while node accordingly.

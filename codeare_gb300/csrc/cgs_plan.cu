@@ -1047,12 +1047,20 @@ static cgs_status build_circulant(cgs_plan *p, const float2 *T, cudaStream_t st)
 
 // z = C(r) = csq . IFFT(kinv . FFT(csq . r)), kinv and csq set for the current
 // lambda and sensitivities (fcg prologue or cgs_precond_apply); out may not alias r
+// The transforms alone, in place on vC = csq . r (the flexible-CG loop bodies
+// form vC in their residual update and apply the output scaling in their next
+// kernel)
+static cgs_status op_circ_core(cgs_plan *p, cudaStream_t st)
+{
+    CGS_TRY(circ_fft2(p, p->vC, -1, p->circ_inv, st));
+    return circ_fft2(p, p->vC, +1, nullptr, st);
+}
+
 static cgs_status op_circ(cgs_plan *p, const float2 *r, float2 *out, cudaStream_t st)
 {
     const int64_t P = p->Nt;
     CGS_TRY(launch_diag_scale(r, nullptr, p->csq, 1, P, p->vC, st));
-    CGS_TRY(circ_fft2(p, p->vC, -1, p->circ_inv, st));
-    CGS_TRY(circ_fft2(p, p->vC, +1, nullptr, st));
+    CGS_TRY(op_circ_core(p, st));
     return launch_diag_scale(p->vC, nullptr, p->csq, 1, P, out, st);
 }
 
@@ -1386,11 +1394,22 @@ cgs_status fcg_alloc(cgs_plan *p)
 // z = M(r): mode 2 d . (t + net(t)) with t = d . r (the network corrects the
 // Jacobi step); mode 1 d^2 . r; mode 3 the circulant C(r); mode 4
 // C(r) + d . net(t) (the network corrects the circulant step); mode 0 (or
-// after the fallback) z = r.  Without `select` the caller makes the
-// fallback's z = r itself (the fused loop body does, with its dots).
-cgs_status fcg_precondition(cgs_plan *p, cgs_net *net, int mode, cudaStream_t st, bool select = true)
+// after the fallback) z = r.  The fused loop body passes `in_body`: its
+// residual update has already formed vC = csq . r and vT = dscale . r with
+// fs->tt, the network's output step adds the circulant's scaled output, and
+// the caller makes the fallback's z = r itself (with its dots).
+cgs_status fcg_precondition(cgs_plan *p, cgs_net *net, int mode, cudaStream_t st, bool in_body = false)
 {
     const int64_t Nt = p->Nt;
+    if (in_body && mode == 4) {
+        CGS_TRY(op_circ_core(p, st));
+        return net_apply_image_combine(net, p->vT, &p->fs->tt, p->N[0], p->N[1], p->dscale, p->csq, p->vC, p->vZ,
+                                       st);
+    }
+    if (in_body && mode == 2) {
+        CGS_TRY(net_apply_image(net, p->vT, &p->fs->tt, p->N[0], p->N[1], p->vZ, st));
+        return launch_diag_scale(p->vZ, p->vT, p->dscale, 1, Nt, p->vZ, st);
+    }
     if (mode == 4) {
         CGS_TRY(op_circ(p, p->vR, p->vCo, st));
         CGS_TRY(launch_diag_scale_nrm(p->vR, p->dscale, Nt, p->vT, p->fpart, p->ftick, &p->fs->tt, st));
@@ -1405,7 +1424,7 @@ cgs_status fcg_precondition(cgs_plan *p, cgs_net *net, int mode, cudaStream_t st
     } else if (mode == 1) {
         CGS_TRY(launch_diag_scale(p->vR, nullptr, p->dscale, 2, Nt, p->vZ, st));
     }
-    if (!select) return CGS_OK;
+    if (in_body) return CGS_OK;
     return launch_fcg_kernels(FCG_SELECT, p->fs, p->vX, p->vR, p->vO, p->vP, p->vQ, p->vZ, Nt,
                               cudaGraphConditionalHandle(), st);
 }
@@ -1478,23 +1497,33 @@ cgs_status build_fcg_graph(cgs_plan *p, int from_data, int toeplitz, int weighte
             // fixed preconditioner: fused updates, Fletcher-Reeves beta
             q = op_normal(p, p->vP, p->vQ, toeplitz, weighted, nullptr, st);
             if (q == CGS_OK) q = launch_axpy_dot(p->vQ, p->vP, &fs->cg.lambda, nullptr, Nt, p->fpart, p->ftick, &fs->pq, st);
-            if (q == CGS_OK) q = launch_fcg_xr_rr(fs, p->vX, p->vR, p->vP, p->vQ, Nt, p->fpart, p->ftick, h, st);
+            // (mode 3: the update also forms csq . r, and the <z, r> kernel
+            // applies the circulant's output scaling)
+            if (q == CGS_OK)
+                q = launch_fcg_xr_rr(fs, p->vX, p->vR, p->vP, p->vQ, Nt, p->fpart, p->ftick, h, st,
+                                     mode == 3 ? p->csq : nullptr, mode == 3 ? p->vC : nullptr);
             if (q == CGS_OK && mode == 1)
                 q = launch_fcg_jacobi_z(fs, p->vZ, p->vR, p->dscale, Nt, p->fpart, p->ftick, h, st);
-            if (q == CGS_OK && mode == 3) q = op_circ(p, p->vR, p->vZ, st);
-            if (q == CGS_OK && mode == 3) q = launch_fcg_zr_check(fs, p->vZ, p->vR, Nt, p->fpart, p->ftick, h, st);
+            if (q == CGS_OK && mode == 3) q = op_circ_core(p, st);
+            if (q == CGS_OK && mode == 3)
+                q = launch_fcg_zr_check(fs, p->vZ, p->vR, Nt, p->fpart, p->ftick, h, st, p->csq, p->vC);
             if (q == CGS_OK) q = K(FCG_P, h);
             cudaGraph_t bb = body;
             if (cudaStreamEndCapture(st, &bb) != cudaSuccess && q == CGS_OK) q = CGS_ERR_CUDA;
             r = q;
         } else {
-        // changing preconditioner: the lambda term with <p, q>, the x / r update
-        // with <r, r> and the stall test, and the fallback's z = r with <z, r>,
-        // <z, r_old> and beta are one kernel each
+        // changing preconditioner: the lambda term with <p, q>; the x / r update
+        // with <r, r>, the stall test and the preconditioner's scaled copies of
+        // r (csq . r for the circulant, dscale . r with its norm for the
+        // network); the fallback's z = r with <z, r>, <z, r_old> and beta: one
+        // kernel each
         q = op_normal(p, p->vP, p->vQ, toeplitz, weighted, nullptr, st);
         if (q == CGS_OK) q = launch_axpy_dot(p->vQ, p->vP, &fs->cg.lambda, nullptr, Nt, p->fpart, p->ftick, &fs->pq, st);
-        if (q == CGS_OK) q = launch_fcg_xr_rr_decide(fs, p->vX, p->vR, p->vO, p->vP, p->vQ, Nt, p->fpart, p->ftick, st);
-        if (q == CGS_OK) q = fcg_precondition(p, net, mode, st, false);
+        if (q == CGS_OK)
+            q = launch_fcg_xr_rr_decide(fs, p->vX, p->vR, p->vO, p->vP, p->vQ, Nt, p->fpart, p->ftick, st,
+                                        mode == 4 ? p->csq : nullptr, mode == 4 ? p->vC : nullptr, p->dscale, p->vT,
+                                        p->partial);
+        if (q == CGS_OK) q = fcg_precondition(p, net, mode, st, true);
         if (q == CGS_OK) q = launch_fcg_zsel_dots_beta(fs, p->vZ, p->vR, p->vO, Nt, p->fpart, p->partial, p->ftick, st);
         if (q == CGS_OK) q = K(FCG_P, h);
         if (q == CGS_OK) q = K(FCG_CHECK, h);

@@ -611,6 +611,36 @@ __device__ __forceinline__ bool finish_reduce(double v, double *partial, unsigne
     return true;
 }
 
+// the same for two sums at once (partial_a and partial_b, gridDim.x each)
+__device__ __forceinline__ bool finish_reduce2(double va, double vb, double *partial_a, double *partial_b,
+                                               unsigned int *ticket, double *ta, double *tb)
+{
+    __shared__ double sred[kThreads];
+    __shared__ bool last;
+    const double ba = block_reduce(va, sred);
+    const double bb = block_reduce(vb, sred);
+    if (threadIdx.x == 0) {
+        partial_a[blockIdx.x] = ba;
+        partial_b[blockIdx.x] = bb;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double sa = 0.0, sb = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += kThreads) {
+        sa += ((volatile double *)partial_a)[b];
+        sb += ((volatile double *)partial_b)[b];
+    }
+    const double a = block_reduce(sa, sred);
+    const double b = block_reduce(sb, sred);
+    if (threadIdx.x == 0) *ticket = 0u;
+    *ta = a;
+    *tb = b;
+    return true;
+}
+
 // q += lambda p (lambda nullable: no update), *out = Re <p, q>; skipped when *done
 __global__ void __launch_bounds__(kThreads)
 axpy_dot_kernel(float2 *__restrict__ q, const float2 *__restrict__ p, const double *lambda, const int *done,
@@ -747,13 +777,14 @@ __global__ void fcg_check_kernel(FCGScalars *fs, cudaGraphConditionalHandle h)
     cudaGraphSetConditional(h, fcg_check_logic(fs));
 }
 
-// plain (mode 0) and Jacobi (mode 1) loops, where z = M r with a fixed M:
-// a = rz / pq; x += a p; r -= a q; rr = |r|^2.  Mode 0 (z = r) also takes the
+// plain (mode 0), Jacobi (mode 1) and circulant (mode 3) loops, where z = M r
+// with a fixed M: a = rz / pq; x += a p; r -= a q; rr = |r|^2; with csq also
+// vc = csq . r (the circulant's input scaling).  Mode 0 (z = r) also takes the
 // Fletcher-Reeves beta = rr / rz here and runs the loop test.
 __global__ void __launch_bounds__(kThreads)
 fcg_xr_rr_kernel(FCGScalars *fs, float2 *__restrict__ x, float2 *__restrict__ r, const float2 *__restrict__ p,
                  const float2 *__restrict__ q, int64_t n, double *partial, unsigned int *ticket,
-                 cudaGraphConditionalHandle h)
+                 cudaGraphConditionalHandle h, const float *__restrict__ csq, float2 *__restrict__ vc)
 {
     const float a = (float)(fs->rz / fs->pq);
     double acc = 0.0;
@@ -764,6 +795,7 @@ fcg_xr_rr_kernel(FCGScalars *fs, float2 *__restrict__ x, float2 *__restrict__ r,
         x[e] = xv;
         const float2 rn = make_float2(fmaf(-a, qv.x, rv.x), fmaf(-a, qv.y, rv.y));
         r[e] = rn;
+        if (vc) { const float f = csq[e]; vc[e] = make_float2(rn.x * f, rn.y * f); }
         acc += (double)fmaf(rn.x, rn.x, rn.y * rn.y);
     }
     double t;
@@ -804,14 +836,26 @@ fcg_jacobi_z_kernel(FCGScalars *fs, float2 *__restrict__ z, const float2 *__rest
     }
 }
 
-// fixed preconditioner given z: zr = Re <z, r>, Fletcher-Reeves beta = zr / rz, loop test
+// fixed preconditioner given z (or, with csq, z = csq . vc written here: the
+// circulant's output scaling): zr = Re <z, r>, Fletcher-Reeves beta = zr / rz,
+// loop test
 __global__ void __launch_bounds__(kThreads)
-fcg_zr_check_kernel(FCGScalars *fs, const float2 *__restrict__ z, const float2 *__restrict__ r, int64_t n,
-                    double *partial, unsigned int *ticket, cudaGraphConditionalHandle h)
+fcg_zr_check_kernel(FCGScalars *fs, float2 *__restrict__ z, const float2 *__restrict__ r, int64_t n,
+                    double *partial, unsigned int *ticket, cudaGraphConditionalHandle h, const float *__restrict__ csq,
+                    const float2 *__restrict__ vc)
 {
     double acc = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-        const float2 zv = z[e], rv = r[e];
+        float2 zv;
+        if (csq) {
+            const float f = csq[e];
+            const float2 c = vc[e];
+            zv = make_float2(c.x * f, c.y * f);
+            z[e] = zv;
+        } else {
+            zv = z[e];
+        }
+        const float2 rv = r[e];
         acc += (double)fmaf(zv.x, rv.x, zv.y * rv.y);
     }
     double t;
@@ -826,14 +870,19 @@ fcg_zr_check_kernel(FCGScalars *fs, const float2 *__restrict__ z, const float2 *
 
 // ---- flexible CG with a changing preconditioner (modes 2 and 4), fused ------
 // alpha = rz / pq; x += alpha p; rold = r; r -= alpha q; rr = |r|^2; then the
-// stall bookkeeping (fcg_update_xr + the rr dot + fcg_decide in one kernel)
+// stall bookkeeping (the update, the rr dot and the decision in one kernel).
+// The preconditioner's scaled copies of the new residual come out of the same
+// pass: with csq, vc = csq . r (the circulant's input); with dsc, vt = dsc . r
+// and fs->tt = |vt|^2 (the network's input and its scale; partial_b then
+// holds the second sums).
 __global__ void __launch_bounds__(kThreads)
 fcg_xr_rr_decide_kernel(FCGScalars *fs, float2 *__restrict__ x, float2 *__restrict__ r, float2 *__restrict__ rold,
                         const float2 *__restrict__ p, const float2 *__restrict__ q, int64_t n, double *partial,
-                        unsigned int *ticket)
+                        unsigned int *ticket, const float *__restrict__ csq, float2 *__restrict__ vc,
+                        const float *__restrict__ dsc, float2 *__restrict__ vt, double *partial_b)
 {
     const float a = (float)(fs->rz / fs->pq);
-    double acc = 0.0;
+    double acc = 0.0, acc_t = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
         const float2 pv = p[e], qv = q[e], rv = r[e];
         float2 xv = x[e];
@@ -843,9 +892,22 @@ fcg_xr_rr_decide_kernel(FCGScalars *fs, float2 *__restrict__ x, float2 *__restri
         const float2 rn = make_float2(fmaf(-a, qv.x, rv.x), fmaf(-a, qv.y, rv.y));
         r[e] = rn;
         acc += (double)fmaf(rn.x, rn.x, rn.y * rn.y);
+        if (vc) { const float f = csq[e]; vc[e] = make_float2(rn.x * f, rn.y * f); }
+        if (vt) {
+            const float f = dsc[e];
+            const float2 o = make_float2(rn.x * f, rn.y * f);
+            vt[e] = o;
+            acc_t += (double)fmaf(o.x, o.x, o.y * o.y);
+        }
     }
-    double t;
-    if (finish_reduce(acc, partial, ticket, &t) && threadIdx.x == 0) {
+    double t, tt;
+    if (vt) {
+        if (finish_reduce2(acc, acc_t, partial, partial_b, ticket, &t, &tt) && threadIdx.x == 0) {
+            fs->rr = t;
+            fs->tt = tt;
+            fcg_decide_logic(fs);
+        }
+    } else if (finish_reduce(acc, partial, ticket, &t) && threadIdx.x == 0) {
         fs->rr = t;
         fcg_decide_logic(fs);
     }
@@ -861,8 +923,6 @@ fcg_zsel_dots_beta_kernel(FCGScalars *fs, float2 *__restrict__ z, const float2 *
                           const float2 *__restrict__ rold, int64_t n, double *partial_a, double *partial_b,
                           unsigned int *ticket)
 {
-    __shared__ double sred[kThreads];
-    __shared__ bool last;
     const bool sel = fs->fallback || fs->mode == 0;
     double acc_r = 0.0, acc_o = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
@@ -873,26 +933,8 @@ fcg_zsel_dots_beta_kernel(FCGScalars *fs, float2 *__restrict__ z, const float2 *
         acc_r += (double)fmaf(zv.x, rv.x, zv.y * rv.y);
         acc_o += (double)fmaf(zv.x, ov.x, zv.y * ov.y);
     }
-    const double ba = block_reduce(acc_r, sred);
-    const double bb = block_reduce(acc_o, sred);
-    if (threadIdx.x == 0) {
-        partial_a[blockIdx.x] = ba;
-        partial_b[blockIdx.x] = bb;
-        __threadfence();
-        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    double sa = 0.0, sb = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += kThreads) {
-        sa += ((volatile double *)partial_a)[b];
-        sb += ((volatile double *)partial_b)[b];
-    }
-    const double ta = block_reduce(sa, sred);
-    const double tb = block_reduce(sb, sred);
-    if (threadIdx.x == 0) {
-        *ticket = 0u;
+    double ta, tb;
+    if (finish_reduce2(acc_r, acc_o, partial_a, partial_b, ticket, &ta, &tb) && threadIdx.x == 0) {
         fs->zr = ta;
         fs->zro = tb;
         fcg_beta_logic(fs);
@@ -1098,9 +1140,10 @@ cgs_status launch_cg_xr_rr(float2 *x, float2 *r, const float2 *p, const float2 *
 }
 
 cgs_status launch_fcg_xr_rr(FCGScalars *fs, float2 *x, float2 *r, const float2 *p, const float2 *q, int64_t n,
-                            double *partial, unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st)
+                            double *partial, unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st,
+                            const float *csq, float2 *vc)
 {
-    fcg_xr_rr_kernel<<<kDotBlocks, kThreads, 0, st>>>(fs, x, r, p, q, n, partial, ticket, h);
+    fcg_xr_rr_kernel<<<kDotBlocks, kThreads, 0, st>>>(fs, x, r, p, q, n, partial, ticket, h, csq, vc);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }
@@ -1267,10 +1310,11 @@ cgs_status launch_diag_scale(const float2 *in, const float2 *add, const float *d
     return CGS_OK;
 }
 
-cgs_status launch_fcg_zr_check(FCGScalars *fs, const float2 *z, const float2 *r, int64_t n, double *partial,
-                               unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st)
+cgs_status launch_fcg_zr_check(FCGScalars *fs, float2 *z, const float2 *r, int64_t n, double *partial,
+                               unsigned int *ticket, cudaGraphConditionalHandle h, cudaStream_t st, const float *csq,
+                               const float2 *vc)
 {
-    fcg_zr_check_kernel<<<kDotBlocks, kThreads, 0, st>>>(fs, z, r, n, partial, ticket, h);
+    fcg_zr_check_kernel<<<kDotBlocks, kThreads, 0, st>>>(fs, z, r, n, partial, ticket, h, csq, vc);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }
@@ -1284,9 +1328,11 @@ cgs_status launch_diag_scale_nrm(const float2 *in, const float *d, int64_t n, fl
 }
 
 cgs_status launch_fcg_xr_rr_decide(FCGScalars *fs, float2 *x, float2 *r, float2 *rold, const float2 *p,
-                                   const float2 *q, int64_t n, double *partial, unsigned int *ticket, cudaStream_t st)
+                                   const float2 *q, int64_t n, double *partial, unsigned int *ticket, cudaStream_t st,
+                                   const float *csq, float2 *vc, const float *dsc, float2 *vt, double *partial_b)
 {
-    fcg_xr_rr_decide_kernel<<<kDotBlocks, kThreads, 0, st>>>(fs, x, r, rold, p, q, n, partial, ticket);
+    fcg_xr_rr_decide_kernel<<<kDotBlocks, kThreads, 0, st>>>(fs, x, r, rold, p, q, n, partial, ticket, csq, vc, dsc,
+                                                             vt, partial_b);
     CGS_LAUNCH_CHECK();
     return CGS_OK;
 }
