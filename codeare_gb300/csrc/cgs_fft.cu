@@ -759,18 +759,45 @@ axis_fft_ct_kernel(const __grid_constant__ AxisPass p, int logBI, int64_t nib)
     }
 }
 
-template <int N>
-cgs_status launch_ct(const AxisPass &p, cudaStream_t st)
+// A narrower column block (1024 values, 4 per thread) for the power-of-two
+// lengths up to 256: a pass over few columns (the 256^2 image of the
+// circulant preconditioner: 16 blocks of 16 columns) then spreads over 4x as
+// many blocks.  Each column's butterflies are the same, so the results are too.
+__host__ __device__ constexpr int ct_logb_small(int n)
 {
-    constexpr int LOGB = ct_logb(N);
+    if (n > 256 || (n & (n - 1)) != 0) return -1;
+    int lb = 0;
+    while ((n << (lb + 1)) <= 1024) ++lb;
+    return lb < ct_logb(n) ? lb : -1;
+}
+constexpr int64_t kCtFewBlocks = 76;   // below this many blocks (half the SMs) take the narrow block
+
+// column blocks of a pass with 2^LOGB columns per block
+struct CtGrid {
+    int logBI;
+    int64_t nib, nblocks;
+};
+inline CtGrid ct_grid(const AxisPass &p, int LOGB)
+{
+    const int B = 1 << LOGB;
+    CtGrid g{};
+    g.logBI = 0;  // largest power of two <= min(inner, B)
+    while ((1 << (g.logBI + 1)) <= B && (int64_t)(1 << (g.logBI + 1)) <= p.inner) ++g.logBI;
+    g.nib = (p.inner + (1 << g.logBI) - 1) >> g.logBI;
+    const int64_t BO = B >> g.logBI;
+    const int64_t nob = (p.outer + BO - 1) / BO;
+    g.nblocks = g.nib * nob;
+    return g;
+}
+
+template <int N, int LOGB>
+cgs_status launch_ct_b(const AxisPass &p, cudaStream_t st)
+{
     constexpr int B = 1 << LOGB;
     static_assert(N * B <= kCtElems && (N * B) % kThreads == 0, "column block");
-    int logBI = 0;  // largest power of two <= min(inner, B)
-    while ((1 << (logBI + 1)) <= B && (int64_t)(1 << (logBI + 1)) <= p.inner) ++logBI;
-    const int64_t nib = (p.inner + (1 << logBI) - 1) >> logBI;
-    const int64_t BO = B >> logBI;
-    const int64_t nob = (p.outer + BO - 1) / BO;
-    const int64_t nblocks = nib * nob;
+    const CtGrid cg = ct_grid(p, LOGB);
+    const int logBI = cg.logBI;
+    const int64_t nib = cg.nib, nblocks = cg.nblocks;
     if (nblocks > 0x7fffffffLL) { set_error("axis pass grid too large"); return CGS_ERR_BAD_ARG; }
     const size_t smem = ((size_t)N + (size_t)ct_rows<N, LOGB>() * B) * sizeof(float2);
     static std::atomic<uint64_t> attr_devs{0};
@@ -784,6 +811,17 @@ cgs_status launch_ct(const AxisPass &p, cudaStream_t st)
     CGS_CUDA(launch_pdl(p.sign < 0 ? axis_fft_ct_kernel<N, LOGB, -1> : axis_fft_ct_kernel<N, LOGB, +1>,
                         dim3((unsigned)nblocks), dim3(kThreads), smem, st, p, logBI, nib));
     return CGS_OK;
+}
+
+template <int N>
+cgs_status launch_ct(const AxisPass &p, cudaStream_t st)
+{
+    constexpr int LOGB = ct_logb(N);
+    constexpr int LS = ct_logb_small(N);
+    if constexpr (LS >= 0) {
+        if (ct_grid(p, LOGB).nblocks < kCtFewBlocks) return launch_ct_b<N, LS>(p, st);
+    }
+    return launch_ct_b<N, LOGB>(p, st);
 }
 
 bool ct_supported(int n)
