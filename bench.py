@@ -753,11 +753,29 @@ def run_profile_case(args):
     captures (prints one summary line, no JSON contract):
       nufft256    -- the 256^2, 32-coil NuFFT of the headline (default tuning);
       kooshball64 -- the 64^3 downsample of the kooshball, 16 coils, E and E^H W;
-      cnn256      -- the learned preconditioner's network on one 256^2 image."""
+      cnn256      -- the learned preconditioner's network on one 256^2 image;
+      cg256       -- 10 iterations each of plain, circulant-preconditioned and
+                     learned flexible CG on one 256^2, 16-coil, 32-spoke problem
+                     (Toeplitz normal operator)."""
     import torch
     import codeare_gb300 as cg
     from codeare_gb300 import capi, synth
     torch.cuda.set_device(0)
+    if args.profile_case == "cg256":
+        from codeare_gb300 import learned
+        net = learned.load_net()
+        pr = learned.Problem(9001, spokes=32)
+        x = torch.zeros((pr.N, pr.N), dtype=torch.complex64, device="cuda")
+        for _ in range(args.warmup + args.steps):
+            for kw in ({}, {"circulant": True}, {"net": net, "circulant": True}):
+                x.zero_()
+                pr.solve(x, cgiter=10, cgeps=1e-12, **kw)
+        torch.cuda.synchronize()
+        pr.close()
+        if net is not None:
+            net.close()
+        print("profile case cg256: %d steps" % (args.warmup + args.steps))
+        return 0
     if args.profile_case == "cnn256":
         from codeare_gb300 import learned
         net = learned.load_net() or capi.Net(max_batch=1, max_h=256, max_w=256)
@@ -810,7 +828,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default gridding decomposition (profiling runs: no candidate launches)")
     ap.add_argument("--no-cgsense", action="store_true", help="skip the CG-SENSE, batch, kooshball, learned-preconditioner and CS sections")
-    ap.add_argument("--profile-case", choices=["nufft256", "kooshball64", "cnn256"],
+    ap.add_argument("--profile-case", choices=["nufft256", "kooshball64", "cnn256", "cg256"],
                     help="run only this workload's forward+adjoint steps (profiler captures; no JSON line)")
     args = ap.parse_args()
     if args.profile_case:
