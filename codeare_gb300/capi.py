@@ -30,7 +30,7 @@ EXPORTED = [
     "cgs_net_forward", "cgs_net_gradients", "cgs_net_train_step", "cgs_solve_fcg", "cgs_normal_apply", "cgs_precond_apply", "cgs_set_frame_sensitivities", "cgs_net_set_conv_kernel",
     "cgs_get_tuning", "cgs_set_tuning", "cgs_autotune", "cgs_autotune_cache", "cgs_batch_create", "cgs_batch_solve",
     "cgs_batch_destroy", "cgs_cs_create", "cgs_cs_destroy", "cgs_cs_adjoint", "cgs_cs_df", "cgs_cs_obj",
-    "cgs_cs_wavelet",
+    "cgs_cs_wavelet", "cgs_diag_wait_timeout",
 ]
 PROFILE_CATEGORIES = ("fft", "interp", "spread")
 
@@ -124,6 +124,7 @@ def load(path: str = LIB_PATH):
     L.cgs_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.cgs_autotune.argtypes = [vp, C.POINTER(Tuning), C.POINTER(C.c_double), vp]
     L.cgs_autotune_cache.argtypes = [C.c_int]
+    L.cgs_diag_wait_timeout.argtypes = [C.c_int64, vp]
     L.cgs_batch_create.argtypes = [C.POINTER(vp), C.POINTER(vp), C.POINTER(SolveOpts), C.c_int, vp]
     L.cgs_batch_solve.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(SolveReport),
                                   C.POINTER(C.c_double)]

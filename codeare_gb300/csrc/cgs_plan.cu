@@ -10,6 +10,7 @@
 // The caller's layouts (coil slowest, nodes in trajectory order) are converted
 // at the boundary only.
 #include "cgs_internal.cuh"
+#include "cgs_tc05.cuh"
 
 #include <algorithm>
 #include <thread>
@@ -1593,6 +1594,38 @@ cgs_status read_scalars(cgs_plan *p, CGScalars *h, cudaStream_t st)
 }
 
 }  // namespace
+
+// One thread waits, with the bounded mbarrier wait of the tensor-core
+// kernels, for the first phase of a barrier that expects one arrival and
+// never gets it; when the wait gives up it raises the timeout flag as those
+// kernels do.  Nothing else is waited on, held or written.
+namespace cgs {
+namespace diagk {
+__global__ void wait_kernel(int64_t limit_ns, int *flag)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x != 0) return;
+    tc05::mbar_init(&bar, 1);
+    tc05::fence_mbar_init();
+    if (!tc05::mbar_wait_ns(&bar, 0, (uint64_t)limit_ns)) *reinterpret_cast<volatile int *>(flag) = 1;
+}
+}  // namespace diagk
+}  // namespace cgs
+
+extern "C" cgs_status cgs_diag_wait_timeout(int64_t limit_ns, void *stream)
+{
+    if (limit_ns <= 0 || limit_ns > 1000000000LL) {
+        set_error("cgs_diag_wait_timeout: the limit must be in (0, 1 s]");
+        return CGS_ERR_BAD_ARG;
+    }
+    int *f = tc_flag();
+    if (!f) { set_error("cgs_diag_wait_timeout: no mapped host flag"); return CGS_ERR_CUDA; }
+    cudaStream_t st = (cudaStream_t)stream;
+    cgs::diagk::wait_kernel<<<1, 32, 0, st>>>(limit_ns, f);
+    CGS_LAUNCH_CHECK();
+    CGS_CUDA(cudaStreamSynchronize(st));
+    return tc_check();
+}
 
 // ===========================================================================
 // C ABI

@@ -340,6 +340,17 @@ void cgs_profile_collect(double *ms, int64_t *count);
 /* Text of the last error on this thread ("" if none). */
 const char *cgs_last_error(void);
 
+/* Diagnostic of the bounded device waits (no reference counterpart: the
+ * reference has no device code).  The tensor-core kernels wait for their
+ * MMAs on an mbarrier with a time limit; when a wait runs out the kernel
+ * skips its epilogue, frees its tensor memory, returns and sets a
+ * process-wide flag, and the library's next call reports CGS_ERR_TIMEOUT
+ * once.  This call runs that wait in a one-thread kernel on a barrier that
+ * nothing completes, for limit_ns nanoseconds (at most 1 s), waits for the
+ * kernel on `stream` and returns what the check reports: CGS_ERR_TIMEOUT,
+ * with the flag cleared and the context still usable. */
+cgs_status cgs_diag_wait_timeout(int64_t limit_ns, void *stream);
+
 /* ------------------------------------------------------------------------
  * Compressed sensing over the NCSENSE operator: codeare's CS_XSENSE with
  * ft = 3 (src/matrix/ft/CS_XSENSE.hpp:73-140), its TV and L1 penalties
