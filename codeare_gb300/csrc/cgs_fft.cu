@@ -770,7 +770,7 @@ __host__ __device__ constexpr int ct_logb_small(int n)
     while ((n << (lb + 1)) <= 1024) ++lb;
     return lb < ct_logb(n) ? lb : -1;
 }
-constexpr int64_t kCtFewBlocks = 76;   // below this many blocks (half the SMs) take the narrow block
+constexpr int64_t kCtFewBlocks = 152;  // below this many blocks (one per SM) take the narrow block
 
 // column blocks of a pass with 2^LOGB columns per block
 struct CtGrid {
