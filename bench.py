@@ -756,7 +756,8 @@ def run_profile_case(args):
       cnn256      -- the learned preconditioner's network on one 256^2 image;
       cg256       -- 10 iterations each of plain, circulant-preconditioned and
                      learned flexible CG on one 256^2, 16-coil, 32-spoke problem
-                     (Toeplitz normal operator)."""
+                     (Toeplitz normal operator), then the normal operator and
+                     the circulant step as ordinary launches."""
     import torch
     import codeare_gb300 as cg
     from codeare_gb300 import capi, synth
@@ -766,10 +767,16 @@ def run_profile_case(args):
         net = learned.load_net()
         pr = learned.Problem(9001, spokes=32)
         x = torch.zeros((pr.N, pr.N), dtype=torch.complex64, device="cuda")
+        q = torch.empty_like(x)
         for _ in range(args.warmup + args.steps):
             for kw in ({}, {"circulant": True}, {"net": net, "circulant": True}):
                 x.zero_()
                 pr.solve(x, cgiter=10, cgeps=1e-12, **kw)
+            # the loops run inside CUDA graphs; the normal operator and the
+            # circulant step once more as ordinary launches, so a launch list
+            # shows their kernels
+            pr.apply(pr.b, q)
+            pr.precond(pr.b, q)
         torch.cuda.synchronize()
         pr.close()
         if net is not None:
