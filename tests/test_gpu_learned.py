@@ -116,7 +116,7 @@ def test_learned_preconditioner_against_plain_cg(gpu):
     must land within 5x plain CG's final-image error against the converged
     plain solve.  The measured ratios are printed: the 3x wall-clock target of
     the learned arm is not reached (median 0.44x over eight problems, the
-    circulant alone 1.19x, in the bench line)."""
+    circulant alone 1.22x, in the bench line)."""
     from codeare_gb300 import capi, learned
     net = learned.load_net()
     if net is None:
